@@ -1,0 +1,166 @@
+/*
+ * mesh_bem_gb300.h -- C ABI of libmeshbem_gb300.so, the sm_103a (GB300) implementation of
+ * the GeCao/Mesh-Ferrofluid boundary-element hot path (RWG method of moments and 3D
+ * Laplace single/double-layer assembly).
+ *
+ * Conventions (all entry points):
+ *   - Array arguments are DEVICE pointers to contiguous row-major data; sizes are element
+ *     counts.  Faces and face-edge indices are int32, everything else float (f32 / c64
+ *     variants) or double (f64 / c128 variants).  "Interleaved complex" arrays store
+ *     (re, im) pairs.
+ *   - `stream` is a cudaStream_t passed as void*; NULL means the legacy default stream.
+ *     Every call is asynchronous with respect to the host.
+ *   - Return value: MB_OK (0) or an MB_ERR_* code; mb_last_error() returns the message of
+ *     the calling thread's last failure.  Invalid arguments are rejected before any launch.
+ *   - Outputs written with "=" are overwritten; outputs documented as "accumulated (+=)"
+ *     must be zeroed by the caller (as the reference's Python wrappers do with torch.zeros).
+ * The reference interface each entry point replaces is cited as file:line within the
+ * reference project.
+ */
+#ifndef MESH_BEM_GB300_H
+#define MESH_BEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MB_ABI_VERSION 1
+
+#define MB_OK 0
+#define MB_ERR_ARG 1         /* invalid argument: null pointer, bad size or range */
+#define MB_ERR_CUDA 2        /* CUDA launch / runtime error */
+#define MB_ERR_UNSUPPORTED 3 /* unsupported rule order, layer or kernel kind */
+#define MB_ERR_SIZE 4        /* problem too large for one launch */
+
+/* Message of the calling thread's last failure ("" if none). */
+const char* mb_last_error(void);
+/* MB_ABI_VERSION of the loaded library. */
+int mb_abi_version(void);
+
+/* ---- Reference-op drop-ins (src/mesh_BEM/cuda/mesh_MOM_3d.cpp:111-121) -------------- */
+
+/* Replaces create_MOM_Zmat_3d_forward (mesh_MOM_3d.cpp:52-77; kernel mesh_MOM_3d.cu:332-496).
+ * EFIE + MFIE face-edge matrix with the collapsed Gauss rule: test rule gp_x/gw_x (n_x
+ * nodes on [0,1]), source rule gp_y/gw_y (n_y nodes), n_x, n_y <= 16.
+ * z_real, z_imag: [batch, 3F, 3F] (row = test face*3 + local edge), overwritten; every
+ * batch slice receives the same matrix, as in the reference. */
+int mb_mom_zmat_fe_f32(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                       const float* face_areas, const float* face_normals, const float* gp_x,
+                       const float* gw_x, int n_x, const float* gp_y, const float* gw_y, int n_y,
+                       double wavenumber, int64_t batch, float* z_real, float* z_imag, void* stream);
+int mb_mom_zmat_fe_f64(const double* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                       const double* face_areas, const double* face_normals, const double* gp_x,
+                       const double* gw_x, int n_x, const double* gp_y, const double* gw_y, int n_y,
+                       double wavenumber, int64_t batch, double* z_real, double* z_imag, void* stream);
+
+/* Replaces create_MOM_rhs_3d_forward (mesh_MOM_3d.cpp:15-36; kernel mesh_MOM_3d.cu:244-330)
+ * with the reference's hard-coded plane wave (mesh_MOM_3d.cu:24-70).
+ * rhs_real, rhs_imag: [batch, F, 3], overwritten. */
+int mb_mom_rhs_fe_f32(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                      const float* face_areas, const float* face_normals, const float* gp,
+                      const float* gw, int n, double wavenumber, int64_t batch, float* rhs_real,
+                      float* rhs_imag, void* stream);
+int mb_mom_rhs_fe_f64(const double* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                      const double* face_areas, const double* face_normals, const double* gp,
+                      const double* gw, int n, double wavenumber, int64_t batch, double* rhs_real,
+                      double* rhs_imag, void* stream);
+
+/* Replaces interpolate_Icoeff_to_Js_3d_forward (mesh_MOM_3d.cpp:90-109; kernel
+ * mesh_MOM_3d.cu:498-565).  i_real, i_imag: [batch, n_edges]; js_real, js_imag:
+ * [batch, 3F, 3], accumulated (+=). */
+int mb_mom_interp_js_f32(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                         const int32_t* face_edge_indices, const float* face_areas,
+                         const float* i_real, const float* i_imag, int64_t n_edges, int64_t batch,
+                         float* js_real, float* js_imag, void* stream);
+int mb_mom_interp_js_f64(const double* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                         const int32_t* face_edge_indices, const double* face_areas,
+                         const double* i_real, const double* i_imag, int64_t n_edges, int64_t batch,
+                         double* js_real, double* js_imag, void* stream);
+
+/* ---- RWG-space operators (fuse the reference's scatter_add_ steps) ------------------- */
+
+/* Replaces MeshMOMZmatKernel.apply + Zmn.scatter_add_ (src/mesh_BEM/kernel_functions.py:39-74,
+ * src/mesh_BEM/mesh_BEM_solver_3d.py:128-147): assembles face-edge rows [row_begin, row_end)
+ * of the same matrix as mb_mom_zmat_fe_* straight into the RWG matrix
+ * z[fei[row], fei[col]], interleaved complex [n_edges, n_edges], accumulated (+=). */
+int mb_mom_zmat_rwg_c64(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                        const float* face_areas, const float* face_normals,
+                        const int32_t* face_edge_indices, int64_t n_edges, const float* gp_x,
+                        const float* gw_x, int n_x, const float* gp_y, const float* gw_y, int n_y,
+                        double wavenumber, int64_t row_begin, int64_t row_end, float* z, void* stream);
+int mb_mom_zmat_rwg_c128(const double* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                         const double* face_areas, const double* face_normals,
+                         const int32_t* face_edge_indices, int64_t n_edges, const double* gp_x,
+                         const double* gw_x, int n_x, const double* gp_y, const double* gw_y, int n_y,
+                         double wavenumber, int64_t row_begin, int64_t row_end, double* z,
+                         void* stream);
+
+/* Replaces MeshMOMRhsKernel.apply + rhs.scatter_add_ (kernel_functions.py:90-121,
+ * mesh_BEM_solver_3d.py:149-164) for n_rhs plane waves at once.  waves: device array of
+ * n_rhs records of 9 doubles (k*khat[3], E polarisation[3], H = khat x E / eta [3]);
+ * rhs: interleaved complex [n_edges, n_rhs], accumulated (+=). */
+int mb_mom_rhs_rwg_c64(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                       const float* face_areas, const float* face_normals,
+                       const int32_t* face_edge_indices, int64_t n_edges, const float* gp,
+                       const float* gw, int n, const double* waves, int n_rhs, float* rhs,
+                       void* stream);
+int mb_mom_rhs_rwg_c128(const double* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                        const double* face_areas, const double* face_normals,
+                        const int32_t* face_edge_indices, int64_t n_edges, const double* gp,
+                        const double* gw, int n, const double* waves, int n_rhs, double* rhs,
+                        void* stream);
+
+/* Replaces MeshMOMInterpolateJsKernel.apply + vert_Js.scatter_add_ (kernel_functions.py:137-171,
+ * mesh_BEM_solver_3d.py:177-192).  i_coeff: interleaved complex [batch, n_edges];
+ * vert_js: interleaved complex [batch, n_verts, 3], accumulated (+=). */
+int mb_mom_interp_vert_c64(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                           const int32_t* face_edge_indices, const float* face_areas,
+                           const float* i_coeff, int64_t n_edges, int64_t batch, float* vert_js,
+                           void* stream);
+int mb_mom_interp_vert_c128(const double* verts, int64_t n_verts, const int32_t* faces,
+                            int64_t n_faces, const int32_t* face_edge_indices,
+                            const double* face_areas, const double* i_coeff, int64_t n_edges,
+                            int64_t batch, double* vert_js, void* stream);
+
+/* ---- Laplace / Helmholtz-BEM layers ------------------------------------------------- */
+
+/* Replaces double_integration_on_panels_3d (src/mesh_BEM/utils/integrations_3d.py:252-452).
+ * table: [rows, 5] of (r1x, r2x, r1y, r2y, w*jacobian) -- the sub-domain maps of
+ * get_rands_and_jacobian_3d (integrations_3d.py:18-249) flattened; segments (HOST array of
+ * 5): the rows of relation r are [segments[r], segments[r+1]) for r = 0 separate,
+ * 1 shared vertex, 2 shared edge, 3 same face.  relations: [F, F] uint8
+ * (compute_panel_relation, src/utils/mesh_utils.py:700-725) or NULL to derive it from
+ * `faces`.  layer: 1 single (G_3d), 2 double (grad_G_y_3d . n of the first panel).
+ * order: 0 planar (P0), 1 linear (P1).  kind: 0 Laplace, 1 Helmholtz e^{+jkR}
+ * (src/utils/BEM_utils.py:72-172).  Rows [row_begin, row_end) of the first ("y") face.
+ * out_real (and out_imag for kind 1): [row_end-row_begin, F, nphi, nphi], overwritten. */
+int mb_laplace_panels_f32(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                          const float* face_areas, const float* face_normals, const float* table,
+                          const int32_t* segments, const uint8_t* relations, int layer, int order,
+                          int kind, double wavenumber, int64_t row_begin, int64_t row_end,
+                          float* out_real, float* out_imag, void* stream);
+int mb_laplace_panels_f64(const double* verts, int64_t n_verts, const int32_t* faces,
+                          int64_t n_faces, const double* face_areas, const double* face_normals,
+                          const double* table, const int32_t* segments, const uint8_t* relations,
+                          int layer, int order, int kind, double wavenumber, int64_t row_begin,
+                          int64_t row_end, double* out_real, double* out_imag, void* stream);
+
+/* Replaces pack_matrix_tight (src/utils/BEM_utils.py:314-357): packed[faces[fy,a], faces[fx,b]]
+ * += m[fy, fx, a, b] (P1) or m[fy, fx]/9 (P0).  packed: [n_verts, n_verts] real, or interleaved
+ * complex when m_imag != NULL; accumulated (+=). */
+int mb_pack_tight_f32(const float* m_real, const float* m_imag, const int32_t* faces, int64_t n_faces,
+                      int64_t n_verts, int order, float* packed, void* stream);
+int mb_pack_tight_f64(const double* m_real, const double* m_imag, const int32_t* faces,
+                      int64_t n_faces, int64_t n_verts, int order, double* packed, void* stream);
+
+/* Replaces compute_panel_relation (src/utils/mesh_utils.py:700-725): relations [F, F] uint8,
+ * overwritten. */
+int mb_panel_relation(const int32_t* faces, int64_t n_faces, uint8_t* relations, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MESH_BEM_GB300_H */

@@ -1,0 +1,85 @@
+"""Build recipe of libmeshbem_gb300.so (nvcc, sm_103a only).
+
+Each ``csrc/*.cu`` translation unit is compiled in parallel with
+``-gencode arch=compute_103a,code=sm_103a -O3 -lineinfo`` and the objects are linked into
+``lib/libmeshbem_gb300.so`` inside the package, next to the sources.  No PyTorch headers
+are involved: the library exposes the plain C ABI of ``include/mesh_bem_gb300.h`` and the
+Python layer binds it with ctypes.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+LIB_DIR = os.path.join(PKG, "lib")
+LIB = os.path.join(LIB_DIR, "libmeshbem_gb300.so")
+HEADER = os.path.join(REPO, "include", "mesh_bem_gb300.h")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = [
+    "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+    "-Xptxas", "-O3",
+]
+
+
+def nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(cand):
+        raise RuntimeError("nvcc not found; the CUDA toolkit is required to build libmeshbem_gb300")
+    return cand
+
+
+def sources() -> list[str]:
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+
+
+def _deps() -> list[str]:
+    hdrs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    return sources() + hdrs + [HEADER, __file__]
+
+
+def stale() -> bool:
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    return any(os.path.getmtime(p) > t for p in _deps())
+
+
+def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> str:
+    if not force and not stale():
+        return LIB
+    os.makedirs(os.path.join(LIB_DIR, "obj"), exist_ok=True)
+    cc = nvcc()
+    flags = NVCC_FLAGS + (extra_flags or [])
+
+    def compile_one(src: str) -> str:
+        obj = os.path.join(LIB_DIR, "obj", os.path.basename(src)[:-3] + ".o")
+        cmd = [cc, *ARCH, *flags, "-c", src, "-o", obj]
+        p = subprocess.run(cmd, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{p.stdout}\n{p.stderr}")
+        if verbose and (p.stdout or p.stderr):
+            print(p.stdout + p.stderr)
+        return obj
+
+    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
+        objs = list(ex.map(compile_one, sources()))
+    tmp = LIB + ".tmp"
+    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(f"link failed:\n{p.stdout}\n{p.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    import sys
+
+    print(build(force=True, verbose="-v" in sys.argv,
+                extra_flags=["-Xptxas", "-v"] if "-v" in sys.argv else None))

@@ -1,0 +1,247 @@
+// capi.cu -- the C ABI of libmeshbem_gb300.so (declared in include/mesh_bem_gb300.h).
+//
+// Every entry point takes device pointers, element counts and a cudaStream_t (as void*;
+// NULL = the legacy default stream), validates its arguments, launches asynchronously on
+// that stream and returns MB_OK or an error code; mb_last_error() returns the message of
+// the calling thread's last failure.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/mesh_bem_gb300.h"
+#include "common.cuh"
+
+namespace mb {
+
+static thread_local char g_err[512] = "";
+
+int set_error(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int check_launch(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(MB_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    return MB_OK;
+}
+
+struct PlaneWave;
+template <typename T>
+int launch_mom_ref_zmat(const T*, int64_t, const int32_t*, int64_t, const T*, const T*, const T*,
+                        const T*, int, const T*, const T*, int, double, const int32_t*, int64_t, int64_t,
+                        int64_t, int64_t, T*, T*, cudaStream_t);
+template <typename T>
+int launch_mom_ref_rhs(const T*, const int32_t*, int64_t, const T*, const T*, const T*, const T*, int,
+                       const PlaneWave*, double, int, int, int64_t, const int32_t*, T*, T*, cudaStream_t);
+template <typename T>
+int launch_mom_interp(const T*, const int32_t*, const int32_t*, const T*, const T*, const T*, int64_t,
+                      int64_t, int64_t, int64_t, int, T*, T*, cudaStream_t);
+template <typename T>
+int launch_laplace_panels(const T*, const int32_t*, int64_t, const T*, const T*, const T*, const int*,
+                          const uint8_t*, int, int, int, double, int64_t, int64_t, T*, T*, cudaStream_t);
+template <typename T>
+int launch_pack_tight(const T*, const T*, const int32_t*, int64_t, int64_t, int, T*, cudaStream_t);
+int launch_panel_relation(const int32_t*, int64_t, uint8_t*, cudaStream_t);
+
+}  // namespace mb
+
+using namespace mb;
+
+#define MB_REQUIRE(cond, ...)                              \
+    do {                                                   \
+        if (!(cond)) return set_error(MB_ERR_ARG, __VA_ARGS__); \
+    } while (0)
+
+static inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+template <typename T>
+static int zmat_fe(const T* verts, int64_t nv, const int32_t* faces, int64_t nf, const T* areas,
+                   const T* normals, const T* gpx, const T* gwx, int nx, const T* gpy, const T* gwy,
+                   int ny, double k, int64_t batch, T* zr, T* zi, void* stream) {
+    MB_REQUIRE(nf >= 0 && nv >= 0 && batch >= 1, "bad sizes (n_faces=%lld, batch=%lld)", (long long)nf,
+               (long long)batch);
+    if (nf == 0) return MB_OK;
+    MB_REQUIRE(verts && faces && areas && normals && gpx && gwx && gpy && gwy && zr && zi,
+               "null pointer argument");
+    return launch_mom_ref_zmat<T>(verts, nv, faces, nf, areas, normals, gpx, gwx, nx, gpy, gwy, ny, k,
+                                  nullptr, 0, 0, 3 * nf, batch, zr, zi, as_stream(stream));
+}
+
+template <typename T>
+static int zmat_rwg(const T* verts, int64_t nv, const int32_t* faces, int64_t nf, const T* areas,
+                    const T* normals, const int32_t* fei, int64_t ne, const T* gpx, const T* gwx, int nx,
+                    const T* gpy, const T* gwy, int ny, double k, int64_t row_begin, int64_t row_end,
+                    T* z, void* stream) {
+    MB_REQUIRE(nf >= 0 && ne >= 0, "bad sizes");
+    if (nf == 0) return MB_OK;
+    MB_REQUIRE(verts && faces && areas && normals && fei && gpx && gwx && gpy && gwy && z,
+               "null pointer argument");
+    MB_REQUIRE(0 <= row_begin && row_begin <= row_end && row_end <= 3 * nf,
+               "row range [%lld, %lld) outside [0, 3F)", (long long)row_begin, (long long)row_end);
+    return launch_mom_ref_zmat<T>(verts, nv, faces, nf, areas, normals, gpx, gwx, nx, gpy, gwy, ny, k,
+                                  fei, ne, row_begin, row_end, 1, z, nullptr, as_stream(stream));
+}
+
+extern "C" {
+
+const char* mb_last_error(void) { return g_err; }
+
+int mb_abi_version(void) { return MB_ABI_VERSION; }
+
+int mb_mom_zmat_fe_f32(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                       const float* face_areas, const float* face_normals, const float* gp_x,
+                       const float* gw_x, int n_x, const float* gp_y, const float* gw_y, int n_y,
+                       double wavenumber, int64_t batch, float* z_real, float* z_imag, void* stream) {
+    return zmat_fe<float>(verts, n_verts, faces, n_faces, face_areas, face_normals, gp_x, gw_x, n_x,
+                          gp_y, gw_y, n_y, wavenumber, batch, z_real, z_imag, stream);
+}
+
+int mb_mom_zmat_fe_f64(const double* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                       const double* face_areas, const double* face_normals, const double* gp_x,
+                       const double* gw_x, int n_x, const double* gp_y, const double* gw_y, int n_y,
+                       double wavenumber, int64_t batch, double* z_real, double* z_imag, void* stream) {
+    return zmat_fe<double>(verts, n_verts, faces, n_faces, face_areas, face_normals, gp_x, gw_x, n_x,
+                           gp_y, gw_y, n_y, wavenumber, batch, z_real, z_imag, stream);
+}
+
+int mb_mom_zmat_rwg_c64(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                        const float* face_areas, const float* face_normals,
+                        const int32_t* face_edge_indices, int64_t n_edges, const float* gp_x,
+                        const float* gw_x, int n_x, const float* gp_y, const float* gw_y, int n_y,
+                        double wavenumber, int64_t row_begin, int64_t row_end, float* z, void* stream) {
+    return zmat_rwg<float>(verts, n_verts, faces, n_faces, face_areas, face_normals, face_edge_indices,
+                           n_edges, gp_x, gw_x, n_x, gp_y, gw_y, n_y, wavenumber, row_begin, row_end, z,
+                           stream);
+}
+
+int mb_mom_zmat_rwg_c128(const double* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                         const double* face_areas, const double* face_normals,
+                         const int32_t* face_edge_indices, int64_t n_edges, const double* gp_x,
+                         const double* gw_x, int n_x, const double* gp_y, const double* gw_y, int n_y,
+                         double wavenumber, int64_t row_begin, int64_t row_end, double* z, void* stream) {
+    return zmat_rwg<double>(verts, n_verts, faces, n_faces, face_areas, face_normals, face_edge_indices,
+                            n_edges, gp_x, gw_x, n_x, gp_y, gw_y, n_y, wavenumber, row_begin, row_end, z,
+                            stream);
+}
+
+#define MB_RHS_FE(SFX, T)                                                                             \
+    int mb_mom_rhs_fe_##SFX(const T* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,     \
+                            const T* face_areas, const T* face_normals, const T* gp, const T* gw, int n, \
+                            double wavenumber, int64_t batch, T* rhs_real, T* rhs_imag, void* stream) { \
+        (void)n_verts;                                                                                \
+        MB_REQUIRE(n_faces >= 0 && batch >= 1, "bad sizes");                                          \
+        if (n_faces == 0) return MB_OK;                                                               \
+        MB_REQUIRE(verts && faces && face_areas && face_normals && gp && gw && rhs_real && rhs_imag,    \
+                   "null pointer argument");                                                          \
+        return launch_mom_ref_rhs<T>(verts, faces, n_faces, face_areas, face_normals, gp, gw, n,       \
+                                     nullptr, wavenumber, 1, 0, batch, nullptr, rhs_real, rhs_imag,    \
+                                     as_stream(stream));                                              \
+    }
+MB_RHS_FE(f32, float)
+MB_RHS_FE(f64, double)
+#undef MB_RHS_FE
+
+#define MB_RHS_RWG(SFX, T)                                                                            \
+    int mb_mom_rhs_rwg_##SFX(const T* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,    \
+                             const T* face_areas, const T* face_normals,                              \
+                             const int32_t* face_edge_indices, int64_t n_edges, const T* gp,          \
+                             const T* gw, int n, const double* waves, int n_rhs, T* rhs,              \
+                             void* stream) {                                                          \
+        (void)n_verts; (void)n_edges;                                                                 \
+        MB_REQUIRE(n_faces >= 0 && n_rhs >= 1, "bad sizes");                                          \
+        if (n_faces == 0) return MB_OK;                                                               \
+        MB_REQUIRE(verts && faces && face_areas && face_normals && face_edge_indices && gp && gw &&     \
+                       waves && rhs,                                                                  \
+                   "null pointer argument");                                                          \
+        return launch_mom_ref_rhs<T>(verts, faces, n_faces, face_areas, face_normals, gp, gw, n,       \
+                                     reinterpret_cast<const PlaneWave*>(waves), 0.0, n_rhs, 1, 1,      \
+                                     face_edge_indices, rhs, nullptr, as_stream(stream));              \
+    }
+MB_RHS_RWG(c64, float)
+MB_RHS_RWG(c128, double)
+#undef MB_RHS_RWG
+
+#define MB_INTERP_FE(SFX, T)                                                                          \
+    int mb_mom_interp_js_##SFX(const T* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,  \
+                               const int32_t* face_edge_indices, const T* face_areas,                  \
+                               const T* i_real, const T* i_imag, int64_t n_edges, int64_t batch,       \
+                               T* js_real, T* js_imag, void* stream) {                                 \
+        MB_REQUIRE(n_faces >= 0 && batch >= 0 && n_edges >= 0, "bad sizes");                          \
+        if (n_faces == 0 || batch == 0) return MB_OK;                                                 \
+        MB_REQUIRE(verts && faces && face_edge_indices && face_areas && i_real && i_imag && js_real && \
+                       js_imag,                                                                       \
+                   "null pointer argument");                                                          \
+        return launch_mom_interp<T>(verts, faces, face_edge_indices, face_areas, i_real, i_imag,      \
+                                    n_edges, n_faces, n_verts, batch, 0, js_real, js_imag,             \
+                                    as_stream(stream));                                               \
+    }
+MB_INTERP_FE(f32, float)
+MB_INTERP_FE(f64, double)
+#undef MB_INTERP_FE
+
+#define MB_INTERP_V(SFX, T)                                                                           \
+    int mb_mom_interp_vert_##SFX(const T* verts, int64_t n_verts, const int32_t* faces,                \
+                                 int64_t n_faces, const int32_t* face_edge_indices,                   \
+                                 const T* face_areas, const T* i_coeff, int64_t n_edges,               \
+                                 int64_t batch, T* vert_js, void* stream) {                            \
+        MB_REQUIRE(n_faces >= 0 && batch >= 0 && n_edges >= 0, "bad sizes");                          \
+        if (n_faces == 0 || batch == 0) return MB_OK;                                                 \
+        MB_REQUIRE(verts && faces && face_edge_indices && face_areas && i_coeff && vert_js,            \
+                   "null pointer argument");                                                          \
+        return launch_mom_interp<T>(verts, faces, face_edge_indices, face_areas, i_coeff, nullptr,    \
+                                    n_edges, n_faces, n_verts, batch, 1, vert_js, nullptr,             \
+                                    as_stream(stream));                                               \
+    }
+MB_INTERP_V(c64, float)
+MB_INTERP_V(c128, double)
+#undef MB_INTERP_V
+
+#define MB_LAP(SFX, T)                                                                                \
+    int mb_laplace_panels_##SFX(const T* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces, \
+                                const T* face_areas, const T* face_normals, const T* table,           \
+                                const int32_t* segments, const uint8_t* relations, int layer,          \
+                                int order, int kind, double wavenumber, int64_t row_begin,             \
+                                int64_t row_end, T* out_real, T* out_imag, void* stream) {             \
+        (void)n_verts;                                                                                \
+        MB_REQUIRE(n_faces >= 0, "bad sizes");                                                        \
+        if (n_faces == 0) return MB_OK;                                                               \
+        MB_REQUIRE(verts && faces && face_areas && face_normals && table && segments && out_real,     \
+                   "null pointer argument");                                                          \
+        MB_REQUIRE(0 <= row_begin && row_begin <= row_end && row_end <= n_faces, "bad row range");    \
+        for (int s = 0; s < 4; ++s)                                                                   \
+            MB_REQUIRE(segments[s] >= 0 && segments[s] <= segments[s + 1], "bad rule segments");      \
+        return launch_laplace_panels<T>(verts, faces, n_faces, face_areas, face_normals, table,       \
+                                        segments, relations, layer, order, kind, wavenumber,           \
+                                        row_begin, row_end, out_real, out_imag, as_stream(stream));    \
+    }
+MB_LAP(f32, float)
+MB_LAP(f64, double)
+#undef MB_LAP
+
+#define MB_PACK(SFX, T)                                                                               \
+    int mb_pack_tight_##SFX(const T* m_real, const T* m_imag, const int32_t* faces, int64_t n_faces,   \
+                            int64_t n_verts, int order, T* packed, void* stream) {                    \
+        MB_REQUIRE(n_faces >= 0 && n_verts >= 0, "bad sizes");                                        \
+        if (n_faces == 0) return MB_OK;                                                               \
+        MB_REQUIRE(m_real && faces && packed, "null pointer argument");                               \
+        MB_REQUIRE(order == 0 || order == 1, "order must be 0 or 1");                                 \
+        return launch_pack_tight<T>(m_real, m_imag, faces, n_faces, n_verts, order, packed,           \
+                                    as_stream(stream));                                               \
+    }
+MB_PACK(f32, float)
+MB_PACK(f64, double)
+#undef MB_PACK
+
+int mb_panel_relation(const int32_t* faces, int64_t n_faces, uint8_t* relations, void* stream) {
+    MB_REQUIRE(n_faces >= 0, "bad sizes");
+    if (n_faces == 0) return MB_OK;
+    MB_REQUIRE(faces && relations, "null pointer argument");
+    return launch_panel_relation(faces, n_faces, relations, as_stream(stream));
+}
+
+}  // extern "C"

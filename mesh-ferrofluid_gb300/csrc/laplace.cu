@@ -1,0 +1,236 @@
+// laplace.cu -- Galerkin single/double-layer panel integrals for the 3D Laplace (and
+// Helmholtz-BEM) boundary integral operators, with the reference's quadrature.
+//
+// Reference: double_integration_on_panels_3d (src/mesh_BEM/utils/integrations_3d.py:252-452).
+// For every ordered face pair (fy, fx) -- fy the "y" (first) panel, fx the "x" panel -- it
+// sums, over the 4-D rule of the pair's relation (separate / shared vertex / shared edge /
+// same face, sub-domain maps of get_rands_and_jacobian_3d :18-249),
+//     f(x, y) * 4 A_fy A_fx * phi_a(y) * phi_b(x) * w * jac
+// with f = 1/(4 pi R) (single layer, BEM_utils.py:72-104) or grad_y G . n_fy (double layer,
+// BEM_utils.py:141-172), phi the P1 shape functions (1-r1, r1-r2, r2) or 1 (P0).
+//
+// The host flattens the sub-domain maps into one table of rows (r1x, r2x, r1y, r2y, w*jac)
+// with per-relation segments, computed in the caller's dtype exactly like the reference; the
+// kernel walks the segment of each pair's relation.  One thread per face pair, 128 pairs
+// (one fy row segment) per block; the nine results of each thread go through shared memory
+// so the [F, F, nphi, nphi] output is written with coalesced 16-byte stores.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace mb {
+
+constexpr int kLapThreads = 128;
+
+template <typename T>
+__device__ __forceinline__ int relation_of(const int32_t* faces, int64_t i, int64_t j) {
+    const int32_t a0 = __ldg(faces + 3 * i), a1 = __ldg(faces + 3 * i + 1), a2 = __ldg(faces + 3 * i + 2);
+    const int32_t b0 = __ldg(faces + 3 * j), b1 = __ldg(faces + 3 * j + 1), b2 = __ldg(faces + 3 * j + 2);
+    const int cnt = (a0 == b0) + (a0 == b1) + (a0 == b2) + (a1 == b0) + (a1 == b1) + (a1 == b2) +
+                    (a2 == b0) + (a2 == b1) + (a2 == b2);
+    return cnt <= 3 ? cnt : 0;
+}
+
+// KIND 0: Laplace (real).  KIND 1: Helmholtz e^{+jkR} (BEM_utils.py:95-102, :161-170).
+// LAYER 1: single, 2: double.
+template <typename T, int NPHI, int KIND, int LAYER>
+__global__ void __launch_bounds__(kLapThreads) laplace_panels_kernel(
+    const T* __restrict__ verts, const int32_t* __restrict__ faces, const T* __restrict__ areas,
+    const T* __restrict__ normals, const T* __restrict__ tab, int4 seg_lo, int seg_end,
+    const uint8_t* __restrict__ rel, int64_t nf, int64_t row_begin, int64_t col_blocks, T k,
+    T* __restrict__ out_r, T* __restrict__ out_i) {
+    constexpr int NN = NPHI * NPHI;
+    __shared__ __align__(16) T s_out[KIND == 1 ? 2 : 1][kLapThreads * NN];
+    const int64_t row_local = (int64_t)blockIdx.x / col_blocks;
+    const int64_t fy = row_begin + row_local;
+    const int64_t col0 = ((int64_t)blockIdx.x % col_blocks) * kLapThreads;
+    const int64_t fx = col0 + threadIdx.x;
+    T accr[NN], acci[NN];
+#pragma unroll
+    for (int c = 0; c < NN; ++c) { accr[c] = 0; acci[c] = 0; }
+    if (fx < nf) {
+        const int r = rel ? (int)rel[fy * nf + fx] : relation_of<T>(faces, fy, fx);
+        const int beg = r == 0 ? seg_lo.x : r == 1 ? seg_lo.y : r == 2 ? seg_lo.z : seg_lo.w;
+        const int end = r == 0 ? seg_lo.y : r == 1 ? seg_lo.z : r == 2 ? seg_lo.w : seg_end;
+        const V3<T> o = load3(verts, __ldg(faces + 3 * fy));
+        const V3<T> Y1 = load3(verts, __ldg(faces + 3 * fy + 1)) - o;
+        const V3<T> Y2 = load3(verts, __ldg(faces + 3 * fy + 2)) - o;
+        const V3<T> X0 = load3(verts, __ldg(faces + 3 * fx)) - o;
+        const V3<T> X1 = load3(verts, __ldg(faces + 3 * fx + 1)) - o;
+        const V3<T> X2 = load3(verts, __ldg(faces + 3 * fx + 2)) - o;
+        const V3<T> ny = load3(normals, fy);
+        for (int t = beg; t < end; ++t) {
+            const T r1x = __ldg(tab + 5 * t), r2x = __ldg(tab + 5 * t + 1);
+            const T r1y = __ldg(tab + 5 * t + 2), r2y = __ldg(tab + 5 * t + 3);
+            const T wj = __ldg(tab + 5 * t + 4);
+            const V3<T> x = (T(1) - r1x) * X0 + (r1x - r2x) * X1 + r2x * X2;
+            const V3<T> y = (r1y - r2y) * Y1 + r2y * Y2;  // Y0 = 0 after the shift
+            const V3<T> d = x - y;
+            const T r2d = dot(d, d);
+            const T rinv = rsqrt_t(r2d);
+            T fr, fi = 0;
+            if constexpr (LAYER == 1) {
+                fr = rinv;
+            } else {
+                fr = dot(d, ny) * rinv * rinv * rinv;
+            }
+            if constexpr (KIND == 1) {
+                const T R = r2d * rinv;
+                T sn, cs;
+                sincos_turns(k * R * T(kInv2Pi), &sn, &cs);
+                if constexpr (LAYER == 1) {
+                    fi = fr * sn;
+                    fr = fr * cs;
+                } else {
+                    const T kR = k * R;
+                    fi = fr * (sn - kR * cs);
+                    fr = fr * (cs + kR * sn);
+                }
+            }
+            fr *= wj;
+            fi *= wj;
+            T py[3], px[3];
+            if constexpr (NPHI == 3) {
+                py[0] = T(1) - r1y; py[1] = r1y - r2y; py[2] = r2y;
+                px[0] = T(1) - r1x; px[1] = r1x - r2x; px[2] = r2x;
+            } else {
+                py[0] = T(1); px[0] = T(1);
+            }
+#pragma unroll
+            for (int a = 0; a < NPHI; ++a) {
+                const T ta = fr * py[a];
+                const T tb = fi * py[a];
+#pragma unroll
+                for (int b = 0; b < NPHI; ++b) {
+                    accr[a * NPHI + b] += ta * px[b];
+                    if constexpr (KIND == 1) acci[a * NPHI + b] += tb * px[b];
+                }
+            }
+        }
+        const T scale = T(4) * __ldg(areas + fy) * __ldg(areas + fx) * T(kInv4Pi);
+#pragma unroll
+        for (int c = 0; c < NN; ++c) {
+            accr[c] *= scale;
+            acci[c] *= scale;
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < NN; ++c) {
+        s_out[0][threadIdx.x * NN + c] = accr[c];
+        if constexpr (KIND == 1) s_out[KIND == 1 ? 1 : 0][threadIdx.x * NN + c] = acci[c];
+    }
+    __syncthreads();
+    const int64_t valid = (nf - col0) < kLapThreads ? (nf - col0) : kLapThreads;
+    const int64_t base = (row_local * nf + col0) * NN;
+    const int64_t n_out = valid * NN;
+    for (int64_t c = threadIdx.x; c < n_out; c += kLapThreads) {
+        out_r[base + c] = s_out[0][c];
+        if constexpr (KIND == 1) out_i[base + c] = s_out[KIND == 1 ? 1 : 0][c];
+    }
+}
+
+template <typename T>
+int launch_laplace_panels(const T* verts, const int32_t* faces, int64_t nf, const T* areas,
+                          const T* normals, const T* tab, const int* seg, const uint8_t* rel,
+                          int layer, int order, int kind, double k, int64_t row_begin,
+                          int64_t row_end, T* out_r, T* out_i, cudaStream_t stream) {
+    if (nf <= 0 || row_end <= row_begin) return MB_OK;
+    if (layer != 1 && layer != 2)
+        return set_error(MB_ERR_UNSUPPORTED, "layer %d not supported (1 single, 2 double)", layer);
+    if (order != 0 && order != 1) return set_error(MB_ERR_ARG, "order must be 0 or 1");
+    if (kind != 0 && kind != 1) return set_error(MB_ERR_ARG, "kind must be 0 or 1");
+    if (kind == 1 && out_i == nullptr) return set_error(MB_ERR_ARG, "Helmholtz kernel needs out_i");
+    const int64_t col_blocks = (nf + kLapThreads - 1) / kLapThreads;
+    const int64_t blocks = (row_end - row_begin) * col_blocks;
+    if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "mesh too large for one launch");
+    const int4 lo = make_int4(seg[0], seg[1], seg[2], seg[3]);
+    const int se = seg[4];
+#define MB_LAP(NP, KD, LY)                                                                          \
+    laplace_panels_kernel<T, NP, KD, LY><<<(unsigned)blocks, kLapThreads, 0, stream>>>(             \
+        verts, faces, areas, normals, tab, lo, se, rel, nf, row_begin, col_blocks, (T)k, out_r, out_i)
+    const int sel = (order == 1 ? 4 : 0) + kind * 2 + (layer - 1);
+    switch (sel) {
+        case 0: MB_LAP(1, 0, 1); break;
+        case 1: MB_LAP(1, 0, 2); break;
+        case 2: MB_LAP(1, 1, 1); break;
+        case 3: MB_LAP(1, 1, 2); break;
+        case 4: MB_LAP(3, 0, 1); break;
+        case 5: MB_LAP(3, 0, 2); break;
+        case 6: MB_LAP(3, 1, 1); break;
+        case 7: MB_LAP(3, 1, 2); break;
+    }
+#undef MB_LAP
+    return check_launch("laplace_panels");
+}
+
+template int launch_laplace_panels<float>(const float*, const int32_t*, int64_t, const float*,
+                                          const float*, const float*, const int*, const uint8_t*, int,
+                                          int, int, double, int64_t, int64_t, float*, float*,
+                                          cudaStream_t);
+template int launch_laplace_panels<double>(const double*, const int32_t*, int64_t, const double*,
+                                           const double*, const double*, const int*, const uint8_t*,
+                                           int, int, int, double, int64_t, int64_t, double*, double*,
+                                           cudaStream_t);
+
+// pack_matrix_tight (src/utils/BEM_utils.py:314-357): packed[faces[fy,a], faces[fx,b]] +=
+// M[fy, fx, a, b]; P0 spreads M[fy, fx]/9 over the nine vertex pairs.  packed is [V, V]
+// (real) or interleaved complex [V, V] when m_i != nullptr; the caller zeroes it.
+template <typename T>
+__global__ void pack_tight_kernel(const T* __restrict__ m_r, const T* __restrict__ m_i,
+                                  const int32_t* __restrict__ faces, int64_t nf, int64_t nv, int nphi,
+                                  T* __restrict__ packed) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nf * nf) return;
+    const int64_t fy = idx / nf, fx = idx % nf;
+    const int32_t vy[3] = {faces[3 * fy], faces[3 * fy + 1], faces[3 * fy + 2]};
+    const int32_t vx[3] = {faces[3 * fx], faces[3 * fx + 1], faces[3 * fx + 2]};
+    const int nn = nphi * nphi;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            const int64_t src = idx * nn + (nphi == 3 ? a * 3 + b : 0);
+            const T div = nphi == 3 ? T(1) : T(1) / T(9);
+            const int64_t dst = (int64_t)vy[a] * nv + vx[b];
+            if (m_i == nullptr) {
+                atomicAdd(packed + dst, m_r[src] * div);
+            } else {
+                atomicAdd(packed + 2 * dst, m_r[src] * div);
+                atomicAdd(packed + 2 * dst + 1, m_i[src] * div);
+            }
+        }
+}
+
+template <typename T>
+int launch_pack_tight(const T* m_r, const T* m_i, const int32_t* faces, int64_t nf, int64_t nv,
+                      int order, T* packed, cudaStream_t stream) {
+    if (nf <= 0) return MB_OK;
+    const int threads = 256;
+    const int64_t blocks = (nf * nf + threads - 1) / threads;
+    if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "mesh too large for one launch");
+    pack_tight_kernel<T><<<(unsigned)blocks, threads, 0, stream>>>(m_r, m_i, faces, nf, nv,
+                                                                    order == 1 ? 3 : 1, packed);
+    return check_launch("pack_tight");
+}
+template int launch_pack_tight<float>(const float*, const float*, const int32_t*, int64_t, int64_t, int,
+                                      float*, cudaStream_t);
+template int launch_pack_tight<double>(const double*, const double*, const int32_t*, int64_t, int64_t,
+                                       int, double*, cudaStream_t);
+
+// compute_panel_relation (src/utils/mesh_utils.py:700-725): shared-vertex count per pair.
+__global__ void panel_relation_kernel(const int32_t* __restrict__ faces, int64_t nf,
+                                      uint8_t* __restrict__ rel) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nf * nf) return;
+    rel[idx] = (uint8_t)relation_of<float>(faces, idx / nf, idx % nf);
+}
+
+int launch_panel_relation(const int32_t* faces, int64_t nf, uint8_t* rel, cudaStream_t stream) {
+    if (nf <= 0) return MB_OK;
+    const int threads = 256;
+    const int64_t blocks = (nf * nf + threads - 1) / threads;
+    if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "mesh too large for one launch");
+    panel_relation_kernel<<<(unsigned)blocks, threads, 0, stream>>>(faces, nf, rel);
+    return check_launch("panel_relation");
+}
+
+}  // namespace mb

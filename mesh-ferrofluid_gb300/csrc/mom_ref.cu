@@ -1,0 +1,454 @@
+// mom_ref.cu -- RWG MoM kernels with the reference's quadrature rule.
+//
+// The reference (GeCao/Mesh-Ferrofluid, src/mesh_BEM/cuda/mesh_MOM_3d.cu) integrates each
+// face-edge pair (test face f1 / local edge e1, source face f2 / local edge e2) with a
+// collapsed Gauss-Legendre rule whose points are laid out from the vertex opposite the
+// local edge (x = (1-r1) v_e + (r1-r2) v_{e+1} + r2 v_{e+2}, r2 = p_j r1, weight w_i w_j 2A,
+// Jacobian r1; :410-421).  The rule is not invariant under vertex rotation, so the nine
+// entries of a triangle pair use nine different point sets: the work per entry is
+// irreducible at Nt x Ns kernel evaluations, exactly as in the reference.  What this file
+// removes is everything around it:
+//   * one sincos per point pair shared by G and grad G (the reference evaluates both
+//     separately, :461-465), a MUFU rsqrt instead of sqrt + divide;
+//   * the per-test-point moment form: with the origin moved to the source vertex B0,
+//       L1 = jk c2 S1,   L2 = -(j/k) div2 S0,   K = -c2 (H1 x x)
+//     where S0 = sum w G, S1 = sum w G y, H1 = sum w h y and grad_x G = -h (x - y), so the
+//     inner loop only accumulates four complex moments (see `mom_entry`);
+//   * RWG constants computed once per thread instead of per point (:167-242);
+//   * float arithmetic stays float (the reference's M_PI / 0.5 / 1.0 literals promote the
+//     float build to FP64, :93-94, :123-124, :434, :479-480);
+//   * 64-bit indexing (the reference's `int idx` overflows at F > 15447, :364-374);
+//   * coordinates are shifted to a per-pair origin so FP32 keeps the precision of the
+//     short near-field distances.
+// Entry algebra: with c = s l/(2A) (RWG scale) and div = 2c, every term of the entry is
+// proportional to c1 c2, so the entry is
+//   c1 c2 sum_i w_i [ -H1_i . (x_i x ((x_i - A0) x n1)) + jk (x_i - A0) . S1_i - (4j/k) S0_i ]
+//   + (same face only) c1 c2 sum_i w_i 0.5 (x_i - A0) . (x_i - B0)
+// which reproduces :408-493 term by term.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace mb {
+
+// Rule tables are passed per launch as device pointers (at most 16 nodes per direction);
+// each block copies them to shared memory.
+
+// ---------------------------------------------------------------------------------------
+// One face-edge entry (row = f1*3+e1, col = f2*3+e2), reference rule.
+// NS > 0: source points held in registers (NS = ny*ny); NS == 0: recomputed per use.
+// ---------------------------------------------------------------------------------------
+template <typename T, int NS>
+__device__ __forceinline__ void mom_entry(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                          const T* __restrict__ areas, const T* __restrict__ normals,
+                                          const T* s_px, const T* s_wx, int nx, const T* s_py,
+                                          const T* s_wy, int ny, T k, int64_t f1, int e1, int64_t f2,
+                                          int e2, T* out_re, T* out_im) {
+    const int32_t a0 = __ldg(faces + 3 * f1 + e1);
+    const int32_t a1 = __ldg(faces + 3 * f1 + (e1 + 1) % 3);
+    const int32_t a2 = __ldg(faces + 3 * f1 + (e1 + 2) % 3);
+    const int32_t b0 = __ldg(faces + 3 * f2 + e2);
+    const int32_t b1 = __ldg(faces + 3 * f2 + (e2 + 1) % 3);
+    const int32_t b2 = __ldg(faces + 3 * f2 + (e2 + 2) % 3);
+    const V3<T> o = load3(verts, b0);
+    const V3<T> A0 = load3(verts, a0) - o;
+    const V3<T> A1 = load3(verts, a1) - o;
+    const V3<T> A2 = load3(verts, a2) - o;
+    const V3<T> B1 = load3(verts, b1) - o;
+    const V3<T> B2 = load3(verts, b2) - o;
+    const V3<T> n1 = load3(normals, f1);
+    const T area1 = __ldg(areas + f1), area2 = __ldg(areas + f2);
+    const V3<T> d1 = A2 - A1, d2 = B2 - B1;
+    const T c1 = (a1 < a2 ? T(1) : T(-1)) * sqrt_t(dot(d1, d1)) / (T(2) * area1);
+    const T c2 = (b1 < b2 ? T(1) : T(-1)) * sqrt_t(dot(d2, d2)) / (T(2) * area2);
+    const T k_turn = k * T(kInv2Pi);  // kR / (2 pi) per unit R
+    const T inv_k = T(1) / k;
+    const T src_scale = T(2) * area2 * T(kInv4Pi);
+
+    T ysx[NS > 0 ? NS : 1], ysy[NS > 0 ? NS : 1], ysz[NS > 0 ? NS : 1], ysw[NS > 0 ? NS : 1];
+    if constexpr (NS > 0) {
+#pragma unroll
+        for (int j = 0; j < NS; ++j) {
+            constexpr int NY = NS == 1 ? 1 : (NS == 4 ? 2 : (NS == 9 ? 3 : 4));
+            const int ji = j / NY, jj = j % NY;
+            const T r3 = s_py[ji];
+            const T r4 = s_py[jj] * r3;
+            // y - B0 = (r3 - r4)(B1 - B0) + r4 (B2 - B0), B0 = 0 after the shift
+            ysx[j] = (r3 - r4) * B1.x + r4 * B2.x;
+            ysy[j] = (r3 - r4) * B1.y + r4 * B2.y;
+            ysz[j] = (r3 - r4) * B1.z + r4 * B2.z;
+            ysw[j] = s_wy[ji] * s_wy[jj] * src_scale * r3;
+        }
+    }
+
+    T acc_re = 0, acc_im = 0, self_acc = 0;
+    const bool same = (f1 == f2);
+    const int nt = nx * nx;
+    for (int i = 0; i < nt; ++i) {
+        const T r1 = s_px[i / nx];
+        const T r2 = s_px[i % nx] * r1;
+        const T w1 = s_wx[i / nx] * s_wx[i % nx] * (T(2) * area1) * r1;
+        const V3<T> x = (T(1) - r1) * A0 + (r1 - r2) * A1 + r2 * A2;
+        T s0r = 0, s0i = 0, s1xr = 0, s1xi = 0, s1yr = 0, s1yi = 0, s1zr = 0, s1zi = 0;
+        T h1xr = 0, h1xi = 0, h1yr = 0, h1yi = 0, h1zr = 0, h1zi = 0;
+        const int ns = (NS > 0) ? NS : ny * ny;
+#pragma unroll
+        for (int j = 0; j < (NS > 0 ? NS : 1); ++j) {
+            // NS > 0 branch (registers); NS == 0 handled in the loop below
+            if constexpr (NS > 0) {
+                const T dx = x.x - ysx[j], dy = x.y - ysy[j], dz = x.z - ysz[j];
+                const T r2d = dx * dx + dy * dy + dz * dz;
+                const T rinv = rsqrt_t(r2d);
+                const T R = r2d * rinv;
+                T sn, cs;
+                sincos_turns(k_turn * R, &sn, &cs);
+                const T g = ysw[j] * rinv;
+                const T gr = g * cs, gi = -g * sn;  // e^{-jkR}/(4 pi R) * weight
+                const T kR = k * R;
+                const T rinv2 = rinv * rinv;
+                const T hr = (gr - gi * kR) * rinv2;  // G (1 + jkR) / R^2
+                const T hi = (gi + gr * kR) * rinv2;
+                s0r += gr; s0i += gi;
+                s1xr += gr * ysx[j]; s1xi += gi * ysx[j];
+                s1yr += gr * ysy[j]; s1yi += gi * ysy[j];
+                s1zr += gr * ysz[j]; s1zi += gi * ysz[j];
+                h1xr += hr * ysx[j]; h1xi += hi * ysx[j];
+                h1yr += hr * ysy[j]; h1yi += hi * ysy[j];
+                h1zr += hr * ysz[j]; h1zi += hi * ysz[j];
+            }
+        }
+        if constexpr (NS == 0) {
+            for (int j = 0; j < ns; ++j) {
+                const T r3 = s_py[j / ny];
+                const T r4 = s_py[j % ny] * r3;
+                const T yx = (r3 - r4) * B1.x + r4 * B2.x;
+                const T yy = (r3 - r4) * B1.y + r4 * B2.y;
+                const T yz = (r3 - r4) * B1.z + r4 * B2.z;
+                const T yw = s_wy[j / ny] * s_wy[j % ny] * src_scale * r3;
+                const T dx = x.x - yx, dy = x.y - yy, dz = x.z - yz;
+                const T r2d = dx * dx + dy * dy + dz * dz;
+                const T rinv = rsqrt_t(r2d);
+                const T R = r2d * rinv;
+                T sn, cs;
+                sincos_turns(k_turn * R, &sn, &cs);
+                const T g = yw * rinv;
+                const T gr = g * cs, gi = -g * sn;
+                const T kR = k * R;
+                const T rinv2 = rinv * rinv;
+                const T hr = (gr - gi * kR) * rinv2;
+                const T hi = (gi + gr * kR) * rinv2;
+                s0r += gr; s0i += gi;
+                s1xr += gr * yx; s1xi += gi * yx;
+                s1yr += gr * yy; s1yi += gi * yy;
+                s1zr += gr * yz; s1zi += gi * yz;
+                h1xr += hr * yx; h1xi += hi * yx;
+                h1yr += hr * yy; h1yi += hi * yy;
+                h1zr += hr * yz; h1zi += hi * yz;
+            }
+        }
+        const V3<T> a = x - A0;
+        const V3<T> u = cross(x, cross(a, n1));
+        const T hu_r = h1xr * u.x + h1yr * u.y + h1zr * u.z;
+        const T hu_i = h1xi * u.x + h1yi * u.y + h1zi * u.z;
+        const T p_r = s1xr * a.x + s1yr * a.y + s1zr * a.z;
+        const T p_i = s1xi * a.x + s1yi * a.y + s1zi * a.z;
+        // -H1.u + jk (a.S1) - (4j/k) S0
+        const T t_re = -hu_r - k * p_i + T(4) * inv_k * s0i;
+        const T t_im = -hu_i + k * p_r - T(4) * inv_k * s0r;
+        acc_re += w1 * t_re;
+        acc_im += w1 * t_im;
+        if (same) self_acc += w1 * dot(a, x);  // (x - A0) . (x - B0), B0 = 0
+    }
+    const T cc = c1 * c2;
+    *out_re = cc * (acc_re + T(0.5) * self_acc);
+    *out_im = cc * acc_im;
+}
+
+// Face-edge layout [batch, 3F, 3F], split real/imag (drop-in for the reference op).
+// grid.x = rows * col_blocks, block = kThreads columns.
+template <typename T, int NS>
+__global__ void __launch_bounds__(128) mom_ref_zmat_fe_kernel(
+    const T* __restrict__ verts, const int32_t* __restrict__ faces, const T* __restrict__ areas,
+    const T* __restrict__ normals, const T* __restrict__ gpx, const T* __restrict__ gwx, int nx,
+    const T* __restrict__ gpy, const T* __restrict__ gwy, int ny, T k, int64_t nf, int64_t batch,
+    int64_t col_blocks, T* __restrict__ zr, T* __restrict__ zi) {
+    __shared__ T s_px[16], s_wx[16], s_py[16], s_wy[16];
+    if (threadIdx.x < nx) { s_px[threadIdx.x] = gpx[threadIdx.x]; s_wx[threadIdx.x] = gwx[threadIdx.x]; }
+    if (threadIdx.x < ny) { s_py[threadIdx.x] = gpy[threadIdx.x]; s_wy[threadIdx.x] = gwy[threadIdx.x]; }
+    __syncthreads();
+    const int64_t ncol = 3 * nf;
+    const int64_t row = (int64_t)blockIdx.x / col_blocks;
+    const int64_t col = ((int64_t)blockIdx.x % col_blocks) * blockDim.x + threadIdx.x;
+    if (col >= ncol) return;
+    T re, im;
+    mom_entry<T, NS>(verts, faces, areas, normals, s_px, s_wx, nx, s_py, s_wy, ny, k, row / 3,
+                     (int)(row % 3), col / 3, (int)(col % 3), &re, &im);
+    for (int64_t b = 0; b < batch; ++b) {
+        const int64_t o = (b * ncol + row) * ncol + col;
+        zr[o] = re;
+        zi[o] = im;
+    }
+}
+
+// RWG layout: Z[fei[row], fei[col]] += entry, interleaved complex [E, E] (caller zeroes).
+// Every Z_mn receives its four face-pair contributions through vector atomics.
+template <typename T>
+__device__ __forceinline__ void atomic_add_c(T* p, T re, T im);
+template <>
+__device__ __forceinline__ void atomic_add_c<float>(float* p, float re, float im) {
+    atomicAdd(reinterpret_cast<float2*>(p), make_float2(re, im));
+}
+template <>
+__device__ __forceinline__ void atomic_add_c<double>(double* p, double re, double im) {
+    atomicAdd(p, re);
+    atomicAdd(p + 1, im);
+}
+
+template <typename T, int NS>
+__global__ void __launch_bounds__(128) mom_ref_zmat_rwg_kernel(
+    const T* __restrict__ verts, const int32_t* __restrict__ faces, const T* __restrict__ areas,
+    const T* __restrict__ normals, const int32_t* __restrict__ fei, int64_t n_edges,
+    const T* __restrict__ gpx, const T* __restrict__ gwx, int nx, const T* __restrict__ gpy,
+    const T* __restrict__ gwy, int ny, T k, int64_t nf, int64_t row_begin, int64_t col_blocks,
+    T* __restrict__ z) {
+    __shared__ T s_px[16], s_wx[16], s_py[16], s_wy[16];
+    if (threadIdx.x < nx) { s_px[threadIdx.x] = gpx[threadIdx.x]; s_wx[threadIdx.x] = gwx[threadIdx.x]; }
+    if (threadIdx.x < ny) { s_py[threadIdx.x] = gpy[threadIdx.x]; s_wy[threadIdx.x] = gwy[threadIdx.x]; }
+    __syncthreads();
+    const int64_t ncol = 3 * nf;
+    const int64_t row = row_begin + (int64_t)blockIdx.x / col_blocks;
+    const int64_t col = ((int64_t)blockIdx.x % col_blocks) * blockDim.x + threadIdx.x;
+    if (col >= ncol) return;
+    T re, im;
+    mom_entry<T, NS>(verts, faces, areas, normals, s_px, s_wx, nx, s_py, s_wy, ny, k, row / 3,
+                     (int)(row % 3), col / 3, (int)(col % 3), &re, &im);
+    const int64_t m = __ldg(fei + row), n = __ldg(fei + col);
+    atomic_add_c<T>(z + 2 * (m * n_edges + n), re, im);
+}
+
+// ---------------------------------------------------------------------------------------
+// Excitation (mesh_MOM_3d.cu:244-330).  One thread per face-edge and right-hand side.
+// Plane wave E = e0 exp(-j k khat.x), H = (khat x e0)/eta exp(-j k khat.x); the
+// reference's hard-coded wave is khat = (cos 30, sin 30, 0), e0 = z, eta = 1.
+// out_mode 0: face-edge split [B, F, 3] (batch copies identical, as the reference).
+// out_mode 1: RWG interleaved complex [E, nrhs] accumulated via atomics (caller zeroes).
+// ---------------------------------------------------------------------------------------
+struct PlaneWave {
+    double kx, ky, kz;     // k * khat
+    double ex, ey, ez;     // E polarisation
+    double hx, hy, hz;     // H = khat x e0 / eta
+};
+
+template <typename T>
+__global__ void mom_ref_rhs_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                   const T* __restrict__ areas, const T* __restrict__ normals,
+                                   const T* __restrict__ gp, const T* __restrict__ gw, int n,
+                                   const PlaneWave* __restrict__ waves, PlaneWave w0, int nrhs, int64_t nf,
+                                   int out_mode, int64_t batch, const int32_t* __restrict__ fei,
+                                   T* __restrict__ out_r, T* __restrict__ out_i) {
+    __shared__ T s_p[16], s_w[16];
+    if (threadIdx.x < n) { s_p[threadIdx.x] = gp[threadIdx.x]; s_w[threadIdx.x] = gw[threadIdx.x]; }
+    __syncthreads();
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 3 * nf * nrhs) return;
+    const int rhs = (int)(idx / (3 * nf));
+    const int64_t fe = idx % (3 * nf);
+    const int64_t f = fe / 3;
+    const int e = (int)(fe % 3);
+    const int32_t i0 = faces[3 * f + e], i1 = faces[3 * f + (e + 1) % 3], i2 = faces[3 * f + (e + 2) % 3];
+    const V3<T> v0 = load3(verts, i0), v1 = load3(verts, i1), v2 = load3(verts, i2);
+    const V3<T> nrm = load3(normals, f);
+    const T area = areas[f];
+    const V3<T> d = v2 - v1;
+    const T c = (i1 < i2 ? T(1) : T(-1)) * sqrt_t(dot(d, d)) / (T(2) * area);
+    const PlaneWave pw = waves ? waves[rhs] : w0;
+    const V3<T> kv = v3<T>((T)pw.kx, (T)pw.ky, (T)pw.kz);
+    const V3<T> E0 = v3<T>((T)pw.ex, (T)pw.ey, (T)pw.ez);
+    const V3<T> H0 = v3<T>((T)pw.hx, (T)pw.hy, (T)pw.hz);
+    const V3<T> nxh = cross(nrm, H0);
+    T acc_r = 0, acc_i = 0;
+    for (int i = 0; i < n * n; ++i) {
+        const T r1 = s_p[i / n];
+        const T r2 = s_p[i % n] * r1;
+        const T w = s_w[i / n] * s_w[i % n] * (T(2) * area) * r1;
+        const V3<T> x = (T(1) - r1) * v0 + (r1 - r2) * v1 + r2 * v2;
+        const V3<T> fv = c * (x - v0);
+        T sn, cs;
+        sincos_turns(dot(kv, x) * T(kInv2Pi), &sn, &cs);  // e^{-j k.x} = cs - j sn
+        const T proj = dot(fv, E0) + dot(fv, nxh);
+        acc_r += w * proj * cs;
+        acc_i -= w * proj * sn;
+    }
+    if (out_mode == 0) {
+        for (int64_t b = 0; b < batch; ++b) {
+            out_r[b * 3 * nf + fe] = acc_r;
+            out_i[b * 3 * nf + fe] = acc_i;
+        }
+    } else {
+        const int64_t m = fei[fe];
+        atomic_add_c<T>(out_r + 2 * (m * nrhs + rhs), acc_r, acc_i);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Edge coefficients -> vertex currents (mesh_MOM_3d.cu:498-565).
+// mode 0: per-face vertex slots [B, 3F, 3] split real/imag, accumulated (+=) exactly like
+//         the reference (each thread owns its face's nine slots).
+// mode 1: fused with the vertex scatter of solve_MOM (mesh_BEM_solver_3d.py:185-192):
+//         interleaved complex [B, V, 3] accumulated with atomics.
+// I is interleaved complex [B, E] in mode 1, split real/imag in mode 0.
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__global__ void mom_interp_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                  const int32_t* __restrict__ fei, const T* __restrict__ areas,
+                                  const T* __restrict__ ir, const T* __restrict__ ii, int64_t n_edges,
+                                  int64_t nf, int64_t nv, int64_t batch, int mode,
+                                  T* __restrict__ jr, T* __restrict__ ji) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= batch * nf) return;
+    const int64_t b = idx / nf, f = idx % nf;
+    const int32_t vid[3] = {faces[3 * f], faces[3 * f + 1], faces[3 * f + 2]};
+    const V3<T> p[3] = {load3(verts, vid[0]), load3(verts, vid[1]), load3(verts, vid[2])};
+    const T area = areas[f];
+    T accr[3][3] = {}, acci[3][3] = {};
+    for (int e = 0; e < 3; ++e) {
+        const int64_t edge = fei[3 * f + e];
+        const int e1 = (e + 1) % 3, e2 = (e + 2) % 3;
+        const V3<T> d = p[e2] - p[e1];
+        const T c = (vid[e1] < vid[e2] ? T(1) : T(-1)) * sqrt_t(dot(d, d)) / (T(2) * area);
+        T Ir, Ii;
+        if (mode == 0) {
+            Ir = ir[b * n_edges + edge];
+            Ii = ii[b * n_edges + edge];
+        } else {
+            Ir = ir[2 * (b * n_edges + edge)];
+            Ii = ir[2 * (b * n_edges + edge) + 1];
+        }
+        const V3<T> g1 = c * (p[e1] - p[e]);
+        const V3<T> g2 = c * (p[e2] - p[e]);
+        const T g1a[3] = {g1.x, g1.y, g1.z}, g2a[3] = {g2.x, g2.y, g2.z};
+        for (int a = 0; a < 3; ++a) {
+            accr[e1][a] += g1a[a] * Ir; acci[e1][a] += g1a[a] * Ii;
+            accr[e2][a] += g2a[a] * Ir; acci[e2][a] += g2a[a] * Ii;
+        }
+    }
+    if (mode == 0) {
+        const int64_t base = b * nf * 9 + f * 9;
+        for (int s = 0; s < 3; ++s)
+            for (int a = 0; a < 3; ++a) {
+                jr[base + s * 3 + a] += accr[s][a];
+                ji[base + s * 3 + a] += acci[s][a];
+            }
+    } else {
+        for (int s = 0; s < 3; ++s)
+            for (int a = 0; a < 3; ++a)
+                atomic_add_c<T>(jr + 2 * ((b * nv + vid[s]) * 3 + a), accr[s][a], acci[s][a]);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------------------
+template <typename T>
+int launch_mom_ref_zmat(const T* verts, int64_t nv, const int32_t* faces, int64_t nf, const T* areas,
+                        const T* normals, const T* gpx, const T* gwx, int nx, const T* gpy,
+                        const T* gwy, int ny, double k, const int32_t* fei, int64_t n_edges,
+                        int64_t row_begin, int64_t row_end, int64_t batch, T* zr, T* zi,
+                        cudaStream_t stream) {
+    (void)nv;
+    if (nf <= 0) return MB_OK;
+    if (nx < 1 || nx > 16 || ny < 1 || ny > 16)
+        return set_error(MB_ERR_UNSUPPORTED, "quadrature order must be in [1, 16] (got %d, %d)", nx, ny);
+    if (!(k > 0)) return set_error(MB_ERR_ARG, "wavenumber must be > 0");
+    constexpr int threads = 128;
+    const int64_t ncol = 3 * nf;
+    const int64_t col_blocks = (ncol + threads - 1) / threads;
+    const int64_t rows = row_end - row_begin;
+    const int64_t blocks = rows * col_blocks;
+    if (blocks <= 0) return MB_OK;
+    if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "mesh too large for one launch");
+    const int ns = ny * ny;
+#define MB_ZMAT_LAUNCH(NSV)                                                                              \
+    do {                                                                                                \
+        if (fei == nullptr)                                                                             \
+            mom_ref_zmat_fe_kernel<T, NSV><<<(unsigned)blocks, threads, 0, stream>>>(                    \
+                verts, faces, areas, normals, gpx, gwx, nx, gpy, gwy, ny, (T)k, nf, batch, col_blocks, zr, \
+                zi);                                                                                    \
+        else                                                                                            \
+            mom_ref_zmat_rwg_kernel<T, NSV><<<(unsigned)blocks, threads, 0, stream>>>(                   \
+                verts, faces, areas, normals, fei, n_edges, gpx, gwx, nx, gpy, gwy, ny, (T)k, nf,        \
+                row_begin, col_blocks, zr);                                                             \
+    } while (0)
+    switch (ns) {
+        case 1: MB_ZMAT_LAUNCH(1); break;
+        case 4: MB_ZMAT_LAUNCH(4); break;
+        case 9: MB_ZMAT_LAUNCH(9); break;
+        case 16: MB_ZMAT_LAUNCH(16); break;
+        default: MB_ZMAT_LAUNCH(0); break;
+    }
+#undef MB_ZMAT_LAUNCH
+    return check_launch("mom_ref_zmat");
+}
+
+template int launch_mom_ref_zmat<float>(const float*, int64_t, const int32_t*, int64_t, const float*,
+                                        const float*, const float*, const float*, int, const float*,
+                                        const float*, int, double, const int32_t*, int64_t, int64_t,
+                                        int64_t, int64_t, float*, float*, cudaStream_t);
+template int launch_mom_ref_zmat<double>(const double*, int64_t, const int32_t*, int64_t, const double*,
+                                         const double*, const double*, const double*, int,
+                                         const double*, const double*, int, double, const int32_t*,
+                                         int64_t, int64_t, int64_t, int64_t, double*, double*,
+                                         cudaStream_t);
+
+// The reference's hard-coded incidence (mesh_MOM_3d.cu:24-70): k along azimuth 30 deg in
+// the xy plane, E along z, H along azimuth -60 deg, eta = 1.
+PlaneWave reference_wave(double k) {
+    const double az = 30.0 / 180.0 * kPi, hdir = az - 0.5 * kPi;
+    return PlaneWave{k * cos(az), k * sin(az), 0.0, 0.0, 0.0, 1.0, cos(hdir), sin(hdir), 0.0};
+}
+
+template <typename T>
+int launch_mom_ref_rhs(const T* verts, const int32_t* faces, int64_t nf, const T* areas,
+                       const T* normals, const T* gp, const T* gw, int n, const PlaneWave* waves_dev,
+                       double k_ref, int nrhs, int out_mode, int64_t batch, const int32_t* fei, T* out_r,
+                       T* out_i, cudaStream_t stream) {
+    if (nf <= 0) return MB_OK;
+    if (n < 1 || n > 16) return set_error(MB_ERR_UNSUPPORTED, "quadrature order must be in [1, 16]");
+    const int threads = 256;
+    const int64_t total = 3 * nf * nrhs;
+    const int64_t blocks = (total + threads - 1) / threads;
+    if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "too many right-hand sides for one launch");
+    mom_ref_rhs_kernel<T><<<(unsigned)blocks, threads, 0, stream>>>(
+        verts, faces, areas, normals, gp, gw, n, waves_dev, reference_wave(k_ref), nrhs, nf, out_mode,
+        batch, fei, out_r, out_i);
+    return check_launch("mom_ref_rhs");
+}
+template int launch_mom_ref_rhs<float>(const float*, const int32_t*, int64_t, const float*, const float*,
+                                       const float*, const float*, int, const PlaneWave*, double, int,
+                                       int, int64_t, const int32_t*, float*, float*, cudaStream_t);
+template int launch_mom_ref_rhs<double>(const double*, const int32_t*, int64_t, const double*,
+                                        const double*, const double*, const double*, int,
+                                        const PlaneWave*, double, int, int, int64_t, const int32_t*,
+                                        double*, double*, cudaStream_t);
+
+template <typename T>
+int launch_mom_interp(const T* verts, const int32_t* faces, const int32_t* fei, const T* areas,
+                      const T* ir, const T* ii, int64_t n_edges, int64_t nf, int64_t nv, int64_t batch,
+                      int mode, T* jr, T* ji, cudaStream_t stream) {
+    if (nf <= 0 || batch <= 0) return MB_OK;
+    const int threads = 256;
+    const int64_t total = batch * nf;
+    const int64_t blocks = (total + threads - 1) / threads;
+    mom_interp_kernel<T><<<(unsigned)blocks, threads, 0, stream>>>(verts, faces, fei, areas, ir, ii,
+                                                                    n_edges, nf, nv, batch, mode, jr, ji);
+    return check_launch("mom_interp");
+}
+template int launch_mom_interp<float>(const float*, const int32_t*, const int32_t*, const float*,
+                                      const float*, const float*, int64_t, int64_t, int64_t, int64_t, int,
+                                      float*, float*, cudaStream_t);
+template int launch_mom_interp<double>(const double*, const int32_t*, const int32_t*, const double*,
+                                       const double*, const double*, int64_t, int64_t, int64_t, int64_t,
+                                       int, double*, double*, cudaStream_t);
+
+}  // namespace mb

@@ -1,0 +1,152 @@
+"""``MeshBEMSolver3d``: the reference's solver facade on the sm_103a kernels.
+
+Same constructor and public methods as ``src/mesh_BEM/mesh_BEM_solver_3d.py:31-373``:
+
+* ``MeshBEMSolver3d(gaussQR, order_type, BEM_type, wavenumber, logger, dtype, device)``
+  builds the test rule (gaussQR) and source rule (gaussQR - 1) (:85-94) and the single,
+  double and rhs layers (:54-83).
+* ``solve_MOM(verts, faces, edges, face_edge_indices) -> vert_Js [1, V, 3] complex``
+  (:96-195).  The face-edge matrix, its scatter onto RWG edges and the excitation scatter
+  are fused into two kernels (``assemble_Z_rwg``, ``assemble_rhs_rwg``); the dense solve is
+  ``torch.linalg.solve`` as in the reference (:174); the interpolation and vertex scatter
+  are one kernel (``interpolate_vert_js``).
+* ``solve(verts, faces, vert_bc_Dirichlet, vert_bc_Neumann, vert_bc_flags, Amat_scaler=None)
+  -> (Neumann [B, V, 1], Dirichlet [B, V, 1])`` (:197-373) for all-Dirichlet data, the only
+  boundary case the reference can run (mixed and Neumann data need its unimplemented
+  hypersingular layer).
+
+Extra keyword ``solver`` selects "lu" (reference behaviour).  All tensors must live on a
+CUDA device: there is no CPU implementation.
+"""
+from __future__ import annotations
+
+from typing import List
+
+import torch
+
+from .layers import DoubleLayer3d, RhsLayer3d, SingleLayer3d
+from .mesh_MOM_3d import (
+    assemble_rhs_rwg,
+    assemble_Z_rwg,
+    interpolate_vert_js,
+    reference_plane_wave,
+)
+from .utils import (
+    BEMType,
+    BoundaryType,
+    compute_face_areas,
+    compute_face_normals,
+    compute_panel_relation,
+    compute_vert_areas,
+    get_gaussion_integration_points_and_weights,
+)
+
+
+class MeshBEMSolver3d:
+    rank = 3
+
+    def __init__(self, gaussQR: int, order_type: int, BEM_type: int, wavenumber: float, logger=None,
+                 dtype: torch.dtype = torch.float32, device: torch.device = torch.device("cpu"),
+                 solver: str = "lu"):
+        self._gaussQR = gaussQR
+        self._order_type = order_type
+        self._BEM_type = BEM_type
+        self._wavenumber = wavenumber
+        self.logger = logger
+        self.device = torch.device(device)
+        self.dtype = dtype
+        if solver not in ("lu",):
+            raise ValueError(f"unknown solver {solver!r}")
+        self.solver = solver
+        self.hypersingular_layer = None
+        kw = dict(gaussQR=gaussQR, order_type=order_type, BEM_type=BEM_type, wavenumber=wavenumber,
+                  logger=logger, dtype=dtype, device=self.device)
+        self.single_layer = SingleLayer3d(**kw)
+        self.double_layer = DoubleLayer3d(**kw)
+        self.rhs_layer = RhsLayer3d(parent=self, **kw)
+        self.gaussian_points_1d_x, self.gaussian_weights_1d_x = \
+            get_gaussion_integration_points_and_weights(gaussQR, device=self.device, dtype=dtype)
+        self.gaussian_points_1d_y, self.gaussian_weights_1d_y = \
+            get_gaussion_integration_points_and_weights(gaussQR - 1, device=self.device, dtype=dtype)
+
+    gaussQR = property(lambda self: self._gaussQR)
+    order_type = property(lambda self: self._order_type)
+    BEM_type = property(lambda self: self._BEM_type)
+    wavenumber = property(lambda self: self._wavenumber)
+
+    def InfoLog(self, *a, **k):
+        return self.logger.InfoLog(*a, **k) if self.logger is not None else None
+
+    # ------------------------------------------------------------------ MoM
+    def _rules_on(self, dev, dt):
+        return [t.to(device=dev, dtype=dt).contiguous() for t in (
+            self.gaussian_points_1d_x, self.gaussian_weights_1d_x,
+            self.gaussian_points_1d_y, self.gaussian_weights_1d_y,
+            self.rhs_layer.gaussian_points_1d, self.rhs_layer.gaussian_weights_1d)]
+
+    def assemble_MOM(self, verts: torch.Tensor, faces: torch.Tensor, n_edges: int,
+                     face_edge_indices: torch.Tensor, waves: torch.Tensor | None = None):
+        """RWG matrix Z [E, E] and excitation [E, n_rhs] (reference wave when ``waves`` is None)."""
+        verts = verts.contiguous()
+        faces = faces.to(torch.int32).contiguous()
+        fei = face_edge_indices.to(torch.int32).reshape(-1).contiguous()
+        dev, dt = verts.device, verts.dtype
+        gpx, gwx, gpy, gwy, gp, gw = self._rules_on(dev, dt)
+        areas = compute_face_areas(vertices=verts, faces=faces, keepdim=True).contiguous()
+        normals = compute_face_normals(vertices=verts, faces=faces).contiguous()
+        Z = assemble_Z_rwg(verts, faces, areas, normals, fei, n_edges, gpx, gwx, gpy, gwy,
+                           self.wavenumber)
+        if waves is None:
+            waves = reference_plane_wave(self.wavenumber, device=dev)
+        rhs = assemble_rhs_rwg(verts, faces, areas, normals, fei, n_edges, gp, gw, waves)
+        return Z, rhs, areas
+
+    def solve_MOM(self, verts: torch.Tensor, faces: torch.Tensor, edges: torch.Tensor,
+                  face_edge_indices: torch.Tensor) -> torch.Tensor:
+        """Mesh-based MoM solve; returns [1, N_verts, 3] complex vertex currents."""
+        assert self._BEM_type == int(BEMType.HELMHOLTZ_MOM)
+        n_edges = edges.shape[0]
+        Z, rhs, areas = self.assemble_MOM(verts, faces, n_edges, face_edge_indices)
+        I_coeff = torch.linalg.solve(Z, rhs)  # [E, 1]
+        fei = face_edge_indices.to(torch.int32).reshape(-1).contiguous()
+        return interpolate_vert_js(verts.contiguous(), faces.to(torch.int32).contiguous(), fei,
+                                   areas, I_coeff.reshape(1, n_edges))
+
+    # ------------------------------------------------------------------ Laplace / BEM
+    def solve(self, verts: torch.Tensor, faces: torch.Tensor, vert_bc_Dirichlet: torch.Tensor,
+              vert_bc_Neumann: torch.Tensor, vert_bc_flags: torch.Tensor,
+              Amat_scaler: float = None) -> List[torch.Tensor]:
+        n_verts = verts.shape[-2]
+        batch = vert_bc_flags.shape[0]
+        faces = faces.to(torch.int32).contiguous()
+        verts = verts.contiguous()
+        areas = compute_face_areas(vertices=verts, faces=faces, keepdim=True).contiguous()
+        normals = compute_face_normals(vertices=verts, faces=faces).contiguous()
+        panel_relations = compute_panel_relation(faces)
+        neu_list, dir_list = [], []
+        V_tight = None
+        for b in range(batch):
+            is_d = vert_bc_flags[b] == int(BoundaryType.DIRICHLET)
+            is_n = vert_bc_flags[b] == int(BoundaryType.NEUMANN)
+            n_d, n_n = int(is_d.sum()), int(is_n.sum())
+            self.InfoLog(f"Batch [{b}]: (Vertex attached) number of Dirichlet B.C. = {n_d}, "
+                         f"number of Neumann B.C. = {n_n}, number of whole zone = "
+                         f"{vert_bc_flags[b].numel()}")
+            if n_n > 0:
+                raise NotImplementedError(
+                    "Neumann / mixed boundary data need the hypersingular operator, which the "
+                    "reference does not implement (integrations_3d.py:440-442)")
+            if V_tight is None:
+                self.single_layer.compute_Vmat(verts, faces, areas, normals, panel_relations)
+                V_tight = self.single_layer.get_Vmat_tight(verts=verts, faces=faces)
+                self.double_layer.compute_Kmat(verts, faces, areas, normals, panel_relations)
+                K_tight = self.double_layer.get_Kmat_tight(verts=verts, faces=faces)
+            self.rhs_layer.compute_rhs(verts, faces, vert_bc_Dirichlet[b:b + 1],
+                                       vert_bc_Neumann[b:b + 1], vert_bc_flags[b:b + 1],
+                                       K_tight=K_tight)
+            rhs = self.rhs_layer.get_rhs_vec().reshape(-1)
+            A = V_tight if Amat_scaler is None else Amat_scaler * V_tight
+            sol = torch.linalg.solve(A, rhs.to(A.dtype))
+            neu_list.append(sol.reshape(n_verts, 1))
+            dir_list.append(vert_bc_Dirichlet[b].reshape(n_verts, 1))
+        return torch.stack(neu_list, 0), torch.stack(dir_list, 0)

@@ -1,0 +1,260 @@
+"""Drop-in for the reference's JIT extension ``mesh_MOM_3d`` plus the RWG-space operators.
+
+The reference builds ``mesh_MOM_3d`` with ``torch.utils.cpp_extension.load``
+(``src/mesh_BEM/kernel_functions.py:14-23``) and exports three in-place forward ops
+(``src/mesh_BEM/cuda/mesh_MOM_3d.cpp:111-121``).  This module exports the same three
+functions with the same argument order, meaning and in-place outputs, backed by
+libmeshbem_gb300 (sm_103a).  Differences from the reference, all in the safe direction:
+inputs are checked (device, dtype, shape, contiguity) and errors raise ``MeshBEMError`` /
+``ValueError`` instead of failing silently; launches go to the caller's current stream
+instead of the legacy default stream; indexing is 64-bit.
+
+``register_torch_ops()`` also exposes them as ``torch.ops.mesh_MOM_3d.*`` (the reference
+registers ``TORCH_LIBRARY(mesh_MOM_3d, m)``).
+
+The RWG-space operators fuse the reference's scatter steps:
+``assemble_Z_rwg`` (face-edge matrix straight into the [E, E] RWG matrix),
+``assemble_rhs_rwg`` (many plane waves at once into [E, n_rhs]),
+``interpolate_vert_js`` (edge coefficients straight to [B, V, 3] vertex currents).
+"""
+from __future__ import annotations
+
+import math
+
+import torch
+
+from . import _lib
+
+_FLOATS = (torch.float32, torch.float64)
+
+
+def _mesh_args(verts, faces, face_areas, face_normals):
+    _lib.check_tensor(verts, "verts", dtype=_FLOATS, ndim=2)
+    dt, dev = verts.dtype, verts.device
+    if verts.shape[1] != 3:
+        raise ValueError("verts must be [N_verts, 3]")
+    _lib.check_tensor(faces, "faces", dtype=torch.int32, device=dev, ndim=2)
+    if faces.shape[1] != 3:
+        raise ValueError("faces must be [N_faces, 3]")
+    nf = faces.shape[0]
+    _lib.check_tensor(face_areas, "face_areas", dtype=dt, device=dev)
+    if face_areas.numel() != nf:
+        raise ValueError("face_areas must have N_faces entries")
+    _lib.check_tensor(face_normals, "face_normals", dtype=dt, device=dev)
+    if face_normals.numel() != 3 * nf:
+        raise ValueError("face_normals must be [N_faces, 3]")
+    return dt, dev, verts.shape[0], nf
+
+
+def _rule(p, w, name, dt, dev):
+    _lib.check_tensor(p, f"{name} points", dtype=dt, device=dev)
+    _lib.check_tensor(w, f"{name} weights", dtype=dt, device=dev)
+    if p.numel() != w.numel():
+        raise ValueError(f"{name}: points and weights differ in length")
+    if not 1 <= p.numel() <= 16:
+        raise ValueError(f"{name}: 1..16 Gauss nodes supported (got {p.numel()})")
+    return p.numel()
+
+
+# ---------------------------------------------------------------------------------------
+# reference-op drop-ins
+# ---------------------------------------------------------------------------------------
+def create_MOM_Zmat_3d_forward(verts, faces, face_areas, face_normals, gaussian_points_1d_x,
+                               gaussian_weights_1d_x, gaussian_points_1d_y, gaussian_weights_1d_y,
+                               face_edge_Zmat_real, face_edge_Zmat_imag, wavenumber):
+    """Face-edge CFIE matrix into [B, 3F, 3F] real/imag outputs (mesh_MOM_3d.cu:332-496)."""
+    dt, dev, nv, nf = _mesh_args(verts, faces, face_areas, face_normals)
+    nx = _rule(gaussian_points_1d_x, gaussian_weights_1d_x, "test rule", dt, dev)
+    ny = _rule(gaussian_points_1d_y, gaussian_weights_1d_y, "source rule", dt, dev)
+    for t, n in ((face_edge_Zmat_real, "face_edge_Zmat_real"), (face_edge_Zmat_imag, "face_edge_Zmat_imag")):
+        _lib.check_tensor(t, n, dtype=dt, device=dev)
+        if t.numel() != t.shape[0] * 9 * nf * nf:
+            raise ValueError(f"{n} must hold [B, 3F, 3F] entries")
+    batch = face_edge_Zmat_real.shape[0]
+    _lib.call(f"mb_mom_zmat_fe_{_lib.sfx(dt)}", _lib.ptr(verts), nv, _lib.ptr(faces), nf,
+              _lib.ptr(face_areas), _lib.ptr(face_normals), _lib.ptr(gaussian_points_1d_x),
+              _lib.ptr(gaussian_weights_1d_x), nx, _lib.ptr(gaussian_points_1d_y),
+              _lib.ptr(gaussian_weights_1d_y), ny, float(wavenumber), batch,
+              _lib.ptr(face_edge_Zmat_real), _lib.ptr(face_edge_Zmat_imag), _lib.stream_of(verts))
+
+
+def create_MOM_rhs_3d_forward(verts, faces, face_areas, face_normals, gaussian_points_1d,
+                              gaussian_weights_1d, face_edge_rhs_real, face_edge_rhs_imag, wavenumber):
+    """Face-edge excitation of the reference's plane wave into [B, F, 3, 1] (mesh_MOM_3d.cu:244-330)."""
+    dt, dev, nv, nf = _mesh_args(verts, faces, face_areas, face_normals)
+    n = _rule(gaussian_points_1d, gaussian_weights_1d, "rule", dt, dev)
+    for t, nm in ((face_edge_rhs_real, "face_edge_rhs_real"), (face_edge_rhs_imag, "face_edge_rhs_imag")):
+        _lib.check_tensor(t, nm, dtype=dt, device=dev)
+        if t.numel() != t.shape[0] * 3 * nf:
+            raise ValueError(f"{nm} must hold [B, F, 3, 1] entries")
+    batch = face_edge_rhs_real.shape[0]
+    _lib.call(f"mb_mom_rhs_fe_{_lib.sfx(dt)}", _lib.ptr(verts), nv, _lib.ptr(faces), nf,
+              _lib.ptr(face_areas), _lib.ptr(face_normals), _lib.ptr(gaussian_points_1d),
+              _lib.ptr(gaussian_weights_1d), n, float(wavenumber), batch,
+              _lib.ptr(face_edge_rhs_real), _lib.ptr(face_edge_rhs_imag), _lib.stream_of(verts))
+
+
+def interpolate_Icoeff_to_Js_3d_forward(verts, faces, face_edge_indices, face_areas, edge_I_coeff_real,
+                                        edge_I_coeff_imag, face_vert_Js_real, face_vert_Js_imag):
+    """Edge coefficients [B, E] -> per-face vertex currents [B, 3F, 3] (+=) (mesh_MOM_3d.cu:498-565)."""
+    _lib.check_tensor(verts, "verts", dtype=_FLOATS, ndim=2)
+    dt, dev = verts.dtype, verts.device
+    _lib.check_tensor(faces, "faces", dtype=torch.int32, device=dev, ndim=2)
+    nf = faces.shape[0]
+    _lib.check_tensor(face_edge_indices, "face_edge_indices", dtype=torch.int32, device=dev)
+    if face_edge_indices.numel() != 3 * nf:
+        raise ValueError("face_edge_indices must have 3F entries")
+    _lib.check_tensor(face_areas, "face_areas", dtype=dt, device=dev)
+    _lib.check_tensor(edge_I_coeff_real, "edge_I_coeff_real", dtype=dt, device=dev)
+    _lib.check_tensor(edge_I_coeff_imag, "edge_I_coeff_imag", dtype=dt, device=dev)
+    batch = face_vert_Js_real.shape[0]
+    n_edges = edge_I_coeff_imag.shape[1]
+    if edge_I_coeff_real.numel() < batch * n_edges:
+        raise ValueError("edge coefficients must be [B, E]")
+    for t, nm in ((face_vert_Js_real, "face_vert_Js_real"), (face_vert_Js_imag, "face_vert_Js_imag")):
+        _lib.check_tensor(t, nm, dtype=dt, device=dev)
+        if t.numel() != batch * 9 * nf:
+            raise ValueError(f"{nm} must be [B, 3F, 3]")
+    if nf:
+        fei_max = int(face_edge_indices.max().item())
+        if fei_max >= n_edges or int(face_edge_indices.min().item()) < 0:
+            raise ValueError("face_edge_indices out of range of the edge coefficients")
+    _lib.call(f"mb_mom_interp_js_{_lib.sfx(dt)}", _lib.ptr(verts), verts.shape[0], _lib.ptr(faces), nf,
+              _lib.ptr(face_edge_indices), _lib.ptr(face_areas), _lib.ptr(edge_I_coeff_real),
+              _lib.ptr(edge_I_coeff_imag), n_edges, batch, _lib.ptr(face_vert_Js_real),
+              _lib.ptr(face_vert_Js_imag), _lib.stream_of(verts))
+
+
+# ---------------------------------------------------------------------------------------
+# RWG-space operators
+# ---------------------------------------------------------------------------------------
+def _check_fei(face_edge_indices, nf, n_edges, dev):
+    _lib.check_tensor(face_edge_indices, "face_edge_indices", dtype=torch.int32, device=dev)
+    if face_edge_indices.numel() != 3 * nf:
+        raise ValueError("face_edge_indices must have 3F entries")
+    if nf and (int(face_edge_indices.max().item()) >= n_edges or int(face_edge_indices.min().item()) < 0):
+        raise ValueError("face_edge_indices out of range [0, n_edges)")
+
+
+def assemble_Z_rwg(verts, faces, face_areas, face_normals, face_edge_indices, n_edges,
+                   gaussian_points_1d_x, gaussian_weights_1d_x, gaussian_points_1d_y,
+                   gaussian_weights_1d_y, wavenumber, out=None, rows=None, check_indices=True):
+    """RWG impedance matrix Z [E, E] complex (complex64 for float32 meshes).
+
+    Same entries as ``create_MOM_Zmat_3d_forward`` followed by the reference's
+    ``scatter_add_`` onto face_edge_indices (mesh_BEM_solver_3d.py:128-147), in one pass.
+    ``out`` (complex [E, E]) is accumulated into if given, else a zeroed matrix is made.
+    ``rows`` = (begin, end) restricts the face-edge test rows (for chunked assembly).
+    """
+    dt, dev, nv, nf = _mesh_args(verts, faces, face_areas, face_normals)
+    nx = _rule(gaussian_points_1d_x, gaussian_weights_1d_x, "test rule", dt, dev)
+    ny = _rule(gaussian_points_1d_y, gaussian_weights_1d_y, "source rule", dt, dev)
+    if check_indices:
+        _check_fei(face_edge_indices, nf, n_edges, dev)
+    cdt = torch.complex64 if dt == torch.float32 else torch.complex128
+    if out is None:
+        out = torch.zeros((n_edges, n_edges), dtype=cdt, device=dev)
+    else:
+        _lib.check_tensor(out, "out", dtype=cdt, device=dev, shape=(n_edges, n_edges))
+    r0, r1 = (0, 3 * nf) if rows is None else rows
+    _lib.call(f"mb_mom_zmat_rwg_{_lib.csfx(dt)}", _lib.ptr(verts), nv, _lib.ptr(faces), nf,
+              _lib.ptr(face_areas), _lib.ptr(face_normals), _lib.ptr(face_edge_indices), n_edges,
+              _lib.ptr(gaussian_points_1d_x), _lib.ptr(gaussian_weights_1d_x), nx,
+              _lib.ptr(gaussian_points_1d_y), _lib.ptr(gaussian_weights_1d_y), ny, float(wavenumber),
+              int(r0), int(r1), _lib.ptr(out), _lib.stream_of(verts))
+    return out
+
+
+def plane_waves(wavenumber: float, directions, polarizations, eta: float = 1.0,
+                device=None) -> torch.Tensor:
+    """Pack plane waves for ``assemble_rhs_rwg``: [n, 9] float64 (k*khat, E, khat x E / eta)."""
+    d = torch.as_tensor(directions, dtype=torch.float64).reshape(-1, 3)
+    e = torch.as_tensor(polarizations, dtype=torch.float64).reshape(-1, 3)
+    d = d / d.norm(dim=-1, keepdim=True)
+    h = torch.cross(d, e, dim=-1) / eta
+    return torch.cat((wavenumber * d, e, h), dim=-1).contiguous().to(device)
+
+
+def reference_plane_wave(wavenumber: float, device=None) -> torch.Tensor:
+    """The reference's hard-coded incidence (mesh_MOM_3d.cu:24-70) in ``plane_waves`` form."""
+    az = 30 / 180.0 * math.pi
+    hdir = az - 0.5 * math.pi
+    w = torch.tensor([[wavenumber * math.cos(az), wavenumber * math.sin(az), 0.0, 0.0, 0.0, 1.0,
+                       math.cos(hdir), math.sin(hdir), 0.0]], dtype=torch.float64)
+    return w.to(device)
+
+
+def assemble_rhs_rwg(verts, faces, face_areas, face_normals, face_edge_indices, n_edges,
+                     gaussian_points_1d, gaussian_weights_1d, waves, out=None):
+    """Excitation vectors [E, n_rhs] complex for the plane waves ``waves`` ([n_rhs, 9] float64)."""
+    dt, dev, nv, nf = _mesh_args(verts, faces, face_areas, face_normals)
+    n = _rule(gaussian_points_1d, gaussian_weights_1d, "rule", dt, dev)
+    _check_fei(face_edge_indices, nf, n_edges, dev)
+    waves = waves.to(device=dev, dtype=torch.float64).contiguous()
+    _lib.check_tensor(waves, "waves", dtype=torch.float64, device=dev, ndim=2)
+    if waves.shape[1] != 9:
+        raise ValueError("waves must be [n_rhs, 9]")
+    n_rhs = waves.shape[0]
+    cdt = torch.complex64 if dt == torch.float32 else torch.complex128
+    if out is None:
+        out = torch.zeros((n_edges, n_rhs), dtype=cdt, device=dev)
+    else:
+        _lib.check_tensor(out, "out", dtype=cdt, device=dev, shape=(n_edges, n_rhs))
+    _lib.call(f"mb_mom_rhs_rwg_{_lib.csfx(dt)}", _lib.ptr(verts), nv, _lib.ptr(faces), nf,
+              _lib.ptr(face_areas), _lib.ptr(face_normals), _lib.ptr(face_edge_indices), n_edges,
+              _lib.ptr(gaussian_points_1d), _lib.ptr(gaussian_weights_1d), n, _lib.ptr(waves), n_rhs,
+              _lib.ptr(out), _lib.stream_of(verts))
+    return out
+
+
+def interpolate_vert_js(verts, faces, face_edge_indices, face_areas, i_coeff, out=None):
+    """Edge coefficients [B, E] complex -> vertex currents [B, V, 3] complex."""
+    _lib.check_tensor(verts, "verts", dtype=_FLOATS, ndim=2)
+    dt, dev = verts.dtype, verts.device
+    _lib.check_tensor(faces, "faces", dtype=torch.int32, device=dev, ndim=2)
+    nf, nv = faces.shape[0], verts.shape[0]
+    cdt = torch.complex64 if dt == torch.float32 else torch.complex128
+    i_coeff = i_coeff.reshape(i_coeff.shape[0] if i_coeff.dim() > 1 else 1, -1).to(cdt).contiguous()
+    batch, n_edges = i_coeff.shape
+    _check_fei(face_edge_indices, nf, n_edges, dev)
+    _lib.check_tensor(face_areas, "face_areas", dtype=dt, device=dev)
+    if out is None:
+        out = torch.zeros((batch, nv, 3), dtype=cdt, device=dev)
+    else:
+        _lib.check_tensor(out, "out", dtype=cdt, device=dev, shape=(batch, nv, 3))
+    _lib.call(f"mb_mom_interp_vert_{_lib.csfx(dt)}", _lib.ptr(verts), nv, _lib.ptr(faces), nf,
+              _lib.ptr(face_edge_indices), _lib.ptr(face_areas), _lib.ptr(i_coeff), n_edges, batch,
+              _lib.ptr(out), _lib.stream_of(verts))
+    return out
+
+
+# ---------------------------------------------------------------------------------------
+# torch.ops registration (TORCH_LIBRARY(mesh_MOM_3d), mesh_MOM_3d.cpp:117-121)
+# ---------------------------------------------------------------------------------------
+_registered = None
+
+
+def register_torch_ops():
+    """Expose the three reference ops as ``torch.ops.mesh_MOM_3d.*`` (CUDA dispatch key)."""
+    global _registered
+    if _registered is not None:
+        return _registered
+    lib = torch.library.Library("mesh_MOM_3d", "DEF")
+    lib.define(
+        "create_MOM_rhs_3d_forward(Tensor verts, Tensor faces, Tensor face_areas, Tensor face_normals, "
+        "Tensor gaussian_points_1d, Tensor gaussian_weights_1d, Tensor(a!) face_edge_rhs_real, "
+        "Tensor(b!) face_edge_rhs_imag, float wavenumber) -> ()")
+    lib.define(
+        "create_MOM_Zmat_3d_forward(Tensor verts, Tensor faces, Tensor face_areas, Tensor face_normals, "
+        "Tensor gaussian_points_1d_x, Tensor gaussian_weights_1d_x, Tensor gaussian_points_1d_y, "
+        "Tensor gaussian_weights_1d_y, Tensor(a!) face_edge_Zmat_real, Tensor(b!) face_edge_Zmat_imag, "
+        "float wavenumber) -> ()")
+    lib.define(
+        "interpolate_Icoeff_to_Js_3d_forward(Tensor verts, Tensor faces, Tensor face_edge_indices, "
+        "Tensor face_areas, Tensor edge_I_coeff_real, Tensor edge_I_coeff_imag, "
+        "Tensor(a!) face_vert_Js_real, Tensor(b!) face_vert_Js_imag) -> ()")
+    lib.impl("create_MOM_rhs_3d_forward", create_MOM_rhs_3d_forward, "CUDA")
+    lib.impl("create_MOM_Zmat_3d_forward", create_MOM_Zmat_3d_forward, "CUDA")
+    lib.impl("interpolate_Icoeff_to_Js_3d_forward", interpolate_Icoeff_to_Js_3d_forward, "CUDA")
+    _registered = lib
+    return lib

@@ -1,0 +1,197 @@
+"""numpy front end of the CPU oracle (test infrastructure only).
+
+Wraps ``oracle/_build/libmeshbem_oracle.so`` (the C restatement) and, where it was built,
+``oracle/_ref/libref_mom.so`` (the reference's own kernel bodies compiled for the host).
+Only tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` use it.
+
+Every function takes numpy arrays and returns new numpy arrays; ``dtype`` selects the
+float64 or float32 build.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build_oracle as _bo
+
+_lib = None
+_ref = None
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I = ctypes.c_int
+_D = ctypes.c_double
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        path = _bo.build()
+        lib = ctypes.CDLL(path)
+        for sfx in ("f64", "f32"):
+            getattr(lib, f"orc_mom_zmat_fe_{sfx}").argtypes = [
+                _P, _P, _I64, _P, _P, _P, _P, _I, _P, _P, _I, _D, _I64, _I64, _P, _P]
+            getattr(lib, f"orc_mom_rhs_fe_{sfx}").argtypes = [
+                _P, _P, _I64, _P, _P, _P, _P, _I, _D, _I, _P, _P, _D, _P, _P]
+            getattr(lib, f"orc_mom_interp_js_{sfx}").argtypes = [
+                _P, _P, _P, _I64, _P, _P, _P, _I64, _I64, _P, _P]
+            getattr(lib, f"orc_laplace_panels_{sfx}").argtypes = [
+                _P, _P, _I64, _P, _P, _P, _P, _I, _P, _I, _I, _I, _D, _I64, _I64, _P, _P]
+            getattr(lib, f"orc_panel_relation_{sfx}").argtypes = [_P, _I64, _P]
+        _lib = lib
+    return _lib
+
+
+def ref_lib():
+    """The host build of the reference kernels, or None where the checkout is absent."""
+    global _ref
+    if _ref is None:
+        path = _bo.build_ref()
+        if path is None:
+            return None
+        lib = ctypes.CDLL(path)
+        lib.ref_zmat_f64.argtypes = [_P, _P, _P, _P, _P, _P, _I, _P, _P, _I, _P, _P, _I, _I, _D]
+        lib.ref_zmat_f32.argtypes = [_P, _P, _P, _P, _P, _P, _I, _P, _P, _I, _P, _P, _I, _I, _D]
+        lib.ref_rhs_f64.argtypes = [_P, _P, _P, _P, _P, _P, _I, _P, _P, _I, _I, _D]
+        lib.ref_interp_f64.argtypes = [_P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I]
+        _ref = lib
+    return _ref
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _sfx(dtype):
+    return "f64" if np.dtype(dtype) == np.float64 else "f32"
+
+
+def mom_zmat_fe(verts, faces, areas, normals, gpx, gwx, gpy, gwy, k, rows=None, dtype=np.float64):
+    """Face-edge CFIE matrix [3F, 3F] complex (rows: optional (begin, end) slice)."""
+    lib = _load()
+    v, f = _c(verts, dtype), _c(faces, np.int32)
+    a, n = _c(np.reshape(areas, -1), dtype), _c(normals, dtype)
+    gpx, gwx, gpy, gwy = (_c(t, dtype) for t in (gpx, gwx, gpy, gwy))
+    nf = f.shape[0]
+    r0, r1 = (0, 3 * nf) if rows is None else rows
+    zr = np.zeros((r1 - r0, 3 * nf), dtype)
+    zi = np.zeros_like(zr)
+    getattr(lib, f"orc_mom_zmat_fe_{_sfx(dtype)}")(
+        _ptr(v), _ptr(f), nf, _ptr(a), _ptr(n), _ptr(gpx), _ptr(gwx), gpx.size,
+        _ptr(gpy), _ptr(gwy), gpy.size, float(k), r0, r1, _ptr(zr), _ptr(zi))
+    return zr + 1j * zi
+
+
+def mom_rhs_fe(verts, faces, areas, normals, gp, gw, k, khat=None, e0=None, eta=1.0,
+               dtype=np.float64):
+    """Face-edge excitation [F, 3] complex.  khat/e0 None -> the reference's hard-coded wave."""
+    lib = _load()
+    v, f = _c(verts, dtype), _c(faces, np.int32)
+    a, n = _c(np.reshape(areas, -1), dtype), _c(normals, dtype)
+    gp, gw = _c(gp, dtype), _c(gw, dtype)
+    nf = f.shape[0]
+    rr = np.zeros(3 * nf, dtype)
+    ri = np.zeros_like(rr)
+    ref = khat is None
+    kh = _c([1, 0, 0] if ref else khat, np.float64)
+    ee = _c([0, 0, 1] if ref else e0, np.float64)
+    getattr(lib, f"orc_mom_rhs_fe_{_sfx(dtype)}")(
+        _ptr(v), _ptr(f), nf, _ptr(a), _ptr(n), _ptr(gp), _ptr(gw), gp.size, float(k),
+        1 if ref else 0, _ptr(kh), _ptr(ee), float(eta), _ptr(rr), _ptr(ri))
+    return (rr + 1j * ri).reshape(nf, 3)
+
+
+def mom_interp_js(verts, faces, fei, areas, icoeff, dtype=np.float64):
+    """Per-face vertex currents [B, 3F, 3] complex from edge coefficients icoeff [B, E]."""
+    lib = _load()
+    v, f, e = _c(verts, dtype), _c(faces, np.int32), _c(np.reshape(fei, -1), np.int32)
+    a = _c(np.reshape(areas, -1), dtype)
+    icoeff = np.atleast_2d(icoeff)
+    b, ne = icoeff.shape
+    ir, ii = _c(icoeff.real, dtype), _c(icoeff.imag, dtype)
+    nf = f.shape[0]
+    jr = np.zeros((b, 3 * nf, 3), dtype)
+    ji = np.zeros_like(jr)
+    getattr(lib, f"orc_mom_interp_js_{_sfx(dtype)}")(
+        _ptr(v), _ptr(f), _ptr(e), nf, _ptr(a), _ptr(ir), _ptr(ii), ne, b, _ptr(jr), _ptr(ji))
+    return jr + 1j * ji
+
+
+def panel_relation(faces):
+    lib = _load()
+    f = _c(faces, np.int32)
+    nf = f.shape[0]
+    rel = np.zeros((nf, nf), np.uint8)
+    lib.orc_panel_relation_f64(_ptr(f), nf, _ptr(rel))
+    return rel
+
+
+def laplace_panels(verts, faces, areas, normals, rands, weights, rel, layer, order, kind=0,
+                   k=1.0, rows=None, dtype=np.float64):
+    """double_integration_on_panels_3d: [F, F, nphi, nphi] (complex when kind=1)."""
+    lib = _load()
+    v, f = _c(verts, dtype), _c(faces, np.int32)
+    a, n = _c(np.reshape(areas, -1), dtype), _c(normals, dtype)
+    rd, w = _c(np.reshape(rands, (-1, 2)), dtype), _c(np.reshape(weights, -1), dtype)
+    rel = _c(rel, np.uint8)
+    nf = f.shape[0]
+    r0, r1 = (0, nf) if rows is None else rows
+    nphi = 3 if order == 1 else 1
+    out_r = np.zeros((r1 - r0, nf, nphi, nphi), dtype)
+    out_i = np.zeros_like(out_r) if kind == 1 else None
+    getattr(lib, f"orc_laplace_panels_{_sfx(dtype)}")(
+        _ptr(v), _ptr(f), nf, _ptr(a), _ptr(n), _ptr(rd), _ptr(w), w.size, _ptr(rel),
+        int(layer), int(order), int(kind), float(k), r0, r1, _ptr(out_r), _ptr(out_i))
+    return out_r if kind == 0 else out_r + 1j * out_i
+
+
+# ---- reference kernels compiled for the host (pinning only) ----------------------------
+
+def ref_zmat_fe(verts, faces, areas, normals, gpx, gwx, gpy, gwy, k, dtype=np.float64):
+    lib = ref_lib()
+    if lib is None:
+        raise RuntimeError("reference checkout not available")
+    v, f = _c(verts, dtype), _c(faces, np.int32)
+    a, n = _c(np.reshape(areas, -1), dtype), _c(normals, dtype)
+    gpx, gwx, gpy, gwy = (_c(t, dtype) for t in (gpx, gwx, gpy, gwy))
+    nf = f.shape[0]
+    zr = np.zeros((3 * nf, 3 * nf), dtype)
+    zi = np.zeros_like(zr)
+    fn = lib.ref_zmat_f64 if np.dtype(dtype) == np.float64 else lib.ref_zmat_f32
+    fn(_ptr(v), _ptr(f), _ptr(a), _ptr(n), _ptr(gpx), _ptr(gwx), gpx.size, _ptr(gpy), _ptr(gwy),
+       gpy.size, _ptr(zr), _ptr(zi), v.shape[0], nf, float(k))
+    return zr + 1j * zi
+
+
+def ref_rhs_fe(verts, faces, areas, normals, gp, gw, k):
+    lib = ref_lib()
+    v, f = _c(verts, np.float64), _c(faces, np.int32)
+    a, n = _c(np.reshape(areas, -1), np.float64), _c(normals, np.float64)
+    gp, gw = _c(gp, np.float64), _c(gw, np.float64)
+    nf = f.shape[0]
+    rr = np.zeros(3 * nf)
+    ri = np.zeros(3 * nf)
+    lib.ref_rhs_f64(_ptr(v), _ptr(f), _ptr(a), _ptr(n), _ptr(gp), _ptr(gw), gp.size, _ptr(rr),
+                    _ptr(ri), v.shape[0], nf, float(k))
+    return (rr + 1j * ri).reshape(nf, 3)
+
+
+def ref_interp_js(verts, faces, fei, areas, icoeff):
+    lib = ref_lib()
+    v, f, e = _c(verts, np.float64), _c(faces, np.int32), _c(np.reshape(fei, -1), np.int32)
+    a = _c(np.reshape(areas, -1), np.float64)
+    icoeff = np.atleast_2d(icoeff)
+    b, ne = icoeff.shape
+    ir, ii = _c(icoeff.real, np.float64), _c(icoeff.imag, np.float64)
+    nf = f.shape[0]
+    jr = np.zeros((b, 3 * nf, 3))
+    ji = np.zeros((b, 3 * nf, 3))
+    lib.ref_interp_f64(_ptr(v), _ptr(f), _ptr(e), _ptr(a), _ptr(ir), _ptr(ii), _ptr(jr), _ptr(ji),
+                       v.shape[0], nf, ne, b)
+    return jr + 1j * ji

@@ -1,0 +1,133 @@
+"""Host-side logic on the CPU: tables, mesh helpers, rule flattening, the C ABI surface."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import REPO, rel_err
+
+
+def test_gauss_tables_match_reference(pkg, gauss_golden):
+    U = pkg.utils
+    prev = torch.get_default_dtype()
+    torch.set_default_dtype(torch.float64)
+    try:
+        for n in (1, 2, 3, 4, 5, 6, 7, 8, 12):
+            p, w = U.get_gaussion_integration_points_and_weights(n, dtype=torch.float64)
+            assert np.abs(p.numpy() - gauss_golden[f"p{n}"]).max() < 1e-15
+            assert np.abs(w.numpy() - gauss_golden[f"w{n}"]).max() < 1e-15
+    finally:
+        torch.set_default_dtype(prev)
+    # with the default float32 dtype the reference's tables are float32-rounded before the
+    # map to [0, 1] (done in the solver dtype)
+    torch.set_default_dtype(torch.float32)
+    p, _ = U.get_gaussion_integration_points_and_weights(4, dtype=torch.float64)
+    x32 = (np.polynomial.legendre.leggauss(4)[0].astype(np.float32).astype(np.float64) + 1.0) / 2.0
+    assert np.array_equal(p.numpy(), x32)
+    torch.set_default_dtype(prev)
+    with pytest.raises(NotImplementedError):
+        U.get_gaussion_integration_points_and_weights(9)
+
+
+@pytest.mark.parametrize("name", ["ico0", "ico1", "ell1"])
+def test_mesh_helpers_match_reference(pkg, golden, name):
+    U = pkg.utils
+    g = golden[name]
+    v = torch.tensor(g["verts"])
+    f = torch.tensor(g["faces"])
+    assert np.array_equal(U.compute_face_areas(v, f).numpy(), g["face_areas"])
+    assert np.array_equal(U.compute_face_normals(v, f).numpy(), g["face_normals"])
+    assert np.abs(U.compute_vert_areas(v, f).numpy() - g["vert_areas"]).max() < 1e-15
+    edges, fei, adj = U.get_edge_unique(v, f)
+    assert np.array_equal(edges.numpy(), g["edges"])
+    assert np.array_equal(fei.numpy(), g["face_edge_indices"])
+    assert np.array_equal(adj.numpy(), g["edge_adjacent_faces"])
+
+
+def test_rule_table_reproduces_reference_panels(pkg, golden, oracle):
+    """The flattened sub-domain table, walked on the host, reproduces the reference's V."""
+    U = pkg.utils
+    g = golden["ico0"]
+    rands = torch.tensor(g["lap_gq2_o1_rands"])
+    w = torch.tensor(g["lap_gq2_o1_weights"])
+    table, seg = U.panel_rule_table(rands, rands, w, w)
+    assert seg[0] == 0 and seg[-1] == table.shape[0] == 16 * (1 + 2 + 5 + 3)
+    tab = table.numpy()
+    verts, faces, areas = g["verts"], g["faces"], g["face_areas"].reshape(-1)
+    rel = g["panel_relations"]
+    out = np.zeros((20, 20, 3, 3))
+    for fy in range(20):
+        Y = verts[faces[fy]]
+        for fx in range(20):
+            X = verts[faces[fx]]
+            r = rel[fy, fx]
+            t = tab[seg[r]:seg[r + 1]]
+            x = (1 - t[:, 0:1]) * X[0] + (t[:, 0:1] - t[:, 1:2]) * X[1] + t[:, 1:2] * X[2]
+            y = (1 - t[:, 2:3]) * Y[0] + (t[:, 2:3] - t[:, 3:4]) * Y[1] + t[:, 3:4] * Y[2]
+            G = 1 / (4 * np.pi * np.linalg.norm(x - y, axis=1))
+            py = np.stack([1 - t[:, 2], t[:, 2] - t[:, 3], t[:, 3]], 1)
+            px = np.stack([1 - t[:, 0], t[:, 0] - t[:, 1], t[:, 1]], 1)
+            out[fy, fx] = np.einsum("q,qa,qb->ab", G * t[:, 4], py, px) * 4 * areas[fy] * areas[fx]
+    assert rel_err(out, g["lap_gq2_o1_V_unpacked"]) < 1e-12
+
+
+def test_meshes_are_closed_and_outward(pkg):
+    for lvl in range(4):
+        v, f = pkg.meshes.icosphere(lvl)
+        assert f.shape[0] == 20 * 4 ** lvl and v.shape[0] == 10 * 4 ** lvl + 2
+        vt, ft = torch.tensor(v), torch.tensor(f)
+        edges, fei, adj = pkg.utils.get_edge_unique(vt, ft)
+        assert edges.shape[0] == 30 * 4 ** lvl
+        counts = np.bincount(fei.numpy(), minlength=edges.shape[0])
+        assert np.all(counts == 2)
+        n = pkg.utils.compute_face_normals(vt, ft).numpy()
+        c = v[f].mean(axis=1)
+        assert np.all((n * c).sum(1) > 0)
+    v, f = pkg.meshes.ellipsoid(2, seed=0)
+    v2, _ = pkg.meshes.ellipsoid(2, seed=0)
+    assert np.array_equal(v, v2)
+    v, f = pkg.meshes.star_shape(2, seed=5)
+    r = np.linalg.norm(v, axis=1)
+    assert r.min() > 0.3 and np.isfinite(r).all()
+    d = pkg.meshes.fibonacci_lattice(256)
+    assert np.allclose(np.linalg.norm(d, axis=1), 1.0)
+
+
+def _header_symbols():
+    hdr = open(os.path.join(REPO, "include", "mesh_bem_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(mb_[a-z0-9_]+)\s*\(", hdr)))
+
+
+def test_capi_library_exports_header_symbols(pkg):
+    from importlib import import_module
+
+    build = import_module("mesh-ferrofluid_gb300.build")
+    if not os.path.exists(build.LIB):
+        build.build()
+    lib = ctypes.CDLL(build.LIB)
+    syms = _header_symbols()
+    assert len(syms) >= 19
+    for s in syms:
+        assert hasattr(lib, s), s
+    lib.mb_abi_version.restype = ctypes.c_int
+    assert lib.mb_abi_version() == 1
+    # the Python binding declares exactly the header's entry points
+    from importlib import import_module as im
+
+    bound = set(im("mesh-ferrofluid_gb300._lib").exported_symbols())
+    assert bound == set(syms)
+
+
+def test_ops_reject_cpu_tensors(pkg):
+    """No CPU fallback: host tensors are refused before any launch."""
+    v = torch.zeros((3, 3))
+    f = torch.zeros((1, 3), dtype=torch.int32)
+    a = torch.ones((1, 1))
+    n = torch.zeros((1, 3))
+    p, w = pkg.utils.get_gaussion_integration_points_and_weights(2)
+    z = torch.zeros((1, 3, 3))
+    with pytest.raises(ValueError, match="CUDA"):
+        pkg.mesh_MOM_3d.create_MOM_Zmat_3d_forward(v, f, a, n, p, w, p, w, z, z.clone(), 1.0)

@@ -1,0 +1,129 @@
+"""GPU parity of the Laplace single/double-layer path against the reference's own results.
+
+The golden fixtures come from the reference's ``MeshBEMSolver3d.solve`` run in float64
+(tests/golden/make_golden.py).  Tolerances: 1e-10 (float64), 1e-5 (float32 vs float64
+oracle), relative Frobenius.
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _mesh(g, dev, dt):
+    v = torch.tensor(g["verts"], dtype=dt, device=dev)
+    f = torch.tensor(g["faces"], dtype=torch.int32, device=dev)
+    a = torch.tensor(g["face_areas"], dtype=dt, device=dev)
+    n = torch.tensor(g["face_normals"], dtype=dt, device=dev)
+    return v, f, a, n
+
+
+CASES = [("ico0", 2, 1), ("ico0", 3, 1), ("ico0", 2, 0), ("ell1", 2, 1)]
+
+
+@pytest.mark.parametrize("name,gq,order", CASES)
+@pytest.mark.parametrize("layer", [1, 2])
+def test_panels_f64_match_reference(pkg, cuda, golden, name, gq, order, layer):
+    g = golden[name]
+    v, f, a, n = _mesh(g, cuda, torch.float64)
+    tag = f"lap_gq{gq}_o{order}"
+    rands = torch.tensor(g[f"{tag}_rands"], device=cuda)
+    w = torch.tensor(g[f"{tag}_weights"], device=cuda)
+    rel = torch.tensor(g["panel_relations"], device=cuda)
+    out = pkg.double_integration_on_panels_3d(int(pkg.BEMType.LAPLACE), order, v, f, a, n, w, w, rands,
+                                              rands, rel, 1.0, layer)
+    key = f"{tag}_{'V' if layer == 1 else 'K'}_unpacked"
+    got = out.cpu().numpy()
+    if key in g:
+        assert rel_err(got, g[key]) < 1e-10
+    elif key + "_rows" in g:
+        ref = g[key + "_rows"]
+        assert rel_err(got[: ref.shape[0]], ref) < 1e-10
+    fro = float(g[f"{tag}_{'V' if layer == 1 else 'K'}_fro"])
+    assert abs(np.linalg.norm(got) / fro - 1) < 1e-10
+    # packing (pack_matrix_tight) of the same matrix
+    packed = pkg.utils.pack_matrix_tight(order, out, v, f).cpu().numpy()
+    assert rel_err(packed, g[f"{tag}_{'V' if layer == 1 else 'K'}_packed"]) < 1e-10
+
+
+def test_panels_relation_derived_on_device(pkg, cuda, golden):
+    g = golden["ell1"]
+    v, f, a, n = _mesh(g, cuda, torch.float64)
+    rel = pkg.utils.compute_panel_relation(f)
+    assert np.array_equal(rel.cpu().numpy(), g["panel_relations"])
+    rands = torch.tensor(g["lap_gq2_o1_rands"], device=cuda)
+    w = torch.tensor(g["lap_gq2_o1_weights"], device=cuda)
+    a1 = pkg.double_integration_on_panels_3d(0, 1, v, f, a, n, w, w, rands, rands, rel, 1.0, 1)
+    a2 = pkg.double_integration_on_panels_3d(0, 1, v, f, a, n, w, w, rands, rands, None, 1.0, 1)
+    assert torch.equal(a1, a2)
+
+
+@pytest.mark.parametrize("layer", [1, 2])
+@pytest.mark.parametrize("order", [0, 1])
+def test_panels_f32_vs_oracle(pkg, cuda, oracle, layer, order):
+    v_np, f_np = pkg.meshes.ellipsoid(2, jitter=0.02, seed=1)
+    v = torch.tensor(v_np, dtype=torch.float32, device=cuda)
+    f = torch.tensor(f_np, dtype=torch.int32, device=cuda)
+    a = pkg.utils.compute_face_areas(v, f).contiguous()
+    n = pkg.utils.compute_face_normals(v, f).contiguous()
+    p, w1 = pkg.utils.get_gaussion_integration_points_and_weights(3, device=cuda)
+    rands, w = pkg.utils.collapsed_rule_2d(p, w1)
+    rel = pkg.utils.compute_panel_relation(f)
+    out = pkg.double_integration_on_panels_3d(0, order, v, f, a, n, w, w, rands, rands, rel, 1.0, layer)
+    h = lambda t: t.cpu().double().numpy()  # noqa: E731
+    ref = oracle.laplace_panels(h(v), f_np, h(a), h(n), h(rands), h(w), rel.cpu().numpy(), layer, order)
+    assert rel_err(out.cpu().numpy(), ref) < 1e-5
+
+
+@pytest.mark.parametrize("layer", [1, 2])
+def test_panels_helmholtz_f64_vs_oracle(pkg, cuda, oracle, layer):
+    v_np, f_np = pkg.meshes.icosphere(1)
+    v = torch.tensor(v_np, dtype=torch.float64, device=cuda)
+    f = torch.tensor(f_np, dtype=torch.int32, device=cuda)
+    a = pkg.utils.compute_face_areas(v, f).contiguous()
+    n = pkg.utils.compute_face_normals(v, f).contiguous()
+    p, w1 = pkg.utils.get_gaussion_integration_points_and_weights(2, device=cuda, dtype=torch.float64)
+    rands, w = pkg.utils.collapsed_rule_2d(p, w1)
+    rel = pkg.utils.compute_panel_relation(f)
+    out = pkg.double_integration_on_panels_3d(int(pkg.BEMType.HELMHOLTZ_BEM), 1, v, f, a, n, w, w, rands,
+                                              rands, rel, 3.0, layer)
+    h = lambda t: t.cpu().double().numpy()  # noqa: E731
+    ref = oracle.laplace_panels(h(v), f_np, h(a), h(n), h(rands), h(w), rel.cpu().numpy(), layer, 1,
+                                kind=1, k=3.0)
+    assert rel_err(out.cpu().numpy(), ref) < 1e-10
+
+
+@pytest.mark.parametrize("name,gq,order", [("ico0", 2, 1), ("ico1", 2, 1), ("ico1", 3, 1),
+                                           ("ell1", 2, 1), ("ell1", 2, 0)])
+def test_solve_f64_matches_reference(pkg, cuda, golden, name, gq, order):
+    g = golden[name]
+    torch.set_default_dtype(torch.float64)
+    try:
+        solver = pkg.MeshBEMSolver3d(gaussQR=gq, order_type=order, BEM_type=int(pkg.BEMType.LAPLACE),
+                                     wavenumber=1.0, logger=None, dtype=torch.float64, device=cuda)
+    finally:
+        torch.set_default_dtype(torch.float32)
+    v = torch.tensor(g["verts"], dtype=torch.float64, device=cuda)
+    f = torch.tensor(g["faces"], dtype=torch.int32, device=cuda)
+    fv = (v[:, 0] ** 2 - v[:, 1] ** 2).reshape(1, -1, 1)
+    flags = torch.zeros_like(fv, dtype=torch.uint8)
+    neu, dirv = solver.solve(v, f, fv, torch.zeros_like(fv), flags)
+    tag = f"lap_gq{gq}_o{order}"
+    assert rel_err(solver.rhs_layer.get_rhs_vec().cpu().numpy(), g[f"{tag}_rhs"]) < 1e-10
+    assert rel_err(neu.cpu().numpy(), g[f"{tag}_neumann"]) < 1e-9
+    assert rel_err(dirv.cpu().numpy(), g[f"{tag}_dirichlet"]) == 0.0
+
+
+def test_neumann_data_rejected(pkg, cuda):
+    v_np, f_np = pkg.meshes.icosphere(1)
+    v = torch.tensor(v_np, dtype=torch.float32, device=cuda)
+    f = torch.tensor(f_np, dtype=torch.int32, device=cuda)
+    solver = pkg.MeshBEMSolver3d(gaussQR=2, order_type=1, BEM_type=0, wavenumber=1.0, logger=None,
+                                 dtype=torch.float32, device=cuda)
+    fv = torch.zeros((1, v.shape[0], 1), device=cuda)
+    flags = torch.ones_like(fv, dtype=torch.uint8)
+    with pytest.raises(NotImplementedError):
+        solver.solve(v, f, fv, fv, flags)

@@ -1,0 +1,239 @@
+"""GPU parity of the RWG MoM operators against the reference's own results and the oracle.
+
+Tolerances (relative Frobenius): 1e-10 for float64 paths, 1e-5 for float32 paths against
+the float64 oracle (the reference's FP32 build is itself ~1e-6 away from its FP64 result).
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-10
+TOL32 = 1e-5
+
+
+def _dev_mesh(g, dev, dt):
+    v = torch.tensor(g["verts"], dtype=dt, device=dev)
+    f = torch.tensor(g["faces"], dtype=torch.int32, device=dev)
+    a = torch.tensor(g["face_areas"], dtype=dt, device=dev)
+    n = torch.tensor(g["face_normals"], dtype=dt, device=dev)
+    return v, f, a, n
+
+
+def _rules(pkg, gq, dev, dt):
+    U = pkg.utils
+    torch.set_default_dtype(torch.float64)  # the golden run used float64 literal tables
+    try:
+        px, wx = U.get_gaussion_integration_points_and_weights(gq, device=dev, dtype=dt)
+        py, wy = U.get_gaussion_integration_points_and_weights(gq - 1, device=dev, dtype=dt)
+    finally:
+        torch.set_default_dtype(torch.float32)
+    return px, wx, py, wy
+
+
+@pytest.mark.parametrize("name", ["ico0", "ico1", "ell1"])
+@pytest.mark.parametrize("gq", [4, 3])
+def test_zmat_fe_f64_matches_reference(pkg, cuda, golden, name, gq):
+    g = golden[name]
+    v, f, a, n = _dev_mesh(g, cuda, torch.float64)
+    px, wx, py, wy = _rules(pkg, gq, cuda, torch.float64)
+    nf = f.shape[0]
+    zr = torch.zeros((1, 3 * nf, 3 * nf), dtype=torch.float64, device=cuda)
+    zi = torch.zeros_like(zr)
+    k = float(g[f"mom_gq{gq}_k"])
+    pkg.mesh_MOM_3d.create_MOM_Zmat_3d_forward(v, f, a, n, px, wx, py, wy, zr, zi, k)
+    z = (zr + 1j * zi)[0].cpu().numpy()
+    if f"mom_gq{gq}_zfe" in g:
+        assert rel_err(z, g[f"mom_gq{gq}_zfe"]) < TOL64
+    else:
+        ref_rows = g[f"mom_gq{gq}_zfe_rows"]
+        assert rel_err(z[: ref_rows.shape[0]], ref_rows) < TOL64
+    assert abs(np.linalg.norm(z) / float(g[f"mom_gq{gq}_zfe_fro"]) - 1) < TOL64
+
+
+def test_zmat_fe_batch_copies(pkg, cuda, golden):
+    g = golden["ico0"]
+    v, f, a, n = _dev_mesh(g, cuda, torch.float64)
+    px, wx, py, wy = _rules(pkg, 4, cuda, torch.float64)
+    nf = f.shape[0]
+    zr = torch.zeros((2, 3 * nf, 3 * nf), dtype=torch.float64, device=cuda)
+    zi = torch.zeros_like(zr)
+    pkg.mesh_MOM_3d.create_MOM_Zmat_3d_forward(v, f, a, n, px, wx, py, wy, zr, zi, 2.0)
+    assert torch.equal(zr[0], zr[1]) and torch.equal(zi[0], zi[1])
+    assert rel_err((zr[1] + 1j * zi[1]).cpu().numpy(), g["mom_gq4_zfe"]) < TOL64
+
+
+@pytest.mark.parametrize("level,k", [(1, 2.0), (2, 6.0)])
+def test_zmat_fe_f32_vs_oracle(pkg, cuda, oracle, level, k):
+    v_np, f_np = pkg.meshes.icosphere(level)
+    v = torch.tensor(v_np, dtype=torch.float32, device=cuda)
+    f = torch.tensor(f_np, dtype=torch.int32, device=cuda)
+    a = pkg.utils.compute_face_areas(v, f).contiguous()
+    n = pkg.utils.compute_face_normals(v, f).contiguous()
+    px, wx = pkg.utils.get_gaussion_integration_points_and_weights(4, device=cuda)
+    py, wy = pkg.utils.get_gaussion_integration_points_and_weights(3, device=cuda)
+    nf = f.shape[0]
+    zr = torch.zeros((1, 3 * nf, 3 * nf), dtype=torch.float32, device=cuda)
+    zi = torch.zeros_like(zr)
+    pkg.mesh_MOM_3d.create_MOM_Zmat_3d_forward(v, f, a, n, px, wx, py, wy, zr, zi, k)
+    z = (zr[0].double() + 1j * zi[0].double()).cpu().numpy()
+    h = lambda t: t.cpu().double().numpy()  # noqa: E731
+    ref = oracle.mom_zmat_fe(h(v), f_np, h(a), h(n), h(px), h(wx), h(py), h(wy), k)
+    assert rel_err(z, ref) < TOL32
+
+
+@pytest.mark.parametrize("dt,tol", [(torch.float32, TOL32), (torch.float64, TOL64)])
+def test_zmat_rwg_equals_scattered_face_edge(pkg, cuda, golden, oracle, dt, tol):
+    g = golden["ell1"]
+    v, f, a, n = _dev_mesh(g, cuda, dt)
+    px, wx, py, wy = _rules(pkg, 4, cuda, dt)
+    fei = torch.tensor(g["face_edge_indices"], dtype=torch.int32, device=cuda)
+    ne = g["edges"].shape[0]
+    Z = pkg.mesh_MOM_3d.assemble_Z_rwg(v, f, a, n, fei, ne, px, wx, py, wy, 2.0)
+    h = lambda t: t.cpu().double().numpy()  # noqa: E731
+    zfe = oracle.mom_zmat_fe(h(v), g["faces"], h(a), h(n), h(px), h(wx), h(py), h(wy), 2.0)
+    e = g["face_edge_indices"].astype(np.int64)
+    zref = np.zeros((ne, ne), np.complex128)
+    np.add.at(zref, (e[:, None], e[None, :]), zfe)
+    assert rel_err(Z.cpu().numpy(), zref) < tol
+
+
+def test_zmat_rwg_row_chunks_sum_to_full(pkg, cuda):
+    v_np, f_np = pkg.meshes.icosphere(2)
+    v = torch.tensor(v_np, dtype=torch.float32, device=cuda)
+    f = torch.tensor(f_np, dtype=torch.int32, device=cuda)
+    edges, fei, _ = pkg.utils.get_edge_unique(v, f)
+    a = pkg.utils.compute_face_areas(v, f).contiguous()
+    n = pkg.utils.compute_face_normals(v, f).contiguous()
+    px, wx = pkg.utils.get_gaussion_integration_points_and_weights(4, device=cuda)
+    py, wy = pkg.utils.get_gaussion_integration_points_and_weights(3, device=cuda)
+    ne = edges.shape[0]
+    full = pkg.mesh_MOM_3d.assemble_Z_rwg(v, f, a, n, fei, ne, px, wx, py, wy, 3.0)
+    part = torch.zeros_like(full)
+    nrow = 3 * f.shape[0]
+    for r0 in range(0, nrow, 257):
+        pkg.mesh_MOM_3d.assemble_Z_rwg(v, f, a, n, fei, ne, px, wx, py, wy, 3.0, out=part,
+                                       rows=(r0, min(nrow, r0 + 257)))
+    assert rel_err(part.cpu().numpy(), full.cpu().numpy()) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["ico0", "ell1"])
+def test_rhs_fe_matches_reference(pkg, cuda, golden, name):
+    g = golden[name]
+    v, f, a, n = _dev_mesh(g, cuda, torch.float64)
+    px, wx, _, _ = _rules(pkg, 4, cuda, torch.float64)
+    nf = f.shape[0]
+    rr = torch.zeros((1, nf, 3, 1), dtype=torch.float64, device=cuda)
+    ri = torch.zeros_like(rr)
+    pkg.mesh_MOM_3d.create_MOM_rhs_3d_forward(v, f, a, n, px, wx, rr, ri, 2.0)
+    r = (rr + 1j * ri)[0, :, :, 0].cpu().numpy()
+    assert rel_err(r, g["mom_gq4_rhsfe"]) < TOL64
+
+
+def test_rhs_rwg_multi_wave(pkg, cuda, golden, oracle):
+    g = golden["ell1"]
+    v, f, a, n = _dev_mesh(g, cuda, torch.float32)
+    px, wx, _, _ = _rules(pkg, 4, cuda, torch.float32)
+    fei = torch.tensor(g["face_edge_indices"], dtype=torch.int32, device=cuda)
+    ne = g["edges"].shape[0]
+    dirs = pkg.meshes.fibonacci_lattice(6)
+    pol = np.cross(dirs, [0.3, 0.5, 0.81])
+    pol /= np.linalg.norm(pol, axis=1, keepdims=True)
+    waves = pkg.mesh_MOM_3d.plane_waves(2.0, dirs, pol, device=cuda)
+    R = pkg.mesh_MOM_3d.assemble_rhs_rwg(v, f, a, n, fei, ne, px, wx, waves).cpu().numpy()
+    h = lambda t: t.cpu().double().numpy()  # noqa: E731
+    e = g["face_edge_indices"].astype(np.int64)
+    for i in range(6):
+        fe = oracle.mom_rhs_fe(h(v), g["faces"], h(a), h(n), h(px), h(wx), 2.0, khat=dirs[i],
+                               e0=pol[i]).reshape(-1)
+        ref = np.zeros(ne, np.complex128)
+        np.add.at(ref, e, fe)
+        assert rel_err(R[:, i], ref) < TOL32
+    # the packed reference wave reproduces the face-edge op after scattering
+    w0 = pkg.mesh_MOM_3d.reference_plane_wave(2.0, device=cuda)
+    R0 = pkg.mesh_MOM_3d.assemble_rhs_rwg(v, f, a, n, fei, ne, px, wx, w0).cpu().numpy()[:, 0]
+    ref0 = np.zeros(ne, np.complex128)
+    np.add.at(ref0, e, g["mom_gq4_rhsfe"].reshape(-1))
+    assert rel_err(R0, ref0) < TOL32
+
+
+@pytest.mark.parametrize("name", ["ico0", "ell1"])
+def test_interp_matches_reference(pkg, cuda, golden, name):
+    g = golden[name]
+    v, f, a, _ = _dev_mesh(g, cuda, torch.float64)
+    fei = torch.tensor(g["face_edge_indices"], dtype=torch.int32, device=cuda)
+    ic = torch.tensor(g["mom_gq4_icoeff"], device=cuda)
+    nf = f.shape[0]
+    jr = torch.zeros((1, 3 * nf, 3), dtype=torch.float64, device=cuda)
+    ji = torch.zeros_like(jr)
+    pkg.mesh_MOM_3d.interpolate_Icoeff_to_Js_3d_forward(v, f, fei, a, ic.real.contiguous(),
+                                                        ic.imag.contiguous(), jr, ji)
+    assert rel_err((jr + 1j * ji).cpu().numpy(), g["mom_gq4_face_vert_js"]) < TOL64
+    vj = pkg.mesh_MOM_3d.interpolate_vert_js(v, f, fei, a, ic)
+    assert rel_err(vj.cpu().numpy(), g["mom_gq4_vert_js"]) < TOL64
+
+
+@pytest.mark.parametrize("name", ["ico0", "ico1", "ell1"])
+def test_solve_MOM_f64_matches_reference(pkg, cuda, golden, name):
+    g = golden[name]
+    torch.set_default_dtype(torch.float64)
+    try:
+        solver = pkg.MeshBEMSolver3d(gaussQR=4, order_type=1, BEM_type=int(pkg.BEMType.HELMHOLTZ_MOM),
+                                     wavenumber=float(g["mom_gq4_k"]), logger=None,
+                                     dtype=torch.float64, device=cuda)
+    finally:
+        torch.set_default_dtype(torch.float32)
+    v = torch.tensor(g["verts"], dtype=torch.float64, device=cuda)
+    f = torch.tensor(g["faces"], dtype=torch.int32, device=cuda)
+    edges = torch.tensor(g["edges"], device=cuda)
+    fei = torch.tensor(g["face_edge_indices"], dtype=torch.int32, device=cuda)
+    js = solver.solve_MOM(v, f, edges, fei)
+    assert js.shape == (1, v.shape[0], 3)
+    assert rel_err(js.cpu().numpy(), g["mom_gq4_vert_js"]) < 1e-9
+
+
+def test_solve_MOM_f32_close_to_reference(pkg, cuda, golden):
+    g = golden["ell1"]
+    torch.set_default_dtype(torch.float64)
+    try:
+        solver = pkg.MeshBEMSolver3d(gaussQR=4, order_type=1, BEM_type=int(pkg.BEMType.HELMHOLTZ_MOM),
+                                     wavenumber=float(g["mom_gq4_k"]), logger=None,
+                                     dtype=torch.float32, device=cuda)
+    finally:
+        torch.set_default_dtype(torch.float32)
+    v = torch.tensor(g["verts"], dtype=torch.float32, device=cuda)
+    f = torch.tensor(g["faces"], dtype=torch.int32, device=cuda)
+    edges = torch.tensor(g["edges"], device=cuda)
+    fei = torch.tensor(g["face_edge_indices"], dtype=torch.int32, device=cuda)
+    js = solver.solve_MOM(v, f, edges, fei)
+    # FP32 assembly + complex64 LU: the current inherits cond(Z) * 1e-7-level input error.
+    assert rel_err(js.cpu().numpy(), g["mom_gq4_vert_js"]) < 1e-4
+
+
+def test_bad_inputs_raise(pkg, cuda):
+    v = torch.zeros((3, 3), device=cuda)
+    f = torch.zeros((1, 3), dtype=torch.int64, device=cuda)
+    a = torch.ones((1, 1), device=cuda)
+    n = torch.zeros((1, 3), device=cuda)
+    p, w = pkg.utils.get_gaussion_integration_points_and_weights(2, device=cuda)
+    zr = torch.zeros((1, 3, 3), device=cuda)
+    with pytest.raises(TypeError):
+        pkg.mesh_MOM_3d.create_MOM_Zmat_3d_forward(v, f, a, n, p, w, p, w, zr, zr.clone(), 1.0)
+    with pytest.raises(ValueError):
+        pkg.mesh_MOM_3d.create_MOM_Zmat_3d_forward(v.cpu(), f.int().cpu(), a, n, p, w, p, w, zr,
+                                                   zr.clone(), 1.0)
+    with pytest.raises(pkg.MeshBEMError):
+        pkg.mesh_MOM_3d.create_MOM_Zmat_3d_forward(v, f.int(), a, n, p, w, p, w, zr, zr.clone(), 0.0)
+
+
+def test_empty_mesh_is_noop(pkg, cuda):
+    v = torch.zeros((0, 3), device=cuda)
+    f = torch.zeros((0, 3), dtype=torch.int32, device=cuda)
+    a = torch.zeros((0, 1), device=cuda)
+    n = torch.zeros((0, 3), device=cuda)
+    p, w = pkg.utils.get_gaussion_integration_points_and_weights(2, device=cuda)
+    zr = torch.zeros((1, 0, 0), device=cuda)
+    pkg.mesh_MOM_3d.create_MOM_Zmat_3d_forward(v, f, a, n, p, w, p, w, zr, zr.clone(), 1.0)

@@ -1,0 +1,103 @@
+"""The CPU oracle (oracle/mesh_bem_oracle.c) pinned against the reference's own results.
+
+The golden fixtures were produced by running the reference itself (its CUDA kernel bodies
+compiled for the host, and its Python Laplace path), see tests/golden/make_golden.py.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+
+@pytest.mark.parametrize("name", ["ico0", "ico1", "ell1"])
+@pytest.mark.parametrize("gq", [4, 3])
+def test_oracle_zmat_fe_matches_reference(oracle, golden, gauss_golden, name, gq):
+    g = golden[name]
+    px, wx = gauss_golden[f"p{gq}"], gauss_golden[f"w{gq}"]
+    py, wy = gauss_golden[f"p{gq - 1}"], gauss_golden[f"w{gq - 1}"]
+    k = float(g[f"mom_gq{gq}_k"])
+    if f"mom_gq{gq}_zfe" in g:
+        z = oracle.mom_zmat_fe(g["verts"], g["faces"], g["face_areas"], g["face_normals"], px, wx, py, wy, k)
+        assert rel_err(z, g[f"mom_gq{gq}_zfe"]) < 1e-12
+    else:
+        ref = g[f"mom_gq{gq}_zfe_rows"]
+        z = oracle.mom_zmat_fe(g["verts"], g["faces"], g["face_areas"], g["face_normals"], px, wx, py, wy,
+                               k, rows=(0, ref.shape[0]))
+        assert rel_err(z, ref) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["ico0", "ico1", "ell1"])
+def test_oracle_rhs_and_interp_match_reference(oracle, golden, gauss_golden, name):
+    g = golden[name]
+    for gq in (4, 3):
+        k = float(g[f"mom_gq{gq}_k"])
+        r = oracle.mom_rhs_fe(g["verts"], g["faces"], g["face_areas"], g["face_normals"],
+                              gauss_golden[f"p{gq}"], gauss_golden[f"w{gq}"], k)
+        assert rel_err(r, g[f"mom_gq{gq}_rhsfe"]) < 1e-12
+        j = oracle.mom_interp_js(g["verts"], g["faces"], g["face_edge_indices"], g["face_areas"],
+                                 g[f"mom_gq{gq}_icoeff"])
+        assert rel_err(j, g[f"mom_gq{gq}_face_vert_js"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["ico0", "ico1", "ell1"])
+def test_oracle_mom_pipeline_matches_reference(oracle, golden, gauss_golden, name):
+    """Scatter + dense solve + interpolation from the oracle's pieces reproduce vert_Js."""
+    g = golden[name]
+    gq = 4
+    e = g["face_edge_indices"].astype(np.int64)
+    ne = g["edges"].shape[0]
+    k = float(g[f"mom_gq{gq}_k"])
+    args = (g["verts"], g["faces"], g["face_areas"], g["face_normals"])
+    zfe = oracle.mom_zmat_fe(*args, gauss_golden["p4"], gauss_golden["w4"], gauss_golden["p3"],
+                             gauss_golden["w3"], k)
+    Z = np.zeros((ne, ne), np.complex128)
+    np.add.at(Z, (e[:, None], e[None, :]), zfe)
+    rfe = oracle.mom_rhs_fe(*args, gauss_golden["p4"], gauss_golden["w4"], k).reshape(-1)
+    b = np.zeros(ne, np.complex128)
+    np.add.at(b, e, rfe)
+    x = np.linalg.solve(Z, b)
+    assert rel_err(x, g[f"mom_gq{gq}_icoeff"][0]) < 1e-9
+    fj = oracle.mom_interp_js(g["verts"], g["faces"], e, g["face_areas"], x[None])
+    vj = np.zeros((1, g["verts"].shape[0], 3), np.complex128)
+    np.add.at(vj[0], g["faces"].reshape(-1), fj[0])
+    assert rel_err(vj, g[f"mom_gq{gq}_vert_js"]) < 1e-9
+
+
+@pytest.mark.parametrize("name", ["ico0", "ico1", "ell1"])
+def test_oracle_panel_relation(oracle, golden, name):
+    g = golden[name]
+    assert np.array_equal(oracle.panel_relation(g["faces"]), g["panel_relations"])
+
+
+@pytest.mark.parametrize("tag", ["lap_gq2_o1", "lap_gq3_o1", "lap_gq2_o0"])
+@pytest.mark.parametrize("layer", [1, 2])
+def test_oracle_laplace_panels_match_reference(oracle, golden, tag, layer):
+    gq, order = int(tag[6]), int(tag[-1])
+    for name in ("ico0", "ell1"):
+        g = golden[name]
+        key = f"{tag}_{'V' if layer == 1 else 'K'}_unpacked"
+        full = key in g
+        if not full and key + "_rows" not in g:
+            continue
+        ref = g[key] if full else g[key + "_rows"]
+        out = oracle.laplace_panels(g["verts"], g["faces"], g["face_areas"], g["face_normals"],
+                                    g[f"{tag}_rands"], g[f"{tag}_weights"], g["panel_relations"], layer,
+                                    order, rows=None if full else (0, ref.shape[0]))
+        assert rel_err(out, ref) < 1e-12, (name, gq)
+
+
+def test_oracle_float32_build_close(oracle, golden, gauss_golden):
+    g = golden["ico0"]
+    z32 = oracle.mom_zmat_fe(g["verts"], g["faces"], g["face_areas"], g["face_normals"], gauss_golden["p4"],
+                             gauss_golden["w4"], gauss_golden["p3"], gauss_golden["w3"], 2.0,
+                             dtype=np.float32)
+    assert rel_err(z32, g["mom_gq4_zfe"]) < 1e-5
+
+
+def test_oracle_reference_build_bit_exact_where_available(oracle, golden, gauss_golden):
+    if oracle.ref_lib() is None:
+        pytest.skip("reference checkout not present on this machine")
+    g = golden["ell1"]
+    args = (g["verts"], g["faces"], g["face_areas"], g["face_normals"], gauss_golden["p4"],
+            gauss_golden["w4"], gauss_golden["p3"], gauss_golden["w3"], 2.0)
+    assert np.array_equal(oracle.mom_zmat_fe(*args), oracle.ref_zmat_fe(*args))
