@@ -1,0 +1,365 @@
+"""Benchmark of the MoM impedance-matrix assembly (triangle pairs per second).
+
+Workload (default ``mom_ref_L5``): icosphere level 5 -- 20480 triangles, 10242 vertices,
+30720 RWG unknowns -- radius 1 m, ka = 10 (k = 10), the reference's formulation and rule
+(EFIE + MFIE summed, collapsed Gauss-Legendre gaussQR = 4: 16 test x 9 source points per
+face-edge entry, rotated per local edge, i.e. 1296 kernel evaluations per triangle pair),
+float32 arithmetic, Z accumulated straight into the [E, E] complex64 RWG matrix (7.55 GB).
+A step zeroes Z and assembles all F^2 triangle pairs.  Synthetic mesh (the reference's
+mesh assets are not shipped); the output (7.55 GB) is larger than L2 and is rewritten
+every step, so no stale lines survive between steps.
+
+``python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]``
+prints one JSON line (rank 0).  Under torchrun each rank assembles its own replica (the
+path has no exchange step: replicas only) and the slowest rank's time is reported.
+
+``--impl reference`` times the reference's own algorithm on the host cores instead: the
+host build of its CUDA kernel bodies where that exists (oracle/_ref), else the CPU
+restatement in oracle/ (float32 build), on a bounded sample of face-edge rows.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+WORKLOADS = {
+    # name: (icosphere level, k, gaussQR)
+    "mom_ref_L5": (5, 10.0, 4),
+    "mom_ref_L4": (4, 6.0, 4),
+    "mom_ref_L3": (3, 2.0, 4),
+}
+
+
+def _args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--workload", choices=sorted(WORKLOADS), default="mom_ref_L5")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=10.0,
+                   help="target CPU work per reference-arm / baseline sample")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._proc = None
+        self._thread = None
+
+    def start(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self._proc = None
+            return
+        self._thread = threading.Thread(target=self._read, daemon=True)
+        self._thread.start()
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+        if self._thread is not None:
+            self._thread.join(timeout=5)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        smax = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for i, n in enumerate(names):
+                if s[4 + i].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------------------------------
+# CPU reference / baseline
+# ---------------------------------------------------------------------------------------
+def _mesh_np(level):
+    pkg = importlib.import_module("mesh-ferrofluid_gb300")
+    v, f = pkg.meshes.icosphere(level)
+    v32 = v.astype(np.float32)
+    p0, p1, p2 = (v32[f[:, i]].astype(np.float32) for i in range(3))
+    cr = np.cross(p1 - p0, p2 - p1)
+    areas = (0.5 * np.linalg.norm(cr, axis=1)).astype(np.float32)
+    normals = (cr / np.linalg.norm(cr, axis=1, keepdims=True)).astype(np.float32)
+    return v32, f, areas, normals
+
+
+def _rules_np(gq):
+    def gl(n):
+        x, w = np.polynomial.legendre.leggauss(n)
+        x = x.astype(np.float32)
+        w = w.astype(np.float32)
+        return (x + np.float32(1)) / np.float32(2), w / np.float32(2)
+    px, wx = gl(gq)
+    py, wy = gl(gq - 1)
+    return px, wx, py, wy
+
+
+def cpu_sample_run(workload, seconds, steps=1, warmup=0):
+    """Time the reference algorithm on host cores over a bounded sample of face-edge rows.
+
+    Runs the C restatement of the reference kernel (oracle/, float32 build, one OpenMP
+    thread per host core).  The host build of the reference's own kernel bodies
+    (oracle/_ref) is not used for timing: its 32-bit flat index overflows beyond
+    F = 15447 faces (mesh_MOM_3d.cu:364-374) and it has no row window.  Returns
+    (pairs_per_s list, info dict).
+    """
+    from oracle import oracle as O
+
+    level, k, gq = WORKLOADS[workload]
+    v, f, a, n = _mesh_np(level)
+    px, wx, py, wy = _rules_np(gq)
+    nf = f.shape[0]
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+
+    def run(rows):
+        t0 = time.perf_counter()
+        O.mom_zmat_fe(v, f, a, n, px, wx, py, wy, k, rows=(0, rows), dtype=np.float32)
+        return time.perf_counter() - t0
+
+    calib_rows = 6
+    t = run(calib_rows)
+    rate_rows = calib_rows / max(t, 1e-6)
+    rows = max(3, min(3 * nf, int(rate_rows * seconds)))
+    for _ in range(warmup):
+        run(max(3, rows // 4))
+    vals = []
+    for _ in range(steps):
+        dt = run(rows)
+        vals.append(rows * 3 * nf / 9.0 / dt)  # face-edge entries / 9 = triangle pairs
+    info = {"kind": "port", "cores": threads,
+            "sample": f"{rows} of {3 * nf} face-edge test rows x all {3 * nf} columns "
+                      f"({rows * nf // 3} triangle-pair equivalents), float32 C restatement"}
+    return vals, info
+
+
+# ---------------------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------------------
+def main():
+    args = _args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    level, k, gq = WORKLOADS[args.workload]
+    n_faces = 20 * 4 ** level
+    n_edges = 30 * 4 ** level
+    pairs = float(n_faces) ** 2
+    config = {"workload": args.workload, "mesh": f"icosphere L{level}", "n_faces": n_faces,
+              "n_edges": n_edges, "ka": k, "rule": f"reference collapsed Gauss-Legendre gaussQR={gq} "
+              f"({gq * gq} test x {(gq - 1) ** 2} source points, rotated per local edge)",
+              "formulation": "EFIE+MFIE (reference CFIE)", "output": "RWG Z [E,E] complex64",
+              "l2": "Z (7.55 GB at L5) > L2, rewritten every step", "parallelism": "replicas"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        vals, info = cpu_sample_run(args.workload, args.cpu_seconds, steps=args.steps,
+                                    warmup=min(args.warmup, 1))
+        v = statistics.mean(vals)
+        line = {"metric": "Z-assembly triangle pairs/s", "value": v, "unit": "pairs/s",
+                "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": pairs / v * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": v, "unit": "pairs/s", **info},
+                "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+
+    pkg = importlib.import_module("mesh-ferrofluid_gb300")
+    R = pkg.roofline
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local_rank if world > 1 else 0)
+    torch.cuda.set_device(dev)
+
+    v_np, f_np = pkg.meshes.icosphere(level)
+    verts = torch.tensor(v_np, dtype=torch.float32, device=dev)
+    faces = torch.tensor(f_np, dtype=torch.int32, device=dev)
+    edges, fei, _ = pkg.utils.get_edge_unique(verts, faces)
+    areas = pkg.utils.compute_face_areas(verts, faces).contiguous()
+    normals = pkg.utils.compute_face_normals(verts, faces).contiguous()
+    px, wx = pkg.utils.get_gaussion_integration_points_and_weights(gq, device=dev)
+    py, wy = pkg.utils.get_gaussion_integration_points_and_weights(gq - 1, device=dev)
+    Z = torch.zeros((n_edges, n_edges), dtype=torch.complex64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    M = pkg.mesh_MOM_3d
+
+    def step():
+        Z.zero_()
+        M.assemble_Z_rwg(verts, faces, areas, normals, fei, n_edges, px, wx, py, wy, k, out=Z,
+                         check_indices=False)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.3)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    for e0, e1, e2 in ev:
+        e0.record(stream)
+        Z.zero_()
+        e1.record(stream)
+        M.assemble_Z_rwg(verts, faces, areas, normals, fei, n_edges, px, wx, py, wy, k, out=Z,
+                         check_indices=False)
+        e2.record(stream)
+    barrier()
+    clocks.stop()
+    step_ms = [a.elapsed_time(c) for a, _, c in ev]
+    kern_ms = [b.elapsed_time(c) for _, b, c in ev]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * pairs / (ms_per_step / 1e3)
+    kern_avg_s = statistics.mean(kern_ms) / 1e3
+
+    # roofline of the dominant kernel (assembly), per launch
+    evals = pairs * R.ref_rule_evals_per_pair(gq)
+    flop = evals * R.CFIE_FLOP_PER_EVAL
+    mufu = evals * R.CFIE_MUFU_PER_EVAL
+    peaks = R.measured_peaks(REPO)
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = R.fp32_peak_tflops(sm_max)
+    mufu_peak = R.mufu_peak_gops(sm_max)
+    achieved = flop / kern_avg_s / 1e12
+    traffic = None
+    prof = os.path.join(REPO, "profiles", f"{args.workload}_traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as fh:
+            traffic = json.load(fh).get("dram_bytes_per_launch")
+    roof = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": achieved / fp32_peak, "traffic": traffic,
+            "peak_source": f"152 SMs x 256 FP32 FLOP/clk x {sm_max:.0f} MHz (max SM clock of "
+                           "MEASURED_PEAKS.json; the file has no FP32-SIMT figure)",
+            "mufu": {"achieved_gops": mufu / kern_avg_s / 1e9, "peak_gops": mufu_peak,
+                     "frac": mufu / kern_avg_s / 1e9 / mufu_peak},
+            "algorithmic": f"{R.CFIE_FLOP_PER_EVAL} FLOP + {R.CFIE_MUFU_PER_EVAL} MUFU per evaluation x "
+                           f"{R.ref_rule_evals_per_pair(gq)} evaluations per pair x F^2 pairs",
+            "kernel_ms": kern_avg_s * 1e3}
+
+    line = {"metric": "Z-assembly triangle pairs/s", "value": value, "unit": "pairs/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": config, "roofline": roof, "clocks": clocks.summary(),
+            "gpu_launches": args.steps}
+
+    # end to end through the public operator: host (pinned) inputs in, Z back to host memory
+    if not args.no_e2e:
+        h_verts = torch.tensor(v_np, dtype=torch.float32).pin_memory()
+        h_faces = torch.tensor(f_np, dtype=torch.int32).pin_memory()
+        h_fei = fei.cpu().pin_memory()
+        h_rules = [t.cpu().pin_memory() for t in (px, wx, py, wy)]
+        h_Z = torch.empty((n_edges, n_edges), dtype=torch.complex64).pin_memory()
+        d_verts = torch.empty_like(verts)
+        d_faces = torch.empty_like(faces)
+        d_fei = torch.empty_like(fei)
+        d_rules = [torch.empty_like(t) for t in (px, wx, py, wy)]
+
+        def e2e_step():
+            d_verts.copy_(h_verts, non_blocking=True)
+            d_faces.copy_(h_faces, non_blocking=True)
+            d_fei.copy_(h_fei, non_blocking=True)
+            for d, h in zip(d_rules, h_rules):
+                d.copy_(h, non_blocking=True)
+            a = pkg.utils.compute_face_areas(d_verts, d_faces).contiguous()
+            nn = pkg.utils.compute_face_normals(d_verts, d_faces).contiguous()
+            Z.zero_()
+            M.assemble_Z_rwg(d_verts, d_faces, a, nn, d_fei, n_edges, *d_rules, k, out=Z,
+                             check_indices=False)
+            h_Z.copy_(Z, non_blocking=True)
+
+        e2e_step()
+        barrier()
+        e2e_steps = max(2, min(args.steps, 3))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(stream)
+        for _ in range(e2e_steps):
+            e2e_step()
+        e1.record(stream)
+        barrier()
+        e2e_ms = e0.elapsed_time(e1) / e2e_steps
+        h2d = (h_verts.numel() * 4 + h_faces.numel() * 4 + h_fei.numel() * 4
+               + sum(t.numel() * 4 for t in h_rules))
+        line["e2e"] = {"value": world * pairs / (e2e_ms / 1e3), "unit": "pairs/s",
+                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h_Z.numel() * 8,
+                       "ms_per_step": e2e_ms, "steps": e2e_steps,
+                       "path": "mesh_MOM_3d.assemble_Z_rwg (C ABI mb_mom_zmat_rwg_c64), pinned host "
+                               "buffers, H2D inputs + Z D2H inside the timed region"}
+        del h_Z
+
+    if rank == 0 and not args.no_cpu_baseline:
+        vals, info = cpu_sample_run(args.workload, args.cpu_seconds, steps=1)
+        line["cpu_baseline"] = {"value": vals[0], "unit": "pairs/s", **info}
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

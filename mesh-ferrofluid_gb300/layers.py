@@ -18,6 +18,7 @@ from __future__ import annotations
 import torch
 
 from . import _lib
+from .mesh_MOM_3d import check_face_range
 from .utils import (
     BEMType,
     BoundaryType,
@@ -48,7 +49,10 @@ def double_integration_on_panels_3d(BEM_type: int, order_type: int, verts: torch
     faces = faces.to(torch.int32).contiguous()
     _lib.check_tensor(faces, "faces", device=dev, ndim=2)
     nf = faces.shape[0]
+    check_face_range(faces, verts.shape[0])
     areas = face_areas.to(dt).contiguous()
+    if areas.numel() != nf or face_normals.numel() != 3 * nf:
+        raise ValueError("face_areas / face_normals must have F / 3F entries")
     normals = face_normals.to(dt).contiguous()
     table, seg = panel_rule_table(rands_x.to(dt), rands_y.to(dt), gauss_weightsx.to(dt),
                                   gauss_weightsy.to(dt))

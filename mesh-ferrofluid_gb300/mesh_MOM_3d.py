@@ -43,7 +43,16 @@ def _mesh_args(verts, faces, face_areas, face_normals):
     _lib.check_tensor(face_normals, "face_normals", dtype=dt, device=dev)
     if face_normals.numel() != 3 * nf:
         raise ValueError("face_normals must be [N_faces, 3]")
+    check_face_range(faces, verts.shape[0])
     return dt, dev, verts.shape[0], nf
+
+
+def check_face_range(faces, n_verts):
+    """Vertex ids must index ``verts``; the kernels trust them (one reduction, one sync)."""
+    if faces.numel():
+        lo, hi = torch.aminmax(faces)
+        if int(lo) < 0 or int(hi) >= n_verts:
+            raise ValueError(f"faces reference vertex ids outside [0, {n_verts})")
 
 
 def _rule(p, w, name, dt, dev):
@@ -101,6 +110,7 @@ def interpolate_Icoeff_to_Js_3d_forward(verts, faces, face_edge_indices, face_ar
     dt, dev = verts.dtype, verts.device
     _lib.check_tensor(faces, "faces", dtype=torch.int32, device=dev, ndim=2)
     nf = faces.shape[0]
+    check_face_range(faces, verts.shape[0])
     _lib.check_tensor(face_edge_indices, "face_edge_indices", dtype=torch.int32, device=dev)
     if face_edge_indices.numel() != 3 * nf:
         raise ValueError("face_edge_indices must have 3F entries")
@@ -213,6 +223,7 @@ def interpolate_vert_js(verts, faces, face_edge_indices, face_areas, i_coeff, ou
     dt, dev = verts.dtype, verts.device
     _lib.check_tensor(faces, "faces", dtype=torch.int32, device=dev, ndim=2)
     nf, nv = faces.shape[0], verts.shape[0]
+    check_face_range(faces, nv)
     cdt = torch.complex64 if dt == torch.float32 else torch.complex128
     i_coeff = i_coeff.reshape(i_coeff.shape[0] if i_coeff.dim() > 1 else 1, -1).to(cdt).contiguous()
     batch, n_edges = i_coeff.shape

@@ -1,0 +1,55 @@
+"""Canonical algorithmic work counts of the hot-path kernels (one source of truth).
+
+Per kernel evaluation (one test point x one source point):
+
+* MoM CFIE (the reference's EFIE + MFIE integrand, per-test-point moment form
+  sum_j G, sum_j G y_j, sum_j h, sum_j h y_j):           50 FP32 FLOP, 3 MUFU (rsqrt, sin, cos)
+* MoM EFIE only:                                       30 FP32 FLOP, 3 MUFU
+* Laplace single layer (1/4 pi R times P1 products):   15 FP32 FLOP, 1 MUFU (rsqrt)
+* Laplace double layer (grad_y G . n times P1):        22 FP32 FLOP, 1 MUFU
+
+An FMA counts as 2 FLOP.  Units: a "triangle pair" is one ordered (test, source) face
+pair; with the reference's collapsed Gauss rule of order q (test q^2 points, source
+(q-1)^2 points, rotated per local edge) a pair costs 9 * q^2 * (q-1)^2 evaluations.
+Matrix-vector products are HBM-bound: 8 E^2 + 16 E bytes per complex64 matvec.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+CFIE_FLOP_PER_EVAL = 50
+CFIE_MUFU_PER_EVAL = 3
+EFIE_FLOP_PER_EVAL = 30
+EFIE_MUFU_PER_EVAL = 3
+LAPLACE_SL_FLOP_PER_EVAL = 15
+LAPLACE_DL_FLOP_PER_EVAL = 22
+LAPLACE_MUFU_PER_EVAL = 1
+
+GB300_SMS = 152
+FP32_FLOP_PER_CLK_PER_SM = 256   # 128 FP32 lanes x FMA
+MUFU_OPS_PER_CLK_PER_SM = 16
+
+
+def ref_rule_evals_per_pair(gauss_qr: int) -> int:
+    """Evaluations per triangle pair with the reference rule (9 face-edge entries)."""
+    return 9 * gauss_qr * gauss_qr * (gauss_qr - 1) * (gauss_qr - 1)
+
+
+def measured_peaks(repo_root: str) -> dict:
+    path = os.path.join(repo_root, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        d["source"] = "measured"
+        return d
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+            "sm_max_mhz": 2070.0, "source": "fallback"}
+
+
+def fp32_peak_tflops(sm_mhz: float, sms: int = GB300_SMS) -> float:
+    return sms * FP32_FLOP_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e12
+
+
+def mufu_peak_gops(sm_mhz: float, sms: int = GB300_SMS) -> float:
+    return sms * MUFU_OPS_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e9

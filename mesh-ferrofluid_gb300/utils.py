@@ -241,7 +241,13 @@ def pack_matrix_tight(order_type: int, unpacked_matrix: torch.Tensor, verts: tor
     n_verts = verts.shape[-2]
     faces = _lib.check_tensor(faces.contiguous(), "faces", dtype=torch.int32, ndim=2)
     nf = faces.shape[0]
+    if nf and (int(faces.min()) < 0 or int(faces.max()) >= n_verts):
+        raise ValueError(f"faces reference vertex ids outside [0, {n_verts})")
     m = unpacked_matrix.contiguous()
+    if m.shape[:2] != (nf, nf) or m.shape[2] != m.shape[3] or m.shape[2] not in (1, 3):
+        raise ValueError("unpacked_matrix must be [F, F, nphi, nphi] with nphi 1 or 3")
+    if (m.shape[2] == 3) != (int(order_type) == int(OrderType.LINEAR)):
+        raise ValueError("unpacked_matrix shape does not match order_type")
     _lib.check_tensor(m, "unpacked_matrix", device=faces.device)
     if m.is_complex():
         base = m.real.dtype

@@ -43,7 +43,8 @@ def build(force: bool = False) -> str:
     for real, sfx in (("double", "f64"), ("float", "f32")):
         obj = os.path.join(BUILD_DIR, f"oracle_{sfx}.o")
         subprocess.check_call(
-            ["gcc", *_CFLAGS, f"-DREAL={real}", f"-DSFX={sfx}", "-c", src, "-o", obj]
+            ["gcc", *_CFLAGS, f"-DREAL={real}", f"-DSFX={sfx}",
+             *(["-DORC_FLOAT"] if real == "float" else []), "-c", src, "-o", obj]
         )
         objs.append(obj)
     tmp = LIB + ".tmp"

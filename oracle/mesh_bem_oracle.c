@@ -30,6 +30,17 @@
 #ifndef SFX
 #define SFX f64
 #endif
+/* Math in the working precision: the reference's float build calls the float overloads
+   (CUDA's sqrt/cos/sin on float arguments). */
+#ifdef ORC_FLOAT
+#define R_SQRT(x) sqrtf(x)
+#define R_COS(x) cosf(x)
+#define R_SIN(x) sinf(x)
+#else
+#define R_SQRT(x) sqrt(x)
+#define R_COS(x) cos(x)
+#define R_SIN(x) sin(x)
+#endif
 #define CAT2(a, b) a##_##b
 #define CAT(a, b) CAT2(a, b)
 #define ORC(name) CAT(orc_##name, SFX)
@@ -50,20 +61,20 @@ static void ORC(cross3)(const REAL* t, const REAL* b, REAL* n) {
 /* e^{-jkR}/(4 pi R)  (mesh_MOM_3d.cu:72-95) */
 static void ORC(green)(REAL k, const REAL* p1, const REAL* p2, REAL* gr, REAL* gi) {
     REAL d0 = p1[0] - p2[0], d1 = p1[1] - p2[1], d2 = p1[2] - p2[2];
-    REAL dist = (REAL)sqrt((double)(d0 * d0 + d1 * d1 + d2 * d2));
+    REAL dist = R_SQRT((d0 * d0 + d1 * d1 + d2 * d2));
     REAL inv = (REAL)1 / dist;
     REAL th = -k * dist;
-    *gr = (REAL)(cos((double)th) / (4 * ORC_PI)) * inv;
-    *gi = (REAL)(sin((double)th) / (4 * ORC_PI)) * inv;
+    *gr = (REAL)(R_COS(th) / (4 * ORC_PI)) * inv;
+    *gi = (REAL)(R_SIN(th) / (4 * ORC_PI)) * inv;
 }
 
 /* grad_x G = -grad_y G  (mesh_MOM_3d.cu:97-152) */
 static void ORC(grad_green_x)(REAL k, const REAL* p1, const REAL* p2, REAL* gr, REAL* gi) {
     REAL r[3] = {p1[0] - p2[0], p1[1] - p2[1], p1[2] - p2[2]};
-    REAL dist = (REAL)sqrt((double)(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]));
+    REAL dist = R_SQRT((r[0] * r[0] + r[1] * r[1] + r[2] * r[2]));
     REAL inv = (REAL)1 / dist;
     REAL th = -k * dist;
-    REAL c = (REAL)cos((double)th), s = (REAL)sin((double)th);
+    REAL c = R_COS(th), s = R_SIN(th);
     REAL fr = (REAL)((c + th * s) / (4 * ORC_PI)) * inv * inv * inv;
     REAL fi = (REAL)((s - th * c) / (4 * ORC_PI)) * inv * inv * inv;
     for (int a = 0; a < 3; ++a) {
@@ -80,7 +91,7 @@ static void ORC(rwg)(const REAL* x, const REAL* verts, REAL area, int32_t i0, in
     const REAL* v1 = verts + 3 * (int64_t)i1;
     const REAL* v2 = verts + 3 * (int64_t)i2;
     REAL e0 = v2[0] - v1[0], e1 = v2[1] - v1[1], e2 = v2[2] - v1[2];
-    REAL len = (REAL)sqrt((double)(e0 * e0 + e1 * e1 + e2 * e2));
+    REAL len = R_SQRT((e0 * e0 + e1 * e1 + e2 * e2));
     REAL sc = len / (2 * area);
     int plus = i1 < i2;
     for (int a = 0; a < 3; ++a) out[a] = (plus ? x[a] - v0[a] : v0[a] - x[a]) * sc;
@@ -91,7 +102,7 @@ static REAL ORC(div_rwg)(const REAL* verts, REAL area, int32_t i1, int32_t i2) {
     const REAL* v1 = verts + 3 * (int64_t)i1;
     const REAL* v2 = verts + 3 * (int64_t)i2;
     REAL e0 = v2[0] - v1[0], e1 = v2[1] - v1[1], e2 = v2[2] - v1[2];
-    REAL len = (REAL)sqrt((double)(e0 * e0 + e1 * e1 + e2 * e2));
+    REAL len = R_SQRT((e0 * e0 + e1 * e1 + e2 * e2));
     REAL sc = len / (2 * area);
     return (i1 < i2) ? sc * 2 : -sc * 2;
 }
@@ -202,14 +213,14 @@ void ORC(mom_rhs_fe)(const REAL* verts, const int32_t* faces, int64_t nf, const 
     REAL kv[3], E0[3], H0[3];
     if (ref_incidence) {
         REAL az = (REAL)(30 / 180.0 * ORC_PI);
-        kv[0] = k * (REAL)cos((double)az);
-        kv[1] = k * (REAL)sin((double)az);
+        kv[0] = k * R_COS(az);
+        kv[1] = k * R_SIN(az);
         kv[2] = 0;
         REAL hdir = (REAL)(az - 0.5 * ORC_PI);
         E0[0] = 0; E0[1] = 0; E0[2] = 1;
         REAL inv_eta = (REAL)1 / (REAL)sqrt(1.0);
-        H0[0] = inv_eta * (REAL)cos((double)hdir);
-        H0[1] = inv_eta * (REAL)sin((double)hdir);
+        H0[0] = inv_eta * R_COS(hdir);
+        H0[1] = inv_eta * R_SIN(hdir);
         H0[2] = 0;
     } else {
         for (int a = 0; a < 3; ++a) {
@@ -241,7 +252,7 @@ void ORC(mom_rhs_fe)(const REAL* verts, const int32_t* faces, int64_t nf, const 
             REAL fv[3];
             ORC(rwg)(x, verts, area, i0, i1, i2, fv);
             REAL kx = kv[0] * x[0] + kv[1] * x[1] + kv[2] * x[2];
-            REAL ph_r = (REAL)cos((double)-kx), ph_i = (REAL)sin((double)-kx);
+            REAL ph_r = R_COS(-kx), ph_i = R_SIN(-kx);
             REAL Er[3], Ei[3], Hr[3], Hi[3];
             for (int a = 0; a < 3; ++a) {
                 Er[a] = E0[a] * ph_r; Ei[a] = E0[a] * ph_i;
@@ -397,15 +408,15 @@ void ORC(laplace_panels)(const REAL* verts, const int32_t* faces, int64_t nf, co
                         y[a] = (1 - r1y) * Y0[a] + (r1y - r2y) * Y1[a] + r2y * Y2[a];
                     }
                     REAL dv[3] = {x[0] - y[0], x[1] - y[1], x[2] - y[2]};
-                    REAL dist = (REAL)sqrt((double)(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]));
+                    REAL dist = R_SQRT((dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]));
                     REAL fr, fi = 0;
                     if (layer == 1) {
                         if (kind == 0) {
                             fr = inv4pi / dist;
                         } else {
                             REAL b = inv4pi / dist;
-                            fr = b * (REAL)cos((double)(k * dist));
-                            fi = b * (REAL)sin((double)(k * dist));
+                            fr = b * R_COS((k * dist));
+                            fi = b * R_SIN((k * dist));
                         }
                     } else {
                         REAL dsq = dist * dist;
@@ -414,7 +425,7 @@ void ORC(laplace_panels)(const REAL* verts, const int32_t* faces, int64_t nf, co
                             fr = inv4pi * dn / dsq;
                         } else {
                             REAL b = inv4pi * dn / dsq;
-                            REAL c = (REAL)cos((double)(k * dist)), sn = (REAL)sin((double)(k * dist));
+                            REAL c = R_COS((k * dist)), sn = R_SIN((k * dist));
                             /* (1 - jkd)(c + j s) */
                             fr = b * (c + k * dist * sn);
                             fi = b * (sn - k * dist * c);
