@@ -312,7 +312,7 @@ def main():
         h_faces = torch.tensor(f_np, dtype=torch.int32).pin_memory()
         h_fei = fei.cpu().pin_memory()
         h_rules = [t.cpu().pin_memory() for t in (px, wx, py, wy)]
-        h_Z = torch.empty((n_edges, n_edges), dtype=torch.complex64).pin_memory()
+        h_Z = torch.empty((n_edges, n_edges), dtype=torch.complex64, pin_memory=True)
         d_verts = torch.empty_like(verts)
         d_faces = torch.empty_like(faces)
         d_fei = torch.empty_like(fei)

@@ -20,6 +20,7 @@
 #ifndef MESH_BEM_GB300_H
 #define MESH_BEM_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -123,6 +124,40 @@ int mb_mom_interp_vert_c128(const double* verts, int64_t n_verts, const int32_t*
                             int64_t n_faces, const int32_t* face_edge_indices,
                             const double* face_areas, const double* i_coeff, int64_t n_edges,
                             int64_t batch, double* vert_js, void* stream);
+
+/* ---- Dense iterative solve (replaces torch.linalg.solve, mesh_BEM_solver_3d.py:174) -- */
+
+/* Outcome of mb_gmres_c64. status: 0 converged to tol, 1 stopped at max_iters. */
+typedef struct mb_gmres_info {
+    int64_t iterations;  /* Arnoldi steps (matrix-vector products with Z) */
+    int64_t restarts;    /* restart cycles, each started from an FP64 residual */
+    double rel_residual; /* ||b - Z x|| / ||b|| in FP64 at return */
+    int32_t status;
+    int32_t reserved;
+} mb_gmres_info;
+
+/* Device workspace (bytes) mb_gmres_c64 needs for n unknowns and restart length m. */
+size_t mb_gmres_workspace_bytes(int64_t n, int restart);
+
+/* Replaces torch.linalg.solve(Zmn, rhs) (src/mesh_BEM/mesh_BEM_solver_3d.py:174).
+ * GMRES(restart) on Z x = b with Z interleaved complex64 [n, n]: FP32 matrix-vector
+ * products, FP64 Arnoldi (CGS2) and Givens rotations, and an FP64 residual b - Z x at the
+ * start of every restart cycle (iterative refinement).  b, x: interleaved complex128 [n];
+ * x holds the initial guess on entry and the solution on return.  restart in [1, 128].
+ * Runs on `stream` and returns after synchronising it (the host drives the Arnoldi loop).
+ * workspace: >= mb_gmres_workspace_bytes(n, restart) bytes of device memory owned by the
+ * caller.  info (host pointer, may be NULL) receives the outcome. */
+int mb_gmres_c64(const float* z, int64_t n, const double* b, double* x, int restart, int max_iters,
+                 double tol, void* workspace, size_t workspace_bytes, mb_gmres_info* info,
+                 void* stream);
+
+/* y = Z v: Z interleaved complex64 [n, n], v complex64 [n], y complex128 [n] (FP32 products,
+ * FP64 row reduction).  The HBM-bound kernel inside mb_gmres_c64. */
+int mb_matvec_c64(const float* z, const float* v, int64_t n, double* y, void* stream);
+
+/* r = b - Z x in FP64: Z complex64 [n, n], x, b, r complex128 [n]. */
+int mb_residual_c128(const float* z, const double* x, const double* b, int64_t n, double* r,
+                     void* stream);
 
 /* ---- Laplace / Helmholtz-BEM layers ------------------------------------------------- */
 

@@ -44,7 +44,21 @@ _SIGS = {
     "mb_pack_tight_f32": [_P, _P, _P, _I64, _I64, _I, _P, _P],
     "mb_pack_tight_f64": [_P, _P, _P, _I64, _I64, _I, _P, _P],
     "mb_panel_relation": [_P, _I64, _P, _P],
+    "mb_gmres_workspace_bytes": [_I64, _I],
+    "mb_gmres_c64": [_P, _I64, _P, _P, _I, _I, _D, _P, ctypes.c_size_t, _P, _P],
+    "mb_matvec_c64": [_P, _P, _I64, _P, _P],
+    "mb_residual_c128": [_P, _P, _P, _I64, _P, _P],
 }
+
+_RESTYPES = {"mb_gmres_workspace_bytes": ctypes.c_size_t}
+
+
+class GmresInfo(ctypes.Structure):
+    """mb_gmres_info (include/mesh_bem_gb300.h)."""
+
+    _fields_ = [("iterations", ctypes.c_int64), ("restarts", ctypes.c_int64),
+                ("rel_residual", ctypes.c_double), ("status", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 ABI_VERSION = 1
 
@@ -79,7 +93,7 @@ def load():
         for name, args in _SIGS.items():
             fn = getattr(lib, name)
             fn.argtypes = args
-            fn.restype = ctypes.c_int
+            fn.restype = _RESTYPES.get(name, ctypes.c_int)
         v = lib.mb_abi_version()
         if v != ABI_VERSION:
             raise ImportError(f"libmeshbem_gb300 ABI {v} != expected {ABI_VERSION}; rebuild it")

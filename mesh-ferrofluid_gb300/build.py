@@ -23,7 +23,7 @@ HEADER = os.path.join(REPO, "include", "mesh_bem_gb300.h")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-    "-Xptxas", "-O3",
+    "-Xptxas", "-O3", "-ftz=true",
 ]
 
 

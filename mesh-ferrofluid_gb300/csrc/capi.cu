@@ -47,6 +47,11 @@ int launch_laplace_panels(const T*, const int32_t*, int64_t, const T*, const T*,
 template <typename T>
 int launch_pack_tight(const T*, const T*, const int32_t*, int64_t, int64_t, int, T*, cudaStream_t);
 int launch_panel_relation(const int32_t*, int64_t, uint8_t*, cudaStream_t);
+size_t gmres_workspace_bytes(int64_t n, int m);
+int gmres_c64(const float*, int64_t, const double*, double*, int, int, double, void*, size_t, int64_t*,
+              int64_t*, double*, int*, cudaStream_t);
+int launch_matvec_c64(const float*, const float*, int64_t, double*, cudaStream_t);
+int launch_residual_c128(const float*, const double*, const double*, int64_t, double*, cudaStream_t);
 
 }  // namespace mb
 
@@ -236,6 +241,44 @@ MB_LAP(f64, double)
 MB_PACK(f32, float)
 MB_PACK(f64, double)
 #undef MB_PACK
+
+size_t mb_gmres_workspace_bytes(int64_t n, int restart) {
+    if (n <= 0 || restart < 1) return 0;
+    return gmres_workspace_bytes(n, restart);
+}
+
+int mb_gmres_c64(const float* z, int64_t n, const double* b, double* x, int restart, int max_iters,
+                 double tol, void* workspace, size_t workspace_bytes, mb_gmres_info* info, void* stream) {
+    MB_REQUIRE(n > 0, "n must be > 0");
+    MB_REQUIRE(z && b && x && workspace, "null pointer argument");
+    int64_t it = 0, cyc = 0;
+    double rr = 0.0;
+    int st = 1;
+    const int rc = gmres_c64(z, n, b, x, restart, max_iters, tol, workspace, workspace_bytes, &it, &cyc, &rr,
+                             &st, as_stream(stream));
+    if (rc == MB_OK && info) {
+        info->iterations = it;
+        info->restarts = cyc;
+        info->rel_residual = rr;
+        info->status = st;
+        info->reserved = 0;
+    }
+    return rc;
+}
+
+int mb_matvec_c64(const float* z, const float* v, int64_t n, double* y, void* stream) {
+    MB_REQUIRE(n >= 0, "bad sizes");
+    if (n == 0) return MB_OK;
+    MB_REQUIRE(z && v && y, "null pointer argument");
+    return launch_matvec_c64(z, v, n, y, as_stream(stream));
+}
+
+int mb_residual_c128(const float* z, const double* x, const double* b, int64_t n, double* r, void* stream) {
+    MB_REQUIRE(n >= 0, "bad sizes");
+    if (n == 0) return MB_OK;
+    MB_REQUIRE(z && x && b && r, "null pointer argument");
+    return launch_residual_c128(z, x, b, n, r, as_stream(stream));
+}
 
 int mb_panel_relation(const int32_t* faces, int64_t n_faces, uint8_t* relations, void* stream) {
     MB_REQUIRE(n_faces >= 0, "bad sizes");

@@ -228,6 +228,227 @@ __global__ void __launch_bounds__(128) mom_ref_zmat_rwg_kernel(
 }
 
 // ---------------------------------------------------------------------------------------
+// float fast path: compile-time rule sizes, projected moments, packed f32x2 arithmetic.
+//
+// Per test point x_i the entry needs only three complex sums over the source points:
+//   S0 = sum G,   P = sum G (y.a),   Q = sum G (1 + jkR) R^-2 (y.u)
+// with a = x - A0 and u = x x (a x n1) = a (x.n1) - n1 (x.a), because the old vector
+// moments were only ever used as a.S1 and u.H1.  y.a = r1 (y.e1) + r2 (y.e2) with the test
+// edge vectors e1 = A1 - A0, e2 = A2 - A1, so per source point the kernel keeps (y, w,
+// y.e1, y.e2, y.n1) in registers and an evaluation costs ~26 FP32 ops.  Two source points
+// ride in one packed f32x2 instruction (Blackwell `fma/mul/add/sub.rn.f32x2`); the SFU does
+// rsqrt, sin and cos.  The entry is then
+//   c1 c2 sum_i w_i [ -Q + jk P - (4j/k) S0 ]  (+ self term), identical to mom_entry.
+// ---------------------------------------------------------------------------------------
+typedef unsigned long long u64;
+__device__ __forceinline__ u64 pk(float2 a) { return *reinterpret_cast<u64*>(&a); }
+__device__ __forceinline__ float2 upk(u64 a) { return *reinterpret_cast<float2*>(&a); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    u64 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)), "l"(pk(c)));
+    return upk(d);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+    u64 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
+    return upk(d);
+}
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+    u64 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
+    return upk(d);
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    u64 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
+    return upk(d);
+}
+__device__ __forceinline__ float2 bc(float v) { return make_float2(v, v); }
+
+// Rule tables staged in shared memory: test (r1, r2, w_a w_b r1), source
+// (r3, r4, w_a w_b r3 / (4 pi)); index b*n + a as in the reference loops (:410-415).
+template <int NX, int NY>
+__device__ __forceinline__ void stage_rules(const float* gpx, const float* gwx, const float* gpy,
+                                            const float* gwy, float4* s_t, float4* s_s) {
+    const int t = threadIdx.x;
+    if (t < NX * NX) {
+        const float r1 = gpx[t / NX];
+        s_t[t] = make_float4(r1, gpx[t % NX] * r1, gwx[t / NX] * gwx[t % NX] * r1, 0.f);
+    } else if (t < NX * NX + NY * NY) {
+        const int j = t - NX * NX;
+        const float r3 = gpy[j / NY];
+        s_s[j] = make_float4(r3, gpy[j % NY] * r3, gwy[j / NY] * gwy[j % NY] * r3 * float(kInv4Pi), 0.f);
+    }
+}
+
+template <int NX, int NY>
+__device__ __forceinline__ void mom_entry_fast(const float* __restrict__ verts,
+                                               const int32_t* __restrict__ faces,
+                                               const float* __restrict__ areas,
+                                               const float* __restrict__ normals, const float4* s_t,
+                                               const float4* s_s, float k, int64_t f1, int e1, int64_t f2,
+                                               int e2, float* out_re, float* out_im) {
+    constexpr int NT = NX * NX, NS = NY * NY, NP = (NS + 1) / 2;
+    const int32_t a0 = __ldg(faces + 3 * f1 + e1);
+    const int32_t a1 = __ldg(faces + 3 * f1 + (e1 + 1) % 3);
+    const int32_t a2 = __ldg(faces + 3 * f1 + (e1 + 2) % 3);
+    const int32_t b0 = __ldg(faces + 3 * f2 + e2);
+    const int32_t b1 = __ldg(faces + 3 * f2 + (e2 + 1) % 3);
+    const int32_t b2 = __ldg(faces + 3 * f2 + (e2 + 2) % 3);
+    const V3<float> o = load3(verts, b0);
+    const V3<float> A0 = load3(verts, a0) - o;
+    const V3<float> A1 = load3(verts, a1) - o;
+    const V3<float> A2 = load3(verts, a2) - o;
+    const V3<float> B1 = load3(verts, b1) - o;
+    const V3<float> B2 = load3(verts, b2) - o;
+    const V3<float> n1 = load3(normals, f1);
+    const float area1 = __ldg(areas + f1), area2 = __ldg(areas + f2);
+    const V3<float> ev1 = A1 - A0, ev2 = A2 - A1;
+    const V3<float> d2 = B2 - B1;
+    const float c1 = (a1 < a2 ? 1.f : -1.f) * sqrtf(dot(ev2, ev2)) / (2.f * area1);
+    const float c2 = (b1 < b2 ? 1.f : -1.f) * sqrtf(dot(d2, d2)) / (2.f * area2);
+
+    // Source points (origin B0) packed two per register pair: coordinates, weight and the
+    // projections on the test edge vectors and normal.  An odd count is padded with a
+    // zero-weight copy of the last point (it adds exactly 0 to every sum).
+    float2 yx[NP], yy[NP], yz[NP], yw[NP], ye1[NP], ye2[NP], yn[NP];
+#pragma unroll
+    for (int j = 0; j < 2 * NP; ++j) {
+        const int js = j < NS ? j : NS - 1;
+        const float4 r = s_s[js];
+        const V3<float> y = (r.x - r.y) * B1 + r.y * B2;
+        const float w = j < NS ? r.z * (2.f * area2) : 0.f;
+        float* px = reinterpret_cast<float*>(&yx[j / 2]) + (j & 1);
+        px[0] = y.x;
+        (reinterpret_cast<float*>(&yy[j / 2]) + (j & 1))[0] = y.y;
+        (reinterpret_cast<float*>(&yz[j / 2]) + (j & 1))[0] = y.z;
+        (reinterpret_cast<float*>(&yw[j / 2]) + (j & 1))[0] = w;
+        (reinterpret_cast<float*>(&ye1[j / 2]) + (j & 1))[0] = dot(y, ev1);
+        (reinterpret_cast<float*>(&ye2[j / 2]) + (j & 1))[0] = dot(y, ev2);
+        (reinterpret_cast<float*>(&yn[j / 2]) + (j & 1))[0] = dot(y, n1);
+    }
+    const float2 K2 = bc(k), M4K = bc(-4.f / k);
+    float2 acc_re = bc(0.f), acc_im = bc(0.f);
+    float self_acc = 0.f;
+    const bool same = (f1 == f2);
+    // The test-point loop stays rolled: its body (the unrolled source loop) is ~2 KB of
+    // code, and unrolling it 16 times overflows the instruction cache.
+#pragma unroll 1
+    for (int i = 0; i < NT; ++i) {
+        const float4 t = s_t[i];
+        const float w1 = t.z * (2.f * area1);
+        const V3<float> a = t.x * ev1 + t.y * ev2;
+        const V3<float> x = A0 + a;
+        const float xn = dot(x, n1), xa = dot(x, a);
+        const float2 X = bc(x.x), Y = bc(x.y), Z = bc(x.z), R1 = bc(t.x), R2 = bc(t.y), XN = bc(xn),
+                     NXA = bc(-xa);
+        float2 s0r = bc(0.f), s0i = bc(0.f), pr = bc(0.f), pi = bc(0.f), qr = bc(0.f), qi = bc(0.f);
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            const float2 dx = sub2(X, yx[p]);
+            const float2 dy = sub2(Y, yy[p]);
+            const float2 dz = sub2(Z, yz[p]);
+            const float2 r2d = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+            float2 rinv;
+            rinv.x = rsqrtf(r2d.x);
+            rinv.y = rsqrtf(r2d.y);
+            const float2 kR = mul2(K2, mul2(r2d, rinv));
+            float2 sn, cs;
+            __sincosf(kR.x, &sn.x, &cs.x);
+            __sincosf(kR.y, &sn.y, &cs.y);
+            const float2 g = mul2(yw[p], rinv);
+            const float2 gr = mul2(g, cs), gs = mul2(g, sn);  // G = gr - j gs
+            const float2 ya = fma2(R1, ye1[p], mul2(R2, ye2[p]));
+            const float2 yu = fma2(ya, XN, mul2(yn[p], NXA));
+            s0r = add2(s0r, gr);
+            s0i = add2(s0i, gs);
+            pr = fma2(gr, ya, pr);
+            pi = fma2(gs, ya, pi);
+            const float2 m = mul2(mul2(rinv, rinv), yu);
+            const float2 t1 = fma2(gs, kR, gr);        // Re G(1 + jkR)
+            const float2 t2 = sub2(mul2(gr, kR), gs);  // Im G(1 + jkR)
+            qr = fma2(m, t1, qr);
+            qi = fma2(m, t2, qi);
+        }
+        // t_re = -Qr + k Pi - (4/k) S0i,  t_im = -Qi + k Pr - (4/k) S0r   (Pi, S0i hold +sum gs)
+        const float2 t_re = sub2(fma2(K2, pi, mul2(M4K, s0i)), qr);
+        const float2 t_im = sub2(fma2(K2, pr, mul2(M4K, s0r)), qi);
+        const float2 W1 = bc(w1);
+        acc_re = fma2(W1, t_re, acc_re);
+        acc_im = fma2(W1, t_im, acc_im);
+        if (same) self_acc += w1 * xa;  // (x - A0) . (x - B0), B0 = 0
+    }
+    const float cc = c1 * c2;
+    *out_re = cc * (acc_re.x + acc_re.y + 0.5f * self_acc);
+    *out_im = cc * (acc_im.x + acc_im.y);
+}
+
+#ifndef MB_FAST_MIN_BLOCKS
+#define MB_FAST_MIN_BLOCKS 4
+#endif
+template <int NX, int NY, bool RWG>
+__global__ void __launch_bounds__(128, NX <= 4 ? MB_FAST_MIN_BLOCKS : 2) mom_ref_zmat_fast_kernel(
+    const float* __restrict__ verts, const int32_t* __restrict__ faces, const float* __restrict__ areas,
+    const float* __restrict__ normals, const int32_t* __restrict__ fei, int64_t n_edges,
+    const float* __restrict__ gpx, const float* __restrict__ gwx, const float* __restrict__ gpy,
+    const float* __restrict__ gwy, float k, int64_t nf, int64_t batch, int64_t row_begin,
+    int64_t col_blocks, float* __restrict__ zr, float* __restrict__ zi) {
+    __shared__ float4 s_t[NX * NX], s_s[NY * NY];
+    stage_rules<NX, NY>(gpx, gwx, gpy, gwy, s_t, s_s);
+    __syncthreads();
+    const int64_t ncol = 3 * nf;
+    const int64_t row = row_begin + (int64_t)blockIdx.x / col_blocks;
+    const int64_t col = ((int64_t)blockIdx.x % col_blocks) * blockDim.x + threadIdx.x;
+    if (col >= ncol) return;
+    float re, im;
+    mom_entry_fast<NX, NY>(verts, faces, areas, normals, s_t, s_s, k, row / 3, (int)(row % 3), col / 3,
+                           (int)(col % 3), &re, &im);
+    if constexpr (RWG) {
+        const int64_t m = __ldg(fei + row), n = __ldg(fei + col);
+        atomicAdd(reinterpret_cast<float2*>(zr + 2 * (m * n_edges + n)), make_float2(re, im));
+    } else {
+        for (int64_t b = 0; b < batch; ++b) {
+            const int64_t o = (b * ncol + row) * ncol + col;
+            zr[o] = re;
+            zi[o] = im;
+        }
+    }
+}
+
+// Launches the fast path for float and supported rule sizes; returns false otherwise.
+template <typename T>
+bool launch_fast_zmat(const T*, const int32_t*, const T*, const T*, const int32_t*, int64_t, const T*,
+                      const T*, int, const T*, const T*, int, double, int64_t, int64_t, int64_t, int64_t,
+                      unsigned, T*, T*, cudaStream_t) {
+    return false;
+}
+template <>
+bool launch_fast_zmat<float>(const float* verts, const int32_t* faces, const float* areas,
+                             const float* normals, const int32_t* fei, int64_t n_edges, const float* gpx,
+                             const float* gwx, int nx, const float* gpy, const float* gwy, int ny, double k,
+                             int64_t nf, int64_t batch, int64_t row_begin, int64_t col_blocks,
+                             unsigned blocks, float* zr, float* zi, cudaStream_t stream) {
+#define MB_FAST(NXV, NYV)                                                                          \
+    if (nx == NXV && ny == NYV) {                                                                  \
+        if (fei)                                                                                   \
+            mom_ref_zmat_fast_kernel<NXV, NYV, true><<<blocks, 128, 0, stream>>>(                   \
+                verts, faces, areas, normals, fei, n_edges, gpx, gwx, gpy, gwy, (float)k, nf, batch,  \
+                row_begin, col_blocks, zr, zi);                                                    \
+        else                                                                                       \
+            mom_ref_zmat_fast_kernel<NXV, NYV, false><<<blocks, 128, 0, stream>>>(                  \
+                verts, faces, areas, normals, fei, n_edges, gpx, gwx, gpy, gwy, (float)k, nf, batch,  \
+                row_begin, col_blocks, zr, zi);                                                    \
+        return true;                                                                               \
+    }
+    MB_FAST(4, 3)
+    MB_FAST(3, 2)
+    MB_FAST(2, 1)
+    MB_FAST(5, 4)
+#undef MB_FAST
+    return false;
+}
+
+// ---------------------------------------------------------------------------------------
 // Excitation (mesh_MOM_3d.cu:244-330).  One thread per face-edge and right-hand side.
 // Plane wave E = e0 exp(-j k khat.x), H = (khat x e0)/eta exp(-j k khat.x); the
 // reference's hard-coded wave is khat = (cos 30, sin 30, 0), e0 = z, eta = 1.
@@ -368,6 +589,9 @@ int launch_mom_ref_zmat(const T* verts, int64_t nv, const int32_t* faces, int64_
     const int64_t blocks = rows * col_blocks;
     if (blocks <= 0) return MB_OK;
     if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "mesh too large for one launch");
+    if (launch_fast_zmat<T>(verts, faces, areas, normals, fei, n_edges, gpx, gwx, nx, gpy, gwy, ny, k, nf,
+                            batch, row_begin, col_blocks, (unsigned)blocks, zr, zi, stream))
+        return check_launch("mom_ref_zmat");
     const int ns = ny * ny;
 #define MB_ZMAT_LAUNCH(NSV)                                                                              \
     do {                                                                                                \

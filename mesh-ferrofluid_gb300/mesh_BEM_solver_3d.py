@@ -15,7 +15,9 @@ Same constructor and public methods as ``src/mesh_BEM/mesh_BEM_solver_3d.py:31-3
   boundary case the reference can run (mixed and Neumann data need its unimplemented
   hypersingular layer).
 
-Extra keyword ``solver`` selects "lu" (reference behaviour).  All tensors must live on a
+Extra keyword ``solver`` selects "lu" (reference behaviour, ``torch.linalg.solve``) or
+"gmres" (``mb_gmres_c64``: FP32 matrix-vector products on the complex64 matrix, FP64
+Arnoldi and refinement residual; float32 meshes only, float64 meshes keep LU).  All tensors must live on a
 CUDA device: there is no CPU implementation.
 """
 from __future__ import annotations
@@ -28,6 +30,7 @@ from .layers import DoubleLayer3d, RhsLayer3d, SingleLayer3d
 from .mesh_MOM_3d import (
     assemble_rhs_rwg,
     assemble_Z_rwg,
+    gmres,
     interpolate_vert_js,
     reference_plane_wave,
 )
@@ -47,7 +50,8 @@ class MeshBEMSolver3d:
 
     def __init__(self, gaussQR: int, order_type: int, BEM_type: int, wavenumber: float, logger=None,
                  dtype: torch.dtype = torch.float32, device: torch.device = torch.device("cpu"),
-                 solver: str = "lu"):
+                 solver: str = "lu", gmres_restart: int = 50, gmres_tol: float = 1e-6,
+                 gmres_max_iters: int = 2000):
         self._gaussQR = gaussQR
         self._order_type = order_type
         self._BEM_type = BEM_type
@@ -55,9 +59,13 @@ class MeshBEMSolver3d:
         self.logger = logger
         self.device = torch.device(device)
         self.dtype = dtype
-        if solver not in ("lu",):
+        if solver not in ("lu", "gmres"):
             raise ValueError(f"unknown solver {solver!r}")
         self.solver = solver
+        self.gmres_restart = gmres_restart
+        self.gmres_tol = gmres_tol
+        self.gmres_max_iters = gmres_max_iters
+        self.last_solve_info = None
         self.hypersingular_layer = None
         kw = dict(gaussQR=gaussQR, order_type=order_type, BEM_type=BEM_type, wavenumber=wavenumber,
                   logger=logger, dtype=dtype, device=self.device)
@@ -107,7 +115,12 @@ class MeshBEMSolver3d:
         assert self._BEM_type == int(BEMType.HELMHOLTZ_MOM)
         n_edges = edges.shape[0]
         Z, rhs, areas = self.assemble_MOM(verts, faces, n_edges, face_edge_indices)
-        I_coeff = torch.linalg.solve(Z, rhs)  # [E, 1]
+        if self.solver == "gmres" and Z.dtype == torch.complex64:
+            I_coeff, self.last_solve_info = gmres(Z, rhs, restart=self.gmres_restart,
+                                                  tol=self.gmres_tol, max_iters=self.gmres_max_iters)
+            I_coeff = I_coeff.to(Z.dtype)
+        else:
+            I_coeff = torch.linalg.solve(Z, rhs)  # [E, 1], as the reference (:174)
         fei = face_edge_indices.to(torch.int32).reshape(-1).contiguous()
         return interpolate_vert_js(verts.contiguous(), faces.to(torch.int32).contiguous(), fei,
                                    areas, I_coeff.reshape(1, n_edges))

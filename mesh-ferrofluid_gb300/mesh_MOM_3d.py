@@ -240,6 +240,77 @@ def interpolate_vert_js(verts, faces, face_edge_indices, face_areas, i_coeff, ou
 
 
 # ---------------------------------------------------------------------------------------
+# dense iterative solve (replaces torch.linalg.solve at mesh_BEM_solver_3d.py:174)
+# ---------------------------------------------------------------------------------------
+def gmres_workspace_bytes(n: int, restart: int = 50) -> int:
+    return int(_lib.load().mb_gmres_workspace_bytes(int(n), int(restart)))
+
+
+def gmres(Z, b, x0=None, restart: int = 50, max_iters: int = 2000, tol: float = 1e-6,
+          workspace=None):
+    """Solve Z x = b by GMRES(restart) with FP64 refinement residuals (``mb_gmres_c64``).
+
+    Z: complex64 [n, n] CUDA tensor.  b: [n] or [n, k] (any complex/real dtype; solved in
+    complex128).  Returns (x complex128 with b's shape, list of per-column info dicts with
+    ``iterations``, ``restarts``, ``rel_residual`` and ``converged``).  ``workspace`` is an
+    optional uint8 CUDA tensor of at least ``gmres_workspace_bytes(n, restart)`` bytes.
+    """
+    _lib.check_tensor(Z, "Z", dtype=torch.complex64, ndim=2)
+    n = Z.shape[0]
+    if Z.shape[1] != n:
+        raise ValueError("Z must be square")
+    dev = Z.device
+    bb = b.to(device=dev, dtype=torch.complex128)
+    single = bb.dim() == 1
+    bb = bb.reshape(n, -1)
+    if x0 is None:
+        xx = torch.zeros_like(bb)
+    else:
+        xx = x0.to(device=dev, dtype=torch.complex128).reshape(n, -1).clone()
+    need = gmres_workspace_bytes(n, restart)
+    if workspace is None:
+        workspace = torch.empty(need, dtype=torch.uint8, device=dev)
+    else:
+        _lib.check_tensor(workspace, "workspace", dtype=torch.uint8, device=dev)
+        if workspace.numel() < need:
+            raise ValueError(f"workspace needs {need} bytes")
+    infos = []
+    for c in range(bb.shape[1]):
+        bc_ = bb[:, c].contiguous()
+        xc = xx[:, c].contiguous()
+        info = _lib.GmresInfo()
+        _lib.call("mb_gmres_c64", _lib.ptr(Z), n, _lib.ptr(bc_), _lib.ptr(xc), int(restart),
+                  int(max_iters), float(tol), _lib.ptr(workspace), workspace.numel(),
+                  __import__("ctypes").byref(info), _lib.stream_of(Z))
+        xx[:, c] = xc
+        infos.append({"iterations": info.iterations, "restarts": info.restarts,
+                      "rel_residual": info.rel_residual, "converged": info.status == 0})
+    return (xx[:, 0] if single else xx), infos
+
+
+def matvec(Z, v):
+    """y = Z v (complex64 Z, v cast to complex64) with FP64 row sums -> complex128 [n]."""
+    _lib.check_tensor(Z, "Z", dtype=torch.complex64, ndim=2)
+    n = Z.shape[0]
+    vv = v.to(device=Z.device, dtype=torch.complex64).reshape(n).contiguous()
+    y = torch.empty(n, dtype=torch.complex128, device=Z.device)
+    _lib.call("mb_matvec_c64", _lib.ptr(Z), _lib.ptr(vv), n, _lib.ptr(y), _lib.stream_of(Z))
+    return y
+
+
+def residual(Z, x, b):
+    """r = b - Z x in FP64 (complex64 Z; x, b complex128 [n])."""
+    _lib.check_tensor(Z, "Z", dtype=torch.complex64, ndim=2)
+    n = Z.shape[0]
+    xx = x.to(device=Z.device, dtype=torch.complex128).reshape(n).contiguous()
+    bb = b.to(device=Z.device, dtype=torch.complex128).reshape(n).contiguous()
+    r = torch.empty(n, dtype=torch.complex128, device=Z.device)
+    _lib.call("mb_residual_c128", _lib.ptr(Z), _lib.ptr(xx), _lib.ptr(bb), n, _lib.ptr(r),
+              _lib.stream_of(Z))
+    return r
+
+
+# ---------------------------------------------------------------------------------------
 # torch.ops registration (TORCH_LIBRARY(mesh_MOM_3d), mesh_MOM_3d.cpp:117-121)
 # ---------------------------------------------------------------------------------------
 _registered = None

@@ -85,6 +85,27 @@ def test_zmat_fe_f32_vs_oracle(pkg, cuda, oracle, level, k):
     assert rel_err(z, ref) < TOL32
 
 
+def test_zmat_fe_f32_high_k_row_slice_vs_oracle(pkg, cuda, oracle):
+    """ka = 10 on the 1280-face sphere: phases kR up to ~20 rad through the SFU sin/cos."""
+    v_np, f_np = pkg.meshes.icosphere(3)
+    k = 10.0
+    v = torch.tensor(v_np, dtype=torch.float32, device=cuda)
+    f = torch.tensor(f_np, dtype=torch.int32, device=cuda)
+    a = pkg.utils.compute_face_areas(v, f).contiguous()
+    n = pkg.utils.compute_face_normals(v, f).contiguous()
+    px, wx = pkg.utils.get_gaussion_integration_points_and_weights(4, device=cuda)
+    py, wy = pkg.utils.get_gaussion_integration_points_and_weights(3, device=cuda)
+    nf = f.shape[0]
+    zr = torch.zeros((1, 3 * nf, 3 * nf), dtype=torch.float32, device=cuda)
+    zi = torch.zeros_like(zr)
+    pkg.mesh_MOM_3d.create_MOM_Zmat_3d_forward(v, f, a, n, px, wx, py, wy, zr, zi, k)
+    rows = (1200, 1500)
+    z = (zr[0, rows[0]:rows[1]].double() + 1j * zi[0, rows[0]:rows[1]].double()).cpu().numpy()
+    h = lambda t: t.cpu().double().numpy()  # noqa: E731
+    ref = oracle.mom_zmat_fe(h(v), f_np, h(a), h(n), h(px), h(wx), h(py), h(wy), k, rows=rows)
+    assert rel_err(z, ref) < TOL32
+
+
 @pytest.mark.parametrize("dt,tol", [(torch.float32, TOL32), (torch.float64, TOL64)])
 def test_zmat_rwg_equals_scattered_face_edge(pkg, cuda, golden, oracle, dt, tol):
     g = golden["ell1"]
