@@ -151,6 +151,22 @@ int mb_gmres_c64(const float* z, int64_t n, const double* b, double* x, int rest
                  double tol, void* workspace, size_t workspace_bytes, mb_gmres_info* info,
                  void* stream);
 
+/* No counterpart in the reference.  The same solver as mb_gmres_c64 for callers that
+ * cannot allocate device memory -- for example a host application or plugin that must
+ * budget all GPU memory at start-up, or a foreign-language caller (Go, Java, ...) that has
+ * no access to a CUDA allocator.  It takes no workspace and allocates nothing: the device
+ * scratch is a fixed array inside this library (about 7 MB, held on every GPU that loads
+ * the library until the process exits), sized for at most MB_GMRES_NOALLOC_MAX_N unknowns
+ * and restart <= MB_GMRES_NOALLOC_MAX_RESTART; larger requests fail with MB_ERR_SIZE.
+ * The first call on each device looks up that array's device address (a one-time set-up
+ * with that device current); make that first call before any stream capture.  All calls
+ * share the array, which keeps the previous call's contents (the solver writes every
+ * scratch value before reading it); calls that overlap on the GPU race on it. */
+#define MB_GMRES_NOALLOC_MAX_N 8192
+#define MB_GMRES_NOALLOC_MAX_RESTART 50
+int mb_gmres_c64_noalloc(const float* z, int64_t n, const double* b, double* x, int restart,
+                         int max_iters, double tol, mb_gmres_info* info, void* stream);
+
 /* y = Z v: Z interleaved complex64 [n, n], v complex64 [n], y complex128 [n] (FP32 products,
  * FP64 row reduction).  The HBM-bound kernel inside mb_gmres_c64. */
 int mb_matvec_c64(const float* z, const float* v, int64_t n, double* y, void* stream);

@@ -50,6 +50,8 @@ int launch_panel_relation(const int32_t*, int64_t, uint8_t*, cudaStream_t);
 size_t gmres_workspace_bytes(int64_t n, int m);
 int gmres_c64(const float*, int64_t, const double*, double*, int, int, double, void*, size_t, int64_t*,
               int64_t*, double*, int*, cudaStream_t);
+int gmres_c64_noalloc(const float*, int64_t, const double*, double*, int, int, double, int64_t*, int64_t*,
+                      double*, int*, cudaStream_t);
 int launch_matvec_c64(const float*, const float*, int64_t, double*, cudaStream_t);
 int launch_residual_c128(const float*, const double*, const double*, int64_t, double*, cudaStream_t);
 
@@ -256,6 +258,24 @@ int mb_gmres_c64(const float* z, int64_t n, const double* b, double* x, int rest
     int st = 1;
     const int rc = gmres_c64(z, n, b, x, restart, max_iters, tol, workspace, workspace_bytes, &it, &cyc, &rr,
                              &st, as_stream(stream));
+    if (rc == MB_OK && info) {
+        info->iterations = it;
+        info->restarts = cyc;
+        info->rel_residual = rr;
+        info->status = st;
+        info->reserved = 0;
+    }
+    return rc;
+}
+
+int mb_gmres_c64_noalloc(const float* z, int64_t n, const double* b, double* x, int restart, int max_iters,
+                         double tol, mb_gmres_info* info, void* stream) {
+    MB_REQUIRE(n > 0, "n must be > 0");
+    MB_REQUIRE(z && b && x, "null pointer argument");
+    int64_t it = 0, cyc = 0;
+    double rr = 0.0;
+    int st = 1;
+    const int rc = gmres_c64_noalloc(z, n, b, x, restart, max_iters, tol, &it, &cyc, &rr, &st, as_stream(stream));
     if (rc == MB_OK && info) {
         info->iterations = it;
         info->restarts = cyc;

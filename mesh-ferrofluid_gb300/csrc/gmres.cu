@@ -18,6 +18,7 @@
 
 #include <cmath>
 #include <complex>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -227,11 +228,14 @@ struct GmresWork {
     double* nrm;    // [2]
 };
 
-size_t gmres_workspace_bytes(int64_t n, int m) {
-    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
-    return al(sizeof(double) * 2 * (size_t)(m + 1) * n) + 2 * al(sizeof(double) * 2 * n) +
-           al(sizeof(float) * 2 * n) + al(sizeof(double) * 2 * (m + 2)) + al(sizeof(double) * 4);
+constexpr size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
+
+constexpr size_t gmres_ws_bytes(int64_t n, int m) {
+    return al256(sizeof(double) * 2 * (size_t)(m + 1) * n) + 2 * al256(sizeof(double) * 2 * n) +
+           al256(sizeof(float) * 2 * n) + al256(sizeof(double) * 2 * (m + 2)) + al256(sizeof(double) * 4);
 }
+
+size_t gmres_workspace_bytes(int64_t n, int m) { return gmres_ws_bytes(n, m); }
 
 static GmresWork carve(void* ws, int64_t n, int m) {
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
@@ -267,6 +271,21 @@ static int norm_of(const double* w, int64_t n, double* d_out, double* h_out, cud
     return rc;
 }
 
+// Host-side bookkeeping of one GMRES(m) run (Hessenberg columns, rotations, rhs), sized for m.
+struct GmresHost {
+    std::complex<double>* H;     // [(m+1) * m]
+    std::complex<double>* cs;    // [m]
+    std::complex<double>* sn;    // [m]
+    std::complex<double>* gvec;  // [m+1]
+    std::complex<double>* hcol;  // [m+2]
+    std::complex<double>* yv;    // [m]
+    double* hbuf;                // [2 (m+1)]
+};
+
+static int gmres_core(const float* z, int64_t n, const double* b, double* x, int m, int max_iters,
+                      double tol, void* workspace, const GmresHost& hs, int64_t* iters_out,
+                      int64_t* cycles_out, double* relres_out, int* status_out, cudaStream_t s);
+
 int gmres_c64(const float* z, int64_t n, const double* b, double* x, int m, int max_iters, double tol,
               void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out,
               double* relres_out, int* status_out, cudaStream_t s) {
@@ -275,7 +294,22 @@ int gmres_c64(const float* z, int64_t n, const double* b, double* x, int m, int 
     if (max_iters < 1) return set_error(MB_ERR_ARG, "max_iters must be >= 1");
     if (!(tol > 0)) return set_error(MB_ERR_ARG, "tol must be > 0");
     if (ws_bytes < gmres_workspace_bytes(n, m)) return set_error(MB_ERR_ARG, "workspace too small");
+    std::vector<std::complex<double>> H((size_t)(m + 1) * m), cs(m), sn(m), gvec(m + 1), hcol(m + 2), yv(m);
+    std::vector<double> hbuf(2 * (m + 1));
+    const GmresHost hs{H.data(), cs.data(), sn.data(), gvec.data(), hcol.data(), yv.data(), hbuf.data()};
+    return gmres_core(z, n, b, x, m, max_iters, tol, workspace, hs, iters_out, cycles_out, relres_out,
+                      status_out, s);
+}
+
+static int gmres_core(const float* z, int64_t n, const double* b, double* x, int m, int max_iters,
+                      double tol, void* workspace, const GmresHost& hs, int64_t* iters_out,
+                      int64_t* cycles_out, double* relres_out, int* status_out, cudaStream_t s) {
     GmresWork g = carve(workspace, n, m);
+    std::complex<double>* H = hs.H;
+    std::complex<double>* cs = hs.cs;
+    std::complex<double>* sn = hs.sn;
+    std::complex<double>* gvec = hs.gvec;
+    double* hbuf = hs.hbuf;
     const int tb = 256;
     const unsigned vblocks = (unsigned)((n + tb - 1) / tb);
     const unsigned rblocks = (unsigned)((n + 7) / 8);
@@ -284,8 +318,6 @@ int gmres_c64(const float* z, int64_t n, const double* b, double* x, int m, int 
     double bnorm;
     if ((rc = norm_of(b, n, g.nrm, &bnorm, s))) return rc;
     if (bnorm == 0.0) bnorm = 1.0;
-    std::vector<std::complex<double>> H((size_t)(m + 1) * m), cs(m), sn(m), gvec(m + 1);
-    std::vector<double> hbuf(2 * (m + 1));
     int64_t iters = 0, cycles = 0;
     double relres = 0.0;
     int status = 1;
@@ -302,18 +334,19 @@ int gmres_c64(const float* z, int64_t n, const double* b, double* x, int m, int 
         if (iters >= max_iters) break;
         ++cycles;
         scale_kernel<<<vblocks, tb, 0, s>>>(g.r, 1.0 / beta, n, g.V, g.v32);
-        std::fill(gvec.begin(), gvec.end(), std::complex<double>(0.0));
+        for (int i = 0; i <= m; ++i) gvec[i] = 0.0;
         gvec[0] = beta;
         int j = 0;
         for (; j < m && iters < max_iters; ++j, ++iters) {
             matvec_c64_kernel<<<rblocks, 256, 0, s>>>(z, g.v32, n, g.w);
             // CGS2: two passes of h = V^H w; w -= V h
-            std::vector<std::complex<double>> hcol(j + 2, 0.0);
+            std::complex<double>* hcol = hs.hcol;
+            for (int i = 0; i < j + 2; ++i) hcol[i] = 0.0;
             for (int pass = 0; pass < 2; ++pass) {
                 cudaMemsetAsync(g.h, 0, sizeof(double) * 2 * (j + 1), s);
                 dots_kernel<<<dblocks, 256, 0, s>>>(g.V, g.w, n, j + 1, g.h);
                 subtract_basis_kernel<<<vblocks, tb, 0, s>>>(g.V, g.h, n, j + 1, g.w);
-                cudaMemcpyAsync(hbuf.data(), g.h, sizeof(double) * 2 * (j + 1), cudaMemcpyDeviceToHost, s);
+                cudaMemcpyAsync(hbuf, g.h, sizeof(double) * 2 * (j + 1), cudaMemcpyDeviceToHost, s);
                 if ((rc = sync_check(s, "gmres arnoldi"))) return rc;
                 for (int i = 0; i <= j; ++i) hcol[i] += std::complex<double>(hbuf[2 * i], hbuf[2 * i + 1]);
             }
@@ -350,7 +383,7 @@ int gmres_c64(const float* z, int64_t n, const double* b, double* x, int m, int 
             }
         }
         // back substitution H y = g (upper triangular j x j), then x += V y
-        std::vector<std::complex<double>> yv(j);
+        std::complex<double>* yv = hs.yv;
         for (int i = j - 1; i >= 0; --i) {
             std::complex<double> acc = gvec[i];
             for (int q = i + 1; q < j; ++q) acc -= H[(size_t)i * m + q] * yv[q];
@@ -360,7 +393,7 @@ int gmres_c64(const float* z, int64_t n, const double* b, double* x, int m, int 
             hbuf[2 * i] = yv[i].real();
             hbuf[2 * i + 1] = yv[i].imag();
         }
-        cudaMemcpyAsync(g.h, hbuf.data(), sizeof(double) * 2 * j, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(g.h, hbuf, sizeof(double) * 2 * j, cudaMemcpyHostToDevice, s);
         add_basis_kernel<<<vblocks, tb, 0, s>>>(g.V, g.h, n, j, x);
         if ((rc = sync_check(s, "gmres update"))) return rc;
     }
@@ -369,6 +402,78 @@ int gmres_c64(const float* z, int64_t n, const double* b, double* x, int m, int 
     if (relres_out) *relres_out = relres;
     if (status_out) *status_out = status;
     return MB_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// GMRES without any allocation, for callers that cannot allocate device memory.
+//
+// The device scratch is a fixed array in this library's own device memory: every GPU
+// that loads the library holds it (about 7 MB) until the process exits.  The host-side
+// bookkeeping uses per-thread static storage.  Limits: n <= kNoAllocMaxN unknowns,
+// restart <= kNoAllocMaxRestart.
+// The first call on each device looks up the array's device address with
+// cudaGetSymbolAddress (with that device current) and caches it; make that first call
+// before any stream capture.  All calls on a device share the one array and it keeps the
+// previous call's contents; the solver writes every scratch value before reading it.
+// Calls that overlap on the GPU (other streams, other host threads) race on the array.
+// ---------------------------------------------------------------------------------------
+constexpr int64_t kNoAllocMaxN = 8192;
+constexpr int kNoAllocMaxRestart = 50;
+constexpr size_t kNoAllocScratchBytes = gmres_ws_bytes(kNoAllocMaxN, kNoAllocMaxRestart);
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_gmres_scratch[kNoAllocScratchBytes];
+
+static thread_local double tl_H[2 * (kNoAllocMaxRestart + 1) * kNoAllocMaxRestart];
+static thread_local double tl_cs[2 * kNoAllocMaxRestart];
+static thread_local double tl_sn[2 * kNoAllocMaxRestart];
+static thread_local double tl_g[2 * (kNoAllocMaxRestart + 1)];
+static thread_local double tl_hcol[2 * (kNoAllocMaxRestart + 2)];
+static thread_local double tl_y[2 * kNoAllocMaxRestart];
+static thread_local double tl_hbuf[2 * (kNoAllocMaxRestart + 1)];
+
+static std::mutex g_scratch_mu;
+static void* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_gmres_scratch on the current device (looked up once per device).
+static int scratch_for_current_device(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(MB_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return set_error(MB_ERR_UNSUPPORTED, "device ordinal %d too large", dev);
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (g_scratch_ptr[dev] == nullptr) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_gmres_scratch);
+        if (e != cudaSuccess || p == nullptr)
+            return set_error(MB_ERR_CUDA, "cudaGetSymbolAddress(gmres scratch): %s", cudaGetErrorString(e));
+        g_scratch_ptr[dev] = p;
+    }
+    *out = g_scratch_ptr[dev];
+    return MB_OK;
+}
+
+int gmres_c64_noalloc(const float* z, int64_t n, const double* b, double* x, int m, int max_iters, double tol,
+                      int64_t* iters_out, int64_t* cycles_out, double* relres_out, int* status_out,
+                      cudaStream_t s) {
+    if (n <= 0) return set_error(MB_ERR_ARG, "n must be > 0");
+    if (n > kNoAllocMaxN)
+        return set_error(MB_ERR_SIZE,
+                         "mb_gmres_c64_noalloc: n = %lld unknowns exceeds the built-in scratch limit of %lld; "
+                         "use mb_gmres_c64 with a caller-owned workspace",
+                         (long long)n, (long long)kNoAllocMaxN);
+    if (m < 1 || m > kNoAllocMaxRestart)
+        return set_error(MB_ERR_SIZE, "mb_gmres_c64_noalloc: restart = %d outside [1, %d]", m, kNoAllocMaxRestart);
+    if (max_iters < 1) return set_error(MB_ERR_ARG, "max_iters must be >= 1");
+    if (!(tol > 0)) return set_error(MB_ERR_ARG, "tol must be > 0");
+    void* ws = nullptr;
+    int rc = scratch_for_current_device(&ws);
+    if (rc) return rc;
+    using cd = std::complex<double>;
+    const GmresHost hs{reinterpret_cast<cd*>(tl_H), reinterpret_cast<cd*>(tl_cs), reinterpret_cast<cd*>(tl_sn),
+                       reinterpret_cast<cd*>(tl_g), reinterpret_cast<cd*>(tl_hcol), reinterpret_cast<cd*>(tl_y),
+                       tl_hbuf};
+    return gmres_core(z, n, b, x, m, max_iters, tol, ws, hs, iters_out, cycles_out, relres_out, status_out, s);
 }
 
 int launch_matvec_c64(const float* z, const float* v, int64_t n, double* y, cudaStream_t s) {
