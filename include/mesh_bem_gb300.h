@@ -125,6 +125,21 @@ int mb_mom_interp_vert_c128(const double* verts, int64_t n_verts, const int32_t*
                             const double* face_areas, const double* i_coeff, int64_t n_edges,
                             int64_t batch, double* vert_js, void* stream);
 
+/* ---- Radiated field (post-solve) ---------------------------------------------------- */
+
+/* Replaces the scattered-field sum after solve_MOM (demo/demo_Helmholtz_MOM_3d.py:246-257,
+ * gradG_y / G of src/utils/functions.py:807-868):
+ *   h[p] = sum_v vert_areas[v] * ( js[v] x gradG_y(k, points[p], verts[v]) ),
+ * gradG_y = e^{+jkR} (1 + jkR) / (4 pi R^2) * (p - v)/R, vertices closer than 1e-6 skipped.
+ * points [n_points, 3], verts [n_verts, 3], vert_areas [n_verts]; js: interleaved complex
+ * [n_verts, 3]; h: interleaved complex [n_points, 3], overwritten. */
+int mb_radiate_h_c64(const float* points, int64_t n_points, const float* verts,
+                     const float* vert_areas, const float* js, int64_t n_verts, double wavenumber,
+                     float* h, void* stream);
+int mb_radiate_h_c128(const double* points, int64_t n_points, const double* verts,
+                      const double* vert_areas, const double* js, int64_t n_verts,
+                      double wavenumber, double* h, void* stream);
+
 /* ---- Dense iterative solve (replaces torch.linalg.solve, mesh_BEM_solver_3d.py:174) -- */
 
 /* Outcome of mb_gmres_c64. status: 0 converged to tol, 1 stopped at max_iters. */

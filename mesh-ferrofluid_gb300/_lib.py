@@ -44,6 +44,8 @@ _SIGS = {
     "mb_pack_tight_f32": [_P, _P, _P, _I64, _I64, _I, _P, _P],
     "mb_pack_tight_f64": [_P, _P, _P, _I64, _I64, _I, _P, _P],
     "mb_panel_relation": [_P, _I64, _P, _P],
+    "mb_radiate_h_c64": [_P, _I64, _P, _P, _P, _I64, _D, _P, _P],
+    "mb_radiate_h_c128": [_P, _I64, _P, _P, _P, _I64, _D, _P, _P],
     "mb_gmres_workspace_bytes": [_I64, _I],
     "mb_gmres_c64": [_P, _I64, _P, _P, _I, _I, _D, _P, ctypes.c_size_t, _P, _P],
     "mb_gmres_c64_noalloc": [_P, _I64, _P, _P, _I, _I, _D, _P, _P],

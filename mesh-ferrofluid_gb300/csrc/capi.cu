@@ -48,6 +48,8 @@ template <typename T>
 int launch_pack_tight(const T*, const T*, const int32_t*, int64_t, int64_t, int, T*, cudaStream_t);
 int launch_panel_relation(const int32_t*, int64_t, uint8_t*, cudaStream_t);
 size_t gmres_workspace_bytes(int64_t n, int m);
+template <typename T>
+int launch_radiate_h(const T*, int64_t, const T*, const T*, const T*, int64_t, double, T*, cudaStream_t);
 int gmres_c64(const float*, int64_t, const double*, double*, int, int, double, void*, size_t, int64_t*,
               int64_t*, double*, int*, cudaStream_t);
 int gmres_c64_noalloc(const float*, int64_t, const double*, double*, int, int, double, int64_t*, int64_t*,
@@ -243,6 +245,20 @@ MB_LAP(f64, double)
 MB_PACK(f32, float)
 MB_PACK(f64, double)
 #undef MB_PACK
+
+#define MB_RAD(SFX, T)                                                                                \
+    int mb_radiate_h_##SFX(const T* points, int64_t n_points, const T* verts, const T* vert_areas,       \
+                           const T* js, int64_t n_verts, double wavenumber, T* h, void* stream) {       \
+        MB_REQUIRE(n_points >= 0 && n_verts >= 0, "bad sizes");                                       \
+        if (n_points == 0) return MB_OK;                                                              \
+        MB_REQUIRE(points && h && (n_verts == 0 || (verts && vert_areas && js)),                       \
+                   "null pointer argument");                                                          \
+        return launch_radiate_h<T>(points, n_points, verts, vert_areas, js, n_verts, wavenumber, h,    \
+                                   as_stream(stream));                                                \
+    }
+MB_RAD(c64, float)
+MB_RAD(c128, double)
+#undef MB_RAD
 
 size_t mb_gmres_workspace_bytes(int64_t n, int restart) {
     if (n <= 0 || restart < 1) return 0;

@@ -1,0 +1,102 @@
+// field.cu -- scattered magnetic field radiated by the solved vertex currents.
+//
+// Reference: the post-solve step of demo/demo_Helmholtz_MOM_3d.py:246-257,
+//   H(p) = -sum_v A_v ( J_v x (-gradG_y(k, p, v)) )
+// with gradG_y / G of src/utils/functions.py:807-868 (pos_k = False), which evaluate to
+//   gradG_y = e^{+jkR} (1 + jkR) / (4 pi R^2) * (p - v)/R,   zero where R < 1e-6.
+// (The +jkR phase is what those helpers compute -- G is called with the already negated
+// wavenumber -- and is reproduced as is.)
+//
+// A dense P x V sum: each thread owns one observation point and accumulates the six
+// components of H; 256 vertices at a time (position and A_v J_v, 9 values) are staged in
+// shared memory so each vertex is read once per block.  Per interaction: ~40 FP32 ops and
+// 3 SFU ops (rsqrt, sin, cos).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace mb {
+
+constexpr int kFieldThreads = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(kFieldThreads) radiate_h_kernel(const T* __restrict__ points, int64_t np,
+                                                                  const T* __restrict__ verts,
+                                                                  const T* __restrict__ vert_areas,
+                                                                  const T* __restrict__ js, int64_t nv, T k,
+                                                                  T* __restrict__ h) {
+    __shared__ T s_v[kFieldThreads][9];
+    const int64_t m = (int64_t)blockIdx.x * kFieldThreads + threadIdx.x;
+    V3<T> p = v3<T>(0, 0, 0);
+    if (m < np) p = load3(points, m);
+    T hr[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    const T k_turn = k * T(kInv2Pi);
+    const T eps2 = T(1e-12);  // R < 1e-6 contributes nothing (functions.py:832-834, :860-862)
+    for (int64_t base = 0; base < nv; base += kFieldThreads) {
+        const int64_t v = base + threadIdx.x;
+        if (v < nv) {
+            const T a = vert_areas[v];
+            s_v[threadIdx.x][0] = verts[3 * v];
+            s_v[threadIdx.x][1] = verts[3 * v + 1];
+            s_v[threadIdx.x][2] = verts[3 * v + 2];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                s_v[threadIdx.x][3 + c] = a * js[2 * (3 * v + c)];
+                s_v[threadIdx.x][6 + c] = a * js[2 * (3 * v + c) + 1];
+            }
+        }
+        __syncthreads();
+        const int cnt = (int)((nv - base) < kFieldThreads ? (nv - base) : kFieldThreads);
+        if (m < np) {
+            for (int t = 0; t < cnt; ++t) {
+                const T* q = s_v[t];
+                const T dx = p.x - q[0], dy = p.y - q[1], dz = p.z - q[2];
+                const T r2 = dx * dx + dy * dy + dz * dz;
+                if (r2 < eps2) continue;
+                const T rinv = rsqrt_t(r2);
+                const T R = r2 * rinv;
+                T sn, cs;
+                sincos_turns(k_turn * R, &sn, &cs);  // e^{+jkR} = cs + j sn
+                const T kR = k * R;
+                const T s = rinv * rinv * rinv * T(kInv4Pi);
+                const T fr = (cs - kR * sn) * s;  // (1 + jkR) e^{+jkR} / (4 pi R^3)
+                const T fi = (sn + kR * cs) * s;
+                // (A J) x d, real and imaginary parts
+                const T crx = q[4] * dz - q[5] * dy, cry = q[5] * dx - q[3] * dz, crz = q[3] * dy - q[4] * dx;
+                const T cix = q[7] * dz - q[8] * dy, ciy = q[8] * dx - q[6] * dz, ciz = q[6] * dy - q[7] * dx;
+                hr[0] += fr * crx - fi * cix;
+                hr[1] += fr * cry - fi * ciy;
+                hr[2] += fr * crz - fi * ciz;
+                hi[0] += fr * cix + fi * crx;
+                hi[1] += fr * ciy + fi * cry;
+                hi[2] += fr * ciz + fi * crz;
+            }
+        }
+        __syncthreads();
+    }
+    if (m < np) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            h[2 * (3 * m + c)] = hr[c];
+            h[2 * (3 * m + c) + 1] = hi[c];
+        }
+    }
+}
+
+template <typename T>
+int launch_radiate_h(const T* points, int64_t np, const T* verts, const T* vert_areas, const T* js, int64_t nv,
+                     double k, T* h, cudaStream_t stream) {
+    if (np <= 0) return MB_OK;
+    const int64_t blocks = (np + kFieldThreads - 1) / kFieldThreads;
+    if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "too many observation points for one launch");
+    radiate_h_kernel<T><<<(unsigned)blocks, kFieldThreads, 0, stream>>>(points, np, verts, vert_areas, js, nv,
+                                                                        (T)k, h);
+    return check_launch("radiate_h");
+}
+template int launch_radiate_h<float>(const float*, int64_t, const float*, const float*, const float*, int64_t,
+                                     double, float*, cudaStream_t);
+template int launch_radiate_h<double>(const double*, int64_t, const double*, const double*, const double*,
+                                      int64_t, double, double*, cudaStream_t);
+
+}  // namespace mb

@@ -240,6 +240,34 @@ def interpolate_vert_js(verts, faces, face_edge_indices, face_areas, i_coeff, ou
 
 
 # ---------------------------------------------------------------------------------------
+# radiated field after the solve (demo/demo_Helmholtz_MOM_3d.py:246-257)
+# ---------------------------------------------------------------------------------------
+def radiate_H(points, verts, vert_areas, vert_Js, wavenumber, out=None):
+    """Scattered H [P, 3] complex at ``points`` [P, 3] from vertex currents ``vert_Js`` [V, 3].
+
+    Equals the reference's ``-(vert_areas * cross(Js, -gradG_y(k, p1=points, p2=verts))).sum(-2)``
+    (its helpers' e^{+jkR} phase and 1e-6 singularity mask included), as one fused kernel.
+    """
+    _lib.check_tensor(verts, "verts", dtype=_FLOATS, ndim=2)
+    dt, dev = verts.dtype, verts.device
+    cdt = torch.complex64 if dt == torch.float32 else torch.complex128
+    pts = points.to(device=dev, dtype=dt).reshape(-1, 3).contiguous()
+    va = vert_areas.to(device=dev, dtype=dt).reshape(-1).contiguous()
+    js = vert_Js.to(device=dev, dtype=cdt).reshape(-1, 3).contiguous()
+    nv = verts.shape[0]
+    if va.numel() != nv or js.shape[0] != nv:
+        raise ValueError("vert_areas / vert_Js must have one entry per vertex")
+    n_pts = pts.shape[0]
+    if out is None:
+        out = torch.empty((n_pts, 3), dtype=cdt, device=dev)
+    else:
+        _lib.check_tensor(out, "out", dtype=cdt, device=dev, shape=(n_pts, 3))
+    _lib.call(f"mb_radiate_h_{_lib.csfx(dt)}", _lib.ptr(pts), n_pts, _lib.ptr(verts), _lib.ptr(va),
+              _lib.ptr(js), nv, float(wavenumber), _lib.ptr(out), _lib.stream_of(verts))
+    return out
+
+
+# ---------------------------------------------------------------------------------------
 # dense iterative solve (replaces torch.linalg.solve at mesh_BEM_solver_3d.py:174)
 # ---------------------------------------------------------------------------------------
 def gmres_workspace_bytes(n: int, restart: int = 50) -> int:

@@ -11,6 +11,8 @@
  *   - kernel_interpolate_Icoeff_to_Js_3d_forward  src/mesh_BEM/cuda/mesh_MOM_3d.cu:498-565
  *     with the helpers G :72-95, gradG_y :97-126, gradG_x :128-152, is_Tn_plus :154-165,
  *     RWG :167-206, div_RWG :208-242, calculate_Einc :24-38, calculate_Hinc :40-70
+ *   - the scattered-field sum after the solve  demo/demo_Helmholtz_MOM_3d.py:246-257 with
+ *     G / gradG_y                           src/utils/functions.py:807-868
  *   - get_rands_and_jacobian_3d           src/mesh_BEM/utils/integrations_3d.py:18-249
  *   - double_integration_on_panels_3d     src/mesh_BEM/utils/integrations_3d.py:252-452
  *     with G_3d / grad_G_y_3d / shape_function  src/utils/BEM_utils.py:72-104,141-207
@@ -465,4 +467,51 @@ void ORC(panel_relation)(const int32_t* faces, int64_t nf, uint8_t* rel) {
                 for (int b = 0; b < 3; ++b) cnt += faces[3 * i + a] == faces[3 * j + b];
             rel[i * nf + j] = (uint8_t)(cnt <= 3 ? cnt : 0);
         }
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Scattered magnetic field radiated from vertex currents                               */
+/* (demo/demo_Helmholtz_MOM_3d.py:246-257 with gradG_y / G, src/utils/functions.py:807-868):*/
+/*   H(p) = -sum_v A_v ( J_v x (-gradG_y(k, p, v)) ),                                    */
+/*   gradG_y = G(+k) / R * (1 + jkR) * (p - v)/R,  G(+k) = e^{+jkR} / (4 pi R),           */
+/* with the reference's mask: a vertex closer than 1e-6 contributes nothing.             */
+/* js: [V, 3] split real/imag; h: [P, 3] split real/imag (overwritten).                  */
+/* ------------------------------------------------------------------------------------ */
+void ORC(radiate_h)(const REAL* points, int64_t np, const REAL* verts, const REAL* vert_areas,
+                    const REAL* jr, const REAL* ji, int64_t nv, double wavenumber, REAL* hr,
+                    REAL* hi) {
+    const REAL k = (REAL)wavenumber;
+#pragma omp parallel for schedule(static)
+    for (int64_t m = 0; m < np; ++m) {
+        REAL ar[3] = {0, 0, 0}, ai[3] = {0, 0, 0};
+        for (int64_t v = 0; v < nv; ++v) {
+            REAL d[3];
+            for (int a = 0; a < 3; ++a) d[a] = points[3 * m + a] - verts[3 * v + a];
+            REAL dist = R_SQRT((d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
+            if (dist < (REAL)1e-6) continue;
+            REAL inv = (REAL)1 / dist;
+            REAL kr = k * dist;
+            REAL gr = (REAL)(R_COS(kr) / (4 * ORC_PI)) * inv;
+            REAL gi = (REAL)(R_SIN(kr) / (4 * ORC_PI)) * inv;
+            /* G * inv * (1 + j k R) */
+            REAL fr = (gr - gi * kr) * inv, fi = (gi + gr * kr) * inv;
+            REAL rd[3] = {d[0] * inv, d[1] * inv, d[2] * inv};
+            REAL Jr[3], Ji[3];
+            for (int a = 0; a < 3; ++a) {
+                Jr[a] = jr[3 * v + a];
+                Ji[a] = ji[3 * v + a];
+            }
+            REAL cr[3], ci[3];
+            ORC(cross3)(Jr, rd, cr);
+            ORC(cross3)(Ji, rd, ci);
+            for (int a = 0; a < 3; ++a) {
+                ar[a] += vert_areas[v] * (fr * cr[a] - fi * ci[a]);
+                ai[a] += vert_areas[v] * (fr * ci[a] + fi * cr[a]);
+            }
+        }
+        for (int a = 0; a < 3; ++a) {
+            hr[3 * m + a] = ar[a];
+            hi[3 * m + a] = ai[a];
+        }
+    }
 }

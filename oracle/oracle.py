@@ -40,6 +40,7 @@ def _load():
             getattr(lib, f"orc_laplace_panels_{sfx}").argtypes = [
                 _P, _P, _I64, _P, _P, _P, _P, _I, _P, _I, _I, _I, _D, _I64, _I64, _P, _P]
             getattr(lib, f"orc_panel_relation_{sfx}").argtypes = [_P, _I64, _P]
+            getattr(lib, f"orc_radiate_h_{sfx}").argtypes = [_P, _I64, _P, _P, _P, _P, _I64, _D, _P, _P]
         _lib = lib
     return _lib
 
@@ -149,6 +150,20 @@ def laplace_panels(verts, faces, areas, normals, rands, weights, rel, layer, ord
         _ptr(v), _ptr(f), nf, _ptr(a), _ptr(n), _ptr(rd), _ptr(w), w.size, _ptr(rel),
         int(layer), int(order), int(kind), float(k), r0, r1, _ptr(out_r), _ptr(out_i))
     return out_r if kind == 0 else out_r + 1j * out_i
+
+
+def radiate_h(points, verts, vert_areas, vert_js, k, dtype=np.float64):
+    """Scattered H [P, 3] complex at points from vertex currents vert_js [V, 3] complex."""
+    lib = _load()
+    p, v = _c(points, dtype), _c(verts, dtype)
+    a = _c(np.reshape(vert_areas, -1), dtype)
+    js = np.asarray(vert_js).reshape(-1, 3)
+    jr, ji = _c(js.real, dtype), _c(js.imag, dtype)
+    hr = np.zeros((p.shape[0], 3), dtype)
+    hi = np.zeros_like(hr)
+    getattr(lib, f"orc_radiate_h_{_sfx(dtype)}")(_ptr(p), p.shape[0], _ptr(v), _ptr(a), _ptr(jr), _ptr(ji),
+                                                 v.shape[0], float(k), _ptr(hr), _ptr(hi))
+    return hr + 1j * hi
 
 
 # ---- reference kernels compiled for the host (pinning only) ----------------------------

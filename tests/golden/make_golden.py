@@ -227,6 +227,23 @@ def main():
             rec[f"{tag}_face_vert_js"] = captured["interp"].numpy()
             rec[f"{tag}_vert_js"] = js.numpy()
 
+        # ---- scattered H radiated from the solved vertex currents (demo_Helmholtz_MOM_3d.py:246-257)
+        F = importlib.import_module("src.utils.functions")
+        g1 = np.linspace(-2.0, 2.0, 9)
+        gx, gz = np.meshgrid(g1, g1, indexing="ij")
+        pts = np.stack([gx.ravel(), np.zeros(gx.size), gz.ravel()], -1)
+        pts = np.concatenate([pts, vn[0:1], vn[1:2] + np.array([[4e-7, 0.0, 0.0]]),
+                              1.5 * vn[2:3]], 0)
+        pm = torch.from_numpy(pts).reshape(-1, 1, 3)
+        ejs = torch.from_numpy(rec["mom_gq4_vert_js"][0])
+        va = torch.from_numpy(rec["vert_areas"])
+        kk = float(rec["mom_gq4_k"])
+        nm = pm.shape[0]
+        h_sc = -(va * torch.cross(ejs[None].repeat(nm, 1, 1),
+                                  -F.gradG_y(wavenumber=kk, p1=pm, p2=verts), dim=-1))
+        rec["field_points"] = pts
+        rec["field_H"] = h_sc.sum(dim=-2).numpy()
+
         # ---- Laplace all-Dirichlet (demo_Laplace_3d.py), P1 and P0, gaussQR = 2 and 3 ----
         vb = verts.unsqueeze(0)
         f_val = (vb[..., 0] * vb[..., 0] - vb[..., 1] * vb[..., 1]).unsqueeze(-1)

@@ -258,3 +258,31 @@ def test_empty_mesh_is_noop(pkg, cuda):
     p, w = pkg.utils.get_gaussion_integration_points_and_weights(2, device=cuda)
     zr = torch.zeros((1, 0, 0), device=cuda)
     pkg.mesh_MOM_3d.create_MOM_Zmat_3d_forward(v, f, a, n, p, w, p, w, zr, zr.clone(), 1.0)
+
+
+@pytest.mark.parametrize("name", ["ico0", "ico1", "ell1"])
+def test_radiate_H_f64_matches_reference(pkg, cuda, golden, name):
+    g = golden[name]
+    v = torch.tensor(g["verts"], device=cuda)
+    H = pkg.mesh_MOM_3d.radiate_H(torch.tensor(g["field_points"], device=cuda), v,
+                                  torch.tensor(g["vert_areas"], device=cuda),
+                                  torch.tensor(g["mom_gq4_vert_js"][0], device=cuda), float(g["mom_gq4_k"]))
+    assert rel_err(H.cpu().numpy(), g["field_H"]) < TOL64
+
+
+def test_radiate_H_f32_large_vs_oracle(pkg, cuda, oracle):
+    """A 64 x 64 observation grid around the 2562-vertex sphere, float32 against float64."""
+    v_np, f_np = pkg.meshes.icosphere(4)
+    rng = np.random.default_rng(0)
+    js = rng.normal(size=(v_np.shape[0], 3)) + 1j * rng.normal(size=(v_np.shape[0], 3))
+    va = rng.uniform(0.5, 1.5, size=v_np.shape[0]) * 1e-3
+    g1 = np.linspace(-3, 3, 64)
+    gx, gz = np.meshgrid(g1, g1, indexing="ij")
+    pts = np.stack([gx.ravel(), 0.05 * np.ones(gx.size), gz.ravel()], -1)
+    H = pkg.mesh_MOM_3d.radiate_H(torch.tensor(pts, dtype=torch.float32, device=cuda),
+                                  torch.tensor(v_np, dtype=torch.float32, device=cuda),
+                                  torch.tensor(va, dtype=torch.float32, device=cuda),
+                                  torch.tensor(js, dtype=torch.complex64, device=cuda), 10.0)
+    f32 = lambda a: a.astype(np.float32).astype(np.float64)  # noqa: E731
+    ref = oracle.radiate_h(f32(pts), f32(v_np), f32(va), f32(js.real) + 1j * f32(js.imag), 10.0)
+    assert rel_err(H.cpu().numpy(), ref) < TOL32

@@ -101,3 +101,14 @@ def test_oracle_reference_build_bit_exact_where_available(oracle, golden, gauss_
     args = (g["verts"], g["faces"], g["face_areas"], g["face_normals"], gauss_golden["p4"],
             gauss_golden["w4"], gauss_golden["p3"], gauss_golden["w3"], 2.0)
     assert np.array_equal(oracle.mom_zmat_fe(*args), oracle.ref_zmat_fe(*args))
+
+
+@pytest.mark.parametrize("name", ["ico0", "ico1", "ell1"])
+def test_oracle_radiated_field_matches_reference(oracle, golden, name):
+    """Scattered H of the reference's post-solve step (its gradG_y helper, 1e-6 mask)."""
+    g = golden[name]
+    h = oracle.radiate_h(g["field_points"], g["verts"], g["vert_areas"], g["mom_gq4_vert_js"][0],
+                         float(g["mom_gq4_k"]))
+    assert rel_err(h, g["field_H"]) < 1e-12
+    # the two points on / within 1e-6 of a vertex skip that vertex, as the reference does
+    assert np.isfinite(h).all()
