@@ -36,10 +36,12 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 WORKLOADS = {
-    # name: (icosphere level, k, gaussQR)
+    # name: (icosphere level, k, gaussQR of the reference rule, or 0 for the 7-point EFIE)
     "mom_ref_L5": (5, 10.0, 4),
     "mom_ref_L4": (4, 6.0, 4),
     "mom_ref_L3": (3, 2.0, 4),
+    "mom_sym_L5": (5, 10.0, 0),
+    "mom_sym_L4": (4, 6.0, 0),
 }
 
 
@@ -193,14 +195,24 @@ def main():
     n_faces = 20 * 4 ** level
     n_edges = 30 * 4 ** level
     pairs = float(n_faces) ** 2
+    sym = gq == 0
     config = {"workload": args.workload, "mesh": f"icosphere L{level}", "n_faces": n_faces,
-              "n_edges": n_edges, "ka": k, "rule": f"reference collapsed Gauss-Legendre gaussQR={gq} "
-              f"({gq * gq} test x {(gq - 1) ** 2} source points, rotated per local edge)",
-              "formulation": "EFIE+MFIE (reference CFIE)", "output": "RWG Z [E,E] complex64",
+              "n_edges": n_edges, "ka": k,
+              "rule": ("7-point degree-5 rule on both triangles; pairs sharing a vertex in FP64 with "
+                       "closed-form 1/R integrals" if sym else
+                       f"reference collapsed Gauss-Legendre gaussQR={gq} ({gq * gq} test x "
+                       f"{(gq - 1) ** 2} source points, rotated per local edge)"),
+              "formulation": "EFIE" if sym else "EFIE+MFIE (reference CFIE)",
+              "output": "RWG Z [E,E] complex64",
               "l2": "Z (7.55 GB at L5) > L2, rewritten every step", "parallelism": "replicas"}
 
     if args.impl == "reference":
         if rank != 0:
+            return
+        if sym:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no symmetric-rule "
+                              "EFIE with singularity extraction (new capability); its own algorithm is "
+                              "timed by the mom_ref_* workloads"}), flush=True)
             return
         vals, info = cpu_sample_run(args.workload, args.cpu_seconds, steps=args.steps,
                                     warmup=min(args.warmup, 1))
@@ -232,16 +244,25 @@ def main():
     edges, fei, _ = pkg.utils.get_edge_unique(verts, faces)
     areas = pkg.utils.compute_face_areas(verts, faces).contiguous()
     normals = pkg.utils.compute_face_normals(verts, faces).contiguous()
-    px, wx = pkg.utils.get_gaussion_integration_points_and_weights(gq, device=dev)
-    py, wy = pkg.utils.get_gaussion_integration_points_and_weights(gq - 1, device=dev)
+    if not sym:
+        px, wx = pkg.utils.get_gaussion_integration_points_and_weights(gq, device=dev)
+        py, wy = pkg.utils.get_gaussion_integration_points_and_weights(gq - 1, device=dev)
     Z = torch.zeros((n_edges, n_edges), dtype=torch.complex64, device=dev)
     stream = torch.cuda.current_stream(dev)
     M = pkg.mesh_MOM_3d
+    pairs = M.near_pairs(faces) if sym else None
+    n_near = int(pairs.shape[0]) if sym else 0
+
+    def assemble(out):
+        if sym:
+            M.assemble_Z_rwg_sym(verts, faces, fei, n_edges, k, out=out, pairs=pairs, check_indices=False)
+        else:
+            M.assemble_Z_rwg(verts, faces, areas, normals, fei, n_edges, px, wx, py, wy, k, out=out,
+                             check_indices=False)
 
     def step():
         Z.zero_()
-        M.assemble_Z_rwg(verts, faces, areas, normals, fei, n_edges, px, wx, py, wy, k, out=Z,
-                         check_indices=False)
+        assemble(Z)
 
     def barrier():
         if world > 1:
@@ -262,8 +283,7 @@ def main():
         e0.record(stream)
         Z.zero_()
         e1.record(stream)
-        M.assemble_Z_rwg(verts, faces, areas, normals, fei, n_edges, px, wx, py, wy, k, out=Z,
-                         check_indices=False)
+        assemble(Z)
         e2.record(stream)
     barrier()
     clocks.stop()
@@ -279,9 +299,18 @@ def main():
     kern_avg_s = statistics.mean(kern_ms) / 1e3
 
     # roofline of the dominant kernel (assembly), per launch
-    evals = pairs * R.ref_rule_evals_per_pair(gq)
-    flop = evals * R.CFIE_FLOP_PER_EVAL
-    mufu = evals * R.CFIE_MUFU_PER_EVAL
+    if sym:
+        evals = (pairs - n_near) * 49.0  # separated pairs in the FP32 kernel (near pairs: FP64)
+        flop = evals * R.EFIE_FLOP_PER_EVAL
+        mufu = evals * R.EFIE_MUFU_PER_EVAL
+        per_eval = f"{R.EFIE_FLOP_PER_EVAL} FLOP + {R.EFIE_MUFU_PER_EVAL} MUFU per evaluation x 49 " \
+                   f"evaluations per separated pair x (F^2 - {n_near} near pairs); kernel time = both kernels"
+    else:
+        evals = pairs * R.ref_rule_evals_per_pair(gq)
+        flop = evals * R.CFIE_FLOP_PER_EVAL
+        mufu = evals * R.CFIE_MUFU_PER_EVAL
+        per_eval = f"{R.CFIE_FLOP_PER_EVAL} FLOP + {R.CFIE_MUFU_PER_EVAL} MUFU per evaluation x " \
+                   f"{R.ref_rule_evals_per_pair(gq)} evaluations per pair x F^2 pairs"
     peaks = R.measured_peaks(REPO)
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
     fp32_peak = R.fp32_peak_tflops(sm_max)
@@ -298,23 +327,26 @@ def main():
                            "MEASURED_PEAKS.json; the file has no FP32-SIMT figure)",
             "mufu": {"achieved_gops": mufu / kern_avg_s / 1e9, "peak_gops": mufu_peak,
                      "frac": mufu / kern_avg_s / 1e9 / mufu_peak},
-            "algorithmic": f"{R.CFIE_FLOP_PER_EVAL} FLOP + {R.CFIE_MUFU_PER_EVAL} MUFU per evaluation x "
-                           f"{R.ref_rule_evals_per_pair(gq)} evaluations per pair x F^2 pairs",
+            "algorithmic": per_eval,
             "kernel_ms": kern_avg_s * 1e3}
 
     line = {"metric": "Z-assembly triangle pairs/s", "value": value, "unit": "pairs/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": config, "roofline": roof, "clocks": clocks.summary(),
-            "gpu_launches": args.steps}
+            "gpu_launches": args.steps * (2 if sym else 1)}
 
     # time to solution (reported beside the headline): excitation + GMRES on the assembled Z
     if not args.no_solve:
         pw = pkg.mesh_MOM_3d.plane_waves(k, [[0.0, 0.0, 1.0]], [[1.0, 0.0, 0.0]], device=dev)
-        gp, gw = pkg.utils.get_gaussion_integration_points_and_weights(gq, device=dev)
+        if not sym:
+            gp, gw = pkg.utils.get_gaussion_integration_points_and_weights(gq, device=dev)
         s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s0.record(stream)
-        rhs = M.assemble_rhs_rwg(verts, faces, areas, normals, fei, n_edges, gp, gw, pw)
+        if sym:
+            rhs = M.assemble_rhs_rwg_sym(verts, faces, fei, n_edges, pw)
+        else:
+            rhs = M.assemble_rhs_rwg(verts, faces, areas, normals, fei, n_edges, gp, gw, pw)
         x, infos = M.gmres(Z, rhs[:, 0], restart=50, tol=1e-6, max_iters=3000)
         s1.record(stream)
         torch.cuda.synchronize(dev)
@@ -331,12 +363,12 @@ def main():
         h_verts = torch.tensor(v_np, dtype=torch.float32).pin_memory()
         h_faces = torch.tensor(f_np, dtype=torch.int32).pin_memory()
         h_fei = fei.cpu().pin_memory()
-        h_rules = [t.cpu().pin_memory() for t in (px, wx, py, wy)]
+        h_rules = [] if sym else [t.cpu().pin_memory() for t in (px, wx, py, wy)]
         h_Z = torch.empty((n_edges, n_edges), dtype=torch.complex64, pin_memory=True)
         d_verts = torch.empty_like(verts)
         d_faces = torch.empty_like(faces)
         d_fei = torch.empty_like(fei)
-        d_rules = [torch.empty_like(t) for t in (px, wx, py, wy)]
+        d_rules = [torch.empty_like(t, device=dev) for t in h_rules]
 
         def e2e_step():
             d_verts.copy_(h_verts, non_blocking=True)
@@ -347,8 +379,12 @@ def main():
             a = pkg.utils.compute_face_areas(d_verts, d_faces).contiguous()
             nn = pkg.utils.compute_face_normals(d_verts, d_faces).contiguous()
             Z.zero_()
-            M.assemble_Z_rwg(d_verts, d_faces, a, nn, d_fei, n_edges, *d_rules, k, out=Z,
-                             check_indices=False)
+            if sym:
+                M.assemble_Z_rwg_sym(d_verts, d_faces, d_fei, n_edges, k, out=Z, pairs=pairs,
+                                     check_indices=False)
+            else:
+                M.assemble_Z_rwg(d_verts, d_faces, a, nn, d_fei, n_edges, *d_rules, k, out=Z,
+                                 check_indices=False)
             h_Z.copy_(Z, non_blocking=True)
 
         e2e_step()
@@ -367,13 +403,20 @@ def main():
         line["e2e"] = {"value": world * pairs / (e2e_ms / 1e3), "unit": "pairs/s",
                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h_Z.numel() * 8,
                        "ms_per_step": e2e_ms, "steps": e2e_steps,
-                       "path": "mesh_MOM_3d.assemble_Z_rwg (C ABI mb_mom_zmat_rwg_c64), pinned host "
-                               "buffers, H2D inputs + Z D2H inside the timed region"}
+                       "path": ("mesh_MOM_3d.assemble_Z_rwg_sym (C ABI mb_mom_sym_zmat_rwg_c64 + "
+                                "mb_mom_sym_near_c64)" if sym else
+                                "mesh_MOM_3d.assemble_Z_rwg (C ABI mb_mom_zmat_rwg_c64)")
+                               + ", pinned host buffers, H2D inputs + Z D2H inside the timed region"}
         del h_Z
 
     if rank == 0 and not args.no_cpu_baseline:
-        vals, info = cpu_sample_run(args.workload, args.cpu_seconds, steps=1)
-        line["cpu_baseline"] = {"value": vals[0], "unit": "pairs/s", **info}
+        wl = args.workload if not sym else args.workload.replace("sym", "ref")
+        if wl in WORKLOADS:
+            vals, info = cpu_sample_run(wl, args.cpu_seconds, steps=1)
+            if sym:
+                info["sample"] += " (the reference's own rule on the same mesh: the reference has no " \
+                                  "symmetric-rule path)"
+            line["cpu_baseline"] = {"value": vals[0], "unit": "pairs/s", **info}
     if world > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()

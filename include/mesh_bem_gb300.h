@@ -125,6 +125,42 @@ int mb_mom_interp_vert_c128(const double* verts, int64_t n_verts, const int32_t*
                             const double* face_areas, const double* i_coeff, int64_t n_edges,
                             int64_t batch, double* vert_js, void* stream);
 
+/* ---- EFIE with a symmetric rule and singularity extraction (new capability) ---------- */
+
+/* No single reference counterpart: the reference's only rule is the per-edge collapsed
+ * Gauss rule above.  These build the EFIE part of the reference's operator (its terms
+ * jk G f_m.f_n - (j/k) G div f_m div f_n, mesh_MOM_3d.cu:474-480, RWG convention :154-242)
+ * with the 7-point degree-5 rule on both triangles.
+ * mb_mom_sym_zmat_rwg_*: every pair (test face in [face_begin, face_end), any source face)
+ *   that shares no vertex, in the working precision, accumulated (+=) into z
+ *   (interleaved complex [n_edges, n_edges]).
+ * mb_mom_sym_near_*: the pairs listed in `pairs` ([n_pairs, 2] int32 (test, source); give
+ *   every pair that shares a vertex, including each face with itself), in FP64 with the
+ *   1/R part integrated in closed form, accumulated (+=) into z.
+ * mb_mom_sym_rhs_rwg_*: EFIE excitation of n_rhs plane waves (records as for
+ *   mb_mom_rhs_rwg_*), accumulated (+=) into rhs [n_edges, n_rhs]. */
+int mb_mom_sym_zmat_rwg_c64(const float* verts, int64_t n_verts, const int32_t* faces,
+                            int64_t n_faces, const int32_t* face_edge_indices, int64_t n_edges,
+                            double wavenumber, int64_t face_begin, int64_t face_end, float* z,
+                            void* stream);
+int mb_mom_sym_zmat_rwg_c128(const double* verts, int64_t n_verts, const int32_t* faces,
+                             int64_t n_faces, const int32_t* face_edge_indices, int64_t n_edges,
+                             double wavenumber, int64_t face_begin, int64_t face_end, double* z,
+                             void* stream);
+int mb_mom_sym_near_c64(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                        const int32_t* face_edge_indices, int64_t n_edges, const int32_t* pairs,
+                        int64_t n_pairs, double wavenumber, float* z, void* stream);
+int mb_mom_sym_near_c128(const double* verts, int64_t n_verts, const int32_t* faces,
+                         int64_t n_faces, const int32_t* face_edge_indices, int64_t n_edges,
+                         const int32_t* pairs, int64_t n_pairs, double wavenumber, double* z,
+                         void* stream);
+int mb_mom_sym_rhs_rwg_c64(const float* verts, int64_t n_verts, const int32_t* faces,
+                           int64_t n_faces, const int32_t* face_edge_indices, int64_t n_edges,
+                           const double* waves, int n_rhs, float* rhs, void* stream);
+int mb_mom_sym_rhs_rwg_c128(const double* verts, int64_t n_verts, const int32_t* faces,
+                            int64_t n_faces, const int32_t* face_edge_indices, int64_t n_edges,
+                            const double* waves, int n_rhs, double* rhs, void* stream);
+
 /* ---- Radiated field (post-solve) ---------------------------------------------------- */
 
 /* Replaces the scattered-field sum after solve_MOM (demo/demo_Helmholtz_MOM_3d.py:246-257,

@@ -44,6 +44,12 @@ _SIGS = {
     "mb_pack_tight_f32": [_P, _P, _P, _I64, _I64, _I, _P, _P],
     "mb_pack_tight_f64": [_P, _P, _P, _I64, _I64, _I, _P, _P],
     "mb_panel_relation": [_P, _I64, _P, _P],
+    "mb_mom_sym_zmat_rwg_c64": [_P, _I64, _P, _I64, _P, _I64, _D, _I64, _I64, _P, _P],
+    "mb_mom_sym_zmat_rwg_c128": [_P, _I64, _P, _I64, _P, _I64, _D, _I64, _I64, _P, _P],
+    "mb_mom_sym_near_c64": [_P, _I64, _P, _I64, _P, _I64, _P, _I64, _D, _P, _P],
+    "mb_mom_sym_near_c128": [_P, _I64, _P, _I64, _P, _I64, _P, _I64, _D, _P, _P],
+    "mb_mom_sym_rhs_rwg_c64": [_P, _I64, _P, _I64, _P, _I64, _P, _I, _P, _P],
+    "mb_mom_sym_rhs_rwg_c128": [_P, _I64, _P, _I64, _P, _I64, _P, _I, _P, _P],
     "mb_radiate_h_c64": [_P, _I64, _P, _P, _P, _I64, _D, _P, _P],
     "mb_radiate_h_c128": [_P, _I64, _P, _P, _P, _I64, _D, _P, _P],
     "mb_gmres_workspace_bytes": [_I64, _I],

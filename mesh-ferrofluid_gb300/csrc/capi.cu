@@ -49,6 +49,14 @@ int launch_pack_tight(const T*, const T*, const int32_t*, int64_t, int64_t, int,
 int launch_panel_relation(const int32_t*, int64_t, uint8_t*, cudaStream_t);
 size_t gmres_workspace_bytes(int64_t n, int m);
 template <typename T>
+int launch_mom_sym_regular(const T*, const int32_t*, const int32_t*, int64_t, double, int64_t, int64_t, int64_t,
+                           T*, cudaStream_t);
+template <typename T>
+int launch_mom_sym_near(const T*, const int32_t*, const int32_t*, int64_t, const int32_t*, int64_t, double, T*,
+                        cudaStream_t);
+template <typename T>
+int launch_mom_sym_rhs(const T*, const int32_t*, const int32_t*, const double*, int, int64_t, T*, cudaStream_t);
+template <typename T>
 int launch_radiate_h(const T*, int64_t, const T*, const T*, const T*, int64_t, double, T*, cudaStream_t);
 int gmres_c64(const float*, int64_t, const double*, double*, int, int, double, void*, size_t, int64_t*,
               int64_t*, double*, int*, cudaStream_t);
@@ -245,6 +253,41 @@ MB_LAP(f64, double)
 MB_PACK(f32, float)
 MB_PACK(f64, double)
 #undef MB_PACK
+
+#define MB_SYM(SFX, T)                                                                                \
+    int mb_mom_sym_zmat_rwg_##SFX(const T* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,   \
+                                  const int32_t* fei, int64_t n_edges, double wavenumber,               \
+                                  int64_t face_begin, int64_t face_end, T* z, void* stream) {           \
+        (void)n_verts;                                                                                \
+        MB_REQUIRE(n_faces >= 0 && n_edges >= 0, "bad sizes");                                        \
+        if (n_faces == 0) return MB_OK;                                                               \
+        MB_REQUIRE(verts && faces && fei && z, "null pointer argument");                              \
+        MB_REQUIRE(0 <= face_begin && face_begin <= face_end && face_end <= n_faces, "bad face range");  \
+        return launch_mom_sym_regular<T>(verts, faces, fei, n_edges, wavenumber, n_faces, face_begin,    \
+                                         face_end, z, as_stream(stream));                              \
+    }                                                                                                 \
+    int mb_mom_sym_near_##SFX(const T* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,       \
+                              const int32_t* fei, int64_t n_edges, const int32_t* pairs, int64_t n_pairs, \
+                              double wavenumber, T* z, void* stream) {                                \
+        (void)n_verts; (void)n_faces;                                                                 \
+        MB_REQUIRE(n_pairs >= 0 && n_edges >= 0, "bad sizes");                                        \
+        if (n_pairs == 0) return MB_OK;                                                               \
+        MB_REQUIRE(verts && faces && fei && pairs && z, "null pointer argument");                     \
+        return launch_mom_sym_near<T>(verts, faces, fei, n_edges, pairs, n_pairs, wavenumber, z,       \
+                                      as_stream(stream));                                             \
+    }                                                                                                 \
+    int mb_mom_sym_rhs_rwg_##SFX(const T* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,    \
+                                 const int32_t* fei, int64_t n_edges, const double* waves, int n_rhs,   \
+                                 T* rhs, void* stream) {                                              \
+        (void)n_verts; (void)n_edges;                                                                 \
+        MB_REQUIRE(n_faces >= 0 && n_rhs >= 1, "bad sizes");                                          \
+        if (n_faces == 0) return MB_OK;                                                               \
+        MB_REQUIRE(verts && faces && fei && waves && rhs, "null pointer argument");                   \
+        return launch_mom_sym_rhs<T>(verts, faces, fei, waves, n_rhs, n_faces, rhs, as_stream(stream)); \
+    }
+MB_SYM(c64, float)
+MB_SYM(c128, double)
+#undef MB_SYM
 
 #define MB_RAD(SFX, T)                                                                                \
     int mb_radiate_h_##SFX(const T* points, int64_t n_points, const T* verts, const T* vert_areas,       \

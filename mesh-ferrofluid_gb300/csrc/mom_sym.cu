@@ -1,0 +1,350 @@
+// mom_sym.cu -- EFIE with a symmetric triangle rule and analytic singularity extraction.
+//
+// A capability the reference does not have (its rule, mom_ref.cu, rotates with each local
+// edge and has no singular treatment).  Both triangles use the 7-point degree-5 rule
+// (Radon 1948; Dunavant 1985), whose points do not depend on the local edge, so one set
+// of 49 kernel evaluations serves all nine RWG entries of a triangle pair:
+//   Z_mn += c_m c_n [ jk (Txy - B_n.Tx - A_m.Ty + (A_m.B_n) T0) - (4j/k) T0 ]
+// with the pair moments T0 = sum_i W_i S0_i, Tx = sum_i W_i x_i S0_i, Ty = sum_i W_i S1_i,
+// Txy = sum_i W_i x_i.S1_i and S0_i = sum_j w_j G(x_i, y_j), S1_i = sum_j w_j G y_j.  The
+// integrand terms are the reference's EFIE terms jk G f_m.f_n - (j/k) G div f_m div f_n
+// (mesh_MOM_3d.cu:474-480) with its RWG convention (:154-242).
+//
+// Pairs that share a vertex (self, edge- and vertex-adjacent; ~13 per face) are skipped by
+// the FP32 kernel and computed by an FP64 kernel that splits G = 1/(4 pi R) +
+// (e^{-jkR} - 1)/(4 pi R): the smooth part with the source rule, the singular part with the
+// closed-form potential integrals of D. R. Wilton, S. M. Rao, A. W. Glisson,
+// D. H. Schaubert, O. M. Al-Bundak, C. M. Butler, IEEE Trans. AP-32(3):276-281, 1984:
+//   int_T 1/R   = sum_i P0_i ln((R+_i + l+_i)/(R-_i + l-_i)) - |d| sum_i (beta+_i - beta-_i)
+//   int_T (y-x)/R = 1/2 sum_i u_i [ R0_i^2 ln(...) + l+_i R+_i - l-_i R-_i ] - d n int_T 1/R.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace mb {
+
+// 7-point rule: barycentric coordinates and weights (sum 1), from the closed forms
+// a = (6 -+ sqrt 15)/21, w = (155 -+ sqrt 15)/1200, centroid weight 9/40.
+__constant__ double c_d7[7][4] = {
+    {0.33333333333333333, 0.33333333333333333, 0.33333333333333333, 0.225},
+    {0.10128650732345634, 0.10128650732345634, 0.79742698535308732, 0.12593918054482715},
+    {0.10128650732345634, 0.79742698535308732, 0.10128650732345634, 0.12593918054482715},
+    {0.79742698535308732, 0.10128650732345634, 0.10128650732345634, 0.12593918054482715},
+    {0.47014206410511509, 0.47014206410511509, 0.05971587178976982, 0.13239415278850619},
+    {0.47014206410511509, 0.05971587178976982, 0.47014206410511509, 0.13239415278850619},
+    {0.05971587178976982, 0.47014206410511509, 0.47014206410511509, 0.13239415278850619},
+};
+
+template <typename T>
+__device__ __forceinline__ void add_c(T* p, T re, T im);
+template <>
+__device__ __forceinline__ void add_c<float>(float* p, float re, float im) {
+    atomicAdd(reinterpret_cast<float2*>(p), make_float2(re, im));
+}
+template <>
+__device__ __forceinline__ void add_c<double>(double* p, double re, double im) {
+    atomicAdd(p, re);
+    atomicAdd(p + 1, im);
+}
+
+__device__ __forceinline__ int shared_vertices(const int32_t* f, int64_t p, int64_t q) {
+    const int32_t a0 = __ldg(f + 3 * p), a1 = __ldg(f + 3 * p + 1), a2 = __ldg(f + 3 * p + 2);
+    const int32_t b0 = __ldg(f + 3 * q), b1 = __ldg(f + 3 * q + 1), b2 = __ldg(f + 3 * q + 2);
+    return (a0 == b0) + (a0 == b1) + (a0 == b2) + (a1 == b0) + (a1 == b1) + (a1 == b2) + (a2 == b0) +
+           (a2 == b1) + (a2 == b2);
+}
+
+template <typename T>
+__device__ __forceinline__ void rwg_consts(const int32_t* f, int64_t p, const V3<T> P[3], T c[3], T* area) {
+    const V3<T> e0 = P[1] - P[0], e1 = P[2] - P[1];
+    const V3<T> cr = cross(e0, e1);
+    *area = T(0.5) * sqrt_t(dot(cr, cr));
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const int32_t i1 = __ldg(f + 3 * p + (e + 1) % 3), i2 = __ldg(f + 3 * p + (e + 2) % 3);
+        const V3<T> d = P[(e + 2) % 3] - P[(e + 1) % 3];
+        c[e] = (i1 < i2 ? T(1) : T(-1)) * sqrt_t(dot(d, d)) / (T(2) * *area);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// separated pairs (no shared vertex): one thread per (test p, source q), 128 q per block
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128) mom_sym_regular_kernel(const T* __restrict__ verts,
+                                                              const int32_t* __restrict__ faces,
+                                                              const int32_t* __restrict__ fei, int64_t n_edges,
+                                                              T k, int64_t nf, int64_t p_begin, int64_t q_blocks,
+                                                              T* __restrict__ z) {
+    __shared__ T s_b[7][4];
+    if (threadIdx.x < 28) s_b[threadIdx.x / 4][threadIdx.x % 4] = (T)c_d7[threadIdx.x / 4][threadIdx.x % 4];
+    __syncthreads();
+    const int64_t p = p_begin + (int64_t)blockIdx.x / q_blocks;
+    const int64_t q = ((int64_t)blockIdx.x % q_blocks) * 128 + threadIdx.x;
+    if (q >= nf) return;
+    if (shared_vertices(faces, p, q) != 0) return;  // done by the FP64 near-pair kernel
+    const V3<T> o = load3(verts, __ldg(faces + 3 * q));
+    V3<T> A[3], B[3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+        A[v] = load3(verts, __ldg(faces + 3 * p + v)) - o;
+        B[v] = load3(verts, __ldg(faces + 3 * q + v)) - o;
+    }
+    T cm[3], cn[3], ap, aq;
+    rwg_consts<T>(faces, p, A, cm, &ap);
+    rwg_consts<T>(faces, q, B, cn, &aq);
+    V3<T> y[7];
+    T wy[7];
+#pragma unroll
+    for (int j = 0; j < 7; ++j) {
+        y[j] = s_b[j][0] * B[0] + s_b[j][1] * B[1] + s_b[j][2] * B[2];
+        wy[j] = s_b[j][3] * aq * T(kInv4Pi);
+    }
+    const T k_turn = k * T(kInv2Pi);
+    T t0r = 0, t0i = 0, txr[3] = {0, 0, 0}, txi[3] = {0, 0, 0}, tyr[3] = {0, 0, 0}, tyi[3] = {0, 0, 0};
+    T txyr = 0, txyi = 0;
+#pragma unroll 1
+    for (int i = 0; i < 7; ++i) {
+        const V3<T> x = s_b[i][0] * A[0] + s_b[i][1] * A[1] + s_b[i][2] * A[2];
+        const T wi = s_b[i][3] * ap;
+        T s0r = 0, s0i = 0, s1r[3] = {0, 0, 0}, s1i[3] = {0, 0, 0};
+#pragma unroll
+        for (int j = 0; j < 7; ++j) {
+            const V3<T> d = x - y[j];
+            const T r2 = dot(d, d);
+            const T rinv = rsqrt_t(r2);
+            T sn, cs;
+            sincos_turns(k_turn * (r2 * rinv), &sn, &cs);
+            const T g = wy[j] * rinv;
+            const T gr = g * cs, gi = -g * sn;
+            s0r += gr;
+            s0i += gi;
+            s1r[0] += gr * y[j].x; s1i[0] += gi * y[j].x;
+            s1r[1] += gr * y[j].y; s1i[1] += gi * y[j].y;
+            s1r[2] += gr * y[j].z; s1i[2] += gi * y[j].z;
+        }
+        t0r += wi * s0r;
+        t0i += wi * s0i;
+        const T xs[3] = {x.x, x.y, x.z};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            txr[a] += wi * xs[a] * s0r;
+            txi[a] += wi * xs[a] * s0i;
+            tyr[a] += wi * s1r[a];
+            tyi[a] += wi * s1i[a];
+        }
+        txyr += wi * (xs[0] * s1r[0] + xs[1] * s1r[1] + xs[2] * s1r[2]);
+        txyi += wi * (xs[0] * s1i[0] + xs[1] * s1i[1] + xs[2] * s1i[2]);
+    }
+    const V3<T> Txr = v3<T>(txr[0], txr[1], txr[2]), Txi = v3<T>(txi[0], txi[1], txi[2]);
+    const V3<T> Tyr = v3<T>(tyr[0], tyr[1], tyr[2]), Tyi = v3<T>(tyi[0], tyi[1], tyi[2]);
+    const T inv_k4 = T(4) / k;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        const T amr = dot(A[m], Tyr), ami = dot(A[m], Tyi);
+        const int64_t row = __ldg(fei + 3 * p + m);
+#pragma unroll
+        for (int n = 0; n < 3; ++n) {
+            const T ab = dot(A[m], B[n]);
+            const T fr = txyr - dot(B[n], Txr) - amr + ab * t0r;  // int int (x-A_m).(y-B_n) G
+            const T fi = txyi - dot(B[n], Txi) - ami + ab * t0i;
+            const T cc = cm[m] * cn[n];
+            // jk cc f - (4j/k) cc T0
+            const T re = cc * (-k * fi + inv_k4 * t0i);
+            const T im = cc * (k * fr - inv_k4 * t0r);
+            add_c<T>(z + 2 * (row * n_edges + __ldg(fei + 3 * q + n)), re, im);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// pairs sharing a vertex: FP64 with the singular part in closed form; one thread per pair
+// ---------------------------------------------------------------------------------------
+__device__ void potential_integrals(const V3<double>& x, const V3<double> P[3], double* I1, V3<double>* Iv) {
+    V3<double> n = cross(P[1] - P[0], P[2] - P[1]);
+    n = (1.0 / sqrt(dot(n, n))) * n;
+    const double d = dot(x - P[0], n);
+    const V3<double> rho = x - d * n;
+    const double ad = fabs(d);
+    double s1 = 0.0;
+    V3<double> sv = v3<double>(0, 0, 0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const V3<double> pm = P[i], pp = P[(i + 1) % 3];
+        V3<double> l = pp - pm;
+        l = (1.0 / sqrt(dot(l, l))) * l;
+        const V3<double> u = cross(l, n);
+        const double lp = dot(pp - rho, l), lm = dot(pm - rho, l);
+        const double p0 = dot(pp - rho, u);
+        const double r0sq = p0 * p0 + d * d;
+        const double rp = sqrt(r0sq + lp * lp), rm = sqrt(r0sq + lm * lm);
+        double lg;
+        if ((lm >= 0.0 || lp >= 0.0) && rm + lm > 0.0)
+            lg = log((rp + lp) / (rm + lm));
+        else
+            lg = log((rm - lm) / (rp - lp));
+        s1 += p0 * lg - ad * (atan2(p0 * lp, r0sq + ad * rp) - atan2(p0 * lm, r0sq + ad * rm));
+        sv = sv + (0.5 * (r0sq * lg + lp * rp - lm * rm)) * u;
+    }
+    *I1 = s1;
+    *Iv = sv - (d * s1) * n;
+}
+
+template <typename T>
+__global__ void mom_sym_near_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                    const int32_t* __restrict__ fei, int64_t n_edges,
+                                    const int32_t* __restrict__ pairs, int64_t n_pairs, double k,
+                                    T* __restrict__ z) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_pairs) return;
+    const int64_t p = pairs[2 * t], q = pairs[2 * t + 1];
+    V3<double> A[3], B[3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+        const int64_t ia = faces[3 * p + v], ib = faces[3 * q + v];
+        A[v] = v3<double>(verts[3 * ia], verts[3 * ia + 1], verts[3 * ia + 2]);
+        B[v] = v3<double>(verts[3 * ib], verts[3 * ib + 1], verts[3 * ib + 2]);
+    }
+    double cm[3], cn[3], ap, aq;
+    rwg_consts<double>(faces, p, A, cm, &ap);
+    rwg_consts<double>(faces, q, B, cn, &aq);
+    const double inv4pi = kInv4Pi;
+    double accr[3][3] = {}, acci[3][3] = {};
+    for (int i = 0; i < 7; ++i) {
+        const V3<double> x = c_d7[i][0] * A[0] + c_d7[i][1] * A[1] + c_d7[i][2] * A[2];
+        double g0r = 0, g0i = 0;
+        V3<double> gyr = v3<double>(0, 0, 0), gyi = v3<double>(0, 0, 0);
+        for (int j = 0; j < 7; ++j) {
+            const V3<double> y = c_d7[j][0] * B[0] + c_d7[j][1] * B[1] + c_d7[j][2] * B[2];
+            const V3<double> dd = x - y;
+            const double R = sqrt(dot(dd, dd));
+            double gr, gi;
+            if (R < 1e-300) {  // coincident points of the self pair: limit of the smooth part
+                gr = 0.0;
+                gi = -k * inv4pi;
+            } else {
+                double sn, cs;
+                sincos(k * R, &sn, &cs);
+                const double sh = sin(0.5 * k * R);
+                gr = -2.0 * sh * sh / R * inv4pi;  // (cos kR - 1) / (4 pi R)
+                gi = -sn / R * inv4pi;
+            }
+            const double wj = c_d7[j][3] * aq;
+            g0r += wj * gr;
+            g0i += wj * gi;
+            gyr = gyr + (wj * gr) * y;
+            gyi = gyi + (wj * gi) * y;
+        }
+        double I1;
+        V3<double> Iv;
+        potential_integrals(x, B, &I1, &Iv);
+        g0r += inv4pi * I1;
+        gyr = gyr + inv4pi * (Iv + I1 * x);
+        const double wi = c_d7[i][3] * ap;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            const V3<double> xm = x - A[m];
+#pragma unroll
+            for (int n = 0; n < 3; ++n) {
+                const double fr = dot(xm, gyr - g0r * B[n]);
+                const double fi = dot(xm, gyi - g0i * B[n]);
+                const double cc = cm[m] * cn[n];
+                accr[m][n] += wi * cc * (-k * fi + 4.0 / k * g0i);
+                acci[m][n] += wi * cc * (k * fr - 4.0 / k * g0r);
+            }
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        const int64_t row = fei[3 * p + m];
+#pragma unroll
+        for (int n = 0; n < 3; ++n)
+            add_c<T>(z + 2 * (row * n_edges + fei[3 * q + n]), (T)accr[m][n], (T)acci[m][n]);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// EFIE excitation with the same rule: rhs[fei, r] += int f_m . E0 e^{-j k khat.x}
+// waves: [n_rhs, 9] float64 (k khat, E0, H0); one thread per (face, wave)
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__global__ void mom_sym_rhs_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                   const int32_t* __restrict__ fei, const double* __restrict__ waves, int nrhs,
+                                   int64_t nf, T* __restrict__ rhs) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nf * nrhs) return;
+    const int r = (int)(t / nf);
+    const int64_t p = t % nf;
+    V3<T> A[3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) A[v] = load3(verts, faces[3 * p + v]);
+    T c[3], area;
+    rwg_consts<T>(faces, p, A, c, &area);
+    const double* w = waves + 9 * r;
+    const V3<T> kv = v3<T>((T)w[0], (T)w[1], (T)w[2]), E0 = v3<T>((T)w[3], (T)w[4], (T)w[5]);
+    T sr[3] = {0, 0, 0}, si[3] = {0, 0, 0};
+    for (int i = 0; i < 7; ++i) {
+        const V3<T> x = (T)c_d7[i][0] * A[0] + (T)c_d7[i][1] * A[1] + (T)c_d7[i][2] * A[2];
+        T sn, cs;
+        sincos_turns(dot(kv, x) * T(kInv2Pi), &sn, &cs);
+        const T wi = (T)c_d7[i][3] * area;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            const T proj = wi * c[m] * dot(x - A[m], E0);
+            sr[m] += proj * cs;
+            si[m] -= proj * sn;
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) add_c<T>(rhs + 2 * ((int64_t)fei[3 * p + m] * nrhs + r), sr[m], si[m]);
+}
+
+// ---------------------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------------------
+template <typename T>
+int launch_mom_sym_regular(const T* verts, const int32_t* faces, const int32_t* fei, int64_t n_edges, double k,
+                           int64_t nf, int64_t p_begin, int64_t p_end, T* z, cudaStream_t s) {
+    if (nf <= 0 || p_end <= p_begin) return MB_OK;
+    if (!(k > 0)) return set_error(MB_ERR_ARG, "wavenumber must be > 0");
+    const int64_t q_blocks = (nf + 127) / 128;
+    const int64_t blocks = (p_end - p_begin) * q_blocks;
+    if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "mesh too large for one launch");
+    mom_sym_regular_kernel<T><<<(unsigned)blocks, 128, 0, s>>>(verts, faces, fei, n_edges, (T)k, nf, p_begin,
+                                                                q_blocks, z);
+    return check_launch("mom_sym_regular");
+}
+
+template <typename T>
+int launch_mom_sym_near(const T* verts, const int32_t* faces, const int32_t* fei, int64_t n_edges,
+                        const int32_t* pairs, int64_t n_pairs, double k, T* z, cudaStream_t s) {
+    if (n_pairs <= 0) return MB_OK;
+    if (!(k > 0)) return set_error(MB_ERR_ARG, "wavenumber must be > 0");
+    const int64_t blocks = (n_pairs + 127) / 128;
+    if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "too many near pairs for one launch");
+    mom_sym_near_kernel<T><<<(unsigned)blocks, 128, 0, s>>>(verts, faces, fei, n_edges, pairs, n_pairs, k, z);
+    return check_launch("mom_sym_near");
+}
+
+template <typename T>
+int launch_mom_sym_rhs(const T* verts, const int32_t* faces, const int32_t* fei, const double* waves, int nrhs,
+                       int64_t nf, T* rhs, cudaStream_t s) {
+    if (nf <= 0 || nrhs <= 0) return MB_OK;
+    const int64_t total = nf * nrhs;
+    mom_sym_rhs_kernel<T><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(verts, faces, fei, waves, nrhs, nf, rhs);
+    return check_launch("mom_sym_rhs");
+}
+
+#define MB_INST(T)                                                                                       \
+    template int launch_mom_sym_regular<T>(const T*, const int32_t*, const int32_t*, int64_t, double, int64_t, \
+                                           int64_t, int64_t, T*, cudaStream_t);                         \
+    template int launch_mom_sym_near<T>(const T*, const int32_t*, const int32_t*, int64_t, const int32_t*,   \
+                                        int64_t, double, T*, cudaStream_t);                             \
+    template int launch_mom_sym_rhs<T>(const T*, const int32_t*, const int32_t*, const double*, int, int64_t, \
+                                       T*, cudaStream_t);
+MB_INST(float)
+MB_INST(double)
+#undef MB_INST
+
+}  // namespace mb

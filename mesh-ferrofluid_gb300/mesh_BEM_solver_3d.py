@@ -17,7 +17,11 @@ Same constructor and public methods as ``src/mesh_BEM/mesh_BEM_solver_3d.py:31-3
 
 Extra keyword ``solver`` selects "lu" (reference behaviour, ``torch.linalg.solve``) or
 "gmres" (``mb_gmres_c64``: FP32 matrix-vector products on the complex64 matrix, FP64
-Arnoldi and refinement residual; float32 meshes only, float64 meshes keep LU).  All tensors must live on a
+Arnoldi and refinement residual; float32 meshes only, float64 meshes keep LU).  Extra
+keyword ``rule`` selects "reference" (the reference's EFIE + MFIE operator and collapsed
+Gauss rule, parity path) or "dunavant7" (EFIE with the 7-point rule on both triangles and
+closed-form singular integrals for pairs sharing a vertex, in FP64; excitation = the
+incident E field only).  All tensors must live on a
 CUDA device: there is no CPU implementation.
 """
 from __future__ import annotations
@@ -29,7 +33,9 @@ import torch
 from .layers import DoubleLayer3d, RhsLayer3d, SingleLayer3d
 from .mesh_MOM_3d import (
     assemble_rhs_rwg,
+    assemble_rhs_rwg_sym,
     assemble_Z_rwg,
+    assemble_Z_rwg_sym,
     gmres,
     interpolate_vert_js,
     reference_plane_wave,
@@ -51,7 +57,7 @@ class MeshBEMSolver3d:
     def __init__(self, gaussQR: int, order_type: int, BEM_type: int, wavenumber: float, logger=None,
                  dtype: torch.dtype = torch.float32, device: torch.device = torch.device("cpu"),
                  solver: str = "lu", gmres_restart: int = 50, gmres_tol: float = 1e-6,
-                 gmres_max_iters: int = 2000):
+                 gmres_max_iters: int = 2000, rule: str = "reference"):
         self._gaussQR = gaussQR
         self._order_type = order_type
         self._BEM_type = BEM_type
@@ -66,6 +72,9 @@ class MeshBEMSolver3d:
         self.gmres_tol = gmres_tol
         self.gmres_max_iters = gmres_max_iters
         self.last_solve_info = None
+        if rule not in ("reference", "dunavant7"):
+            raise ValueError(f"unknown rule {rule!r}")
+        self.rule = rule
         self.hypersingular_layer = None
         kw = dict(gaussQR=gaussQR, order_type=order_type, BEM_type=BEM_type, wavenumber=wavenumber,
                   logger=logger, dtype=dtype, device=self.device)
@@ -99,13 +108,17 @@ class MeshBEMSolver3d:
         faces = faces.to(torch.int32).contiguous()
         fei = face_edge_indices.to(torch.int32).reshape(-1).contiguous()
         dev, dt = verts.device, verts.dtype
-        gpx, gwx, gpy, gwy, gp, gw = self._rules_on(dev, dt)
         areas = compute_face_areas(vertices=verts, faces=faces, keepdim=True).contiguous()
+        if waves is None:
+            waves = reference_plane_wave(self.wavenumber, device=dev)
+        if self.rule == "dunavant7":
+            Z = assemble_Z_rwg_sym(verts, faces, fei, n_edges, self.wavenumber)
+            rhs = assemble_rhs_rwg_sym(verts, faces, fei, n_edges, waves)
+            return Z, rhs, areas
+        gpx, gwx, gpy, gwy, gp, gw = self._rules_on(dev, dt)
         normals = compute_face_normals(vertices=verts, faces=faces).contiguous()
         Z = assemble_Z_rwg(verts, faces, areas, normals, fei, n_edges, gpx, gwx, gpy, gwy,
                            self.wavenumber)
-        if waves is None:
-            waves = reference_plane_wave(self.wavenumber, device=dev)
         rhs = assemble_rhs_rwg(verts, faces, areas, normals, fei, n_edges, gp, gw, waves)
         return Z, rhs, areas
 

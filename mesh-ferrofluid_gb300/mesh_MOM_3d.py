@@ -240,6 +240,74 @@ def interpolate_vert_js(verts, faces, face_edge_indices, face_areas, i_coeff, ou
 
 
 # ---------------------------------------------------------------------------------------
+# EFIE with the symmetric 7-point rule and singularity extraction (new capability)
+# ---------------------------------------------------------------------------------------
+def near_pairs(faces) -> torch.Tensor:
+    """All ordered face pairs sharing at least one vertex (incl. self), [n, 2] int32."""
+    from .utils import compute_panel_relation
+
+    rel = compute_panel_relation(faces)
+    return torch.nonzero(rel > 0).to(torch.int32).contiguous()
+
+
+def assemble_Z_rwg_sym(verts, faces, face_edge_indices, n_edges, wavenumber, out=None, pairs=None,
+                       faces_range=None, check_indices=True):
+    """EFIE RWG matrix [E, E] with the 7-point rule on both triangles.
+
+    Separated pairs run in the mesh dtype; pairs sharing a vertex (``pairs``, default
+    ``near_pairs(faces)``) run in FP64 with the 1/R part integrated in closed form.
+    ``faces_range`` restricts the separated pairs to test faces [begin, end) (the near
+    pairs are then left to the caller).
+    """
+    _lib.check_tensor(verts, "verts", dtype=_FLOATS, ndim=2)
+    dt, dev = verts.dtype, verts.device
+    _lib.check_tensor(faces, "faces", dtype=torch.int32, device=dev, ndim=2)
+    nf = faces.shape[0]
+    check_face_range(faces, verts.shape[0])
+    if check_indices:
+        _check_fei(face_edge_indices, nf, n_edges, dev)
+    cdt = torch.complex64 if dt == torch.float32 else torch.complex128
+    if out is None:
+        out = torch.zeros((n_edges, n_edges), dtype=cdt, device=dev)
+    else:
+        _lib.check_tensor(out, "out", dtype=cdt, device=dev, shape=(n_edges, n_edges))
+    f0, f1 = (0, nf) if faces_range is None else faces_range
+    st = _lib.stream_of(verts)
+    _lib.call(f"mb_mom_sym_zmat_rwg_{_lib.csfx(dt)}", _lib.ptr(verts), verts.shape[0], _lib.ptr(faces), nf,
+              _lib.ptr(face_edge_indices), n_edges, float(wavenumber), int(f0), int(f1), _lib.ptr(out), st)
+    if faces_range is None:
+        if pairs is None:
+            pairs = near_pairs(faces)
+        _lib.check_tensor(pairs, "pairs", dtype=torch.int32, device=dev, ndim=2)
+        _lib.call(f"mb_mom_sym_near_{_lib.csfx(dt)}", _lib.ptr(verts), verts.shape[0], _lib.ptr(faces), nf,
+                  _lib.ptr(face_edge_indices), n_edges, _lib.ptr(pairs), pairs.shape[0], float(wavenumber),
+                  _lib.ptr(out), st)
+    return out
+
+
+def assemble_rhs_rwg_sym(verts, faces, face_edge_indices, n_edges, waves, out=None):
+    """EFIE excitation [E, n_rhs] with the 7-point rule for plane waves [n_rhs, 9] float64."""
+    _lib.check_tensor(verts, "verts", dtype=_FLOATS, ndim=2)
+    dt, dev = verts.dtype, verts.device
+    _lib.check_tensor(faces, "faces", dtype=torch.int32, device=dev, ndim=2)
+    nf = faces.shape[0]
+    check_face_range(faces, verts.shape[0])
+    _check_fei(face_edge_indices, nf, n_edges, dev)
+    waves = waves.to(device=dev, dtype=torch.float64).contiguous()
+    if waves.dim() != 2 or waves.shape[1] != 9:
+        raise ValueError("waves must be [n_rhs, 9]")
+    cdt = torch.complex64 if dt == torch.float32 else torch.complex128
+    if out is None:
+        out = torch.zeros((n_edges, waves.shape[0]), dtype=cdt, device=dev)
+    else:
+        _lib.check_tensor(out, "out", dtype=cdt, device=dev, shape=(n_edges, waves.shape[0]))
+    _lib.call(f"mb_mom_sym_rhs_rwg_{_lib.csfx(dt)}", _lib.ptr(verts), verts.shape[0], _lib.ptr(faces), nf,
+              _lib.ptr(face_edge_indices), n_edges, _lib.ptr(waves), waves.shape[0], _lib.ptr(out),
+              _lib.stream_of(verts))
+    return out
+
+
+# ---------------------------------------------------------------------------------------
 # radiated field after the solve (demo/demo_Helmholtz_MOM_3d.py:246-257)
 # ---------------------------------------------------------------------------------------
 def radiate_H(points, verts, vert_areas, vert_Js, wavenumber, out=None):

@@ -515,3 +515,228 @@ void ORC(radiate_h)(const REAL* points, int64_t np, const REAL* verts, const REA
         }
     }
 }
+
+/* ==================================================================================== */
+/* Symmetric-rule EFIE (a capability the reference does not have; checker for the       */
+/* "dunavant7" GPU path).  7-point degree-5 rule (Radon; Dunavant 1985) on both         */
+/* triangles; pairs that share a vertex (self, edge- and vertex-adjacent) integrate     */
+/* G = 1/(4 pi R) + (e^{-jkR} - 1)/(4 pi R): the smooth part with the source rule, the  */
+/* singular part analytically (Wilton, Rao, Glisson, Schaubert, Al-Bundak, Butler 1984, */
+/* IEEE Trans. AP-32(3):276-281).  Entries follow the reference's EFIE terms             */
+/* jk G f_m . f_n - (j/k) G div f_m div f_n (mesh_MOM_3d.cu:474-480) with its RWG        */
+/* convention (mesh_MOM_3d.cu:154-242).  Everything in double.                          */
+/* ==================================================================================== */
+#ifndef ORC_SYM_DEFINED_ONCE
+#define ORC_SYM_DEFINED_ONCE
+static void orc_d7(double bary[7][3], double w[7]) {
+    const double s15 = sqrt(15.0);
+    const double a1 = (6.0 - s15) / 21.0, b1 = 1.0 - 2.0 * a1, w1 = (155.0 - s15) / 1200.0;
+    const double a2 = (6.0 + s15) / 21.0, b2 = 1.0 - 2.0 * a2, w2 = (155.0 + s15) / 1200.0;
+    const double t[7][4] = {
+        {1.0 / 3, 1.0 / 3, 1.0 / 3, 9.0 / 40},
+        {a1, a1, b1, w1}, {a1, b1, a1, w1}, {b1, a1, a1, w1},
+        {a2, a2, b2, w2}, {a2, b2, a2, w2}, {b2, a2, a2, w2},
+    };
+    for (int i = 0; i < 7; ++i) {
+        bary[i][0] = t[i][0]; bary[i][1] = t[i][1]; bary[i][2] = t[i][2];
+        w[i] = t[i][3];
+    }
+}
+
+/* I1 = int_T 1/|x - y| dS_y and Iv = int_T (y - x)/|x - y| dS_y over triangle P. */
+static void orc_pot_integrals(const double* x, const double P[3][3], double* I1, double Iv[3]) {
+    double e0[3], e1[3], n[3];
+    for (int a = 0; a < 3; ++a) { e0[a] = P[1][a] - P[0][a]; e1[a] = P[2][a] - P[1][a]; }
+    n[0] = e0[1] * e1[2] - e0[2] * e1[1];
+    n[1] = e0[2] * e1[0] - e0[0] * e1[2];
+    n[2] = e0[0] * e1[1] - e0[1] * e1[0];
+    double nn = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (int a = 0; a < 3; ++a) n[a] /= nn;
+    double d = (x[0] - P[0][0]) * n[0] + (x[1] - P[0][1]) * n[1] + (x[2] - P[0][2]) * n[2];
+    double rho[3] = {x[0] - d * n[0], x[1] - d * n[1], x[2] - d * n[2]};
+    double s1 = 0, sv[3] = {0, 0, 0};
+    const double ad = fabs(d);
+    for (int i = 0; i < 3; ++i) {
+        const double* pm = P[i];
+        const double* pp = P[(i + 1) % 3];
+        double l[3] = {pp[0] - pm[0], pp[1] - pm[1], pp[2] - pm[2]};
+        double ll = sqrt(l[0] * l[0] + l[1] * l[1] + l[2] * l[2]);
+        for (int a = 0; a < 3; ++a) l[a] /= ll;
+        double u[3] = {l[1] * n[2] - l[2] * n[1], l[2] * n[0] - l[0] * n[2], l[0] * n[1] - l[1] * n[0]};
+        double lp = (pp[0] - rho[0]) * l[0] + (pp[1] - rho[1]) * l[1] + (pp[2] - rho[2]) * l[2];
+        double lm = (pm[0] - rho[0]) * l[0] + (pm[1] - rho[1]) * l[1] + (pm[2] - rho[2]) * l[2];
+        double p0 = (pp[0] - rho[0]) * u[0] + (pp[1] - rho[1]) * u[1] + (pp[2] - rho[2]) * u[2];
+        double r0sq = p0 * p0 + d * d;
+        double rp = sqrt(r0sq + lp * lp), rm = sqrt(r0sq + lm * lm);
+        double lg;
+        if ((lm >= 0 || lp >= 0) && rm + lm > 0) lg = log((rp + lp) / (rm + lm));
+        else lg = log((rm - lm) / (rp - lp));
+        s1 += p0 * lg - ad * (atan2(p0 * lp, r0sq + ad * rp) - atan2(p0 * lm, r0sq + ad * rm));
+        double t = 0.5 * (r0sq * lg + lp * rp - lm * rm);
+        for (int a = 0; a < 3; ++a) sv[a] += t * u[a];
+    }
+    *I1 = s1;
+    for (int a = 0; a < 3; ++a) Iv[a] = sv[a] - d * n[a] * s1;
+}
+#endif
+
+/*
+ * Z (RWG, [E, E], split real/imag, accumulated) of the EFIE with the symmetric rule.
+ * Test faces [f_begin, f_end) only (row window); all source faces.
+ */
+void ORC(mom_sym_zmat_rwg)(const REAL* verts_r, const int32_t* faces, int64_t nf, const int32_t* fei,
+                           int64_t ne, double k, int64_t f_begin, int64_t f_end, double* zr, double* zi) {
+    double bary[7][3], w7[7];
+    orc_d7(bary, w7);
+    const double inv4pi = 1.0 / (4.0 * ORC_PI);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t p = f_begin; p < f_end; ++p) {
+        double A[3][3];
+        for (int v = 0; v < 3; ++v)
+            for (int a = 0; a < 3; ++a) A[v][a] = (double)verts_r[3 * (int64_t)faces[3 * p + v] + a];
+        double ap[3] = {A[1][0] - A[0][0], A[1][1] - A[0][1], A[1][2] - A[0][2]};
+        double bp[3] = {A[2][0] - A[1][0], A[2][1] - A[1][1], A[2][2] - A[1][2]};
+        double cpr[3] = {ap[1] * bp[2] - ap[2] * bp[1], ap[2] * bp[0] - ap[0] * bp[2], ap[0] * bp[1] - ap[1] * bp[0]};
+        double areap = 0.5 * sqrt(cpr[0] * cpr[0] + cpr[1] * cpr[1] + cpr[2] * cpr[2]);
+        double cm[3];
+        for (int e = 0; e < 3; ++e) {
+            int i1 = faces[3 * p + (e + 1) % 3], i2 = faces[3 * p + (e + 2) % 3];
+            double dl = 0;
+            for (int a = 0; a < 3; ++a) dl += (A[(e + 2) % 3][a] - A[(e + 1) % 3][a]) * (A[(e + 2) % 3][a] - A[(e + 1) % 3][a]);
+            cm[e] = (i1 < i2 ? 1.0 : -1.0) * sqrt(dl) / (2.0 * areap);
+        }
+        double X[7][3];
+        for (int i = 0; i < 7; ++i)
+            for (int a = 0; a < 3; ++a) X[i][a] = bary[i][0] * A[0][a] + bary[i][1] * A[1][a] + bary[i][2] * A[2][a];
+        for (int64_t q = 0; q < nf; ++q) {
+            double B[3][3];
+            for (int v = 0; v < 3; ++v)
+                for (int a = 0; a < 3; ++a) B[v][a] = (double)verts_r[3 * (int64_t)faces[3 * q + v] + a];
+            int shared = 0;
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) shared += faces[3 * p + a] == faces[3 * q + b];
+            double aq[3] = {B[1][0] - B[0][0], B[1][1] - B[0][1], B[1][2] - B[0][2]};
+            double bq[3] = {B[2][0] - B[1][0], B[2][1] - B[1][1], B[2][2] - B[1][2]};
+            double cq[3] = {aq[1] * bq[2] - aq[2] * bq[1], aq[2] * bq[0] - aq[0] * bq[2], aq[0] * bq[1] - aq[1] * bq[0]};
+            double areaq = 0.5 * sqrt(cq[0] * cq[0] + cq[1] * cq[1] + cq[2] * cq[2]);
+            double cn[3];
+            for (int e = 0; e < 3; ++e) {
+                int i1 = faces[3 * q + (e + 1) % 3], i2 = faces[3 * q + (e + 2) % 3];
+                double dl = 0;
+                for (int a = 0; a < 3; ++a) dl += (B[(e + 2) % 3][a] - B[(e + 1) % 3][a]) * (B[(e + 2) % 3][a] - B[(e + 1) % 3][a]);
+                cn[e] = (i1 < i2 ? 1.0 : -1.0) * sqrt(dl) / (2.0 * areaq);
+            }
+            double Y[7][3];
+            for (int j = 0; j < 7; ++j)
+                for (int a = 0; a < 3; ++a) Y[j][a] = bary[j][0] * B[0][a] + bary[j][1] * B[1][a] + bary[j][2] * B[2][a];
+            double accr[3][3] = {{0}}, acci[3][3] = {{0}};
+            for (int i = 0; i < 7; ++i) {
+                /* inner integrals: g0 = int G, gy = int y G (complex) */
+                double g0r = 0, g0i = 0, gyr[3] = {0, 0, 0}, gyi[3] = {0, 0, 0};
+                for (int j = 0; j < 7; ++j) {
+                    double dd[3] = {X[i][0] - Y[j][0], X[i][1] - Y[j][1], X[i][2] - Y[j][2]};
+                    double R = sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+                    double gr, gi;
+                    if (shared == 0) {
+                        gr = cos(k * R) / R * inv4pi;
+                        gi = -sin(k * R) / R * inv4pi;
+                    } else if (R < 1e-300) {
+                        gr = 0.0;
+                        gi = -k * inv4pi;
+                    } else {
+                        double sh = sin(0.5 * k * R);
+                        gr = -2.0 * sh * sh / R * inv4pi;
+                        gi = -sin(k * R) / R * inv4pi;
+                    }
+                    double wj = w7[j] * areaq;
+                    g0r += wj * gr; g0i += wj * gi;
+                    for (int a = 0; a < 3; ++a) { gyr[a] += wj * gr * Y[j][a]; gyi[a] += wj * gi * Y[j][a]; }
+                }
+                if (shared) {
+                    double I1, Iv[3];
+                    orc_pot_integrals(X[i], B, &I1, Iv);
+                    g0r += inv4pi * I1;
+                    for (int a = 0; a < 3; ++a) gyr[a] += inv4pi * (Iv[a] + X[i][a] * I1);
+                }
+                double wi = w7[i] * areap;
+                for (int m = 0; m < 3; ++m) {
+                    for (int nn = 0; nn < 3; ++nn) {
+                        /* int f_n G = c_n (gy - v_n g0);  f_m(x) = c_m (x - v_m) */
+                        double fr = 0, fi = 0;
+                        for (int a = 0; a < 3; ++a) {
+                            double vn = B[nn][a];
+                            double tr = gyr[a] - vn * g0r, ti = gyi[a] - vn * g0i;
+                            double xm = X[i][a] - A[m][a];
+                            fr += xm * tr;
+                            fi += xm * ti;
+                        }
+                        double cc = cm[m] * cn[nn];
+                        /* jk cc (fr + j fi) - (4j/k) cc (g0r + j g0i) */
+                        accr[m][nn] += wi * cc * (-k * fi + 4.0 / k * g0i);
+                        acci[m][nn] += wi * cc * (k * fr - 4.0 / k * g0r);
+                    }
+                }
+            }
+            for (int m = 0; m < 3; ++m)
+                for (int nn = 0; nn < 3; ++nn) {
+                    int64_t row = fei[3 * p + m], col = fei[3 * q + nn];
+                    int64_t o = (row * ne + col);
+#pragma omp atomic
+                    zr[o] += accr[m][nn];
+#pragma omp atomic
+                    zi[o] += acci[m][nn];
+                }
+        }
+    }
+}
+
+/* EFIE excitation with the symmetric rule: rhs[fei, w] += int f_m . E0 e^{-j k khat.x}. */
+void ORC(mom_sym_rhs_rwg)(const REAL* verts_r, const int32_t* faces, int64_t nf, const int32_t* fei,
+                          int64_t ne, const double* waves, int nrhs, double* rr, double* ri) {
+    double bary[7][3], w7[7];
+    orc_d7(bary, w7);
+    for (int64_t p = 0; p < nf; ++p) {
+        double A[3][3];
+        for (int v = 0; v < 3; ++v)
+            for (int a = 0; a < 3; ++a) A[v][a] = (double)verts_r[3 * (int64_t)faces[3 * p + v] + a];
+        double ap[3] = {A[1][0] - A[0][0], A[1][1] - A[0][1], A[1][2] - A[0][2]};
+        double bp[3] = {A[2][0] - A[1][0], A[2][1] - A[1][1], A[2][2] - A[1][2]};
+        double cpr[3] = {ap[1] * bp[2] - ap[2] * bp[1], ap[2] * bp[0] - ap[0] * bp[2], ap[0] * bp[1] - ap[1] * bp[0]};
+        double areap = 0.5 * sqrt(cpr[0] * cpr[0] + cpr[1] * cpr[1] + cpr[2] * cpr[2]);
+        for (int m = 0; m < 3; ++m) {
+            int i1 = faces[3 * p + (m + 1) % 3], i2 = faces[3 * p + (m + 2) % 3];
+            double dl = 0;
+            for (int a = 0; a < 3; ++a) dl += (A[(m + 2) % 3][a] - A[(m + 1) % 3][a]) * (A[(m + 2) % 3][a] - A[(m + 1) % 3][a]);
+            double c = (i1 < i2 ? 1.0 : -1.0) * sqrt(dl) / (2.0 * areap);
+            for (int r = 0; r < nrhs; ++r) {
+                const double* wv = waves + 9 * r;
+                double sr = 0, si = 0;
+                for (int i = 0; i < 7; ++i) {
+                    double x[3], proj = 0, ph = 0;
+                    for (int a = 0; a < 3; ++a) x[a] = bary[i][0] * A[0][a] + bary[i][1] * A[1][a] + bary[i][2] * A[2][a];
+                    for (int a = 0; a < 3; ++a) { proj += (x[a] - A[m][a]) * wv[3 + a]; ph += wv[a] * x[a]; }
+                    double wi = w7[i] * areap * c * proj;
+                    sr += wi * cos(ph);
+                    si -= wi * sin(ph);
+                }
+                int64_t o = (int64_t)fei[3 * p + m] * nrhs + r;
+                rr[o] += sr;
+                ri[o] += si;
+            }
+        }
+    }
+}
+
+/* Exported for tests: closed-form int_T 1/R and int_T (y - x)/R (see orc_pot_integrals). */
+#ifndef ORC_POT_EXPORTED
+#define ORC_POT_EXPORTED
+#ifdef ORC_FLOAT
+#else
+void orc_potential_integrals(const double* x, const double* tri, double* I1, double* Iv) {
+    double P[3][3];
+    for (int v = 0; v < 3; ++v)
+        for (int a = 0; a < 3; ++a) P[v][a] = tri[3 * v + a];
+    orc_pot_integrals(x, P, I1, Iv);
+}
+#endif
+#endif

@@ -41,6 +41,9 @@ def _load():
                 _P, _P, _I64, _P, _P, _P, _P, _I, _P, _I, _I, _I, _D, _I64, _I64, _P, _P]
             getattr(lib, f"orc_panel_relation_{sfx}").argtypes = [_P, _I64, _P]
             getattr(lib, f"orc_radiate_h_{sfx}").argtypes = [_P, _I64, _P, _P, _P, _P, _I64, _D, _P, _P]
+            getattr(lib, f"orc_mom_sym_zmat_rwg_{sfx}").argtypes = [_P, _P, _I64, _P, _I64, _D, _I64, _I64, _P, _P]
+            getattr(lib, f"orc_mom_sym_rhs_rwg_{sfx}").argtypes = [_P, _P, _I64, _P, _I64, _P, _I, _P, _P]
+        lib.orc_potential_integrals.argtypes = [_P, _P, _P, _P]
         _lib = lib
     return _lib
 
@@ -164,6 +167,40 @@ def radiate_h(points, verts, vert_areas, vert_js, k, dtype=np.float64):
     getattr(lib, f"orc_radiate_h_{_sfx(dtype)}")(_ptr(p), p.shape[0], _ptr(v), _ptr(a), _ptr(jr), _ptr(ji),
                                                  v.shape[0], float(k), _ptr(hr), _ptr(hi))
     return hr + 1j * hi
+
+
+def potential_integrals(x, tri):
+    """Closed-form (int_T 1/R dS, int_T (y - x)/R dS) for point x and triangle tri [3, 3]."""
+    lib = _load()
+    xx, t = _c(x, np.float64), _c(tri, np.float64)
+    i1 = np.zeros(1)
+    iv = np.zeros(3)
+    lib.orc_potential_integrals(_ptr(xx), _ptr(t), _ptr(i1), _ptr(iv))
+    return float(i1[0]), iv
+
+
+def mom_sym_zmat(verts, faces, fei, n_edges, k, faces_range=None):
+    """EFIE RWG matrix [E, E] complex128 with the symmetric 7-point rule + singular extraction."""
+    lib = _load()
+    v, f, e = _c(verts, np.float64), _c(faces, np.int32), _c(np.reshape(fei, -1), np.int32)
+    nf = f.shape[0]
+    f0, f1 = (0, nf) if faces_range is None else faces_range
+    zr = np.zeros((n_edges, n_edges))
+    zi = np.zeros_like(zr)
+    lib.orc_mom_sym_zmat_rwg_f64(_ptr(v), _ptr(f), nf, _ptr(e), n_edges, float(k), f0, f1, _ptr(zr), _ptr(zi))
+    return zr + 1j * zi
+
+
+def mom_sym_rhs(verts, faces, fei, n_edges, waves):
+    """EFIE excitation [E, n_rhs] complex128 with the symmetric rule; waves [n, 9] float64."""
+    lib = _load()
+    v, f, e = _c(verts, np.float64), _c(faces, np.int32), _c(np.reshape(fei, -1), np.int32)
+    w = _c(np.reshape(waves, (-1, 9)), np.float64)
+    nr = w.shape[0]
+    rr = np.zeros((n_edges, nr))
+    ri = np.zeros_like(rr)
+    lib.orc_mom_sym_rhs_rwg_f64(_ptr(v), _ptr(f), f.shape[0], _ptr(e), n_edges, _ptr(w), nr, _ptr(rr), _ptr(ri))
+    return rr + 1j * ri
 
 
 # ---- reference kernels compiled for the host (pinning only) ----------------------------
