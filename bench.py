@@ -250,12 +250,12 @@ def main():
     Z = torch.zeros((n_edges, n_edges), dtype=torch.complex64, device=dev)
     stream = torch.cuda.current_stream(dev)
     M = pkg.mesh_MOM_3d
-    pairs = M.near_pairs(faces) if sym else None
-    n_near = int(pairs.shape[0]) if sym else 0
+    near = M.near_pairs(faces) if sym else None
+    n_near = int(near.shape[0]) if sym else 0
 
     def assemble(out):
         if sym:
-            M.assemble_Z_rwg_sym(verts, faces, fei, n_edges, k, out=out, pairs=pairs, check_indices=False)
+            M.assemble_Z_rwg_sym(verts, faces, fei, n_edges, k, out=out, pairs=near, check_indices=False)
         else:
             M.assemble_Z_rwg(verts, faces, areas, normals, fei, n_edges, px, wx, py, wy, k, out=out,
                              check_indices=False)
@@ -380,7 +380,7 @@ def main():
             nn = pkg.utils.compute_face_normals(d_verts, d_faces).contiguous()
             Z.zero_()
             if sym:
-                M.assemble_Z_rwg_sym(d_verts, d_faces, d_fei, n_edges, k, out=Z, pairs=pairs,
+                M.assemble_Z_rwg_sym(d_verts, d_faces, d_fei, n_edges, k, out=Z, pairs=near,
                                      check_indices=False)
             else:
                 M.assemble_Z_rwg(d_verts, d_faces, a, nn, d_fei, n_edges, *d_rules, k, out=Z,

@@ -16,7 +16,7 @@ import sys as _sys
 
 _sys.modules.setdefault("mesh_ferrofluid_gb300", _sys.modules[__name__])
 
-from . import meshes, mesh_MOM_3d, roofline, utils  # noqa: E402
+from . import mesh_io, meshes, mesh_MOM_3d, roofline, utils  # noqa: E402
 from ._lib import MeshBEMError, load as load_library  # noqa: E402
 from .kernel_functions import (  # noqa: E402
     MeshMOMInterpolateJsKernel,
