@@ -42,6 +42,8 @@ WORKLOADS = {
     "mom_ref_L3": (3, 2.0, 4),
     "mom_sym_L5": (5, 10.0, 0),
     "mom_sym_L4": (4, 6.0, 0),
+    # ray queries: (terrain cells per side, icospheres, cameras); 512 x 256 skydome rays each
+    "ray_skydome": (512, 12, 8),
 }
 
 
@@ -184,6 +186,168 @@ def cpu_sample_run(workload, seconds, steps=1, warmup=0):
 
 
 # ---------------------------------------------------------------------------------------
+# ray-query workload
+# ---------------------------------------------------------------------------------------
+def ray_scene(cells, n_spheres, seed=0):
+    """Height-field terrain (2 cells^2 faces) on [-50, 50]^2 plus icospheres (L5) above it."""
+    pkg = importlib.import_module("mesh-ferrofluid_gb300")
+    xs = np.linspace(-50.0, 50.0, cells + 1)
+    X, Y = np.meshgrid(xs, xs, indexing="ij")
+    Z = 2.0 * np.sin(0.11 * X) * np.cos(0.07 * Y) + 0.5 * np.sin(0.5 * X + 0.3 * Y)
+    verts = [np.stack([X, Y, Z], -1).reshape(-1, 3)]
+    i, j = np.meshgrid(np.arange(cells), np.arange(cells), indexing="ij")
+    a = (i * (cells + 1) + j).ravel()
+    b, c, d = a + cells + 1, a + 1, a + cells + 2
+    faces = [np.stack([np.stack([a, b, c], -1), np.stack([b, d, c], -1)], 1).reshape(-1, 3)]
+    sv, sf = pkg.meshes.icosphere(5, 1.0)
+    rng = np.random.default_rng(seed)
+    off = verts[0].shape[0]
+    for _ in range(n_spheres):
+        r = rng.uniform(1.0, 4.0)
+        ctr = np.array([rng.uniform(-40, 40), rng.uniform(-40, 40), rng.uniform(4.0, 12.0)])
+        verts.append(sv * r + ctr)
+        faces.append(sf + off)
+        off += sv.shape[0]
+    return np.concatenate(verts).astype(np.float32), np.concatenate(faces).astype(np.int32)
+
+
+def skydome_dirs(n_theta):
+    th = (np.arange(n_theta) + 0.5) * np.pi / n_theta
+    ph = (np.arange(2 * n_theta) + 0.5) * np.pi / n_theta
+    T, P = np.meshgrid(th, ph, indexing="ij")
+    return np.stack([np.sin(T) * np.cos(P), np.sin(T) * np.sin(P), np.cos(T)], -1).reshape(-1, 3)
+
+
+def ray_cameras(n, seed=1):
+    rng = np.random.default_rng(seed)
+    return np.stack([rng.uniform(-30, 30, n), rng.uniform(-30, 30, n), rng.uniform(3.0, 15.0, n)], 1)
+
+
+def main_rays(args, rank, world, local_rank):
+    cells, n_spheres, n_cam = WORKLOADS[args.workload]
+    n_theta = 256
+    n_rays = 2 * n_theta * n_theta
+    config = {"workload": args.workload, "scene": f"height-field terrain {cells}x{cells} cells + "
+              f"{n_spheres} icospheres L5", "cameras": n_cam, "rays_per_camera": n_rays,
+              "image": f"{2 * n_theta}x{n_theta} skydome (equirectangular)", "tmin": 0.001, "tmax": 10000.0,
+              "parallelism": "replicas"}
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference's ray query is a Vulkan "
+                              "ray-tracing pipeline; no graphics stack: unavailable on this box"}), flush=True)
+        return
+    import torch
+
+    pkg = importlib.import_module("mesh-ferrofluid_gb300")
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local_rank if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    v_np, f_np = ray_scene(cells, n_spheres)
+    config["n_faces"] = int(f_np.shape[0])
+    verts = torch.from_numpy(v_np).to(dev)
+    faces = torch.from_numpy(f_np).to(dev)
+    stream = torch.cuda.current_stream(dev)
+    b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    b0.record(stream)
+    app = pkg.ray_query.RayQueryApp(verts, faces, device=dev)
+    b1.record(stream)
+    torch.cuda.synchronize(dev)
+    build_ms = b0.elapsed_time(b1)
+    cams_np = ray_cameras(n_cam).astype(np.float32)
+    dirs_np = np.broadcast_to(skydome_dirs(n_theta), (n_cam, n_rays, 3)).astype(np.float32)
+    origins = torch.from_numpy(cams_np).to(dev)
+    dirs = torch.from_numpy(np.ascontiguousarray(dirs_np)).to(dev)
+    out = torch.empty(n_cam, n_rays, 4, dtype=torch.float32, device=dev)
+    total_rays = n_cam * n_rays
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    for _ in range(args.warmup):
+        app.query(origins, dirs, out=out)
+    barrier()
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.3)
+    # inputs (12.6 MB) + output (16.8 MB) fit in L2; the BVH (~50 MB) too: steady-state
+    # numbers for repeated queries of one scene, as a renderer issues them
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    for e0, e1 in ev:
+        e0.record(stream)
+        app.query(origins, dirs, out=out)
+        e1.record(stream)
+    barrier()
+    clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * total_rays / (ms_per_step / 1e3)
+    hit_frac = float((out[..., 0] >= 0).float().mean())
+    peaks = pkg.roofline.measured_peaks(REPO)
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    stream_bytes = total_rays * (12 + 16) + n_cam * 12
+    ach = stream_bytes / (ms_per_step / 1e3) / 1e9
+    line = {"metric": "closest-hit rays/s", "value": value, "unit": "rays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                         "traffic": None,
+                         "algorithmic": "28 B per ray (direction in, result out); traversal reads BVH "
+                                        "records from L2, so the kernel is latency/L2 bound, not HBM bound",
+                         "kernel_ms": ms_per_step},
+            "clocks": clocks.summary(), "gpu_launches": args.steps, "bvh_build_ms": build_ms,
+            "hit_fraction": hit_frac}
+    if not args.no_e2e:
+        # the plugin call with host arrays: QueryForNLOS(numpy, numpy) -> numpy
+        h_o = cams_np.reshape(-1)
+        h_d = np.ascontiguousarray(dirs_np).reshape(-1)
+        app.QueryForNLOS(h_o, h_d)
+        barrier()
+        t0 = time.perf_counter()
+        e2e_steps = max(2, min(args.steps, 3))
+        for _ in range(e2e_steps):
+            res = app.QueryForNLOS(h_o, h_d)
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+        assert res.shape == (total_rays * 4,)
+        line["e2e"] = {"value": world * total_rays / e2e_s, "unit": "rays/s",
+                       "h2d_bytes_per_step": h_o.nbytes + h_d.nbytes, "d2h_bytes_per_step": total_rays * 16,
+                       "ms_per_step": e2e_s * 1e3, "steps": e2e_steps,
+                       "path": "ray_query.RayQueryApp.QueryForNLOS with numpy arrays in and out (C ABI "
+                               "mb_ray_query_f32), host wall clock"}
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+
+        threads = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+        t0 = time.perf_counter()
+        O.ray_query(v_np, f_np, cams_np[:1], dirs_np[:1, :64])
+        per_ray = (time.perf_counter() - t0) / 64
+        n = int(max(64, min(n_rays, args.cpu_seconds / max(per_ray, 1e-9))))
+        t0 = time.perf_counter()
+        O.ray_query(v_np, f_np, cams_np[:1], dirs_np[:1, :n])
+        line["cpu_baseline"] = {"value": n / (time.perf_counter() - t0), "unit": "rays/s", "cores": threads,
+                                "kind": "port", "sample": f"{n} rays of camera 0, brute force over all "
+                                f"{f_np.shape[0]} faces (double, no acceleration structure: the reference's "
+                                "own query is a Vulkan pipeline)"}
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------------------
 def main():
@@ -191,6 +355,8 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload.startswith("ray_"):
+        return main_rays(args, rank, world, local_rank)
     level, k, gq = WORKLOADS[args.workload]
     n_faces = 20 * 4 ** level
     n_edges = 30 * 4 ** level

@@ -176,6 +176,27 @@ int mb_radiate_h_c128(const double* points, int64_t n_points, const double* vert
                       const double* vert_areas, const double* js, int64_t n_verts,
                       double wavenumber, double* h, void* stream);
 
+/* ---- Closest-hit ray queries (replaces the Vulkan ray-query plugin) ------------------ */
+
+/* Replaces VulkanRayTracing.RayQueryApp (src/vulkan_ray_tracing/pybind.cpp:14-28;
+ * QueryForLOS / QueryForNLOS at ray_query_App.hpp:881-1000; shaders raygen.rgen:23-64,
+ * closesthit.rchit, miss.rmiss).  mb_ray_bvh_build_f32 builds a linear BVH of the mesh in a
+ * caller-owned, 256-byte aligned device buffer of mb_ray_bvh_bytes(n_faces) bytes; the
+ * finished buffer is self-contained (the mesh arrays are not read by queries).
+ * mb_ray_query_f32 casts n_rows x n_cols rays: ray (r, c) starts at origins[r] and runs
+ * along dirs[r * n_cols + c] (normalised inside); opaque, no culling, hits with t in
+ * [tmin, tmax].  out (16-byte aligned): [n_rows * n_cols, 4] float (face index, 0, 0,
+ * distance) or (-1, 0, 0, -1) on a miss, as the plugin returns.  Equal distances keep the
+ * lower face index.  mb_ray_status reports (synchronously) whether any traversal since the
+ * build stopped early (bit 0: 64-entry stack full; bit 1: more visits than the tree has
+ * nodes, i.e. the buffer does not hold a BVH of n_faces faces). */
+size_t mb_ray_bvh_bytes(int64_t n_faces);
+int mb_ray_bvh_build_f32(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                         void* bvh, size_t bvh_bytes, void* stream);
+int mb_ray_query_f32(const void* bvh, int64_t n_faces, const float* origins, const float* dirs,
+                     int64_t n_rows, int64_t n_cols, double tmin, double tmax, float* out, void* stream);
+int mb_ray_status(const void* bvh, int64_t n_faces, int32_t* overflow, void* stream);
+
 /* ---- Dense iterative solve (replaces torch.linalg.solve, mesh_BEM_solver_3d.py:174) -- */
 
 /* Outcome of mb_gmres_c64. status: 0 converged to tol, 1 stopped at max_iters. */

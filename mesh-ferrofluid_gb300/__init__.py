@@ -9,14 +9,15 @@ The directory name contains a hyphen, so import it with
 Public surface (mirrors the reference's ``src.mesh_BEM`` / ``src.utils`` entry points):
 ``MeshBEMSolver3d``, ``MeshMOMZmatKernel``, ``MeshMOMRhsKernel``,
 ``MeshMOMInterpolateJsKernel``, the op module ``mesh_MOM_3d``,
-``double_integration_on_panels_3d``, the layer classes and the utilities of ``utils``.
+``double_integration_on_panels_3d``, the layer classes and the utilities of ``utils``;
+``ray_query.RayQueryApp`` replaces the Vulkan ray-query plugin.
 The compute path is libmeshbem_gb300.so (``build.py``); nothing falls back to the CPU.
 """
 import sys as _sys
 
 _sys.modules.setdefault("mesh_ferrofluid_gb300", _sys.modules[__name__])
 
-from . import mesh_io, meshes, mesh_MOM_3d, roofline, utils  # noqa: E402
+from . import mesh_io, meshes, mesh_MOM_3d, ray_query, roofline, utils  # noqa: E402
 from ._lib import MeshBEMError, load as load_library  # noqa: E402
 from .kernel_functions import (  # noqa: E402
     MeshMOMInterpolateJsKernel,
@@ -30,6 +31,7 @@ from .layers import (  # noqa: E402
     double_integration_on_panels_3d,
 )
 from .mesh_BEM_solver_3d import MeshBEMSolver3d  # noqa: E402
+from .ray_query import RayQueryApp  # noqa: E402
 from .utils import (  # noqa: E402
     BEMType,
     BoundaryType,
@@ -43,5 +45,5 @@ __all__ = [
     "MeshBEMSolver3d", "MeshMOMZmatKernel", "MeshMOMRhsKernel", "MeshMOMInterpolateJsKernel",
     "mesh_MOM_3d", "double_integration_on_panels_3d", "SingleLayer3d", "DoubleLayer3d",
     "RhsLayer3d", "BEMType", "BoundaryType", "LayerType", "OrderType", "PanelRelationType",
-    "Logger", "MeshBEMError", "load_library", "meshes", "utils",
+    "Logger", "MeshBEMError", "load_library", "meshes", "utils", "ray_query", "RayQueryApp",
 ]

@@ -50,6 +50,10 @@ _SIGS = {
     "mb_mom_sym_near_c128": [_P, _I64, _P, _I64, _P, _I64, _P, _I64, _D, _P, _P],
     "mb_mom_sym_rhs_rwg_c64": [_P, _I64, _P, _I64, _P, _I64, _P, _I, _P, _P],
     "mb_mom_sym_rhs_rwg_c128": [_P, _I64, _P, _I64, _P, _I64, _P, _I, _P, _P],
+    "mb_ray_bvh_bytes": [_I64],
+    "mb_ray_bvh_build_f32": [_P, _I64, _P, _I64, _P, ctypes.c_size_t, _P],
+    "mb_ray_query_f32": [_P, _I64, _P, _P, _I64, _I64, _D, _D, _P, _P],
+    "mb_ray_status": [_P, _I64, _P, _P],
     "mb_radiate_h_c64": [_P, _I64, _P, _P, _P, _I64, _D, _P, _P],
     "mb_radiate_h_c128": [_P, _I64, _P, _P, _P, _I64, _D, _P, _P],
     "mb_gmres_workspace_bytes": [_I64, _I],
@@ -59,7 +63,7 @@ _SIGS = {
     "mb_residual_c128": [_P, _P, _P, _I64, _P, _P],
 }
 
-_RESTYPES = {"mb_gmres_workspace_bytes": ctypes.c_size_t}
+_RESTYPES = {"mb_gmres_workspace_bytes": ctypes.c_size_t, "mb_ray_bvh_bytes": ctypes.c_size_t}
 
 
 class GmresInfo(ctypes.Structure):

@@ -48,6 +48,11 @@ template <typename T>
 int launch_pack_tight(const T*, const T*, const int32_t*, int64_t, int64_t, int, T*, cudaStream_t);
 int launch_panel_relation(const int32_t*, int64_t, uint8_t*, cudaStream_t);
 size_t gmres_workspace_bytes(int64_t n, int m);
+size_t bvh_bytes(int64_t n);
+int bvh_build(const float*, const int32_t*, int64_t, void*, size_t, cudaStream_t);
+int ray_query(const void*, int64_t, const float*, const float*, int64_t, int64_t, double, double, float*,
+              cudaStream_t);
+int ray_status(const void*, int64_t, int32_t*, cudaStream_t);
 template <typename T>
 int launch_mom_sym_regular(const T*, const int32_t*, const int32_t*, int64_t, double, int64_t, int64_t, int64_t,
                            T*, cudaStream_t);
@@ -288,6 +293,30 @@ MB_PACK(f64, double)
 MB_SYM(c64, float)
 MB_SYM(c128, double)
 #undef MB_SYM
+
+size_t mb_ray_bvh_bytes(int64_t n_faces) { return n_faces > 0 ? bvh_bytes(n_faces) : 0; }
+
+int mb_ray_bvh_build_f32(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces, void* bvh,
+                         size_t bvh_nbytes, void* stream) {
+    (void)n_verts;
+    MB_REQUIRE(n_faces > 0, "mesh has no faces");
+    MB_REQUIRE(verts && faces && bvh, "null pointer argument");
+    return bvh_build(verts, faces, n_faces, bvh, bvh_nbytes, as_stream(stream));
+}
+
+int mb_ray_query_f32(const void* bvh, int64_t n_faces, const float* origins, const float* dirs, int64_t n_rows,
+                     int64_t n_cols, double tmin, double tmax, float* out, void* stream) {
+    MB_REQUIRE(n_faces > 0 && n_rows >= 0 && n_cols >= 0, "bad sizes");
+    if (n_rows == 0 || n_cols == 0) return MB_OK;
+    MB_REQUIRE(bvh && origins && dirs && out, "null pointer argument");
+    MB_REQUIRE(tmin <= tmax, "tmin > tmax");
+    return ray_query(bvh, n_faces, origins, dirs, n_rows, n_cols, tmin, tmax, out, as_stream(stream));
+}
+
+int mb_ray_status(const void* bvh, int64_t n_faces, int32_t* overflow, void* stream) {
+    MB_REQUIRE(bvh && overflow && n_faces > 0, "bad arguments");
+    return ray_status(bvh, n_faces, overflow, as_stream(stream));
+}
 
 #define MB_RAD(SFX, T)                                                                                \
     int mb_radiate_h_##SFX(const T* points, int64_t n_points, const T* verts, const T* vert_areas,       \

@@ -740,3 +740,56 @@ void orc_potential_integrals(const double* x, const double* tri, double* I1, dou
 }
 #endif
 #endif
+
+/* ------------------------------------------------------------------------------------ */
+/* Closest-hit ray query (the reference's Vulkan ray-query plugin,                      */
+/* src/vulkan_ray_tracing/shaders/raygen.rgen:23-64, closesthit.rchit, miss.rmiss;       */
+/* QueryForNLOS / QueryForLOS at ray_query_App.hpp:881-1000): rays from origin[row] along */
+/* normalised dir[row*W + col], opaque, no culling, t in [tmin, tmax]; result per ray     */
+/* (face index, 0, 0, distance to the hit) or (-1, 0, 0, -1).  Brute force over all       */
+/* triangles with the Moller-Trumbore test (Moller & Trumbore 1997), in double.           */
+/* ------------------------------------------------------------------------------------ */
+void ORC(ray_query)(const REAL* verts, const int32_t* faces, int64_t nf, const REAL* origins,
+                    const REAL* dirs, int64_t h, int64_t w, double tmin, double tmax, REAL* out) {
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < h * w; ++r) {
+        const int64_t row = r / w;
+        double o[3] = {origins[3 * row], origins[3 * row + 1], origins[3 * row + 2]};
+        double d[3] = {dirs[3 * r], dirs[3 * r + 1], dirs[3 * r + 2]};
+        double dn = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        for (int a = 0; a < 3; ++a) d[a] /= dn;
+        double best = tmax;
+        int64_t hit = -1;
+        for (int64_t f = 0; f < nf; ++f) {
+            const REAL* v0 = verts + 3 * (int64_t)faces[3 * f];
+            const REAL* v1 = verts + 3 * (int64_t)faces[3 * f + 1];
+            const REAL* v2 = verts + 3 * (int64_t)faces[3 * f + 2];
+            double e1[3], e2[3], s[3];
+            for (int a = 0; a < 3; ++a) {
+                e1[a] = v1[a] - v0[a];
+                e2[a] = v2[a] - v0[a];
+                s[a] = o[a] - v0[a];
+            }
+            double p[3] = {d[1] * e2[2] - d[2] * e2[1], d[2] * e2[0] - d[0] * e2[2], d[0] * e2[1] - d[1] * e2[0]};
+            double det = e1[0] * p[0] + e1[1] * p[1] + e1[2] * p[2];
+            if (fabs(det) < 1e-300) continue;
+            double inv = 1.0 / det;
+            double u = (s[0] * p[0] + s[1] * p[1] + s[2] * p[2]) * inv;
+            if (u < 0.0 || u > 1.0) continue;
+            double q[3] = {s[1] * e1[2] - s[2] * e1[1], s[2] * e1[0] - s[0] * e1[2], s[0] * e1[1] - s[1] * e1[0]};
+            double v = (d[0] * q[0] + d[1] * q[1] + d[2] * q[2]) * inv;
+            if (v < 0.0 || u + v > 1.0) continue;
+            double t = (e2[0] * q[0] + e2[1] * q[1] + e2[2] * q[2]) * inv;
+            if (t >= tmin && t <= best) {
+                if (t < best || hit < 0 || f < hit) {
+                    best = t;
+                    hit = f;
+                }
+            }
+        }
+        out[4 * r + 0] = (REAL)(hit >= 0 ? (double)hit : -1.0);
+        out[4 * r + 1] = 0;
+        out[4 * r + 2] = 0;
+        out[4 * r + 3] = (REAL)(hit >= 0 ? best : -1.0);
+    }
+}

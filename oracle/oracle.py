@@ -43,6 +43,7 @@ def _load():
             getattr(lib, f"orc_radiate_h_{sfx}").argtypes = [_P, _I64, _P, _P, _P, _P, _I64, _D, _P, _P]
             getattr(lib, f"orc_mom_sym_zmat_rwg_{sfx}").argtypes = [_P, _P, _I64, _P, _I64, _D, _I64, _I64, _P, _P]
             getattr(lib, f"orc_mom_sym_rhs_rwg_{sfx}").argtypes = [_P, _P, _I64, _P, _I64, _P, _I, _P, _P]
+            getattr(lib, f"orc_ray_query_{sfx}").argtypes = [_P, _P, _I64, _P, _P, _I64, _I64, _D, _D, _P]
         lib.orc_potential_integrals.argtypes = [_P, _P, _P, _P]
         _lib = lib
     return _lib
@@ -177,6 +178,20 @@ def potential_integrals(x, tri):
     iv = np.zeros(3)
     lib.orc_potential_integrals(_ptr(xx), _ptr(t), _ptr(i1), _ptr(iv))
     return float(i1[0]), iv
+
+
+def ray_query(verts, faces, origins, dirs, tmin=0.001, tmax=10000.0):
+    """Closest hits [H, W, 4] (face, 0, 0, distance) / (-1, 0, 0, -1) for rays dirs [H, W, 3]."""
+    lib = _load()
+    v, f = _c(verts, np.float64), _c(faces, np.int32)
+    o = _c(np.reshape(origins, (-1, 3)), np.float64)
+    h = o.shape[0]
+    d = _c(np.reshape(dirs, (h, -1, 3)), np.float64)
+    w = d.shape[1]
+    out = np.zeros((h, w, 4))
+    lib.orc_ray_query_f64(_ptr(v), _ptr(f), f.shape[0], _ptr(o), _ptr(d), h, w, float(tmin), float(tmax),
+                          _ptr(out))
+    return out
 
 
 def mom_sym_zmat(verts, faces, fei, n_edges, k, faces_range=None):
