@@ -44,6 +44,9 @@ WORKLOADS = {
     "mom_sym_L4": (4, 6.0, 0),
     # ray queries: (terrain cells per side, icospheres, cameras); 512 x 256 skydome rays each
     "ray_skydome": (512, 12, 8),
+    # Laplace single-layer collocation, unit Dirichlet data on the sphere: (level, radius, dtype)
+    "laplace_col_L5": (5, 1.0, "f32"),
+    "laplace_col_L5_f64": (5, 1.0, "f64"),
 }
 
 
@@ -348,6 +351,161 @@ def main_rays(args, rank, world, local_rank):
 
 
 # ---------------------------------------------------------------------------------------
+# Laplace single-layer collocation workload
+# ---------------------------------------------------------------------------------------
+def main_laplace(args, rank, world, local_rank):
+    level, radius, dts = WORKLOADS[args.workload]
+    nf = 20 * 4 ** level
+    pairs = float(nf) ** 2
+    config = {"workload": args.workload, "mesh": f"icosphere L{level}, radius {radius}", "n_faces": nf,
+              "system": "P0 single-layer collocation at centroids, V sigma = 1 (exact sigma = 1/a)",
+              "rule": "7-point rule per source face; faces sharing a vertex with the collocation face in "
+                      "closed form (FP64)", "matrix": f"[F, F] {dts}",
+              "l2": f"A ({pairs * (4 if dts == 'f32' else 8) / 1e9:.2f} GB) > L2, rewritten every step",
+              "parallelism": "replicas"}
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no collocation system "
+                              "(its Laplace path is the Galerkin one; new capability)"}), flush=True)
+        return
+    import torch
+
+    pkg = importlib.import_module("mesh-ferrofluid_gb300")
+    R = pkg.roofline
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local_rank if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    dt = torch.float32 if dts == "f32" else torch.float64
+    v_np, f_np = pkg.meshes.icosphere(level, radius)
+    verts = torch.tensor(v_np, dtype=dt, device=dev)
+    faces = torch.tensor(f_np, dtype=torch.int32, device=dev)
+    A = torch.empty((nf, nf), dtype=dt, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    L = pkg.layers
+    near = L.laplace_near_pairs(faces)  # mesh topology, computed once like the edge numbering
+
+    def assemble(v, f):
+        L.laplace_colloc_sl(v, f, out=A, near=near, check_indices=False)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    for _ in range(args.warmup):
+        assemble(verts, faces)
+    barrier()
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.3)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    for e0, e1 in ev:
+        e0.record(stream)
+        assemble(verts, faces)
+        e1.record(stream)
+    barrier()
+    clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * pairs / (ms_per_step / 1e3)
+    peaks = R.measured_peaks(REPO)
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    evals = pairs * 7.0
+    flop = evals * R.LAPLACE_SL_FLOP_PER_EVAL
+    kern_s = statistics.mean(ms) / 1e3
+    fp32_peak = R.fp32_peak_tflops(sm_max)
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    out_bytes = pairs * (4 if dts == "f32" else 8)
+    peak = fp32_peak if dts == "f32" else R.FP64_NOMINAL_TFLOPS
+    line = {"metric": "collocation-matrix face pairs/s", "value": value, "unit": "pairs/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": dts, "data": "synthetic", "config": config,
+            "roofline": {"bound": "fp32" if dts == "f32" else "fp64",
+                         "achieved": flop / kern_s / 1e12, "peak": peak, "unit": "TFLOP/s",
+                         "frac": flop / kern_s / 1e12 / peak,
+                         "peak_source": "derived FP32 SIMT peak at the max SM clock" if dts == "f32" else
+                                        "nominal GB300 FP64 (no measured FP64 figure)",
+                         "hbm": {"achieved_gbs": out_bytes / kern_s / 1e9, "peak_gbs": hbm,
+                                 "frac": out_bytes / kern_s / 1e9 / hbm},
+                         "traffic": None,
+                         "algorithmic": f"{R.LAPLACE_SL_FLOP_PER_EVAL} FLOP + {R.LAPLACE_MUFU_PER_EVAL} MUFU per "
+                                        "evaluation x 7 evaluations per face pair x F^2; output "
+                                        f"{4 if dts == 'f32' else 8} B per pair",
+                         "kernel_ms": kern_s * 1e3},
+            "clocks": clocks.summary(), "gpu_launches": args.steps}
+    if not args.no_solve:
+        ones = torch.ones(nf, dtype=torch.float64, device=dev)
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        sigma, infos = pkg.mesh_MOM_3d.gmres_real(A, ones, restart=50, tol=1e-8, max_iters=1000)
+        s1.record(stream)
+        torch.cuda.synchronize(dev)
+        err = float((sigma * radius - 1).abs().max())
+        line["solve"] = {"what": "GMRES(50) to 1e-8 on V sigma = 1 (FP64 refinement residual)",
+                         "gmres_ms": s0.elapsed_time(s1), "iterations": infos[0]["iterations"],
+                         "rel_residual": infos[0]["rel_residual"], "converged": infos[0]["converged"],
+                         "max_rel_err_sigma_vs_1_over_a": err,
+                         "time_to_solution_ms": ms_per_step + s0.elapsed_time(s1)}
+    if not args.no_e2e:
+        h_v = torch.tensor(v_np, dtype=dt).pin_memory()
+        h_f = torch.tensor(f_np, dtype=torch.int32).pin_memory()
+        h_A = torch.empty((nf, nf), dtype=dt, pin_memory=True)
+        d_v, d_f = torch.empty_like(verts), torch.empty_like(faces)
+
+        def e2e_step():
+            d_v.copy_(h_v, non_blocking=True)
+            d_f.copy_(h_f, non_blocking=True)
+            assemble(d_v, d_f)
+            h_A.copy_(A, non_blocking=True)
+
+        e2e_step()
+        barrier()
+        n_e2e = max(2, min(args.steps, 3))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n_e2e):
+            e2e_step()
+        e1.record(stream)
+        barrier()
+        e2e_ms = e0.elapsed_time(e1) / n_e2e
+        line["e2e"] = {"value": world * pairs / (e2e_ms / 1e3), "unit": "pairs/s",
+                       "h2d_bytes_per_step": h_v.numel() * h_v.element_size() + h_f.numel() * 4,
+                       "d2h_bytes_per_step": h_A.numel() * h_A.element_size(), "ms_per_step": e2e_ms,
+                       "steps": n_e2e, "path": "layers.laplace_colloc_sl (C ABI mb_laplace_colloc_sl_*), pinned "
+                                               "host mesh in, matrix back to pinned host memory"}
+        del h_A
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+
+        threads = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+        sub_level = max(1, level - 2)
+        sv, sf = pkg.meshes.icosphere(sub_level, radius)
+        t0 = time.perf_counter()
+        O.laplace_colloc_sl(sv, sf)
+        dt_cpu = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": float(sf.shape[0]) ** 2 / dt_cpu, "unit": "pairs/s", "cores": threads,
+                                "kind": "port", "sample": f"the full collocation matrix of icosphere L{sub_level} "
+                                f"({sf.shape[0]} faces) with the double C oracle (same rule); the reference has "
+                                "no collocation path"}
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------------------
 def main():
@@ -357,6 +515,8 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.workload.startswith("ray_"):
         return main_rays(args, rank, world, local_rank)
+    if args.workload.startswith("laplace_"):
+        return main_laplace(args, rank, world, local_rank)
     level, k, gq = WORKLOADS[args.workload]
     n_faces = 20 * 4 ** level
     n_edges = 30 * 4 ** level

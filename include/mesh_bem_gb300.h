@@ -223,6 +223,19 @@ int mb_gmres_c64(const float* z, int64_t n, const double* b, double* x, int rest
                  double tol, void* workspace, size_t workspace_bytes, mb_gmres_info* info,
                  void* stream);
 
+/* The same solver for a real system A x = b (the Laplace single-layer collocation system;
+ * the reference solves its Laplace systems with torch.linalg.solve,
+ * mesh_BEM_solver_3d.py:345): A float32 (FP32 products) or float64 (FP64 products)
+ * [n, n] row-major; b, x float64 [n] (x: initial guess in, solution out).  Workspace:
+ * mb_gmres_real_workspace_bytes(n, restart) bytes. */
+size_t mb_gmres_real_workspace_bytes(int64_t n, int restart);
+int mb_gmres_f32(const float* a, int64_t n, const double* b, double* x, int restart, int max_iters,
+                 double tol, void* workspace, size_t workspace_bytes, mb_gmres_info* info,
+                 void* stream);
+int mb_gmres_f64(const double* a, int64_t n, const double* b, double* x, int restart, int max_iters,
+                 double tol, void* workspace, size_t workspace_bytes, mb_gmres_info* info,
+                 void* stream);
+
 /* No counterpart in the reference.  The same solver as mb_gmres_c64 for callers that
  * cannot allocate device memory -- for example a host application or plugin that must
  * budget all GPU memory at start-up, or a foreign-language caller (Go, Java, ...) that has
@@ -277,6 +290,45 @@ int mb_pack_tight_f32(const float* m_real, const float* m_imag, const int32_t* f
                       int64_t n_verts, int order, float* packed, void* stream);
 int mb_pack_tight_f64(const double* m_real, const double* m_imag, const int32_t* faces,
                       int64_t n_faces, int64_t n_verts, int order, double* packed, void* stream);
+
+/* Hypersingular operator, P1 Galerkin, for the Neumann and mixed branches of
+ * MeshBEMSolver3d.solve (src/mesh_BEM/mesh_BEM_solver_3d.py:268-281, 306-341), which the
+ * reference declares (hypersingular_layer/hypersingular_layer_3d.py) but never computes
+ * (integrations_3d.py:440-442).  Maue's formula: out[fy, fx, a, b] = curl phi_a(fy) .
+ * curl phi_b(fx) * v0[fy, fx], with v0 [F, F] the P0 single-layer panel integrals
+ * (mb_laplace_panels_* with layer 1, order 0) and curl phi_a = (p_{a+1} - p_{a+2}) / (2 A).
+ * out: [F, F, 3, 3], overwritten. */
+int mb_laplace_hypersingular_f32(const float* verts, int64_t n_verts, const int32_t* faces,
+                                 int64_t n_faces, const float* v0, float* out, void* stream);
+int mb_laplace_hypersingular_f64(const double* verts, int64_t n_verts, const int32_t* faces,
+                                 int64_t n_faces, const double* v0, double* out, void* stream);
+
+/* Symmetric-rule Laplace operators (an accurate mode next to the reference's rule of
+ * double_integration_on_panels_3d, integrations_3d.py:252-452; same output layout):
+ * out[fy, fx, a, b] = int_fy int_fx phi_a(y) phi_b(x) k(x, y) for rows fy in
+ * [row_begin, row_end), k = 1/(4 pi R) (layer 1) or n_fy.(x - y)/(4 pi R^3) (layer 2),
+ * order 0 (P0, nphi 1) or 1 (P1, nphi 3).  7 x 7 points per separated pair; near_pairs
+ * [n_near, 2] lists every ordered pair (fy, fx) sharing a vertex (compute_panel_relation
+ * > 0), integrated with the inner integral in closed form in FP64.  out:
+ * [row_end - row_begin, F, nphi, nphi], overwritten. */
+int mb_laplace_sym_f32(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                       int layer, int order, const int32_t* near_pairs, int64_t n_near,
+                       int64_t row_begin, int64_t row_end, float* out, void* stream);
+int mb_laplace_sym_f64(const double* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                       int layer, int order, const int32_t* near_pairs, int64_t n_near,
+                       int64_t row_begin, int64_t row_end, double* out, void* stream);
+
+/* Single-layer collocation system at face centroids (the Laplace form of the large sphere
+ * solve; no counterpart in the reference): out[i - row_begin, j] = int_{T_j} 1/(4 pi
+ * |c_i - y|) dS_y, the 7-point rule for faces without a shared vertex; the pairs (i, j)
+ * listed in near_pairs [n_near, 2] (every pair sharing a vertex, as for mb_laplace_sym_*)
+ * in closed form (FP64).  out: [row_end - row_begin, F], overwritten. */
+int mb_laplace_colloc_sl_f32(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                             const int32_t* near_pairs, int64_t n_near, int64_t row_begin,
+                             int64_t row_end, float* out, void* stream);
+int mb_laplace_colloc_sl_f64(const double* verts, int64_t n_verts, const int32_t* faces,
+                             int64_t n_faces, const int32_t* near_pairs, int64_t n_near,
+                             int64_t row_begin, int64_t row_end, double* out, void* stream);
 
 /* Replaces compute_panel_relation (src/utils/mesh_utils.py:700-725): relations [F, F] uint8,
  * overwritten. */

@@ -17,7 +17,7 @@ import sys as _sys
 
 _sys.modules.setdefault("mesh_ferrofluid_gb300", _sys.modules[__name__])
 
-from . import mesh_io, meshes, mesh_MOM_3d, ray_query, roofline, utils  # noqa: E402
+from . import layers, mesh_io, meshes, mesh_MOM_3d, ray_query, roofline, utils  # noqa: E402
 from ._lib import MeshBEMError, load as load_library  # noqa: E402
 from .kernel_functions import (  # noqa: E402
     MeshMOMInterpolateJsKernel,
@@ -26,11 +26,13 @@ from .kernel_functions import (  # noqa: E402
 )
 from .layers import (  # noqa: E402
     DoubleLayer3d,
+    HyperSingularLayer3d,
     RhsLayer3d,
     SingleLayer3d,
     double_integration_on_panels_3d,
 )
 from .mesh_BEM_solver_3d import MeshBEMSolver3d  # noqa: E402
+from .mesh_pressure import MeshPressure  # noqa: E402
 from .ray_query import RayQueryApp  # noqa: E402
 from .utils import (  # noqa: E402
     BEMType,
@@ -39,6 +41,7 @@ from .utils import (  # noqa: E402
     Logger,
     OrderType,
     PanelRelationType,
+    VertexType,
 )
 
 __all__ = [
@@ -46,4 +49,5 @@ __all__ = [
     "mesh_MOM_3d", "double_integration_on_panels_3d", "SingleLayer3d", "DoubleLayer3d",
     "RhsLayer3d", "BEMType", "BoundaryType", "LayerType", "OrderType", "PanelRelationType",
     "Logger", "MeshBEMError", "load_library", "meshes", "utils", "ray_query", "RayQueryApp",
+    "HyperSingularLayer3d", "MeshPressure", "VertexType", "layers",
 ]

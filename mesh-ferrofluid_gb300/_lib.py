@@ -50,6 +50,12 @@ _SIGS = {
     "mb_mom_sym_near_c128": [_P, _I64, _P, _I64, _P, _I64, _P, _I64, _D, _P, _P],
     "mb_mom_sym_rhs_rwg_c64": [_P, _I64, _P, _I64, _P, _I64, _P, _I, _P, _P],
     "mb_mom_sym_rhs_rwg_c128": [_P, _I64, _P, _I64, _P, _I64, _P, _I, _P, _P],
+    "mb_laplace_hypersingular_f32": [_P, _I64, _P, _I64, _P, _P, _P],
+    "mb_laplace_hypersingular_f64": [_P, _I64, _P, _I64, _P, _P, _P],
+    "mb_laplace_sym_f32": [_P, _I64, _P, _I64, _I, _I, _P, _I64, _I64, _I64, _P, _P],
+    "mb_laplace_sym_f64": [_P, _I64, _P, _I64, _I, _I, _P, _I64, _I64, _I64, _P, _P],
+    "mb_laplace_colloc_sl_f32": [_P, _I64, _P, _I64, _P, _I64, _I64, _I64, _P, _P],
+    "mb_laplace_colloc_sl_f64": [_P, _I64, _P, _I64, _P, _I64, _I64, _I64, _P, _P],
     "mb_ray_bvh_bytes": [_I64],
     "mb_ray_bvh_build_f32": [_P, _I64, _P, _I64, _P, ctypes.c_size_t, _P],
     "mb_ray_query_f32": [_P, _I64, _P, _P, _I64, _I64, _D, _D, _P, _P],
@@ -58,12 +64,16 @@ _SIGS = {
     "mb_radiate_h_c128": [_P, _I64, _P, _P, _P, _I64, _D, _P, _P],
     "mb_gmres_workspace_bytes": [_I64, _I],
     "mb_gmres_c64": [_P, _I64, _P, _P, _I, _I, _D, _P, ctypes.c_size_t, _P, _P],
+    "mb_gmres_real_workspace_bytes": [_I64, _I],
+    "mb_gmres_f32": [_P, _I64, _P, _P, _I, _I, _D, _P, ctypes.c_size_t, _P, _P],
+    "mb_gmres_f64": [_P, _I64, _P, _P, _I, _I, _D, _P, ctypes.c_size_t, _P, _P],
     "mb_gmres_c64_noalloc": [_P, _I64, _P, _P, _I, _I, _D, _P, _P],
     "mb_matvec_c64": [_P, _P, _I64, _P, _P],
     "mb_residual_c128": [_P, _P, _P, _I64, _P, _P],
 }
 
-_RESTYPES = {"mb_gmres_workspace_bytes": ctypes.c_size_t, "mb_ray_bvh_bytes": ctypes.c_size_t}
+_RESTYPES = {"mb_gmres_workspace_bytes": ctypes.c_size_t, "mb_ray_bvh_bytes": ctypes.c_size_t,
+             "mb_gmres_real_workspace_bytes": ctypes.c_size_t}
 
 
 class GmresInfo(ctypes.Structure):

@@ -46,8 +46,20 @@ int launch_laplace_panels(const T*, const int32_t*, int64_t, const T*, const T*,
                           const uint8_t*, int, int, int, double, int64_t, int64_t, T*, T*, cudaStream_t);
 template <typename T>
 int launch_pack_tight(const T*, const T*, const int32_t*, int64_t, int64_t, int, T*, cudaStream_t);
+template <typename T>
+int launch_hypersingular(const T*, const int32_t*, int64_t, const T*, T*, cudaStream_t);
+template <typename T>
+int launch_laplace_sym(const T*, const int32_t*, int64_t, int, int, const int32_t*, int64_t, int64_t, int64_t, T*,
+                       cudaStream_t);
+template <typename T>
+int launch_laplace_colloc_sl(const T*, const int32_t*, int64_t, const int32_t*, int64_t, int64_t, int64_t, T*,
+                             cudaStream_t);
 int launch_panel_relation(const int32_t*, int64_t, uint8_t*, cudaStream_t);
 size_t gmres_workspace_bytes(int64_t n, int m);
+size_t gmres_real_workspace_bytes(int64_t n, int m);
+int gmres_real(int kind, const void* a, int64_t n, const double* b, double* x, int m, int max_iters, double tol,
+               void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out, double* relres_out,
+               int* status_out, cudaStream_t s);
 size_t bvh_bytes(int64_t n);
 int bvh_build(const float*, const int32_t*, int64_t, void*, size_t, cudaStream_t);
 int ray_query(const void*, int64_t, const float*, const float*, int64_t, int64_t, double, double, float*,
@@ -259,6 +271,46 @@ MB_PACK(f32, float)
 MB_PACK(f64, double)
 #undef MB_PACK
 
+#define MB_HYP(SFX, T)                                                                                \
+    int mb_laplace_hypersingular_##SFX(const T* verts, int64_t n_verts, const int32_t* faces,           \
+                                       int64_t n_faces, const T* v0, T* out, void* stream) {           \
+        (void)n_verts;                                                                                \
+        MB_REQUIRE(n_faces >= 0, "bad sizes");                                                        \
+        if (n_faces == 0) return MB_OK;                                                               \
+        MB_REQUIRE(verts && faces && v0 && out, "null pointer argument");                             \
+        return launch_hypersingular<T>(verts, faces, n_faces, v0, out, as_stream(stream));            \
+    }
+MB_HYP(f32, float)
+MB_HYP(f64, double)
+#undef MB_HYP
+
+#define MB_LSYM(SFX, T)                                                                               \
+    int mb_laplace_sym_##SFX(const T* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,    \
+                             int layer, int order, const int32_t* near_pairs, int64_t n_near,          \
+                             int64_t row_begin, int64_t row_end, T* out, void* stream) {               \
+        (void)n_verts;                                                                                \
+        MB_REQUIRE(n_faces >= 0 && n_near >= 0, "bad sizes");                                         \
+        if (n_faces == 0) return MB_OK;                                                               \
+        MB_REQUIRE(verts && faces && out && (near_pairs || n_near == 0), "null pointer argument");    \
+        MB_REQUIRE(0 <= row_begin && row_begin <= row_end && row_end <= n_faces, "bad row range");    \
+        return launch_laplace_sym<T>(verts, faces, n_faces, layer, order, near_pairs, n_near,         \
+                                     row_begin, row_end, out, as_stream(stream));                     \
+    }                                                                                                 \
+    int mb_laplace_colloc_sl_##SFX(const T* verts, int64_t n_verts, const int32_t* faces,               \
+                                   int64_t n_faces, const int32_t* near_pairs, int64_t n_near,         \
+                                   int64_t row_begin, int64_t row_end, T* out, void* stream) {         \
+        (void)n_verts;                                                                                \
+        MB_REQUIRE(n_faces >= 0 && n_near >= 0, "bad sizes");                                         \
+        if (n_faces == 0) return MB_OK;                                                               \
+        MB_REQUIRE(verts && faces && out && (near_pairs || n_near == 0), "null pointer argument");    \
+        MB_REQUIRE(0 <= row_begin && row_begin <= row_end && row_end <= n_faces, "bad row range");    \
+        return launch_laplace_colloc_sl<T>(verts, faces, n_faces, near_pairs, n_near, row_begin,      \
+                                           row_end, out, as_stream(stream));                          \
+    }
+MB_LSYM(f32, float)
+MB_LSYM(f64, double)
+#undef MB_LSYM
+
 #define MB_SYM(SFX, T)                                                                                \
     int mb_mom_sym_zmat_rwg_##SFX(const T* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,   \
                                   const int32_t* fei, int64_t n_edges, double wavenumber,               \
@@ -335,6 +387,41 @@ MB_RAD(c128, double)
 size_t mb_gmres_workspace_bytes(int64_t n, int restart) {
     if (n <= 0 || restart < 1) return 0;
     return gmres_workspace_bytes(n, restart);
+}
+
+size_t mb_gmres_real_workspace_bytes(int64_t n, int restart) {
+    if (n <= 0 || restart < 1) return 0;
+    return gmres_real_workspace_bytes(n, restart);
+}
+
+static int gmres_real_entry(int kind, const void* a, int64_t n, const double* b, double* x, int restart,
+                            int max_iters, double tol, void* workspace, size_t workspace_bytes,
+                            mb_gmres_info* info, void* stream) {
+    MB_REQUIRE(n > 0, "n must be > 0");
+    MB_REQUIRE(a && b && x && workspace, "null pointer argument");
+    int64_t it = 0, cyc = 0;
+    double rr = 0.0;
+    int st = 1;
+    const int rc = gmres_real(kind, a, n, b, x, restart, max_iters, tol, workspace, workspace_bytes, &it, &cyc,
+                              &rr, &st, as_stream(stream));
+    if (rc == MB_OK && info) {
+        info->iterations = it;
+        info->restarts = cyc;
+        info->rel_residual = rr;
+        info->status = st;
+        info->reserved = 0;
+    }
+    return rc;
+}
+
+int mb_gmres_f32(const float* a, int64_t n, const double* b, double* x, int restart, int max_iters, double tol,
+                 void* workspace, size_t workspace_bytes, mb_gmres_info* info, void* stream) {
+    return gmres_real_entry(1, a, n, b, x, restart, max_iters, tol, workspace, workspace_bytes, info, stream);
+}
+
+int mb_gmres_f64(const double* a, int64_t n, const double* b, double* x, int restart, int max_iters, double tol,
+                 void* workspace, size_t workspace_bytes, mb_gmres_info* info, void* stream) {
+    return gmres_real_entry(2, a, n, b, x, restart, max_iters, tol, workspace, workspace_bytes, info, stream);
 }
 
 int mb_gmres_c64(const float* z, int64_t n, const double* b, double* x, int restart, int max_iters,

@@ -119,6 +119,121 @@ __global__ void __launch_bounds__(256) residual_c128_kernel(const float* __restr
     }
 }
 
+// Real matrices (the Laplace collocation system): y = A v with A real [n, n] row-major and
+// v complex (the Krylov vectors stay complex; for real data their imaginary parts stay 0).
+// A float32: lane reads float4 (four entries) and the matching four complex64 of v.
+__global__ void __launch_bounds__(256) matvec_r32_kernel(const float* __restrict__ a,
+                                                         const float* __restrict__ v, int64_t n,
+                                                         double* __restrict__ y) {
+    const int64_t row = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    const float* ar = a + row * n;
+    float sr = 0.f, si = 0.f;
+    int64_t done = 0;
+    if ((reinterpret_cast<uintptr_t>(ar) & 15) == 0 && (reinterpret_cast<uintptr_t>(v) & 15) == 0) {
+        const float4* a4 = reinterpret_cast<const float4*>(ar);
+        const float4* v4 = reinterpret_cast<const float4*>(v);
+        const int64_t nq = n >> 2;
+#define MB_RMAC(A, P)                                                            \
+    {                                                                            \
+        const float4 u0 = __ldg(v4 + 2 * (P)), u1 = __ldg(v4 + 2 * (P) + 1);     \
+        sr = fmaf(A.x, u0.x, fmaf(A.y, u0.z, fmaf(A.z, u1.x, fmaf(A.w, u1.z, sr)))); \
+        si = fmaf(A.x, u0.y, fmaf(A.y, u0.w, fmaf(A.z, u1.y, fmaf(A.w, u1.w, si)))); \
+    }
+        int64_t p = lane;
+        for (; p + 96 < nq; p += 128) {
+            const float4 a0 = __ldcs(a4 + p), a1 = __ldcs(a4 + p + 32), a2 = __ldcs(a4 + p + 64),
+                         a3 = __ldcs(a4 + p + 96);
+            MB_RMAC(a0, p) MB_RMAC(a1, p + 32) MB_RMAC(a2, p + 64) MB_RMAC(a3, p + 96)
+        }
+        for (; p < nq; p += 32) {
+            const float4 a0 = __ldcs(a4 + p);
+            MB_RMAC(a0, p)
+        }
+#undef MB_RMAC
+        done = nq << 2;
+    }
+    for (int64_t j = done + lane; j < n; j += 32) {
+        sr = fmaf(ar[j], v[2 * j], sr);
+        si = fmaf(ar[j], v[2 * j + 1], si);
+    }
+    const double tr = warp_sum((double)sr), ti = warp_sum((double)si);
+    if (lane == 0) {
+        y[2 * row] = tr;
+        y[2 * row + 1] = ti;
+    }
+}
+
+// A float64, v complex128 (the FP64 basis vector itself).
+__global__ void __launch_bounds__(256) matvec_r64_kernel(const double* __restrict__ a,
+                                                         const double* __restrict__ v, int64_t n,
+                                                         double* __restrict__ y) {
+    const int64_t row = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    const double* ar = a + row * n;
+    const double2* v2 = reinterpret_cast<const double2*>(v);
+    double sr = 0.0, si = 0.0;
+    int64_t j = lane;
+    for (; j + 96 < n; j += 128) {
+        const double a0 = __ldcs(ar + j), a1 = __ldcs(ar + j + 32), a2 = __ldcs(ar + j + 64), a3 = __ldcs(ar + j + 96);
+        const double2 u0 = __ldg(v2 + j), u1 = __ldg(v2 + j + 32), u2 = __ldg(v2 + j + 64), u3 = __ldg(v2 + j + 96);
+        sr = fma(a0, u0.x, fma(a1, u1.x, fma(a2, u2.x, fma(a3, u3.x, sr))));
+        si = fma(a0, u0.y, fma(a1, u1.y, fma(a2, u2.y, fma(a3, u3.y, si))));
+    }
+    for (; j < n; j += 32) {
+        const double a0 = __ldcs(ar + j);
+        const double2 u0 = __ldg(v2 + j);
+        sr = fma(a0, u0.x, sr);
+        si = fma(a0, u0.y, si);
+    }
+    sr = warp_sum(sr);
+    si = warp_sum(si);
+    if (lane == 0) {
+        y[2 * row] = sr;
+        y[2 * row + 1] = si;
+    }
+}
+
+// r = b - A x in FP64 for real A (float32 or float64), x, b, r complex128.
+template <typename T>
+__global__ void __launch_bounds__(256) residual_real_kernel(const T* __restrict__ a, const double* __restrict__ x,
+                                                            const double* __restrict__ b, int64_t n,
+                                                            double* __restrict__ r) {
+    const int64_t row = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    const T* ar = a + row * n;
+    const double2* x2 = reinterpret_cast<const double2*>(x);
+    double sr = 0.0, si = 0.0;
+    for (int64_t j = lane; j < n; j += 32) {
+        const double aj = (double)__ldcs(ar + j);
+        const double2 u = __ldg(x2 + j);
+        sr = fma(aj, u.x, sr);
+        si = fma(aj, u.y, si);
+    }
+    sr = warp_sum(sr);
+    si = warp_sum(si);
+    if (lane == 0) {
+        r[2 * row] = b[2 * row] - sr;
+        r[2 * row + 1] = b[2 * row + 1] - si;
+    }
+}
+
+// dst complex128 = (src, 0); and back: dst real = Re(src).
+__global__ void real_to_c128_kernel(const double* __restrict__ src, int64_t n, double* __restrict__ dst) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    dst[2 * k] = src ? src[k] : 0.0;
+    dst[2 * k + 1] = 0.0;
+}
+__global__ void c128_real_part_kernel(const double* __restrict__ src, int64_t n, double* __restrict__ dst) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    dst[k] = src[2 * k];
+}
+
 // h[i] += sum_k conj(V[i, k]) w[k] for i < m (FP64); h is interleaved complex, pre-zeroed.
 __global__ void __launch_bounds__(256) dots_kernel(const double* __restrict__ V, const double* __restrict__ w,
                                                    int64_t n, int m, double* __restrict__ h) {
@@ -282,7 +397,14 @@ struct GmresHost {
     double* hbuf;                // [2 (m+1)]
 };
 
-static int gmres_core(const float* z, int64_t n, const double* b, double* x, int m, int max_iters,
+// The system matrix: complex64 (kind 0, the RWG impedance matrix), real float32 (1) or real
+// float64 (2).
+struct GmresMatrix {
+    int kind;
+    const void* a;
+};
+
+static int gmres_core(const GmresMatrix& A, int64_t n, const double* b, double* x, int m, int max_iters,
                       double tol, void* workspace, const GmresHost& hs, int64_t* iters_out,
                       int64_t* cycles_out, double* relres_out, int* status_out, cudaStream_t s);
 
@@ -297,11 +419,39 @@ int gmres_c64(const float* z, int64_t n, const double* b, double* x, int m, int 
     std::vector<std::complex<double>> H((size_t)(m + 1) * m), cs(m), sn(m), gvec(m + 1), hcol(m + 2), yv(m);
     std::vector<double> hbuf(2 * (m + 1));
     const GmresHost hs{H.data(), cs.data(), sn.data(), gvec.data(), hcol.data(), yv.data(), hbuf.data()};
-    return gmres_core(z, n, b, x, m, max_iters, tol, workspace, hs, iters_out, cycles_out, relres_out,
-                      status_out, s);
+    return gmres_core(GmresMatrix{0, z}, n, b, x, m, max_iters, tol, workspace, hs, iters_out, cycles_out,
+                      relres_out, status_out, s);
 }
 
-static int gmres_core(const float* z, int64_t n, const double* b, double* x, int m, int max_iters,
+// Real system A x = b (A float32 or float64 [n, n]; b, x float64 [n]).  The complex core
+// runs on complex copies of b and x kept after the complex workspace.
+size_t gmres_real_workspace_bytes(int64_t n, int m) { return gmres_ws_bytes(n, m) + 2 * al256(16 * (size_t)n); }
+
+int gmres_real(int kind, const void* a, int64_t n, const double* b, double* x, int m, int max_iters, double tol,
+               void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out, double* relres_out,
+               int* status_out, cudaStream_t s) {
+    if (n <= 0) return set_error(MB_ERR_ARG, "n must be > 0");
+    if (m < 1 || m > kGmresMaxRestart) return set_error(MB_ERR_ARG, "restart must be in [1, %d]", kGmresMaxRestart);
+    if (max_iters < 1) return set_error(MB_ERR_ARG, "max_iters must be >= 1");
+    if (!(tol > 0)) return set_error(MB_ERR_ARG, "tol must be > 0");
+    if (ws_bytes < gmres_real_workspace_bytes(n, m)) return set_error(MB_ERR_ARG, "workspace too small");
+    char* extra = static_cast<char*>(workspace) + gmres_ws_bytes(n, m);
+    double* bc = reinterpret_cast<double*>(extra);
+    double* xc = reinterpret_cast<double*>(extra + al256(16 * (size_t)n));
+    const unsigned vb = (unsigned)((n + 255) / 256);
+    real_to_c128_kernel<<<vb, 256, 0, s>>>(b, n, bc);
+    real_to_c128_kernel<<<vb, 256, 0, s>>>(x, n, xc);
+    std::vector<std::complex<double>> H((size_t)(m + 1) * m), cs(m), sn(m), gvec(m + 1), hcol(m + 2), yv(m);
+    std::vector<double> hbuf(2 * (m + 1));
+    const GmresHost hs{H.data(), cs.data(), sn.data(), gvec.data(), hcol.data(), yv.data(), hbuf.data()};
+    int rc = gmres_core(GmresMatrix{kind, a}, n, bc, xc, m, max_iters, tol, workspace, hs, iters_out, cycles_out,
+                        relres_out, status_out, s);
+    if (rc) return rc;
+    c128_real_part_kernel<<<vb, 256, 0, s>>>(xc, n, x);
+    return sync_check(s, "gmres real result");
+}
+
+static int gmres_core(const GmresMatrix& A, int64_t n, const double* b, double* x, int m, int max_iters,
                       double tol, void* workspace, const GmresHost& hs, int64_t* iters_out,
                       int64_t* cycles_out, double* relres_out, int* status_out, cudaStream_t s) {
     GmresWork g = carve(workspace, n, m);
@@ -323,7 +473,12 @@ static int gmres_core(const float* z, int64_t n, const double* b, double* x, int
     int status = 1;
     while (true) {
         // FP64 residual of the current iterate
-        residual_c128_kernel<<<rblocks, 256, 0, s>>>(z, x, b, n, g.r);
+        if (A.kind == 0)
+            residual_c128_kernel<<<rblocks, 256, 0, s>>>(static_cast<const float*>(A.a), x, b, n, g.r);
+        else if (A.kind == 1)
+            residual_real_kernel<float><<<rblocks, 256, 0, s>>>(static_cast<const float*>(A.a), x, b, n, g.r);
+        else
+            residual_real_kernel<double><<<rblocks, 256, 0, s>>>(static_cast<const double*>(A.a), x, b, n, g.r);
         double beta;
         if ((rc = norm_of(g.r, n, g.nrm, &beta, s))) return rc;
         relres = beta / bnorm;
@@ -338,7 +493,13 @@ static int gmres_core(const float* z, int64_t n, const double* b, double* x, int
         gvec[0] = beta;
         int j = 0;
         for (; j < m && iters < max_iters; ++j, ++iters) {
-            matvec_c64_kernel<<<rblocks, 256, 0, s>>>(z, g.v32, n, g.w);
+            if (A.kind == 0)
+                matvec_c64_kernel<<<rblocks, 256, 0, s>>>(static_cast<const float*>(A.a), g.v32, n, g.w);
+            else if (A.kind == 1)
+                matvec_r32_kernel<<<rblocks, 256, 0, s>>>(static_cast<const float*>(A.a), g.v32, n, g.w);
+            else
+                matvec_r64_kernel<<<rblocks, 256, 0, s>>>(static_cast<const double*>(A.a),
+                                                          g.V + 2 * (int64_t)j * n, n, g.w);
             // CGS2: two passes of h = V^H w; w -= V h
             std::complex<double>* hcol = hs.hcol;
             for (int i = 0; i < j + 2; ++i) hcol[i] = 0.0;
@@ -473,7 +634,8 @@ int gmres_c64_noalloc(const float* z, int64_t n, const double* b, double* x, int
     const GmresHost hs{reinterpret_cast<cd*>(tl_H), reinterpret_cast<cd*>(tl_cs), reinterpret_cast<cd*>(tl_sn),
                        reinterpret_cast<cd*>(tl_g), reinterpret_cast<cd*>(tl_hcol), reinterpret_cast<cd*>(tl_y),
                        tl_hbuf};
-    return gmres_core(z, n, b, x, m, max_iters, tol, ws, hs, iters_out, cycles_out, relres_out, status_out, s);
+    return gmres_core(GmresMatrix{0, z}, n, b, x, m, max_iters, tol, ws, hs, iters_out, cycles_out, relres_out,
+                      status_out, s);
 }
 
 int launch_matvec_c64(const float* z, const float* v, int64_t n, double* y, cudaStream_t s) {

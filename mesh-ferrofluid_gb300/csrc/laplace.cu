@@ -216,6 +216,57 @@ template int launch_pack_tight<float>(const float*, const float*, const int32_t*
 template int launch_pack_tight<double>(const double*, const double*, const int32_t*, int64_t, int64_t,
                                        int, double*, cudaStream_t);
 
+// Hypersingular operator of the Laplace problem, P1 Galerkin, by Maue's integration by parts
+// (J.-C. Nedelec 1982; O. Steinbach, Numerical Approximation Methods for Elliptic Boundary
+// Value Problems, 2008, Thm 6.17):
+//   <D phi_j, phi_i> = int int G(x, y) curl phi_j(y) . curl phi_i(x)  dS_y dS_x,
+// and on a flat triangle (p0, p1, p2) with area A the surface curl n x grad phi_a of the P1
+// hat function of vertex a is the constant (p_{a+1} - p_{a+2}) / (2 A).  So every face pair
+// contributes curl_a(fy) . curl_b(fx) times the P0 single-layer integral V0[fy, fx].
+// One thread per face pair; out[fy, fx, a, b] (same layout as the single / double layer).
+template <typename T>
+__device__ __forceinline__ void face_curls(const T* verts, const int32_t* faces, int64_t f, V3<T> c[3]) {
+    const V3<T> p0 = load3(verts, faces[3 * f]), p1 = load3(verts, faces[3 * f + 1]),
+                p2 = load3(verts, faces[3 * f + 2]);
+    const V3<T> nr = cross(p1 - p0, p2 - p1);
+    const T inv2a = T(1) / sqrt_t(dot(nr, nr));  // 1 / (2 A)
+    c[0] = inv2a * (p1 - p2);
+    c[1] = inv2a * (p2 - p0);
+    c[2] = inv2a * (p0 - p1);
+}
+
+template <typename T>
+__global__ void hypersingular_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces, int64_t nf,
+                                     const T* __restrict__ v0, T* __restrict__ out) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nf * nf) return;
+    const int64_t fy = idx / nf, fx = idx % nf;
+    V3<T> cy[3], cx[3];
+    face_curls(verts, faces, fy, cy);
+    face_curls(verts, faces, fx, cx);
+    const T w = v0[idx];
+    T* o = out + 9 * idx;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) o[3 * a + b] = dot(cy[a], cx[b]) * w;
+}
+
+template <typename T>
+int launch_hypersingular(const T* verts, const int32_t* faces, int64_t nf, const T* v0, T* out,
+                         cudaStream_t stream) {
+    if (nf <= 0) return MB_OK;
+    const int threads = 256;
+    const int64_t blocks = (nf * nf + threads - 1) / threads;
+    if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "mesh too large for one launch");
+    hypersingular_kernel<T><<<(unsigned)blocks, threads, 0, stream>>>(verts, faces, nf, v0, out);
+    return check_launch("hypersingular");
+}
+template int launch_hypersingular<float>(const float*, const int32_t*, int64_t, const float*, float*,
+                                         cudaStream_t);
+template int launch_hypersingular<double>(const double*, const int32_t*, int64_t, const double*, double*,
+                                          cudaStream_t);
+
 // compute_panel_relation (src/utils/mesh_utils.py:700-725): shared-vertex count per pair.
 __global__ void panel_relation_kernel(const int32_t* __restrict__ faces, int64_t nf,
                                       uint8_t* __restrict__ rel) {

@@ -20,21 +20,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "closed_form.cuh"
 #include "common.cuh"
 
 namespace mb {
-
-// 7-point rule: barycentric coordinates and weights (sum 1), from the closed forms
-// a = (6 -+ sqrt 15)/21, w = (155 -+ sqrt 15)/1200, centroid weight 9/40.
-__constant__ double c_d7[7][4] = {
-    {0.33333333333333333, 0.33333333333333333, 0.33333333333333333, 0.225},
-    {0.10128650732345634, 0.10128650732345634, 0.79742698535308732, 0.12593918054482715},
-    {0.10128650732345634, 0.79742698535308732, 0.10128650732345634, 0.12593918054482715},
-    {0.79742698535308732, 0.10128650732345634, 0.10128650732345634, 0.12593918054482715},
-    {0.47014206410511509, 0.47014206410511509, 0.05971587178976982, 0.13239415278850619},
-    {0.47014206410511509, 0.05971587178976982, 0.47014206410511509, 0.13239415278850619},
-    {0.05971587178976982, 0.47014206410511509, 0.47014206410511509, 0.13239415278850619},
-};
 
 template <typename T>
 __device__ __forceinline__ void add_c(T* p, T re, T im);
@@ -161,36 +150,6 @@ __global__ void __launch_bounds__(128) mom_sym_regular_kernel(const T* __restric
 // ---------------------------------------------------------------------------------------
 // pairs sharing a vertex: FP64 with the singular part in closed form; one thread per pair
 // ---------------------------------------------------------------------------------------
-__device__ void potential_integrals(const V3<double>& x, const V3<double> P[3], double* I1, V3<double>* Iv) {
-    V3<double> n = cross(P[1] - P[0], P[2] - P[1]);
-    n = (1.0 / sqrt(dot(n, n))) * n;
-    const double d = dot(x - P[0], n);
-    const V3<double> rho = x - d * n;
-    const double ad = fabs(d);
-    double s1 = 0.0;
-    V3<double> sv = v3<double>(0, 0, 0);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const V3<double> pm = P[i], pp = P[(i + 1) % 3];
-        V3<double> l = pp - pm;
-        l = (1.0 / sqrt(dot(l, l))) * l;
-        const V3<double> u = cross(l, n);
-        const double lp = dot(pp - rho, l), lm = dot(pm - rho, l);
-        const double p0 = dot(pp - rho, u);
-        const double r0sq = p0 * p0 + d * d;
-        const double rp = sqrt(r0sq + lp * lp), rm = sqrt(r0sq + lm * lm);
-        double lg;
-        if ((lm >= 0.0 || lp >= 0.0) && rm + lm > 0.0)
-            lg = log((rp + lp) / (rm + lm));
-        else
-            lg = log((rm - lm) / (rp - lp));
-        s1 += p0 * lg - ad * (atan2(p0 * lp, r0sq + ad * rp) - atan2(p0 * lm, r0sq + ad * rm));
-        sv = sv + (0.5 * (r0sq * lg + lp * rp - lm * rm)) * u;
-    }
-    *I1 = s1;
-    *Iv = sv - (d * s1) * n;
-}
-
 template <typename T>
 __global__ void mom_sym_near_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces,
                                     const int32_t* __restrict__ fei, int64_t n_edges,

@@ -4,14 +4,20 @@ Mirrors the reference's layer classes and the integration routine they share:
 
 * ``double_integration_on_panels_3d`` (src/mesh_BEM/utils/integrations_3d.py:252-452) --
   same signature and result ([F_y, F_x, nphi, nphi]); the O(F^2 * rule) work runs in the
-  sm_103a panel kernel (``mb_laplace_panels_*``);
-* ``SingleLayer3d`` / ``DoubleLayer3d`` (single_layer/single_layer_3d.py:43-68,
-  double_layer/double_layer_3d.py:43-68, abstract layers :17-98) with ``compute_Vmat`` /
-  ``compute_Kmat``, ``get_*mat_unpacked`` and ``get_*mat_tight``;
-* ``RhsLayer3d.compute_rhs`` (rhs_layer/rhs_layer_3d.py:74-203), Dirichlet branch
-  gk = 1/2 f |A_v| + K^T f.  Mixed/Neumann data need the hypersingular operator, which the
-  reference never implemented (integrations_3d.py:440-442); they raise
-  NotImplementedError here instead of crashing on an attribute of ``None``.
+  sm_103a panel kernel (``mb_laplace_panels_*``).  ``layer_type`` HYPERSINGULAR, which
+  the reference leaves unimplemented (:440-442), returns the P1 hypersingular operator by
+  Maue's formula from the P0 single layer of the same rule (``mb_laplace_hypersingular_*``);
+* ``SingleLayer3d`` / ``DoubleLayer3d`` / ``HyperSingularLayer3d`` (single_layer_3d.py:43-68,
+  double_layer_3d.py:43-68, hypersingular_layer_3d.py, abstract layers :17-98) with
+  ``compute_*mat``, ``get_*mat_unpacked`` and ``get_*mat_tight``;
+* ``RhsLayer3d.compute_rhs`` (rhs_layer/rhs_layer_3d.py:74-203) for Dirichlet, Neumann and
+  mixed data.
+
+Every layer takes ``rule``: ``"reference"`` (the reference's collapsed Gauss rule, results
+equal to the reference's) or ``"dunavant7"`` (7-point rule, singular and near-singular
+pairs in closed form, ``mb_laplace_sym_*``), which is accurate enough for the Neumann and
+mixed problems (the reference rule's P0 single layer makes the hypersingular operator
+indefinite on coarse meshes).
 """
 from __future__ import annotations
 
@@ -41,7 +47,14 @@ def double_integration_on_panels_3d(BEM_type: int, order_type: int, verts: torch
                                     layer_type: int = int(LayerType.SINGLE_LAYER)) -> torch.Tensor:
     """[F_y, F_x, nphi, nphi] panel integrals; ``panel_relations`` may be None (derived)."""
     if layer_type == int(LayerType.HYPERSINGULAR_LAYER):
-        raise NotImplementedError("Not implemented for hypersingular")
+        if BEMType.belong_Helmholtz(BEM_type):
+            raise NotImplementedError("hypersingular operator: Laplace only")
+        if int(order_type) != int(OrderType.LINEAR):
+            raise ValueError("the hypersingular operator needs P1 (OrderType.LINEAR) functions")
+        v0 = double_integration_on_panels_3d(BEM_type, int(OrderType.PLANAR), verts, faces, face_areas,
+                                             face_normals, gauss_weightsx, gauss_weightsy, rands_x, rands_y,
+                                             panel_relations, wavenumber, int(LayerType.SINGLE_LAYER))
+        return hypersingular_from_v0(verts, faces.to(torch.int32).contiguous(), v0)
     if layer_type not in (int(LayerType.SINGLE_LAYER), int(LayerType.DOUBLE_LAYER)):
         raise ValueError(f"unknown layer_type {layer_type}")
     _lib.check_tensor(verts, "verts", dtype=(torch.float32, torch.float64), ndim=2)
@@ -75,12 +88,102 @@ def double_integration_on_panels_3d(BEM_type: int, order_type: int, verts: torch
     return torch.complex(out_r, out_i) if kind == 1 else out_r
 
 
+def hypersingular_from_v0(verts: torch.Tensor, faces: torch.Tensor, v0: torch.Tensor) -> torch.Tensor:
+    """P1 hypersingular panels [F, F, 3, 3] from P0 single-layer panels v0 [F, F(, 1, 1)]."""
+    _lib.check_tensor(verts, "verts", dtype=(torch.float32, torch.float64), ndim=2)
+    nf = faces.shape[0]
+    v0 = v0.reshape(nf, nf).to(verts.dtype).contiguous()
+    _lib.check_tensor(faces, "faces", dtype=torch.int32, device=verts.device, ndim=2)
+    out = torch.empty((nf, nf, 3, 3), dtype=verts.dtype, device=verts.device)
+    _lib.call(f"mb_laplace_hypersingular_{_lib.sfx(verts.dtype)}", _lib.ptr(verts), verts.shape[0],
+              _lib.ptr(faces), nf, _lib.ptr(v0), _lib.ptr(out), _lib.stream_of(verts))
+    return out
+
+
+def laplace_near_pairs(faces: torch.Tensor) -> torch.Tensor:
+    """Ordered face pairs sharing a vertex (incl. self), [n, 2] int32, sorted by first face."""
+    from .utils import compute_panel_relation
+
+    return torch.nonzero(compute_panel_relation(faces) > 0).to(torch.int32).contiguous()
+
+
+def laplace_sym_panels(verts: torch.Tensor, faces: torch.Tensor, layer: int, order: int,
+                       near: torch.Tensor | None = None, rows=None, out=None) -> torch.Tensor:
+    """Symmetric-rule Galerkin panels [F_y, F_x, nphi, nphi] (``mb_laplace_sym_*``).
+
+    layer 1: single layer 1/(4 pi R); 2: double layer n_y.(x - y)/(4 pi R^3) with the
+    normal of the first ("y") face, as ``double_integration_on_panels_3d``.
+    """
+    _lib.check_tensor(verts, "verts", dtype=(torch.float32, torch.float64), ndim=2)
+    faces = faces.to(torch.int32).contiguous()
+    _lib.check_tensor(faces, "faces", device=verts.device, ndim=2)
+    nf = faces.shape[0]
+    check_face_range(faces, verts.shape[0])
+    if near is None:
+        near = laplace_near_pairs(faces)
+    _lib.check_tensor(near, "near", dtype=torch.int32, device=verts.device)
+    r0, r1 = (0, nf) if rows is None else rows
+    nphi = 3 if int(order) == int(OrderType.LINEAR) else 1
+    shape = (r1 - r0, nf, nphi, nphi)
+    if out is None:
+        out = torch.empty(shape, dtype=verts.dtype, device=verts.device)
+    else:
+        _lib.check_tensor(out, "out", dtype=verts.dtype, device=verts.device, shape=shape)
+    _lib.call(f"mb_laplace_sym_{_lib.sfx(verts.dtype)}", _lib.ptr(verts), verts.shape[0], _lib.ptr(faces), nf,
+              int(layer), 1 if nphi == 3 else 0, _lib.ptr(near), near.shape[0], r0, r1, _lib.ptr(out),
+              _lib.stream_of(verts))
+    return out
+
+
+def laplace_colloc_sl(verts: torch.Tensor, faces: torch.Tensor, rows=None, out=None,
+                      near: torch.Tensor | None = None, check_indices: bool = True) -> torch.Tensor:
+    """Single-layer collocation matrix [F, F] at face centroids (``mb_laplace_colloc_sl_*``).
+
+    ``near``: the pairs sharing a vertex (``laplace_near_pairs(faces)``), computed when None.
+    """
+    _lib.check_tensor(verts, "verts", dtype=(torch.float32, torch.float64), ndim=2)
+    faces = faces.to(torch.int32).contiguous()
+    _lib.check_tensor(faces, "faces", device=verts.device, ndim=2)
+    nf = faces.shape[0]
+    if check_indices:
+        check_face_range(faces, verts.shape[0])
+    if near is None:
+        near = laplace_near_pairs(faces)
+    _lib.check_tensor(near, "near", dtype=torch.int32, device=verts.device)
+    r0, r1 = (0, nf) if rows is None else rows
+    if out is None:
+        out = torch.empty((r1 - r0, nf), dtype=verts.dtype, device=verts.device)
+    else:
+        _lib.check_tensor(out, "out", dtype=verts.dtype, device=verts.device, shape=(r1 - r0, nf))
+    _lib.call(f"mb_laplace_colloc_sl_{_lib.sfx(verts.dtype)}", _lib.ptr(verts), verts.shape[0], _lib.ptr(faces),
+              nf, _lib.ptr(near), near.shape[0], r0, r1, _lib.ptr(out), _lib.stream_of(verts))
+    return out
+
+
+def p1_mass_apply(verts: torch.Tensor, faces: torch.Tensor, g: torch.Tensor) -> torch.Tensor:
+    """(M g) with the consistent P1 mass matrix M_ij = int phi_i phi_j; g [V, k] -> [V, k]."""
+    from .utils import compute_face_areas
+
+    f = faces.to(torch.int64)
+    a = compute_face_areas(vertices=verts, faces=faces, keepdim=True).to(g.dtype)  # [F, 1]
+    gv = g[f]  # [F, 3, k]
+    s = gv.sum(1, keepdim=True)  # [F, 1, k]
+    loc = (gv + s) * (a[:, :, None] / 12.0)  # A/12 (2 g_i + g_j + g_k)
+    out = torch.zeros_like(g)
+    out.index_add_(0, f.reshape(-1), loc.reshape(-1, g.shape[1]))
+    return out
+
+
 class _AbstractLayer:
     rank = 3
     layer_type = int(LayerType.SINGLE_LAYER)
 
     def __init__(self, gaussQR: int, order_type: int, BEM_type: int, wavenumber: float, logger,
-                 dtype: torch.dtype = torch.float32, device: torch.device = torch.device("cpu")):
+                 dtype: torch.dtype = torch.float32, device: torch.device = torch.device("cpu"),
+                 rule: str = "reference"):
+        if rule not in ("reference", "dunavant7"):
+            raise ValueError(f"unknown rule {rule!r} (reference or dunavant7)")
+        self.rule = rule
         self._gaussQR = gaussQR
         self._order_type = order_type
         self._BEM_type = BEM_type
@@ -102,6 +205,15 @@ class _AbstractLayer:
     wavenumber = property(lambda self: self._wavenumber)
 
     def _compute(self, verts, faces, face_areas, face_normals, panel_relations):
+        if self.rule == "dunavant7":
+            if BEMType.belong_Helmholtz(self.BEM_type):
+                raise NotImplementedError("rule dunavant7: Laplace kernels only")
+            near = None
+            if panel_relations is not None:
+                near = torch.nonzero(panel_relations > 0).to(torch.int32).contiguous()
+            self._unpacked = self._sym(verts, faces, near)
+            self.initialized = True
+            return
         rands = torch.cat((self.r1, self.r2), dim=-1)
         self._unpacked = double_integration_on_panels_3d(
             BEM_type=self.BEM_type, order_type=self.order_type, verts=verts, faces=faces,
@@ -120,6 +232,9 @@ class _AbstractLayer:
 class SingleLayer3d(_AbstractLayer):
     layer_type = int(LayerType.SINGLE_LAYER)
 
+    def _sym(self, verts, faces, near):
+        return laplace_sym_panels(verts, faces, 1, self.order_type, near)
+
     def compute_Vmat(self, verts, faces, face_areas, face_normals, panel_relations=None):
         self._compute(verts, faces, face_areas, face_normals, panel_relations)
 
@@ -133,6 +248,9 @@ class SingleLayer3d(_AbstractLayer):
 class DoubleLayer3d(_AbstractLayer):
     layer_type = int(LayerType.DOUBLE_LAYER)
 
+    def _sym(self, verts, faces, near):
+        return laplace_sym_panels(verts, faces, 2, self.order_type, near)
+
     def compute_Kmat(self, verts, faces, face_areas, face_normals, panel_relations=None):
         self._compute(verts, faces, face_areas, face_normals, panel_relations)
 
@@ -143,12 +261,34 @@ class DoubleLayer3d(_AbstractLayer):
         return self._tight(verts, faces)
 
 
+class HyperSingularLayer3d(_AbstractLayer):
+    """P1 hypersingular operator (the reference declares the class but never computes it)."""
+
+    layer_type = int(LayerType.HYPERSINGULAR_LAYER)
+
+    def _sym(self, verts, faces, near):
+        if int(self.order_type) != int(OrderType.LINEAR):
+            raise ValueError("the hypersingular operator needs P1 (OrderType.LINEAR) functions")
+        v0 = laplace_sym_panels(verts, faces, 1, int(OrderType.PLANAR), near)
+        return hypersingular_from_v0(verts, faces.to(torch.int32).contiguous(), v0)
+
+    def compute_Dmat(self, verts, faces, face_areas, face_normals, panel_relations=None):
+        self._compute(verts, faces, face_areas, face_normals, panel_relations)
+
+    def get_Dmat_unpacked(self):
+        return self._unpacked
+
+    def get_Dmat_tight(self, verts, faces):
+        return self._tight(verts, faces)
+
+
 class RhsLayer3d:
     rank = 3
 
     def __init__(self, parent, gaussQR: int, order_type: int, BEM_type: int, wavenumber: float,
-                 logger, dtype=torch.float32, device=torch.device("cpu")):
+                 logger, dtype=torch.float32, device=torch.device("cpu"), rule: str = "reference"):
         self.parent = parent
+        self.rule = rule
         self._gaussQR = gaussQR
         self._order_type = order_type
         self._BEM_type = BEM_type
@@ -169,35 +309,61 @@ class RhsLayer3d:
     BEM_type = property(lambda self: self._BEM_type)
     wavenumber = property(lambda self: self._wavenumber)
 
-    def compute_rhs(self, verts, faces, vert_bc_Dirichlet, vert_bc_Neumann, vert_bc_flags,
-                    K_tight=None):
-        """rhs [B, V, 1]: Dirichlet data f -> 1/2 f |A_v| + K^T f (rhs_layer_3d.py:122-160).
+    def _mass(self, verts, faces, g):
+        if self.rule == "dunavant7":
+            return p1_mass_apply(verts, faces, g)
+        return g * compute_vert_areas(vertices=verts, faces=faces, keepdim=True).to(g.dtype)
 
-        K^T f equals the reference's unpacked contraction
-        ``(K[fy, fx, a, b] * f[faces[fy, a]]).sum(fy, a)`` scattered to faces[fx, b], taken on
-        the packed K.  ``K_tight`` defaults to the parent's packed double layer.
+    def compute_rhs(self, verts, faces, vert_bc_Dirichlet, vert_bc_Neumann, vert_bc_flags,
+                    K_tight=None, V_tight=None, D_tight=None):
+        """rhs [B, V, 1] of the direct formulation (rhs_layer_3d.py:74-203).
+
+        With g the Dirichlet data (zero off Gamma_D), f the Neumann data (zero off Gamma_N),
+        M the mass matrix (lumped vertex areas for the reference rule, as the reference;
+        the consistent P1 mass matrix for rule dunavant7) and K = K_tight^T the Galerkin
+        double layer <phi_i, K phi_j>:
+            Dirichlet rows:  1/2 M g + K g - V f
+            Neumann rows:    1/2 M f - K^T f - D g
+        (O. Steinbach, Numerical Approximation Methods for Elliptic Boundary Value Problems,
+        2008, sec. 7.4).  Each vertex carries the row of its own boundary type.  The
+        reference's Neumann rows use K f instead of K^T f and never run (its hypersingular
+        layer is None).  The matrices default to the parent's layers.
         """
         batch = vert_bc_Dirichlet.shape[0]
-        vert_areas = compute_vert_areas(vertices=verts, faces=faces, keepdim=True)  # [V, 1]
+        P = self.parent
         if K_tight is None:
-            K_tight = self.parent.double_layer.get_Kmat_tight(verts=verts, faces=faces)
+            K_tight = P.double_layer.get_Kmat_tight(verts=verts, faces=faces)
         out = []
         for b in range(batch):
-            is_d = vert_bc_flags[b] == int(BoundaryType.DIRICHLET)
-            is_n = vert_bc_flags[b] == int(BoundaryType.NEUMANN)
-            if int(is_n.sum()) > 0:
-                raise NotImplementedError(
-                    "Neumann / mixed boundary data need the hypersingular operator, which the "
-                    "reference does not implement (integrations_3d.py:440-442)")
-            if int(is_d.sum()) == 0:
+            is_d = (vert_bc_flags[b] == int(BoundaryType.DIRICHLET)).reshape(-1)
+            is_n = (vert_bc_flags[b] == int(BoundaryType.NEUMANN)).reshape(-1)
+            n_d, n_n = int(is_d.sum()), int(is_n.sum())
+            if n_d + n_n == 0:
                 raise ValueError("no boundary data")
-            f = vert_bc_Dirichlet[b].to(K_tight.dtype)  # [V, 1]
-            gk1 = 0.5 * vert_bc_Dirichlet[b] * vert_areas
-            gk2 = K_tight.transpose(0, 1) @ f
-            gk = gk1 + gk2
-            if self.BEM_type == int(BEMType.HELMHOLTZ_MOM):
-                gk = gk1 * 2
-            out.append(gk)
+            g = torch.where(is_d[:, None], vert_bc_Dirichlet[b].reshape(-1, 1), 0).to(K_tight.dtype)
+            f = torch.where(is_n[:, None], vert_bc_Neumann[b].reshape(-1, 1), 0).to(K_tight.dtype)
+            rhs = torch.zeros_like(g)
+            if n_d:
+                gk1 = 0.5 * self._mass(verts, faces, g)
+                gk = gk1 + K_tight.transpose(0, 1) @ g
+                if n_n:
+                    Vt = V_tight if V_tight is not None else P.single_layer.get_Vmat_tight(verts=verts,
+                                                                                            faces=faces)
+                    gk = gk - Vt @ f
+                if self.BEM_type == int(BEMType.HELMHOLTZ_MOM):
+                    gk = gk1 * 2
+                rhs = torch.where(is_d[:, None], gk, rhs)
+            if n_n:
+                fi1 = 0.5 * self._mass(verts, faces, f)
+                fi = fi1 - K_tight @ f
+                if n_d:
+                    Dt = D_tight if D_tight is not None else P.hypersingular_layer.get_Dmat_tight(
+                        verts=verts, faces=faces)
+                    fi = fi - Dt @ g
+                if self.BEM_type == int(BEMType.HELMHOLTZ_MOM):
+                    fi = fi1 * 2
+                rhs = torch.where(is_n[:, None], fi, rhs)
+            out.append(rhs)
         self.rhs_vec = torch.stack(out, dim=0)
         self.initialized = True
 

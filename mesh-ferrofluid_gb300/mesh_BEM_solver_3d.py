@@ -11,9 +11,14 @@ Same constructor and public methods as ``src/mesh_BEM/mesh_BEM_solver_3d.py:31-3
   ``torch.linalg.solve`` as in the reference (:174); the interpolation and vertex scatter
   are one kernel (``interpolate_vert_js``).
 * ``solve(verts, faces, vert_bc_Dirichlet, vert_bc_Neumann, vert_bc_flags, Amat_scaler=None)
-  -> (Neumann [B, V, 1], Dirichlet [B, V, 1])`` (:197-373) for all-Dirichlet data, the only
-  boundary case the reference can run (mixed and Neumann data need its unimplemented
-  hypersingular layer).
+  -> (Neumann [B, V, 1], Dirichlet [B, V, 1])`` (:197-373) for Dirichlet, Neumann and mixed
+  vertex data.  The reference runs only the all-Dirichlet case (its hypersingular layer is
+  None); here the Neumann and mixed cases use ``HyperSingularLayer3d`` and the block
+  system of the reference's layout [[V, -K], [K^T, D]] (:306-341) with the masks taken
+  from ``vert_bc_flags`` (the reference builds them from the data values) and the rows of
+  the right-hand side matched to the unknowns.  The pure Neumann matrix D is singular
+  (constants); it is solved as D + a a^T with a_i = int phi_i (solution of zero mean for
+  compatible data).  For these cases use ``rule="dunavant7"``.
 
 Extra keyword ``solver`` selects "lu" (reference behaviour, ``torch.linalg.solve``) or
 "gmres" (``mb_gmres_c64``: FP32 matrix-vector products on the complex64 matrix, FP64
@@ -30,7 +35,7 @@ from typing import List
 
 import torch
 
-from .layers import DoubleLayer3d, RhsLayer3d, SingleLayer3d
+from .layers import DoubleLayer3d, HyperSingularLayer3d, RhsLayer3d, SingleLayer3d
 from .mesh_MOM_3d import (
     assemble_rhs_rwg,
     assemble_rhs_rwg_sym,
@@ -75,11 +80,11 @@ class MeshBEMSolver3d:
         if rule not in ("reference", "dunavant7"):
             raise ValueError(f"unknown rule {rule!r}")
         self.rule = rule
-        self.hypersingular_layer = None
         kw = dict(gaussQR=gaussQR, order_type=order_type, BEM_type=BEM_type, wavenumber=wavenumber,
-                  logger=logger, dtype=dtype, device=self.device)
+                  logger=logger, dtype=dtype, device=self.device, rule=rule)
         self.single_layer = SingleLayer3d(**kw)
         self.double_layer = DoubleLayer3d(**kw)
+        self.hypersingular_layer = HyperSingularLayer3d(**kw)
         self.rhs_layer = RhsLayer3d(parent=self, **kw)
         self.gaussian_points_1d_x, self.gaussian_weights_1d_x = \
             get_gaussion_integration_points_and_weights(gaussQR, device=self.device, dtype=dtype)
@@ -150,29 +155,63 @@ class MeshBEMSolver3d:
         normals = compute_face_normals(vertices=verts, faces=faces).contiguous()
         panel_relations = compute_panel_relation(faces)
         neu_list, dir_list = [], []
-        V_tight = None
+        mats = {}
+
+        def tight(name):
+            if name not in mats:
+                if name == "V":
+                    self.single_layer.compute_Vmat(verts, faces, areas, normals, panel_relations)
+                    mats[name] = self.single_layer.get_Vmat_tight(verts=verts, faces=faces)
+                elif name == "K":
+                    self.double_layer.compute_Kmat(verts, faces, areas, normals, panel_relations)
+                    mats[name] = self.double_layer.get_Kmat_tight(verts=verts, faces=faces)
+                else:
+                    self.hypersingular_layer.compute_Dmat(verts, faces, areas, normals, panel_relations)
+                    mats[name] = self.hypersingular_layer.get_Dmat_tight(verts=verts, faces=faces)
+            return mats[name]
+
         for b in range(batch):
-            is_d = vert_bc_flags[b] == int(BoundaryType.DIRICHLET)
-            is_n = vert_bc_flags[b] == int(BoundaryType.NEUMANN)
+            is_d = (vert_bc_flags[b] == int(BoundaryType.DIRICHLET)).reshape(-1)
+            is_n = (vert_bc_flags[b] == int(BoundaryType.NEUMANN)).reshape(-1)
             n_d, n_n = int(is_d.sum()), int(is_n.sum())
             self.InfoLog(f"Batch [{b}]: (Vertex attached) number of Dirichlet B.C. = {n_d}, "
                          f"number of Neumann B.C. = {n_n}, number of whole zone = "
                          f"{vert_bc_flags[b].numel()}")
-            if n_n > 0:
-                raise NotImplementedError(
-                    "Neumann / mixed boundary data need the hypersingular operator, which the "
-                    "reference does not implement (integrations_3d.py:440-442)")
-            if V_tight is None:
-                self.single_layer.compute_Vmat(verts, faces, areas, normals, panel_relations)
-                V_tight = self.single_layer.get_Vmat_tight(verts=verts, faces=faces)
-                self.double_layer.compute_Kmat(verts, faces, areas, normals, panel_relations)
-                K_tight = self.double_layer.get_Kmat_tight(verts=verts, faces=faces)
-            self.rhs_layer.compute_rhs(verts, faces, vert_bc_Dirichlet[b:b + 1],
-                                       vert_bc_Neumann[b:b + 1], vert_bc_flags[b:b + 1],
-                                       K_tight=K_tight)
+            if n_d + n_n == 0:
+                raise ValueError("no boundary data")
+            K = tight("K")
+            V = tight("V") if n_d else None
+            D = tight("D") if n_n and self.BEM_type != int(BEMType.HELMHOLTZ_MOM) else None
+            self.rhs_layer.compute_rhs(verts, faces, vert_bc_Dirichlet[b:b + 1], vert_bc_Neumann[b:b + 1],
+                                       vert_bc_flags[b:b + 1], K_tight=K, V_tight=V, D_tight=D)
             rhs = self.rhs_layer.get_rhs_vec().reshape(-1)
-            A = V_tight if Amat_scaler is None else Amat_scaler * V_tight
-            sol = torch.linalg.solve(A, rhs.to(A.dtype))
-            neu_list.append(sol.reshape(n_verts, 1))
-            dir_list.append(vert_bc_Dirichlet[b].reshape(n_verts, 1))
+            neu = vert_bc_Neumann[b].reshape(n_verts, 1).clone()
+            dirv = vert_bc_Dirichlet[b].reshape(n_verts, 1).clone()
+            if n_n == 0:
+                A = V
+            elif n_d == 0:
+                if self.BEM_type == int(BEMType.HELMHOLTZ_MOM):
+                    A = K.clone()
+                    va = compute_vert_areas(vertices=verts, faces=faces).reshape(-1).to(K.dtype)
+                    A[torch.arange(n_verts), torch.arange(n_verts)] = -0.5 * va
+                else:
+                    a = compute_vert_areas(vertices=verts, faces=faces).reshape(-1, 1).to(D.dtype)
+                    A = D + a @ a.T
+            else:
+                ks = K.transpose(0, 1)  # Galerkin <phi_i, K phi_j>
+                A = torch.cat((torch.cat((V[is_d][:, is_d], -ks[is_d][:, is_n]), 1),
+                               torch.cat((ks.transpose(0, 1)[is_n][:, is_d], D[is_n][:, is_n]), 1)), 0)
+                rhs = torch.cat((rhs[is_d], rhs[is_n]))
+            if Amat_scaler is not None:
+                A = Amat_scaler * A
+            sol = torch.linalg.solve(A, rhs.to(A.dtype)).to(neu.dtype)
+            if n_n == 0:
+                neu = sol.reshape(n_verts, 1)
+            elif n_d == 0:
+                dirv = sol.reshape(n_verts, 1)
+            else:
+                neu[is_d] = sol[:n_d, None]
+                dirv[is_n] = sol[n_d:, None]
+            neu_list.append(neu)
+            dir_list.append(dirv)
         return torch.stack(neu_list, 0), torch.stack(dir_list, 0)

@@ -384,6 +384,44 @@ def gmres(Z, b, x0=None, restart: int = 50, max_iters: int = 2000, tol: float = 
     return (xx[:, 0] if single else xx), infos
 
 
+def gmres_real(A, b, x0=None, restart: int = 50, max_iters: int = 2000, tol: float = 1e-6,
+               workspace=None):
+    """Solve the real system A x = b by GMRES(restart) (``mb_gmres_f32`` / ``mb_gmres_f64``).
+
+    A: float32 (FP32 products) or float64 (FP64 products) [n, n] CUDA tensor; b: [n] or
+    [n, k].  Returns (x float64 with b's shape, list of per-column info dicts).  The
+    refinement residual b - A x is FP64 in both cases.
+    """
+    _lib.check_tensor(A, "A", dtype=(torch.float32, torch.float64), ndim=2)
+    n = A.shape[0]
+    if A.shape[1] != n:
+        raise ValueError("A must be square")
+    dev = A.device
+    bb = b.to(device=dev, dtype=torch.float64)
+    single = bb.dim() == 1
+    bb = bb.reshape(n, -1)
+    xx = torch.zeros_like(bb) if x0 is None else x0.to(device=dev, dtype=torch.float64).reshape(n, -1).clone()
+    need = int(_lib.load().mb_gmres_real_workspace_bytes(int(n), int(restart)))
+    if workspace is None:
+        workspace = torch.empty(need, dtype=torch.uint8, device=dev)
+    else:
+        _lib.check_tensor(workspace, "workspace", dtype=torch.uint8, device=dev)
+        if workspace.numel() < need:
+            raise ValueError(f"workspace needs {need} bytes")
+    fn = "mb_gmres_f32" if A.dtype == torch.float32 else "mb_gmres_f64"
+    infos = []
+    for c in range(bb.shape[1]):
+        bc_ = bb[:, c].contiguous()
+        xc = xx[:, c].contiguous()
+        info = _lib.GmresInfo()
+        _lib.call(fn, _lib.ptr(A), n, _lib.ptr(bc_), _lib.ptr(xc), int(restart), int(max_iters), float(tol),
+                  _lib.ptr(workspace), workspace.numel(), __import__("ctypes").byref(info), _lib.stream_of(A))
+        xx[:, c] = xc
+        infos.append({"iterations": info.iterations, "restarts": info.restarts,
+                      "rel_residual": info.rel_residual, "converged": info.status == 0})
+    return (xx[:, 0] if single else xx), infos
+
+
 def matvec(Z, v):
     """y = Z v (complex64 Z, v cast to complex64) with FP64 row sums -> complex128 [n]."""
     _lib.check_tensor(Z, "Z", dtype=torch.complex64, ndim=2)

@@ -25,6 +25,9 @@ EFIE_MUFU_PER_EVAL = 3
 LAPLACE_SL_FLOP_PER_EVAL = 15
 LAPLACE_DL_FLOP_PER_EVAL = 22
 LAPLACE_MUFU_PER_EVAL = 1
+# nominal FP64 rate of a GB300 (far below its FP32 SIMT rate); used only as the denominator
+# of FP64 kernels, which have no measured figure
+FP64_NOMINAL_TFLOPS = 1.25
 
 GB300_SMS = 152
 FP32_FLOP_PER_CLK_PER_SM = 256   # 128 FP32 lanes x FMA

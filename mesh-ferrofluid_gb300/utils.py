@@ -73,6 +73,16 @@ class OrderType(_IntEnum):
     LINEAR = 1
 
 
+class VertexType(_IntEnum):
+    AIR = 0
+    FLUID = 1
+    OBSTACLE = 2
+    AIR_FLUID = 3
+    FLUID_OBSTACLE = 4
+    OBSTACLE_AIR = 5
+    TRIPLE_JUNCTION = 6
+
+
 class PanelRelationType(_IntEnum):
     SEPARATE = 0
     SAME_VERTEX = 1
@@ -179,6 +189,66 @@ def compute_vert_normals(vertices: torch.Tensor, faces: torch.Tensor):
     idx = faces.reshape(-1, 1).long().repeat(1, 3)
     out.scatter_add_(-2, idx, (areas * normals).repeat_interleave(3, dim=-2))
     return F.normalize(out, dim=-1)
+
+
+def cot_laplacian(vertices: torch.Tensor, faces: torch.Tensor, eps: float = 1e-12):
+    """Cotangent weights and inverse vertex areas of a triangle mesh.
+
+    Returns (L, inv_areas): L is a sparse symmetric [V, V] matrix whose (i, j) entry is
+    cot(alpha_ij) + cot(beta_ij), the cotangents of the angles opposite edge (i, j) in its
+    two faces (U. Pinkall and K. Polthier, Experiment. Math. 2(1), 1993; M. Meyer et al.,
+    Visualization and Mathematics III, 2003); inv_areas [V, 1] is 1 / (sum of the areas of
+    the faces around each vertex), 0 for isolated vertices.  Same convention as the
+    ``cot_laplacian`` the reference's pressure solver imports (mesh_pressure.py:112-115).
+    """
+    f = faces.long()
+    p = [vertices[f[:, k]] for k in range(3)]
+    rows, cols, vals = [], [], []
+    for k in range(3):
+        i, j = (k + 1) % 3, (k + 2) % 3  # edge (i, j) opposite corner k
+        a, b = p[i] - p[k], p[j] - p[k]
+        cr = torch.cross(a, b, dim=-1).norm(dim=-1).clamp_min(eps)
+        cot = (a * b).sum(-1) / cr
+        rows += [f[:, i], f[:, j]]
+        cols += [f[:, j], f[:, i]]
+        vals += [cot, cot]
+    n = vertices.shape[0]
+    L = torch.sparse_coo_tensor(torch.stack((torch.cat(rows), torch.cat(cols))), torch.cat(vals), (n, n),
+                                check_invariants=False)
+    L = L.coalesce()
+    area = compute_face_areas(vertices, faces, keepdim=False)
+    tot = torch.zeros(n, dtype=vertices.dtype, device=vertices.device)
+    tot.index_add_(0, f.reshape(-1), area.repeat_interleave(3))
+    inv = torch.where(tot > 0, 1.0 / tot.clamp_min(1e-300), torch.zeros_like(tot))
+    return L, inv.reshape(n, 1)
+
+
+def compute_mesh_face_tangent_gradient(vert_p: torch.Tensor, verts: torch.Tensor, faces: torch.Tensor,
+                                       face_normals: torch.Tensor = None) -> torch.Tensor:
+    """Surface gradient of the P1 interpolant of vert_p [B, V, 1] on each face -> [B, F, 3].
+
+    grad p = sum_a p_a n x (P_{a+2} - P_{a+1}) / (2 A) (src/utils/mesh_utils.py:501-548).
+    """
+    if face_normals is None:
+        face_normals = compute_face_normals(verts, faces)
+    f = faces.long()
+    area = compute_face_areas(verts, faces, keepdim=True)  # [F, 1]
+    P = [verts[f[:, k]] for k in range(3)]
+    g = 0
+    for a in range(3):
+        edge = P[(a + 2) % 3] - P[(a + 1) % 3]
+        g = g + vert_p[:, f[:, a], :] * torch.cross(face_normals, edge, dim=-1)
+    return g / 2.0 / area
+
+
+def compute_mesh_vert_tangent_gradient(vert_p: torch.Tensor, verts: torch.Tensor, faces: torch.Tensor,
+                                       face_normals: torch.Tensor = None) -> torch.Tensor:
+    """Face gradients spread to vertices with weight 1/3 each -> [B, V, 3] (mesh_utils.py:574-615)."""
+    fg = compute_mesh_face_tangent_gradient(vert_p, verts, faces, face_normals)  # [B, F, 3]
+    out = torch.zeros((vert_p.shape[0], verts.shape[0], 3), dtype=fg.dtype, device=fg.device)
+    idx = faces.long().reshape(-1)
+    out.index_add_(1, idx, (fg / 3.0).repeat_interleave(3, dim=1))
+    return out
 
 
 def get_vertices_from_index(vertices: torch.Tensor, index: torch.Tensor):

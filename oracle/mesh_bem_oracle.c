@@ -742,6 +742,193 @@ void orc_potential_integrals(const double* x, const double* tri, double* I1, dou
 #endif
 
 /* ------------------------------------------------------------------------------------ */
+/* Symmetric-rule Laplace operators (checker for csrc/laplace_sym.cu; the reference has  */
+/* no such mode).  Galerkin: out[fy, fx, a, b] = int_fy int_fx phi_a(y) phi_b(x) k(x, y)  */
+/* with k = 1/(4 pi R) (layer 1) or n_y.(x - y)/(4 pi R^3) (layer 2), P1 (order 1) or P0; */
+/* 7 x 7 points for pairs without a shared vertex, else 7 points on fx and the inner     */
+/* integral over fy in closed form (Wilton et al. 1984; van Oosterom & Strackee 1983 for  */
+/* the solid angle; int (rho_y - rho)/R^3 = -sum_i u_i ln((R+ + l+)/(R- + l-))).           */
+/* Collocation: A[i, j] = int_{T_j} 1/(4 pi |c_i - y|), c_i the centroid of face i.      */
+/* Double precision only.                                                               */
+/* ------------------------------------------------------------------------------------ */
+#ifndef ORC_FLOAT
+static double orc_dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static void orc_cross3d(const double* a, const double* b, double* c) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+/* omega = int_T n.(y - x)/R^3 (signed solid angle), J = int_T (rho_y - rho)/R^3, d = n.(x - P0);
+ * both 0 when |d| <= dtol (x in the plane of T, where the double-layer kernel vanishes). */
+static void orc_dl_integrals(const double* x, const double P[3][3], double dtol, double* omega, double J[3],
+                             double* dout) {
+    double e0[3], e1[3], n[3];
+    for (int a = 0; a < 3; ++a) { e0[a] = P[1][a] - P[0][a]; e1[a] = P[2][a] - P[1][a]; }
+    orc_cross3d(e0, e1, n);
+    const double nn = sqrt(orc_dot3(n, n));
+    for (int a = 0; a < 3; ++a) n[a] /= nn;
+    double xp[3] = {x[0] - P[0][0], x[1] - P[0][1], x[2] - P[0][2]};
+    const double d = orc_dot3(xp, n);
+    *dout = d;
+    J[0] = J[1] = J[2] = 0.0;
+    if (fabs(d) <= dtol) {
+        *omega = 0.0;
+        return;
+    }
+    double r[3][3], l[3];
+    for (int v = 0; v < 3; ++v) {
+        for (int a = 0; a < 3; ++a) r[v][a] = P[v][a] - x[a];
+        l[v] = sqrt(orc_dot3(r[v], r[v]));
+    }
+    double c12[3];
+    orc_cross3d(r[1], r[2], c12);
+    const double num = orc_dot3(r[0], c12);
+    const double den = l[0] * l[1] * l[2] + orc_dot3(r[0], r[1]) * l[2] + orc_dot3(r[0], r[2]) * l[1] +
+                       orc_dot3(r[1], r[2]) * l[0];
+    *omega = 2.0 * atan2(num, den);
+    double rho[3] = {x[0] - d * n[0], x[1] - d * n[1], x[2] - d * n[2]};
+    for (int i = 0; i < 3; ++i) {
+        const double* pm = P[i];
+        const double* pp = P[(i + 1) % 3];
+        double ed[3] = {pp[0] - pm[0], pp[1] - pm[1], pp[2] - pm[2]};
+        const double el = sqrt(orc_dot3(ed, ed));
+        for (int a = 0; a < 3; ++a) ed[a] /= el;
+        double u[3];
+        orc_cross3d(ed, n, u);
+        double dp[3] = {pp[0] - rho[0], pp[1] - rho[1], pp[2] - rho[2]};
+        double dm[3] = {pm[0] - rho[0], pm[1] - rho[1], pm[2] - rho[2]};
+        const double lp = orc_dot3(dp, ed), lm = orc_dot3(dm, ed), p0 = orc_dot3(dp, u);
+        const double r0sq = p0 * p0 + d * d;
+        const double rp = sqrt(r0sq + lp * lp), rm = sqrt(r0sq + lm * lm);
+        double lg;
+        if ((lm >= 0 || lp >= 0) && rm + lm > 0) lg = log((rp + lp) / (rm + lm));
+        else lg = log((rm - lm) / (rp - lp));
+        for (int a = 0; a < 3; ++a) J[a] -= lg * u[a];
+    }
+}
+
+static void orc_face(const double* verts, const int32_t* faces, int64_t f, double P[3][3]) {
+    for (int v = 0; v < 3; ++v)
+        for (int a = 0; a < 3; ++a) P[v][a] = verts[3 * (int64_t)faces[3 * f + v] + a];
+}
+
+static int orc_share_vertex(const int32_t* faces, int64_t p, int64_t q) {
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            if (faces[3 * p + i] == faces[3 * q + j]) return 1;
+    return 0;
+}
+
+void orc_laplace_sym_f64(const double* verts, const int32_t* faces, int64_t nf, int layer, int order,
+                         int64_t row_begin, int64_t row_end, double* out) {
+    double bary[7][3], w7[7];
+    orc_d7(bary, w7);
+    const int nphi = order == 1 ? 3 : 1, nn = nphi * nphi;
+    const double inv4pi = 1.0 / (4.0 * ORC_PI);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t fy = row_begin; fy < row_end; ++fy) {
+        double P[3][3], e0[3], e1[3], ny[3];
+        orc_face(verts, faces, fy, P);
+        for (int a = 0; a < 3; ++a) { e0[a] = P[1][a] - P[0][a]; e1[a] = P[2][a] - P[1][a]; }
+        orc_cross3d(e0, e1, ny);
+        const double two_ay = sqrt(orc_dot3(ny, ny));
+        for (int a = 0; a < 3; ++a) ny[a] /= two_ay;
+        double grad[3][3], cy[3], hmax = 0.0;
+        for (int a = 0; a < 3; ++a) {
+            double ed[3];
+            for (int c = 0; c < 3; ++c) ed[c] = P[(a + 2) % 3][c] - P[(a + 1) % 3][c];
+            orc_cross3d(ny, ed, grad[a]);
+            for (int c = 0; c < 3; ++c) grad[a][c] /= two_ay;
+            cy[a] = (P[0][a] + P[1][a] + P[2][a]) / 3.0;
+            double eb[3];
+            for (int c = 0; c < 3; ++c) eb[c] = P[(a + 1) % 3][c] - P[a][c];
+            hmax = fmax(hmax, sqrt(orc_dot3(eb, eb)));
+        }
+        double ys[7][3];
+        for (int j = 0; j < 7; ++j)
+            for (int c = 0; c < 3; ++c) ys[j][c] = bary[j][0] * P[0][c] + bary[j][1] * P[1][c] + bary[j][2] * P[2][c];
+        for (int64_t fx = 0; fx < nf; ++fx) {
+            double Q[3][3], f0[3], f1[3], nx[3];
+            orc_face(verts, faces, fx, Q);
+            for (int a = 0; a < 3; ++a) { f0[a] = Q[1][a] - Q[0][a]; f1[a] = Q[2][a] - Q[1][a]; }
+            orc_cross3d(f0, f1, nx);
+            const double ax = 0.5 * sqrt(orc_dot3(nx, nx));
+            const int near = orc_share_vertex(faces, fy, fx);
+            double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            for (int i = 0; i < 7; ++i) {
+                double x[3];
+                for (int c = 0; c < 3; ++c) x[c] = bary[i][0] * Q[0][c] + bary[i][1] * Q[1][c] + bary[i][2] * Q[2][c];
+                double sa[3] = {0, 0, 0};
+                if (near) {
+                    double xc[3] = {x[0] - cy[0], x[1] - cy[1], x[2] - cy[2]};
+                    if (layer == 1) {
+                        double I0, I1[3];
+                        orc_pot_integrals(x, P, &I0, I1);
+                        for (int a = 0; a < nphi; ++a)
+                            sa[a] = nphi == 3 ? (1.0 / 3.0 + orc_dot3(grad[a], xc)) * I0 + orc_dot3(grad[a], I1) : I0;
+                    } else {
+                        double om, J[3], d;
+                        orc_dl_integrals(x, P, 1e-10 * hmax, &om, J, &d);
+                        for (int a = 0; a < nphi; ++a)
+                            sa[a] = nphi == 3 ? -(1.0 / 3.0 + orc_dot3(grad[a], xc)) * om + d * orc_dot3(grad[a], J)
+                                              : -om;
+                    }
+                } else {
+                    for (int j = 0; j < 7; ++j) {
+                        double dd[3] = {x[0] - ys[j][0], x[1] - ys[j][1], x[2] - ys[j][2]};
+                        const double R = sqrt(orc_dot3(dd, dd));
+                        double g = w7[j] * 0.5 * two_ay / R;
+                        if (layer == 2) g *= orc_dot3(ny, dd) / (R * R);
+                        for (int a = 0; a < nphi; ++a) sa[a] += g * (nphi == 3 ? bary[j][a] : 1.0);
+                    }
+                }
+                const double wx = w7[i] * ax;
+                for (int a = 0; a < nphi; ++a)
+                    for (int b = 0; b < nphi; ++b) acc[a * nphi + b] += sa[a] * wx * (nphi == 3 ? bary[i][b] : 1.0);
+            }
+            double* o = out + ((fy - row_begin) * nf + fx) * nn;
+            for (int c = 0; c < nn; ++c) o[c] = acc[c] * inv4pi;
+        }
+    }
+}
+
+void orc_laplace_colloc_sl_f64(const double* verts, const int32_t* faces, int64_t nf, double* out) {
+    double bary[7][3], w7[7];
+    orc_d7(bary, w7);
+    const double inv4pi = 1.0 / (4.0 * ORC_PI);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t i = 0; i < nf; ++i) {
+        double A[3][3], c[3];
+        orc_face(verts, faces, i, A);
+        for (int a = 0; a < 3; ++a) c[a] = (A[0][a] + A[1][a] + A[2][a]) / 3.0;
+        for (int64_t j = 0; j < nf; ++j) {
+            double P[3][3];
+            orc_face(verts, faces, j, P);
+            double v;
+            if (orc_share_vertex(faces, i, j)) {
+                double I1[3];
+                orc_pot_integrals(c, P, &v, I1);
+            } else {
+                double e0[3], e1[3], nr[3];
+                for (int a = 0; a < 3; ++a) { e0[a] = P[1][a] - P[0][a]; e1[a] = P[2][a] - P[1][a]; }
+                orc_cross3d(e0, e1, nr);
+                const double area = 0.5 * sqrt(orc_dot3(nr, nr));
+                v = 0.0;
+                for (int k = 0; k < 7; ++k) {
+                    double y[3];
+                    for (int a = 0; a < 3; ++a)
+                        y[a] = bary[k][0] * P[0][a] + bary[k][1] * P[1][a] + bary[k][2] * P[2][a] - c[a];
+                    v += w7[k] * area / sqrt(orc_dot3(y, y));
+                }
+            }
+            out[i * nf + j] = v * inv4pi;
+        }
+    }
+}
+#endif
+
+/* ------------------------------------------------------------------------------------ */
 /* Closest-hit ray query (the reference's Vulkan ray-query plugin,                      */
 /* src/vulkan_ray_tracing/shaders/raygen.rgen:23-64, closesthit.rchit, miss.rmiss;       */
 /* QueryForNLOS / QueryForLOS at ray_query_App.hpp:881-1000): rays from origin[row] along */

@@ -45,6 +45,8 @@ def _load():
             getattr(lib, f"orc_mom_sym_rhs_rwg_{sfx}").argtypes = [_P, _P, _I64, _P, _I64, _P, _I, _P, _P]
             getattr(lib, f"orc_ray_query_{sfx}").argtypes = [_P, _P, _I64, _P, _P, _I64, _I64, _D, _D, _P]
         lib.orc_potential_integrals.argtypes = [_P, _P, _P, _P]
+        lib.orc_laplace_sym_f64.argtypes = [_P, _P, _I64, _I, _I, _I64, _I64, _P]
+        lib.orc_laplace_colloc_sl_f64.argtypes = [_P, _P, _I64, _P]
         _lib = lib
     return _lib
 
@@ -191,6 +193,28 @@ def ray_query(verts, faces, origins, dirs, tmin=0.001, tmax=10000.0):
     out = np.zeros((h, w, 4))
     lib.orc_ray_query_f64(_ptr(v), _ptr(f), f.shape[0], _ptr(o), _ptr(d), h, w, float(tmin), float(tmax),
                           _ptr(out))
+    return out
+
+
+def laplace_sym(verts, faces, layer, order, rows=None):
+    """Symmetric-rule Galerkin operator [F, F, nphi, nphi] (double; see orc_laplace_sym_f64)."""
+    lib = _load()
+    v, f = _c(verts, np.float64), _c(faces, np.int32)
+    nf = f.shape[0]
+    r0, r1 = (0, nf) if rows is None else rows
+    nphi = 3 if order == 1 else 1
+    out = np.zeros((r1 - r0, nf, nphi, nphi))
+    lib.orc_laplace_sym_f64(_ptr(v), _ptr(f), nf, int(layer), int(order), r0, r1, _ptr(out))
+    return out
+
+
+def laplace_colloc_sl(verts, faces):
+    """P0 single-layer collocation matrix [F, F] at face centroids (double)."""
+    lib = _load()
+    v, f = _c(verts, np.float64), _c(faces, np.int32)
+    nf = f.shape[0]
+    out = np.zeros((nf, nf))
+    lib.orc_laplace_colloc_sl_f64(_ptr(v), _ptr(f), nf, _ptr(out))
     return out
 
 

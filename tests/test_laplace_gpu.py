@@ -115,15 +115,3 @@ def test_solve_f64_matches_reference(pkg, cuda, golden, name, gq, order):
     assert rel_err(solver.rhs_layer.get_rhs_vec().cpu().numpy(), g[f"{tag}_rhs"]) < 1e-10
     assert rel_err(neu.cpu().numpy(), g[f"{tag}_neumann"]) < 1e-9
     assert rel_err(dirv.cpu().numpy(), g[f"{tag}_dirichlet"]) == 0.0
-
-
-def test_neumann_data_rejected(pkg, cuda):
-    v_np, f_np = pkg.meshes.icosphere(1)
-    v = torch.tensor(v_np, dtype=torch.float32, device=cuda)
-    f = torch.tensor(f_np, dtype=torch.int32, device=cuda)
-    solver = pkg.MeshBEMSolver3d(gaussQR=2, order_type=1, BEM_type=0, wavenumber=1.0, logger=None,
-                                 dtype=torch.float32, device=cuda)
-    fv = torch.zeros((1, v.shape[0], 1), device=cuda)
-    flags = torch.ones_like(fv, dtype=torch.uint8)
-    with pytest.raises(NotImplementedError):
-        solver.solve(v, f, fv, fv, flags)
