@@ -197,6 +197,33 @@ int mb_ray_query_f32(const void* bvh, int64_t n_faces, const float* origins, con
                      int64_t n_rows, int64_t n_cols, double tmin, double tmax, float* out, void* stream);
 int mb_ray_status(const void* bvh, int64_t n_faces, int32_t* overflow, void* stream);
 
+/* ---- Tensor-core (tcgen05) multi-right-hand-side product ------------------------------ */
+
+/* Self-test of the tcgen05 path: one 128 x 256 x 32 kind::tf32 tile with the operands in
+ * the 128-byte-swizzled K-major shared-memory layout, accumulated in TMEM and read back;
+ * *max_rel_err receives the largest |D - A B^T| / sum |a b| against a double product
+ * (expected ~1e-7: TF32-exact inputs, FP32 accumulation).  Allocates and frees a few
+ * hundred KB of device memory; synchronous. */
+int mb_tc_selftest(double* max_rel_err, void* stream);
+
+/* Split of an fp32 array into TF32 parts: hi = x rounded to TF32, lo = TF32(x - hi).
+ * Applied once to the impedance matrix (viewed as fp32 [n, 2n]) before mb_cgemm_tf32x3. */
+int mb_split_tf32(const float* src, int64_t count, float* hi, float* lo, void* stream);
+
+/* Multi-right-hand-side product for the block / many-incidence solves (no counterpart in
+ * the reference, which solves one right-hand side with torch.linalg.solve,
+ * mesh_BEM_solver_3d.py:174): Y = Z X with Z complex64 [n, n] given by its TF32 split
+ * (z_hi, z_lo from mb_split_tf32 of Z viewed as fp32 [n, 2n]), X, Y complex64 [n, m]
+ * interleaved.  tcgen05 kind::tf32 products A_hi B_hi + A_hi B_lo + A_lo B_hi with FP32
+ * accumulation in TMEM (FP32-class accuracy); TMA-fed, one 128 x 256 tile per CTA.
+ * n even; operands 16-byte aligned.  workspace: mb_cgemm_workspace_bytes(n, m) bytes
+ * (the split, reordered right-hand sides and a status word); mb_cgemm_status reads that
+ * status (synchronous; nonzero = a pipeline wait ran out and Y is incomplete). */
+size_t mb_cgemm_workspace_bytes(int64_t n, int64_t m);
+int mb_cgemm_tf32x3(const float* z_hi, const float* z_lo, int64_t n, const float* x, int64_t m, float* y,
+                    void* workspace, size_t workspace_bytes, void* stream);
+int mb_cgemm_status(void* workspace, int64_t n, int64_t m, int32_t* status, void* stream);
+
 /* ---- Dense iterative solve (replaces torch.linalg.solve, mesh_BEM_solver_3d.py:174) -- */
 
 /* Outcome of mb_gmres_c64. status: 0 converged to tol, 1 stopped at max_iters. */

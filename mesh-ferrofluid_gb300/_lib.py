@@ -56,6 +56,11 @@ _SIGS = {
     "mb_laplace_sym_f64": [_P, _I64, _P, _I64, _I, _I, _P, _I64, _I64, _I64, _P, _P],
     "mb_laplace_colloc_sl_f32": [_P, _I64, _P, _I64, _P, _I64, _I64, _I64, _P, _P],
     "mb_laplace_colloc_sl_f64": [_P, _I64, _P, _I64, _P, _I64, _I64, _I64, _P, _P],
+    "mb_tc_selftest": [_P, _P],
+    "mb_split_tf32": [_P, _I64, _P, _P, _P],
+    "mb_cgemm_workspace_bytes": [_I64, _I64],
+    "mb_cgemm_tf32x3": [_P, _P, _I64, _P, _I64, _P, _P, ctypes.c_size_t, _P],
+    "mb_cgemm_status": [_P, _I64, _I64, _P, _P],
     "mb_ray_bvh_bytes": [_I64],
     "mb_ray_bvh_build_f32": [_P, _I64, _P, _I64, _P, ctypes.c_size_t, _P],
     "mb_ray_query_f32": [_P, _I64, _P, _P, _I64, _I64, _D, _D, _P, _P],
@@ -73,7 +78,7 @@ _SIGS = {
 }
 
 _RESTYPES = {"mb_gmres_workspace_bytes": ctypes.c_size_t, "mb_ray_bvh_bytes": ctypes.c_size_t,
-             "mb_gmres_real_workspace_bytes": ctypes.c_size_t}
+             "mb_gmres_real_workspace_bytes": ctypes.c_size_t, "mb_cgemm_workspace_bytes": ctypes.c_size_t}
 
 
 class GmresInfo(ctypes.Structure):

@@ -57,6 +57,12 @@ int launch_laplace_colloc_sl(const T*, const int32_t*, int64_t, const int32_t*, 
 int launch_panel_relation(const int32_t*, int64_t, uint8_t*, cudaStream_t);
 size_t gmres_workspace_bytes(int64_t n, int m);
 size_t gmres_real_workspace_bytes(int64_t n, int m);
+int tc_selftest(double* max_rel_err, cudaStream_t s);
+size_t cgemm_workspace_bytes(int64_t n, int64_t m);
+int split_tf32(const float* src, int64_t count, float* hi, float* lo, cudaStream_t s);
+int cgemm_tf32x3(const float* z_hi, const float* z_lo, int64_t n, const float* x, int64_t m, float* y, void* ws,
+                 size_t ws_bytes, cudaStream_t s);
+int cgemm_status(void* ws, int64_t n, int64_t m, int* out, cudaStream_t s);
 int gmres_real(int kind, const void* a, int64_t n, const double* b, double* x, int m, int max_iters, double tol,
                void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out, double* relres_out,
                int* status_out, cudaStream_t s);
@@ -387,6 +393,33 @@ MB_RAD(c128, double)
 size_t mb_gmres_workspace_bytes(int64_t n, int restart) {
     if (n <= 0 || restart < 1) return 0;
     return gmres_workspace_bytes(n, restart);
+}
+
+int mb_tc_selftest(double* max_rel_err, void* stream) {
+    MB_REQUIRE(max_rel_err, "null pointer argument");
+    return tc_selftest(max_rel_err, as_stream(stream));
+}
+
+int mb_split_tf32(const float* src, int64_t count, float* hi, float* lo, void* stream) {
+    MB_REQUIRE(count >= 0, "bad sizes");
+    if (count == 0) return MB_OK;
+    MB_REQUIRE(src && hi && lo, "null pointer argument");
+    return split_tf32(src, count, hi, lo, as_stream(stream));
+}
+
+size_t mb_cgemm_workspace_bytes(int64_t n, int64_t m) { return n > 0 && m > 0 ? cgemm_workspace_bytes(n, m) : 0; }
+
+int mb_cgemm_tf32x3(const float* z_hi, const float* z_lo, int64_t n, const float* x, int64_t m, float* y,
+                    void* workspace, size_t workspace_bytes, void* stream) {
+    MB_REQUIRE(n >= 0 && m >= 0, "bad sizes");
+    if (n == 0 || m == 0) return MB_OK;
+    MB_REQUIRE(z_hi && z_lo && x && y && workspace, "null pointer argument");
+    return cgemm_tf32x3(z_hi, z_lo, n, x, m, y, workspace, workspace_bytes, as_stream(stream));
+}
+
+int mb_cgemm_status(void* workspace, int64_t n, int64_t m, int32_t* status, void* stream) {
+    MB_REQUIRE(workspace && status && n > 0 && m > 0, "bad arguments");
+    return cgemm_status(workspace, n, m, status, as_stream(stream));
 }
 
 size_t mb_gmres_real_workspace_bytes(int64_t n, int restart) {

@@ -220,11 +220,11 @@ __global__ void lap_sym_near_kernel(const T* __restrict__ verts, const int32_t* 
     for (int c = 0; c < nn; ++c) o[c] = (T)(acc[c] * kInv4Pi);
 }
 
-// P0 single-layer collocation at face centroids, separated pairs.  A block covers
+// P0 single-layer collocation at face centroids with the 7-point rule.  A block covers
 // kSymThreads source faces j (one per thread) and kColRows consecutive collocation rows i:
 // each thread builds its source triangle's 7 points once and evaluates them against the
 // kColRows centroids held in shared memory, writing out[(i - row_begin) * nf + j]
-// (coalesced per row).  Pairs sharing a vertex are left to lap_colloc_near_kernel.
+// (coalesced per row).  Pairs sharing a vertex are then rewritten by lap_colloc_near_kernel.
 constexpr int kColRows = 16;
 
 template <typename T>
@@ -232,7 +232,6 @@ __global__ void __launch_bounds__(kSymThreads)
     lap_colloc_sl_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces, int64_t nf,
                          int64_t row_begin, int64_t row_end, T* __restrict__ out) {
     __shared__ T s_c[kColRows][3];
-    __shared__ int32_t s_f[kColRows][3];
     const int64_t i0 = row_begin + (int64_t)blockIdx.y * kColRows;
     const int64_t j = (int64_t)blockIdx.x * kSymThreads + threadIdx.x;
     if (threadIdx.x < kColRows) {
@@ -243,15 +242,12 @@ __global__ void __launch_bounds__(kSymThreads)
             s_c[threadIdx.x][0] = c.x;
             s_c[threadIdx.x][1] = c.y;
             s_c[threadIdx.x][2] = c.z;
-            s_f[threadIdx.x][0] = a0;
-            s_f[threadIdx.x][1] = a1;
-            s_f[threadIdx.x][2] = a2;
         }
     }
     __syncthreads();
     if (j >= nf) return;
-    const int32_t b0 = __ldg(faces + 3 * j), b1 = __ldg(faces + 3 * j + 1), b2 = __ldg(faces + 3 * j + 2);
-    const V3<T> B0 = load3(verts, b0), E1 = load3(verts, b1) - B0, E2 = load3(verts, b2) - B0;
+    const V3<T> B0 = load3(verts, __ldg(faces + 3 * j));
+    const V3<T> E1 = load3(verts, __ldg(faces + 3 * j + 1)) - B0, E2 = load3(verts, __ldg(faces + 3 * j + 2)) - B0;
     const V3<T> nr = cross(E1, E2);
     const T scale = T(0.5) * sqrt_t(dot(nr, nr)) * T(kInv4Pi);
     V3<T> y[7];
@@ -261,21 +257,33 @@ __global__ void __launch_bounds__(kSymThreads)
         y[k] = B0 + ((T)c_d7[k][1] * E1 + (T)c_d7[k][2] * E2);
         w[k] = (T)c_d7[k][3] * scale;
     }
-    const int rows = (int)((row_end - i0) < kColRows ? (row_end - i0) : kColRows);
-    for (int r = 0; r < rows; ++r) {
-        const int32_t a0 = s_f[r][0], a1 = s_f[r][1], a2 = s_f[r][2];
-        const bool near = (a0 == b0) | (a0 == b1) | (a0 == b2) | (a1 == b0) | (a1 == b1) | (a1 == b2) |
-                          (a2 == b0) | (a2 == b1) | (a2 == b2);
-        T acc = 0;
-        if (!near) {
+    // Pairs sharing a vertex are evaluated here too (the value is discarded: the near-pair
+    // kernel, launched next on the same stream, overwrites them); the only coincident point,
+    // the centroid of a face against its own rule, gives +inf, never a fault.
+    const int64_t rows = row_end - i0;
+    if (rows >= kColRows) {
+#pragma unroll 4
+        for (int r = 0; r < kColRows; ++r) {
             const V3<T> c = v3<T>(s_c[r][0], s_c[r][1], s_c[r][2]);
+            T acc = 0;
 #pragma unroll
             for (int k = 0; k < 7; ++k) {
                 const V3<T> d = y[k] - c;
                 acc += w[k] * rcp_sqrt(dot(d, d));
             }
+            out[(i0 - row_begin + r) * nf + j] = acc;
         }
-        out[(i0 - row_begin + r) * nf + j] = acc;
+    } else {
+        for (int r = 0; r < (int)rows; ++r) {
+            const V3<T> c = v3<T>(s_c[r][0], s_c[r][1], s_c[r][2]);
+            T acc = 0;
+#pragma unroll
+            for (int k = 0; k < 7; ++k) {
+                const V3<T> d = y[k] - c;
+                acc += w[k] * rcp_sqrt(dot(d, d));
+            }
+            out[(i0 - row_begin + r) * nf + j] = acc;
+        }
     }
 }
 

@@ -422,6 +422,57 @@ def gmres_real(A, b, x0=None, restart: int = 50, max_iters: int = 2000, tol: flo
     return (xx[:, 0] if single else xx), infos
 
 
+def split_tf32(Z):
+    """(hi, lo) fp32 [n, 2n] TF32 split of a complex64 [n, n] matrix (``mb_split_tf32``)."""
+    _lib.check_tensor(Z, "Z", dtype=torch.complex64, ndim=2)
+    n = Z.shape[0]
+    if Z.shape[1] != n:
+        raise ValueError("Z must be square")
+    real = torch.view_as_real(Z).reshape(n, 2 * n)
+    hi = torch.empty_like(real)
+    lo = torch.empty_like(real)
+    _lib.call("mb_split_tf32", _lib.ptr(real), real.numel(), _lib.ptr(hi), _lib.ptr(lo), _lib.stream_of(real))
+    return hi, lo
+
+
+def cgemm_workspace_bytes(n: int, m: int) -> int:
+    return int(_lib.load().mb_cgemm_workspace_bytes(int(n), int(m)))
+
+
+def multi_rhs_matmul(z_split, X, out=None, workspace=None, check: bool = False):
+    """Y = Z X for many right-hand sides on the tcgen05 tensor cores (``mb_cgemm_tf32x3``).
+
+    z_split: (hi, lo) from ``split_tf32(Z)``; X: complex64 [n, m]; returns complex64 [n, m].
+    Split-TF32 x 3 products with FP32 accumulation (FP32-class accuracy).  ``check`` reads
+    the kernel's status word (a synchronisation) and raises if a pipeline wait ran out.
+    """
+    hi, lo = z_split
+    n = hi.shape[0]
+    _lib.check_tensor(hi, "z_hi", dtype=torch.float32, ndim=2, shape=(n, 2 * n))
+    _lib.check_tensor(lo, "z_lo", dtype=torch.float32, device=hi.device, ndim=2, shape=(n, 2 * n))
+    _lib.check_tensor(X, "X", dtype=torch.complex64, device=hi.device, ndim=2)
+    if X.shape[0] != n:
+        raise ValueError("X must have n rows")
+    m = X.shape[1]
+    if out is None:
+        out = torch.empty((n, m), dtype=torch.complex64, device=hi.device)
+    else:
+        _lib.check_tensor(out, "out", dtype=torch.complex64, device=hi.device, shape=(n, m))
+    need = cgemm_workspace_bytes(n, m)
+    if workspace is None:
+        workspace = torch.empty(need, dtype=torch.uint8, device=hi.device)
+    elif workspace.numel() < need:
+        raise ValueError(f"workspace needs {need} bytes")
+    _lib.call("mb_cgemm_tf32x3", _lib.ptr(hi), _lib.ptr(lo), n, _lib.ptr(X), m, _lib.ptr(out), _lib.ptr(workspace),
+              workspace.numel(), _lib.stream_of(hi))
+    if check:
+        st = __import__("ctypes").c_int32(0)
+        _lib.call("mb_cgemm_status", _lib.ptr(workspace), n, m, __import__("ctypes").byref(st), _lib.stream_of(hi))
+        if st.value:
+            raise _lib.MeshBEMError(f"multi_rhs_matmul: pipeline wait timed out (status {st.value})")
+    return out
+
+
 def matvec(Z, v):
     """y = Z v (complex64 Z, v cast to complex64) with FP64 row sums -> complex128 [n]."""
     _lib.check_tensor(Z, "Z", dtype=torch.complex64, ndim=2)
