@@ -47,6 +47,9 @@ WORKLOADS = {
     # Laplace single-layer collocation, unit Dirichlet data on the sphere: (level, radius, dtype)
     "laplace_col_L5": (5, 1.0, "f32"),
     "laplace_col_L5_f64": (5, 1.0, "f64"),
+    # many incidences on one mesh: (ellipsoid level, k, Fibonacci directions x 2 polarisations)
+    "mrhs_ell4": (4, 6.0, 256),
+    "mrhs_ell4_efie": (4, 6.0, 256),
 }
 
 
@@ -506,6 +509,161 @@ def main_laplace(args, rank, world, local_rank):
 
 
 # ---------------------------------------------------------------------------------------
+# many right-hand sides: tensor-core product + lockstep GMRES vs plain per-incidence GMRES
+# ---------------------------------------------------------------------------------------
+def main_mrhs(args, rank, world, local_rank):
+    level, k, ndir = WORKLOADS[args.workload]
+    import torch
+
+    pkg = importlib.import_module("mesh-ferrofluid_gb300")
+    M = pkg.mesh_MOM_3d
+    nrhs = 2 * ndir
+    efie = args.workload.endswith("_efie")
+    config = {"workload": args.workload, "mesh": f"ellipsoid 1.0/0.7/0.5 from icosphere L{level}, normal jitter "
+              "N(0, 0.01 mean edge), seed 0", "ka": k, "rhs": f"{ndir} Fibonacci directions x 2 orthogonal "
+              "polarisations",
+              "formulation": ("EFIE, 7-point rule, closed-form singular pairs (FP64)" if efie else
+                              "the reference's EFIE + MFIE operator and collapsed Gauss rule (gaussQR 4), its "
+                              "excitation <f, E + n x H> for each plane wave"),
+              "solve": "lockstep GMRES(50), every step one split-TF32x3 tcgen05 product with all right-hand sides",
+              "parallelism": "replicas"}
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference solves one right-hand side per "
+                              "dense LU and has no symmetric-rule EFIE; its own algorithm is timed by mom_ref_*"}),
+                  flush=True)
+        return
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local_rank if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    v_np, f_np = pkg.meshes.ellipsoid(level)
+    verts = torch.tensor(v_np, dtype=torch.float32, device=dev)
+    faces = torch.tensor(f_np, dtype=torch.int32, device=dev)
+    edges, fei, _ = pkg.utils.get_edge_unique(verts, faces)
+    ne = int(edges.shape[0])
+    config["n_edges"] = ne
+    dirs = pkg.meshes.fibonacci_lattice(ndir)
+    ref_axis = np.where(np.abs(dirs[:, 2:3]) < 0.9, [[0.0, 0.0, 1.0]], [[1.0, 0.0, 0.0]])
+    p1 = np.cross(dirs, ref_axis)
+    p1 /= np.linalg.norm(p1, axis=1, keepdims=True)
+    p2 = np.cross(dirs, p1)
+    waves = M.plane_waves(k, np.concatenate([dirs, dirs]), np.concatenate([p1, p2]), device=dev)
+    near = M.near_pairs(faces) if efie else None
+    if not efie:
+        areas = pkg.utils.compute_face_areas(verts, faces).contiguous()
+        normals = pkg.utils.compute_face_normals(verts, faces).contiguous()
+        px, wx = pkg.utils.get_gaussion_integration_points_and_weights(4, device=dev)
+        py, wy = pkg.utils.get_gaussion_integration_points_and_weights(3, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    tol = 1e-5
+
+    def solve_new():
+        e = [ev() for _ in range(5)]
+        e[0].record(stream)
+        if efie:
+            Z = M.assemble_Z_rwg_sym(verts, faces, fei, ne, k, pairs=near, check_indices=False)
+            B = M.assemble_rhs_rwg_sym(verts, faces, fei, ne, waves)
+        else:
+            Z = M.assemble_Z_rwg(verts, faces, areas, normals, fei, ne, px, wx, py, wy, k, check_indices=False)
+            B = M.assemble_rhs_rwg(verts, faces, areas, normals, fei, ne, px, wx, waves)
+        e[1].record(stream)
+        split = M.split_tf32(Z)
+        e[2].record(stream)
+        X, info = M.gmres_multi(split, B, restart=50, tol=tol, max_iters=3000)
+        e[3].record(stream)
+        torch.cuda.synchronize(dev)
+        return Z, B, X, info, [e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2]), e[2].elapsed_time(e[3])]
+
+    for _ in range(max(1, min(args.warmup, 1))):
+        Z, B, X, info, _ = solve_new()
+    barrier = (lambda: (torch.distributed.barrier(), torch.cuda.synchronize(dev))) if world > 1 else \
+        (lambda: torch.cuda.synchronize(dev))
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.3)
+    runs = []
+    for _ in range(args.steps):
+        barrier()
+        Z, B, X, info, parts = solve_new()
+        runs.append(parts)
+    clocks.stop()
+    tot = [sum(p) for p in runs]
+    ms = statistics.mean(tot)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    # accuracy against the FP64 dense solution (outside the timed region)
+    Zd = Z.to(torch.complex128)
+    Xref = torch.linalg.solve(Zd, B.to(torch.complex128))
+    err_new = (torch.linalg.norm(X - Xref, dim=0) / torch.linalg.norm(Xref, dim=0)).cpu()
+    # the plain path: one GMRES per incidence with HBM-bound FP32 matvecs, timed on a sample
+    sample = list(range(0, nrhs, max(1, nrhs // 32)))
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    errs_plain, iters_plain = [], []
+    for c in sample:
+        x1, inf1 = M.gmres(Z, B[:, c], restart=50, tol=tol, max_iters=3000)
+        iters_plain.append(inf1[0]["iterations"])
+        errs_plain.append((torch.linalg.norm(x1 - Xref[:, c]) / torch.linalg.norm(Xref[:, c])).item())
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    plain_ms_per_rhs = e0.elapsed_time(e1) / len(sample)
+    asm_ms = statistics.mean(p[0] for p in runs)
+    plain_total = asm_ms + plain_ms_per_rhs * nrhs
+    # tensor-core product alone (the dominant kernel), for the roofline
+    split = M.split_tf32(Z)
+    X32 = X.to(torch.complex64)
+    ws = torch.empty(M.cgemm_workspace_bytes(ne, nrhs), dtype=torch.uint8, device=dev)
+    Y = torch.empty_like(X32)
+    for _ in range(3):
+        M.multi_rhs_matmul(split, X32, out=Y, workspace=ws)
+    g0, g1 = ev(), ev()
+    g0.record(stream)
+    for _ in range(10):
+        M.multi_rhs_matmul(split, X32, out=Y, workspace=ws)
+    g1.record(stream)
+    torch.cuda.synchronize(dev)
+    gemm_ms = g0.elapsed_time(g1) / 10
+    alg = 8.0 * ne * ne * nrhs
+    peaks = pkg.roofline.measured_peaks(REPO)
+    tf32_peak = float(peaks.get("bf16_tflops", 1900.0)) / 2.0
+    line = {"metric": "incidences solved per second (assembly + solve to 1e-5 relative residual)",
+            "value": world * nrhs / (ms / 1e3), "unit": "rhs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (split-tf32x3 products, FP64 Arnoldi)", "data": "synthetic",
+            "config": config,
+            "breakdown_ms": {"assembly_Z_and_B": asm_ms, "split": statistics.mean(p[1] for p in runs),
+                             "gmres_multi": statistics.mean(p[2] for p in runs)},
+            "solve": {"arnoldi_steps": info["iterations"], "restarts": info["restarts"],
+                      "max_rel_residual": info["max_rel_residual"], "converged": info["converged"],
+                      "max_rel_err_J_vs_fp64_lu": float(err_new.max()),
+                      "median_rel_err_J_vs_fp64_lu": float(err_new.median())},
+            "plain_path": {"what": "per-incidence GMRES(50), FP32 matvec, same tolerance, timed on "
+                                   f"{len(sample)} of {nrhs} incidences and scaled",
+                           "ms_per_rhs": plain_ms_per_rhs, "median_iterations": statistics.median(iters_plain),
+                           "max_rel_err_J": max(errs_plain), "time_to_solution_ms": plain_total},
+            "speedup_vs_plain": plain_total / ms,
+            "roofline": {"bound": "tensor", "kernel": "tc_gemm_tf32x3_kernel (Z X, all right-hand sides)",
+                         "achieved": 3 * alg / (gemm_ms / 1e3) / 1e12, "peak": tf32_peak, "unit": "TFLOP/s",
+                         "frac": 3 * alg / (gemm_ms / 1e3) / 1e12 / tf32_peak, "traffic": None,
+                         "algorithmic": f"8 E^2 m = {alg:.3e} FLOP per product; executed 3x (split TF32)",
+                         "algorithmic_tflops": alg / (gemm_ms / 1e3) / 1e12, "kernel_ms": gemm_ms,
+                         "peak_source": "TF32 dense = half the measured bf16 dense rate (MEASURED_PEAKS.json)"},
+            "clocks": clocks.summary(), "gpu_launches": None}
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------------------
 def main():
@@ -517,6 +675,8 @@ def main():
         return main_rays(args, rank, world, local_rank)
     if args.workload.startswith("laplace_"):
         return main_laplace(args, rank, world, local_rank)
+    if args.workload.startswith("mrhs_"):
+        return main_mrhs(args, rank, world, local_rank)
     level, k, gq = WORKLOADS[args.workload]
     n_faces = 20 * 4 ** level
     n_edges = 30 * 4 ** level

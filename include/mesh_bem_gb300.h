@@ -224,6 +224,7 @@ int mb_cgemm_tf32x3(const float* z_hi, const float* z_lo, int64_t n, const float
                     void* workspace, size_t workspace_bytes, void* stream);
 int mb_cgemm_status(void* workspace, int64_t n, int64_t m, int32_t* status, void* stream);
 
+
 /* ---- Dense iterative solve (replaces torch.linalg.solve, mesh_BEM_solver_3d.py:174) -- */
 
 /* Outcome of mb_gmres_c64. status: 0 converged to tol, 1 stopped at max_iters. */
@@ -262,6 +263,21 @@ int mb_gmres_f32(const float* a, int64_t n, const double* b, double* x, int rest
 int mb_gmres_f64(const double* a, int64_t n, const double* b, double* x, int restart, int max_iters,
                  double tol, void* workspace, size_t workspace_bytes, mb_gmres_info* info,
                  void* stream);
+
+/* GMRES(restart) for m right-hand sides in lockstep (many incidences on one mesh; the
+ * reference solves one right-hand side per dense LU, mesh_BEM_solver_3d.py:174): Z X = B
+ * with Z given by its TF32 split (as for mb_cgemm_tf32x3), B, X complex128 [n, m]
+ * interleaved (X: initial guess in, solution out).  Every Arnoldi step multiplies all m
+ * basis vectors with one tensor-core product; basis, CGS2 and Givens rotations are FP64 per
+ * column; each restart cycle starts from B - Z X through the same product (attainable
+ * relative residual ~1e-6).  info: total Arnoldi steps, restart cycles, the largest
+ * per-column relative residual, status 0 when every column reached tol.  Workspace:
+ * mb_gmres_multi_workspace_bytes(n, m, restart) bytes (the FP64 basis dominates:
+ * 16 n m (restart + 1)). */
+size_t mb_gmres_multi_workspace_bytes(int64_t n, int64_t m, int restart);
+int mb_gmres_multi_c64(const float* z_hi, const float* z_lo, int64_t n, const double* b, double* x,
+                       int64_t m, int restart, int max_iters, double tol, void* workspace,
+                       size_t workspace_bytes, mb_gmres_info* info, void* stream);
 
 /* No counterpart in the reference.  The same solver as mb_gmres_c64 for callers that
  * cannot allocate device memory -- for example a host application or plugin that must

@@ -61,6 +61,8 @@ _SIGS = {
     "mb_cgemm_workspace_bytes": [_I64, _I64],
     "mb_cgemm_tf32x3": [_P, _P, _I64, _P, _I64, _P, _P, ctypes.c_size_t, _P],
     "mb_cgemm_status": [_P, _I64, _I64, _P, _P],
+    "mb_gmres_multi_workspace_bytes": [_I64, _I64, _I],
+    "mb_gmres_multi_c64": [_P, _P, _I64, _P, _P, _I64, _I, _I, _D, _P, ctypes.c_size_t, _P, _P],
     "mb_ray_bvh_bytes": [_I64],
     "mb_ray_bvh_build_f32": [_P, _I64, _P, _I64, _P, ctypes.c_size_t, _P],
     "mb_ray_query_f32": [_P, _I64, _P, _P, _I64, _I64, _D, _D, _P, _P],
@@ -78,7 +80,8 @@ _SIGS = {
 }
 
 _RESTYPES = {"mb_gmres_workspace_bytes": ctypes.c_size_t, "mb_ray_bvh_bytes": ctypes.c_size_t,
-             "mb_gmres_real_workspace_bytes": ctypes.c_size_t, "mb_cgemm_workspace_bytes": ctypes.c_size_t}
+             "mb_gmres_real_workspace_bytes": ctypes.c_size_t, "mb_cgemm_workspace_bytes": ctypes.c_size_t,
+             "mb_gmres_multi_workspace_bytes": ctypes.c_size_t}
 
 
 class GmresInfo(ctypes.Structure):

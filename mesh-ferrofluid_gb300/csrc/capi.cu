@@ -63,6 +63,10 @@ int split_tf32(const float* src, int64_t count, float* hi, float* lo, cudaStream
 int cgemm_tf32x3(const float* z_hi, const float* z_lo, int64_t n, const float* x, int64_t m, float* y, void* ws,
                  size_t ws_bytes, cudaStream_t s);
 int cgemm_status(void* ws, int64_t n, int64_t m, int* out, cudaStream_t s);
+size_t gmres_multi_workspace_bytes(int64_t n, int64_t m, int r);
+int gmres_multi(const float* z_hi, const float* z_lo, int64_t n, const double* b, double* x, int64_t m, int r,
+                int max_iters, double tol, void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out,
+                double* max_relres_out, int* status_out, cudaStream_t s);
 int gmres_real(int kind, const void* a, int64_t n, const double* b, double* x, int m, int max_iters, double tol,
                void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out, double* relres_out,
                int* status_out, cudaStream_t s);
@@ -420,6 +424,31 @@ int mb_cgemm_tf32x3(const float* z_hi, const float* z_lo, int64_t n, const float
 int mb_cgemm_status(void* workspace, int64_t n, int64_t m, int32_t* status, void* stream) {
     MB_REQUIRE(workspace && status && n > 0 && m > 0, "bad arguments");
     return cgemm_status(workspace, n, m, status, as_stream(stream));
+}
+
+size_t mb_gmres_multi_workspace_bytes(int64_t n, int64_t m, int restart) {
+    if (n <= 0 || m <= 0 || restart < 1) return 0;
+    return gmres_multi_workspace_bytes(n, m, restart);
+}
+
+int mb_gmres_multi_c64(const float* z_hi, const float* z_lo, int64_t n, const double* b, double* x, int64_t m,
+                       int restart, int max_iters, double tol, void* workspace, size_t workspace_bytes,
+                       mb_gmres_info* info, void* stream) {
+    MB_REQUIRE(n > 0 && m > 0, "n and m must be > 0");
+    MB_REQUIRE(z_hi && z_lo && b && x && workspace, "null pointer argument");
+    int64_t it = 0, cyc = 0;
+    double rr = 0.0;
+    int st = 1;
+    const int rc = gmres_multi(z_hi, z_lo, n, b, x, m, restart, max_iters, tol, workspace, workspace_bytes, &it,
+                               &cyc, &rr, &st, as_stream(stream));
+    if (rc == MB_OK && info) {
+        info->iterations = it;
+        info->restarts = cyc;
+        info->rel_residual = rr;
+        info->status = st;
+        info->reserved = 0;
+    }
+    return rc;
 }
 
 size_t mb_gmres_real_workspace_bytes(int64_t n, int restart) {

@@ -473,6 +473,36 @@ def multi_rhs_matmul(z_split, X, out=None, workspace=None, check: bool = False):
     return out
 
 
+def gmres_multi(z_split, B, X0=None, restart: int = 50, max_iters: int = 2000, tol: float = 1e-6,
+                workspace=None):
+    """Solve Z X = B for all columns of B in lockstep (``mb_gmres_multi_c64``).
+
+    z_split: (hi, lo) from ``split_tf32(Z)``; B: [n, m] (cast to complex128).  Every Arnoldi
+    step does one tensor-core product with all m basis vectors.  Returns (X complex128
+    [n, m], info dict with ``iterations`` (Arnoldi steps, shared by all columns),
+    ``restarts``, ``max_rel_residual`` and ``converged``).
+    """
+    hi, lo = z_split
+    n = hi.shape[0]
+    _lib.check_tensor(hi, "z_hi", dtype=torch.float32, ndim=2, shape=(n, 2 * n))
+    _lib.check_tensor(lo, "z_lo", dtype=torch.float32, device=hi.device, ndim=2, shape=(n, 2 * n))
+    dev = hi.device
+    bb = B.to(device=dev, dtype=torch.complex128).reshape(n, -1).contiguous()
+    m = bb.shape[1]
+    xx = torch.zeros_like(bb) if X0 is None else X0.to(device=dev, dtype=torch.complex128).reshape(n, m).clone()
+    need = int(_lib.load().mb_gmres_multi_workspace_bytes(int(n), int(m), int(restart)))
+    if workspace is None:
+        workspace = torch.empty(need, dtype=torch.uint8, device=dev)
+    elif workspace.numel() < need:
+        raise ValueError(f"workspace needs {need} bytes")
+    info = _lib.GmresInfo()
+    _lib.call("mb_gmres_multi_c64", _lib.ptr(hi), _lib.ptr(lo), n, _lib.ptr(bb), _lib.ptr(xx), m, int(restart),
+              int(max_iters), float(tol), _lib.ptr(workspace), workspace.numel(), __import__("ctypes").byref(info),
+              _lib.stream_of(hi))
+    return xx, {"iterations": info.iterations, "restarts": info.restarts, "max_rel_residual": info.rel_residual,
+                "converged": info.status == 0}
+
+
 def matvec(Z, v):
     """y = Z v (complex64 Z, v cast to complex64) with FP64 row sums -> complex128 [n]."""
     _lib.check_tensor(Z, "Z", dtype=torch.complex64, ndim=2)
