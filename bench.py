@@ -50,6 +50,8 @@ WORKLOADS = {
     # many incidences on one mesh: (ellipsoid level, k, Fibonacci directions x 2 polarisations)
     "mrhs_ell4": (4, 6.0, 256),
     "mrhs_ell4_efie": (4, 6.0, 256),
+    # the tensor-core product alone: (unknowns E, right-hand sides m)
+    "cgemm_E7680_m512": (7680, 512, 0),
 }
 
 
@@ -663,6 +665,62 @@ def main_mrhs(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def main_cgemm(args, rank, world, local_rank):
+    """Y = Z X on the tensor cores (split TF32 x 3) for E unknowns and m right-hand sides."""
+    n, m, _ = WORKLOADS[args.workload]
+    import torch
+
+    pkg = importlib.import_module("mesh-ferrofluid_gb300")
+    M = pkg.mesh_MOM_3d
+    config = {"workload": args.workload, "E": n, "m": m, "operands": "random complex64 Z [E, E], X [E, m]",
+              "l2": "Z split (2 x 8 E^2 bytes) > L2", "parallelism": "replicas"}
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no multi-right-hand-side "
+                              "product (one dense LU per right-hand side)"}), flush=True)
+        return
+    dev = torch.device("cuda", local_rank if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    g = torch.Generator(device=dev).manual_seed(0)
+    Z = torch.complex(torch.randn(n, n, device=dev, generator=g), torch.randn(n, n, device=dev, generator=g))
+    X = torch.complex(torch.randn(n, m, device=dev, generator=g), torch.randn(n, m, device=dev, generator=g))
+    split = M.split_tf32(Z)
+    del Z
+    ws = torch.empty(M.cgemm_workspace_bytes(n, m), dtype=torch.uint8, device=dev)
+    Y = torch.empty(n, m, dtype=torch.complex64, device=dev)
+    M.multi_rhs_matmul(split, X, out=Y, workspace=ws, check=True)
+    for _ in range(args.warmup):
+        M.multi_rhs_matmul(split, X, out=Y, workspace=ws)
+    torch.cuda.synchronize(dev)
+    stream = torch.cuda.current_stream(dev)
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        M.multi_rhs_matmul(split, X, out=Y, workspace=ws)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    alg = 8.0 * n * n * m
+    peaks = pkg.roofline.measured_peaks(REPO)
+    tf32_peak = float(peaks.get("bf16_tflops", 1900.0)) / 2.0
+    line = {"metric": "complex multi-RHS product, algorithmic TFLOP/s (8 E^2 m per product)",
+            "value": alg / (ms / 1e3) / 1e12, "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (split-tf32x3, FP32 accumulation)", "data": "synthetic",
+            "config": config,
+            "roofline": {"bound": "tensor", "achieved": 3 * alg / (ms / 1e3) / 1e12, "peak": tf32_peak,
+                         "unit": "TFLOP/s", "frac": 3 * alg / (ms / 1e3) / 1e12 / tf32_peak, "traffic": None,
+                         "algorithmic": "3 x 8 E^2 m executed TF32 FLOP per product",
+                         "peak_source": "TF32 dense = half the measured bf16 dense rate (MEASURED_PEAKS.json)"},
+            "clocks": clocks.summary(), "gpu_launches": 2 * args.steps}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------------------
@@ -677,6 +735,8 @@ def main():
         return main_laplace(args, rank, world, local_rank)
     if args.workload.startswith("mrhs_"):
         return main_mrhs(args, rank, world, local_rank)
+    if args.workload.startswith("cgemm_"):
+        return main_cgemm(args, rank, world, local_rank)
     level, k, gq = WORKLOADS[args.workload]
     n_faces = 20 * 4 ** level
     n_edges = 30 * 4 ** level

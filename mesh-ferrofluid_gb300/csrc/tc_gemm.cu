@@ -179,7 +179,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     uint32_t* tslot = reinterpret_cast<uint32_t*>(acce + 2);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int n0 = blockIdx.x * kTcBN, m0 = blockIdx.y * kTcBM;
-    const int nk = (K + kTcBK - 1) / kTcBK;
+    // split K: this CTA owns K-blocks [kb0, kb0 + nk) of the tile
+    const int nk_all = (K + kTcBK - 1) / kTcBK;
+    const int kb0 = (int)(((int64_t)nk_all * blockIdx.z) / gridDim.z);
+    const int nk = (int)(((int64_t)nk_all * (blockIdx.z + 1)) / gridDim.z) - kb0;
+    const bool split = gridDim.z > 1;
     const int nchunks = (nk + kTcChunk - 1) / kTcChunk;
     if (t == 0) {
         prefetch_tmap(&maps.a_hi);
@@ -213,7 +217,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 const uint32_t ph = (uint32_t)(kb / kTcStages) & 1u;
                 if (!mbar_wait(empty + s, ph ^ 1u, kWaitBudget, status, kTcTimeoutEmpty)) break;
                 mbar_arrive_expect_tx(full + s, kStageBytes);
-                const int kx = kb * kTcBK;
+                const int kx = (kb0 + kb) * kTcBK;
                 tma_load_2d(stage_ptr(s, 0), &maps.a_hi, full + s, kx, m0);
                 tma_load_2d(stage_ptr(s, 1), &maps.a_lo, full + s, kx, m0);
                 tma_load_2d(stage_ptr(s, 2), &maps.b_hi, full + s, kx, n0);
@@ -285,14 +289,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 float* drow = d + (int64_t)row * N;
                 const int col0 = n0 + col_base;
                 if ((N & 3) == 0 && col0 + 128 <= N) {
+                    float4* d4 = reinterpret_cast<float4*>(drow + col0);
 #pragma unroll
-                    for (int q = 0; q < 32; ++q)
-                        reinterpret_cast<float4*>(drow + col0)[q] =
-                            make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+                    for (int q = 0; q < 32; ++q) {
+                        const float4 v = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+                        if (split)
+                            atomicAdd(d4 + q, v);  // partial sums of the K split (D zeroed by the host)
+                        else
+                            d4[q] = v;
+                    }
                 } else {
 #pragma unroll
                     for (int i = 0; i < 128; ++i)
-                        if (col0 + i < N) drow[col0 + i] = acc[i];
+                        if (col0 + i < N) {
+                            if (split)
+                                atomicAdd(drow + col0 + i, acc[i]);
+                            else
+                                drow[col0 + i] = acc[i];
+                        }
                 }
             }
         }
@@ -391,7 +405,28 @@ int cgemm_tf32x3(const float* z_hi, const float* z_lo, int64_t n, const float* x
         attr_err = cudaFuncSetAttribute(tc_gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
     });
     if (attr_err != cudaSuccess) return set_error(MB_ERR_CUDA, "smem attribute: %s", cudaGetErrorString(attr_err));
-    const dim3 grid((unsigned)((N + kTcBN - 1) / kTcBN), (unsigned)((M + kTcBM - 1) / kTcBM));
+    // One CTA per SM.  Split K so the number of work items fills whole waves of the SMs
+    // (at least 16 K-blocks per item); split partials are added with vector atomics.
+    const int64_t tiles = ((N + kTcBN - 1) / kTcBN) * ((M + kTcBM - 1) / kTcBM);
+    const int64_t nk_all = (K + kTcBK - 1) / kTcBK;
+    int sms = 152;
+    {
+        int dev = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    int ksplit = 1;
+    double best = 0.0;
+    for (int ks = 1; ks <= 8; ++ks) {
+        if (ks > 1 && nk_all / ks < 16) break;
+        const double waves = (double)(tiles * ks) / sms;
+        const double eff = waves / std::ceil(waves);
+        if (eff > best + 0.02) {
+            best = eff;
+            ksplit = ks;
+        }
+    }
+    if (ksplit > 1) cudaMemsetAsync(y, 0, (size_t)M * N * 4, s);
+    const dim3 grid((unsigned)((N + kTcBN - 1) / kTcBN), (unsigned)((M + kTcBM - 1) / kTcBM), (unsigned)ksplit);
     if (grid.y > 65535) return set_error(MB_ERR_SIZE, "too many row tiles");
     tc_gemm_tf32x3_kernel<<<grid, kTcThreads, kTcSmem, s>>>(maps, (int)M, (int)N, (int)K, y, status);
     return check_launch("cgemm_tf32x3");
