@@ -279,6 +279,67 @@ int mb_gmres_multi_c64(const float* z_hi, const float* z_lo, int64_t n, const do
                        int64_t m, int restart, int max_iters, double tol, void* workspace,
                        size_t workspace_bytes, mb_gmres_info* info, void* stream);
 
+/* ---- Many meshes at once (batched assembly and solve; no counterpart in the reference,
+ * which handles one mesh per solver call) ---------------------------------------------------
+ * The meshes are packed into one vertex array and one face array (vertex ids global);
+ * fei [sum F_i, 3] holds each mesh's local RWG edge ids; desc [n_mesh, 6] int64 =
+ * (first face, faces F_i, edges E_i, offset of Z_i in the flat block-diagonal array in
+ * complex entries, first block of the mesh in the regular launch = sum over earlier meshes
+ * of F_j ceil(F_j / 128), first right-hand-side column); ks [n_mesh] the wavenumbers.
+ * mb_mom_sym_zmat_batched_*: the symmetric-rule EFIE (as mb_mom_sym_zmat_rwg_* +
+ * mb_mom_sym_near_*) of every mesh in one launch of each kernel, accumulated into the flat
+ * array (caller zeroes); total_blocks = the block count above; near_pairs [n_near, 2]
+ * global face ids of all pairs sharing a vertex.
+ * mb_mom_sym_rhs_batched_*: nrhs plane waves per mesh (waves [n_mesh * nrhs, 9]) into the
+ * padded block rhs [max E_i, ld] (row = local edge, column desc[i][5] + r; accumulated). */
+int mb_mom_sym_zmat_batched_c64(const float* verts, const int32_t* faces, const int32_t* fei,
+                                const int64_t* desc, const double* ks, int n_mesh, int64_t total_blocks,
+                                const int32_t* near_pairs, int64_t n_near, float* z, void* stream);
+int mb_mom_sym_zmat_batched_c128(const double* verts, const int32_t* faces, const int32_t* fei,
+                                 const int64_t* desc, const double* ks, int n_mesh, int64_t total_blocks,
+                                 const int32_t* near_pairs, int64_t n_near, double* z, void* stream);
+int mb_mom_sym_rhs_batched_c64(const float* verts, const int32_t* faces, const int32_t* fei,
+                               const int64_t* desc, int n_mesh, int64_t total_faces, const double* waves,
+                               int nrhs, int64_t ld, float* rhs, void* stream);
+int mb_mom_sym_rhs_batched_c128(const double* verts, const int32_t* faces, const int32_t* fei,
+                                const int64_t* desc, int n_mesh, int64_t total_faces, const double* waves,
+                                int nrhs, int64_t ld, double* rhs, void* stream);
+
+/* The reference's operator and rule (as mb_mom_zmat_rwg_c64 / mb_mom_rhs_rwg_c64) for every
+ * mesh of the batch in one launch each: face_areas, face_normals per packed face;
+ * block_offsets [n_mesh + 1] = first block of each mesh with 3 F_i rows of
+ * ceil(3 F_i / 128) blocks (total_blocks = the last entry); gaussQR (nx = gaussQR, ny =
+ * gaussQR - 1) in {2, 3, 4, 5}.  Excitation <f, E + n x H> of nrhs waves per mesh (waves
+ * [n_mesh * nrhs, 9]) into the padded block rhs [max E_i, ld]. */
+int mb_mom_ref_zmat_batched_c64(const float* verts, const int32_t* faces, const float* face_areas,
+                                const float* face_normals, const int32_t* fei, const int64_t* desc,
+                                const int64_t* block_offsets, int64_t total_blocks, const double* ks,
+                                int n_mesh, const float* gpx, const float* gwx, int nx, const float* gpy,
+                                const float* gwy, int ny, float* z, void* stream);
+int mb_mom_ref_rhs_batched_c64(const float* verts, const int32_t* faces, const float* face_areas,
+                               const float* face_normals, const int32_t* fei, const int64_t* desc,
+                               int n_mesh, int64_t total_faces, const float* gp, const float* gw, int n,
+                               const double* waves, int nrhs, int64_t ld, float* rhs, void* stream);
+
+/* Block-diagonal product over the batch: y[r, c] = sum_l Z_i[r, l] x[l, c] for the nc
+ * columns of mesh i (x, y complex64 [max E_i, ld], ld = n_mesh * nc); goff [n_mesh + 1] =
+ * first warp of each mesh with rows_per_warp (1, 2, 4 or 8; 8 for nc <= 4) rows per warp,
+ * goff[n_mesh] = total_warps.  nc in {1, 2, 4, 8}.  Rows beyond E_i are not written. */
+int mb_blockdiag_matvec_c64(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh,
+                            int64_t total_warps, const float* x, int64_t ld, int nc, int rows_per_warp,
+                            float* y, void* stream);
+
+/* GMRES(restart) on every mesh and right-hand side of the batch in lockstep (the algorithm
+ * of mb_gmres_multi_c64 with the block-diagonal product): b, x complex128 [n_rows, n_mesh *
+ * nc] padded (rows beyond E_i zero).  use_graph: capture the restart cycle's Arnoldi steps
+ * once as a CUDA graph and replay it (no host synchronisation inside a cycle; iterations
+ * are counted in whole cycles).  Workspace: mb_gmres_blockdiag_workspace_bytes. */
+size_t mb_gmres_blockdiag_workspace_bytes(int64_t n_rows, int64_t m, int restart);
+int mb_gmres_blockdiag_c64(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh,
+                           int64_t total_warps, int rows_per_warp, int nc, int64_t n_rows, const double* b,
+                           double* x, int restart, int max_iters, double tol, int use_graph, void* workspace,
+                           size_t workspace_bytes, mb_gmres_info* info, void* stream);
+
 /* No counterpart in the reference.  The same solver as mb_gmres_c64 for callers that
  * cannot allocate device memory -- for example a host application or plugin that must
  * budget all GPU memory at start-up, or a foreign-language caller (Go, Java, ...) that has

@@ -62,6 +62,16 @@ _SIGS = {
     "mb_cgemm_tf32x3": [_P, _P, _I64, _P, _I64, _P, _P, ctypes.c_size_t, _P],
     "mb_cgemm_status": [_P, _I64, _I64, _P, _P],
     "mb_gmres_multi_workspace_bytes": [_I64, _I64, _I],
+    "mb_mom_sym_zmat_batched_c64": [_P, _P, _P, _P, _P, _I, _I64, _P, _I64, _P, _P],
+    "mb_mom_sym_zmat_batched_c128": [_P, _P, _P, _P, _P, _I, _I64, _P, _I64, _P, _P],
+    "mb_mom_sym_rhs_batched_c64": [_P, _P, _P, _P, _I, _I64, _P, _I, _I64, _P, _P],
+    "mb_mom_sym_rhs_batched_c128": [_P, _P, _P, _P, _I, _I64, _P, _I, _I64, _P, _P],
+    "mb_mom_ref_zmat_batched_c64": [_P, _P, _P, _P, _P, _P, _P, _I64, _P, _I, _P, _P, _I, _P, _P, _I, _P, _P],
+    "mb_mom_ref_rhs_batched_c64": [_P, _P, _P, _P, _P, _P, _I, _I64, _P, _P, _I, _P, _I, _I64, _P, _P],
+    "mb_blockdiag_matvec_c64": [_P, _P, _P, _I, _I64, _P, _I64, _I, _I, _P, _P],
+    "mb_gmres_blockdiag_workspace_bytes": [_I64, _I64, _I],
+    "mb_gmres_blockdiag_c64": [_P, _P, _P, _I, _I64, _I, _I, _I64, _P, _P, _I, _I, _D, _I, _P, ctypes.c_size_t,
+                               _P, _P],
     "mb_gmres_multi_c64": [_P, _P, _I64, _P, _P, _I64, _I, _I, _D, _P, ctypes.c_size_t, _P, _P],
     "mb_ray_bvh_bytes": [_I64],
     "mb_ray_bvh_build_f32": [_P, _I64, _P, _I64, _P, ctypes.c_size_t, _P],
@@ -81,7 +91,8 @@ _SIGS = {
 
 _RESTYPES = {"mb_gmres_workspace_bytes": ctypes.c_size_t, "mb_ray_bvh_bytes": ctypes.c_size_t,
              "mb_gmres_real_workspace_bytes": ctypes.c_size_t, "mb_cgemm_workspace_bytes": ctypes.c_size_t,
-             "mb_gmres_multi_workspace_bytes": ctypes.c_size_t}
+             "mb_gmres_multi_workspace_bytes": ctypes.c_size_t,
+             "mb_gmres_blockdiag_workspace_bytes": ctypes.c_size_t}
 
 
 class GmresInfo(ctypes.Structure):

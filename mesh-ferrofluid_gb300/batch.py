@@ -1,0 +1,215 @@
+"""Many meshes at once: batched assembly and solve of the MoM systems.
+
+The reference handles one mesh per ``MeshBEMSolver3d`` call.  ``MeshBatch`` packs any number
+of meshes of uneven size (and wavenumber) into one vertex / face array and runs
+
+* the assembly of every mesh's impedance matrix into one flat block-diagonal array: with
+  ``formulation="efie_sym"`` (the 7-point-rule EFIE, pairs sharing a vertex in FP64) one
+  launch of the separated-pair kernel and one of the near-pair kernel
+  (``mb_mom_sym_zmat_batched_c64``); with ``formulation="cfie_ref"`` (the reference's EFIE +
+  MFIE operator and collapsed Gauss rule, gaussQR 4) one launch
+  (``mb_mom_ref_zmat_batched_c64``);
+* the excitation of ``nc`` plane waves per mesh in one launch (``mb_mom_sym_rhs_batched_c64``)
+  into a padded block [max E_i, n_mesh * nc];
+* GMRES on every (mesh, wave) column in lockstep with the block-diagonal product
+  (``mb_gmres_blockdiag_c64``), each restart cycle replayed from a captured CUDA graph; the
+  product's tile shape (rows per warp) is picked by timing the candidates once
+  (``autotune``).
+
+All data live on one CUDA device; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import List, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+from .utils import compute_panel_relation, get_edge_unique
+
+_DESC = 6
+
+
+class MeshBatch:
+    """A batch of triangle meshes with their wavenumbers, packed for batched kernels."""
+
+    def __init__(self, meshes: Sequence, wavenumbers: Sequence[float], device=None, formulation: str = "efie_sym",
+                 gaussQR: int = 4):
+        if len(meshes) != len(wavenumbers) or not meshes:
+            raise ValueError("need one wavenumber per mesh and at least one mesh")
+        if formulation not in ("efie_sym", "cfie_ref"):
+            raise ValueError(f"unknown formulation {formulation!r} (efie_sym or cfie_ref)")
+        self.formulation = formulation
+        dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.device = dev
+        verts, faces, fei, near = [], [], [], []
+        desc = np.zeros((len(meshes), _DESC), np.int64)
+        v_off = f_off = z_off = blk = 0
+        self.n_edges: List[int] = []
+        for i, (v, f) in enumerate(meshes):
+            v = torch.as_tensor(np.asarray(v), dtype=torch.float32).to(dev)
+            f = torch.as_tensor(np.asarray(f)).to(device=dev, dtype=torch.int32)
+            edges, fe, _ = get_edge_unique(v, f)
+            ne, nf = int(edges.shape[0]), int(f.shape[0])
+            rel = compute_panel_relation(f)
+            near.append(torch.nonzero(rel > 0).to(torch.int32) + f_off)
+            verts.append(v)
+            faces.append(f + v_off)
+            fei.append(fe.reshape(-1, 3).to(torch.int32))
+            desc[i] = (f_off, nf, ne, z_off, blk, 0)
+            self.n_edges.append(ne)
+            v_off += v.shape[0]
+            f_off += nf
+            z_off += ne * ne
+            blk += nf * ((nf + 127) // 128)
+        self.n_mesh = len(meshes)
+        self.verts = torch.cat(verts).contiguous()
+        self.faces = torch.cat(faces).contiguous()
+        self.fei = torch.cat(fei).contiguous()
+        self.near = torch.cat(near).contiguous()
+        self.total_faces = f_off
+        self.total_blocks = blk
+        self.z_size = z_off
+        self.n_rows = max(self.n_edges)
+        self._desc_np = desc
+        if formulation == "cfie_ref":
+            from .utils import compute_face_areas, compute_face_normals, \
+                get_gaussion_integration_points_and_weights
+
+            self.areas = compute_face_areas(self.verts, self.faces).reshape(-1).contiguous()
+            self.normals = compute_face_normals(self.verts, self.faces).contiguous()
+            self.gq = gaussQR
+            self.gpx, self.gwx = get_gaussion_integration_points_and_weights(gaussQR, device=dev)
+            self.gpy, self.gwy = get_gaussion_integration_points_and_weights(gaussQR - 1, device=dev)
+            nfs = desc[:, 1]
+            per = 3 * nfs * ((3 * nfs + 127) // 128)
+            self.ref_boff = torch.tensor(np.concatenate([[0], np.cumsum(per)]).astype(np.int64), device=dev)
+        self.ks = torch.tensor(np.asarray(wavenumbers, np.float64), device=dev)
+        if not bool(torch.all(self.ks > 0)):
+            raise ValueError("wavenumbers must be > 0")
+        self.nc = None
+        self.desc = None
+        self.rows_per_warp = None
+        self._goff = {}
+
+    # -- layout --------------------------------------------------------------------------
+    def _set_nc(self, nc: int):
+        if self.nc == nc:
+            return
+        d = self._desc_np.copy()
+        d[:, 5] = np.arange(self.n_mesh) * nc
+        self.desc = torch.tensor(d, device=self.device)
+        self.nc = nc
+
+    def _warp_offsets(self, rows: int):
+        if rows not in self._goff:
+            per = [(e + rows - 1) // rows for e in self.n_edges]
+            off = np.concatenate([[0], np.cumsum(per)]).astype(np.int64)
+            self._goff[rows] = torch.tensor(off, device=self.device)
+        return self._goff[rows]
+
+    def z_block(self, z_flat: torch.Tensor, i: int) -> torch.Tensor:
+        """View of mesh i's impedance matrix [E_i, E_i] in the flat array."""
+        o, e = int(self._desc_np[i, 3]), self.n_edges[i]
+        return z_flat[o:o + e * e].view(e, e)
+
+    def column(self, X: torch.Tensor, i: int, r: int) -> torch.Tensor:
+        """Mesh i, right-hand side r of a padded [n_rows, n_mesh * nc] block."""
+        return X[: self.n_edges[i], i * self.nc + r]
+
+    # -- kernels -------------------------------------------------------------------------
+    def assemble(self, out: torch.Tensor | None = None) -> torch.Tensor:
+        """All impedance matrices, flat complex64 [sum E_i^2] (one launch per kernel)."""
+        if self.desc is None:
+            self._set_nc(1)
+        if out is None:
+            out = torch.zeros(self.z_size, dtype=torch.complex64, device=self.device)
+        else:
+            _lib.check_tensor(out, "out", dtype=torch.complex64, device=self.device)
+            out.zero_()
+        if self.formulation == "cfie_ref":
+            _lib.call("mb_mom_ref_zmat_batched_c64", _lib.ptr(self.verts), _lib.ptr(self.faces), _lib.ptr(self.areas),
+                      _lib.ptr(self.normals), _lib.ptr(self.fei), _lib.ptr(self.desc), _lib.ptr(self.ref_boff),
+                      int(self.ref_boff[-1]), _lib.ptr(self.ks), self.n_mesh, _lib.ptr(self.gpx), _lib.ptr(self.gwx),
+                      self.gq, _lib.ptr(self.gpy), _lib.ptr(self.gwy), self.gq - 1, _lib.ptr(out),
+                      _lib.stream_of(out))
+            return out
+        _lib.call("mb_mom_sym_zmat_batched_c64", _lib.ptr(self.verts), _lib.ptr(self.faces), _lib.ptr(self.fei),
+                  _lib.ptr(self.desc), _lib.ptr(self.ks), self.n_mesh, self.total_blocks, _lib.ptr(self.near),
+                  self.near.shape[0], _lib.ptr(out), _lib.stream_of(out))
+        return out
+
+    def excitation(self, waves: torch.Tensor) -> torch.Tensor:
+        """waves [n_mesh, nc, 9] (``mesh_MOM_3d.plane_waves`` records) -> B complex64
+        [n_rows, n_mesh * nc], rows beyond E_i zero."""
+        waves = waves.to(device=self.device, dtype=torch.float64).contiguous()
+        if waves.dim() != 3 or waves.shape[0] != self.n_mesh or waves.shape[2] != 9:
+            raise ValueError("waves must be [n_mesh, nc, 9]")
+        nc = waves.shape[1]
+        self._set_nc(nc)
+        B = torch.zeros((self.n_rows, self.n_mesh * nc), dtype=torch.complex64, device=self.device)
+        if self.formulation == "cfie_ref":
+            _lib.call("mb_mom_ref_rhs_batched_c64", _lib.ptr(self.verts), _lib.ptr(self.faces), _lib.ptr(self.areas),
+                      _lib.ptr(self.normals), _lib.ptr(self.fei), _lib.ptr(self.desc), self.n_mesh,
+                      self.total_faces, _lib.ptr(self.gpx), _lib.ptr(self.gwx), self.gq, _lib.ptr(waves), nc,
+                      self.n_mesh * nc, _lib.ptr(B), _lib.stream_of(B))
+            return B
+        _lib.call("mb_mom_sym_rhs_batched_c64", _lib.ptr(self.verts), _lib.ptr(self.faces), _lib.ptr(self.fei),
+                  _lib.ptr(self.desc), self.n_mesh, self.total_faces, _lib.ptr(waves), nc, self.n_mesh * nc,
+                  _lib.ptr(B), _lib.stream_of(B))
+        return B
+
+    def matvec(self, z_flat: torch.Tensor, X: torch.Tensor, rows_per_warp: int | None = None,
+               out: torch.Tensor | None = None) -> torch.Tensor:
+        """Block-diagonal product Y = blockdiag(Z_i) X on the padded layout (complex64)."""
+        rows = rows_per_warp or self.rows_per_warp or 2
+        goff = self._warp_offsets(rows)
+        if out is None:
+            out = torch.zeros_like(X)
+        _lib.call("mb_blockdiag_matvec_c64", _lib.ptr(z_flat), _lib.ptr(self.desc), _lib.ptr(goff), self.n_mesh,
+                  int(goff[-1]), _lib.ptr(X), X.shape[1], self.nc, rows, _lib.ptr(out), _lib.stream_of(X))
+        return out
+
+    def autotune(self, z_flat: torch.Tensor, candidates=(1, 2, 4, 8), reps: int = 3) -> int:
+        """Pick the block-diagonal product's rows per warp by timing each candidate."""
+        X = torch.randn(self.n_rows, self.n_mesh * self.nc, dtype=torch.complex64, device=self.device)
+        Y = torch.zeros_like(X)
+        best, best_t = None, None
+        for rows in candidates:
+            if rows == 8 and self.nc > 4:
+                continue
+            self.matvec(z_flat, X, rows, out=Y)  # warm-up
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                self.matvec(z_flat, X, rows, out=Y)
+            e1.record()
+            torch.cuda.synchronize(self.device)
+            t = e0.elapsed_time(e1)
+            if best_t is None or t < best_t:
+                best, best_t = rows, t
+        self.rows_per_warp = best
+        return best
+
+    def solve(self, z_flat: torch.Tensor, B: torch.Tensor, restart: int = 50, max_iters: int = 2000,
+              tol: float = 1e-6, use_graph: bool = True, workspace=None):
+        """Lockstep GMRES on every (mesh, wave) column -> (X complex128 padded, info dict)."""
+        if self.nc is None:
+            raise RuntimeError("call excitation() first")
+        rows = self.rows_per_warp or 2
+        goff = self._warp_offsets(rows)
+        m = self.n_mesh * self.nc
+        bb = B.to(torch.complex128).contiguous()
+        X = torch.zeros_like(bb)
+        need = int(_lib.load().mb_gmres_blockdiag_workspace_bytes(self.n_rows, m, int(restart)))
+        if workspace is None:
+            workspace = torch.empty(need, dtype=torch.uint8, device=self.device)
+        info = _lib.GmresInfo()
+        _lib.call("mb_gmres_blockdiag_c64", _lib.ptr(z_flat), _lib.ptr(self.desc), _lib.ptr(goff), self.n_mesh,
+                  int(goff[-1]), rows, self.nc, self.n_rows, _lib.ptr(bb), _lib.ptr(X), int(restart), int(max_iters),
+                  float(tol), 1 if use_graph else 0, _lib.ptr(workspace), workspace.numel(), ctypes.byref(info),
+                  _lib.stream_of(bb))
+        return X, {"iterations": info.iterations, "restarts": info.restarts, "max_rel_residual": info.rel_residual,
+                   "converged": info.status == 0}

@@ -38,6 +38,12 @@ int launch_mom_ref_zmat(const T*, int64_t, const int32_t*, int64_t, const T*, co
 template <typename T>
 int launch_mom_ref_rhs(const T*, const int32_t*, int64_t, const T*, const T*, const T*, const T*, int,
                        const PlaneWave*, double, int, int, int64_t, const int32_t*, T*, T*, cudaStream_t);
+int launch_mom_ref_zmat_batched(const float*, const int32_t*, const float*, const float*, const int32_t*,
+                                const int64_t*, const int64_t*, int64_t, const double*, int, const float*, const float*,
+                                int, const float*, const float*, int, float*, cudaStream_t);
+template <typename T>
+int launch_mom_ref_rhs_batched(const T*, const int32_t*, const T*, const T*, const int32_t*, const int64_t*, int,
+                               int64_t, const T*, const T*, int, const PlaneWave*, int, int64_t, T*, cudaStream_t);
 template <typename T>
 int launch_mom_interp(const T*, const int32_t*, const int32_t*, const T*, const T*, const T*, int64_t,
                       int64_t, int64_t, int64_t, int, T*, T*, cudaStream_t);
@@ -64,6 +70,19 @@ int cgemm_tf32x3(const float* z_hi, const float* z_lo, int64_t n, const float* x
                  size_t ws_bytes, cudaStream_t s);
 int cgemm_status(void* ws, int64_t n, int64_t m, int* out, cudaStream_t s);
 size_t gmres_multi_workspace_bytes(int64_t n, int64_t m, int r);
+size_t gmres_blockdiag_workspace_bytes(int64_t n, int64_t m, int r);
+int blockdiag_matvec(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
+                     const float* x, int64_t ld, int nc, int rows, float* y, cudaStream_t s);
+int gmres_blockdiag(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
+                    int rows_per_warp, int nc, int64_t n_rows, const double* b, double* x, int r, int max_iters,
+                    double tol, bool use_graph, void* workspace, size_t ws_bytes, int64_t* iters_out,
+                    int64_t* cycles_out, double* max_relres_out, int* status_out, cudaStream_t s);
+template <typename T>
+int launch_mom_sym_batched(const T*, const int32_t*, const int32_t*, const int64_t*, const double*, int, int64_t,
+                           const int32_t*, int64_t, T*, cudaStream_t);
+template <typename T>
+int launch_mom_sym_rhs_batched(const T*, const int32_t*, const int32_t*, const int64_t*, int, int64_t, const double*,
+                               int, int64_t, T*, cudaStream_t);
 int gmres_multi(const float* z_hi, const float* z_lo, int64_t n, const double* b, double* x, int64_t m, int r,
                 int max_iters, double tol, void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out,
                 double* max_relres_out, int* status_out, cudaStream_t s);
@@ -441,6 +460,94 @@ int mb_gmres_multi_c64(const float* z_hi, const float* z_lo, int64_t n, const do
     int st = 1;
     const int rc = gmres_multi(z_hi, z_lo, n, b, x, m, restart, max_iters, tol, workspace, workspace_bytes, &it,
                                &cyc, &rr, &st, as_stream(stream));
+    if (rc == MB_OK && info) {
+        info->iterations = it;
+        info->restarts = cyc;
+        info->rel_residual = rr;
+        info->status = st;
+        info->reserved = 0;
+    }
+    return rc;
+}
+
+#define MB_BATCH(SFX, T)                                                                              \
+    int mb_mom_sym_zmat_batched_##SFX(const T* verts, const int32_t* faces, const int32_t* fei,         \
+                                      const int64_t* desc, const double* ks, int n_mesh,               \
+                                      int64_t total_blocks, const int32_t* near_pairs, int64_t n_near, \
+                                      T* z, void* stream) {                                            \
+        MB_REQUIRE(n_mesh >= 0 && total_blocks >= 0 && n_near >= 0, "bad sizes");                     \
+        if (n_mesh == 0) return MB_OK;                                                                \
+        MB_REQUIRE(verts && faces && fei && desc && ks && z && (near_pairs || n_near == 0),           \
+                   "null pointer argument");                                                          \
+        return launch_mom_sym_batched<T>(verts, faces, fei, desc, ks, n_mesh, total_blocks, near_pairs, \
+                                         n_near, z, as_stream(stream));                              \
+    }                                                                                                 \
+    int mb_mom_sym_rhs_batched_##SFX(const T* verts, const int32_t* faces, const int32_t* fei,          \
+                                     const int64_t* desc, int n_mesh, int64_t total_faces,              \
+                                     const double* waves, int nrhs, int64_t ld, T* rhs, void* stream) { \
+        MB_REQUIRE(n_mesh >= 0 && total_faces >= 0 && nrhs >= 0 && ld >= 0, "bad sizes");             \
+        if (n_mesh == 0 || total_faces == 0 || nrhs == 0) return MB_OK;                               \
+        MB_REQUIRE(verts && faces && fei && desc && waves && rhs, "null pointer argument");           \
+        return launch_mom_sym_rhs_batched<T>(verts, faces, fei, desc, n_mesh, total_faces, waves, nrhs, \
+                                             ld, rhs, as_stream(stream));                            \
+    }
+MB_BATCH(c64, float)
+MB_BATCH(c128, double)
+#undef MB_BATCH
+
+int mb_mom_ref_zmat_batched_c64(const float* verts, const int32_t* faces, const float* face_areas,
+                                const float* face_normals, const int32_t* fei, const int64_t* desc,
+                                const int64_t* block_offsets, int64_t total_blocks, const double* ks, int n_mesh,
+                                const float* gpx, const float* gwx, int nx, const float* gpy, const float* gwy,
+                                int ny, float* z, void* stream) {
+    MB_REQUIRE(n_mesh >= 0 && total_blocks >= 0, "bad sizes");
+    if (n_mesh == 0) return MB_OK;
+    MB_REQUIRE(verts && faces && face_areas && face_normals && fei && desc && block_offsets && ks && gpx && gwx &&
+                   gpy && gwy && z,
+               "null pointer argument");
+    return launch_mom_ref_zmat_batched(verts, faces, face_areas, face_normals, fei, desc, block_offsets,
+                                       total_blocks, ks, n_mesh, gpx, gwx, nx, gpy, gwy, ny, z, as_stream(stream));
+}
+
+int mb_mom_ref_rhs_batched_c64(const float* verts, const int32_t* faces, const float* face_areas,
+                               const float* face_normals, const int32_t* fei, const int64_t* desc, int n_mesh,
+                               int64_t total_faces, const float* gp, const float* gw, int n, const double* waves,
+                               int nrhs, int64_t ld, float* rhs, void* stream) {
+    MB_REQUIRE(n_mesh >= 0 && total_faces >= 0 && nrhs >= 0, "bad sizes");
+    if (n_mesh == 0 || total_faces == 0 || nrhs == 0) return MB_OK;
+    MB_REQUIRE(verts && faces && face_areas && face_normals && fei && desc && gp && gw && waves && rhs,
+               "null pointer argument");
+    return launch_mom_ref_rhs_batched<float>(verts, faces, face_areas, face_normals, fei, desc, n_mesh, total_faces,
+                                             gp, gw, n, reinterpret_cast<const PlaneWave*>(waves), nrhs, ld, rhs,
+                                             as_stream(stream));
+}
+
+int mb_blockdiag_matvec_c64(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh,
+                            int64_t total_warps, const float* x, int64_t ld, int nc, int rows_per_warp, float* y,
+                            void* stream) {
+    MB_REQUIRE(n_mesh >= 0 && total_warps >= 0, "bad sizes");
+    if (n_mesh == 0) return MB_OK;
+    MB_REQUIRE(z && desc && goff && x && y, "null pointer argument");
+    return blockdiag_matvec(z, desc, goff, n_mesh, total_warps, x, ld, nc, rows_per_warp, y, as_stream(stream));
+}
+
+size_t mb_gmres_blockdiag_workspace_bytes(int64_t n_rows, int64_t m, int restart) {
+    if (n_rows <= 0 || m <= 0 || restart < 1) return 0;
+    return gmres_blockdiag_workspace_bytes(n_rows, m, restart);
+}
+
+int mb_gmres_blockdiag_c64(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
+                           int rows_per_warp, int nc, int64_t n_rows, const double* b, double* x, int restart,
+                           int max_iters, double tol, int use_graph, void* workspace, size_t workspace_bytes,
+                           mb_gmres_info* info, void* stream) {
+    MB_REQUIRE(n_mesh > 0 && nc > 0 && n_rows > 0, "bad sizes");
+    MB_REQUIRE(z && desc && goff && b && x && workspace, "null pointer argument");
+    int64_t it = 0, cyc = 0;
+    double rr = 0.0;
+    int st = 1;
+    const int rc = gmres_blockdiag(z, desc, goff, n_mesh, total_warps, rows_per_warp, nc, n_rows, b, x, restart,
+                                   max_iters, tol, use_graph != 0, workspace, workspace_bytes, &it, &cyc, &rr, &st,
+                                   as_stream(stream));
     if (rc == MB_OK && info) {
         info->iterations = it;
         info->restarts = cyc;

@@ -49,7 +49,7 @@ struct MgWork {
 
 static size_t a256(size_t b) { return (b + 255) & ~size_t(255); }
 
-static size_t mg_layout(int64_t n, int64_t m, int r, void* base, MgWork* W) {
+static size_t mg_layout(int64_t n, int64_t m, int r, size_t prod_ws, void* base, MgWork* W) {
     const size_t nm = (size_t)n * m;
     size_t off = 0;
     char* p = static_cast<char*>(base);
@@ -62,7 +62,7 @@ static size_t mg_layout(int64_t n, int64_t m, int r, void* base, MgWork* W) {
     W->w = static_cast<double*>(take(16 * nm));
     W->v32 = static_cast<float*>(take(8 * nm));
     W->y32 = static_cast<float*>(take(8 * nm));
-    W->gemm_ws = take(cgemm_workspace_bytes(n, m));
+    W->gemm_ws = prod_ws ? take(prod_ws) : nullptr;
     W->H = static_cast<double*>(take(16 * (size_t)(r + 1) * r * m));
     W->hc = static_cast<double*>(take(16 * (size_t)(r + 1) * m));
     W->cs = static_cast<double*>(take(16 * (size_t)r * m));
@@ -80,7 +80,12 @@ static size_t mg_layout(int64_t n, int64_t m, int r, void* base, MgWork* W) {
 
 size_t gmres_multi_workspace_bytes(int64_t n, int64_t m, int r) {
     MgWork W;
-    return mg_layout(n, m, r, nullptr, &W);
+    return mg_layout(n, m, r, cgemm_workspace_bytes(n, m), nullptr, &W);
+}
+
+size_t gmres_blockdiag_workspace_bytes(int64_t n, int64_t m, int r) {
+    MgWork W;
+    return mg_layout(n, m, r, 0, nullptr, &W);
 }
 
 // ---- kernels ---------------------------------------------------------------------------
@@ -175,6 +180,7 @@ __global__ void mg_subtract(const double* __restrict__ V, const double* __restri
     if (idx >= n * m) return;
     const int64_t c = idx % m;
     double wr = w[2 * idx], wi = w[2 * idx + 1];
+#pragma unroll 4
     for (int i = 0; i < nb; ++i) {
         const double hr = hc[2 * ((int64_t)i * m + c)], hi = hc[2 * ((int64_t)i * m + c) + 1];
         const double vr = V[2 * ((int64_t)i * n * m + idx)], vi = V[2 * ((int64_t)i * n * m + idx) + 1];
@@ -336,6 +342,7 @@ __global__ void mg_update(const double* __restrict__ V, const double* __restrict
     if (idx >= n * m) return;
     const int64_t c = idx % m;
     double xr = x[2 * idx], xi = x[2 * idx + 1];
+#pragma unroll 4
     for (int i = 0; i < nb; ++i) {
         const double yr = yv[2 * ((int64_t)i * m + c)], yi = yv[2 * ((int64_t)i * m + c) + 1];
         const double vr = V[2 * ((int64_t)i * n * m + idx)], vi = V[2 * ((int64_t)i * n * m + idx) + 1];
@@ -346,6 +353,104 @@ __global__ void mg_update(const double* __restrict__ V, const double* __restrict
     x[2 * idx + 1] = xi;
 }
 
+// ---- block-diagonal product (many meshes) ------------------------------------------------
+// desc[i] = (face offset, faces, edges E_i, offset of Z_i in the flat array (complex entries),
+// -, first right-hand-side column); goff[i] = first warp of mesh i (each warp owns ROWS rows,
+// goff[n_mesh] = total warps).  y[r, col + c] = sum_l Z_i[r, l] x[l, col + c] for the NC
+// columns of mesh i; x, y: [rows_max, ld] interleaved complex64; FP32 products, FP32 lane
+// sums, warp reduction.  Rows of the padded block beyond E_i are never written.
+__device__ __forceinline__ int seg_of(const int64_t* __restrict__ off, int n, int64_t v) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(off + mid) <= v) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int ROWS, int NC>
+__global__ void __launch_bounds__(256) blockdiag_matvec_kernel(const float* __restrict__ z,
+                                                               const int64_t* __restrict__ desc,
+                                                               const int64_t* __restrict__ goff, int n_mesh,
+                                                               const float* __restrict__ x, int64_t ld,
+                                                               float* __restrict__ y) {
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= __ldg(goff + n_mesh)) return;
+    const int i = seg_of(goff, n_mesh, w);
+    const int64_t E = __ldg(desc + 6 * i + 2), zo = __ldg(desc + 6 * i + 3), co = __ldg(desc + 6 * i + 5);
+    const int64_t r0 = (w - __ldg(goff + i)) * ROWS;
+    const float2* zc = reinterpret_cast<const float2*>(z) + zo;
+    const float2* xc = reinterpret_cast<const float2*>(x);
+    float ar[ROWS][NC], ai[ROWS][NC];
+#pragma unroll
+    for (int q = 0; q < ROWS; ++q)
+#pragma unroll
+        for (int c = 0; c < NC; ++c) ar[q][c] = ai[q][c] = 0.f;
+    // the NC complex64 of x[l, co ..] are contiguous: 16-byte loads when NC is even
+    const bool vec = (NC % 2 == 0) && ((ld & 1) == 0) && ((co & 1) == 0);
+#pragma unroll 2
+    for (int64_t l = lane; l < E; l += 32) {
+        float2 xv[NC];
+        if (vec) {
+            const float4* x4 = reinterpret_cast<const float4*>(xc + l * ld + co);
+#pragma unroll
+            for (int c = 0; c < NC / 2; ++c) {
+                const float4 t = __ldg(x4 + c);
+                xv[2 * c] = make_float2(t.x, t.y);
+                xv[2 * c + 1] = make_float2(t.z, t.w);
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < NC; ++c) xv[c] = __ldg(xc + l * ld + co + c);
+        }
+#pragma unroll
+        for (int q = 0; q < ROWS; ++q) {
+            if (r0 + q < E) {
+                const float2 a = __ldcs(zc + (r0 + q) * E + l);
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    ar[q][c] = fmaf(a.x, xv[c].x, fmaf(-a.y, xv[c].y, ar[q][c]));
+                    ai[q][c] = fmaf(a.x, xv[c].y, fmaf(a.y, xv[c].x, ai[q][c]));
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < ROWS; ++q)
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            float vr = ar[q][c], vi = ai[q][c];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                vr += __shfl_xor_sync(0xffffffffu, vr, o);
+                vi += __shfl_xor_sync(0xffffffffu, vi, o);
+            }
+            if (lane == 0 && r0 + q < E)
+                reinterpret_cast<float2*>(y)[(r0 + q) * ld + co + c] = make_float2(vr, vi);
+        }
+}
+
+int blockdiag_matvec(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
+                     const float* x, int64_t ld, int nc, int rows, float* y, cudaStream_t s) {
+    if (n_mesh <= 0 || total_warps <= 0) return MB_OK;
+    const int64_t blocks = (total_warps * 32 + 255) / 256;
+    if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "batch too large for one launch");
+#define MB_BD(R, C)                                                                                           \
+    if (rows == R && nc == C) {                                                                               \
+        blockdiag_matvec_kernel<R, C><<<(unsigned)blocks, 256, 0, s>>>(z, desc, goff, n_mesh, x, ld, y);      \
+        return check_launch("blockdiag_matvec");                                                              \
+    }
+    MB_BD(1, 1) MB_BD(2, 1) MB_BD(4, 1) MB_BD(8, 1)
+    MB_BD(1, 2) MB_BD(2, 2) MB_BD(4, 2) MB_BD(8, 2)
+    MB_BD(1, 4) MB_BD(2, 4) MB_BD(4, 4) MB_BD(8, 4)
+    MB_BD(1, 8) MB_BD(2, 8) MB_BD(4, 8)
+#undef MB_BD
+    return set_error(MB_ERR_UNSUPPORTED, "block-diagonal product: rows per warp in {1, 2, 4, 8} (8 with up to 4 "
+                                         "columns), columns per mesh in {1, 2, 4, 8}");
+}
+
 // ---- host driver -------------------------------------------------------------------------
 static int mg_sync(cudaStream_t s, const char* what) {
     cudaError_t e = cudaStreamSynchronize(s);
@@ -353,27 +458,32 @@ static int mg_sync(cudaStream_t s, const char* what) {
     return check_launch(what);
 }
 
-int gmres_multi(const float* z_hi, const float* z_lo, int64_t n, const double* b, double* x, int64_t m, int r,
-                int max_iters, double tol, void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out,
-                double* max_relres_out, int* status_out, cudaStream_t s) {
+// The lockstep driver.  prod(v32, y32, stream) computes Y = Z V for the [n, m] complex64 blocks.
+// With use_graph, the r Arnoldi steps of a cycle are captured once as a CUDA graph and
+// replayed every cycle (no host synchronisation inside a cycle; a cycle always runs its r
+// steps, columns that converged early are inactive).
+template <typename Prod>
+static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int64_t m, int r, int max_iters,
+                          double tol, size_t prod_ws, void* workspace, size_t ws_bytes, bool use_graph,
+                          int64_t* iters_out, int64_t* cycles_out, double* max_relres_out, int* status_out,
+                          cudaStream_t s) {
     if (n <= 0 || m <= 0) return set_error(MB_ERR_ARG, "n and m must be > 0");
     if (r < 1 || r > kMgMaxRestart) return set_error(MB_ERR_ARG, "restart must be in [1, %d]", kMgMaxRestart);
     if (max_iters < 1 || !(tol > 0)) return set_error(MB_ERR_ARG, "bad max_iters / tol");
-    if (ws_bytes < gmres_multi_workspace_bytes(n, m, r)) return set_error(MB_ERR_ARG, "workspace too small");
     MgWork W;
-    mg_layout(n, m, r, workspace, &W);
+    if (ws_bytes < mg_layout(n, m, r, prod_ws, nullptr, &W)) return set_error(MB_ERR_ARG, "workspace too small");
+    mg_layout(n, m, r, prod_ws, workspace, &W);
     const int64_t nm = n * m;
     const unsigned eb = (unsigned)((nm + 255) / 256);
     const unsigned cb = (unsigned)((m + 127) / 128);
     const dim3 rblk(32, 8);
     // row blocks per column group: enough blocks to fill the GPU, few FP64 atomics per column
-    const unsigned ky = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 63) / 64, (152 * 16 + (m + 31) / 32 - 1) /
-                                                                                        ((m + 31) / 32)));
+    const unsigned ky = (unsigned)std::max<int64_t>(
+        1, std::min<int64_t>((n + 63) / 64, (152 * 16 + (m + 31) / 32 - 1) / ((m + 31) / 32)));
     const dim3 rgrid((unsigned)((m + 31) / 32), ky);
-    const size_t gws = cgemm_workspace_bytes(n, m);
     std::vector<double> hb(m);
     int rc;
-    // |b| per column
+    cudaMemsetAsync(W.y32, 0, 8 * (size_t)nm, s);  // rows a product does not write stay 0
     cudaMemsetAsync(W.bnorm, 0, 8 * m, s);
     mg_colnorm2<<<rgrid, rblk, 0, s>>>(b, n, m, W.bnorm);
     cudaMemcpyAsync(hb.data(), W.bnorm, 8 * m, cudaMemcpyDeviceToHost, s);
@@ -384,14 +494,39 @@ int gmres_multi(const float* z_hi, const float* z_lo, int64_t n, const double* b
     double worst = 0.0;
     int status = 1;
     std::vector<double> hbeta(m);
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cap = nullptr;  // capture needs a stream other than the legacy default stream
+    auto step = [&](int j, cudaStream_t st) -> int {
+        int e;
+        if ((e = prod(W.v32, W.y32, st))) return e;
+        mg_widen<<<eb, 256, 0, st>>>(W.y32, 2 * nm, W.w);
+        for (int pass = 0; pass < 2; ++pass) {
+            cudaMemsetAsync(W.hc, 0, 16 * (size_t)(j + 1) * m, st);
+            mg_dots<<<dim3((unsigned)((m + 31) / 32), ky, (unsigned)(j + 1)), rblk, 0, st>>>(W.V, W.w, n, m, W.hc);
+            mg_subtract<<<eb, 256, 0, st>>>(W.V, W.hc, n, m, j + 1, W.w);
+            mg_accum_h<<<(unsigned)(((j + 1) * m + 255) / 256), 256, 0, st>>>(W.hc, j + 1, j, r, m, W.H);
+        }
+        cudaMemsetAsync(W.hn, 0, 8 * m, st);
+        mg_colnorm2<<<rgrid, rblk, 0, st>>>(W.w, n, m, W.hn);
+        cudaMemsetAsync(W.count, 0, 4, st);
+        mg_givens<<<cb, 128, 0, st>>>(W.H, W.cs, W.sn, W.g, W.hn, W.bnorm, j, r, m, tol, W.active, W.jend, W.count);
+        mg_next_basis<<<eb, 256, 0, st>>>(W.w, W.hn, W.active, n, m, W.V + 2 * (size_t)(j + 1) * nm, W.v32);
+        return check_launch("gmres_multi step");
+    };
+    auto cleanup = [&]() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (cap) cudaStreamDestroy(cap);
+    };
     while (true) {
-        // residual of the current iterate through the tensor-core product
+        // residual of the current iterate through the same product
         mg_to_c64<<<eb, 256, 0, s>>>(x, 2 * nm, W.v32);
-        if ((rc = cgemm_tf32x3(z_hi, z_lo, n, W.v32, m, W.y32, W.gemm_ws, gws, s))) return rc;
+        if ((rc = prod(W.v32, W.y32, s))) return cleanup(), rc;
         cudaMemsetAsync(W.beta, 0, 8 * m, s);
         mg_residual<<<rgrid, rblk, 0, s>>>(b, W.y32, n, m, W.V, W.beta);
         cudaMemcpyAsync(hbeta.data(), W.beta, 8 * m, cudaMemcpyDeviceToHost, s);
-        if ((rc = mg_sync(s, "gmres_multi residual"))) return rc;
+        if ((rc = mg_sync(s, "gmres_multi residual"))) return cleanup(), rc;
         worst = 0.0;
         for (int64_t c = 0; c < m; ++c) worst = std::max(worst, std::sqrt(hbeta[c]) / hb[c]);
         if (worst <= tol) {
@@ -405,39 +540,74 @@ int gmres_multi(const float* z_hi, const float* z_lo, int64_t n, const double* b
         mg_init_g<<<cb, 128, 0, s>>>(W.beta, W.bnorm, r, m, tol, W.g, W.jend, W.count);
         cudaMemsetAsync(W.H, 0, 16 * (size_t)(r + 1) * r * m, s);
         int j = 0;
-        for (; j < r && iters < max_iters; ++j, ++iters) {
-            if ((rc = cgemm_tf32x3(z_hi, z_lo, n, W.v32, m, W.y32, W.gemm_ws, gws, s))) return rc;
-            mg_widen<<<eb, 256, 0, s>>>(W.y32, 2 * nm, W.w);  // w (complex128) <- product
-            for (int pass = 0; pass < 2; ++pass) {
-                cudaMemsetAsync(W.hc, 0, 16 * (size_t)(j + 1) * m, s);
-                mg_dots<<<dim3((unsigned)((m + 31) / 32), ky, (unsigned)(j + 1)), rblk, 0, s>>>(W.V, W.w, n, m, W.hc);
-                mg_subtract<<<eb, 256, 0, s>>>(W.V, W.hc, n, m, j + 1, W.w);
-                mg_accum_h<<<(unsigned)(((j + 1) * m + 255) / 256), 256, 0, s>>>(W.hc, j + 1, j, r, m, W.H);
+        if (use_graph) {
+            if (!exec) {
+                if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess ||
+                    cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+                    return cleanup(), set_error(MB_ERR_CUDA, "gmres_multi: stream capture failed");
+                int e = MB_OK;
+                for (int q = 0; q < r && e == MB_OK; ++q) e = step(q, cap);
+                cudaError_t ce = cudaStreamEndCapture(cap, &graph);
+                if (e) return cleanup(), e;
+                if (ce != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+                    return cleanup(), set_error(MB_ERR_CUDA, "gmres_multi: graph capture / instantiate failed");
             }
-            cudaMemsetAsync(W.hn, 0, 8 * m, s);
-            mg_colnorm2<<<rgrid, rblk, 0, s>>>(W.w, n, m, W.hn);
-            cudaMemsetAsync(W.count, 0, 4, s);
-            mg_givens<<<cb, 128, 0, s>>>(W.H, W.cs, W.sn, W.g, W.hn, W.bnorm, j, r, m, tol, W.active, W.jend,
-                                         W.count);
-            mg_next_basis<<<eb, 256, 0, s>>>(W.w, W.hn, W.active, n, m, W.V + 2 * (size_t)(j + 1) * nm, W.v32);
-            int alive = 0;
-            cudaMemcpyAsync(&alive, W.count, 4, cudaMemcpyDeviceToHost, s);
-            if ((rc = mg_sync(s, "gmres_multi arnoldi"))) return rc;
-            if (alive == 0) {
-                ++j;
-                ++iters;
-                break;
+            if (cudaGraphLaunch(exec, s) != cudaSuccess)
+                return cleanup(), set_error(MB_ERR_CUDA, "gmres_multi: graph launch failed");
+            j = r;
+            iters += r;
+        } else {
+            for (; j < r && iters < max_iters; ++j, ++iters) {
+                if ((rc = step(j, s))) return cleanup(), rc;
+                int alive = 0;
+                cudaMemcpyAsync(&alive, W.count, 4, cudaMemcpyDeviceToHost, s);
+                if ((rc = mg_sync(s, "gmres_multi arnoldi"))) return cleanup(), rc;
+                if (alive == 0) {
+                    ++j;
+                    ++iters;
+                    break;
+                }
             }
         }
         mg_backsolve<<<cb, 128, 0, s>>>(W.H, W.g, W.jend, r, m, W.yv);
         mg_update<<<eb, 256, 0, s>>>(W.V, W.yv, n, m, j, x);
-        if ((rc = mg_sync(s, "gmres_multi update"))) return rc;
+        if ((rc = mg_sync(s, "gmres_multi update"))) return cleanup(), rc;
     }
+    cleanup();
     if (iters_out) *iters_out = iters;
     if (cycles_out) *cycles_out = cycles;
     if (max_relres_out) *max_relres_out = worst;
     if (status_out) *status_out = status;
     return MB_OK;
+}
+
+int gmres_multi(const float* z_hi, const float* z_lo, int64_t n, const double* b, double* x, int64_t m, int r,
+                int max_iters, double tol, void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out,
+                double* max_relres_out, int* status_out, cudaStream_t s) {
+    const size_t gws = cgemm_workspace_bytes(n, m);
+    MgWork W;
+    if (ws_bytes < mg_layout(n, m, r, gws, nullptr, &W)) return set_error(MB_ERR_ARG, "workspace too small");
+    mg_layout(n, m, r, gws, workspace, &W);
+    void* gemm_ws = W.gemm_ws;
+    auto prod = [&](const float* v32, float* y32, cudaStream_t st) {
+        return cgemm_tf32x3(z_hi, z_lo, n, v32, m, y32, gemm_ws, gws, st);
+    };
+    return gmres_lockstep(prod, n, b, x, m, r, max_iters, tol, gws, workspace, ws_bytes, false, iters_out,
+                          cycles_out, max_relres_out, status_out, s);
+}
+
+// Many meshes, each with its own Z_i and nc right-hand sides: the block-diagonal system on
+// the padded [n_rows, m] layout (m = n_mesh * nc columns).
+int gmres_blockdiag(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
+                    int rows_per_warp, int nc, int64_t n_rows, const double* b, double* x, int r, int max_iters,
+                    double tol, bool use_graph, void* workspace, size_t ws_bytes, int64_t* iters_out,
+                    int64_t* cycles_out, double* max_relres_out, int* status_out, cudaStream_t s) {
+    const int64_t m = (int64_t)n_mesh * nc;
+    auto prod = [&](const float* v32, float* y32, cudaStream_t st) {
+        return blockdiag_matvec(z, desc, goff, n_mesh, total_warps, v32, m, nc, rows_per_warp, y32, st);
+    };
+    return gmres_lockstep(prod, n_rows, b, x, m, r, max_iters, tol, 0, workspace, ws_bytes, use_graph, iters_out,
+                          cycles_out, max_relres_out, status_out, s);
 }
 
 }  // namespace mb

@@ -384,7 +384,7 @@ __device__ __forceinline__ void mom_entry_fast(const float* __restrict__ verts,
 }
 
 #ifndef MB_FAST_MIN_BLOCKS
-#define MB_FAST_MIN_BLOCKS 4
+#define MB_FAST_MIN_BLOCKS 5
 #endif
 template <int NX, int NY, bool RWG>
 __global__ void __launch_bounds__(128, NX <= 4 ? MB_FAST_MIN_BLOCKS : 2) mom_ref_zmat_fast_kernel(
@@ -461,29 +461,18 @@ struct PlaneWave {
     double hx, hy, hz;     // H = khat x e0 / eta
 };
 
+// <f_fe, E + n x H> of one face-edge (face f, local edge e) for one plane wave.
 template <typename T>
-__global__ void mom_ref_rhs_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces,
-                                   const T* __restrict__ areas, const T* __restrict__ normals,
-                                   const T* __restrict__ gp, const T* __restrict__ gw, int n,
-                                   const PlaneWave* __restrict__ waves, PlaneWave w0, int nrhs, int64_t nf,
-                                   int out_mode, int64_t batch, const int32_t* __restrict__ fei,
-                                   T* __restrict__ out_r, T* __restrict__ out_i) {
-    __shared__ T s_p[16], s_w[16];
-    if (threadIdx.x < n) { s_p[threadIdx.x] = gp[threadIdx.x]; s_w[threadIdx.x] = gw[threadIdx.x]; }
-    __syncthreads();
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= 3 * nf * nrhs) return;
-    const int rhs = (int)(idx / (3 * nf));
-    const int64_t fe = idx % (3 * nf);
-    const int64_t f = fe / 3;
-    const int e = (int)(fe % 3);
+__device__ __forceinline__ void ref_rhs_entry(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                              const T* __restrict__ areas, const T* __restrict__ normals,
+                                              const T* s_p, const T* s_w, int n, const PlaneWave& pw, int64_t f,
+                                              int e, T* out_re, T* out_im) {
     const int32_t i0 = faces[3 * f + e], i1 = faces[3 * f + (e + 1) % 3], i2 = faces[3 * f + (e + 2) % 3];
     const V3<T> v0 = load3(verts, i0), v1 = load3(verts, i1), v2 = load3(verts, i2);
     const V3<T> nrm = load3(normals, f);
     const T area = areas[f];
     const V3<T> d = v2 - v1;
     const T c = (i1 < i2 ? T(1) : T(-1)) * sqrt_t(dot(d, d)) / (T(2) * area);
-    const PlaneWave pw = waves ? waves[rhs] : w0;
     const V3<T> kv = v3<T>((T)pw.kx, (T)pw.ky, (T)pw.kz);
     const V3<T> E0 = v3<T>((T)pw.ex, (T)pw.ey, (T)pw.ez);
     const V3<T> H0 = v3<T>((T)pw.hx, (T)pw.hy, (T)pw.hz);
@@ -501,6 +490,27 @@ __global__ void mom_ref_rhs_kernel(const T* __restrict__ verts, const int32_t* _
         acc_r += w * proj * cs;
         acc_i -= w * proj * sn;
     }
+    *out_re = acc_r;
+    *out_im = acc_i;
+}
+
+template <typename T>
+__global__ void mom_ref_rhs_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                   const T* __restrict__ areas, const T* __restrict__ normals,
+                                   const T* __restrict__ gp, const T* __restrict__ gw, int n,
+                                   const PlaneWave* __restrict__ waves, PlaneWave w0, int nrhs, int64_t nf,
+                                   int out_mode, int64_t batch, const int32_t* __restrict__ fei,
+                                   T* __restrict__ out_r, T* __restrict__ out_i) {
+    __shared__ T s_p[16], s_w[16];
+    if (threadIdx.x < n) { s_p[threadIdx.x] = gp[threadIdx.x]; s_w[threadIdx.x] = gw[threadIdx.x]; }
+    __syncthreads();
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 3 * nf * nrhs) return;
+    const int rhs = (int)(idx / (3 * nf));
+    const int64_t fe = idx % (3 * nf);
+    T acc_r, acc_i;
+    ref_rhs_entry<T>(verts, faces, areas, normals, s_p, s_w, n, waves ? waves[rhs] : w0, fe / 3, (int)(fe % 3),
+                     &acc_r, &acc_i);
     if (out_mode == 0) {
         for (int64_t b = 0; b < batch; ++b) {
             out_r[b * 3 * nf + fe] = acc_r;
@@ -624,6 +634,109 @@ template int launch_mom_ref_zmat<double>(const double*, int64_t, const int32_t*,
                                          const double*, const double*, int, double, const int32_t*,
                                          int64_t, int64_t, int64_t, int64_t, double*, double*,
                                          cudaStream_t);
+
+// ---------------------------------------------------------------------------------------
+// many meshes, the reference's operator and rule: one launch for all impedance matrices and
+// one for all excitations.  desc[i] = (first face, faces, edges, offset of Z_i in the flat
+// array (complex entries), -, first right-hand-side column); boff [n_mesh + 1] = first
+// block of each mesh (3 F_i rows of ceil(3 F_i / 128) blocks); fei holds local edge ids.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ int seg_find(const int64_t* __restrict__ off, int stride, int n, int64_t v) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(off + (int64_t)stride * mid) <= v) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int NX, int NY>
+__global__ void __launch_bounds__(128, NX <= 4 ? MB_FAST_MIN_BLOCKS : 2) mom_ref_zmat_batched_kernel(
+    const float* __restrict__ verts, const int32_t* __restrict__ faces, const float* __restrict__ areas,
+    const float* __restrict__ normals, const int32_t* __restrict__ fei, const int64_t* __restrict__ desc,
+    const int64_t* __restrict__ boff, const double* __restrict__ ks, int n_mesh, const float* __restrict__ gpx,
+    const float* __restrict__ gwx, const float* __restrict__ gpy, const float* __restrict__ gwy,
+    float* __restrict__ z) {
+    __shared__ float4 s_t[NX * NX], s_s[NY * NY];
+    stage_rules<NX, NY>(gpx, gwx, gpy, gwy, s_t, s_s);
+    __syncthreads();
+    const int64_t b = blockIdx.x;
+    const int i = seg_find(boff, 1, n_mesh, b);
+    const int64_t fo = __ldg(desc + 6 * i), nf = __ldg(desc + 6 * i + 1), ne = __ldg(desc + 6 * i + 2);
+    const int64_t ncol = 3 * nf, cb = (ncol + 127) / 128, local = b - __ldg(boff + i);
+    const int64_t row = local / cb, col = (local % cb) * 128 + threadIdx.x;
+    if (col >= ncol) return;
+    float re, im;
+    mom_entry_fast<NX, NY>(verts, faces, areas, normals, s_t, s_s, (float)__ldg(ks + i), fo + row / 3,
+                           (int)(row % 3), fo + col / 3, (int)(col % 3), &re, &im);
+    const int64_t m = __ldg(fei + 3 * fo + row), n = __ldg(fei + 3 * fo + col);
+    atomicAdd(reinterpret_cast<float2*>(z + 2 * (__ldg(desc + 6 * i + 3) + m * ne + n)), make_float2(re, im));
+}
+
+int launch_mom_ref_zmat_batched(const float* verts, const int32_t* faces, const float* areas, const float* normals,
+                                const int32_t* fei, const int64_t* desc, const int64_t* boff, int64_t total_blocks,
+                                const double* ks, int n_mesh, const float* gpx, const float* gwx, int nx,
+                                const float* gpy, const float* gwy, int ny, float* z, cudaStream_t s) {
+    if (n_mesh <= 0 || total_blocks <= 0) return MB_OK;
+    if (total_blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "batch too large for one launch");
+#define MB_RB(NXV, NYV)                                                                                      \
+    if (nx == NXV && ny == NYV) {                                                                            \
+        mom_ref_zmat_batched_kernel<NXV, NYV><<<(unsigned)total_blocks, 128, 0, s>>>(                        \
+            verts, faces, areas, normals, fei, desc, boff, ks, n_mesh, gpx, gwx, gpy, gwy, z);              \
+        return check_launch("mom_ref_zmat_batched");                                                        \
+    }
+    MB_RB(4, 3)
+    MB_RB(3, 2)
+    MB_RB(2, 1)
+    MB_RB(5, 4)
+#undef MB_RB
+    return set_error(MB_ERR_UNSUPPORTED, "batched reference rule: gaussQR in {2, 3, 4, 5}");
+}
+
+// waves [n_mesh * nrhs] plane-wave records; rhs: [rows, ld] interleaved complex64,
+// row = local edge, column desc[i][5] + r (accumulated).
+template <typename T>
+__global__ void mom_ref_rhs_batched_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                           const T* __restrict__ areas, const T* __restrict__ normals,
+                                           const int32_t* __restrict__ fei, const int64_t* __restrict__ desc,
+                                           int n_mesh, int64_t total_faces, const T* __restrict__ gp,
+                                           const T* __restrict__ gw, int n, const PlaneWave* __restrict__ waves,
+                                           int nrhs, int64_t ld, T* __restrict__ rhs) {
+    __shared__ T s_p[16], s_w[16];
+    if (threadIdx.x < n) { s_p[threadIdx.x] = gp[threadIdx.x]; s_w[threadIdx.x] = gw[threadIdx.x]; }
+    __syncthreads();
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 3 * total_faces * nrhs) return;
+    const int r = (int)(idx / (3 * total_faces));
+    const int64_t fe = idx % (3 * total_faces);
+    const int i = seg_find(desc, 6, n_mesh, fe / 3);
+    T acc_r, acc_i;
+    ref_rhs_entry<T>(verts, faces, areas, normals, s_p, s_w, n, waves[(int64_t)i * nrhs + r], fe / 3, (int)(fe % 3),
+                     &acc_r, &acc_i);
+    atomic_add_c<T>(rhs + 2 * ((int64_t)fei[fe] * ld + desc[6 * i + 5] + r), acc_r, acc_i);
+}
+
+template <typename T>
+int launch_mom_ref_rhs_batched(const T* verts, const int32_t* faces, const T* areas, const T* normals,
+                               const int32_t* fei, const int64_t* desc, int n_mesh, int64_t total_faces, const T* gp,
+                               const T* gw, int n, const PlaneWave* waves, int nrhs, int64_t ld, T* rhs,
+                               cudaStream_t s) {
+    if (n_mesh <= 0 || total_faces <= 0 || nrhs <= 0) return MB_OK;
+    if (n < 1 || n > 16) return set_error(MB_ERR_UNSUPPORTED, "quadrature order must be in [1, 16]");
+    const int64_t total = 3 * total_faces * nrhs;
+    mom_ref_rhs_batched_kernel<T><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(
+        verts, faces, areas, normals, fei, desc, n_mesh, total_faces, gp, gw, n, waves, nrhs, ld, rhs);
+    return check_launch("mom_ref_rhs_batched");
+}
+template int launch_mom_ref_rhs_batched<float>(const float*, const int32_t*, const float*, const float*,
+                                               const int32_t*, const int64_t*, int, int64_t, const float*,
+                                               const float*, int, const PlaneWave*, int, int64_t, float*,
+                                               cudaStream_t);
+template int launch_mom_ref_rhs_batched<double>(const double*, const int32_t*, const double*, const double*,
+                                                const int32_t*, const int64_t*, int, int64_t, const double*,
+                                                const double*, int, const PlaneWave*, int, int64_t, double*,
+                                                cudaStream_t);
 
 // The reference's hard-coded incidence (mesh_MOM_3d.cu:24-70): k along azimuth 30 deg in
 // the xy plane, E along z, H along azimuth -60 deg, eta = 1.

@@ -60,18 +60,12 @@ __device__ __forceinline__ void rwg_consts(const int32_t* f, int64_t p, const V3
 // ---------------------------------------------------------------------------------------
 // separated pairs (no shared vertex): one thread per (test p, source q), 128 q per block
 // ---------------------------------------------------------------------------------------
+// One separated face pair (p test, q source): the nine RWG entries, accumulated into z
+// ([n_edges, n_edges] interleaved complex) at the rows / columns fei gives.
 template <typename T>
-__global__ void __launch_bounds__(128) mom_sym_regular_kernel(const T* __restrict__ verts,
-                                                              const int32_t* __restrict__ faces,
-                                                              const int32_t* __restrict__ fei, int64_t n_edges,
-                                                              T k, int64_t nf, int64_t p_begin, int64_t q_blocks,
-                                                              T* __restrict__ z) {
-    __shared__ T s_b[7][4];
-    if (threadIdx.x < 28) s_b[threadIdx.x / 4][threadIdx.x % 4] = (T)c_d7[threadIdx.x / 4][threadIdx.x % 4];
-    __syncthreads();
-    const int64_t p = p_begin + (int64_t)blockIdx.x / q_blocks;
-    const int64_t q = ((int64_t)blockIdx.x % q_blocks) * 128 + threadIdx.x;
-    if (q >= nf) return;
+__device__ __forceinline__ void sym_regular_pair(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                                 const int32_t* __restrict__ fei, int64_t n_edges, T k, int64_t p,
+                                                 int64_t q, const T (*s_b)[4], T* __restrict__ z) {
     if (shared_vertices(faces, p, q) != 0) return;  // done by the FP64 near-pair kernel
     const V3<T> o = load3(verts, __ldg(faces + 3 * q));
     V3<T> A[3], B[3];
@@ -147,17 +141,28 @@ __global__ void __launch_bounds__(128) mom_sym_regular_kernel(const T* __restric
     }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(128) mom_sym_regular_kernel(const T* __restrict__ verts,
+                                                              const int32_t* __restrict__ faces,
+                                                              const int32_t* __restrict__ fei, int64_t n_edges,
+                                                              T k, int64_t nf, int64_t p_begin, int64_t q_blocks,
+                                                              T* __restrict__ z) {
+    __shared__ T s_b[7][4];
+    if (threadIdx.x < 28) s_b[threadIdx.x / 4][threadIdx.x % 4] = (T)c_d7[threadIdx.x / 4][threadIdx.x % 4];
+    __syncthreads();
+    const int64_t p = p_begin + (int64_t)blockIdx.x / q_blocks;
+    const int64_t q = ((int64_t)blockIdx.x % q_blocks) * 128 + threadIdx.x;
+    if (q >= nf) return;
+    sym_regular_pair<T>(verts, faces, fei, n_edges, k, p, q, s_b, z);
+}
+
 // ---------------------------------------------------------------------------------------
 // pairs sharing a vertex: FP64 with the singular part in closed form; one thread per pair
 // ---------------------------------------------------------------------------------------
 template <typename T>
-__global__ void mom_sym_near_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces,
-                                    const int32_t* __restrict__ fei, int64_t n_edges,
-                                    const int32_t* __restrict__ pairs, int64_t n_pairs, double k,
-                                    T* __restrict__ z) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n_pairs) return;
-    const int64_t p = pairs[2 * t], q = pairs[2 * t + 1];
+__device__ __forceinline__ void sym_near_pair(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                              const int32_t* __restrict__ fei, int64_t n_edges, double k, int64_t p,
+                                              int64_t q, T* __restrict__ z) {
     V3<double> A[3], B[3];
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
@@ -223,24 +228,29 @@ __global__ void mom_sym_near_kernel(const T* __restrict__ verts, const int32_t* 
     }
 }
 
+template <typename T>
+__global__ void mom_sym_near_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                    const int32_t* __restrict__ fei, int64_t n_edges,
+                                    const int32_t* __restrict__ pairs, int64_t n_pairs, double k,
+                                    T* __restrict__ z) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_pairs) return;
+    sym_near_pair<T>(verts, faces, fei, n_edges, k, pairs[2 * t], pairs[2 * t + 1], z);
+}
+
 // ---------------------------------------------------------------------------------------
 // EFIE excitation with the same rule: rhs[fei, r] += int f_m . E0 e^{-j k khat.x}
 // waves: [n_rhs, 9] float64 (k khat, E0, H0); one thread per (face, wave)
 // ---------------------------------------------------------------------------------------
 template <typename T>
-__global__ void mom_sym_rhs_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces,
-                                   const int32_t* __restrict__ fei, const double* __restrict__ waves, int nrhs,
-                                   int64_t nf, T* __restrict__ rhs) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nf * nrhs) return;
-    const int r = (int)(t / nf);
-    const int64_t p = t % nf;
+__device__ __forceinline__ void sym_rhs_face(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                             const int32_t* __restrict__ fei, const double* __restrict__ w,
+                                             int64_t p, int64_t ld, int64_t col, T* __restrict__ rhs) {
     V3<T> A[3];
 #pragma unroll
     for (int v = 0; v < 3; ++v) A[v] = load3(verts, faces[3 * p + v]);
     T c[3], area;
     rwg_consts<T>(faces, p, A, c, &area);
-    const double* w = waves + 9 * r;
     const V3<T> kv = v3<T>((T)w[0], (T)w[1], (T)w[2]), E0 = v3<T>((T)w[3], (T)w[4], (T)w[5]);
     T sr[3] = {0, 0, 0}, si[3] = {0, 0, 0};
     for (int i = 0; i < 7; ++i) {
@@ -256,7 +266,105 @@ __global__ void mom_sym_rhs_kernel(const T* __restrict__ verts, const int32_t* _
         }
     }
 #pragma unroll
-    for (int m = 0; m < 3; ++m) add_c<T>(rhs + 2 * ((int64_t)fei[3 * p + m] * nrhs + r), sr[m], si[m]);
+    for (int m = 0; m < 3; ++m) add_c<T>(rhs + 2 * ((int64_t)fei[3 * p + m] * ld + col), sr[m], si[m]);
+}
+
+template <typename T>
+__global__ void mom_sym_rhs_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                   const int32_t* __restrict__ fei, const double* __restrict__ waves, int nrhs,
+                                   int64_t nf, T* __restrict__ rhs) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nf * nrhs) return;
+    const int r = (int)(t / nf);
+    sym_rhs_face<T>(verts, faces, fei, waves + 9 * r, t % nf, nrhs, r, rhs);
+}
+
+// ---------------------------------------------------------------------------------------
+// many meshes in one launch each.  The meshes are packed into one vertex / face array
+// (vertex ids global, edge ids local to each mesh); desc[i] = (face offset, faces, edges,
+// offset of the mesh's Z in the flat block-diagonal array (complex entries), first block of
+// the mesh in the regular launch, first right-hand-side column); ks[i] its wavenumber.
+// ---------------------------------------------------------------------------------------
+constexpr int kDesc = 6;
+
+__device__ __forceinline__ int mesh_of(const int64_t* __restrict__ desc, int n_mesh, int field, int64_t v) {
+    int lo = 0, hi = n_mesh - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(desc + kDesc * mid + field) <= v) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) mom_sym_regular_batched_kernel(
+    const T* __restrict__ verts, const int32_t* __restrict__ faces, const int32_t* __restrict__ fei,
+    const int64_t* __restrict__ desc, const double* __restrict__ ks, int n_mesh, T* __restrict__ z) {
+    __shared__ T s_b[7][4];
+    if (threadIdx.x < 28) s_b[threadIdx.x / 4][threadIdx.x % 4] = (T)c_d7[threadIdx.x / 4][threadIdx.x % 4];
+    __syncthreads();
+    const int64_t b = blockIdx.x;
+    const int i = mesh_of(desc, n_mesh, 4, b);
+    const int64_t fo = __ldg(desc + kDesc * i), nf = __ldg(desc + kDesc * i + 1);
+    const int64_t qb = (nf + 127) / 128, local = b - __ldg(desc + kDesc * i + 4);
+    const int64_t p = fo + local / qb, q = fo + (local % qb) * 128 + threadIdx.x;
+    if (q >= fo + nf) return;
+    sym_regular_pair<T>(verts, faces, fei, __ldg(desc + kDesc * i + 2), (T)__ldg(ks + i), p, q, s_b,
+                        z + 2 * __ldg(desc + kDesc * i + 3));
+}
+
+template <typename T>
+__global__ void mom_sym_near_batched_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                            const int32_t* __restrict__ fei, const int64_t* __restrict__ desc,
+                                            const double* __restrict__ ks, int n_mesh,
+                                            const int32_t* __restrict__ pairs, int64_t n_pairs,
+                                            T* __restrict__ z) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_pairs) return;
+    const int64_t p = pairs[2 * t];
+    const int i = mesh_of(desc, n_mesh, 0, p);
+    sym_near_pair<T>(verts, faces, fei, desc[kDesc * i + 2], ks[i], p, pairs[2 * t + 1], z + 2 * desc[kDesc * i + 3]);
+}
+
+// waves: [n_mesh * nrhs, 9]; rhs: [rows, ld] interleaved complex, column desc[i][5] + r.
+template <typename T>
+__global__ void mom_sym_rhs_batched_kernel(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                           const int32_t* __restrict__ fei, const int64_t* __restrict__ desc,
+                                           int n_mesh, int64_t total_faces, const double* __restrict__ waves,
+                                           int nrhs, int64_t ld, T* __restrict__ rhs) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total_faces * nrhs) return;
+    const int r = (int)(t / total_faces);
+    const int64_t p = t % total_faces;
+    const int i = mesh_of(desc, n_mesh, 0, p);
+    sym_rhs_face<T>(verts, faces, fei, waves + 9 * ((int64_t)i * nrhs + r), p, ld, desc[kDesc * i + 5] + r, rhs);
+}
+
+template <typename T>
+int launch_mom_sym_batched(const T* verts, const int32_t* faces, const int32_t* fei, const int64_t* desc,
+                           const double* ks, int n_mesh, int64_t total_blocks, const int32_t* pairs,
+                           int64_t n_pairs, T* z, cudaStream_t s) {
+    if (n_mesh <= 0) return MB_OK;
+    if (total_blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "batch too large for one launch");
+    if (total_blocks > 0)
+        mom_sym_regular_batched_kernel<T><<<(unsigned)total_blocks, 128, 0, s>>>(verts, faces, fei, desc, ks, n_mesh,
+                                                                                  z);
+    if (n_pairs > 0)
+        mom_sym_near_batched_kernel<T><<<(unsigned)((n_pairs + 127) / 128), 128, 0, s>>>(verts, faces, fei, desc, ks,
+                                                                                         n_mesh, pairs, n_pairs, z);
+    return check_launch("mom_sym_batched");
+}
+
+template <typename T>
+int launch_mom_sym_rhs_batched(const T* verts, const int32_t* faces, const int32_t* fei, const int64_t* desc,
+                               int n_mesh, int64_t total_faces, const double* waves, int nrhs, int64_t ld, T* rhs,
+                               cudaStream_t s) {
+    if (n_mesh <= 0 || total_faces <= 0 || nrhs <= 0) return MB_OK;
+    const int64_t total = total_faces * nrhs;
+    mom_sym_rhs_batched_kernel<T><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(verts, faces, fei, desc, n_mesh,
+                                                                                   total_faces, waves, nrhs, ld, rhs);
+    return check_launch("mom_sym_rhs_batched");
 }
 
 // ---------------------------------------------------------------------------------------
@@ -296,6 +404,10 @@ int launch_mom_sym_rhs(const T* verts, const int32_t* faces, const int32_t* fei,
 }
 
 #define MB_INST(T)                                                                                       \
+    template int launch_mom_sym_batched<T>(const T*, const int32_t*, const int32_t*, const int64_t*, const double*, \
+                                           int, int64_t, const int32_t*, int64_t, T*, cudaStream_t);     \
+    template int launch_mom_sym_rhs_batched<T>(const T*, const int32_t*, const int32_t*, const int64_t*, int,   \
+                                               int64_t, const double*, int, int64_t, T*, cudaStream_t);   \
     template int launch_mom_sym_regular<T>(const T*, const int32_t*, const int32_t*, int64_t, double, int64_t, \
                                            int64_t, int64_t, T*, cudaStream_t);                         \
     template int launch_mom_sym_near<T>(const T*, const int32_t*, const int32_t*, int64_t, const int32_t*,   \

@@ -1,0 +1,120 @@
+"""Batched meshes: one launch assembles / excites every mesh; lockstep GMRES on the block-
+diagonal system (with and without the captured CUDA graph) against per-mesh results."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _batch(pkg, cuda):
+    M = pkg.meshes
+    meshes = [M.icosphere(1, 1.0), M.ellipsoid(2), M.star_shape(2, seed=3)]
+    ks = [1.5, 2.5, 3.0]
+    return pkg.batch.MeshBatch(meshes, ks, device=cuda), meshes, ks
+
+
+def _waves(pkg, n_mesh, nc, ks, cuda, seed=0):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_mesh):
+        d = rng.normal(size=(nc, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        p = np.cross(d, rng.normal(size=(nc, 3)))
+        p /= np.linalg.norm(p, axis=1, keepdims=True)
+        out.append(pkg.mesh_MOM_3d.plane_waves(ks[i], d, p))
+    return torch.stack(out).to(cuda)
+
+
+def _per_mesh(pkg, cuda, v, f, k, waves):
+    MM = pkg.mesh_MOM_3d
+    vt = torch.tensor(np.asarray(v), dtype=torch.float32, device=cuda)
+    ft = torch.tensor(np.asarray(f), dtype=torch.int32, device=cuda)
+    edges, fei, _ = pkg.utils.get_edge_unique(vt, ft)
+    Z = MM.assemble_Z_rwg_sym(vt, ft, fei, edges.shape[0], k)
+    B = MM.assemble_rhs_rwg_sym(vt, ft, fei, edges.shape[0], waves)
+    return Z, B
+
+
+def test_batched_assembly_and_excitation_match_per_mesh(pkg, cuda):
+    bt, meshes, ks = _batch(pkg, cuda)
+    waves = _waves(pkg, bt.n_mesh, 4, ks, cuda)
+    Z = bt.assemble()
+    B = bt.excitation(waves)
+    for i, (v, f) in enumerate(meshes):
+        Zi, Bi = _per_mesh(pkg, cuda, v, f, ks[i], waves[i])
+        zb = bt.z_block(Z, i)
+        assert (torch.linalg.norm(zb - Zi) / torch.linalg.norm(Zi)).item() < 1e-6
+        for r in range(4):
+            bc = bt.column(B, i, r)
+            assert (torch.linalg.norm(bc - Bi[:, r]) / torch.linalg.norm(Bi[:, r])).item() < 1e-6
+        assert torch.all(B[bt.n_edges[i]:, 4 * i:4 * i + 4] == 0)
+
+
+@pytest.mark.parametrize("nc", [1, 4])
+@pytest.mark.parametrize("rows", [1, 2, 4, 8])
+def test_blockdiag_matvec(pkg, cuda, nc, rows):
+    bt, meshes, ks = _batch(pkg, cuda)
+    bt.excitation(_waves(pkg, bt.n_mesh, nc, ks, cuda))
+    Z = bt.assemble()
+    g = torch.Generator(device="cpu").manual_seed(rows * 10 + nc)
+    X = torch.randn(bt.n_rows, bt.n_mesh * nc, dtype=torch.complex64, generator=g).to(cuda)
+    for i in range(bt.n_mesh):
+        X[bt.n_edges[i]:, i * nc:(i + 1) * nc] = 0
+    Y = bt.matvec(Z, X, rows)
+    for i in range(bt.n_mesh):
+        e = bt.n_edges[i]
+        ref = bt.z_block(Z, i).to(torch.complex128) @ X[:e, i * nc:(i + 1) * nc].to(torch.complex128)
+        got = Y[:e, i * nc:(i + 1) * nc].to(torch.complex128)
+        assert (torch.linalg.norm(got - ref) / torch.linalg.norm(ref)).item() < 1e-5
+        assert torch.all(Y[e:, i * nc:(i + 1) * nc] == 0)
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_batched_solve_matches_dense(pkg, cuda, use_graph):
+    bt, meshes, ks = _batch(pkg, cuda)
+    waves = _waves(pkg, bt.n_mesh, 4, ks, cuda, seed=1)
+    Z = bt.assemble()
+    B = bt.excitation(waves)
+    bt.autotune(Z)
+    X, info = bt.solve(Z, B, restart=50, tol=1e-6, max_iters=3000, use_graph=use_graph)
+    assert info["converged"], info
+    for i in range(bt.n_mesh):
+        Zi = bt.z_block(Z, i).to(torch.complex128)
+        e = bt.n_edges[i]
+        ref = torch.linalg.solve(Zi, B[:e, 4 * i:4 * i + 4].to(torch.complex128))
+        got = X[:e, 4 * i:4 * i + 4]
+        err = (torch.linalg.norm(got - ref, dim=0) / torch.linalg.norm(ref, dim=0)).max().item()
+        assert err < 1e-3, (i, err)
+        assert torch.all(X[e:, 4 * i:4 * i + 4] == 0)
+
+
+def test_batched_reference_cfie_matches_per_mesh_and_solves(pkg, cuda):
+    M = pkg.meshes
+    meshes = [M.icosphere(1, 1.0), M.star_shape(2, seed=5), M.ellipsoid(1)]
+    ks = [2.0, 4.0, 3.0]
+    bt = pkg.batch.MeshBatch(meshes, ks, device=cuda, formulation="cfie_ref")
+    waves = _waves(pkg, bt.n_mesh, 4, ks, cuda, seed=2)
+    Z = bt.assemble()
+    B = bt.excitation(waves)
+    MM, U = pkg.mesh_MOM_3d, pkg.utils
+    px, wx = U.get_gaussion_integration_points_and_weights(4, device=cuda)
+    py, wy = U.get_gaussion_integration_points_and_weights(3, device=cuda)
+    for i, (v, f) in enumerate(meshes):
+        vt = torch.tensor(np.asarray(v), dtype=torch.float32, device=cuda)
+        ft = torch.tensor(np.asarray(f), dtype=torch.int32, device=cuda)
+        edges, fei, _ = U.get_edge_unique(vt, ft)
+        a, n = U.compute_face_areas(vt, ft).contiguous(), U.compute_face_normals(vt, ft).contiguous()
+        Zi = MM.assemble_Z_rwg(vt, ft, a, n, fei, edges.shape[0], px, wx, py, wy, ks[i])
+        Bi = MM.assemble_rhs_rwg(vt, ft, a, n, fei, edges.shape[0], px, wx, waves[i])
+        assert (torch.linalg.norm(bt.z_block(Z, i) - Zi) / torch.linalg.norm(Zi)).item() < 1e-6
+        got = B[: bt.n_edges[i], 4 * i:4 * i + 4]
+        assert (torch.linalg.norm(got - Bi) / torch.linalg.norm(Bi)).item() < 1e-6
+    bt.autotune(Z)
+    X, info = bt.solve(Z, B, restart=50, tol=1e-6, max_iters=500, use_graph=True)
+    assert info["converged"] and info["iterations"] <= 200
+    for i in range(bt.n_mesh):
+        e = bt.n_edges[i]
+        ref = torch.linalg.solve(bt.z_block(Z, i).to(torch.complex128), B[:e, 4 * i:4 * i + 4].to(torch.complex128))
+        err = (torch.linalg.norm(X[:e, 4 * i:4 * i + 4] - ref, dim=0) / torch.linalg.norm(ref, dim=0)).max().item()
+        assert err < 1e-4, (i, err)
