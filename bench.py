@@ -56,6 +56,9 @@ WORKLOADS = {
     "batch_star64": (64, 4, 0),
     "batch_star64_efie": (64, 4, 0),
     "batch_star8": (8, 4, 0),
+    # learned initial guess: (training meshes, held-out meshes, incidences per mesh)
+    "learned_star": (5000, 256, 4),
+    "learned_star_small": (500, 64, 4),
 }
 
 
@@ -855,6 +858,147 @@ def main_batch(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def _incidences(rng, n, nc, ks, MM):
+    waves, dirs = [], []
+    for i in range(n):
+        d = rng.normal(size=(nc, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        p = np.cross(d, rng.normal(size=(nc, 3)))
+        p /= np.linalg.norm(p, axis=1, keepdims=True)
+        waves.append(MM.plane_waves(ks[i], d, p))
+        dirs.append((d, p))
+    return waves, dirs
+
+
+def main_learned(args, rank, world, local_rank):
+    """Generate solves, train the edge-graph network on them, and measure what its initial
+    guess saves on held-out meshes (levels 2-3 of the batched-mesh distribution)."""
+    n_train, n_test, nc = WORKLOADS[args.workload]
+    import torch
+
+    pkg = importlib.import_module("mesh-ferrofluid_gb300")
+    MM, L = pkg.mesh_MOM_3d, pkg.learned
+    config = {"workload": args.workload, "train": f"{n_train} star-shaped meshes (levels 2-3) x {nc} incidences = "
+              f"{n_train * nc} solves, ka ~ U(1, 8)", "test": f"{n_test} held-out meshes x {nc} incidences",
+              "formulation": "the reference's EFIE + MFIE operator and rule", "network": f"{L.LAYERS} message-passing "
+              f"layers, hidden {L.HIDDEN}, BF16 weights / activations, FP32 accumulation", "parallelism": "replicas"}
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned component"}),
+                  flush=True)
+        return
+    dev = torch.device("cuda", local_rank if world > 1 else 0)
+    torch.cuda.set_device(dev)
+
+    def mesh_set(n, seed):
+        rng = np.random.default_rng(seed)
+        levels = rng.integers(2, 4, n)
+        ks = rng.uniform(1.0, 8.0, n)
+        meshes = [pkg.meshes.star_shape(int(levels[i]), seed=seed * 100000 + i) for i in range(n)]
+        waves, dirs = _incidences(rng, n, nc, ks, MM)
+        return meshes, [float(k) for k in ks], waves, dirs
+
+    def solve_chunks(meshes, ks, waves, tol, chunk=64, x0_fn=None, use_graph=True):
+        """Per chunk: batch, assemble, excite, (initial guess), solve. Yields per-chunk results."""
+        for c0 in range(0, len(meshes), chunk):
+            c1 = min(c0 + chunk, len(meshes))
+            bt = pkg.batch.MeshBatch(meshes[c0:c1], ks[c0:c1], device=dev, formulation="cfie_ref")
+            Z = bt.assemble()
+            B = bt.excitation(torch.stack(waves[c0:c1]).to(dev))
+            bt.rows_per_warp = 2
+            X0 = x0_fn(bt, Z, B, c0) if x0_fn else None
+            X, info = bt.solve(Z, B, restart=50, tol=tol, max_iters=2000, use_graph=use_graph, X0=X0)
+            yield bt, Z, B, X, info, c0
+
+    # 1. training data: solves by the batched solver
+    t0 = time.perf_counter()
+    meshes, ks, waves, dirs = mesh_set(n_train, 1)
+    items = []
+    graphs = {}
+    for bt, Z, B, X, info, c0 in solve_chunks(meshes, ks, waves, 1e-6):
+        for i in range(bt.n_mesh):
+            mi = c0 + i
+            v, f = meshes[mi]
+            g = L.edge_graph(torch.tensor(v, dtype=torch.float32, device=dev),
+                             torch.tensor(f, dtype=torch.int32, device=dev))
+            for r in range(nc):
+                b_e, j = bt.column(B, i, r), bt.column(X, i, r)
+                x0 = L.node_features(g, ks[mi], dirs[mi][0][r], dirs[mi][1][r], b_e)
+                items.append((g, x0, j))
+    samples = L.build_samples(items)
+    del items
+    torch.cuda.synchronize(dev)
+    gen_s = time.perf_counter() - t0
+    # 2. training on the GPU kernels
+    t0 = time.perf_counter()
+    net = L.EdgeGNN(dev, seed=0)
+    losses = L.train(net, samples, epochs=8, batch=32, lr=1e-3)
+    torch.cuda.synchronize(dev)
+    train_s = time.perf_counter() - t0
+    del samples
+    # 3. held-out meshes: GMRES from zero vs from the network's guess, tolerance 1e-4
+    tmeshes, tks, twaves, tdirs = mesh_set(n_test, 2)
+
+    tgraphs = {}
+
+    def learned_x0(bt, Z, B, c0):
+        """All columns of the chunk in one forward pass; then the best scale per column."""
+        items = []
+        for i in range(bt.n_mesh):
+            mi = c0 + i
+            if mi not in tgraphs:
+                v, f = tmeshes[mi]
+                tgraphs[mi] = L.edge_graph(torch.tensor(v, dtype=torch.float32, device=dev),
+                                           torch.tensor(f, dtype=torch.int32, device=dev))
+            g = tgraphs[mi]
+            for r in range(nc):
+                b_e = bt.column(B, i, r)
+                items.append((g, L.node_features(g, tks[mi], tdirs[mi][0][r], tdirs[mi][1][r], b_e), b_e))
+        smp = L.build_samples(items)
+        x0, nbr, _ = L.batch_slice(smp, 0, len(items))
+        pred = net.predict(x0, nbr)
+        X0 = torch.zeros((bt.n_rows, bt.n_mesh * bt.nc), dtype=torch.complex64, device=dev)
+        for col, (g, _, _) in enumerate(items):
+            X0[: g.n_edges, col] = pred[smp.starts[col]:smp.starts[col + 1]]
+        ZX = bt.matvec(Z, X0)
+        num = (ZX.conj() * B).sum(0)
+        den = (ZX.abs() ** 2).sum(0).clamp_min(1e-30)
+        return X0 * (num / den)[None, :]
+
+    res = {}
+    for name, fn in (("zero_start", None), ("learned_start", learned_x0)):
+        steps, ms, fit_err = [], 0.0, []
+        for _ in range(2):  # second pass timed (first warms the caches and the graph)
+            steps, ms = [], 0.0
+            for bt, Z, B, X, info, c0 in solve_chunks(tmeshes, tks, twaves, 1e-4, x0_fn=fn, use_graph=False):
+                steps.append(info["iterations"])
+        # time of the whole held-out set (assembly + guess + solve)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for bt, Z, B, X, info, c0 in solve_chunks(tmeshes, tks, twaves, 1e-4, x0_fn=fn, use_graph=False):
+            pass
+        e1.record()
+        torch.cuda.synchronize(dev)
+        res[name] = {"arnoldi_steps_per_chunk": steps, "total_steps": int(sum(steps)), "ms": e0.elapsed_time(e1)}
+    # accuracy of the raw guess on the held-out set (relative error vs the 1e-6 solution)
+    errs = []
+    for bt, Z, B, X, info, c0 in solve_chunks(tmeshes[:64], tks[:64], twaves[:64], 1e-6):
+        X0 = learned_x0(bt, Z, B, c0)
+        num = torch.linalg.norm(X0.to(torch.complex128) - X, dim=0)
+        errs.extend((num / torch.linalg.norm(X, dim=0)).cpu().tolist())
+    line = {"metric": "held-out time to 1e-4 relative residual with the learned initial guess", "value":
+            res["learned_start"]["ms"], "unit": "ms", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": res["learned_start"]["ms"], "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 network, f32 solver", "data": "synthetic", "config": config,
+            "generation_s": gen_s, "training_s": train_s, "epoch_losses": losses,
+            "guess_rel_err_median": float(np.median(errs)), "guess_rel_err_p90": float(np.quantile(errs, 0.9)),
+            "zero_start": res["zero_start"], "learned_start": res["learned_start"],
+            "step_ratio": res["zero_start"]["total_steps"] / max(1, res["learned_start"]["total_steps"]),
+            "time_ratio": res["zero_start"]["ms"] / res["learned_start"]["ms"], "gpu_launches": None}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------------------
@@ -873,6 +1017,8 @@ def main():
         return main_cgemm(args, rank, world, local_rank)
     if args.workload.startswith("batch_"):
         return main_batch(args, rank, world, local_rank)
+    if args.workload.startswith("learned_"):
+        return main_learned(args, rank, world, local_rank)
     level, k, gq = WORKLOADS[args.workload]
     n_faces = 20 * 4 ** level
     n_edges = 30 * 4 ** level

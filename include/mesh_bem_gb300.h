@@ -225,6 +225,27 @@ int mb_cgemm_tf32x3(const float* z_hi, const float* z_lo, int64_t n, const float
 int mb_cgemm_status(void* workspace, int64_t n, int64_t m, int32_t* status, void* stream);
 
 
+/* ---- Learned initial guess: kernels of the message-passing network ----------------------
+ * (no counterpart in the reference).  Row-major matrices; dtype flags 1 = bf16, 0 = fp32.
+ * mb_gnn_gemm: y[n, m] = act(x[n, k] w[k, m] + bias) (w [m, k] used transposed when
+ * trans_w); FP32 accumulation; relu 0/1; bias may be NULL.  Supported: bf16 x bf16 ->
+ * bf16 or fp32; fp32 x bf16^T -> fp32; fp32 x fp32 (either orientation) -> fp32.
+ * mb_gnn_gemm_tn: dw[k, m] += x[n, k]^T dy[n, m] (FP32 atomics).  mb_gnn_colsum:
+ * db[m] += sum_n dy[n, m].  mb_gnn_aggregate: out[n] = [h[n], mean of h over nbr[n, 0..3]
+ * (-1 = none)] (bf16, out [n, 2f]).  mb_gnn_aggregate_bwd: its adjoint into dh (fp32,
+ * accumulated).  mb_gnn_relu_bwd: dz = dy where y > 0.  mb_gnn_adam: one Adam step on fp32
+ * master weights (step counts from 1), refreshing the bf16 copy when w_bf16 != NULL. */
+int mb_gnn_gemm(const void* x, int x_bf16, const void* w, int w_bf16, int trans_w, const float* bias,
+                int64_t n, int k, int m, int relu, void* y, int y_bf16, void* stream);
+int mb_gnn_gemm_tn(const void* x, int x_bf16, const float* dy, int64_t n, int k, int m, float* dw,
+                   void* stream);
+int mb_gnn_colsum(const float* dy, int64_t n, int m, float* db, void* stream);
+int mb_gnn_aggregate(const void* h, const int32_t* nbr, int64_t n, int f, void* out, void* stream);
+int mb_gnn_aggregate_bwd(const float* dcat, const int32_t* nbr, int64_t n, int f, float* dh, void* stream);
+int mb_gnn_relu_bwd(const void* y, const float* dy, int64_t count, float* dz, void* stream);
+int mb_gnn_adam(float* w, float* m1, float* m2, const float* g, int64_t count, double lr, double beta1,
+                double beta2, double eps, int step, void* w_bf16, void* stream);
+
 /* ---- Dense iterative solve (replaces torch.linalg.solve, mesh_BEM_solver_3d.py:174) -- */
 
 /* Outcome of mb_gmres_c64. status: 0 converged to tol, 1 stopped at max_iters. */

@@ -17,7 +17,7 @@ import sys as _sys
 
 _sys.modules.setdefault("mesh_ferrofluid_gb300", _sys.modules[__name__])
 
-from . import batch, layers, mesh_io, meshes, mesh_MOM_3d, ray_query, roofline, utils  # noqa: E402
+from . import batch, layers, learned, mesh_io, meshes, mesh_MOM_3d, ray_query, roofline, utils  # noqa: E402
 from ._lib import MeshBEMError, load as load_library  # noqa: E402
 from .kernel_functions import (  # noqa: E402
     MeshMOMInterpolateJsKernel,

@@ -194,15 +194,17 @@ class MeshBatch:
         return best
 
     def solve(self, z_flat: torch.Tensor, B: torch.Tensor, restart: int = 50, max_iters: int = 2000,
-              tol: float = 1e-6, use_graph: bool = True, workspace=None):
-        """Lockstep GMRES on every (mesh, wave) column -> (X complex128 padded, info dict)."""
+              tol: float = 1e-6, use_graph: bool = True, workspace=None, X0: torch.Tensor | None = None):
+        """Lockstep GMRES on every (mesh, wave) column -> (X complex128 padded, info dict).
+
+        X0: optional initial guess on the padded layout (rows beyond E_i must be zero)."""
         if self.nc is None:
             raise RuntimeError("call excitation() first")
         rows = self.rows_per_warp or 2
         goff = self._warp_offsets(rows)
         m = self.n_mesh * self.nc
         bb = B.to(torch.complex128).contiguous()
-        X = torch.zeros_like(bb)
+        X = torch.zeros_like(bb) if X0 is None else X0.to(torch.complex128).clone().contiguous()
         need = int(_lib.load().mb_gmres_blockdiag_workspace_bytes(self.n_rows, m, int(restart)))
         if workspace is None:
             workspace = torch.empty(need, dtype=torch.uint8, device=self.device)

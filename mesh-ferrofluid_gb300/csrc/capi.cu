@@ -70,6 +70,15 @@ int cgemm_tf32x3(const float* z_hi, const float* z_lo, int64_t n, const float* x
                  size_t ws_bytes, cudaStream_t s);
 int cgemm_status(void* ws, int64_t n, int64_t m, int* out, cudaStream_t s);
 size_t gmres_multi_workspace_bytes(int64_t n, int64_t m, int r);
+int gnn_gemm(const void* X, int x_bf16, const void* W, int w_bf16, int trans_w, const float* bias, int64_t N, int K,
+             int M, int relu, void* Y, int y_bf16, cudaStream_t s);
+int gnn_gemm_tn(const void* X, int x_bf16, const float* dY, int64_t N, int K, int M, float* dW, cudaStream_t s);
+int gnn_colsum(const float* dY, int64_t N, int M, float* db, cudaStream_t s);
+int gnn_aggregate(const void* h, const int32_t* nbr, int64_t N, int F, void* out, cudaStream_t s);
+int gnn_aggregate_bwd(const float* dcat, const int32_t* nbr, int64_t N, int F, float* dh, cudaStream_t s);
+int gnn_relu_bwd(const void* y, const float* dy, int64_t count, float* dz, cudaStream_t s);
+int gnn_adam(float* w, float* m1, float* m2, const float* g, int64_t count, float lr, float b1, float b2, float eps,
+             int step, void* w16, cudaStream_t s);
 size_t gmres_blockdiag_workspace_bytes(int64_t n, int64_t m, int r);
 int blockdiag_matvec(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
                      const float* x, int64_t ld, int nc, int rows, float* y, cudaStream_t s);
@@ -556,6 +565,42 @@ int mb_gmres_blockdiag_c64(const float* z, const int64_t* desc, const int64_t* g
         info->reserved = 0;
     }
     return rc;
+}
+
+int mb_gnn_gemm(const void* x, int x_bf16, const void* w, int w_bf16, int trans_w, const float* bias, int64_t n,
+                int k, int m, int relu, void* y, int y_bf16, void* stream) {
+    MB_REQUIRE(n >= 0 && k >= 0 && m >= 0, "bad sizes");
+    if (n == 0 || k == 0 || m == 0) return MB_OK;
+    MB_REQUIRE(x && w && y, "null pointer argument");
+    return gnn_gemm(x, x_bf16, w, w_bf16, trans_w, bias, n, k, m, relu, y, y_bf16, as_stream(stream));
+}
+int mb_gnn_gemm_tn(const void* x, int x_bf16, const float* dy, int64_t n, int k, int m, float* dw, void* stream) {
+    MB_REQUIRE(n >= 0 && k >= 0 && m >= 0, "bad sizes");
+    if (n == 0 || k == 0 || m == 0) return MB_OK;
+    MB_REQUIRE(x && dy && dw, "null pointer argument");
+    return gnn_gemm_tn(x, x_bf16, dy, n, k, m, dw, as_stream(stream));
+}
+int mb_gnn_colsum(const float* dy, int64_t n, int m, float* db, void* stream) {
+    MB_REQUIRE(n >= 0 && m >= 0 && (n == 0 || (dy && db)), "bad arguments");
+    return gnn_colsum(dy, n, m, db, as_stream(stream));
+}
+int mb_gnn_aggregate(const void* h, const int32_t* nbr, int64_t n, int f, void* out, void* stream) {
+    MB_REQUIRE(n >= 0 && f > 0 && (n == 0 || (h && nbr && out)), "bad arguments");
+    return gnn_aggregate(h, nbr, n, f, out, as_stream(stream));
+}
+int mb_gnn_aggregate_bwd(const float* dcat, const int32_t* nbr, int64_t n, int f, float* dh, void* stream) {
+    MB_REQUIRE(n >= 0 && f > 0 && (n == 0 || (dcat && nbr && dh)), "bad arguments");
+    return gnn_aggregate_bwd(dcat, nbr, n, f, dh, as_stream(stream));
+}
+int mb_gnn_relu_bwd(const void* y, const float* dy, int64_t count, float* dz, void* stream) {
+    MB_REQUIRE(count >= 0 && (count == 0 || (y && dy && dz)), "bad arguments");
+    return gnn_relu_bwd(y, dy, count, dz, as_stream(stream));
+}
+int mb_gnn_adam(float* w, float* m1, float* m2, const float* g, int64_t count, double lr, double beta1, double beta2,
+                double eps, int step, void* w_bf16, void* stream) {
+    MB_REQUIRE(count >= 0 && step >= 1 && (count == 0 || (w && m1 && m2 && g)), "bad arguments");
+    return gnn_adam(w, m1, m2, g, count, (float)lr, (float)beta1, (float)beta2, (float)eps, step, w_bf16,
+                    as_stream(stream));
 }
 
 size_t mb_gmres_real_workspace_bytes(int64_t n, int restart) {
