@@ -288,7 +288,9 @@ __device__ __forceinline__ void mom_entry_fast(const float* __restrict__ verts,
                                                const float* __restrict__ normals, const float4* s_t,
                                                const float4* s_s, float k, int64_t f1, int e1, int64_t f2,
                                                int e2, float* out_re, float* out_im) {
-    constexpr int NT = NX * NX, NS = NY * NY, NP = (NS + 1) / 2;
+    // NP full pairs of source points in packed f32x2 registers; an odd count leaves one
+    // source point (TAIL) that is evaluated with scalar instructions.
+    constexpr int NT = NX * NX, NS = NY * NY, NP = NS / 2, TAIL = NS & 1;
     const int32_t a0 = __ldg(faces + 3 * f1 + e1);
     const int32_t a1 = __ldg(faces + 3 * f1 + (e1 + 1) % 3);
     const int32_t a2 = __ldg(faces + 3 * f1 + (e1 + 2) % 3);
@@ -309,23 +311,32 @@ __device__ __forceinline__ void mom_entry_fast(const float* __restrict__ verts,
     const float c2 = (b1 < b2 ? 1.f : -1.f) * sqrtf(dot(d2, d2)) / (2.f * area2);
 
     // Source points (origin B0) packed two per register pair: coordinates, weight and the
-    // projections on the test edge vectors and normal.  An odd count is padded with a
-    // zero-weight copy of the last point (it adds exactly 0 to every sum).
-    float2 yx[NP], yy[NP], yz[NP], yw[NP], ye1[NP], ye2[NP], yn[NP];
+    // projections on the test edge vectors and normal.
+    float2 yx[NP > 0 ? NP : 1], yy[NP > 0 ? NP : 1], yz[NP > 0 ? NP : 1], yw[NP > 0 ? NP : 1],
+        ye1[NP > 0 ? NP : 1], ye2[NP > 0 ? NP : 1], yn[NP > 0 ? NP : 1];
+    float tx = 0.f, ty = 0.f, tz = 0.f, tw = 0.f, te1 = 0.f, te2 = 0.f, tn = 0.f;  // the tail point
 #pragma unroll
-    for (int j = 0; j < 2 * NP; ++j) {
-        const int js = j < NS ? j : NS - 1;
-        const float4 r = s_s[js];
+    for (int j = 0; j < NS; ++j) {
+        const float4 r = s_s[j];
         const V3<float> y = (r.x - r.y) * B1 + r.y * B2;
-        const float w = j < NS ? r.z * (2.f * area2) : 0.f;
-        float* px = reinterpret_cast<float*>(&yx[j / 2]) + (j & 1);
-        px[0] = y.x;
-        (reinterpret_cast<float*>(&yy[j / 2]) + (j & 1))[0] = y.y;
-        (reinterpret_cast<float*>(&yz[j / 2]) + (j & 1))[0] = y.z;
-        (reinterpret_cast<float*>(&yw[j / 2]) + (j & 1))[0] = w;
-        (reinterpret_cast<float*>(&ye1[j / 2]) + (j & 1))[0] = dot(y, ev1);
-        (reinterpret_cast<float*>(&ye2[j / 2]) + (j & 1))[0] = dot(y, ev2);
-        (reinterpret_cast<float*>(&yn[j / 2]) + (j & 1))[0] = dot(y, n1);
+        const float w = r.z * (2.f * area2);
+        if (j < 2 * NP) {
+            (reinterpret_cast<float*>(&yx[j / 2]) + (j & 1))[0] = y.x;
+            (reinterpret_cast<float*>(&yy[j / 2]) + (j & 1))[0] = y.y;
+            (reinterpret_cast<float*>(&yz[j / 2]) + (j & 1))[0] = y.z;
+            (reinterpret_cast<float*>(&yw[j / 2]) + (j & 1))[0] = w;
+            (reinterpret_cast<float*>(&ye1[j / 2]) + (j & 1))[0] = dot(y, ev1);
+            (reinterpret_cast<float*>(&ye2[j / 2]) + (j & 1))[0] = dot(y, ev2);
+            (reinterpret_cast<float*>(&yn[j / 2]) + (j & 1))[0] = dot(y, n1);
+        } else {
+            tx = y.x;
+            ty = y.y;
+            tz = y.z;
+            tw = w;
+            te1 = dot(y, ev1);
+            te2 = dot(y, ev2);
+            tn = dot(y, n1);
+        }
     }
     const float2 K2 = bc(k), M4K = bc(-4.f / k);
     float2 acc_re = bc(0.f), acc_im = bc(0.f);
@@ -370,6 +381,26 @@ __device__ __forceinline__ void mom_entry_fast(const float* __restrict__ verts,
             qr = fma2(m, t1, qr);
             qi = fma2(m, t2, qi);
         }
+        if constexpr (TAIL) {
+            // the odd source point, scalar: same algebra as one lane of the packed loop
+            const float dx = x.x - tx, dy = x.y - ty, dz = x.z - tz;
+            const float r2d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            const float rinv = rsqrtf(r2d);
+            const float kR = k * (r2d * rinv);
+            float sn, cs;
+            __sincosf(kR, &sn, &cs);
+            const float g = tw * rinv;
+            const float gr = g * cs, gs = g * sn;
+            const float ya = fmaf(t.x, te1, t.y * te2);
+            const float yu = fmaf(ya, xn, -tn * xa);
+            s0r.x += gr;
+            s0i.x += gs;
+            pr.x = fmaf(gr, ya, pr.x);
+            pi.x = fmaf(gs, ya, pi.x);
+            const float m = rinv * rinv * yu;
+            qr.x = fmaf(m, fmaf(gs, kR, gr), qr.x);
+            qi.x = fmaf(m, fmaf(gr, kR, -gs), qi.x);
+        }
         // t_re = -Qr + k Pi - (4/k) S0i,  t_im = -Qi + k Pr - (4/k) S0r   (Pi, S0i hold +sum gs)
         const float2 t_re = sub2(fma2(K2, pi, mul2(M4K, s0i)), qr);
         const float2 t_im = sub2(fma2(K2, pr, mul2(M4K, s0r)), qi);
@@ -384,7 +415,7 @@ __device__ __forceinline__ void mom_entry_fast(const float* __restrict__ verts,
 }
 
 #ifndef MB_FAST_MIN_BLOCKS
-#define MB_FAST_MIN_BLOCKS 5
+#define MB_FAST_MIN_BLOCKS 4
 #endif
 template <int NX, int NY, bool RWG>
 __global__ void __launch_bounds__(128, NX <= 4 ? MB_FAST_MIN_BLOCKS : 2) mom_ref_zmat_fast_kernel(
