@@ -1,15 +1,18 @@
 // mgmres.cu -- GMRES(restart) for many right-hand sides in lockstep, Z X = B, with every
-// Arnoldi step's m matrix-vector products done as one tensor-core product Z [v_1 .. v_m]
-// (mb_cgemm_tf32x3, FP32-class accuracy) instead of m HBM-bound matvecs.
+// Arnoldi step's m matrix-vector products done as one product Z [v_1 .. v_m] (the split-TF32
+// tensor-core GEMM, or the block-diagonal product of many meshes) instead of m HBM-bound
+// matvecs.
 //
 // Each column is an independent GMRES process (its own Hessenberg matrix, Givens rotations
-// and residual estimate); only the product with Z is shared.  The Krylov basis, the
-// Gram-Schmidt coefficients (CGS2, two passes) and the Givens rotations are FP64 / complex128
-// on the device; a column whose estimate reaches tol / 2, or whose new basis vector
-// vanishes, stops (its later basis vectors are zero) while the others continue.  Every
-// restart cycle starts from the residual B - Z X computed with the same product on the
-// complex64 rounding of X, so the attainable relative residual is that product's accuracy
-// (~1e-6).  The host loop synchronises once per Arnoldi step (the active-column count).
+// and residual estimate); only the product is shared.  The Krylov basis is stored in
+// complex64 and the two Gram-Schmidt passes (CGS2) run in FP32 arithmetic with FP64 sums
+// across rows: GB300's FP64 rate (~1.25 TFLOP/s) would bound an FP64 Gram-Schmidt at a
+// quarter of HBM bandwidth, and the FP32-class product already sets the attainable residual
+// (~1e-7 relative).  The Hessenberg matrix, the Givens rotations and the iterate X stay
+// FP64.  A column whose estimate reaches tol / 2, or whose new basis vector vanishes, stops
+// (its later basis vectors are zero) while the others continue.  Every restart cycle starts
+// from the residual B - Z X computed with the same product on the complex64 rounding of X.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -18,6 +21,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "tc_common.cuh"
 
 namespace mb {
 
@@ -28,10 +32,9 @@ int cgemm_tf32x3(const float* z_hi, const float* z_lo, int64_t n, const float* x
 constexpr int kMgMaxRestart = 128;
 
 struct MgWork {
-    double* V;      // [(r+1), n, m] complex128
-    double* w;      // [n, m] complex128
-    float* v32;     // [n, m] complex64 (GEMM input)
-    float* y32;     // [n, m] complex64 (GEMM output)
+    float2* V;      // [(r+1), n, m] complex64 Krylov basis (V_j is the product's input at step j)
+    float2* w;      // [n, m] complex64 working vector (also the complex64 X at a restart)
+    float2* y32;    // [n, m] complex64 product output
     void* gemm_ws;  // cgemm workspace
     double* H;      // [(r+1), r, m] complex128: H[i][j][c]
     double* hc;     // [(r+1), m] complex128 (one CGS pass)
@@ -44,7 +47,10 @@ struct MgWork {
     double* hn;     // [m]
     int* active;    // [m]
     int* jend;      // [m]
+    int* crow;      // [m] rows of each column (block-diagonal systems; rows beyond are zero)
+    float* scale;   // [m] 1 / |v| of the next basis vector (0 for inactive columns)
     int* count;     // [4]
+    int* status;    // [4] mbarrier time-outs of the streamed kernels (0 = none)
 };
 
 static size_t a256(size_t b) { return (b + 255) & ~size_t(255); }
@@ -58,10 +64,9 @@ static size_t mg_layout(int64_t n, int64_t m, int r, size_t prod_ws, void* base,
         off += a256(bytes);
         return at;
     };
-    W->V = static_cast<double*>(take(16 * nm * (r + 1)));
-    W->w = static_cast<double*>(take(16 * nm));
-    W->v32 = static_cast<float*>(take(8 * nm));
-    W->y32 = static_cast<float*>(take(8 * nm));
+    W->V = static_cast<float2*>(take(8 * nm * (r + 1)));
+    W->w = static_cast<float2*>(take(8 * nm));
+    W->y32 = static_cast<float2*>(take(8 * nm));
     W->gemm_ws = prod_ws ? take(prod_ws) : nullptr;
     W->H = static_cast<double*>(take(16 * (size_t)(r + 1) * r * m));
     W->hc = static_cast<double*>(take(16 * (size_t)(r + 1) * m));
@@ -74,121 +79,363 @@ static size_t mg_layout(int64_t n, int64_t m, int r, size_t prod_ws, void* base,
     W->hn = static_cast<double*>(take(8 * m));
     W->active = static_cast<int*>(take(4 * m));
     W->jend = static_cast<int*>(take(4 * m));
+    W->crow = static_cast<int*>(take(4 * m));
+    W->scale = static_cast<float*>(take(4 * m));
     W->count = static_cast<int*>(take(16));
+    W->status = static_cast<int*>(take(16));
     return off;
 }
 
+// internal width: m rounded up to even (TMA row strides are multiples of 16 bytes)
+static int64_t padded_width(int64_t m) { return m + (m & 1); }
+
 size_t gmres_multi_workspace_bytes(int64_t n, int64_t m, int r) {
     MgWork W;
-    return mg_layout(n, m, r, cgemm_workspace_bytes(n, m), nullptr, &W);
+    return mg_layout(n, padded_width(m), r, cgemm_workspace_bytes(n, padded_width(m)), nullptr, &W);
 }
 
 size_t gmres_blockdiag_workspace_bytes(int64_t n, int64_t m, int r) {
     MgWork W;
-    return mg_layout(n, m, r, 0, nullptr, &W);
+    return mg_layout(n, padded_width(m), r, 0, nullptr, &W);
 }
 
 // ---- kernels ---------------------------------------------------------------------------
-__global__ void mg_to_c64(const double* __restrict__ src, int64_t count, float* __restrict__ dst) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
-        dst[i] = (float)src[i];
+// Column-blocked kernels use 256-thread blocks of 32 columns (threadIdx.x) x 8 row lanes
+// (threadIdx.y); crow (optional) limits column c to rows k < crow[c].
+__device__ __forceinline__ int64_t rows_of(const int* __restrict__ crow, int64_t c, int64_t n) {
+    return crow ? (int64_t)__ldg(crow + c) : n;
 }
 
-__global__ void mg_widen(const float* __restrict__ src, int64_t count, double* __restrict__ dst) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
-        dst[i] = (double)src[i];
+// complex128 X [n, m] -> complex64 [n, mp] (padding columns zero); 32 x 8 blocks
+__global__ void mg_to_c64(const double2* __restrict__ src, int64_t n, int64_t m, int64_t mp, float2* __restrict__ dst) {
+    const int64_t c = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    if (c >= mp) return;
+    for (int64_t k = blockIdx.y * blockDim.y + threadIdx.y; k < n; k += (int64_t)gridDim.y * blockDim.y) {
+        const double2 v = c < m ? src[k * m + c] : make_double2(0.0, 0.0);
+        dst[k * mp + c] = make_float2((float)v.x, (float)v.y);
+    }
 }
 
-// R = B - Y (Y complex64 from the product), written into V_0; per-column |R|^2 into beta.
-__global__ void mg_residual(const double* __restrict__ b, const float* __restrict__ y, int64_t n, int64_t m,
-                            double* __restrict__ r, double* __restrict__ sq) {
+// Sum of the 8 row lanes' values of a 32 x 8 block, added to out[c] (FP64 atomics).
+__device__ __forceinline__ void col_sum_add(double v, int64_t c, int64_t m, double* __restrict__ out) {
+    __shared__ double s[8][33];
+    s[threadIdx.y][threadIdx.x] = v;
+    __syncthreads();
+    if (threadIdx.y == 0 && c < m) {
+        double t = 0.0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) t += s[q][threadIdx.x];
+        atomicAdd(out + c, t);
+    }
+}
+
+// R = B - Y (B complex128 [n, m], Y complex64 [n, mp] from the product), complex64 into V_0
+// [n, mp]; per-column |R|^2 (of the FP64 difference) into sq (pre-zeroed).
+__global__ void mg_residual(const double2* __restrict__ b, const float2* __restrict__ y, int64_t n, int64_t m,
+                            int64_t mp, float2* __restrict__ r, double* __restrict__ sq) {
     const int64_t c = (int64_t)blockIdx.x * 32 + threadIdx.x;
     double acc = 0.0;
-    if (c < m) {
+    if (c < mp) {
         for (int64_t k = blockIdx.y * blockDim.y + threadIdx.y; k < n; k += (int64_t)gridDim.y * blockDim.y) {
-            const int64_t e = 2 * (k * m + c);
-            const double re = b[e] - (double)y[e], im = b[e + 1] - (double)y[e + 1];
-            r[e] = re;
-            r[e + 1] = im;
+            const float2 yv = y[k * mp + c];
+            const double2 bv = c < m ? b[k * m + c] : make_double2(0.0, 0.0);
+            const double re = bv.x - (double)yv.x, im = bv.y - (double)yv.y;
+            r[k * mp + c] = make_float2((float)re, (float)im);
             acc += re * re + im * im;
         }
     }
-    __shared__ double s[8][33];
-    s[threadIdx.y][threadIdx.x] = acc;
-    __syncthreads();
-    if (threadIdx.y == 0 && c < m) {
-        double t = 0.0;
-        for (int q = 0; q < (int)blockDim.y; ++q) t += s[q][threadIdx.x];
-        atomicAdd(sq + c, t);
-    }
+    col_sum_add(acc, c, mp, sq);
 }
 
 // per-column |x|^2 of a complex128 [n, m] block into sq (pre-zeroed)
-__global__ void mg_colnorm2(const double* __restrict__ x, int64_t n, int64_t m, double* __restrict__ sq) {
+__global__ void mg_colnorm2(const double2* __restrict__ x, int64_t n, int64_t m, double* __restrict__ sq) {
     const int64_t c = (int64_t)blockIdx.x * 32 + threadIdx.x;
     double acc = 0.0;
     if (c < m) {
         for (int64_t k = blockIdx.y * blockDim.y + threadIdx.y; k < n; k += (int64_t)gridDim.y * blockDim.y) {
-            const int64_t e = 2 * (k * m + c);
-            acc += x[e] * x[e] + x[e + 1] * x[e + 1];
+            const double2 v = x[k * m + c];
+            acc += v.x * v.x + v.y * v.y;
         }
     }
-    __shared__ double s[8][33];
-    s[threadIdx.y][threadIdx.x] = acc;
-    __syncthreads();
-    if (threadIdx.y == 0 && c < m) {
-        double t = 0.0;
-        for (int q = 0; q < (int)blockDim.y; ++q) t += s[q][threadIdx.x];
-        atomicAdd(sq + c, t);
+    col_sum_add(acc, c, m, sq);
+}
+
+// ---- streamed Gram-Schmidt ------------------------------------------------------------------
+// The two bandwidth kernels of an Arnoldi step read every basis vector V_0 .. V_{nb-1} once.
+// Their tiles (64 rows x 32 columns of complex64, 16 KB) come from TMA into an S-stage ring
+// in shared memory (two 16-column boxes per tile, 128-byte swizzle), loaded by one producer
+// warp and read by 8 consumer warps; full / empty mbarriers, every wait bounded (a time-out
+// sets *status and ends the block).  Consumer lane = 4 ly + lx of warp w owns column
+// 4 w + lx and rows ly + 8 t (t < 8) of the tile, so a sum over the tile's rows is a shuffle
+// reduction inside the warp and the 8 warps never combine partial sums.  grid.x = column
+// groups of 32, grid.y = blocks along the rows (persistent).  The internal width mp is even
+// (16-byte TMA row strides).
+constexpr int kGsRows = 64;
+constexpr int kGsStage = 16384;
+constexpr int kGsThreads = 288;  // 8 consumer warps + 1 producer warp
+constexpr long long kGsBudget = 1ll << 30;  // SM clocks per wait (~0.5 s)
+
+struct GsMaps {
+    CUtensorMap v;    // basis: (mp, n, r+1) 8-byte elements, box (16, 64, 1)
+    CUtensorMap src;  // w or y: (mp, n), box (16, 64)
+};
+
+// byte offset of (row r, column cc) in a stage: box cc / 16, 128-byte rows, 16-byte chunk
+// index XOR (row % 8)
+__device__ __forceinline__ uint32_t gs_off(int r, int cc) {
+    const int q = cc & 15;
+    return (uint32_t)((cc >> 4) * 8192 + r * 128 + (((q >> 1) ^ (r & 7)) << 4) + ((q & 1) << 3));
+}
+
+template <int S>
+constexpr size_t gs_smem(size_t aux) {
+    return 1024 + (size_t)S * kGsStage + 16 * S + aux;
+}
+
+struct GsRing {
+    unsigned char* stage;
+    uint64_t* full;
+    uint64_t* empty;
+    unsigned char* aux;
+};
+
+template <int S>
+__device__ __forceinline__ GsRing gs_ring(unsigned char* smem) {
+    GsRing g;
+    g.stage = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem) + 1023) & ~uintptr_t(1023));
+    g.full = reinterpret_cast<uint64_t*>(g.stage + (size_t)S * kGsStage);
+    g.empty = g.full + S;
+    g.aux = reinterpret_cast<unsigned char*>(g.empty + S);
+    return g;
+}
+
+// Producer: items p < count, item_of(p) -> (row tile q, basis index i; -1 = the src matrix).
+// After the loop it waits for the last use of every stage, so no copy is in flight at exit.
+template <int S, typename ItemOf>
+__device__ void gs_produce(const GsMaps& maps, const GsRing& g, int64_t count, int c0, ItemOf item_of,
+                           int* status) {
+    int64_t p = 0;
+    for (; p < count; ++p) {
+        const int s = (int)(p % S);
+        const int64_t use = p / S;
+        if (use > 0 && !tc::mbar_wait(&g.empty[s], (uint32_t)((use - 1) & 1), kGsBudget, status, 1)) break;
+        int64_t q;
+        int i;
+        item_of(p, q, i);
+        unsigned char* dst = g.stage + (size_t)s * kGsStage;
+        tc::mbar_arrive_expect_tx(&g.full[s], kGsStage);
+        const int y = (int)(q * kGsRows);
+        if (i < 0) {
+            tc::tma_load_2d(dst, &maps.src, &g.full[s], c0, y);
+            tc::tma_load_2d(dst + 8192, &maps.src, &g.full[s], c0 + 16, y);
+        } else {
+            tc::tma_load_3d(dst, &maps.v, &g.full[s], c0, y, i);
+            tc::tma_load_3d(dst + 8192, &maps.v, &g.full[s], c0 + 16, y, i);
+        }
+    }
+    for (int s = 0; s < S; ++s) {
+        const int64_t uses = p > s ? (p - s + S - 1) / S : 0;
+        if (uses > 0) tc::mbar_wait(&g.full[s], (uint32_t)((uses - 1) & 1), kGsBudget, status, 2);
     }
 }
 
-// hc[i][c] += sum_k conj(V[i][k][c]) w[k][c] for i < nb (pre-zeroed); grid.z = i.
-__global__ void mg_dots(const double* __restrict__ V, const double* __restrict__ w, int64_t n, int64_t m,
-                        double* __restrict__ hc) {
-    const int64_t c = (int64_t)blockIdx.x * 32 + threadIdx.x;
-    const int i = blockIdx.z;
-    double ar = 0.0, ai = 0.0;
-    if (c < m) {
-        const double* vi = V + 2 * (size_t)i * n * m;
-        for (int64_t k = blockIdx.y * blockDim.y + threadIdx.y; k < n; k += (int64_t)gridDim.y * blockDim.y) {
-            const int64_t e = 2 * (k * m + c);
-            const double vr = vi[e], vim = vi[e + 1], wr = w[e], wi = w[e + 1];
-            ar = fma(vr, wr, fma(vim, wi, ar));
-            ai = fma(vr, wi, fma(-vim, wr, ai));
+template <int S>
+__device__ __forceinline__ void gs_init(const GsRing& g) {
+    if (threadIdx.x == 256) {
+        for (int s = 0; s < S; ++s) {
+            tc::mbar_init(&g.full[s], 1);
+            tc::mbar_init(&g.empty[s], 8);
         }
-    }
-    __shared__ double sr[8][33], si[8][33];
-    sr[threadIdx.y][threadIdx.x] = ar;
-    si[threadIdx.y][threadIdx.x] = ai;
-    __syncthreads();
-    if (threadIdx.y == 0 && c < m) {
-        double tr = 0.0, ti = 0.0;
-        for (int q = 0; q < (int)blockDim.y; ++q) {
-            tr += sr[q][threadIdx.x];
-            ti += si[q][threadIdx.x];
-        }
-        atomicAdd(hc + 2 * ((int64_t)i * m + c), tr);
-        atomicAdd(hc + 2 * ((int64_t)i * m + c) + 1, ti);
+        tc::fence_mbar_init();
     }
 }
 
-// w[k][c] -= sum_{i<nb} V[i][k][c] hc[i][c]
-__global__ void mg_subtract(const double* __restrict__ V, const double* __restrict__ hc, int64_t n, int64_t m, int nb,
-                            double* __restrict__ w) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= n * m) return;
-    const int64_t c = idx % m;
-    double wr = w[2 * idx], wi = w[2 * idx + 1];
-#pragma unroll 4
-    for (int i = 0; i < nb; ++i) {
-        const double hr = hc[2 * ((int64_t)i * m + c)], hi = hc[2 * ((int64_t)i * m + c) + 1];
-        const double vr = V[2 * ((int64_t)i * n * m + idx)], vi = V[2 * ((int64_t)i * n * m + idx) + 1];
-        wr -= hr * vr - hi * vi;
-        wi -= hr * vi + hi * vr;
+// hc[i][c] += sum_k conj(V_i[k][c]) w[k][c] for i < nb (hc pre-zeroed).  A block's work is a
+// contiguous range of the sequence (row tile q, item i = -1 .. nb-1), item -1 being w (kept
+// in registers for the tile); FP32 products over a thread's 8 rows and the warp's 8 row
+// lanes, FP64 sums per (i, column) in shared memory across the block's tiles, FP64 atomics
+// once per block.
+template <int S>
+__global__ void __launch_bounds__(kGsThreads) mg_dots(const __grid_constant__ GsMaps maps,
+                                                      const float2* __restrict__ w, int64_t n, int64_t mp, int nb,
+                                                      double* __restrict__ hc, int* __restrict__ status) {
+    extern __shared__ unsigned char gs_raw[];
+    const GsRing g = gs_ring<S>(gs_raw);
+    double2* acc_s = reinterpret_cast<double2*>(g.aux);  // [nb][32]
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, lx = lane & 3, ly = lane >> 2;
+    const int c0 = blockIdx.x * 32;
+    const int L = nb + 1;
+    const int64_t tiles = (n + kGsRows - 1) / kGsRows;
+    const int64_t items = tiles * L;
+    const int64_t p0 = items * blockIdx.y / gridDim.y, p1 = items * (blockIdx.y + 1) / gridDim.y;
+    if (p0 >= p1) return;
+    gs_init<S>(g);
+    for (int e = tid; e < nb * 32; e += kGsThreads) acc_s[e] = make_double2(0.0, 0.0);
+    __syncthreads();
+    if (warp == 8) {
+        if (lane == 0) {
+            tc::prefetch_tmap(&maps.v);
+            tc::prefetch_tmap(&maps.src);
+            gs_produce<S>(maps, g, p1 - p0, c0,
+                          [&](int64_t p, int64_t& q, int& i) {
+                              const int64_t a = p0 + p;
+                              q = a / L;
+                              i = (int)(a - q * L) - 1;
+                          },
+                          status);
+        }
+    } else {
+        const int cc = warp * 4 + lx;
+        const int64_t c = c0 + cc;
+        float2 wv[8];
+        {
+            // a range that starts inside a tile reads that tile's w directly
+            const int64_t q = p0 / L;
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int64_t k = q * kGsRows + ly + 8 * t;
+                wv[t] = (k < n && c < mp) ? w[k * mp + c] : make_float2(0.f, 0.f);
+            }
+        }
+        for (int64_t p = 0; p < p1 - p0; ++p) {
+            const int s = (int)(p % S);
+            if (!tc::mbar_wait(&g.full[s], (uint32_t)((p / S) & 1), kGsBudget, status, 4)) break;
+            const unsigned char* st = g.stage + (size_t)s * kGsStage;
+            const int i = (int)((p0 + p) % L) - 1;
+            if (i < 0) {
+#pragma unroll
+                for (int t = 0; t < 8; ++t) wv[t] = *reinterpret_cast<const float2*>(st + gs_off(ly + 8 * t, cc));
+            } else {
+                float ar = 0.f, ai = 0.f;
+#pragma unroll
+                for (int t = 0; t < 8; ++t) {
+                    const float2 v = *reinterpret_cast<const float2*>(st + gs_off(ly + 8 * t, cc));
+                    ar = fmaf(v.x, wv[t].x, fmaf(v.y, wv[t].y, ar));
+                    ai = fmaf(v.x, wv[t].y, fmaf(-v.y, wv[t].x, ai));
+                }
+#pragma unroll
+                for (int o = 4; o < 32; o <<= 1) {
+                    ar += __shfl_xor_sync(0xffffffffu, ar, o);
+                    ai += __shfl_xor_sync(0xffffffffu, ai, o);
+                }
+                if (ly == 0) {
+                    double2& a = acc_s[i * 32 + cc];
+                    a.x += (double)ar;
+                    a.y += (double)ai;
+                }
+            }
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&g.empty[s]);
+        }
     }
-    w[2 * idx] = wr;
-    w[2 * idx + 1] = wi;
+    __syncthreads();
+    for (int e = tid; e < nb * 32; e += kGsThreads) {
+        const int i = e / 32, cc = e % 32;
+        if (c0 + cc >= mp) continue;
+        double* h = hc + 2 * ((int64_t)i * mp + c0 + cc);
+        atomicAdd(h, acc_s[e].x);
+        atomicAdd(h + 1, acc_s[e].y);
+    }
+}
+
+// dst[k][c] = src[k][c] + sign * sum_{i<nb} V_i[k][c] coef[i][c] (FP32 products and sums;
+// dst may alias src).  MODE 0: src / dst complex64 [n, mp] (src streamed as item -1 of each
+// tile); MODE 1: the same, plus per-column |dst|^2 added to sq (pre-zeroed); MODE 2: the
+// iterate X, complex128 [n, m] read and written directly (columns c < m).  A block owns row
+// tiles q = blockIdx.y + j gridDim.y of its column group; the group's coefficients sit in
+// shared memory.
+template <int S, int MODE>
+__global__ void __launch_bounds__(kGsThreads) mg_combine(const __grid_constant__ GsMaps maps,
+                                                         const double* __restrict__ coef, int64_t n, int64_t mp,
+                                                         int64_t m, int nb, float sign, void* dst_v,
+                                                         double* __restrict__ sq, int* __restrict__ status) {
+    constexpr bool kStream = MODE != 2;
+    extern __shared__ unsigned char gs_raw[];
+    const GsRing g = gs_ring<S>(gs_raw);
+    float2* s_coef = reinterpret_cast<float2*>(g.aux);  // [nb][32]
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, lx = lane & 3, ly = lane >> 2;
+    const int c0 = blockIdx.x * 32;
+    const int L = nb + (kStream ? 1 : 0);
+    const int64_t tiles = (n + kGsRows - 1) / kGsRows;
+    const int64_t my_tiles = tiles > blockIdx.y ? (tiles - blockIdx.y + gridDim.y - 1) / gridDim.y : 0;
+    if (my_tiles == 0) return;
+    const int64_t count = my_tiles * L;
+    gs_init<S>(g);
+    for (int e = tid; e < nb * 32; e += kGsThreads) {
+        const int i = e / 32, cc = e % 32;
+        const int64_t q = 2 * ((int64_t)i * mp + c0 + cc);
+        s_coef[e] = c0 + cc < mp ? make_float2(sign * (float)coef[q], sign * (float)coef[q + 1]) : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    if (warp == 8) {
+        if (lane == 0) {
+            tc::prefetch_tmap(&maps.v);
+            if (kStream) tc::prefetch_tmap(&maps.src);
+            gs_produce<S>(maps, g, count, c0,
+                          [&](int64_t p, int64_t& q, int& i) {
+                              const int64_t j = p / L;
+                              q = blockIdx.y + j * gridDim.y;
+                              i = (int)(p - j * L) - (kStream ? 1 : 0);
+                          },
+                          status);
+        }
+    } else {
+        const int cc = warp * 4 + lx;
+        const int64_t c = c0 + cc;
+        float2 acc[8];
+        float nrm = 0.f;
+        for (int64_t p = 0; p < count; ++p) {
+            const int s = (int)(p % S);
+            if (!tc::mbar_wait(&g.full[s], (uint32_t)((p / S) & 1), kGsBudget, status, 4)) break;
+            const unsigned char* st = g.stage + (size_t)s * kGsStage;
+            const int64_t j = p / L;
+            const int i = (int)(p - j * L) - (kStream ? 1 : 0);
+            if (p - j * L == 0) {
+#pragma unroll
+                for (int t = 0; t < 8; ++t) acc[t] = make_float2(0.f, 0.f);
+            }
+            if (i < 0) {
+#pragma unroll
+                for (int t = 0; t < 8; ++t) acc[t] = *reinterpret_cast<const float2*>(st + gs_off(ly + 8 * t, cc));
+            } else {
+                const float2 h = s_coef[i * 32 + cc];
+#pragma unroll
+                for (int t = 0; t < 8; ++t) {
+                    const float2 v = *reinterpret_cast<const float2*>(st + gs_off(ly + 8 * t, cc));
+                    acc[t].x = fmaf(h.x, v.x, fmaf(-h.y, v.y, acc[t].x));
+                    acc[t].y = fmaf(h.x, v.y, fmaf(h.y, v.x, acc[t].y));
+                }
+            }
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&g.empty[s]);
+            if (i == nb - 1) {  // tile complete
+                const int64_t q = blockIdx.y + j * gridDim.y;
+#pragma unroll
+                for (int t = 0; t < 8; ++t) {
+                    const int64_t k = q * kGsRows + ly + 8 * t;
+                    if (k >= n) continue;
+                    if (MODE == 2) {
+                        if (c < m) {
+                            double2* x = static_cast<double2*>(dst_v) + k * m + c;
+                            double2 o = *x;
+                            o.x += (double)acc[t].x;
+                            o.y += (double)acc[t].y;
+                            *x = o;
+                        }
+                    } else if (c < mp) {
+                        static_cast<float2*>(dst_v)[k * mp + c] = acc[t];
+                        if (MODE == 1) nrm += acc[t].x * acc[t].x + acc[t].y * acc[t].y;
+                    }
+                }
+            }
+        }
+        if (MODE == 1) {
+#pragma unroll
+            for (int o = 4; o < 32; o <<= 1) nrm += __shfl_xor_sync(0xffffffffu, nrm, o);
+            if (ly == 0 && c < mp) atomicAdd(sq + c, (double)nrm);
+        }
+    }
+    __syncthreads();
 }
 
 // H[i][j][c] += hc[i][c] for i < nb (accumulates the two CGS passes)
@@ -203,33 +450,47 @@ __global__ void mg_accum_h(const double* __restrict__ hc, int nb, int j, int r, 
 }
 
 // One thread per column: H[j+1][j] = |w|, previous rotations applied to column j, a new
-// rotation, the residual estimate; inactive columns are left untouched.
+// rotation, the residual estimate, the scale of the next basis vector; inactive columns are
+// left untouched (their scale stays 0).
 __global__ void mg_givens(double* __restrict__ H, double* __restrict__ cs, double* __restrict__ sn,
                           double* __restrict__ g, const double* __restrict__ hn2, const double* __restrict__ bnorm,
                           int j, int r, int64_t m, double tol, int* __restrict__ active, int* __restrict__ jend,
-                          int* __restrict__ count) {
+                          int* __restrict__ count, float* __restrict__ scale) {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m || !active[c]) return;
     auto hre = [&](int i) -> double& { return H[2 * (((int64_t)i * r + j) * m + c)]; };
     auto him = [&](int i) -> double& { return H[2 * (((int64_t)i * r + j) * m + c) + 1]; };
     const double hn = sqrt(hn2[c]);
-    hre(j + 1) = hn;
-    him(j + 1) = 0.0;
-    for (int i = 0; i < j; ++i) {
-        const double cr = cs[2 * ((int64_t)i * m + c)], ci = cs[2 * ((int64_t)i * m + c) + 1];
-        const double sr = sn[2 * ((int64_t)i * m + c)], si = sn[2 * ((int64_t)i * m + c) + 1];
-        const double ar = hre(i), ai = him(i), br = hre(i + 1), bi = him(i + 1);
-        // t = conj(c) a + conj(s) b ;  b' = -s a + c b
-        const double tr = cr * ar + ci * ai + sr * br + si * bi;
-        const double ti = cr * ai - ci * ar + sr * bi - si * br;
-        const double nbr = -(sr * ar - si * ai) + (cr * br - ci * bi);
-        const double nbi = -(sr * ai + si * ar) + (cr * bi + ci * br);
-        hre(i) = tr;
-        him(i) = ti;
-        hre(i + 1) = nbr;
-        him(i + 1) = nbi;
+    // the rotated column: a carries entry i through the loop.  The rotations and the entries
+    // below come in chunks of 4, all loaded before the chunk's stores (each load otherwise
+    // waits for the previous store to the same array).
+    double ar = hre(0), ai = him(0);
+    for (int i0 = 0; i0 < j; i0 += 4) {
+        double2 cv[4], sv[4], bv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = i0 + u;
+            if (i < j) {
+                cv[u] = make_double2(cs[2 * ((int64_t)i * m + c)], cs[2 * ((int64_t)i * m + c) + 1]);
+                sv[u] = make_double2(sn[2 * ((int64_t)i * m + c)], sn[2 * ((int64_t)i * m + c) + 1]);
+                bv[u] = make_double2(hre(i + 1), him(i + 1));
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = i0 + u;
+            if (i >= j) break;
+            const double cr = cv[u].x, ci = cv[u].y, sr = sv[u].x, si = sv[u].y, br = bv[u].x, bi = bv[u].y;
+            // t = conj(c) a + conj(s) b ;  b' = -s a + c b
+            hre(i) = cr * ar + ci * ai + sr * br + si * bi;
+            him(i) = cr * ai - ci * ar + sr * bi - si * br;
+            const double nbr = -(sr * ar - si * ai) + (cr * br - ci * bi);
+            const double nbi = -(sr * ai + si * ar) + (cr * bi + ci * br);
+            ar = nbr;
+            ai = nbi;
+        }
     }
-    const double ar = hre(j), ai = him(j), br = hre(j + 1), bi = him(j + 1);
+    const double br = hn, bi = 0.0;
     const double rr = sqrt(ar * ar + ai * ai + br * br + bi * bi);
     double cr = 1.0, ci = 0.0, sr = 0.0, si = 0.0;
     if (rr > 0.0) {
@@ -248,54 +509,48 @@ __global__ void mg_givens(double* __restrict__ H, double* __restrict__ cs, doubl
     him(j + 1) = 0.0;
     // g[j+1] = -s g[j];  g[j] = conj(c) g[j]
     const double gr = g[2 * ((int64_t)j * m + c)], gi = g[2 * ((int64_t)j * m + c) + 1];
-    g[2 * ((int64_t)(j + 1) * m + c)] = -(sr * gr - si * gi);
-    g[2 * ((int64_t)(j + 1) * m + c) + 1] = -(sr * gi + si * gr);
+    const double e1 = -(sr * gr - si * gi), e2 = -(sr * gi + si * gr);
+    g[2 * ((int64_t)(j + 1) * m + c)] = e1;
+    g[2 * ((int64_t)(j + 1) * m + c) + 1] = e2;
     g[2 * ((int64_t)j * m + c)] = cr * gr + ci * gi;
     g[2 * ((int64_t)j * m + c) + 1] = cr * gi - ci * gr;
-    const double e1 = g[2 * ((int64_t)(j + 1) * m + c)], e2 = g[2 * ((int64_t)(j + 1) * m + c) + 1];
     const double est = sqrt(e1 * e1 + e2 * e2) / bnorm[c];
     jend[c] = j + 1;
     if (est <= 0.5 * tol || hn <= 1e-300 || j + 1 == r) {
         active[c] = 0;
+        scale[c] = 0.f;
     } else {
+        scale[c] = (float)(1.0 / hn);
         atomicAdd(count, 1);
     }
 }
 
-// V_{j+1} = w / |w| for columns still active (zero otherwise); complex64 copy for the product.
-__global__ void mg_next_basis(const double* __restrict__ w, const double* __restrict__ hn2,
-                              const int* __restrict__ active, int64_t n, int64_t m, double* __restrict__ vnext,
-                              float* __restrict__ v32) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= n * m) return;
-    const int64_t c = idx % m;
-    const double s = active[c] ? 1.0 / sqrt(hn2[c]) : 0.0;
-    const double re = w[2 * idx] * s, im = w[2 * idx + 1] * s;
-    vnext[2 * idx] = re;
-    vnext[2 * idx + 1] = im;
-    v32[2 * idx] = (float)re;
-    v32[2 * idx + 1] = (float)im;
+// dst[k][c] = scale[c] src[k][c] for k < the column's rows, 0 beyond: the next basis vector
+// (src = w) and the start of a cycle (src = dst = V_0).
+__global__ void mg_scale_cols(const float2* src, const float* __restrict__ scale, const int* __restrict__ crow,
+                              int64_t n, int64_t m, float2* dst) {
+    const int64_t c = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    if (c >= m) return;
+    const int64_t nr = rows_of(crow, c, n);
+    const float s = scale[c];
+    for (int64_t k = blockIdx.y * blockDim.y + threadIdx.y; k < n; k += (int64_t)gridDim.y * blockDim.y) {
+        const float2 v = src[k * m + c];
+        dst[k * m + c] = k < nr ? make_float2(v.x * s, v.y * s) : make_float2(0.f, 0.f);
+    }
 }
 
-// Start of a cycle: V_0 = R / beta, g = (beta, 0, ..), columns below tol inactive.
-__global__ void mg_start(double* __restrict__ V0, float* __restrict__ v32, const double* __restrict__ beta2,
-                         const double* __restrict__ bnorm, int64_t n, int64_t m, double tol, int* __restrict__ active) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= n * m) return;
-    const int64_t c = idx % m;
-    const double beta = sqrt(beta2[c]);
-    const bool act = beta / bnorm[c] > tol;
-    const double s = act ? 1.0 / beta : 0.0;
-    const double re = V0[2 * idx] * s, im = V0[2 * idx + 1] * s;
-    V0[2 * idx] = re;
-    V0[2 * idx + 1] = im;
-    v32[2 * idx] = (float)re;
-    v32[2 * idx + 1] = (float)im;
-    if (idx < m) active[idx] = act ? 1 : 0;
+// column c of mesh i (nc columns each) has E_i rows
+// (padding columns c >= m have no rows)
+__global__ void mg_column_rows(const int64_t* __restrict__ desc, int64_t m, int64_t mp, int nc,
+                               int* __restrict__ crow) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < mp) crow[c] = c < m ? (int)desc[6 * (c / nc) + 2] : 0;
 }
 
+// Start of a cycle, per column: g = (beta, 0, ..), active = beta / |b| > tol, scale = 1 / beta.
 __global__ void mg_init_g(const double* __restrict__ beta2, const double* __restrict__ bnorm, int r, int64_t m,
-                          double tol, double* __restrict__ g, int* __restrict__ jend, int* __restrict__ count) {
+                          double tol, double* __restrict__ g, int* __restrict__ jend, int* __restrict__ count,
+                          int* __restrict__ active, float* __restrict__ scale) {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m) return;
     for (int i = 0; i <= r; ++i) {
@@ -305,52 +560,40 @@ __global__ void mg_init_g(const double* __restrict__ beta2, const double* __rest
     const double beta = sqrt(beta2[c]);
     g[2 * c] = beta;
     jend[c] = 0;
-    if (beta / bnorm[c] > tol) atomicAdd(count, 1);
+    const bool act = beta / bnorm[c] > tol;
+    active[c] = act ? 1 : 0;
+    scale[c] = act ? (float)(1.0 / beta) : 0.f;
+    if (act) atomicAdd(count, 1);
 }
 
-// back substitution per column (upper-triangular jend x jend), then y into yv
-__global__ void mg_backsolve(const double* __restrict__ H, const double* __restrict__ g, const int* __restrict__ jend,
-                             int r, int64_t m, double* __restrict__ yv) {
+// back substitution per column (upper-triangular jend x jend), then y into yv.  One warp per
+// block; the solution being built stays in shared memory ([r][32] complex128).
+__global__ void __launch_bounds__(32) mg_backsolve(const double* __restrict__ H, const double* __restrict__ g,
+                                                   const int* __restrict__ jend, int r, int64_t m,
+                                                   double* __restrict__ yv) {
+    extern __shared__ double2 s_y[];
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m) return;
     const int k = jend[c];
-    for (int i = r - 1; i >= k; --i) {
-        yv[2 * ((int64_t)i * m + c)] = 0.0;
-        yv[2 * ((int64_t)i * m + c) + 1] = 0.0;
-    }
+    double2* y = s_y + threadIdx.x;  // y[q * 32]
     for (int i = k - 1; i >= 0; --i) {
         double ar = g[2 * ((int64_t)i * m + c)], ai = g[2 * ((int64_t)i * m + c) + 1];
         for (int q = i + 1; q < k; ++q) {
             const double hr = H[2 * (((int64_t)i * r + q) * m + c)], hi = H[2 * (((int64_t)i * r + q) * m + c) + 1];
-            const double yr = yv[2 * ((int64_t)q * m + c)], yi = yv[2 * ((int64_t)q * m + c) + 1];
-            ar -= hr * yr - hi * yi;
-            ai -= hr * yi + hi * yr;
+            const double2 yq = y[q * 32];
+            ar -= hr * yq.x - hi * yq.y;
+            ai -= hr * yq.y + hi * yq.x;
         }
         const double dr = H[2 * (((int64_t)i * r + i) * m + c)], di = H[2 * (((int64_t)i * r + i) * m + c) + 1];
         const double den = dr * dr + di * di;
-        const double yr = den > 0.0 ? (ar * dr + ai * di) / den : 0.0;
-        const double yi = den > 0.0 ? (ai * dr - ar * di) / den : 0.0;
-        yv[2 * ((int64_t)i * m + c)] = yr;
-        yv[2 * ((int64_t)i * m + c) + 1] = yi;
+        y[i * 32] = den > 0.0 ? make_double2((ar * dr + ai * di) / den, (ai * dr - ar * di) / den)
+                              : make_double2(0.0, 0.0);
     }
-}
-
-// X += sum_i V_i y_i (per column)
-__global__ void mg_update(const double* __restrict__ V, const double* __restrict__ yv, int64_t n, int64_t m, int nb,
-                          double* __restrict__ x) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= n * m) return;
-    const int64_t c = idx % m;
-    double xr = x[2 * idx], xi = x[2 * idx + 1];
-#pragma unroll 4
-    for (int i = 0; i < nb; ++i) {
-        const double yr = yv[2 * ((int64_t)i * m + c)], yi = yv[2 * ((int64_t)i * m + c) + 1];
-        const double vr = V[2 * ((int64_t)i * n * m + idx)], vi = V[2 * ((int64_t)i * n * m + idx) + 1];
-        xr += yr * vr - yi * vi;
-        xi += yr * vi + yi * vr;
+    for (int i = 0; i < r; ++i) {
+        const double2 v = i < k ? y[i * 32] : make_double2(0.0, 0.0);
+        yv[2 * ((int64_t)i * m + c)] = v.x;
+        yv[2 * ((int64_t)i * m + c) + 1] = v.y;
     }
-    x[2 * idx] = xr;
-    x[2 * idx + 1] = xi;
 }
 
 // ---- block-diagonal product (many meshes) ------------------------------------------------
@@ -458,60 +701,117 @@ static int mg_sync(cudaStream_t s, const char* what) {
     return check_launch(what);
 }
 
-// The lockstep driver.  prod(v32, y32, stream) computes Y = Z V for the [n, m] complex64 blocks.
+int tmap_encode(CUtensorMap* map, CUtensorMapDataType type, int rank, const void* ptr, const uint64_t* dims,
+                const uint64_t* strides, const uint32_t* box, CUtensorMapSwizzle swizzle);
+
+// Tensor maps of the streamed kernels: the basis (mp, n, r+1) and one [n, mp] matrix.
+static int gs_maps(GsMaps* g, const float2* V, const float2* src, int64_t n, int64_t mp, int r) {
+    const uint64_t dv[3] = {(uint64_t)mp, (uint64_t)n, (uint64_t)(r + 1)};
+    const uint64_t sv[2] = {(uint64_t)mp * 8, (uint64_t)n * mp * 8};
+    const uint32_t bv[3] = {16, (uint32_t)kGsRows, 1};
+    int rc = tmap_encode(&g->v, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, V, dv, sv, bv, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (rc) return rc;
+    return tmap_encode(&g->src, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, src, dv, sv, bv, CU_TENSOR_MAP_SWIZZLE_128B);
+}
+
+// The lockstep driver.  prod(v, y, stream) computes Y = Z V for [n, mp] complex64 blocks
+// (mp = m rounded up to even; the padding column has b = 0 and stays inactive).
+// desc / nc (optional): block-diagonal layout, column c of mesh c / nc has desc[.][2] rows.
 // With use_graph, the r Arnoldi steps of a cycle are captured once as a CUDA graph and
 // replayed every cycle (no host synchronisation inside a cycle; a cycle always runs its r
 // steps, columns that converged early are inactive).
 template <typename Prod>
 static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int64_t m, int r, int max_iters,
-                          double tol, size_t prod_ws, void* workspace, size_t ws_bytes, bool use_graph,
-                          int64_t* iters_out, int64_t* cycles_out, double* max_relres_out, int* status_out,
-                          cudaStream_t s) {
+                          double tol, size_t prod_ws, const int64_t* desc, int nc, void* workspace, size_t ws_bytes,
+                          bool use_graph, int64_t* iters_out, int64_t* cycles_out, double* max_relres_out,
+                          int* status_out, cudaStream_t s) {
     if (n <= 0 || m <= 0) return set_error(MB_ERR_ARG, "n and m must be > 0");
+    if (((uintptr_t)x | (uintptr_t)b) & 15) return set_error(MB_ERR_ARG, "b and x must be 16-byte aligned");
     if (r < 1 || r > kMgMaxRestart) return set_error(MB_ERR_ARG, "restart must be in [1, %d]", kMgMaxRestart);
     if (max_iters < 1 || !(tol > 0)) return set_error(MB_ERR_ARG, "bad max_iters / tol");
+    if (n > (1ll << 30)) return set_error(MB_ERR_SIZE, "gmres: too many rows");
+    const int64_t mp = padded_width(m);
     MgWork W;
-    if (ws_bytes < mg_layout(n, m, r, prod_ws, nullptr, &W)) return set_error(MB_ERR_ARG, "workspace too small");
-    mg_layout(n, m, r, prod_ws, workspace, &W);
-    const int64_t nm = n * m;
-    const unsigned eb = (unsigned)((nm + 255) / 256);
-    const unsigned cb = (unsigned)((m + 127) / 128);
+    if (ws_bytes < mg_layout(n, mp, r, prod_ws, nullptr, &W)) return set_error(MB_ERR_ARG, "workspace too small");
+    mg_layout(n, mp, r, prod_ws, workspace, &W);
+    const int64_t nm = n * mp;
+    const unsigned cb = (unsigned)((mp + 31) / 32);  // per-column FP64 kernels: one warp per block
+    const unsigned colb = (unsigned)((mp + 31) / 32);
     const dim3 rblk(32, 8);
-    // row blocks per column group: enough blocks to fill the GPU, few FP64 atomics per column
-    const unsigned ky = (unsigned)std::max<int64_t>(
-        1, std::min<int64_t>((n + 63) / 64, (152 * 16 + (m + 31) / 32 - 1) / ((m + 31) / 32)));
-    const dim3 rgrid((unsigned)((m + 31) / 32), ky);
-    std::vector<double> hb(m);
+    int sms = 152;
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    // row blocks per column group for the reductions: enough blocks to fill the GPU
+    const unsigned ky = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 63) / 64, (sms * 16 + colb - 1) / colb));
+    const dim3 rgrid(colb, ky);
+    // streamed Gram-Schmidt: tensor maps and persistent grids (as many blocks as stay resident)
+    constexpr int kS = 4;
+    auto dots_k = mg_dots<kS>;
+    auto comb_k = mg_combine<kS, 0>;
+    auto combn_k = mg_combine<kS, 1>;
+    auto upd_k = mg_combine<kS, 2>;
+    GsMaps maps_y, maps_w;
     int rc;
+    if ((rc = gs_maps(&maps_y, W.V, W.y32, n, mp, r)) || (rc = gs_maps(&maps_w, W.V, W.w, n, mp, r))) return rc;
+    const size_t dots_max = gs_smem<kS>((size_t)(r + 1) * 32 * 16), comb_max = gs_smem<kS>((size_t)(r + 1) * 32 * 8);
+    cudaFuncSetAttribute(dots_k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dots_max);
+    for (auto k : {comb_k, combn_k, upd_k})
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)comb_max);
+    cudaFuncSetAttribute(mg_backsolve, cudaFuncAttributeMaxDynamicSharedMemorySize, r * 32 * 16);
+    int dots_per_sm = 0, comb_per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&dots_per_sm, dots_k, kGsThreads, dots_max);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&comb_per_sm, combn_k, kGsThreads, comb_max);
+    const int64_t tiles = (n + kGsRows - 1) / kGsRows;
+    const dim3 dgrid(colb, (unsigned)std::max<int64_t>(
+                               1, std::min<int64_t>(tiles, ((int64_t)std::max(dots_per_sm, 1) * sms) / colb)));
+    const dim3 cgrid(colb, (unsigned)std::max<int64_t>(
+                               1, std::min<int64_t>(tiles, ((int64_t)std::max(comb_per_sm, 1) * sms) / colb)));
+    const int* crow = nullptr;
+    if (desc) {
+        if (nc < 1 || m % nc) return set_error(MB_ERR_ARG, "gmres: m must be a multiple of nc");
+        mg_column_rows<<<cb, 32, 0, s>>>(desc, m, mp, nc, W.crow);
+        crow = W.crow;
+    }
+    std::vector<double> hb(mp);
     cudaMemsetAsync(W.y32, 0, 8 * (size_t)nm, s);  // rows a product does not write stay 0
-    cudaMemsetAsync(W.bnorm, 0, 8 * m, s);
-    mg_colnorm2<<<rgrid, rblk, 0, s>>>(b, n, m, W.bnorm);
-    cudaMemcpyAsync(hb.data(), W.bnorm, 8 * m, cudaMemcpyDeviceToHost, s);
+    cudaMemsetAsync(W.bnorm, 0, 8 * mp, s);
+    cudaMemsetAsync(W.status, 0, 16, s);
+    mg_colnorm2<<<rgrid, rblk, 0, s>>>(reinterpret_cast<const double2*>(b), n, m, W.bnorm);
+    cudaMemcpyAsync(hb.data(), W.bnorm, 8 * mp, cudaMemcpyDeviceToHost, s);
     if ((rc = mg_sync(s, "gmres_multi |b|"))) return rc;
     for (auto& v : hb) v = v > 0 ? std::sqrt(v) : 1.0;
-    cudaMemcpyAsync(W.bnorm, hb.data(), 8 * m, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(W.bnorm, hb.data(), 8 * mp, cudaMemcpyHostToDevice, s);
     int64_t iters = 0, cycles = 0;
     double worst = 0.0;
     int status = 1;
-    std::vector<double> hbeta(m);
+    std::vector<double> hbeta(mp);
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaStream_t cap = nullptr;  // capture needs a stream other than the legacy default stream
     auto step = [&](int j, cudaStream_t st) -> int {
         int e;
-        if ((e = prod(W.v32, W.y32, st))) return e;
-        mg_widen<<<eb, 256, 0, st>>>(W.y32, 2 * nm, W.w);
-        for (int pass = 0; pass < 2; ++pass) {
-            cudaMemsetAsync(W.hc, 0, 16 * (size_t)(j + 1) * m, st);
-            mg_dots<<<dim3((unsigned)((m + 31) / 32), ky, (unsigned)(j + 1)), rblk, 0, st>>>(W.V, W.w, n, m, W.hc);
-            mg_subtract<<<eb, 256, 0, st>>>(W.V, W.hc, n, m, j + 1, W.w);
-            mg_accum_h<<<(unsigned)(((j + 1) * m + 255) / 256), 256, 0, st>>>(W.hc, j + 1, j, r, m, W.H);
-        }
-        cudaMemsetAsync(W.hn, 0, 8 * m, st);
-        mg_colnorm2<<<rgrid, rblk, 0, st>>>(W.w, n, m, W.hn);
+        const int nb = j + 1;
+        const size_t dsm = gs_smem<kS>((size_t)nb * 32 * 16), csm = gs_smem<kS>((size_t)nb * 32 * 8);
+        if ((e = prod(reinterpret_cast<const float*>(W.V + (size_t)j * nm), reinterpret_cast<float*>(W.y32), st)))
+            return e;
+        // CGS2: pass 1 projects the product output y into w, pass 2 re-orthogonalises w and
+        // accumulates |w|^2
+        cudaMemsetAsync(W.hc, 0, 16 * (size_t)nb * mp, st);
+        dots_k<<<dgrid, kGsThreads, dsm, st>>>(maps_y, W.y32, n, mp, nb, W.hc, W.status);
+        comb_k<<<cgrid, kGsThreads, csm, st>>>(maps_y, W.hc, n, mp, mp, nb, -1.f, W.w, nullptr, W.status);
+        mg_accum_h<<<(unsigned)((nb * mp + 255) / 256), 256, 0, st>>>(W.hc, nb, j, r, mp, W.H);
+        cudaMemsetAsync(W.hc, 0, 16 * (size_t)nb * mp, st);
+        dots_k<<<dgrid, kGsThreads, dsm, st>>>(maps_w, W.w, n, mp, nb, W.hc, W.status);
+        cudaMemsetAsync(W.hn, 0, 8 * mp, st);
+        combn_k<<<cgrid, kGsThreads, csm, st>>>(maps_w, W.hc, n, mp, mp, nb, -1.f, W.w, W.hn, W.status);
+        mg_accum_h<<<(unsigned)((nb * mp + 255) / 256), 256, 0, st>>>(W.hc, nb, j, r, mp, W.H);
         cudaMemsetAsync(W.count, 0, 4, st);
-        mg_givens<<<cb, 128, 0, st>>>(W.H, W.cs, W.sn, W.g, W.hn, W.bnorm, j, r, m, tol, W.active, W.jend, W.count);
-        mg_next_basis<<<eb, 256, 0, st>>>(W.w, W.hn, W.active, n, m, W.V + 2 * (size_t)(j + 1) * nm, W.v32);
+        mg_givens<<<cb, 32, 0, st>>>(W.H, W.cs, W.sn, W.g, W.hn, W.bnorm, j, r, mp, tol, W.active, W.jend, W.count,
+                                     W.scale);
+        mg_scale_cols<<<rgrid, rblk, 0, st>>>(W.w, W.scale, crow, n, mp, W.V + (size_t)(j + 1) * nm);
         return check_launch("gmres_multi step");
     };
     auto cleanup = [&]() {
@@ -519,13 +819,22 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
         if (graph) cudaGraphDestroy(graph);
         if (cap) cudaStreamDestroy(cap);
     };
+    auto check_status = [&]() -> int {
+        int hs = 0;
+        cudaMemcpyAsync(&hs, W.status, 4, cudaMemcpyDeviceToHost, s);
+        int e = mg_sync(s, "gmres_multi status");
+        if (e) return e;
+        if (hs) return set_error(MB_ERR_CUDA, "gmres_multi: streamed kernel wait timed out (code %d)", hs);
+        return MB_OK;
+    };
     while (true) {
-        // residual of the current iterate through the same product
-        mg_to_c64<<<eb, 256, 0, s>>>(x, 2 * nm, W.v32);
-        if ((rc = prod(W.v32, W.y32, s))) return cleanup(), rc;
-        cudaMemsetAsync(W.beta, 0, 8 * m, s);
-        mg_residual<<<rgrid, rblk, 0, s>>>(b, W.y32, n, m, W.V, W.beta);
-        cudaMemcpyAsync(hbeta.data(), W.beta, 8 * m, cudaMemcpyDeviceToHost, s);
+        // residual of the current iterate through the same product (w holds complex64 X)
+        mg_to_c64<<<rgrid, rblk, 0, s>>>(reinterpret_cast<const double2*>(x), n, m, mp, W.w);
+        if ((rc = prod(reinterpret_cast<const float*>(W.w), reinterpret_cast<float*>(W.y32), s)))
+            return cleanup(), rc;
+        cudaMemsetAsync(W.beta, 0, 8 * mp, s);
+        mg_residual<<<rgrid, rblk, 0, s>>>(reinterpret_cast<const double2*>(b), W.y32, n, m, mp, W.V, W.beta);
+        cudaMemcpyAsync(hbeta.data(), W.beta, 8 * mp, cudaMemcpyDeviceToHost, s);
         if ((rc = mg_sync(s, "gmres_multi residual"))) return cleanup(), rc;
         worst = 0.0;
         for (int64_t c = 0; c < m; ++c) worst = std::max(worst, std::sqrt(hbeta[c]) / hb[c]);
@@ -536,9 +845,9 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
         if (iters >= max_iters) break;
         ++cycles;
         cudaMemsetAsync(W.count, 0, 16, s);
-        mg_start<<<eb, 256, 0, s>>>(W.V, W.v32, W.beta, W.bnorm, n, m, tol, W.active);
-        mg_init_g<<<cb, 128, 0, s>>>(W.beta, W.bnorm, r, m, tol, W.g, W.jend, W.count);
-        cudaMemsetAsync(W.H, 0, 16 * (size_t)(r + 1) * r * m, s);
+        mg_init_g<<<cb, 32, 0, s>>>(W.beta, W.bnorm, r, mp, tol, W.g, W.jend, W.count, W.active, W.scale);
+        mg_scale_cols<<<rgrid, rblk, 0, s>>>(W.V, W.scale, crow, n, mp, W.V);
+        cudaMemsetAsync(W.H, 0, 16 * (size_t)(r + 1) * r * mp, s);
         int j = 0;
         if (use_graph) {
             if (!exec) {
@@ -569,9 +878,11 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
                 }
             }
         }
-        mg_backsolve<<<cb, 128, 0, s>>>(W.H, W.g, W.jend, r, m, W.yv);
-        mg_update<<<eb, 256, 0, s>>>(W.V, W.yv, n, m, j, x);
-        if ((rc = mg_sync(s, "gmres_multi update"))) return cleanup(), rc;
+        mg_backsolve<<<cb, 32, (size_t)r * 32 * 16, s>>>(W.H, W.g, W.jend, r, mp, W.yv);
+        if (j > 0)
+            upd_k<<<cgrid, kGsThreads, gs_smem<kS>((size_t)j * 32 * 8), s>>>(maps_w, W.yv, n, mp, m, j, 1.f, x,
+                                                                           nullptr, W.status);
+        if ((rc = check_status())) return cleanup(), rc;
     }
     cleanup();
     if (iters_out) *iters_out = iters;
@@ -584,16 +895,17 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
 int gmres_multi(const float* z_hi, const float* z_lo, int64_t n, const double* b, double* x, int64_t m, int r,
                 int max_iters, double tol, void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out,
                 double* max_relres_out, int* status_out, cudaStream_t s) {
-    const size_t gws = cgemm_workspace_bytes(n, m);
+    const int64_t mp = padded_width(m);
+    const size_t gws = cgemm_workspace_bytes(n, mp);
     MgWork W;
-    if (ws_bytes < mg_layout(n, m, r, gws, nullptr, &W)) return set_error(MB_ERR_ARG, "workspace too small");
-    mg_layout(n, m, r, gws, workspace, &W);
+    if (ws_bytes < mg_layout(n, mp, r, gws, nullptr, &W)) return set_error(MB_ERR_ARG, "workspace too small");
+    mg_layout(n, mp, r, gws, workspace, &W);
     void* gemm_ws = W.gemm_ws;
     auto prod = [&](const float* v32, float* y32, cudaStream_t st) {
-        return cgemm_tf32x3(z_hi, z_lo, n, v32, m, y32, gemm_ws, gws, st);
+        return cgemm_tf32x3(z_hi, z_lo, n, v32, mp, y32, gemm_ws, gws, st);
     };
-    return gmres_lockstep(prod, n, b, x, m, r, max_iters, tol, gws, workspace, ws_bytes, false, iters_out,
-                          cycles_out, max_relres_out, status_out, s);
+    return gmres_lockstep(prod, n, b, x, m, r, max_iters, tol, gws, nullptr, 1, workspace, ws_bytes, false,
+                          iters_out, cycles_out, max_relres_out, status_out, s);
 }
 
 // Many meshes, each with its own Z_i and nc right-hand sides: the block-diagonal system on
@@ -602,12 +914,12 @@ int gmres_blockdiag(const float* z, const int64_t* desc, const int64_t* goff, in
                     int rows_per_warp, int nc, int64_t n_rows, const double* b, double* x, int r, int max_iters,
                     double tol, bool use_graph, void* workspace, size_t ws_bytes, int64_t* iters_out,
                     int64_t* cycles_out, double* max_relres_out, int* status_out, cudaStream_t s) {
-    const int64_t m = (int64_t)n_mesh * nc;
+    const int64_t m = (int64_t)n_mesh * nc, mp = padded_width(m);
     auto prod = [&](const float* v32, float* y32, cudaStream_t st) {
-        return blockdiag_matvec(z, desc, goff, n_mesh, total_warps, v32, m, nc, rows_per_warp, y32, st);
+        return blockdiag_matvec(z, desc, goff, n_mesh, total_warps, v32, mp, nc, rows_per_warp, y32, st);
     };
-    return gmres_lockstep(prod, n_rows, b, x, m, r, max_iters, tol, 0, workspace, ws_bytes, use_graph, iters_out,
-                          cycles_out, max_relres_out, status_out, s);
+    return gmres_lockstep(prod, n_rows, b, x, m, r, max_iters, tol, 0, desc, nc, workspace, ws_bytes, use_graph,
+                          iters_out, cycles_out, max_relres_out, status_out, s);
 }
 
 }  // namespace mb

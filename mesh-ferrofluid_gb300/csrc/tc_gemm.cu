@@ -337,6 +337,27 @@ static EncodeTiledFn encode_fn() {
     return fn;
 }
 
+// General tiled tensor map (rank <= 5): dims / box innermost first, strides in bytes for
+// dimensions 1 .. rank-1.
+int tmap_encode(CUtensorMap* map, CUtensorMapDataType type, int rank, const void* ptr, const uint64_t* dims,
+                const uint64_t* strides, const uint32_t* box, CUtensorMapSwizzle swizzle) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return set_error(MB_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    cuuint64_t d[5], st[4];
+    cuuint32_t b[5], e[5];
+    for (int i = 0; i < rank; ++i) {
+        d[i] = dims[i];
+        b[i] = box[i];
+        e[i] = 1;
+        if (i + 1 < rank) st[i] = strides[i];
+    }
+    const CUresult r = fn(map, type, (cuuint32_t)rank, const_cast<void*>(ptr), d, st, b, e,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(MB_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return MB_OK;
+}
+
 // rows x cols fp32 row-major matrix, box of box_rows x 32 columns, 128-byte swizzle.
 static int make_map(CUtensorMap* m, const float* ptr, int64_t rows, int64_t cols, int box_rows) {
     EncodeTiledFn fn = encode_fn();
