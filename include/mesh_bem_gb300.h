@@ -307,6 +307,8 @@ int mb_gmres_multi_c64(const float* z_hi, const float* z_lo, int64_t n, const do
  * (first face, faces F_i, edges E_i, offset of Z_i in the flat block-diagonal array in
  * complex entries, first block of the mesh in the regular launch = sum over earlier meshes
  * of F_j ceil(F_j / 128), first right-hand-side column); ks [n_mesh] the wavenumbers.
+ * Z_i is row-major with the even row pitch P_i = E_i + (E_i & 1) (the offsets are sums of
+ * E_j P_j); a padding entry is never written.
  * mb_mom_sym_zmat_batched_*: the symmetric-rule EFIE (as mb_mom_sym_zmat_rwg_* +
  * mb_mom_sym_near_*) of every mesh in one launch of each kernel, accumulated into the flat
  * array (caller zeroes); total_blocks = the block count above; near_pairs [n_near, 2]
@@ -343,9 +345,11 @@ int mb_mom_ref_rhs_batched_c64(const float* verts, const int32_t* faces, const f
                                const double* waves, int nrhs, int64_t ld, float* rhs, void* stream);
 
 /* Block-diagonal product over the batch: y[r, c] = sum_l Z_i[r, l] x[l, c] for the nc
- * columns of mesh i (x, y complex64 [max E_i, ld], ld = n_mesh * nc); goff [n_mesh + 1] =
- * first warp of each mesh with rows_per_warp (1, 2, 4 or 8; 8 for nc <= 4) rows per warp,
- * goff[n_mesh] = total_warps.  nc in {1, 2, 4, 8}.  Rows beyond E_i are not written. */
+ * columns of mesh i (x, y complex64 [max E_i, ld], ld >= n_mesh * nc); goff [n_mesh + 1] =
+ * first work unit of each mesh with rows_per_warp rows per unit, goff[n_mesh] =
+ * total_warps: 1, 2, 4 or 8 (8 for nc <= 4) rows per warp reading Z directly, or 32 rows
+ * per block with Z streamed through shared memory by bulk copies (z 16-byte aligned).
+ * nc in {1, 2, 4, 8}.  Rows beyond E_i are not written. */
 int mb_blockdiag_matvec_c64(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh,
                             int64_t total_warps, const float* x, int64_t ld, int nc, int rows_per_warp,
                             float* y, void* stream);

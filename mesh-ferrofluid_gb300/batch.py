@@ -13,8 +13,12 @@ of meshes of uneven size (and wavenumber) into one vertex / face array and runs
   into a padded block [max E_i, n_mesh * nc];
 * GMRES on every (mesh, wave) column in lockstep with the block-diagonal product
   (``mb_gmres_blockdiag_c64``), each restart cycle replayed from a captured CUDA graph; the
-  product's tile shape (rows per warp) is picked by timing the candidates once
-  (``autotune``).
+  product's tile shape (1, 2, 4 or 8 rows per warp reading Z directly, or 32 rows per block
+  with Z streamed through shared memory by bulk copies) is picked by timing the candidates
+  once (``autotune``).
+
+Each Z_i is stored row-major with its row pitch rounded up to even, so every row starts on a
+16-byte boundary.
 
 All data live on one CUDA device; there is no CPU path.
 """
@@ -62,7 +66,7 @@ class MeshBatch:
             self.n_edges.append(ne)
             v_off += v.shape[0]
             f_off += nf
-            z_off += ne * ne
+            z_off += ne * (ne + (ne & 1))  # rows padded to an even pitch (16-byte aligned rows)
             blk += nf * ((nf + 127) // 128)
         self.n_mesh = len(meshes)
         self.verts = torch.cat(verts).contiguous()
@@ -111,9 +115,11 @@ class MeshBatch:
         return self._goff[rows]
 
     def z_block(self, z_flat: torch.Tensor, i: int) -> torch.Tensor:
-        """View of mesh i's impedance matrix [E_i, E_i] in the flat array."""
+        """View of mesh i's impedance matrix [E_i, E_i] in the flat array (row pitch E_i
+        rounded up to even)."""
         o, e = int(self._desc_np[i, 3]), self.n_edges[i]
-        return z_flat[o:o + e * e].view(e, e)
+        p = e + (e & 1)
+        return z_flat[o:o + e * p].view(e, p)[:, :e]
 
     def column(self, X: torch.Tensor, i: int, r: int) -> torch.Tensor:
         """Mesh i, right-hand side r of a padded [n_rows, n_mesh * nc] block."""
@@ -172,8 +178,8 @@ class MeshBatch:
                   int(goff[-1]), _lib.ptr(X), X.shape[1], self.nc, rows, _lib.ptr(out), _lib.stream_of(X))
         return out
 
-    def autotune(self, z_flat: torch.Tensor, candidates=(1, 2, 4, 8), reps: int = 3) -> int:
-        """Pick the block-diagonal product's rows per warp by timing each candidate."""
+    def autotune(self, z_flat: torch.Tensor, candidates=(1, 2, 4, 8, 32), reps: int = 3) -> int:
+        """Pick the block-diagonal product's tile (rows per work unit) by timing each candidate."""
         X = torch.randn(self.n_rows, self.n_mesh * self.nc, dtype=torch.complex64, device=self.device)
         Y = torch.zeros_like(X)
         best, best_t = None, None

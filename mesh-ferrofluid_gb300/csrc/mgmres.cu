@@ -94,9 +94,11 @@ size_t gmres_multi_workspace_bytes(int64_t n, int64_t m, int r) {
     return mg_layout(n, padded_width(m), r, cgemm_workspace_bytes(n, padded_width(m)), nullptr, &W);
 }
 
+// (the product's slot holds the per-mesh tensor maps of the streamed variant: one per column
+// is more than enough)
 size_t gmres_blockdiag_workspace_bytes(int64_t n, int64_t m, int r) {
     MgWork W;
-    return mg_layout(n, padded_width(m), r, 0, nullptr, &W);
+    return mg_layout(n, padded_width(m), r, 128 * (size_t)std::max<int64_t>(m, 1), nullptr, &W);
 }
 
 // ---- kernels ---------------------------------------------------------------------------
@@ -598,10 +600,12 @@ __global__ void __launch_bounds__(32) mg_backsolve(const double* __restrict__ H,
 
 // ---- block-diagonal product (many meshes) ------------------------------------------------
 // desc[i] = (face offset, faces, edges E_i, offset of Z_i in the flat array (complex entries),
-// -, first right-hand-side column); goff[i] = first warp of mesh i (each warp owns ROWS rows,
-// goff[n_mesh] = total warps).  y[r, col + c] = sum_l Z_i[r, l] x[l, col + c] for the NC
-// columns of mesh i; x, y: [rows_max, ld] interleaved complex64; FP32 products, FP32 lane
-// sums, warp reduction.  Rows of the padded block beyond E_i are never written.
+// -, first right-hand-side column); Z_i is stored row-major with the even row pitch
+// P_i = E_i + (E_i & 1), so every row starts on a 16-byte boundary.  goff[i] = first work
+// unit of mesh i (a unit owns ROWS rows), goff[n_mesh] = total units.
+// y[r, col + c] = sum_l Z_i[r, l] x[l, col + c] for the NC columns of mesh i; x, y:
+// [rows_max, ld] interleaved complex64; FP32 products and sums.  Rows of the padded block
+// beyond E_i are never written.
 __device__ __forceinline__ int seg_of(const int64_t* __restrict__ off, int n, int64_t v) {
     int lo = 0, hi = n - 1;
     while (lo < hi) {
@@ -623,6 +627,7 @@ __global__ void __launch_bounds__(256) blockdiag_matvec_kernel(const float* __re
     if (w >= __ldg(goff + n_mesh)) return;
     const int i = seg_of(goff, n_mesh, w);
     const int64_t E = __ldg(desc + 6 * i + 2), zo = __ldg(desc + 6 * i + 3), co = __ldg(desc + 6 * i + 5);
+    const int64_t P = E + (E & 1);
     const int64_t r0 = (w - __ldg(goff + i)) * ROWS;
     const float2* zc = reinterpret_cast<const float2*>(z) + zo;
     const float2* xc = reinterpret_cast<const float2*>(x);
@@ -651,7 +656,7 @@ __global__ void __launch_bounds__(256) blockdiag_matvec_kernel(const float* __re
 #pragma unroll
         for (int q = 0; q < ROWS; ++q) {
             if (r0 + q < E) {
-                const float2 a = __ldcs(zc + (r0 + q) * E + l);
+                const float2 a = __ldcs(zc + (r0 + q) * P + l);
 #pragma unroll
                 for (int c = 0; c < NC; ++c) {
                     ar[q][c] = fmaf(a.x, xv[c].x, fmaf(-a.y, xv[c].y, ar[q][c]));
@@ -675,9 +680,231 @@ __global__ void __launch_bounds__(256) blockdiag_matvec_kernel(const float* __re
         }
 }
 
+// Streamed variant (ROWS = 32): a block takes units u = blockIdx.x + j gridDim.x; per unit and
+// chunk of 64 columns a producer warp loads, by TMA, the 32 x 64 tile of Z_i (one tensor map
+// per mesh, in global memory: rows of pitch P_i, zero fill beyond E_i) and the 64 x 8 tile
+// of x at the mesh's columns (64-byte swizzle) into a kBdStages ring; 8 consumer warps own
+// 4 rows each and lanes stride over the chunk's columns, both operands from shared memory.
+// Waits are bounded (a time-out sets *status and ends the block).
+constexpr int kBdRows = 32, kBdCols = 64, kBdZBytes = kBdRows * kBdCols * 8, kBdXBytes = kBdCols * 64;
+constexpr int kBdStage = kBdZBytes + kBdXBytes, kBdStages = 4;
+constexpr int kBdThreads = 288;
+constexpr size_t kBdSmem = 1024 + (size_t)kBdStages * kBdStage + 16 * kBdStages;
+
+// byte offset of x tile element (row j, byte column cb) under the 64-byte swizzle
+__device__ __forceinline__ uint32_t bd_xoff(int j, int cb) {
+    return (uint32_t)(j * 64 + ((((cb >> 4) ^ (j >> 1)) & 3) << 4) + (cb & 15));
+}
+
+template <int NC>
+__global__ void __launch_bounds__(kBdThreads) blockdiag_stream_kernel(const CUtensorMap* __restrict__ zmaps,
+                                                                      const __grid_constant__ CUtensorMap xmap,
+                                                                      const int64_t* __restrict__ desc,
+                                                                      const int64_t* __restrict__ uoff, int n_mesh,
+                                                                      int64_t ld, float* __restrict__ y,
+                                                                      int* __restrict__ status) {
+    extern __shared__ unsigned char bd_raw[];
+    unsigned char* stage =
+        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(bd_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t* full = reinterpret_cast<uint64_t*>(stage + (size_t)kBdStages * kBdStage);
+    uint64_t* empty = full + kBdStages;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t units = __ldg(uoff + n_mesh);
+    if (threadIdx.x == 256) {
+        for (int s = 0; s < kBdStages; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 8);
+        }
+        tc::fence_mbar_init();
+    }
+    __syncthreads();
+    if (warp == 8) {
+        if (lane == 0) {
+            tc::prefetch_tmap(&xmap);
+            int64_t p = 0;
+            bool ok = true;
+            for (int64_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
+                const int i = seg_of(uoff, n_mesh, u);
+                const int64_t E = __ldg(desc + 6 * i + 2), co = __ldg(desc + 6 * i + 5);
+                const int r0 = (int)((u - __ldg(uoff + i)) * kBdRows);
+                const CUtensorMap* zm = zmaps + i;
+                for (int64_t l0 = 0; l0 < E; l0 += kBdCols, ++p) {
+                    const int s = (int)(p % kBdStages);
+                    const int64_t use = p / kBdStages;
+                    if (use > 0 && !tc::mbar_wait(&empty[s], (uint32_t)((use - 1) & 1), kGsBudget, status, 8)) {
+                        ok = false;
+                        break;
+                    }
+                    unsigned char* st = stage + (size_t)s * kBdStage;
+                    tc::mbar_arrive_expect_tx(&full[s], kBdStage);
+                    tc::tma_load_2d(st, zm, &full[s], (int)l0, r0);
+                    tc::tma_load_2d(st + kBdZBytes, &xmap, &full[s], (int)(co & ~1ll), (int)l0);
+                }
+            }
+            for (int s = 0; s < kBdStages; ++s) {
+                const int64_t uses = p > s ? (p - s + kBdStages - 1) / kBdStages : 0;
+                if (uses > 0) tc::mbar_wait(&full[s], (uint32_t)((uses - 1) & 1), kGsBudget, status, 16);
+            }
+        }
+    } else {
+        int64_t p = 0;
+        bool ok = true;
+        for (int64_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
+            const int i = seg_of(uoff, n_mesh, u);
+            const int64_t E = __ldg(desc + 6 * i + 2), co = __ldg(desc + 6 * i + 5);
+            const int64_t r0 = (u - __ldg(uoff + i)) * kBdRows + warp * 4;
+            const int cb0 = (int)(co & 1) * 8;  // byte column of the mesh's first column in the x tile
+            float ar[4][NC], ai[4][NC];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int c = 0; c < NC; ++c) ar[q][c] = ai[q][c] = 0.f;
+            for (int64_t l0 = 0; l0 < E; l0 += kBdCols, ++p) {
+                const int s = (int)(p % kBdStages);
+                if (!tc::mbar_wait(&full[s], (uint32_t)((p / kBdStages) & 1), kGsBudget, status, 32)) {
+                    ok = false;
+                    break;
+                }
+                const unsigned char* st = stage + (size_t)s * kBdStage;
+                const float2* zt = reinterpret_cast<const float2*>(st);
+                const unsigned char* xt = st + kBdZBytes;
+#pragma unroll
+                for (int t = 0; t < kBdCols / 32; ++t) {
+                    const int j = lane + 32 * t;
+                    if (l0 + j >= E) break;
+                    float2 xv[NC];
+                    if (NC % 2 == 0 && cb0 == 0) {
+#pragma unroll
+                        for (int c = 0; c < NC / 2; ++c) {
+                            const float4 v = *reinterpret_cast<const float4*>(xt + bd_xoff(j, 16 * c));
+                            xv[2 * c] = make_float2(v.x, v.y);
+                            xv[2 * c + 1] = make_float2(v.z, v.w);
+                        }
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < NC; ++c) xv[c] = *reinterpret_cast<const float2*>(xt + bd_xoff(j, cb0 + 8 * c));
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const float2 a = zt[(warp * 4 + q) * kBdCols + j];
+#pragma unroll
+                        for (int c = 0; c < NC; ++c) {
+                            ar[q][c] = fmaf(a.x, xv[c].x, fmaf(-a.y, xv[c].y, ar[q][c]));
+                            ai[q][c] = fmaf(a.x, xv[c].y, fmaf(a.y, xv[c].x, ai[q][c]));
+                        }
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&empty[s]);
+            }
+            if (!ok) break;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    float vr = ar[q][c], vi = ai[q][c];
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        vr += __shfl_xor_sync(0xffffffffu, vr, o);
+                        vi += __shfl_xor_sync(0xffffffffu, vi, o);
+                    }
+                    if (lane == 0 && r0 + q < E)
+                        reinterpret_cast<float2*>(y)[(r0 + q) * ld + co + c] = make_float2(vr, vi);
+                }
+        }
+    }
+    __syncthreads();
+}
+
+int tmap_encode(CUtensorMap* map, CUtensorMapDataType type, int rank, const void* ptr, const uint64_t* dims,
+                const uint64_t* strides, const uint32_t* box, CUtensorMapSwizzle swizzle);
+
+// Per-mesh tensor maps of the flat block-diagonal array (host desc copy), written to dev.
+static int bd_zmaps(const float* z, const int64_t* desc_h, int n_mesh, CUtensorMap* dev, cudaStream_t s) {
+    std::vector<CUtensorMap> maps((size_t)n_mesh);
+    for (int i = 0; i < n_mesh; ++i) {
+        const int64_t E = desc_h[6 * i + 2], zo = desc_h[6 * i + 3], P = E + (E & 1);
+        if (zo & 1) return set_error(MB_ERR_ARG, "block-diagonal product: Z_%d offset must be even", i);
+        const uint64_t dims[2] = {(uint64_t)P, (uint64_t)E};
+        const uint64_t strides[1] = {(uint64_t)P * 8};
+        const uint32_t box[2] = {(uint32_t)kBdCols, (uint32_t)kBdRows};
+        int rc = tmap_encode(&maps[i], CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, z + 2 * zo, dims, strides, box,
+                             CU_TENSOR_MAP_SWIZZLE_NONE);
+        if (rc) return rc;
+    }
+    cudaError_t e = cudaMemcpyAsync(dev, maps.data(), sizeof(CUtensorMap) * n_mesh, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return set_error(MB_ERR_CUDA, "block-diagonal product: tensor maps: %s", cudaGetErrorString(e));
+    return MB_OK;
+}
+
+static int bd_xmap(CUtensorMap* map, const float* x, int64_t n_rows, int64_t ld) {
+    if (ld & 1) return set_error(MB_ERR_ARG, "block-diagonal product (streamed): ld must be even");
+    const uint64_t dims[2] = {(uint64_t)ld, (uint64_t)n_rows};
+    const uint64_t strides[1] = {(uint64_t)ld * 8};
+    const uint32_t box[2] = {8, (uint32_t)kBdCols};
+    return tmap_encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, x, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_64B);
+}
+
+static int bd_launch(const CUtensorMap* zmaps, const float* x, int64_t n_rows, const int64_t* desc,
+                     const int64_t* goff, int n_mesh, int64_t total_units, int64_t ld, int nc, float* y, int* status,
+                     cudaStream_t s) {
+    CUtensorMap xm;
+    int rc = bd_xmap(&xm, x, n_rows, ld);
+    if (rc) return rc;
+    int sms = 152, dev = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+#define MB_BDS(C)                                                                                               \
+    if (nc == C) {                                                                                              \
+        cudaFuncSetAttribute(blockdiag_stream_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBdSmem); \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, blockdiag_stream_kernel<C>, kBdThreads, kBdSmem);   \
+        const int64_t g = std::max<int64_t>(1, std::min<int64_t>(total_units, (int64_t)std::max(per_sm, 1) * sms)); \
+        blockdiag_stream_kernel<C><<<(unsigned)g, kBdThreads, kBdSmem, s>>>(zmaps, xm, desc, goff, n_mesh, ld, y,  \
+                                                                           status);                             \
+        return check_launch("blockdiag_matvec (streamed)");                                                     \
+    }
+    MB_BDS(1) MB_BDS(2) MB_BDS(4) MB_BDS(8)
+#undef MB_BDS
+    return set_error(MB_ERR_UNSUPPORTED, "block-diagonal product: columns per mesh in {1, 2, 4, 8}");
+}
+
 int blockdiag_matvec(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
                      const float* x, int64_t ld, int nc, int rows, float* y, cudaStream_t s) {
     if (n_mesh <= 0 || total_warps <= 0) return MB_OK;
+    if (rows == kBdRows) {
+        // standalone call: tensor maps and the time-out word in private buffers, checked here
+        if (reinterpret_cast<uintptr_t>(z) & 15) return set_error(MB_ERR_ARG, "z must be 16-byte aligned");
+        static int* own = nullptr;
+        static CUtensorMap* maps = nullptr;
+        static int maps_cap = 0;
+        if (!own && cudaMalloc(&own, 16) != cudaSuccess) {
+            own = nullptr;
+            return set_error(MB_ERR_CUDA, "block-diagonal product: status word");
+        }
+        if (maps_cap < n_mesh) {
+            if (maps) cudaFree(maps);
+            maps = nullptr;
+            maps_cap = 0;
+            if (cudaMalloc(&maps, sizeof(CUtensorMap) * n_mesh) != cudaSuccess)
+                return set_error(MB_ERR_CUDA, "block-diagonal product: tensor map buffer");
+            maps_cap = n_mesh;
+        }
+        std::vector<int64_t> dh((size_t)6 * n_mesh);
+        cudaMemcpyAsync(dh.data(), desc, 48 * (size_t)n_mesh, cudaMemcpyDeviceToHost, s);
+        int rc = bd_zmaps(z, dh.data(), n_mesh, maps, s);
+        if (rc) return rc;
+        int64_t rows_max = 0;
+        for (int i = 0; i < n_mesh; ++i) rows_max = std::max(rows_max, dh[6 * i + 2]);
+        cudaMemsetAsync(own, 0, 4, s);
+        if ((rc = bd_launch(maps, x, rows_max, desc, goff, n_mesh, total_warps, ld, nc, y, own, s))) return rc;
+        int hs = 0;
+        cudaMemcpyAsync(&hs, own, 4, cudaMemcpyDeviceToHost, s);
+        const cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return set_error(MB_ERR_CUDA, "blockdiag_matvec: %s", cudaGetErrorString(e));
+        if (hs) return set_error(MB_ERR_CUDA, "blockdiag_matvec: wait timed out (code %d)", hs);
+        return MB_OK;
+    }
     const int64_t blocks = (total_warps * 32 + 255) / 256;
     if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "batch too large for one launch");
 #define MB_BD(R, C)                                                                                           \
@@ -691,7 +918,7 @@ int blockdiag_matvec(const float* z, const int64_t* desc, const int64_t* goff, i
     MB_BD(1, 8) MB_BD(2, 8) MB_BD(4, 8)
 #undef MB_BD
     return set_error(MB_ERR_UNSUPPORTED, "block-diagonal product: rows per warp in {1, 2, 4, 8} (8 with up to 4 "
-                                         "columns), columns per mesh in {1, 2, 4, 8}");
+                                         "columns) or 32 (streamed), columns per mesh in {1, 2, 4, 8}");
 }
 
 // ---- host driver -------------------------------------------------------------------------
@@ -915,10 +1142,25 @@ int gmres_blockdiag(const float* z, const int64_t* desc, const int64_t* goff, in
                     double tol, bool use_graph, void* workspace, size_t ws_bytes, int64_t* iters_out,
                     int64_t* cycles_out, double* max_relres_out, int* status_out, cudaStream_t s) {
     const int64_t m = (int64_t)n_mesh * nc, mp = padded_width(m);
+    MgWork W;
+    const size_t map_bytes = sizeof(CUtensorMap) * (size_t)std::max(n_mesh, 1);
+    if (ws_bytes < mg_layout(n_rows, mp, r, map_bytes, nullptr, &W)) return set_error(MB_ERR_ARG, "workspace too small");
+    mg_layout(n_rows, mp, r, map_bytes, workspace, &W);
+    int* status = W.status;
+    const CUtensorMap* zmaps = static_cast<const CUtensorMap*>(W.gemm_ws);
+    if (rows_per_warp == kBdRows) {
+        if (reinterpret_cast<uintptr_t>(z) & 15) return set_error(MB_ERR_ARG, "z must be 16-byte aligned");
+        std::vector<int64_t> dh((size_t)6 * n_mesh);
+        cudaMemcpyAsync(dh.data(), desc, 48 * (size_t)n_mesh, cudaMemcpyDeviceToHost, s);
+        int rc = bd_zmaps(z, dh.data(), n_mesh, static_cast<CUtensorMap*>(W.gemm_ws), s);
+        if (rc) return rc;
+    }
     auto prod = [&](const float* v32, float* y32, cudaStream_t st) {
+        if (rows_per_warp == kBdRows)
+            return bd_launch(zmaps, v32, n_rows, desc, goff, n_mesh, total_warps, mp, nc, y32, status, st);
         return blockdiag_matvec(z, desc, goff, n_mesh, total_warps, v32, mp, nc, rows_per_warp, y32, st);
     };
-    return gmres_lockstep(prod, n_rows, b, x, m, r, max_iters, tol, 0, desc, nc, workspace, ws_bytes, use_graph,
+    return gmres_lockstep(prod, n_rows, b, x, m, r, max_iters, tol, map_bytes, desc, nc, workspace, ws_bytes, use_graph,
                           iters_out, cycles_out, max_relres_out, status_out, s);
 }
 

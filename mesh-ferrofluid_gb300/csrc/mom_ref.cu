@@ -702,7 +702,8 @@ __global__ void __launch_bounds__(128, NX <= 4 ? MB_FAST_MIN_BLOCKS : 2) mom_ref
     mom_entry_fast<NX, NY>(verts, faces, areas, normals, s_t, s_s, (float)__ldg(ks + i), fo + row / 3,
                            (int)(row % 3), fo + col / 3, (int)(col % 3), &re, &im);
     const int64_t m = __ldg(fei + 3 * fo + row), n = __ldg(fei + 3 * fo + col);
-    atomicAdd(reinterpret_cast<float2*>(z + 2 * (__ldg(desc + 6 * i + 3) + m * ne + n)), make_float2(re, im));
+    atomicAdd(reinterpret_cast<float2*>(z + 2 * (__ldg(desc + 6 * i + 3) + m * (ne + (ne & 1)) + n)),
+              make_float2(re, im));
 }
 
 int launch_mom_ref_zmat_batched(const float* verts, const int32_t* faces, const float* areas, const float* normals,

@@ -310,7 +310,8 @@ __global__ void __launch_bounds__(128) mom_sym_regular_batched_kernel(
     const int64_t qb = (nf + 127) / 128, local = b - __ldg(desc + kDesc * i + 4);
     const int64_t p = fo + local / qb, q = fo + (local % qb) * 128 + threadIdx.x;
     if (q >= fo + nf) return;
-    sym_regular_pair<T>(verts, faces, fei, __ldg(desc + kDesc * i + 2), (T)__ldg(ks + i), p, q, s_b,
+    const int64_t ne = __ldg(desc + kDesc * i + 2);
+    sym_regular_pair<T>(verts, faces, fei, ne + (ne & 1), (T)__ldg(ks + i), p, q, s_b,
                         z + 2 * __ldg(desc + kDesc * i + 3));
 }
 
@@ -324,7 +325,8 @@ __global__ void mom_sym_near_batched_kernel(const T* __restrict__ verts, const i
     if (t >= n_pairs) return;
     const int64_t p = pairs[2 * t];
     const int i = mesh_of(desc, n_mesh, 0, p);
-    sym_near_pair<T>(verts, faces, fei, desc[kDesc * i + 2], ks[i], p, pairs[2 * t + 1], z + 2 * desc[kDesc * i + 3]);
+    const int64_t ne = desc[kDesc * i + 2];
+    sym_near_pair<T>(verts, faces, fei, ne + (ne & 1), ks[i], p, pairs[2 * t + 1], z + 2 * desc[kDesc * i + 3]);
 }
 
 // waves: [n_mesh * nrhs, 9]; rhs: [rows, ld] interleaved complex, column desc[i][5] + r.

@@ -7,10 +7,19 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
+def _bipyramid():
+    """Pentagonal bipyramid: 7 vertices, 10 faces, 15 edges (an odd edge count, so its Z
+    block has padded rows)."""
+    a = 2 * np.pi * np.arange(5) / 5
+    v = np.concatenate([np.stack([np.cos(a), np.sin(a), np.zeros(5)], 1), [[0, 0, 1.2], [0, 0, -1.2]]])
+    f = [[k, (k + 1) % 5, 5] for k in range(5)] + [[(k + 1) % 5, k, 6] for k in range(5)]
+    return v.astype(np.float32), np.asarray(f, np.int32)
+
+
 def _batch(pkg, cuda):
     M = pkg.meshes
-    meshes = [M.icosphere(1, 1.0), M.ellipsoid(2), M.star_shape(2, seed=3)]
-    ks = [1.5, 2.5, 3.0]
+    meshes = [M.icosphere(1, 1.0), _bipyramid(), M.ellipsoid(2), M.star_shape(2, seed=3)]
+    ks = [1.5, 2.0, 2.5, 3.0]
     return pkg.batch.MeshBatch(meshes, ks, device=cuda), meshes, ks
 
 
@@ -52,7 +61,7 @@ def test_batched_assembly_and_excitation_match_per_mesh(pkg, cuda):
 
 
 @pytest.mark.parametrize("nc", [1, 4])
-@pytest.mark.parametrize("rows", [1, 2, 4, 8])
+@pytest.mark.parametrize("rows", [1, 2, 4, 8, 32])
 def test_blockdiag_matvec(pkg, cuda, nc, rows):
     bt, meshes, ks = _batch(pkg, cuda)
     bt.excitation(_waves(pkg, bt.n_mesh, nc, ks, cuda))
@@ -70,13 +79,16 @@ def test_blockdiag_matvec(pkg, cuda, nc, rows):
         assert torch.all(Y[e:, i * nc:(i + 1) * nc] == 0)
 
 
-@pytest.mark.parametrize("use_graph", [False, True])
-def test_batched_solve_matches_dense(pkg, cuda, use_graph):
+@pytest.mark.parametrize("use_graph,rows", [(False, None), (True, None), (True, 32)])
+def test_batched_solve_matches_dense(pkg, cuda, use_graph, rows):
     bt, meshes, ks = _batch(pkg, cuda)
     waves = _waves(pkg, bt.n_mesh, 4, ks, cuda, seed=1)
     Z = bt.assemble()
     B = bt.excitation(waves)
-    bt.autotune(Z)
+    if rows is None:
+        bt.autotune(Z)
+    else:
+        bt.rows_per_warp = rows
     X, info = bt.solve(Z, B, restart=50, tol=1e-6, max_iters=3000, use_graph=use_graph)
     assert info["converged"], info
     for i in range(bt.n_mesh):
