@@ -289,12 +289,13 @@ int mb_gmres_f64(const double* a, int64_t n, const double* b, double* x, int res
  * reference solves one right-hand side per dense LU, mesh_BEM_solver_3d.py:174): Z X = B
  * with Z given by its TF32 split (as for mb_cgemm_tf32x3), B, X complex128 [n, m]
  * interleaved (X: initial guess in, solution out).  Every Arnoldi step multiplies all m
- * basis vectors with one tensor-core product; basis, CGS2 and Givens rotations are FP64 per
- * column; each restart cycle starts from B - Z X through the same product (attainable
- * relative residual ~1e-6).  info: total Arnoldi steps, restart cycles, the largest
- * per-column relative residual, status 0 when every column reached tol.  Workspace:
- * mb_gmres_multi_workspace_bytes(n, m, restart) bytes (the FP64 basis dominates:
- * 16 n m (restart + 1)). */
+ * basis vectors with one tensor-core product; the basis is complex64 and CGS2 runs in FP32
+ * with FP64 sums across rows (TMA-streamed kernels), the Hessenberg matrix, the Givens
+ * rotations and X are FP64 per column; each restart cycle starts from B - Z X through the
+ * same product (attainable relative residual ~1e-6).  info: total Arnoldi steps, restart
+ * cycles, the largest per-column relative residual, status 0 when every column reached
+ * tol.  Workspace: mb_gmres_multi_workspace_bytes(n, m, restart) bytes (the basis
+ * dominates: 8 n m' (restart + 1), m' = m rounded up to even). */
 size_t mb_gmres_multi_workspace_bytes(int64_t n, int64_t m, int restart);
 int mb_gmres_multi_c64(const float* z_hi, const float* z_lo, int64_t n, const double* b, double* x,
                        int64_t m, int restart, int max_iters, double tol, void* workspace,
