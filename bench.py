@@ -1080,13 +1080,14 @@ def main():
     M = pkg.mesh_MOM_3d
     near = M.near_pairs(faces) if sym else None
     n_near = int(near.shape[0]) if sym else 0
+    er_map = None if sym else M.edge_rows(fei, faces.shape[0], n_edges)  # mesh preprocessing, like fei
 
     def assemble(out):
         if sym:
             M.assemble_Z_rwg_sym(verts, faces, fei, n_edges, k, out=out, pairs=near, check_indices=False)
         else:
             M.assemble_Z_rwg(verts, faces, areas, normals, fei, n_edges, px, wx, py, wy, k, out=out,
-                             check_indices=False)
+                             check_indices=False, order="edges", edge_rows_map=er_map)
 
     def step():
         Z.zero_()
@@ -1156,6 +1157,8 @@ def main():
             "mufu": {"achieved_gops": mufu / kern_avg_s / 1e9, "peak_gops": mufu_peak,
                      "frac": mufu / kern_avg_s / 1e9 / mufu_peak},
             "algorithmic": per_eval,
+            "kernel": ("mom_sym_regular_kernel + mom_sym_near_kernel" if sym else
+                       f"mom_ref_zmat_edge_kernel<{gq},{gq - 1}> (Z row by Z row)"),
             "kernel_ms": kern_avg_s * 1e3}
 
     line = {"metric": "Z-assembly triangle pairs/s", "value": value, "unit": "pairs/s",
@@ -1206,14 +1209,15 @@ def main():
                 d.copy_(h, non_blocking=True)
             a = pkg.utils.compute_face_areas(d_verts, d_faces).contiguous()
             nn = pkg.utils.compute_face_normals(d_verts, d_faces).contiguous()
-            Z.zero_()
             if sym:
+                Z.zero_()
                 M.assemble_Z_rwg_sym(d_verts, d_faces, d_fei, n_edges, k, out=Z, pairs=near,
                                      check_indices=False)
+                h_Z.copy_(Z, non_blocking=True)
             else:
+                # Z rows assembled in 16 ranges, each range's copy to host overlapping the next
                 M.assemble_Z_rwg(d_verts, d_faces, a, nn, d_fei, n_edges, *d_rules, k, out=Z,
-                                 check_indices=False)
-            h_Z.copy_(Z, non_blocking=True)
+                                 check_indices=False, out_host=h_Z, chunks=16)
 
         e2e_step()
         barrier()
@@ -1233,7 +1237,8 @@ def main():
                        "ms_per_step": e2e_ms, "steps": e2e_steps,
                        "path": ("mesh_MOM_3d.assemble_Z_rwg_sym (C ABI mb_mom_sym_zmat_rwg_c64 + "
                                 "mb_mom_sym_near_c64)" if sym else
-                                "mesh_MOM_3d.assemble_Z_rwg (C ABI mb_mom_zmat_rwg_c64)")
+                                "mesh_MOM_3d.assemble_Z_rwg(out_host=...) (C ABI mb_mom_zmat_rwg_to_host_c64: "
+                                "Z rows in 16 ranges, each range's D2H overlapping the next range's assembly)")
                                + ", pinned host buffers, H2D inputs + Z D2H inside the timed region"}
         del h_Z
 

@@ -98,6 +98,34 @@ int mb_mom_zmat_rwg_c128(const double* verts, int64_t n_verts, const int32_t* fa
                          double wavenumber, int64_t row_begin, int64_t row_end, double* z,
                          void* stream);
 
+/* No counterpart in the reference (its scatter_add_ runs after the whole face-edge matrix
+ * exists).  edge_rows [2 n_edges + 1] int32: for Z row m (edge m) the face-edge rows 3f + e
+ * of its faces (smaller first; -1 for a missing second face); edge_rows[2 n_edges] = 1 when
+ * some edge has more than two faces (the edge-row operators below then do not apply). */
+int mb_mom_edge_rows(const int32_t* face_edge_indices, int64_t n_faces, int64_t n_edges, int32_t* edge_rows,
+                     void* stream);
+/* The same matrix as mb_mom_zmat_rwg_c64, built Z row by Z row: rows [m_begin, m_end) of z
+ * (accumulated), each entry's (up to two) face-edge contributions summed before one atomic;
+ * float32 meshes with the gaussQR 2-5 rules (n_x = gaussQR, n_y = gaussQR - 1). */
+int mb_mom_zmat_rwg_edges_c64(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                              const float* face_areas, const float* face_normals,
+                              const int32_t* face_edge_indices, const int32_t* edge_rows, int64_t n_edges,
+                              const float* gp_x, const float* gw_x, int n_x, const float* gp_y,
+                              const float* gw_y, int n_y, double wavenumber, int64_t m_begin, int64_t m_end,
+                              float* z, void* stream);
+/* Z into host memory z_host [n_edges, n_edges] complex64 (pinned for overlap): the rows are
+ * assembled in `chunks` ranges into the device scratch z_dev [n_edges, n_edges] and each range
+ * is copied to z_host on a second stream while the next one is assembled; edge_rows device
+ * scratch [2 n_edges + 1].  Meshes with an edge of more than two faces, or rules without an
+ * edge-row instance, are assembled face row by face row and copied once.  Returns when the
+ * work is queued; the calling stream waits for the last copy. */
+int mb_mom_zmat_rwg_to_host_c64(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                                const float* face_areas, const float* face_normals,
+                                const int32_t* face_edge_indices, int64_t n_edges, const float* gp_x,
+                                const float* gw_x, int n_x, const float* gp_y, const float* gw_y, int n_y,
+                                double wavenumber, int32_t* edge_rows, float* z_dev, float* z_host, int chunks,
+                                void* stream);
+
 /* Replaces MeshMOMRhsKernel.apply + rhs.scatter_add_ (kernel_functions.py:90-121,
  * mesh_BEM_solver_3d.py:149-164) for n_rhs plane waves at once.  waves: device array of
  * n_rhs records of 9 doubles (k*khat[3], E polarisation[3], H = khat x E / eta [3]);

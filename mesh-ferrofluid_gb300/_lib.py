@@ -33,6 +33,11 @@ _SIGS = {
                             _I64, _I64, _P, _P],
     "mb_mom_zmat_rwg_c128": [_P, _I64, _P, _I64, _P, _P, _P, _I64, _P, _P, _I, _P, _P, _I, _D,
                              _I64, _I64, _P, _P],
+    "mb_mom_edge_rows": [_P, _I64, _I64, _P, _P],
+    "mb_mom_zmat_rwg_edges_c64": [_P, _I64, _P, _I64, _P, _P, _P, _P, _I64, _P, _P, _I, _P, _P, _I, _D,
+                                  _I64, _I64, _P, _P],
+    "mb_mom_zmat_rwg_to_host_c64": [_P, _I64, _P, _I64, _P, _P, _P, _I64, _P, _P, _I, _P, _P, _I, _D,
+                                    _P, _P, _P, _I, _P],
     "mb_mom_rhs_rwg_c64": [_P, _I64, _P, _I64, _P, _P, _P, _I64, _P, _P, _I, _P, _I, _P, _P],
     "mb_mom_rhs_rwg_c128": [_P, _I64, _P, _I64, _P, _P, _P, _I64, _P, _P, _I, _P, _I, _P, _P],
     "mb_mom_interp_vert_c64": [_P, _I64, _P, _I64, _P, _P, _P, _I64, _I64, _P, _P],

@@ -79,6 +79,15 @@ int gnn_aggregate_bwd(const float* dcat, const int32_t* nbr, int64_t N, int F, f
 int gnn_relu_bwd(const void* y, const float* dy, int64_t count, float* dz, cudaStream_t s);
 int gnn_adam(float* w, float* m1, float* m2, const float* g, int64_t count, float lr, float b1, float b2, float eps,
              int step, void* w16, cudaStream_t s);
+int launch_edge_rows(const int32_t* fei, int64_t nf, int64_t n_edges, int32_t* er, cudaStream_t s);
+bool launch_fast_zmat_edges(const float* verts, const int32_t* faces, const float* areas, const float* normals,
+                            const int32_t* fei, const int32_t* edge_rows, int64_t n_edges, const float* gpx,
+                            const float* gwx, int nx, const float* gpy, const float* gwy, int ny, double k,
+                            int64_t nf, int64_t m_begin, int64_t m_end, float* z, cudaStream_t stream);
+int zmat_edges_to_host(const float* verts, const int32_t* faces, const float* areas, const float* normals,
+                       const int32_t* fei, const int32_t* edge_rows, int64_t n_edges, const float* gpx,
+                       const float* gwx, int nx, const float* gpy, const float* gwy, int ny, double k, int64_t nf,
+                       float* z_dev, float* z_host, int chunks, cudaStream_t s);
 size_t gmres_blockdiag_workspace_bytes(int64_t n, int64_t m, int r);
 int blockdiag_matvec(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
                      const float* x, int64_t ld, int nc, int rows, float* y, cudaStream_t s);
@@ -199,6 +208,68 @@ int mb_mom_zmat_rwg_c128(const double* verts, int64_t n_verts, const int32_t* fa
     return zmat_rwg<double>(verts, n_verts, faces, n_faces, face_areas, face_normals, face_edge_indices,
                             n_edges, gp_x, gw_x, n_x, gp_y, gw_y, n_y, wavenumber, row_begin, row_end, z,
                             stream);
+}
+
+int mb_mom_edge_rows(const int32_t* face_edge_indices, int64_t n_faces, int64_t n_edges, int32_t* edge_rows,
+                     void* stream) {
+    MB_REQUIRE(n_faces >= 0 && n_edges >= 0 && n_edges < (1ll << 30) && 3 * n_faces < (1ll << 31), "bad sizes");
+    MB_REQUIRE(face_edge_indices && edge_rows, "null pointer argument");
+    return launch_edge_rows(face_edge_indices, n_faces, n_edges, edge_rows, as_stream(stream));
+}
+
+int mb_mom_zmat_rwg_edges_c64(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                              const float* face_areas, const float* face_normals,
+                              const int32_t* face_edge_indices, const int32_t* edge_rows, int64_t n_edges,
+                              const float* gp_x, const float* gw_x, int n_x, const float* gp_y,
+                              const float* gw_y, int n_y, double wavenumber, int64_t m_begin, int64_t m_end,
+                              float* z, void* stream) {
+    (void)n_verts;
+    MB_REQUIRE(n_faces >= 0 && n_edges >= 0, "bad sizes");
+    MB_REQUIRE(0 <= m_begin && m_begin <= m_end && m_end <= n_edges, "row range outside [0, n_edges)");
+    MB_REQUIRE(verts && faces && face_areas && face_normals && face_edge_indices && edge_rows && gp_x && gw_x &&
+                   gp_y && gw_y && z,
+               "null pointer argument");
+    MB_REQUIRE(wavenumber > 0, "wavenumber must be > 0");
+    MB_REQUIRE((m_end - m_begin) * ((3 * n_faces + 127) / 128) < 0x7fffffffLL, "mesh too large for one launch");
+    if (!launch_fast_zmat_edges(verts, faces, face_areas, face_normals, face_edge_indices, edge_rows, n_edges,
+                                gp_x, gw_x, n_x, gp_y, gw_y, n_y, wavenumber, n_faces, m_begin, m_end, z,
+                                as_stream(stream)))
+        return set_error(MB_ERR_UNSUPPORTED, "edge-row assembly: no instance for rule sizes (%d, %d)", n_x, n_y);
+    return check_launch("mom_ref_zmat_edges");
+}
+
+int mb_mom_zmat_rwg_to_host_c64(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                                const float* face_areas, const float* face_normals,
+                                const int32_t* face_edge_indices, int64_t n_edges, const float* gp_x,
+                                const float* gw_x, int n_x, const float* gp_y, const float* gw_y, int n_y,
+                                double wavenumber, int32_t* edge_rows, float* z_dev, float* z_host, int chunks,
+                                void* stream) {
+    MB_REQUIRE(n_faces >= 0 && n_edges >= 0 && n_edges < (1ll << 30), "bad sizes");
+    MB_REQUIRE(verts && faces && face_areas && face_normals && face_edge_indices && edge_rows && gp_x && gw_x &&
+                   gp_y && gw_y && z_dev && z_host,
+               "null pointer argument");
+    MB_REQUIRE(wavenumber > 0, "wavenumber must be > 0");
+    if (n_faces == 0 || n_edges == 0) return MB_OK;
+    cudaStream_t s = as_stream(stream);
+    int rc = launch_edge_rows(face_edge_indices, n_faces, n_edges, edge_rows, s);
+    if (rc) return rc;
+    int32_t many = 0;
+    cudaMemcpyAsync(&many, edge_rows + 2 * n_edges, 4, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return check_launch("zmat to host: edge rows");
+    const bool fast = (n_x == 4 && n_y == 3) || (n_x == 3 && n_y == 2) || (n_x == 2 && n_y == 1) ||
+                      (n_x == 5 && n_y == 4);
+    MB_REQUIRE((n_edges / std::max(chunks, 1) + 1) * ((3 * n_faces + 127) / 128) < 0x7fffffffLL,
+               "mesh too large for one launch per chunk");
+    if (!many && fast)
+        return zmat_edges_to_host(verts, faces, face_areas, face_normals, face_edge_indices, edge_rows, n_edges,
+                                  gp_x, gw_x, n_x, gp_y, gw_y, n_y, wavenumber, n_faces, z_dev, z_host, chunks, s);
+    cudaMemsetAsync(z_dev, 0, (size_t)n_edges * n_edges * 8, s);
+    rc = zmat_rwg<float>(verts, n_verts, faces, n_faces, face_areas, face_normals, face_edge_indices, n_edges,
+                         gp_x, gw_x, n_x, gp_y, gw_y, n_y, wavenumber, 0, 3 * n_faces, z_dev, stream);
+    if (rc) return rc;
+    if (cudaMemcpyAsync(z_host, z_dev, (size_t)n_edges * n_edges * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return check_launch("zmat to host: copy");
+    return MB_OK;
 }
 
 #define MB_RHS_FE(SFX, T)                                                                             \

@@ -28,6 +28,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+#include <vector>
+
 #include "common.cuh"
 
 namespace mb {
@@ -444,6 +447,145 @@ __global__ void __launch_bounds__(128, NX <= 4 ? MB_FAST_MIN_BLOCKS : 2) mom_ref
             zi[o] = im;
         }
     }
+}
+
+// Edge-row order (RWG layout): block row m is Z row m, i.e. edge m; its (at most two)
+// face-edge test rows edge_rows[2m], edge_rows[2m + 1] (3 f + e, or -1) are evaluated by the
+// same thread and summed before one atomic per entry, and Z row m is complete when its
+// blocks end -- so row ranges can be assembled and copied out in chunks.
+template <int NX, int NY>
+__global__ void __launch_bounds__(128, NX <= 4 ? MB_FAST_MIN_BLOCKS : 2) mom_ref_zmat_edge_kernel(
+    const float* __restrict__ verts, const int32_t* __restrict__ faces, const float* __restrict__ areas,
+    const float* __restrict__ normals, const int32_t* __restrict__ fei, const int32_t* __restrict__ edge_rows,
+    int64_t n_edges, const float* __restrict__ gpx, const float* __restrict__ gwx, const float* __restrict__ gpy,
+    const float* __restrict__ gwy, float k, int64_t nf, int64_t m_begin, int64_t col_blocks,
+    float* __restrict__ z) {
+    __shared__ float4 s_t[NX * NX], s_s[NY * NY];
+    stage_rules<NX, NY>(gpx, gwx, gpy, gwy, s_t, s_s);
+    __syncthreads();
+    const int64_t ncol = 3 * nf;
+    const int64_t m = m_begin + (int64_t)blockIdx.x / col_blocks;
+    const int64_t col = ((int64_t)blockIdx.x % col_blocks) * blockDim.x + threadIdx.x;
+    if (col >= ncol) return;
+    float re = 0.f, im = 0.f;
+#pragma unroll 1
+    for (int j = 0; j < 2; ++j) {
+        const int32_t row = __ldg(edge_rows + 2 * m + j);
+        if (row < 0) continue;
+        float a, b;
+        mom_entry_fast<NX, NY>(verts, faces, areas, normals, s_t, s_s, k, row / 3, row % 3, col / 3,
+                               (int)(col % 3), &a, &b);
+        re += a;
+        im += b;
+    }
+    atomicAdd(reinterpret_cast<float2*>(z + 2 * (m * n_edges + __ldg(fei + col))), make_float2(re, im));
+}
+
+// Edge -> face-edge rows: slot 0 the smaller row, slot 1 the larger (or -1 for a boundary
+// edge); edge_rows[2E] is set to 1 when some edge has more than two faces.
+__global__ void edge_rows_init(int32_t* __restrict__ er, int64_t n_edges) {
+    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < n_edges) {
+        er[2 * m] = 0x7fffffff;
+        er[2 * m + 1] = -1;
+    }
+    if (m == 0) er[2 * n_edges] = 0;
+}
+__global__ void edge_rows_minmax(const int32_t* __restrict__ fei, int64_t nfe, int32_t* __restrict__ er) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nfe) return;
+    const int32_t m = fei[r];
+    atomicMin(er + 2 * m, (int32_t)r);
+    atomicMax(er + 2 * m + 1, (int32_t)r);
+}
+__global__ void edge_rows_check(const int32_t* __restrict__ fei, int64_t nfe, int64_t n_edges, int32_t* er) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nfe) return;
+    const int32_t m = fei[r];
+    if (r != er[2 * m] && r != er[2 * m + 1]) er[2 * n_edges] = 1;
+}
+__global__ void edge_rows_finish(int32_t* __restrict__ er, int64_t n_edges) {
+    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n_edges) return;
+    if (er[2 * m] == 0x7fffffff) er[2 * m] = -1;
+    if (er[2 * m + 1] == er[2 * m]) er[2 * m + 1] = -1;
+}
+
+int launch_edge_rows(const int32_t* fei, int64_t nf, int64_t n_edges, int32_t* er, cudaStream_t s) {
+    const int64_t nfe = 3 * nf;
+    const unsigned be = (unsigned)((n_edges + 255) / 256 + 1), bf = (unsigned)((nfe + 255) / 256 + 1);
+    edge_rows_init<<<be, 256, 0, s>>>(er, n_edges);
+    edge_rows_minmax<<<bf, 256, 0, s>>>(fei, nfe, er);
+    edge_rows_check<<<bf, 256, 0, s>>>(fei, nfe, n_edges, er);
+    edge_rows_finish<<<be, 256, 0, s>>>(er, n_edges);
+    return check_launch("edge_rows");
+}
+
+// Edge-row launch over Z rows [m_begin, m_end) for the float fast path; false when the rule
+// sizes have no fast instance.
+bool launch_fast_zmat_edges(const float* verts, const int32_t* faces, const float* areas, const float* normals,
+                            const int32_t* fei, const int32_t* edge_rows, int64_t n_edges, const float* gpx,
+                            const float* gwx, int nx, const float* gpy, const float* gwy, int ny, double k,
+                            int64_t nf, int64_t m_begin, int64_t m_end, float* z, cudaStream_t stream) {
+    const int64_t col_blocks = (3 * nf + 127) / 128;
+    const int64_t blocks = (m_end - m_begin) * col_blocks;
+    if (blocks <= 0) return true;
+#define MB_FAST_E(NXV, NYV)                                                                           \
+    if (nx == NXV && ny == NYV) {                                                                     \
+        mom_ref_zmat_edge_kernel<NXV, NYV><<<(unsigned)blocks, 128, 0, stream>>>(                      \
+            verts, faces, areas, normals, fei, edge_rows, n_edges, gpx, gwx, gpy, gwy, (float)k, nf,   \
+            m_begin, col_blocks, z);                                                                  \
+        return true;                                                                                  \
+    }
+    MB_FAST_E(4, 3)
+    MB_FAST_E(3, 2)
+    MB_FAST_E(2, 1)
+    MB_FAST_E(5, 4)
+#undef MB_FAST_E
+    return false;
+}
+
+// Z to host memory with the copy overlapped: Z rows are assembled in `chunks` edge-row
+// ranges on stream s, each range copied to z_host on a second stream as soon as its kernel
+// ends (z_dev: device scratch [E, E]; edge_rows: from launch_edge_rows, every edge at most
+// two faces).  The calling stream waits for the last copy.
+int zmat_edges_to_host(const float* verts, const int32_t* faces, const float* areas, const float* normals,
+                       const int32_t* fei, const int32_t* edge_rows, int64_t n_edges, const float* gpx,
+                       const float* gwx, int nx, const float* gpy, const float* gwy, int ny, double k, int64_t nf,
+                       float* z_dev, float* z_host, int chunks, cudaStream_t s) {
+    chunks = std::max(1, std::min(chunks, 256));
+    cudaStream_t cs = nullptr;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
+        return set_error(MB_ERR_CUDA, "zmat to host: copy stream");
+    std::vector<cudaEvent_t> ev((size_t)chunks + 1, nullptr);
+    int rc = MB_OK;
+    for (auto& e : ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = MB_ERR_CUDA;
+    if (rc == MB_OK) {
+        for (int c = 0; c < chunks; ++c) {
+            const int64_t m0 = n_edges * c / chunks, m1 = n_edges * (c + 1) / chunks;
+            if (m1 <= m0) continue;
+            const size_t off = (size_t)m0 * n_edges * 2, bytes = (size_t)(m1 - m0) * n_edges * 8;
+            cudaMemsetAsync(z_dev + off, 0, bytes, s);
+            if (!launch_fast_zmat_edges(verts, faces, areas, normals, fei, edge_rows, n_edges, gpx, gwx, nx, gpy,
+                                        gwy, ny, k, nf, m0, m1, z_dev, s)) {
+                rc = set_error(MB_ERR_UNSUPPORTED, "zmat to host: no fast rule (%d, %d)", nx, ny);
+                break;
+            }
+            cudaEventRecord(ev[c], s);
+            cudaStreamWaitEvent(cs, ev[c], 0);
+            cudaMemcpyAsync(z_host + off, z_dev + off, bytes, cudaMemcpyDeviceToHost, cs);
+        }
+        cudaEventRecord(ev[chunks], cs);
+        cudaStreamWaitEvent(s, ev[chunks], 0);
+    } else {
+        rc = set_error(MB_ERR_CUDA, "zmat to host: events");
+    }
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    cudaStreamDestroy(cs);
+    if (rc) return rc;
+    return check_launch("zmat to host");
 }
 
 // Launches the fast path for float and supported rule sizes; returns false otherwise.

@@ -148,13 +148,22 @@ def _check_fei(face_edge_indices, nf, n_edges, dev):
 
 def assemble_Z_rwg(verts, faces, face_areas, face_normals, face_edge_indices, n_edges,
                    gaussian_points_1d_x, gaussian_weights_1d_x, gaussian_points_1d_y,
-                   gaussian_weights_1d_y, wavenumber, out=None, rows=None, check_indices=True):
+                   gaussian_weights_1d_y, wavenumber, out=None, rows=None, check_indices=True,
+                   order="auto", edge_rows_map=None, out_host=None, chunks=16):
     """RWG impedance matrix Z [E, E] complex (complex64 for float32 meshes).
 
     Same entries as ``create_MOM_Zmat_3d_forward`` followed by the reference's
     ``scatter_add_`` onto face_edge_indices (mesh_BEM_solver_3d.py:128-147), in one pass.
     ``out`` (complex [E, E]) is accumulated into if given, else a zeroed matrix is made.
-    ``rows`` = (begin, end) restricts the face-edge test rows (for chunked assembly).
+    ``rows`` = (begin, end) restricts the test rows (for chunked assembly): face-edge rows
+    with ``order="faces"``, Z rows (edges) with ``order="edges"`` (float32, gaussQR 2-5: each
+    Z row built by one block row, its two face contributions summed before one atomic).
+    ``order="auto"`` (default) takes the edge order when it applies (float32, a fast rule, no
+    ``rows``, every edge on at most two faces) and the face order otherwise.
+    ``edge_rows_map``: ``edge_rows(face_edge_indices, F, E)`` computed once by the caller.
+    ``out_host`` (complex64 [E, E] CPU tensor, pinned for overlap): Z goes to host memory,
+    assembled in ``chunks`` Z-row ranges with each range's copy overlapping the next range's
+    assembly; ``out`` is then the device scratch (overwritten).  Returns ``out_host`` then.
     """
     dt, dev, nv, nf = _mesh_args(verts, faces, face_areas, face_normals)
     nx = _rule(gaussian_points_1d_x, gaussian_weights_1d_x, "test rule", dt, dev)
@@ -166,13 +175,58 @@ def assemble_Z_rwg(verts, faces, face_areas, face_normals, face_edge_indices, n_
         out = torch.zeros((n_edges, n_edges), dtype=cdt, device=dev)
     else:
         _lib.check_tensor(out, "out", dtype=cdt, device=dev, shape=(n_edges, n_edges))
+    rules = (_lib.ptr(gaussian_points_1d_x), _lib.ptr(gaussian_weights_1d_x), nx,
+             _lib.ptr(gaussian_points_1d_y), _lib.ptr(gaussian_weights_1d_y), ny, float(wavenumber))
+    if out_host is not None:
+        if dt != torch.float32:
+            raise ValueError("out_host needs a float32 mesh")
+        if (out_host.device.type != "cpu" or out_host.dtype != torch.complex64 or not out_host.is_contiguous()
+                or tuple(out_host.shape) != (n_edges, n_edges)):
+            raise ValueError("out_host must be a contiguous complex64 CPU tensor [E, E]")
+        er = torch.empty(2 * n_edges + 1, dtype=torch.int32, device=dev)
+        _lib.call("mb_mom_zmat_rwg_to_host_c64", _lib.ptr(verts), nv, _lib.ptr(faces), nf,
+                  _lib.ptr(face_areas), _lib.ptr(face_normals), _lib.ptr(face_edge_indices), n_edges, *rules,
+                  _lib.ptr(er), _lib.ptr(out), out_host.data_ptr(), int(chunks), _lib.stream_of(verts))
+        return out_host
+    if order == "auto":
+        order = "faces"
+        if dt == torch.float32 and rows is None and (nx, ny) in _EDGE_RULES:
+            try:
+                edge_rows_map = edge_rows(face_edge_indices, nf, n_edges) if edge_rows_map is None else edge_rows_map
+                order = "edges"
+            except ValueError:
+                pass
+    if order == "edges":
+        if dt != torch.float32:
+            raise ValueError("order='edges' needs a float32 mesh")
+        er = edge_rows(face_edge_indices, nf, n_edges) if edge_rows_map is None else edge_rows_map
+        m0, m1 = (0, n_edges) if rows is None else rows
+        _lib.call("mb_mom_zmat_rwg_edges_c64", _lib.ptr(verts), nv, _lib.ptr(faces), nf, _lib.ptr(face_areas),
+                  _lib.ptr(face_normals), _lib.ptr(face_edge_indices), _lib.ptr(er), n_edges, *rules, int(m0),
+                  int(m1), _lib.ptr(out), _lib.stream_of(verts))
+        return out
+    if order != "faces":
+        raise ValueError("order must be 'faces' or 'edges'")
     r0, r1 = (0, 3 * nf) if rows is None else rows
     _lib.call(f"mb_mom_zmat_rwg_{_lib.csfx(dt)}", _lib.ptr(verts), nv, _lib.ptr(faces), nf,
-              _lib.ptr(face_areas), _lib.ptr(face_normals), _lib.ptr(face_edge_indices), n_edges,
-              _lib.ptr(gaussian_points_1d_x), _lib.ptr(gaussian_weights_1d_x), nx,
-              _lib.ptr(gaussian_points_1d_y), _lib.ptr(gaussian_weights_1d_y), ny, float(wavenumber),
+              _lib.ptr(face_areas), _lib.ptr(face_normals), _lib.ptr(face_edge_indices), n_edges, *rules,
               int(r0), int(r1), _lib.ptr(out), _lib.stream_of(verts))
     return out
+
+
+_EDGE_RULES = {(4, 3), (3, 2), (2, 1), (5, 4)}  # (n_x, n_y) with an edge-row kernel
+
+
+def edge_rows(face_edge_indices, n_faces: int, n_edges: int) -> torch.Tensor:
+    """Z row -> face-edge rows map for ``order='edges'``: int32 [2 E + 1] (see
+    ``mb_mom_edge_rows``); raises if some edge has more than two faces."""
+    dev = face_edge_indices.device
+    er = torch.empty(2 * n_edges + 1, dtype=torch.int32, device=dev)
+    _lib.call("mb_mom_edge_rows", _lib.ptr(face_edge_indices), int(n_faces), int(n_edges), _lib.ptr(er),
+              _lib.stream_of(face_edge_indices))
+    if int(er[-1].item()):
+        raise ValueError("an edge has more than two faces: use order='faces'")
+    return er
 
 
 def plane_waves(wavenumber: float, directions, polarizations, eta: float = 1.0,

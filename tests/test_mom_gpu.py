@@ -141,6 +141,64 @@ def test_zmat_rwg_row_chunks_sum_to_full(pkg, cuda):
     assert rel_err(part.cpu().numpy(), full.cpu().numpy()) < 1e-6
 
 
+def _ico_setup(pkg, cuda, level):
+    v_np, f_np = pkg.meshes.icosphere(level)
+    v = torch.tensor(v_np, dtype=torch.float32, device=cuda)
+    f = torch.tensor(f_np, dtype=torch.int32, device=cuda)
+    edges, fei, _ = pkg.utils.get_edge_unique(v, f)
+    a = pkg.utils.compute_face_areas(v, f).contiguous()
+    n = pkg.utils.compute_face_normals(v, f).contiguous()
+    px, wx = pkg.utils.get_gaussion_integration_points_and_weights(4, device=cuda)
+    py, wy = pkg.utils.get_gaussion_integration_points_and_weights(3, device=cuda)
+    return v, f, a, n, fei, edges.shape[0], (px, wx, py, wy)
+
+
+def test_edge_rows_map(pkg, cuda):
+    v, f, a, n, fei, ne, _ = _ico_setup(pkg, cuda, 2)
+    er = pkg.mesh_MOM_3d.edge_rows(fei, f.shape[0], ne).cpu().numpy()
+    e = fei.cpu().numpy().reshape(-1).astype(np.int64)
+    ref = np.full((ne, 2), -1, np.int64)
+    for r in np.argsort(e, kind="stable"):  # rows of each edge in increasing order
+        m = e[r]
+        ref[m, 0 if ref[m, 0] < 0 else 1] = r
+    assert er[-1] == 0
+    assert np.array_equal(er[:-1].reshape(ne, 2), ref)
+
+
+def test_edge_rows_reject_more_than_two_faces(pkg, cuda):
+    # three triangles on one edge (0, 1)
+    v = torch.tensor([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1]], dtype=torch.float32, device=cuda)
+    f = torch.tensor([[0, 1, 2], [1, 0, 3], [0, 1, 4]], dtype=torch.int32, device=cuda)
+    edges, fei, _ = pkg.utils.get_edge_unique(v, f)
+    with pytest.raises(ValueError):
+        pkg.mesh_MOM_3d.edge_rows(fei, 3, edges.shape[0])
+
+
+@pytest.mark.parametrize("level,k", [(2, 3.0), (3, 8.0)])
+def test_zmat_rwg_edge_order_equals_face_order(pkg, cuda, level, k):
+    v, f, a, n, fei, ne, rules = _ico_setup(pkg, cuda, level)
+    M = pkg.mesh_MOM_3d
+    zf = M.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, k)
+    ze = M.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, k, order="edges")
+    assert rel_err(ze.cpu().numpy(), zf.cpu().numpy()) < 1e-6
+    part = torch.zeros_like(ze)
+    for m0 in range(0, ne, 101):  # Z-row chunks sum to the whole
+        M.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, k, out=part, order="edges", rows=(m0, min(ne, m0 + 101)))
+    assert torch.equal(part, ze)
+
+
+@pytest.mark.parametrize("chunks", [1, 7])
+def test_zmat_rwg_to_host_equals_device(pkg, cuda, chunks):
+    v, f, a, n, fei, ne, rules = _ico_setup(pkg, cuda, 3)
+    M = pkg.mesh_MOM_3d
+    zd = M.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, 5.0, order="edges")
+    h = torch.empty((ne, ne), dtype=torch.complex64, pin_memory=True)
+    scratch = torch.full((ne, ne), float("nan"), dtype=torch.complex64, device=cuda)  # overwritten
+    M.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, 5.0, out=scratch, out_host=h, chunks=chunks)
+    torch.cuda.synchronize()
+    assert torch.equal(h, zd.cpu())
+
+
 @pytest.mark.parametrize("name", ["ico0", "ell1"])
 def test_rhs_fe_matches_reference(pkg, cuda, golden, name):
     g = golden[name]
