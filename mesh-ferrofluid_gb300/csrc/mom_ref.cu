@@ -313,8 +313,9 @@ __device__ __forceinline__ void mom_entry_fast(const float* __restrict__ verts,
     const float c1 = (a1 < a2 ? 1.f : -1.f) * sqrtf(dot(ev2, ev2)) / (2.f * area1);
     const float c2 = (b1 < b2 ? 1.f : -1.f) * sqrtf(dot(d2, d2)) / (2.f * area2);
 
-    // Source points (origin B0) packed two per register pair: coordinates, weight and the
-    // projections on the test edge vectors and normal.
+    // Source points (origin B0) packed two per register pair: coordinates scaled by k (only
+    // distances use them: |k x - k y| = kR), the weight k w (so g = w / R = (k w) / (kR)), and
+    // the projections k (y.e1), k (y.e2) on the test edge vectors and y.n1 on the normal.
     float2 yx[NP > 0 ? NP : 1], yy[NP > 0 ? NP : 1], yz[NP > 0 ? NP : 1], yw[NP > 0 ? NP : 1],
         ye1[NP > 0 ? NP : 1], ye2[NP > 0 ? NP : 1], yn[NP > 0 ? NP : 1];
     float tx = 0.f, ty = 0.f, tz = 0.f, tw = 0.f, te1 = 0.f, te2 = 0.f, tn = 0.f;  // the tail point
@@ -322,26 +323,31 @@ __device__ __forceinline__ void mom_entry_fast(const float* __restrict__ verts,
     for (int j = 0; j < NS; ++j) {
         const float4 r = s_s[j];
         const V3<float> y = (r.x - r.y) * B1 + r.y * B2;
-        const float w = r.z * (2.f * area2);
+        const float w = r.z * (2.f * area2) * k;
         if (j < 2 * NP) {
-            (reinterpret_cast<float*>(&yx[j / 2]) + (j & 1))[0] = y.x;
-            (reinterpret_cast<float*>(&yy[j / 2]) + (j & 1))[0] = y.y;
-            (reinterpret_cast<float*>(&yz[j / 2]) + (j & 1))[0] = y.z;
+            (reinterpret_cast<float*>(&yx[j / 2]) + (j & 1))[0] = k * y.x;
+            (reinterpret_cast<float*>(&yy[j / 2]) + (j & 1))[0] = k * y.y;
+            (reinterpret_cast<float*>(&yz[j / 2]) + (j & 1))[0] = k * y.z;
             (reinterpret_cast<float*>(&yw[j / 2]) + (j & 1))[0] = w;
-            (reinterpret_cast<float*>(&ye1[j / 2]) + (j & 1))[0] = dot(y, ev1);
-            (reinterpret_cast<float*>(&ye2[j / 2]) + (j & 1))[0] = dot(y, ev2);
+            (reinterpret_cast<float*>(&ye1[j / 2]) + (j & 1))[0] = k * dot(y, ev1);
+            (reinterpret_cast<float*>(&ye2[j / 2]) + (j & 1))[0] = k * dot(y, ev2);
             (reinterpret_cast<float*>(&yn[j / 2]) + (j & 1))[0] = dot(y, n1);
         } else {
-            tx = y.x;
-            ty = y.y;
-            tz = y.z;
+            tx = k * y.x;
+            ty = k * y.y;
+            tz = k * y.z;
             tw = w;
-            te1 = dot(y, ev1);
-            te2 = dot(y, ev2);
+            te1 = k * dot(y, ev1);
+            te2 = k * dot(y, ev2);
             tn = dot(y, n1);
         }
     }
-    const float2 K2 = bc(k), M4K = bc(-4.f / k);
+    // Per evaluation, with c = k (y.a) - 4/k and yu = (y.a)(x.n1) - (y.n1)(x.a):
+    //   t_re += gs c - R^-2 yu Re[G(1 + jkR)] / g-scaled,  t_im += gr c - R^-2 yu Im[...]
+    // i.e. the per-test-point combination -Q + jk P - (4j/k) S0 of the three sums, summed
+    // directly.  yu = c (x.n1)/k + (4 (x.n1)/k^2 - (y.n1)(x.a)) and R^-2 = k^2 (kR)^-2, so
+    // -R^-2 yu = (kR)^-2 [c (-k (x.n1)) + (y.n1) k^2 (x.a) - 4 (x.n1)].
+    const float2 M4K = bc(-4.f / k);
     float2 acc_re = bc(0.f), acc_im = bc(0.f);
     float self_acc = 0.f;
     const bool same = (f1 == f2);
@@ -354,62 +360,51 @@ __device__ __forceinline__ void mom_entry_fast(const float* __restrict__ verts,
         const V3<float> a = t.x * ev1 + t.y * ev2;
         const V3<float> x = A0 + a;
         const float xn = dot(x, n1), xa = dot(x, a);
-        const float2 X = bc(x.x), Y = bc(x.y), Z = bc(x.z), R1 = bc(t.x), R2 = bc(t.y), XN = bc(xn),
-                     NXA = bc(-xa);
-        float2 s0r = bc(0.f), s0i = bc(0.f), pr = bc(0.f), pi = bc(0.f), qr = bc(0.f), qi = bc(0.f);
+        const float2 X = bc(k * x.x), Y = bc(k * x.y), Z = bc(k * x.z), R1 = bc(t.x), R2 = bc(t.y),
+                     CN = bc(-k * xn), CA = bc(k * k * xa), C4 = bc(-4.f * xn);
+        float2 tr = bc(0.f), ti = bc(0.f);
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
             const float2 dx = sub2(X, yx[p]);
             const float2 dy = sub2(Y, yy[p]);
             const float2 dz = sub2(Z, yz[p]);
-            const float2 r2d = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
-            float2 rinv;
+            const float2 r2d = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));  // (kR)^2
+            float2 rinv;                                                 // (kR)^-1
             rinv.x = rsqrtf(r2d.x);
             rinv.y = rsqrtf(r2d.y);
-            const float2 kR = mul2(K2, mul2(r2d, rinv));
+            const float2 kR = mul2(r2d, rinv);
             float2 sn, cs;
             __sincosf(kR.x, &sn.x, &cs.x);
             __sincosf(kR.y, &sn.y, &cs.y);
             const float2 g = mul2(yw[p], rinv);
             const float2 gr = mul2(g, cs), gs = mul2(g, sn);  // G = gr - j gs
-            const float2 ya = fma2(R1, ye1[p], mul2(R2, ye2[p]));
-            const float2 yu = fma2(ya, XN, mul2(yn[p], NXA));
-            s0r = add2(s0r, gr);
-            s0i = add2(s0i, gs);
-            pr = fma2(gr, ya, pr);
-            pi = fma2(gs, ya, pi);
-            const float2 m = mul2(mul2(rinv, rinv), yu);
-            const float2 t1 = fma2(gs, kR, gr);        // Re G(1 + jkR)
-            const float2 t2 = sub2(mul2(gr, kR), gs);  // Im G(1 + jkR)
-            qr = fma2(m, t1, qr);
-            qi = fma2(m, t2, qi);
+            const float2 c = fma2(R1, ye1[p], fma2(R2, ye2[p], M4K));
+            const float2 nyu = fma2(c, CN, fma2(yn[p], CA, C4));  // -k^2 yu
+            const float2 m = mul2(mul2(rinv, rinv), nyu);         // -R^-2 yu
+            const float2 t1 = fma2(gs, kR, gr);                   // Re G(1 + jkR)
+            const float2 t2 = sub2(mul2(gr, kR), gs);             // Im G(1 + jkR)
+            tr = fma2(m, t1, fma2(gs, c, tr));
+            ti = fma2(m, t2, fma2(gr, c, ti));
         }
         if constexpr (TAIL) {
             // the odd source point, scalar: same algebra as one lane of the packed loop
-            const float dx = x.x - tx, dy = x.y - ty, dz = x.z - tz;
+            const float dx = k * x.x - tx, dy = k * x.y - ty, dz = k * x.z - tz;
             const float r2d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
             const float rinv = rsqrtf(r2d);
-            const float kR = k * (r2d * rinv);
+            const float kR = r2d * rinv;
             float sn, cs;
             __sincosf(kR, &sn, &cs);
             const float g = tw * rinv;
             const float gr = g * cs, gs = g * sn;
-            const float ya = fmaf(t.x, te1, t.y * te2);
-            const float yu = fmaf(ya, xn, -tn * xa);
-            s0r.x += gr;
-            s0i.x += gs;
-            pr.x = fmaf(gr, ya, pr.x);
-            pi.x = fmaf(gs, ya, pi.x);
-            const float m = rinv * rinv * yu;
-            qr.x = fmaf(m, fmaf(gs, kR, gr), qr.x);
-            qi.x = fmaf(m, fmaf(gr, kR, -gs), qi.x);
+            const float c = fmaf(t.x, te1, fmaf(t.y, te2, -4.f / k));
+            const float nyu = fmaf(c, -k * xn, fmaf(tn, k * k * xa, -4.f * xn));
+            const float m = rinv * rinv * nyu;
+            tr.x = fmaf(m, fmaf(gs, kR, gr), fmaf(gs, c, tr.x));
+            ti.x = fmaf(m, fmaf(gr, kR, -gs), fmaf(gr, c, ti.x));
         }
-        // t_re = -Qr + k Pi - (4/k) S0i,  t_im = -Qi + k Pr - (4/k) S0r   (Pi, S0i hold +sum gs)
-        const float2 t_re = sub2(fma2(K2, pi, mul2(M4K, s0i)), qr);
-        const float2 t_im = sub2(fma2(K2, pr, mul2(M4K, s0r)), qi);
         const float2 W1 = bc(w1);
-        acc_re = fma2(W1, t_re, acc_re);
-        acc_im = fma2(W1, t_im, acc_im);
+        acc_re = fma2(W1, tr, acc_re);
+        acc_im = fma2(W1, ti, acc_im);
         if (same) self_acc += w1 * xa;  // (x - A0) . (x - B0), B0 = 0
     }
     const float cc = c1 * c2;
