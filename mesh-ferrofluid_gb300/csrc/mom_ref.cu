@@ -342,10 +342,10 @@ __device__ __forceinline__ void mom_entry_fast(const float* __restrict__ verts,
             tn = dot(y, n1);
         }
     }
-    // Per evaluation, with c = k (y.a) - 4/k and yu = (y.a)(x.n1) - (y.n1)(x.a):
-    //   t_re += gs c - R^-2 yu Re[G(1 + jkR)] / g-scaled,  t_im += gr c - R^-2 yu Im[...]
-    // i.e. the per-test-point combination -Q + jk P - (4j/k) S0 of the three sums, summed
-    // directly.  yu = c (x.n1)/k + (4 (x.n1)/k^2 - (y.n1)(x.a)) and R^-2 = k^2 (kR)^-2, so
+    // Per evaluation, with c = k (y.a) - 4/k, yu = (y.a)(x.n1) - (y.n1)(x.a), m = -R^-2 yu and
+    // G = gr - j gs:  t_re += gs c + m Re[G(1 + jkR)],  t_im += gr c + m Im[G(1 + jkR)]
+    // (Re = gr + gs kR, Im = gr kR - gs), i.e. the per-test-point combination
+    // -Q + jk P - (4j/k) S0 of the three sums, summed directly.  yu = c (x.n1)/k + (4 (x.n1)/k^2 - (y.n1)(x.a)) and R^-2 = k^2 (kR)^-2, so
     // -R^-2 yu = (kR)^-2 [c (-k (x.n1)) + (y.n1) k^2 (x.a) - 4 (x.n1)].
     const float2 M4K = bc(-4.f / k);
     float2 acc_re = bc(0.f), acc_im = bc(0.f);
@@ -381,10 +381,10 @@ __device__ __forceinline__ void mom_entry_fast(const float* __restrict__ verts,
             const float2 c = fma2(R1, ye1[p], fma2(R2, ye2[p], M4K));
             const float2 nyu = fma2(c, CN, fma2(yn[p], CA, C4));  // -k^2 yu
             const float2 m = mul2(mul2(rinv, rinv), nyu);         // -R^-2 yu
-            const float2 t1 = fma2(gs, kR, gr);                   // Re G(1 + jkR)
-            const float2 t2 = sub2(mul2(gr, kR), gs);             // Im G(1 + jkR)
-            tr = fma2(m, t1, fma2(gs, c, tr));
-            ti = fma2(m, t2, fma2(gr, c, ti));
+            // m G(1 + jkR) + c G in the conjugate form (gr + j gs)(u + j m), u = m kR + c
+            const float2 u = fma2(m, kR, c);
+            tr = fma2(gs, u, fma2(m, gr, tr));
+            ti = sub2(fma2(gr, u, ti), mul2(m, gs));
         }
         if constexpr (TAIL) {
             // the odd source point, scalar: same algebra as one lane of the packed loop
@@ -399,8 +399,9 @@ __device__ __forceinline__ void mom_entry_fast(const float* __restrict__ verts,
             const float c = fmaf(t.x, te1, fmaf(t.y, te2, -4.f / k));
             const float nyu = fmaf(c, -k * xn, fmaf(tn, k * k * xa, -4.f * xn));
             const float m = rinv * rinv * nyu;
-            tr.x = fmaf(m, fmaf(gs, kR, gr), fmaf(gs, c, tr.x));
-            ti.x = fmaf(m, fmaf(gr, kR, -gs), fmaf(gr, c, ti.x));
+            const float u = fmaf(m, kR, c);
+            tr.x = fmaf(gs, u, fmaf(m, gr, tr.x));
+            ti.x = fmaf(gr, u, fmaf(-m, gs, ti.x));
         }
         const float2 W1 = bc(w1);
         acc_re = fma2(W1, tr, acc_re);
