@@ -389,6 +389,13 @@ int mb_blockdiag_matvec_c64(const float* z, const int64_t* desc, const int64_t* 
  * once as a CUDA graph and replay it (no host synchronisation inside a cycle; iterations
  * are counted in whole cycles).  Workspace: mb_gmres_blockdiag_workspace_bytes. */
 size_t mb_gmres_blockdiag_workspace_bytes(int64_t n_rows, int64_t m, int restart);
+/* Arnoldi steps each column took (while it was active, over all restart cycles) in the last
+ * mb_gmres_blockdiag_c64 / mb_gmres_multi_c64 call on `workspace`: int32 [m] into out
+ * (device or host memory; stream-ordered). */
+int mb_gmres_blockdiag_column_steps(const void* workspace, int64_t n_rows, int64_t m, int restart, int32_t* out,
+                                    void* stream);
+int mb_gmres_multi_column_steps(const void* workspace, int64_t n, int64_t m, int restart, int32_t* out,
+                                void* stream);
 int mb_gmres_blockdiag_c64(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh,
                            int64_t total_warps, int rows_per_warp, int nc, int64_t n_rows, const double* b,
                            double* x, int restart, int max_iters, double tol, int use_graph, void* workspace,

@@ -97,14 +97,20 @@ class MeshBatch:
         self.desc = None
         self.rows_per_warp = None
         self._goff = {}
+        self._descs = {}
 
     # -- layout --------------------------------------------------------------------------
+    def _desc_for(self, nc: int) -> torch.Tensor:
+        if nc not in self._descs:
+            d = self._desc_np.copy()
+            d[:, 5] = np.arange(self.n_mesh) * nc
+            self._descs[nc] = torch.tensor(d, device=self.device)
+        return self._descs[nc]
+
     def _set_nc(self, nc: int):
         if self.nc == nc:
             return
-        d = self._desc_np.copy()
-        d[:, 5] = np.arange(self.n_mesh) * nc
-        self.desc = torch.tensor(d, device=self.device)
+        self.desc = self._desc_for(nc)
         self.nc = nc
 
     def _warp_offsets(self, rows: int):
@@ -168,14 +174,18 @@ class MeshBatch:
         return B
 
     def matvec(self, z_flat: torch.Tensor, X: torch.Tensor, rows_per_warp: int | None = None,
-               out: torch.Tensor | None = None) -> torch.Tensor:
-        """Block-diagonal product Y = blockdiag(Z_i) X on the padded layout (complex64)."""
+               out: torch.Tensor | None = None, nc: int | None = None) -> torch.Tensor:
+        """Block-diagonal product Y = blockdiag(Z_i) X on the padded layout (complex64); ``nc``
+        columns per mesh (default: the excitation's)."""
         rows = rows_per_warp or self.rows_per_warp or 2
         goff = self._warp_offsets(rows)
+        nc = nc or self.nc
+        if X.shape[1] != self.n_mesh * nc:
+            raise ValueError(f"X must have n_mesh * nc = {self.n_mesh * nc} columns")
         if out is None:
             out = torch.zeros_like(X)
-        _lib.call("mb_blockdiag_matvec_c64", _lib.ptr(z_flat), _lib.ptr(self.desc), _lib.ptr(goff), self.n_mesh,
-                  int(goff[-1]), _lib.ptr(X), X.shape[1], self.nc, rows, _lib.ptr(out), _lib.stream_of(X))
+        _lib.call("mb_blockdiag_matvec_c64", _lib.ptr(z_flat), _lib.ptr(self._desc_for(nc)), _lib.ptr(goff),
+                  self.n_mesh, int(goff[-1]), _lib.ptr(X), X.shape[1], nc, rows, _lib.ptr(out), _lib.stream_of(X))
         return out
 
     def autotune(self, z_flat: torch.Tensor, candidates=(1, 2, 4, 8, 32), reps: int = 3) -> int:
@@ -219,5 +229,8 @@ class MeshBatch:
                   int(goff[-1]), rows, self.nc, self.n_rows, _lib.ptr(bb), _lib.ptr(X), int(restart), int(max_iters),
                   float(tol), 1 if use_graph else 0, _lib.ptr(workspace), workspace.numel(), ctypes.byref(info),
                   _lib.stream_of(bb))
+        steps = torch.empty(m, dtype=torch.int32, device=self.device)
+        _lib.call("mb_gmres_blockdiag_column_steps", _lib.ptr(workspace), self.n_rows, m, int(restart), _lib.ptr(steps),
+                  _lib.stream_of(bb))
         return X, {"iterations": info.iterations, "restarts": info.restarts, "max_rel_residual": info.rel_residual,
-                   "converged": info.status == 0}
+                   "converged": info.status == 0, "column_iterations": steps}

@@ -89,6 +89,8 @@ int zmat_edges_to_host(const float* verts, const int32_t* faces, const float* ar
                        const float* gwx, int nx, const float* gpy, const float* gwy, int ny, double k, int64_t nf,
                        float* z_dev, float* z_host, int chunks, cudaStream_t s);
 size_t gmres_blockdiag_workspace_bytes(int64_t n, int64_t m, int r);
+int gmres_multi_column_steps(const void* ws, int64_t n, int64_t m, int r, int32_t* out, cudaStream_t s);
+int gmres_blockdiag_column_steps(const void* ws, int64_t n, int64_t m, int r, int32_t* out, cudaStream_t s);
 int blockdiag_matvec(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
                      const float* x, int64_t ld, int nc, int rows, float* y, cudaStream_t s);
 int gmres_blockdiag(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
@@ -270,6 +272,18 @@ int mb_mom_zmat_rwg_to_host_c64(const float* verts, int64_t n_verts, const int32
     if (cudaMemcpyAsync(z_host, z_dev, (size_t)n_edges * n_edges * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess)
         return check_launch("zmat to host: copy");
     return MB_OK;
+}
+
+int mb_gmres_multi_column_steps(const void* workspace, int64_t n, int64_t m, int restart, int32_t* out,
+                                void* stream) {
+    MB_REQUIRE(workspace && out && n > 0 && m > 0 && restart >= 1, "bad arguments");
+    return gmres_multi_column_steps(workspace, n, m, restart, out, as_stream(stream));
+}
+
+int mb_gmres_blockdiag_column_steps(const void* workspace, int64_t n_rows, int64_t m, int restart, int32_t* out,
+                                    void* stream) {
+    MB_REQUIRE(workspace && out && n_rows > 0 && m > 0 && restart >= 1, "bad arguments");
+    return gmres_blockdiag_column_steps(workspace, n_rows, m, restart, out, as_stream(stream));
 }
 
 #define MB_RHS_FE(SFX, T)                                                                             \

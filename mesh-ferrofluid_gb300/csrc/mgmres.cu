@@ -51,6 +51,7 @@ struct MgWork {
     float* scale;   // [m] 1 / |v| of the next basis vector (0 for inactive columns)
     int* count;     // [4]
     int* status;    // [4] mbarrier time-outs of the streamed kernels (0 = none)
+    int* colsteps;  // [m] Arnoldi steps each column took (while active), over all cycles
 };
 
 static size_t a256(size_t b) { return (b + 255) & ~size_t(255); }
@@ -83,6 +84,7 @@ static size_t mg_layout(int64_t n, int64_t m, int r, size_t prod_ws, void* base,
     W->scale = static_cast<float*>(take(4 * m));
     W->count = static_cast<int*>(take(16));
     W->status = static_cast<int*>(take(16));
+    W->colsteps = static_cast<int*>(take(4 * m));
     return off;
 }
 
@@ -457,9 +459,10 @@ __global__ void mg_accum_h(const double* __restrict__ hc, int nb, int j, int r, 
 __global__ void mg_givens(double* __restrict__ H, double* __restrict__ cs, double* __restrict__ sn,
                           double* __restrict__ g, const double* __restrict__ hn2, const double* __restrict__ bnorm,
                           int j, int r, int64_t m, double tol, int* __restrict__ active, int* __restrict__ jend,
-                          int* __restrict__ count, float* __restrict__ scale) {
+                          int* __restrict__ count, float* __restrict__ scale, int* __restrict__ colsteps) {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m || !active[c]) return;
+    colsteps[c] += 1;
     auto hre = [&](int i) -> double& { return H[2 * (((int64_t)i * r + j) * m + c)]; };
     auto him = [&](int i) -> double& { return H[2 * (((int64_t)i * r + j) * m + c) + 1]; };
     const double hn = sqrt(hn2[c]);
@@ -1006,6 +1009,7 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
     cudaMemsetAsync(W.y32, 0, 8 * (size_t)nm, s);  // rows a product does not write stay 0
     cudaMemsetAsync(W.bnorm, 0, 8 * mp, s);
     cudaMemsetAsync(W.status, 0, 16, s);
+    cudaMemsetAsync(W.colsteps, 0, 4 * mp, s);
     mg_colnorm2<<<rgrid, rblk, 0, s>>>(reinterpret_cast<const double2*>(b), n, m, W.bnorm);
     cudaMemcpyAsync(hb.data(), W.bnorm, 8 * mp, cudaMemcpyDeviceToHost, s);
     if ((rc = mg_sync(s, "gmres_multi |b|"))) return rc;
@@ -1037,7 +1041,7 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
         mg_accum_h<<<(unsigned)((nb * mp + 255) / 256), 256, 0, st>>>(W.hc, nb, j, r, mp, W.H);
         cudaMemsetAsync(W.count, 0, 4, st);
         mg_givens<<<cb, 32, 0, st>>>(W.H, W.cs, W.sn, W.g, W.hn, W.bnorm, j, r, mp, tol, W.active, W.jend, W.count,
-                                     W.scale);
+                                     W.scale, W.colsteps);
         mg_scale_cols<<<rgrid, rblk, 0, st>>>(W.w, W.scale, crow, n, mp, W.V + (size_t)(j + 1) * nm);
         return check_launch("gmres_multi step");
     };
@@ -1119,6 +1123,23 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
     return MB_OK;
 }
 
+// Per-column Arnoldi step counts of the last solve that used `workspace` (int32 [m], to a
+// device or host pointer).
+static int column_steps(const void* workspace, int64_t n, int64_t m, int r, size_t prod_ws, int32_t* out,
+                        cudaStream_t s) {
+    MgWork W;
+    mg_layout(n, padded_width(m), r, prod_ws, const_cast<void*>(workspace), &W);
+    const cudaError_t e = cudaMemcpyAsync(out, W.colsteps, 4 * (size_t)m, cudaMemcpyDefault, s);
+    if (e != cudaSuccess) return set_error(MB_ERR_CUDA, "column steps: %s", cudaGetErrorString(e));
+    return MB_OK;
+}
+int gmres_multi_column_steps(const void* ws, int64_t n, int64_t m, int r, int32_t* out, cudaStream_t s) {
+    return column_steps(ws, n, m, r, cgemm_workspace_bytes(n, padded_width(m)), out, s);
+}
+int gmres_blockdiag_column_steps(const void* ws, int64_t n, int64_t m, int r, int32_t* out, cudaStream_t s) {
+    return column_steps(ws, n, m, r, 128 * (size_t)std::max<int64_t>(m, 1), out, s);
+}
+
 int gmres_multi(const float* z_hi, const float* z_lo, int64_t n, const double* b, double* x, int64_t m, int r,
                 int max_iters, double tol, void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out,
                 double* max_relres_out, int* status_out, cudaStream_t s) {
@@ -1143,7 +1164,7 @@ int gmres_blockdiag(const float* z, const int64_t* desc, const int64_t* goff, in
                     int64_t* cycles_out, double* max_relres_out, int* status_out, cudaStream_t s) {
     const int64_t m = (int64_t)n_mesh * nc, mp = padded_width(m);
     MgWork W;
-    const size_t map_bytes = sizeof(CUtensorMap) * (size_t)std::max(n_mesh, 1);
+    const size_t map_bytes = 128 * (size_t)std::max<int64_t>(m, 1);  // >= n_mesh tensor maps
     if (ws_bytes < mg_layout(n_rows, mp, r, map_bytes, nullptr, &W)) return set_error(MB_ERR_ARG, "workspace too small");
     mg_layout(n_rows, mp, r, map_bytes, workspace, &W);
     int* status = W.status;

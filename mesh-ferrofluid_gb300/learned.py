@@ -6,8 +6,9 @@ direction, the normals of the adjacent triangles, ka, the incidence direction an
 polarisation, the incident phase at the midpoint and the excitation coefficient b_e
 (normalised per incidence).  Network: a 32 -> 128 embedding, six layers
 h' = relu([h, mean_nbr h] W + b) with hidden width 128, and a 128 -> 2 read-out giving the
-edge current J_e (normalised; its scale is fitted with one product: alpha = (Z x)^H b /
-|Z x|^2).  Weights and activations are BF16, every product is accumulated in FP32, master
+edge current J_e (normalised).  The initial guess of a column is the residual-minimising
+combination of the real and imaginary parts of the predictions for all incidences of its
+mesh (``subspace_guess``: a least-squares fit over a 2 nc-vector learned subspace).  Weights and activations are BF16, every product is accumulated in FP32, master
 weights and Adam moments are FP32; forward and backward run on this library's kernels
 (``mb_gnn_*``).  The prediction is used as the GMRES initial guess; plain GMRES from zero
 stays the fallback and the judge of the result.
@@ -89,6 +90,95 @@ def node_features(g: EdgeGraph, k: float, khat, pol, b: torch.Tensor) -> torch.T
     out = torch.zeros((E, F_IN), dtype=torch.bfloat16, device=dev)
     out[:, :N_FEATURES] = x.to(torch.bfloat16)
     return out
+
+
+@dataclass
+class BatchGraph:
+    """The edge graphs of a batch of meshes back to back (edge ids local to each mesh)."""
+    nbr: torch.Tensor       # [S, 4] int32, local ids, -1 where absent
+    mid: torch.Tensor       # [S, 3]
+    length_n: torch.Tensor  # [S] edge length / the mesh's mean edge length
+    tdir: torch.Tensor      # [S, 3]
+    n1: torch.Tensor        # [S, 3]
+    n2: torch.Tensor        # [S, 3]
+    start: torch.Tensor     # [n_mesh + 1] int64, first edge of each mesh
+    n_edges: List[int]
+
+
+def batch_graph(graphs) -> BatchGraph:
+    """Concatenate the edge graphs of a batch's meshes (in the batch's mesh order)."""
+    graphs = list(graphs)
+    dev = graphs[0].mid.device
+    ne = [g.n_edges for g in graphs]
+    start = torch.tensor(np.concatenate([[0], np.cumsum(ne)]).astype(np.int64), device=dev)
+    return BatchGraph(torch.cat([g.nbr for g in graphs]).contiguous(), torch.cat([g.mid for g in graphs]),
+                      torch.cat([g.length / g.length.mean() for g in graphs]), torch.cat([g.tdir for g in graphs]),
+                      torch.cat([g.n1 for g in graphs]), torch.cat([g.n2 for g in graphs]), start, ne)
+
+
+def batch_node_features(bg: BatchGraph, ks, khat, pol, B: torch.Tensor, nc: int):
+    """The features of ``node_features`` for every (mesh, incidence) column of a batch's
+    excitation block B [n_rows, n_mesh * nc] in one pass.  ks [n_mesh]; khat, pol
+    [n_mesh, nc, 3].  Nodes run mesh by mesh, incidence by incidence, edge by edge.
+    Returns (x0 [N, 32] bf16, nbr [N, 4] int32 node ids, flat [N] int64 positions in B)."""
+    dev = bg.mid.device
+    n_mesh = len(bg.n_edges)
+    E = torch.tensor(bg.n_edges, dtype=torch.int64, device=dev)
+    blk = E * nc
+    bstart = torch.cat([torch.zeros(1, dtype=torch.int64, device=dev), torch.cumsum(blk, 0)])
+    n = int(bstart[-1])
+    node = torch.arange(n, device=dev)
+    mesh = torch.repeat_interleave(torch.arange(n_mesh, device=dev), blk)
+    t = node - bstart[mesh]
+    em = E[mesh]
+    r = t // em
+    e = t - r * em
+    g = bg.start[mesh] + e
+    col = mesh * nc + r
+    flat = e * B.shape[1] + col
+    b = B.reshape(-1)[flat].to(torch.complex64)
+    sq = torch.zeros(n_mesh * nc, dtype=torch.float32, device=dev).index_add_(0, col, b.abs() ** 2)
+    rms = (sq / E.repeat_interleave(nc).to(torch.float32)).sqrt().clamp_min(1e-30)
+    bs = b / rms[col]
+    kt = torch.as_tensor(np.asarray(ks, np.float32), device=dev)[mesh]
+    kh = torch.as_tensor(np.asarray(khat, np.float32), device=dev).reshape(-1, 3)[col]
+    po = torch.as_tensor(np.asarray(pol, np.float32), device=dev).reshape(-1, 3)[col]
+    mid, tdir = bg.mid[g], bg.tdir[g]
+    ph = kt * (mid * kh).sum(1)
+    x = torch.cat([mid, bg.length_n[g][:, None], tdir, bg.n1[g], bg.n2[g], (kt / 8.0)[:, None], kh, po,
+                   torch.cos(ph)[:, None], torch.sin(ph)[:, None], bs.real[:, None], bs.imag[:, None],
+                   (tdir * po).sum(1, keepdim=True)], 1)
+    out = torch.zeros((n, F_IN), dtype=torch.bfloat16, device=dev)
+    out[:, :N_FEATURES] = x.to(torch.bfloat16)
+    nl = bg.nbr[g].long()
+    base = bstart[mesh] + r * em
+    nbr = torch.where(nl >= 0, base[:, None] + nl, torch.full_like(nl, -1)).to(torch.int32).contiguous()
+    return out, nbr, flat
+
+
+def subspace_guess(bt, Z: torch.Tensor, B: torch.Tensor, pred: torch.Tensor, flat: torch.Tensor, nc: int,
+                   reg: float = 1e-8) -> torch.Tensor:
+    """Initial guess of every column of a MeshBatch: the combination of the real and imaginary
+    parts of the network's predictions for all nc incidences of the same mesh (2 nc vectors)
+    that minimises that column's residual |Z x - b| -- a least-squares fit over a small learned
+    subspace (one block-diagonal product with 2 nc columns per mesh, then a 2 nc x 2 nc normal
+    system per mesh in FP64).  Returns X0 [n_rows, n_mesh * nc] complex128, rows beyond E_i 0."""
+    n_rows, m = B.shape
+    n_mesh = bt.n_mesh
+    P = torch.zeros((n_rows, m), dtype=torch.complex64, device=B.device)
+    P.view(-1)[flat] = pred.to(torch.complex64)
+    P3 = P.view(n_rows, n_mesh, nc)
+    W = torch.cat([P3.real, P3.imag], 2).to(torch.complex64).contiguous()  # [n_rows, n_mesh, 2 nc]
+    ZW = bt.matvec(Z, W.view(n_rows, n_mesh * 2 * nc), nc=2 * nc).view(n_rows, n_mesh, 2 * nc)
+    A = ZW.permute(1, 0, 2).to(torch.complex128)
+    Bm = B.view(n_rows, n_mesh, nc).permute(1, 0, 2).to(torch.complex128)
+    G = A.mH @ A
+    R = A.mH @ Bm
+    lam = reg * G.diagonal(dim1=1, dim2=2).real.sum(-1) / (2 * nc) + 1e-300
+    G = G + lam[:, None, None] * torch.eye(2 * nc, dtype=G.dtype, device=G.device)
+    alpha = torch.linalg.solve(G, R)  # [n_mesh, 2 nc, nc]
+    X0 = W.permute(1, 0, 2).to(torch.complex128) @ alpha
+    return X0.permute(1, 0, 2).reshape(n_rows, m).contiguous()
 
 
 class EdgeGNN:

@@ -553,8 +553,11 @@ def gmres_multi(z_split, B, X0=None, restart: int = 50, max_iters: int = 2000, t
     _lib.call("mb_gmres_multi_c64", _lib.ptr(hi), _lib.ptr(lo), n, _lib.ptr(bb), _lib.ptr(xx), m, int(restart),
               int(max_iters), float(tol), _lib.ptr(workspace), workspace.numel(), __import__("ctypes").byref(info),
               _lib.stream_of(hi))
+    steps = torch.empty(m, dtype=torch.int32, device=bb.device)
+    _lib.call("mb_gmres_multi_column_steps", _lib.ptr(workspace), n, m, int(restart), _lib.ptr(steps),
+              _lib.stream_of(bb))
     return xx, {"iterations": info.iterations, "restarts": info.restarts, "max_rel_residual": info.rel_residual,
-                "converged": info.status == 0}
+                "converged": info.status == 0, "column_iterations": steps}
 
 
 def matvec(Z, v):
