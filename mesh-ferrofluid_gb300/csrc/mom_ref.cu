@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "packed.cuh"
 
 namespace mb {
 
@@ -243,30 +244,7 @@ __global__ void __launch_bounds__(128) mom_ref_zmat_rwg_kernel(
 // rsqrt, sin and cos.  The entry is then
 //   c1 c2 sum_i w_i [ -Q + jk P - (4j/k) S0 ]  (+ self term), identical to mom_entry.
 // ---------------------------------------------------------------------------------------
-typedef unsigned long long u64;
-__device__ __forceinline__ u64 pk(float2 a) { return *reinterpret_cast<u64*>(&a); }
-__device__ __forceinline__ float2 upk(u64 a) { return *reinterpret_cast<float2*>(&a); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
-    u64 d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)), "l"(pk(c)));
-    return upk(d);
-}
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
-    u64 d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
-    return upk(d);
-}
-__device__ __forceinline__ float2 add2(float2 a, float2 b) {
-    u64 d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
-    return upk(d);
-}
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
-    u64 d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk(a)), "l"(pk(b)));
-    return upk(d);
-}
-__device__ __forceinline__ float2 bc(float v) { return make_float2(v, v); }
+
 
 // Rule tables staged in shared memory: test (r1, r2, w_a w_b r1), source
 // (r3, r4, w_a w_b r3 / (4 pi)); index b*n + a as in the reference loops (:410-415).

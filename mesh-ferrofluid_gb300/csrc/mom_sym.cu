@@ -22,6 +22,7 @@
 
 #include "closed_form.cuh"
 #include "common.cuh"
+#include "packed.cuh"
 
 namespace mb {
 
@@ -137,6 +138,141 @@ __device__ __forceinline__ void sym_regular_pair(const T* __restrict__ verts, co
             const T re = cc * (-k * fi + inv_k4 * t0i);
             const T im = cc * (k * fr - inv_k4 * t0r);
             add_c<T>(z + 2 * (row * n_edges + __ldg(fei + 3 * q + n)), re, im);
+        }
+    }
+}
+
+// float separated pairs, the same entries with packed arithmetic: source points in f32x2
+// pairs (3 pairs + the seventh point scalar), coordinates scaled by k so kR = |k x - k y|
+// feeds the SFU sine / cosine directly, the weight k w so g = w / R = (k w) / (kR); the
+// source moments are accumulated as k sum G y and the 1/k and the sign of Im G (G = gr - j gs)
+// are applied once per test point / at the end.
+template <>
+__device__ __forceinline__ void sym_regular_pair<float>(const float* __restrict__ verts,
+                                                        const int32_t* __restrict__ faces,
+                                                        const int32_t* __restrict__ fei, int64_t n_edges, float k,
+                                                        int64_t p, int64_t q, const float (*s_b)[4],
+                                                        float* __restrict__ z) {
+    if (shared_vertices(faces, p, q) != 0) return;  // done by the FP64 near-pair kernel
+    const V3<float> o = load3(verts, __ldg(faces + 3 * q));
+    V3<float> A[3], B[3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+        A[v] = load3(verts, __ldg(faces + 3 * p + v)) - o;
+        B[v] = load3(verts, __ldg(faces + 3 * q + v)) - o;
+    }
+    float cm[3], cn[3], ap, aq;
+    rwg_consts<float>(faces, p, A, cm, &ap);
+    rwg_consts<float>(faces, q, B, cn, &aq);
+    float2 yx[3], yy[3], yz[3], yw[3];
+    float tx, ty, tz, tw;
+#pragma unroll
+    for (int j = 0; j < 7; ++j) {
+        const V3<float> y = s_b[j][0] * B[0] + s_b[j][1] * B[1] + s_b[j][2] * B[2];
+        const float w = s_b[j][3] * aq * float(kInv4Pi) * k;
+        if (j < 6) {
+            (reinterpret_cast<float*>(&yx[j / 2]) + (j & 1))[0] = k * y.x;
+            (reinterpret_cast<float*>(&yy[j / 2]) + (j & 1))[0] = k * y.y;
+            (reinterpret_cast<float*>(&yz[j / 2]) + (j & 1))[0] = k * y.z;
+            (reinterpret_cast<float*>(&yw[j / 2]) + (j & 1))[0] = w;
+        } else {
+            tx = k * y.x;
+            ty = k * y.y;
+            tz = k * y.z;
+            tw = w;
+        }
+    }
+    // per pair: t0 = sum_i w_i S0_i, tx = sum_i w_i x_i S0_i, ty' = sum_i w_i S1'_i,
+    // txy' = sum_i w_i x_i . S1'_i with S1' = k S1 (S0 = sum_j G, S1 = sum_j G y)
+    float t0r = 0.f, t0i = 0.f, txr[3] = {0.f, 0.f, 0.f}, txi[3] = {0.f, 0.f, 0.f};
+    float tyr[3] = {0.f, 0.f, 0.f}, tyi[3] = {0.f, 0.f, 0.f}, txyr = 0.f, txyi = 0.f;
+#pragma unroll 1
+    for (int i = 0; i < 7; ++i) {
+        const V3<float> x = s_b[i][0] * A[0] + s_b[i][1] * A[1] + s_b[i][2] * A[2];
+        const float wi = s_b[i][3] * ap;
+        const float2 X = bc(k * x.x), Y = bc(k * x.y), Zc = bc(k * x.z);
+        float2 s0r = bc(0.f), s0s = bc(0.f), sxr = bc(0.f), sxs = bc(0.f), syr = bc(0.f), sys = bc(0.f),
+               szr = bc(0.f), szs = bc(0.f);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const float2 dx = sub2(X, yx[j]);
+            const float2 dy = sub2(Y, yy[j]);
+            const float2 dz = sub2(Zc, yz[j]);
+            const float2 r2d = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));  // (kR)^2
+            float2 rinv;
+            rinv.x = rsqrtf(r2d.x);
+            rinv.y = rsqrtf(r2d.y);
+            const float2 kR = mul2(r2d, rinv);
+            float2 sn, cs;
+            __sincosf(kR.x, &sn.x, &cs.x);
+            __sincosf(kR.y, &sn.y, &cs.y);
+            const float2 g = mul2(yw[j], rinv);
+            const float2 gr = mul2(g, cs), gs = mul2(g, sn);  // G = gr - j gs
+            s0r = add2(s0r, gr);
+            s0s = add2(s0s, gs);
+            sxr = fma2(gr, yx[j], sxr);
+            sxs = fma2(gs, yx[j], sxs);
+            syr = fma2(gr, yy[j], syr);
+            sys = fma2(gs, yy[j], sys);
+            szr = fma2(gr, yz[j], szr);
+            szs = fma2(gs, yz[j], szs);
+        }
+        float a0r = s0r.x + s0r.y, a0s = s0s.x + s0s.y;
+        float a1r[3] = {sxr.x + sxr.y, syr.x + syr.y, szr.x + szr.y};
+        float a1s[3] = {sxs.x + sxs.y, sys.x + sys.y, szs.x + szs.y};
+        {
+            // the seventh source point, scalar
+            const float dx = k * x.x - tx, dy = k * x.y - ty, dz = k * x.z - tz;
+            const float r2d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            const float rinv = rsqrtf(r2d);
+            const float kR = r2d * rinv;
+            float sn, cs;
+            __sincosf(kR, &sn, &cs);
+            const float g = tw * rinv;
+            const float gr = g * cs, gs = g * sn;
+            a0r += gr;
+            a0s += gs;
+            a1r[0] = fmaf(gr, tx, a1r[0]);
+            a1s[0] = fmaf(gs, tx, a1s[0]);
+            a1r[1] = fmaf(gr, ty, a1r[1]);
+            a1s[1] = fmaf(gs, ty, a1s[1]);
+            a1r[2] = fmaf(gr, tz, a1r[2]);
+            a1s[2] = fmaf(gs, tz, a1s[2]);
+        }
+        // Im G = -gs: the imaginary sums enter with a minus sign
+        t0r = fmaf(wi, a0r, t0r);
+        t0i = fmaf(-wi, a0s, t0i);
+        const float xs[3] = {x.x, x.y, x.z};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            txr[a] = fmaf(wi * xs[a], a0r, txr[a]);
+            txi[a] = fmaf(-wi * xs[a], a0s, txi[a]);
+            tyr[a] = fmaf(wi, a1r[a], tyr[a]);
+            tyi[a] = fmaf(-wi, a1s[a], tyi[a]);
+        }
+        txyr = fmaf(wi, xs[0] * a1r[0] + xs[1] * a1r[1] + xs[2] * a1r[2], txyr);
+        txyi = fmaf(-wi, xs[0] * a1s[0] + xs[1] * a1s[1] + xs[2] * a1s[2], txyi);
+    }
+    const float ik = 1.f / k;
+    const V3<float> Txr = v3<float>(txr[0], txr[1], txr[2]), Txi = v3<float>(txi[0], txi[1], txi[2]);
+    const V3<float> Tyr = v3<float>(tyr[0] * ik, tyr[1] * ik, tyr[2] * ik);
+    const V3<float> Tyi = v3<float>(tyi[0] * ik, tyi[1] * ik, tyi[2] * ik);
+    txyr *= ik;
+    txyi *= ik;
+    const float inv_k4 = 4.f / k;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        const float amr = dot(A[m], Tyr), ami = dot(A[m], Tyi);
+        const int64_t row = __ldg(fei + 3 * p + m);
+#pragma unroll
+        for (int n = 0; n < 3; ++n) {
+            const float ab = dot(A[m], B[n]);
+            const float fr = txyr - dot(B[n], Txr) - amr + ab * t0r;  // int int (x-A_m).(y-B_n) G
+            const float fi = txyi - dot(B[n], Txi) - ami + ab * t0i;
+            const float cc = cm[m] * cn[n];
+            const float re = cc * (-k * fi + inv_k4 * t0i);
+            const float im = cc * (k * fr - inv_k4 * t0r);
+            add_c<float>(z + 2 * (row * n_edges + __ldg(fei + 3 * q + n)), re, im);
         }
     }
 }
