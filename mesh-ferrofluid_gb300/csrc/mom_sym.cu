@@ -310,31 +310,76 @@ __device__ __forceinline__ void sym_near_pair(const T* __restrict__ verts, const
     rwg_consts<double>(faces, p, A, cm, &ap);
     rwg_consts<double>(faces, q, B, cn, &aq);
     const double inv4pi = kInv4Pi;
-    double accr[3][3] = {}, acci[3][3] = {};
+    // moments over the test points (FP64): t0 = sum_i w_i g0_i, tx = sum_i w_i x_i g0_i,
+    // ty = sum_i w_i gy_i, txy = sum_i w_i x_i . gy_i, with g0 = int G, gy = int G y over q
+    double t0r = 0, t0i = 0, txyr = 0, txyi = 0;
+    V3<double> txr = v3<double>(0, 0, 0), txi = v3<double>(0, 0, 0), tyr = v3<double>(0, 0, 0),
+               tyi = v3<double>(0, 0, 0);
     for (int i = 0; i < 7; ++i) {
         const V3<double> x = c_d7[i][0] * A[0] + c_d7[i][1] * A[1] + c_d7[i][2] * A[2];
         double g0r = 0, g0i = 0;
         V3<double> gyr = v3<double>(0, 0, 0), gyi = v3<double>(0, 0, 0);
-        for (int j = 0; j < 7; ++j) {
-            const V3<double> y = c_d7[j][0] * B[0] + c_d7[j][1] * B[1] + c_d7[j][2] * B[2];
-            const V3<double> dd = x - y;
-            const double R = sqrt(dot(dd, dd));
-            double gr, gi;
-            if (R < 1e-300) {  // coincident points of the self pair: limit of the smooth part
-                gr = 0.0;
-                gi = -k * inv4pi;
-            } else {
-                double sn, cs;
-                sincos(k * R, &sn, &cs);
-                const double sh = sin(0.5 * k * R);
-                gr = -2.0 * sh * sh / R * inv4pi;  // (cos kR - 1) / (4 pi R)
-                gi = -sn / R * inv4pi;
+        if constexpr (sizeof(T) == 4) {
+            // complex64 output: the smooth part (e^{-jkR} - 1) / (4 pi R) in FP32 (point
+            // differences taken in FP64, moments relative to B0), the singular 1/R part below
+            // in FP64 and closed form
+            const float kf = (float)k;
+            float s0r = 0.f, s0i = 0.f, syr[3] = {0.f, 0.f, 0.f}, syi[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+            for (int j = 0; j < 7; ++j) {
+                const V3<double> y = c_d7[j][0] * B[0] + c_d7[j][1] * B[1] + c_d7[j][2] * B[2];
+                const V3<double> dd = x - y;
+                const float dx = (float)dd.x, dy = (float)dd.y, dz = (float)dd.z;
+                const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                const float wj = (float)(c_d7[j][3] * aq * inv4pi);
+                float gr, gi;
+                if (r2 <= 0.f) {  // coincident points of the self pair: limit of the smooth part
+                    gr = 0.f;
+                    gi = -kf * wj;
+                } else {
+                    const float rinv = rsqrtf(r2);
+                    const float kR = kf * (r2 * rinv);
+                    float sn, cs, sh, ch;
+                    __sincosf(kR, &sn, &cs);
+                    __sincosf(0.5f * kR, &sh, &ch);
+                    gr = -2.f * sh * sh * rinv * wj;  // (cos kR - 1) / R without cancellation
+                    gi = -sn * rinv * wj;
+                }
+                const float yl[3] = {(float)(y.x - B[0].x), (float)(y.y - B[0].y), (float)(y.z - B[0].z)};
+                s0r += gr;
+                s0i += gi;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    syr[a] = fmaf(gr, yl[a], syr[a]);
+                    syi[a] = fmaf(gi, yl[a], syi[a]);
+                }
             }
-            const double wj = c_d7[j][3] * aq;
-            g0r += wj * gr;
-            g0i += wj * gi;
-            gyr = gyr + (wj * gr) * y;
-            gyi = gyi + (wj * gi) * y;
+            g0r = s0r;
+            g0i = s0i;
+            gyr = v3<double>(syr[0], syr[1], syr[2]) + g0r * B[0];
+            gyi = v3<double>(syi[0], syi[1], syi[2]) + g0i * B[0];
+        } else {
+            for (int j = 0; j < 7; ++j) {
+                const V3<double> y = c_d7[j][0] * B[0] + c_d7[j][1] * B[1] + c_d7[j][2] * B[2];
+                const V3<double> dd = x - y;
+                const double R = sqrt(dot(dd, dd));
+                double gr, gi;
+                if (R < 1e-300) {  // coincident points of the self pair: limit of the smooth part
+                    gr = 0.0;
+                    gi = -k * inv4pi;
+                } else {
+                    double sn, cs;
+                    sincos(k * R, &sn, &cs);
+                    const double sh = sin(0.5 * k * R);
+                    gr = -2.0 * sh * sh / R * inv4pi;  // (cos kR - 1) / (4 pi R)
+                    gi = -sn / R * inv4pi;
+                }
+                const double wj = c_d7[j][3] * aq;
+                g0r += wj * gr;
+                g0i += wj * gi;
+                gyr = gyr + (wj * gr) * y;
+                gyi = gyi + (wj * gi) * y;
+            }
         }
         double I1;
         V3<double> Iv;
@@ -342,25 +387,28 @@ __device__ __forceinline__ void sym_near_pair(const T* __restrict__ verts, const
         g0r += inv4pi * I1;
         gyr = gyr + inv4pi * (Iv + I1 * x);
         const double wi = c_d7[i][3] * ap;
-#pragma unroll
-        for (int m = 0; m < 3; ++m) {
-            const V3<double> xm = x - A[m];
-#pragma unroll
-            for (int n = 0; n < 3; ++n) {
-                const double fr = dot(xm, gyr - g0r * B[n]);
-                const double fi = dot(xm, gyi - g0i * B[n]);
-                const double cc = cm[m] * cn[n];
-                accr[m][n] += wi * cc * (-k * fi + 4.0 / k * g0i);
-                acci[m][n] += wi * cc * (k * fr - 4.0 / k * g0r);
-            }
-        }
+        t0r += wi * g0r;
+        t0i += wi * g0i;
+        txr = txr + (wi * g0r) * x;
+        txi = txi + (wi * g0i) * x;
+        tyr = tyr + wi * gyr;
+        tyi = tyi + wi * gyi;
+        txyr += wi * dot(x, gyr);
+        txyi += wi * dot(x, gyi);
     }
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
         const int64_t row = fei[3 * p + m];
+        const double amr = dot(A[m], tyr), ami = dot(A[m], tyi);
 #pragma unroll
-        for (int n = 0; n < 3; ++n)
-            add_c<T>(z + 2 * (row * n_edges + fei[3 * q + n]), (T)accr[m][n], (T)acci[m][n]);
+        for (int n = 0; n < 3; ++n) {
+            const double ab = dot(A[m], B[n]);
+            const double fr = txyr - dot(B[n], txr) - amr + ab * t0r;  // sum_i w_i (x - A_m).(gy - g0 B_n)
+            const double fi = txyi - dot(B[n], txi) - ami + ab * t0i;
+            const double cc = cm[m] * cn[n];
+            add_c<T>(z + 2 * (row * n_edges + fei[3 * q + n]), (T)(cc * (-k * fi + 4.0 / k * t0i)),
+                     (T)(cc * (k * fr - 4.0 / k * t0r)));
+        }
     }
 }
 
