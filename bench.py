@@ -1207,10 +1207,9 @@ def main():
             a = pkg.utils.compute_face_areas(d_verts, d_faces).contiguous()
             nn = pkg.utils.compute_face_normals(d_verts, d_faces).contiguous()
             if sym:
-                Z.zero_()
+                # test faces in 16 ranges; finished Z rows drained to host while the next range runs
                 M.assemble_Z_rwg_sym(d_verts, d_faces, d_fei, n_edges, k, out=Z, pairs=near,
-                                     check_indices=False)
-                h_Z.copy_(Z, non_blocking=True)
+                                     check_indices=False, out_host=h_Z, chunks=16)
             else:
                 # Z rows assembled in 16 ranges, each range's copy to host overlapping the next
                 M.assemble_Z_rwg(d_verts, d_faces, a, nn, d_fei, n_edges, *d_rules, k, out=Z,
@@ -1232,8 +1231,9 @@ def main():
         line["e2e"] = {"value": world * pairs / (e2e_ms / 1e3), "unit": "pairs/s",
                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h_Z.numel() * 8,
                        "ms_per_step": e2e_ms, "steps": e2e_steps,
-                       "path": ("mesh_MOM_3d.assemble_Z_rwg_sym (C ABI mb_mom_sym_zmat_rwg_c64 + "
-                                "mb_mom_sym_near_c64)" if sym else
+                       "path": ("mesh_MOM_3d.assemble_Z_rwg_sym(out_host=...) (C ABI "
+                                "mb_mom_sym_zmat_rwg_to_host_c64: test faces in 16 ranges, finished Z rows "
+                                "written to host memory while the next range is assembled)" if sym else
                                 "mesh_MOM_3d.assemble_Z_rwg(out_host=...) (C ABI mb_mom_zmat_rwg_to_host_c64: "
                                 "Z rows in 16 ranges, each range's D2H overlapping the next range's assembly)")
                                + ", pinned host buffers, H2D inputs + Z D2H inside the timed region"}

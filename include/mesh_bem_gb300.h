@@ -182,6 +182,15 @@ int mb_mom_sym_near_c128(const double* verts, int64_t n_verts, const int32_t* fa
                          int64_t n_faces, const int32_t* face_edge_indices, int64_t n_edges,
                          const int32_t* pairs, int64_t n_pairs, double wavenumber, double* z,
                          void* stream);
+/* The whole symmetric-rule Z (complex64: separated pairs + the near pairs, sorted by test
+ * face as mb_near_pairs / near_pairs give them) into pinned host memory z_host [E, E] with the
+ * copy overlapped: test faces are assembled in `chunks` ranges into the device scratch z_dev
+ * [E, E], and after each range the Z rows whose faces are all done are written to z_host by a
+ * drain kernel on a second stream.  The calling stream waits for the last row. */
+int mb_mom_sym_zmat_rwg_to_host_c64(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                                    const int32_t* face_edge_indices, int64_t n_edges, double wavenumber,
+                                    const int32_t* pairs, int64_t n_pairs, float* z_dev, float* z_host,
+                                    int chunks, void* stream);
 int mb_mom_sym_rhs_rwg_c64(const float* verts, int64_t n_verts, const int32_t* faces,
                            int64_t n_faces, const int32_t* face_edge_indices, int64_t n_edges,
                            const double* waves, int n_rhs, float* rhs, void* stream);

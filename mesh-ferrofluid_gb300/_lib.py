@@ -34,6 +34,7 @@ _SIGS = {
     "mb_mom_zmat_rwg_c128": [_P, _I64, _P, _I64, _P, _P, _P, _I64, _P, _P, _I, _P, _P, _I, _D,
                              _I64, _I64, _P, _P],
     "mb_mom_edge_rows": [_P, _I64, _I64, _P, _P],
+    "mb_mom_sym_zmat_rwg_to_host_c64": [_P, _I64, _P, _I64, _P, _I64, _D, _P, _I64, _P, _P, _I, _P],
     "mb_gmres_blockdiag_column_steps": [_P, _I64, _I64, _I, _P, _P],
     "mb_gmres_multi_column_steps": [_P, _I64, _I64, _I, _P, _P],
     "mb_mom_zmat_rwg_edges_c64": [_P, _I64, _P, _I64, _P, _P, _P, _P, _I64, _P, _P, _I, _P, _P, _I, _D,

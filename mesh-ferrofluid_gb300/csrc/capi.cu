@@ -122,6 +122,9 @@ int launch_mom_sym_near(const T*, const int32_t*, const int32_t*, int64_t, const
                         cudaStream_t);
 template <typename T>
 int launch_mom_sym_rhs(const T*, const int32_t*, const int32_t*, const double*, int, int64_t, T*, cudaStream_t);
+int sym_zmat_to_host(const float* verts, const int32_t* faces, const int32_t* fei, int64_t nf, int64_t n_edges,
+                     double k, const int32_t* pairs, int64_t n_pairs, float* z_dev, float* z_host, int chunks,
+                     cudaStream_t s);
 template <typename T>
 int launch_radiate_h(const T*, int64_t, const T*, const T*, const T*, int64_t, double, T*, cudaStream_t);
 int gmres_c64(const float*, int64_t, const double*, double*, int, int, double, void*, size_t, int64_t*,
@@ -468,6 +471,18 @@ MB_LSYM(f64, double)
 MB_SYM(c64, float)
 MB_SYM(c128, double)
 #undef MB_SYM
+
+int mb_mom_sym_zmat_rwg_to_host_c64(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                                    const int32_t* fei, int64_t n_edges, double wavenumber, const int32_t* pairs,
+                                    int64_t n_pairs, float* z_dev, float* z_host, int chunks, void* stream) {
+    (void)n_verts;
+    MB_REQUIRE(n_faces >= 0 && n_edges >= 0 && n_pairs >= 0 && n_edges < (1ll << 31), "bad sizes");
+    if (n_faces == 0 || n_edges == 0) return MB_OK;
+    MB_REQUIRE(verts && faces && fei && z_dev && z_host && (pairs || n_pairs == 0), "null pointer argument");
+    MB_REQUIRE(wavenumber > 0, "wavenumber must be > 0");
+    return sym_zmat_to_host(verts, faces, fei, n_faces, n_edges, wavenumber, pairs, n_pairs, z_dev, z_host, chunks,
+                            as_stream(stream));
+}
 
 size_t mb_ray_bvh_bytes(int64_t n_faces) { return n_faces > 0 ? bvh_bytes(n_faces) : 0; }
 

@@ -20,6 +20,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+#include <vector>
+
 #include "closed_form.cuh"
 #include "common.cuh"
 #include "packed.cuh"
@@ -556,6 +559,118 @@ int launch_mom_sym_rhs_batched(const T* verts, const int32_t* faces, const int32
 // ---------------------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------------------
+// Z rows -> host memory: rows[] of src copied to the same rows of dst (device-accessible host
+// memory); a few blocks loop over the rows so the copy leaves the SMs to the assembly.
+__global__ void drain_rows_kernel(const float2* __restrict__ src, float2* dst, const int32_t* __restrict__ rows,
+                                  int64_t n_rows, int64_t n_edges) {
+    for (int64_t r = blockIdx.x; r < n_rows; r += gridDim.x) {
+        const int64_t m = rows[r];
+        const float2* sp = src + m * n_edges;
+        float2* dp = dst + m * n_edges;
+        for (int64_t j = threadIdx.x; j < n_edges; j += blockDim.x) dp[j] = sp[j];
+    }
+}
+
+template <typename T>
+int launch_mom_sym_regular(const T* verts, const int32_t* faces, const int32_t* fei, int64_t n_edges, double k,
+                           int64_t nf, int64_t p_begin, int64_t p_end, T* z, cudaStream_t s);
+template <typename T>
+int launch_mom_sym_near(const T* verts, const int32_t* faces, const int32_t* fei, int64_t n_edges,
+                        const int32_t* pairs, int64_t n_pairs, double k, T* z, cudaStream_t s);
+
+// The symmetric-rule Z (separated pairs + near pairs, complex64) into pinned host memory with
+// the copy overlapped: test faces in `chunks` ranges; after each range the Z rows whose faces
+// have all been processed are written to z_host by a small drain kernel on a second stream
+// while the next range is assembled.  pairs must be sorted by test face (near_pairs order).
+int sym_zmat_to_host(const float* verts, const int32_t* faces, const int32_t* fei, int64_t nf, int64_t n_edges,
+                     double k, const int32_t* pairs, int64_t n_pairs, float* z_dev, float* z_host, int chunks,
+                     cudaStream_t s) {
+    chunks = std::max(1, std::min<int>(chunks, (int)std::max<int64_t>(1, nf)));
+    float2* hdst = nullptr;
+    if (cudaHostGetDevicePointer(reinterpret_cast<void**>(&hdst), z_host, 0) != cudaSuccess || !hdst) {
+        cudaGetLastError();
+        return set_error(MB_ERR_ARG, "z_host must be page-locked host memory (pinned)");
+    }
+    // host copies of the face-edge map and the near-pair list
+    std::vector<int32_t> hfei((size_t)3 * nf), hp((size_t)2 * n_pairs);
+    cudaMemcpyAsync(hfei.data(), fei, 12 * (size_t)nf, cudaMemcpyDeviceToHost, s);
+    if (n_pairs) cudaMemcpyAsync(hp.data(), pairs, 8 * (size_t)n_pairs, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return check_launch("sym zmat to host: maps");
+    for (int64_t t = 1; t < n_pairs; ++t)
+        if (hp[2 * t] < hp[2 * (t - 1)]) return set_error(MB_ERR_ARG, "near pairs must be sorted by test face");
+    std::vector<int64_t> fb((size_t)chunks + 1);
+    for (int c = 0; c <= chunks; ++c) fb[c] = nf * c / chunks;
+    // chunk after which each Z row is complete: the range of its last face
+    std::vector<int32_t> last((size_t)n_edges, -1);
+    for (int64_t r = 0; r < 3 * nf; ++r) {
+        const int32_t m = hfei[r];
+        if (m < 0 || m >= n_edges) return set_error(MB_ERR_ARG, "face_edge_indices out of range");
+        last[m] = std::max<int32_t>(last[m], (int32_t)(r / 3));
+    }
+    std::vector<int64_t> off((size_t)chunks + 1, 0);
+    std::vector<int32_t> chunk_of((size_t)n_edges);
+    for (int64_t m = 0; m < n_edges; ++m) {
+        const int64_t f = std::max<int32_t>(last[m], 0);
+        int c = (int)std::min<int64_t>(chunks - 1, f * chunks / std::max<int64_t>(nf, 1));
+        while (c > 0 && fb[c] > f) --c;
+        while (c + 1 < chunks && fb[c + 1] <= f) ++c;
+        chunk_of[m] = c;
+        ++off[c + 1];
+    }
+    for (int c = 0; c < chunks; ++c) off[c + 1] += off[c];
+    std::vector<int32_t> rows((size_t)n_edges);
+    {
+        std::vector<int64_t> pos(off.begin(), off.end() - 1);
+        for (int64_t m = 0; m < n_edges; ++m) rows[pos[chunk_of[m]]++] = (int32_t)m;
+    }
+    std::vector<int64_t> pb((size_t)chunks + 1);
+    for (int c = 0; c <= chunks; ++c) {
+        int64_t lo = 0, hi = n_pairs;  // first pair with test face >= fb[c]
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) / 2;
+            if (hp[2 * mid] < fb[c]) lo = mid + 1;
+            else hi = mid;
+        }
+        pb[c] = lo;
+    }
+    int32_t* drows = nullptr;
+    if (cudaMallocAsync(reinterpret_cast<void**>(&drows), 4 * (size_t)n_edges, s) != cudaSuccess)
+        return set_error(MB_ERR_CUDA, "sym zmat to host: row list");
+    cudaMemcpyAsync(drows, rows.data(), 4 * (size_t)n_edges, cudaMemcpyHostToDevice, s);
+    cudaStream_t cs = nullptr;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaFreeAsync(drows, s);
+        return set_error(MB_ERR_CUDA, "sym zmat to host: copy stream");
+    }
+    std::vector<cudaEvent_t> ev((size_t)chunks + 1, nullptr);
+    int rc = MB_OK;
+    for (auto& e : ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = MB_ERR_CUDA;
+    if (rc) rc = set_error(MB_ERR_CUDA, "sym zmat to host: events");
+    cudaMemsetAsync(z_dev, 0, (size_t)n_edges * n_edges * 8, s);
+    for (int c = 0; c < chunks && rc == MB_OK; ++c) {
+        if ((rc = launch_mom_sym_regular<float>(verts, faces, fei, n_edges, k, nf, fb[c], fb[c + 1], z_dev, s)))
+            break;
+        if (pb[c + 1] > pb[c] &&
+            (rc = launch_mom_sym_near<float>(verts, faces, fei, n_edges, pairs + 2 * pb[c], pb[c + 1] - pb[c], k,
+                                             z_dev, s)))
+            break;
+        cudaEventRecord(ev[c], s);
+        cudaStreamWaitEvent(cs, ev[c], 0);
+        if (off[c + 1] > off[c])
+            drain_rows_kernel<<<32, 512, 0, cs>>>(reinterpret_cast<const float2*>(z_dev), hdst, drows + off[c],
+                                                   off[c + 1] - off[c], n_edges);
+    }
+    cudaEventRecord(ev[chunks], cs);
+    cudaStreamWaitEvent(s, ev[chunks], 0);
+    cudaFreeAsync(drows, s);
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    cudaStreamDestroy(cs);
+    if (rc) return rc;
+    return check_launch("sym zmat to host");
+}
+
 template <typename T>
 int launch_mom_sym_regular(const T* verts, const int32_t* faces, const int32_t* fei, int64_t n_edges, double k,
                            int64_t nf, int64_t p_begin, int64_t p_end, T* z, cudaStream_t s) {

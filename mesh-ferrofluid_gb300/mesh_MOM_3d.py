@@ -305,13 +305,15 @@ def near_pairs(faces) -> torch.Tensor:
 
 
 def assemble_Z_rwg_sym(verts, faces, face_edge_indices, n_edges, wavenumber, out=None, pairs=None,
-                       faces_range=None, check_indices=True):
+                       faces_range=None, check_indices=True, out_host=None, chunks=16):
     """EFIE RWG matrix [E, E] with the 7-point rule on both triangles.
 
     Separated pairs run in the mesh dtype; pairs sharing a vertex (``pairs``, default
-    ``near_pairs(faces)``) run in FP64 with the 1/R part integrated in closed form.
-    ``faces_range`` restricts the separated pairs to test faces [begin, end) (the near
-    pairs are then left to the caller).
+    ``near_pairs(faces)``, sorted by test face) have the 1/R part integrated in closed form in
+    FP64.  ``faces_range`` restricts the separated pairs to test faces [begin, end) (the near
+    pairs are then left to the caller).  ``out_host`` (pinned complex64 CPU tensor [E, E],
+    float32 meshes): Z goes to host memory with the copy overlapped with the assembly
+    (``chunks`` test-face ranges); ``out`` is then the device scratch.  Returns ``out_host``.
     """
     _lib.check_tensor(verts, "verts", dtype=_FLOATS, ndim=2)
     dt, dev = verts.dtype, verts.device
@@ -325,8 +327,21 @@ def assemble_Z_rwg_sym(verts, faces, face_edge_indices, n_edges, wavenumber, out
         out = torch.zeros((n_edges, n_edges), dtype=cdt, device=dev)
     else:
         _lib.check_tensor(out, "out", dtype=cdt, device=dev, shape=(n_edges, n_edges))
-    f0, f1 = (0, nf) if faces_range is None else faces_range
     st = _lib.stream_of(verts)
+    if out_host is not None:
+        if dt != torch.float32 or faces_range is not None:
+            raise ValueError("out_host needs a float32 mesh and no faces_range")
+        if (out_host.device.type != "cpu" or out_host.dtype != torch.complex64 or not out_host.is_contiguous()
+                or tuple(out_host.shape) != (n_edges, n_edges) or not out_host.is_pinned()):
+            raise ValueError("out_host must be a pinned contiguous complex64 CPU tensor [E, E]")
+        if pairs is None:
+            pairs = near_pairs(faces)
+        _lib.check_tensor(pairs, "pairs", dtype=torch.int32, device=dev, ndim=2)
+        _lib.call("mb_mom_sym_zmat_rwg_to_host_c64", _lib.ptr(verts), verts.shape[0], _lib.ptr(faces), nf,
+                  _lib.ptr(face_edge_indices), n_edges, float(wavenumber), _lib.ptr(pairs), pairs.shape[0],
+                  _lib.ptr(out), out_host.data_ptr(), int(chunks), st)
+        return out_host
+    f0, f1 = (0, nf) if faces_range is None else faces_range
     _lib.call(f"mb_mom_sym_zmat_rwg_{_lib.csfx(dt)}", _lib.ptr(verts), verts.shape[0], _lib.ptr(faces), nf,
               _lib.ptr(face_edge_indices), n_edges, float(wavenumber), int(f0), int(f1), _lib.ptr(out), st)
     if faces_range is None:

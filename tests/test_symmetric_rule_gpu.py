@@ -80,3 +80,20 @@ def test_sym_gmres_current_matches_mie(pkg, cuda):
         s = np.where(i1 < i2, 1.0, -1.0) * l / (2 * A)
         J += (s * I[fe.reshape(-1, 3)[:, e]])[:, None] * (c - P[:, e])
     assert rel_err(J, mie.surface_current(c, k, 1.0)) < 0.05
+
+
+@pytest.mark.parametrize("chunks", [1, 5])
+def test_sym_zmat_to_host_equals_device(pkg, cuda, chunks):
+    """The overlapped host-output assembly returns the same Z as the device path."""
+    v_np, f_np = pkg.meshes.icosphere(3)
+    v = torch.tensor(v_np, dtype=torch.float32, device=cuda)
+    f = torch.tensor(f_np, dtype=torch.int32, device=cuda)
+    edges, fei, _ = pkg.utils.get_edge_unique(v, f)
+    ne = edges.shape[0]
+    M = pkg.mesh_MOM_3d
+    zd = M.assemble_Z_rwg_sym(v, f, fei, ne, 4.0)
+    h = torch.empty((ne, ne), dtype=torch.complex64, pin_memory=True)
+    M.assemble_Z_rwg_sym(v, f, fei, ne, 4.0, out_host=h, chunks=chunks)
+    torch.cuda.synchronize()
+    ref = zd.cpu()
+    assert (torch.linalg.norm(h - ref) / torch.linalg.norm(ref)).item() < 1e-6
