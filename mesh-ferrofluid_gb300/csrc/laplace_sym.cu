@@ -23,6 +23,7 @@
 
 #include "closed_form.cuh"
 #include "common.cuh"
+#include "packed.cuh"
 
 namespace mb {
 
@@ -225,7 +226,7 @@ __global__ void lap_sym_near_kernel(const T* __restrict__ verts, const int32_t* 
 // each thread builds its source triangle's 7 points once and evaluates them against the
 // kColRows centroids held in shared memory, writing out[(i - row_begin) * nf + j]
 // (coalesced per row).  Pairs sharing a vertex are then rewritten by lap_colloc_near_kernel.
-constexpr int kColRows = 16;
+constexpr int kColRows = 64;
 
 template <typename T>
 __global__ void __launch_bounds__(kSymThreads)
@@ -234,14 +235,14 @@ __global__ void __launch_bounds__(kSymThreads)
     __shared__ T s_c[kColRows][3];
     const int64_t i0 = row_begin + (int64_t)blockIdx.y * kColRows;
     const int64_t j = (int64_t)blockIdx.x * kSymThreads + threadIdx.x;
-    if (threadIdx.x < kColRows) {
-        const int64_t i = i0 + threadIdx.x;
+    for (int t = threadIdx.x; t < kColRows; t += blockDim.x) {
+        const int64_t i = i0 + t;
         if (i < row_end) {
             const int32_t a0 = faces[3 * i], a1 = faces[3 * i + 1], a2 = faces[3 * i + 2];
             const V3<T> c = T(1.0 / 3.0) * (load3(verts, a0) + load3(verts, a1) + load3(verts, a2));
-            s_c[threadIdx.x][0] = c.x;
-            s_c[threadIdx.x][1] = c.y;
-            s_c[threadIdx.x][2] = c.z;
+            s_c[t][0] = c.x;
+            s_c[t][1] = c.y;
+            s_c[t][2] = c.z;
         }
     }
     __syncthreads();
@@ -261,6 +262,38 @@ __global__ void __launch_bounds__(kSymThreads)
     // kernel, launched next on the same stream, overwrites them); the only coincident point,
     // the centroid of a face against its own rule, gives +inf, never a fault.
     const int64_t rows = row_end - i0;
+    if constexpr (sizeof(T) == 4) {
+        if (rows >= kColRows) {
+            // two collocation rows per packed f32x2 instruction (the source points broadcast)
+            float2 yx[7], yy[7], yz[7], wk[7];
+#pragma unroll
+            for (int k = 0; k < 7; ++k) {
+                yx[k] = bc(y[k].x);
+                yy[k] = bc(y[k].y);
+                yz[k] = bc(y[k].z);
+                wk[k] = bc(w[k]);
+            }
+#pragma unroll 2
+            for (int r = 0; r < kColRows; r += 2) {
+                const float2 cx = make_float2(s_c[r][0], s_c[r + 1][0]);
+                const float2 cy = make_float2(s_c[r][1], s_c[r + 1][1]);
+                const float2 cz = make_float2(s_c[r][2], s_c[r + 1][2]);
+                float2 acc = bc(0.f);
+#pragma unroll
+                for (int k = 0; k < 7; ++k) {
+                    const float2 dx = sub2(yx[k], cx), dy = sub2(yy[k], cy), dz = sub2(yz[k], cz);
+                    const float2 r2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+                    float2 ri;
+                    ri.x = rsqrtf(r2.x);
+                    ri.y = rsqrtf(r2.y);
+                    acc = fma2(wk[k], ri, acc);
+                }
+                out[(i0 - row_begin + r) * nf + j] = acc.x;
+                out[(i0 - row_begin + r + 1) * nf + j] = acc.y;
+            }
+            return;
+        }
+    }
     if (rows >= kColRows) {
 #pragma unroll 4
         for (int r = 0; r < kColRows; ++r) {
