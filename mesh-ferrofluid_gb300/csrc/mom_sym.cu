@@ -149,42 +149,54 @@ __device__ __forceinline__ void sym_regular_pair(const T* __restrict__ verts, co
 // pairs (3 pairs + the seventh point scalar), coordinates scaled by k so kR = |k x - k y|
 // feeds the SFU sine / cosine directly, the weight k w so g = w / R = (k w) / (kR); the
 // source moments are accumulated as k sum G y and the 1/k and the sign of Im G (G = gr - j gs)
-// are applied once per test point / at the end.
-template <>
-__device__ __forceinline__ void sym_regular_pair<float>(const float* __restrict__ verts,
-                                                        const int32_t* __restrict__ faces,
-                                                        const int32_t* __restrict__ fei, int64_t n_edges, float k,
-                                                        int64_t p, int64_t q, const float (*s_b)[4],
-                                                        float* __restrict__ z) {
-    if (shared_vertices(faces, p, q) != 0) return;  // done by the FP64 near-pair kernel
-    const V3<float> o = load3(verts, __ldg(faces + 3 * q));
-    V3<float> A[3], B[3];
+// are applied once per test point / at the end.  The source side (origin o = its vertex 0)
+// is set up once per source face and reused for every test face a thread meets.
+struct SymSource {
+    V3<float> o;                                // source vertex 0 (absolute)
+    V3<float> B[3];                             // source vertices relative to o
+    float cn[3];                                // RWG constants of the source edges
+    int32_t v[3];                               // vertex ids (shared-vertex test)
+    int32_t col[3];                             // RWG edge ids of the source edges
+    float2 yx[3], yy[3], yz[3], yw[3];          // 6 source points, k-scaled, packed
+    float tx, ty, tz, tw;                       // the seventh point
+};
+
+__device__ __forceinline__ void sym_source(const float* __restrict__ verts, const int32_t* __restrict__ faces,
+                                           const int32_t* __restrict__ fei, float k, int64_t q,
+                                           const float (*s_b)[4], SymSource& S) {
+#pragma unroll
+    for (int v = 0; v < 3; ++v) S.v[v] = __ldg(faces + 3 * q + v);
+    S.o = load3(verts, S.v[0]);
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
-        A[v] = load3(verts, __ldg(faces + 3 * p + v)) - o;
-        B[v] = load3(verts, __ldg(faces + 3 * q + v)) - o;
+        S.B[v] = load3(verts, S.v[v]) - S.o;
+        S.col[v] = __ldg(fei + 3 * q + v);
     }
-    float cm[3], cn[3], ap, aq;
-    rwg_consts<float>(faces, p, A, cm, &ap);
-    rwg_consts<float>(faces, q, B, cn, &aq);
-    float2 yx[3], yy[3], yz[3], yw[3];
-    float tx, ty, tz, tw;
+    float aq;
+    rwg_consts<float>(faces, q, S.B, S.cn, &aq);
 #pragma unroll
     for (int j = 0; j < 7; ++j) {
-        const V3<float> y = s_b[j][0] * B[0] + s_b[j][1] * B[1] + s_b[j][2] * B[2];
+        const V3<float> y = s_b[j][0] * S.B[0] + s_b[j][1] * S.B[1] + s_b[j][2] * S.B[2];
         const float w = s_b[j][3] * aq * float(kInv4Pi) * k;
         if (j < 6) {
-            (reinterpret_cast<float*>(&yx[j / 2]) + (j & 1))[0] = k * y.x;
-            (reinterpret_cast<float*>(&yy[j / 2]) + (j & 1))[0] = k * y.y;
-            (reinterpret_cast<float*>(&yz[j / 2]) + (j & 1))[0] = k * y.z;
-            (reinterpret_cast<float*>(&yw[j / 2]) + (j & 1))[0] = w;
+            (reinterpret_cast<float*>(&S.yx[j / 2]) + (j & 1))[0] = k * y.x;
+            (reinterpret_cast<float*>(&S.yy[j / 2]) + (j & 1))[0] = k * y.y;
+            (reinterpret_cast<float*>(&S.yz[j / 2]) + (j & 1))[0] = k * y.z;
+            (reinterpret_cast<float*>(&S.yw[j / 2]) + (j & 1))[0] = w;
         } else {
-            tx = k * y.x;
-            ty = k * y.y;
-            tz = k * y.z;
-            tw = w;
+            S.tx = k * y.x;
+            S.ty = k * y.y;
+            S.tz = k * y.z;
+            S.tw = w;
         }
     }
+}
+
+// The nine entries of one separated pair: test vertices A (relative to the source origin),
+// their RWG constants cm, area ap and RWG edge ids rows.
+__device__ __forceinline__ void sym_pair_eval(const SymSource& S, const V3<float> A[3], const float cm[3], float ap,
+                                              const int32_t rows[3], float k, int64_t n_edges,
+                                              const float (*s_b)[4], float* __restrict__ z) {
     // per pair: t0 = sum_i w_i S0_i, tx = sum_i w_i x_i S0_i, ty' = sum_i w_i S1'_i,
     // txy' = sum_i w_i x_i . S1'_i with S1' = k S1 (S0 = sum_j G, S1 = sum_j G y)
     float t0r = 0.f, t0i = 0.f, txr[3] = {0.f, 0.f, 0.f}, txi[3] = {0.f, 0.f, 0.f};
@@ -198,9 +210,9 @@ __device__ __forceinline__ void sym_regular_pair<float>(const float* __restrict_
                szr = bc(0.f), szs = bc(0.f);
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            const float2 dx = sub2(X, yx[j]);
-            const float2 dy = sub2(Y, yy[j]);
-            const float2 dz = sub2(Zc, yz[j]);
+            const float2 dx = sub2(X, S.yx[j]);
+            const float2 dy = sub2(Y, S.yy[j]);
+            const float2 dz = sub2(Zc, S.yz[j]);
             const float2 r2d = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));  // (kR)^2
             float2 rinv;
             rinv.x = rsqrtf(r2d.x);
@@ -209,38 +221,38 @@ __device__ __forceinline__ void sym_regular_pair<float>(const float* __restrict_
             float2 sn, cs;
             __sincosf(kR.x, &sn.x, &cs.x);
             __sincosf(kR.y, &sn.y, &cs.y);
-            const float2 g = mul2(yw[j], rinv);
+            const float2 g = mul2(S.yw[j], rinv);
             const float2 gr = mul2(g, cs), gs = mul2(g, sn);  // G = gr - j gs
             s0r = add2(s0r, gr);
             s0s = add2(s0s, gs);
-            sxr = fma2(gr, yx[j], sxr);
-            sxs = fma2(gs, yx[j], sxs);
-            syr = fma2(gr, yy[j], syr);
-            sys = fma2(gs, yy[j], sys);
-            szr = fma2(gr, yz[j], szr);
-            szs = fma2(gs, yz[j], szs);
+            sxr = fma2(gr, S.yx[j], sxr);
+            sxs = fma2(gs, S.yx[j], sxs);
+            syr = fma2(gr, S.yy[j], syr);
+            sys = fma2(gs, S.yy[j], sys);
+            szr = fma2(gr, S.yz[j], szr);
+            szs = fma2(gs, S.yz[j], szs);
         }
         float a0r = s0r.x + s0r.y, a0s = s0s.x + s0s.y;
         float a1r[3] = {sxr.x + sxr.y, syr.x + syr.y, szr.x + szr.y};
         float a1s[3] = {sxs.x + sxs.y, sys.x + sys.y, szs.x + szs.y};
         {
             // the seventh source point, scalar
-            const float dx = k * x.x - tx, dy = k * x.y - ty, dz = k * x.z - tz;
+            const float dx = k * x.x - S.tx, dy = k * x.y - S.ty, dz = k * x.z - S.tz;
             const float r2d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
             const float rinv = rsqrtf(r2d);
             const float kR = r2d * rinv;
             float sn, cs;
             __sincosf(kR, &sn, &cs);
-            const float g = tw * rinv;
+            const float g = S.tw * rinv;
             const float gr = g * cs, gs = g * sn;
             a0r += gr;
             a0s += gs;
-            a1r[0] = fmaf(gr, tx, a1r[0]);
-            a1s[0] = fmaf(gs, tx, a1s[0]);
-            a1r[1] = fmaf(gr, ty, a1r[1]);
-            a1s[1] = fmaf(gs, ty, a1s[1]);
-            a1r[2] = fmaf(gr, tz, a1r[2]);
-            a1s[2] = fmaf(gs, tz, a1s[2]);
+            a1r[0] = fmaf(gr, S.tx, a1r[0]);
+            a1s[0] = fmaf(gs, S.tx, a1s[0]);
+            a1r[1] = fmaf(gr, S.ty, a1r[1]);
+            a1s[1] = fmaf(gs, S.ty, a1s[1]);
+            a1r[2] = fmaf(gr, S.tz, a1r[2]);
+            a1s[2] = fmaf(gs, S.tz, a1s[2]);
         }
         // Im G = -gs: the imaginary sums enter with a minus sign
         t0r = fmaf(wi, a0r, t0r);
@@ -266,17 +278,95 @@ __device__ __forceinline__ void sym_regular_pair<float>(const float* __restrict_
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
         const float amr = dot(A[m], Tyr), ami = dot(A[m], Tyi);
-        const int64_t row = __ldg(fei + 3 * p + m);
+        const int64_t row = rows[m];
 #pragma unroll
         for (int n = 0; n < 3; ++n) {
-            const float ab = dot(A[m], B[n]);
-            const float fr = txyr - dot(B[n], Txr) - amr + ab * t0r;  // int int (x-A_m).(y-B_n) G
-            const float fi = txyi - dot(B[n], Txi) - ami + ab * t0i;
-            const float cc = cm[m] * cn[n];
+            const float ab = dot(A[m], S.B[n]);
+            const float fr = txyr - dot(S.B[n], Txr) - amr + ab * t0r;  // int int (x-A_m).(y-B_n) G
+            const float fi = txyi - dot(S.B[n], Txi) - ami + ab * t0i;
+            const float cc = cm[m] * S.cn[n];
             const float re = cc * (-k * fi + inv_k4 * t0i);
             const float im = cc * (k * fr - inv_k4 * t0r);
-            add_c<float>(z + 2 * (row * n_edges + __ldg(fei + 3 * q + n)), re, im);
+            add_c<float>(z + 2 * (row * n_edges + S.col[n]), re, im);
         }
+    }
+}
+
+template <>
+__device__ __forceinline__ void sym_regular_pair<float>(const float* __restrict__ verts,
+                                                        const int32_t* __restrict__ faces,
+                                                        const int32_t* __restrict__ fei, int64_t n_edges, float k,
+                                                        int64_t p, int64_t q, const float (*s_b)[4],
+                                                        float* __restrict__ z) {
+    if (shared_vertices(faces, p, q) != 0) return;  // done by the FP64 near-pair kernel
+    SymSource S;
+    sym_source(verts, faces, fei, k, q, s_b, S);
+    V3<float> A[3];
+    int32_t rows[3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+        A[v] = load3(verts, __ldg(faces + 3 * p + v)) - S.o;
+        rows[v] = __ldg(fei + 3 * p + v);
+    }
+    float cm[3], ap;
+    rwg_consts<float>(faces, p, A, cm, &ap);
+    sym_pair_eval(S, A, cm, ap, rows, k, n_edges, s_b, z);
+}
+
+// Single-mesh float separated pairs: a block owns kSymRows test faces (their vertices, RWG
+// constants and edge ids staged in shared memory) and 128 source faces; each thread sets up
+// its source face once and evaluates it against every test face of the block.
+constexpr int kSymRows = 8;
+__global__ void __launch_bounds__(128) mom_sym_regular_rows_kernel(const float* __restrict__ verts,
+                                                                   const int32_t* __restrict__ faces,
+                                                                   const int32_t* __restrict__ fei,
+                                                                   int64_t n_edges, float k, int64_t nf,
+                                                                   int64_t p_begin, int64_t p_end,
+                                                                   float* __restrict__ z) {
+    __shared__ float s_b[7][4];
+    __shared__ float s_A[kSymRows][9], s_cm[kSymRows][3], s_ap[kSymRows];
+    __shared__ int32_t s_v[kSymRows][3], s_row[kSymRows][3];
+    if (threadIdx.x < 28) s_b[threadIdx.x / 4][threadIdx.x % 4] = (float)c_d7[threadIdx.x / 4][threadIdx.x % 4];
+    const int64_t p0 = p_begin + (int64_t)blockIdx.y * kSymRows;
+    if (threadIdx.x < kSymRows && p0 + threadIdx.x < p_end) {
+        const int64_t p = p0 + threadIdx.x;
+        V3<float> A[3];
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {
+            s_v[threadIdx.x][v] = __ldg(faces + 3 * p + v);
+            s_row[threadIdx.x][v] = __ldg(fei + 3 * p + v);
+            A[v] = load3(verts, s_v[threadIdx.x][v]);
+            s_A[threadIdx.x][3 * v] = A[v].x;
+            s_A[threadIdx.x][3 * v + 1] = A[v].y;
+            s_A[threadIdx.x][3 * v + 2] = A[v].z;
+        }
+        float cm[3], ap;
+        rwg_consts<float>(faces, p, A, cm, &ap);
+        s_cm[threadIdx.x][0] = cm[0];
+        s_cm[threadIdx.x][1] = cm[1];
+        s_cm[threadIdx.x][2] = cm[2];
+        s_ap[threadIdx.x] = ap;
+    }
+    __syncthreads();
+    const int64_t q = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    if (q >= nf) return;
+    SymSource S;
+    sym_source(verts, faces, fei, k, q, s_b, S);
+    const int nr = (int)min((int64_t)kSymRows, p_end - p0);
+#pragma unroll 1
+    for (int r = 0; r < nr; ++r) {
+        int shared = 0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) shared += s_v[r][a] == S.v[b];
+        if (shared) continue;  // done by the FP64 near-pair kernel
+        V3<float> A[3];
+#pragma unroll
+        for (int v = 0; v < 3; ++v) A[v] = v3<float>(s_A[r][3 * v], s_A[r][3 * v + 1], s_A[r][3 * v + 2]) - S.o;
+        const float cm[3] = {s_cm[r][0], s_cm[r][1], s_cm[r][2]};
+        const int32_t rows[3] = {s_row[r][0], s_row[r][1], s_row[r][2]};
+        sym_pair_eval(S, A, cm, s_ap[r], rows, k, n_edges, s_b, z);
     }
 }
 
@@ -677,6 +767,13 @@ int launch_mom_sym_regular(const T* verts, const int32_t* faces, const int32_t* 
     if (nf <= 0 || p_end <= p_begin) return MB_OK;
     if (!(k > 0)) return set_error(MB_ERR_ARG, "wavenumber must be > 0");
     const int64_t q_blocks = (nf + 127) / 128;
+    if constexpr (sizeof(T) == 4) {
+        const int64_t py = (p_end - p_begin + kSymRows - 1) / kSymRows;
+        if (q_blocks > 0x7fffffffLL || py > 65535) return set_error(MB_ERR_SIZE, "mesh too large for one launch");
+        mom_sym_regular_rows_kernel<<<dim3((unsigned)q_blocks, (unsigned)py), 128, 0, s>>>(
+            verts, faces, fei, n_edges, (float)k, nf, p_begin, p_end, z);
+        return check_launch("mom_sym_regular");
+    }
     const int64_t blocks = (p_end - p_begin) * q_blocks;
     if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "mesh too large for one launch");
     mom_sym_regular_kernel<T><<<(unsigned)blocks, 128, 0, s>>>(verts, faces, fei, n_edges, (T)k, nf, p_begin,
