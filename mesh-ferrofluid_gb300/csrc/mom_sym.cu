@@ -316,7 +316,7 @@ __device__ __forceinline__ void sym_regular_pair<float>(const float* __restrict_
 // Single-mesh float separated pairs: a block owns kSymRows test faces (their vertices, RWG
 // constants and edge ids staged in shared memory) and 128 source faces; each thread sets up
 // its source face once and evaluates it against every test face of the block.
-constexpr int kSymRows = 8;
+constexpr int kSymRows = 32;
 __global__ void __launch_bounds__(128) mom_sym_regular_rows_kernel(const float* __restrict__ verts,
                                                                    const int32_t* __restrict__ faces,
                                                                    const int32_t* __restrict__ fei,
