@@ -876,34 +876,30 @@ int blockdiag_matvec(const float* z, const int64_t* desc, const int64_t* goff, i
                      const float* x, int64_t ld, int nc, int rows, float* y, cudaStream_t s) {
     if (n_mesh <= 0 || total_warps <= 0) return MB_OK;
     if (rows == kBdRows) {
-        // standalone call: tensor maps and the time-out word in private buffers, checked here
+        // standalone call: the tensor maps and the time-out word in stream-ordered buffers of
+        // this call, the word checked here
         if (reinterpret_cast<uintptr_t>(z) & 15) return set_error(MB_ERR_ARG, "z must be 16-byte aligned");
-        static int* own = nullptr;
-        static CUtensorMap* maps = nullptr;
-        static int maps_cap = 0;
-        if (!own && cudaMalloc(&own, 16) != cudaSuccess) {
-            own = nullptr;
-            return set_error(MB_ERR_CUDA, "block-diagonal product: status word");
-        }
-        if (maps_cap < n_mesh) {
-            if (maps) cudaFree(maps);
-            maps = nullptr;
-            maps_cap = 0;
-            if (cudaMalloc(&maps, sizeof(CUtensorMap) * n_mesh) != cudaSuccess)
-                return set_error(MB_ERR_CUDA, "block-diagonal product: tensor map buffer");
-            maps_cap = n_mesh;
-        }
         std::vector<int64_t> dh((size_t)6 * n_mesh);
         cudaMemcpyAsync(dh.data(), desc, 48 * (size_t)n_mesh, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return check_launch("blockdiag_matvec: descriptors");
+        void* buf = nullptr;
+        const size_t map_bytes = sizeof(CUtensorMap) * (size_t)n_mesh;
+        if (cudaMallocAsync(&buf, map_bytes + 256, s) != cudaSuccess)
+            return set_error(MB_ERR_CUDA, "block-diagonal product: scratch");
+        CUtensorMap* maps = static_cast<CUtensorMap*>(buf);
+        int* own = reinterpret_cast<int*>(static_cast<char*>(buf) + map_bytes);
         int rc = bd_zmaps(z, dh.data(), n_mesh, maps, s);
-        if (rc) return rc;
         int64_t rows_max = 0;
         for (int i = 0; i < n_mesh; ++i) rows_max = std::max(rows_max, dh[6 * i + 2]);
-        cudaMemsetAsync(own, 0, 4, s);
-        if ((rc = bd_launch(maps, x, rows_max, desc, goff, n_mesh, total_warps, ld, nc, y, own, s))) return rc;
+        if (!rc) {
+            cudaMemsetAsync(own, 0, 4, s);
+            rc = bd_launch(maps, x, rows_max, desc, goff, n_mesh, total_warps, ld, nc, y, own, s);
+        }
         int hs = 0;
-        cudaMemcpyAsync(&hs, own, 4, cudaMemcpyDeviceToHost, s);
+        if (!rc) cudaMemcpyAsync(&hs, own, 4, cudaMemcpyDeviceToHost, s);
+        cudaFreeAsync(buf, s);
         const cudaError_t e = cudaStreamSynchronize(s);
+        if (rc) return rc;
         if (e != cudaSuccess) return set_error(MB_ERR_CUDA, "blockdiag_matvec: %s", cudaGetErrorString(e));
         if (hs) return set_error(MB_ERR_CUDA, "blockdiag_matvec: wait timed out (code %d)", hs);
         return MB_OK;
