@@ -97,3 +97,21 @@ def test_sym_zmat_to_host_equals_device(pkg, cuda, chunks):
     torch.cuda.synchronize()
     ref = zd.cpu()
     assert (torch.linalg.norm(h - ref) / torch.linalg.norm(ref)).item() < 1e-6
+
+
+def test_sym_zmat_to_host_rejects_bad_buffers(pkg, cuda):
+    """The host-output assembly refuses pageable host memory and near-pair lists that are not
+    sorted by test face (the chunked schedule depends on that order)."""
+    v_np, f_np = pkg.meshes.icosphere(1)
+    v = torch.tensor(v_np, dtype=torch.float32, device=cuda)
+    f = torch.tensor(f_np, dtype=torch.int32, device=cuda)
+    edges, fei, _ = pkg.utils.get_edge_unique(v, f)
+    ne = edges.shape[0]
+    M = pkg.mesh_MOM_3d
+    with pytest.raises(ValueError):
+        M.assemble_Z_rwg_sym(v, f, fei, ne, 2.0, out_host=torch.empty((ne, ne), dtype=torch.complex64))
+    pairs = M.near_pairs(f)
+    shuffled = pairs.flip(0).contiguous()
+    h = torch.empty((ne, ne), dtype=torch.complex64, pin_memory=True)
+    with pytest.raises(pkg._lib.MeshBEMError, match="sorted"):
+        M.assemble_Z_rwg_sym(v, f, fei, ne, 2.0, pairs=shuffled, out_host=h)
