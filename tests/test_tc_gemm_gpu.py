@@ -41,10 +41,12 @@ def test_multi_rhs_matmul_rejects_odd_n(pkg, cuda):
         M.multi_rhs_matmul(M.split_tf32(Z), torch.zeros(5, 3, dtype=torch.complex64, device=cuda))
 
 
-def test_gmres_multi_random_system(pkg, cuda):
-    """Lockstep multi-RHS GMRES on a well-conditioned complex system against dense LU."""
+@pytest.mark.parametrize("m", [64, 7, 1])
+def test_gmres_multi_random_system(pkg, cuda, m):
+    """Lockstep multi-RHS GMRES on a well-conditioned complex system against dense LU (odd
+    column counts run on the internal even width with an inactive padding column)."""
     M = pkg.mesh_MOM_3d
-    n, m = 512, 64
+    n = 512
     g = torch.Generator(device="cpu").manual_seed(3)
     Z = (torch.complex(torch.randn(n, n, generator=g), torch.randn(n, n, generator=g)) / n ** 0.5
          + 3 * torch.eye(n, dtype=torch.complex64))
@@ -58,6 +60,8 @@ def test_gmres_multi_random_system(pkg, cuda):
     # FP64 residual of every column, independent of the solver's own estimate
     res = torch.linalg.norm(B - Z.to(torch.complex128) @ X.cpu(), dim=0) / torch.linalg.norm(B, dim=0)
     assert res.max().item() < 3e-6
+    steps = info["column_iterations"].cpu()
+    assert steps.shape[0] == m and int(steps.max()) <= info["iterations"]
 
 
 def test_gmres_multi_matches_single_rhs_on_mom_system(pkg, cuda):
