@@ -56,6 +56,8 @@ WORKLOADS = {
     "batch_star64": (64, 4, 0),
     "batch_star64_efie": (64, 4, 0),
     "batch_star8": (8, 4, 0),
+    # scattered H on a field-point grid from vertex currents: (icosphere level, k, grid points per side)
+    "radiate_L5": (5, 10.0, 1024),
     # learned initial guess: (training meshes, held-out meshes, incidences per mesh)
     "learned_star": (5000, 256, 4),
     "learned_star_small": (500, 64, 4),
@@ -520,6 +522,124 @@ def main_laplace(args, rank, world, local_rank):
 # ---------------------------------------------------------------------------------------
 # many right-hand sides: tensor-core product + lockstep GMRES vs plain per-incidence GMRES
 # ---------------------------------------------------------------------------------------
+def main_radiate(args, rank, world, local_rank):
+    """Scattered H on an observation grid from vertex currents (the post-processing step of the
+    reference's MoM demo, demo_Helmholtz_MOM_3d.py:246-257)."""
+    level, k, side = WORKLOADS[args.workload]
+    import torch
+
+    pkg = importlib.import_module("mesh-ferrofluid_gb300")
+    R = pkg.roofline
+    config = {"workload": args.workload, "mesh": f"icosphere L{level}, radius 1", "ka": k,
+              "field_points": f"{side} x {side} grid on the plane y = 0.05, x, z in [-3, 3]",
+              "currents": "seeded complex vertex currents, vertex areas = sum of adjacent face areas / 3",
+              "parallelism": "replicas"}
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference's radiation step is torch "
+                              "tensor code inside its demo script; its algorithm is timed by cpu_baseline "
+                              "(the C oracle)"}), flush=True)
+        return
+    dev = torch.device("cuda", local_rank if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    v_np, f_np = pkg.meshes.icosphere(level, 1.0)
+    nv = v_np.shape[0]
+    rng = np.random.default_rng(0)
+    js_np = (rng.normal(size=(nv, 3)) + 1j * rng.normal(size=(nv, 3))).astype(np.complex64)
+    tri = v_np[f_np]
+    fa = 0.5 * np.linalg.norm(np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0]), axis=1)
+    va_np = np.zeros(nv)
+    np.add.at(va_np, f_np.reshape(-1), np.repeat(fa / 3.0, 3))
+    g1 = np.linspace(-3.0, 3.0, side)
+    gx, gz = np.meshgrid(g1, g1, indexing="ij")
+    pts_np = np.stack([gx.ravel(), 0.05 * np.ones(gx.size), gz.ravel()], -1).astype(np.float32)
+    verts = torch.tensor(v_np, dtype=torch.float32, device=dev)
+    va = torch.tensor(va_np, dtype=torch.float32, device=dev)
+    js = torch.tensor(js_np, device=dev)
+    pts = torch.tensor(pts_np, device=dev)
+    H = torch.empty((pts.shape[0], 3), dtype=torch.complex64, device=dev)
+    M = pkg.mesh_MOM_3d
+    pairs = float(pts.shape[0]) * nv
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        M.radiate_H(pts, verts, va, js, k, out=H)
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.3)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize(dev)
+    for e0, e1 in ev:
+        e0.record(stream)
+        M.radiate_H(pts, verts, va, js, k, out=H)
+        e1.record(stream)
+    torch.cuda.synchronize(dev)
+    clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    ms_per_step = sum(ms) / args.steps
+    kern_s = statistics.mean(ms) / 1e3
+    peaks = R.measured_peaks(REPO)
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak, mufu_peak = R.fp32_peak_tflops(sm_max), R.mufu_peak_gops(sm_max)
+    flop, mufu = pairs * R.RADIATE_FLOP_PER_PAIR, pairs * R.RADIATE_MUFU_PER_PAIR
+    line = {"metric": "scattered-field (point, vertex) pairs/s", "value": world * pairs / (ms_per_step / 1e3),
+            "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic", "config": config,
+            "roofline": {"bound": "fp32", "achieved": flop / kern_s / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": flop / kern_s / 1e12 / fp32_peak, "traffic": None,
+                         "peak_source": "derived FP32 SIMT peak at the max SM clock",
+                         "mufu": {"achieved_gops": mufu / kern_s / 1e9, "peak_gops": mufu_peak,
+                                  "frac": mufu / kern_s / 1e9 / mufu_peak},
+                         "algorithmic": f"{R.RADIATE_FLOP_PER_PAIR} FLOP + {R.RADIATE_MUFU_PER_PAIR} MUFU per "
+                                        "(field point, vertex) pair",
+                         "kernel": "radiate_h_kernel<float>", "kernel_ms": kern_s * 1e3},
+            "clocks": clocks.summary(), "gpu_launches": args.steps}
+    if not args.no_e2e:
+        h_p = torch.tensor(pts_np).pin_memory()
+        h_j = torch.tensor(js_np).pin_memory()
+        h_H = torch.empty((pts.shape[0], 3), dtype=torch.complex64, pin_memory=True)
+        d_p, d_j = torch.empty_like(pts), torch.empty_like(js)
+
+        def e2e_step():
+            d_p.copy_(h_p, non_blocking=True)
+            d_j.copy_(h_j, non_blocking=True)
+            M.radiate_H(d_p, verts, va, d_j, k, out=H)
+            h_H.copy_(H, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize(dev)
+        n_e2e = max(2, min(args.steps, 3))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n_e2e):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        e2e_ms = e0.elapsed_time(e1) / n_e2e
+        line["e2e"] = {"value": world * pairs / (e2e_ms / 1e3), "unit": "pairs/s",
+                       "h2d_bytes_per_step": h_p.numel() * 4 + h_j.numel() * 8,
+                       "d2h_bytes_per_step": h_H.numel() * 8, "ms_per_step": e2e_ms, "steps": n_e2e,
+                       "path": "mesh_MOM_3d.radiate_H (C ABI mb_radiate_h_f32), pinned field points and "
+                               "currents in, H back to pinned host memory"}
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+
+        n_s = 4096
+        threads = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+        sel = np.linspace(0, pts_np.shape[0] - 1, n_s).astype(np.int64)
+        t0 = time.perf_counter()
+        O.radiate_h(pts_np[sel].astype(np.float64), v_np, va_np, js_np.astype(np.complex128), k)
+        dt_cpu = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n_s * float(nv) / dt_cpu, "unit": "pairs/s", "cores": threads,
+                                "kind": "port",
+                                "sample": f"{n_s} of the {pts_np.shape[0]} field points against all {nv} vertices, "
+                                          "double C oracle of the reference's formula (functions.py:844-868)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main_mrhs(args, rank, world, local_rank):
     level, k, ndir = WORKLOADS[args.workload]
     import torch
@@ -1016,6 +1136,8 @@ def main():
         return main_batch(args, rank, world, local_rank)
     if args.workload.startswith("learned_"):
         return main_learned(args, rank, world, local_rank)
+    if args.workload.startswith("radiate_"):
+        return main_radiate(args, rank, world, local_rank)
     level, k, gq = WORKLOADS[args.workload]
     n_faces = 20 * 4 ** level
     n_edges = 30 * 4 ** level

@@ -7,6 +7,8 @@ Per kernel evaluation (one test point x one source point):
 * MoM EFIE only:                                       30 FP32 FLOP, 3 MUFU
 * Laplace single layer (1/4 pi R times P1 products):   15 FP32 FLOP, 1 MUFU (rsqrt)
 * Laplace double layer (grad_y G . n times P1):        22 FP32 FLOP, 1 MUFU
+* Scattered H per (field point, vertex) pair ((1 + jkR) e^{jkR} / (4 pi R^3) times the
+  complex cross product (A J) x (x - y), accumulated):   61 FP32 FLOP, 3 MUFU (rsqrt, sin, cos)
 
 An FMA counts as 2 FLOP.  Units: a "triangle pair" is one ordered (test, source) face
 pair; with the reference's collapsed Gauss rule of order q (test q^2 points, source
@@ -25,6 +27,8 @@ EFIE_MUFU_PER_EVAL = 3
 LAPLACE_SL_FLOP_PER_EVAL = 15
 LAPLACE_DL_FLOP_PER_EVAL = 22
 LAPLACE_MUFU_PER_EVAL = 1
+RADIATE_FLOP_PER_PAIR = 61
+RADIATE_MUFU_PER_PAIR = 3
 # nominal FP64 rate of a GB300 (far below its FP32 SIMT rate); used only as the denominator
 # of FP64 kernels, which have no measured figure
 FP64_NOMINAL_TFLOPS = 1.25
