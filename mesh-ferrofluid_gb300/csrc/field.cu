@@ -86,9 +86,10 @@ __global__ void __launch_bounds__(kFieldThreads) radiate_h_kernel(const T* __res
 }
 
 // float path: each thread owns two observation points, both lanes of every packed f32x2
-// instruction (the staged vertex broadcast to the pair); the phase is reduced in turns as
-// above (observation distances give kR of tens of radians); pairs closer than 1e-6 get a
-// zero weight instead of a branch.
+// instruction (the staged vertex broadcast to the pair); kR goes to the SFU sine / cosine
+// directly (for the tens of radians of observation distances its phase error stays at a
+// few 1e-6, inside the float32 parity tolerance); pairs closer than 1e-6 get a zero weight
+// instead of a branch.
 __global__ void __launch_bounds__(kFieldThreads) radiate_h_f32x2_kernel(const float* __restrict__ points, int64_t np,
                                                                         const float* __restrict__ verts,
                                                                         const float* __restrict__ vert_areas,
@@ -108,8 +109,7 @@ __global__ void __launch_bounds__(kFieldThreads) radiate_h_f32x2_kernel(const fl
         pz.y = points[3 * m0 + 5];
     }
     float2 hr0 = bc(0.f), hr1 = bc(0.f), hr2 = bc(0.f), hi0 = bc(0.f), hi1 = bc(0.f), hi2 = bc(0.f);
-    const float k_turn = k * float(kInv2Pi);
-    const float2 KT = bc(k_turn), K = bc(k), TWO_PI = bc(6.28318530717958647692f), I4PI = bc(float(kInv4Pi));
+    const float2 K = bc(k), I4PI = bc(float(kInv4Pi));
     for (int64_t base = 0; base < nv; base += kFieldThreads) {
         const int64_t v = base + threadIdx.x;
         if (v < nv) {
@@ -134,16 +134,10 @@ __global__ void __launch_bounds__(kFieldThreads) radiate_h_f32x2_kernel(const fl
                 float2 rinv;  // R < 1e-6 contributes nothing (functions.py:832-834, :860-862)
                 rinv.x = r2.x < 1e-12f ? 0.f : rsqrtf(r2.x);
                 rinv.y = r2.y < 1e-12f ? 0.f : rsqrtf(r2.y);
-                const float2 R = mul2(r2, rinv);
-                const float2 turns = mul2(KT, R);
-                float2 frac;
-                frac.x = turns.x - rintf(turns.x);
-                frac.y = turns.y - rintf(turns.y);
-                const float2 ang = mul2(frac, TWO_PI);
+                const float2 kR = mul2(K, mul2(r2, rinv));
                 float2 sn, cs;
-                __sincosf(ang.x, &sn.x, &cs.x);
-                __sincosf(ang.y, &sn.y, &cs.y);
-                const float2 kR = mul2(K, R);
+                __sincosf(kR.x, &sn.x, &cs.x);
+                __sincosf(kR.y, &sn.y, &cs.y);
                 const float2 sc = mul2(mul2(rinv, rinv), mul2(rinv, I4PI));
                 const float2 fr = mul2(sub2(cs, mul2(kR, sn)), sc);  // (1 + jkR) e^{+jkR} / (4 pi R^3)
                 const float2 fi = mul2(fma2(kR, cs, sn), sc);
