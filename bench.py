@@ -58,6 +58,8 @@ WORKLOADS = {
     "batch_star8": (8, 4, 0),
     # scattered H on a field-point grid from vertex currents: (icosphere level, k, grid points per side)
     "radiate_L5": (5, 10.0, 1024),
+    # GPU mesh topology (unique edges + face-edge map + edge faces, near-pair list, Z-row map)
+    "topology_L7": (7,),
     # learned initial guess: (training meshes, held-out meshes, incidences per mesh)
     "learned_star": (5000, 256, 4),
     "learned_star_small": (500, 64, 4),
@@ -640,6 +642,102 @@ def main_radiate(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def main_topology(args, rank, world, local_rank):
+    """Mesh topology on the GPU: get_edge_unique (mesh_utils.py:921-977), the near-pair list
+    (the nonzeros of compute_panel_relation, mesh_utils.py:700-725, built in O(F)) and the
+    Z-row -> face-edge-row map of the edge-ordered assembly."""
+    (level,) = WORKLOADS[args.workload]
+    import torch
+
+    pkg = importlib.import_module("mesh-ferrofluid_gb300")
+    U, M = pkg.utils, pkg.mesh_MOM_3d
+    v_np, f_np = pkg.meshes.icosphere(level, 1.0)
+    nf, nv = f_np.shape[0], v_np.shape[0]
+    config = {"workload": args.workload, "mesh": f"icosphere L{level}", "n_faces": nf, "n_verts": nv,
+              "outputs": "edges [E, 2], face-edge map [3F], edge faces [E, 2], near pairs [n, 2], Z-row map [2E + 1]",
+              "parallelism": "replicas"}
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "topology is not the headline path; its CPU "
+                              "run is the cpu_baseline of this workload"}), flush=True)
+        return
+    dev = torch.device("cuda", local_rank if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    verts = torch.tensor(v_np, dtype=torch.float32, device=dev)
+    faces = torch.tensor(f_np, dtype=torch.int32, device=dev)
+
+    def topo(v, f):
+        edges, fei, adj = U.get_edge_unique(v, f)
+        pairs = U.shared_vertex_pairs(f)
+        er = torch.empty(2 * edges.shape[0] + 1, dtype=torch.int32, device=f.device)
+        pkg._lib.call("mb_mom_edge_rows", pkg._lib.ptr(fei), f.shape[0], edges.shape[0], pkg._lib.ptr(er),
+                      pkg._lib.stream_of(f))
+        return edges, fei, adj, pairs, er
+
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        out = topo(verts, faces)
+    torch.cuda.synchronize(dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    for e0, e1 in ev:
+        e0.record(stream)
+        out = topo(verts, faces)
+        e1.record(stream)
+    torch.cuda.synchronize(dev)
+    clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    ms_per_step = sum(ms) / args.steps
+    edges, fei, adj, pairs, er = out
+    ne, npairs = int(edges.shape[0]), int(pairs.shape[0])
+    io_bytes = 12 * nf + 8 * ne + 12 * nf + 8 * ne + 8 * npairs + 4 * (2 * ne + 1)
+    hbm = float(pkg.roofline.measured_peaks(REPO).get("hbm_gbs", 6800.0))
+    line = {"metric": "mesh-topology faces/s", "value": world * nf / (ms_per_step / 1e3), "unit": "faces/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32 / int64",
+            "data": "synthetic", "config": config, "n_edges": ne, "near_pairs": npairs,
+            "roofline": {"bound": "hbm", "achieved": io_bytes / (ms_per_step / 1e3) / 1e9, "peak": hbm,
+                         "unit": "GB/s", "frac": io_bytes / (ms_per_step / 1e3) / 1e9 / hbm, "traffic": None,
+                         "algorithmic": "faces in + every output written once (sort passes not counted)",
+                         "note": "sort / unique based (torch), latency-bound at this size"},
+            "clocks": clocks.summary(), "gpu_launches": None}
+    if not args.no_e2e:
+        h_f = torch.tensor(f_np, dtype=torch.int32).pin_memory()
+        d_f = torch.empty_like(faces)
+
+        def e2e_step():
+            d_f.copy_(h_f, non_blocking=True)
+            res = topo(verts, d_f)
+            return [t.to("cpu", non_blocking=True) for t in res]
+
+        e2e_step()
+        torch.cuda.synchronize(dev)
+        n_e2e = max(2, min(args.steps, 3))
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            outs = e2e_step()
+        torch.cuda.synchronize(dev)
+        e2e_s = (time.perf_counter() - t0) / n_e2e
+        line["e2e"] = {"value": world * nf / e2e_s, "unit": "faces/s", "h2d_bytes_per_step": h_f.numel() * 4,
+                       "d2h_bytes_per_step": sum(t.numel() * t.element_size() for t in outs),
+                       "ms_per_step": e2e_s * 1e3, "steps": n_e2e,
+                       "path": "utils.get_edge_unique + utils.shared_vertex_pairs + mb_mom_edge_rows, faces from "
+                               "pinned host memory, every output back to the host"}
+    if rank == 0 and not args.no_cpu_baseline:
+        vc, fc = torch.tensor(v_np), torch.tensor(f_np, dtype=torch.int32)
+        t0 = time.perf_counter()
+        U.get_edge_unique(vc, fc)
+        U.shared_vertex_pairs(fc)
+        dt_cpu = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": nf / dt_cpu, "unit": "faces/s", "cores": torch.get_num_threads(),
+                                "kind": "port", "sample": "the same unique-edge and near-pair construction with "
+                                "torch on the host (the reference's get_edge_unique is this torch.unique; its "
+                                "near pairs come from the dense O(F^2) relation, infeasible at this size)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main_mrhs(args, rank, world, local_rank):
     level, k, ndir = WORKLOADS[args.workload]
     import torch
@@ -1138,6 +1236,8 @@ def main():
         return main_learned(args, rank, world, local_rank)
     if args.workload.startswith("radiate_"):
         return main_radiate(args, rank, world, local_rank)
+    if args.workload.startswith("topology_"):
+        return main_topology(args, rank, world, local_rank)
     level, k, gq = WORKLOADS[args.workload]
     n_faces = 20 * 4 ** level
     n_edges = 30 * 4 ** level

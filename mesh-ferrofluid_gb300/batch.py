@@ -31,7 +31,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .utils import compute_panel_relation, get_edge_unique
+from .utils import get_edge_unique, shared_vertex_pairs
 
 _DESC = 6
 
@@ -57,8 +57,7 @@ class MeshBatch:
             f = torch.as_tensor(np.asarray(f)).to(device=dev, dtype=torch.int32)
             edges, fe, _ = get_edge_unique(v, f)
             ne, nf = int(edges.shape[0]), int(f.shape[0])
-            rel = compute_panel_relation(f)
-            near.append(torch.nonzero(rel > 0).to(torch.int32) + f_off)
+            near.append(shared_vertex_pairs(f) + f_off)
             verts.append(v)
             faces.append(f + v_off)
             fei.append(fe.reshape(-1, 3).to(torch.int32))

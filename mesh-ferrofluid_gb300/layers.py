@@ -102,9 +102,9 @@ def hypersingular_from_v0(verts: torch.Tensor, faces: torch.Tensor, v0: torch.Te
 
 def laplace_near_pairs(faces: torch.Tensor) -> torch.Tensor:
     """Ordered face pairs sharing a vertex (incl. self), [n, 2] int32, sorted by first face."""
-    from .utils import compute_panel_relation
+    from .utils import shared_vertex_pairs
 
-    return torch.nonzero(compute_panel_relation(faces) > 0).to(torch.int32).contiguous()
+    return shared_vertex_pairs(faces)
 
 
 def laplace_sym_panels(verts: torch.Tensor, faces: torch.Tensor, layer: int, order: int,

@@ -297,11 +297,11 @@ def interpolate_vert_js(verts, faces, face_edge_indices, face_areas, i_coeff, ou
 # EFIE with the symmetric 7-point rule and singularity extraction (new capability)
 # ---------------------------------------------------------------------------------------
 def near_pairs(faces) -> torch.Tensor:
-    """All ordered face pairs sharing at least one vertex (incl. self), [n, 2] int32."""
-    from .utils import compute_panel_relation
+    """All ordered face pairs sharing at least one vertex (incl. self), [n, 2] int32, sorted by
+    test face (``utils.shared_vertex_pairs``: O(F) memory)."""
+    from .utils import shared_vertex_pairs
 
-    rel = compute_panel_relation(faces)
-    return torch.nonzero(rel > 0).to(torch.int32).contiguous()
+    return shared_vertex_pairs(faces)
 
 
 def assemble_Z_rwg_sym(verts, faces, face_edge_indices, n_edges, wavenumber, out=None, pairs=None,

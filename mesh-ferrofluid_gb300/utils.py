@@ -281,6 +281,34 @@ def get_edge_unique(verts: torch.Tensor, faces: torch.Tensor):
     return edges, inv.to(faces.dtype), adj.to(faces.dtype)
 
 
+def shared_vertex_pairs(faces: torch.Tensor) -> torch.Tensor:
+    """All ordered face pairs sharing at least one vertex (each face with itself included),
+    [n, 2] int32 sorted by first face, then second: the nonzeros of
+    ``compute_panel_relation`` (mesh_utils.py:700-725) in row-major order, built in O(F) memory
+    instead of from the dense [F, F] relation -- the vertex-face incidences sorted by vertex,
+    every ordered pair of faces around each vertex, one sorted unique of the pair keys."""
+    faces = faces.reshape(-1, 3)
+    nf = faces.shape[0]
+    dev = faces.device
+    if nf == 0:
+        return torch.zeros((0, 2), dtype=torch.int32, device=dev)
+    v = faces.reshape(-1).long()
+    f = torch.arange(nf, device=dev, dtype=torch.long).repeat_interleave(3)
+    order = torch.argsort(v, stable=True)
+    vs, fs = v[order], f[order]
+    _, counts = torch.unique_consecutive(vs, return_counts=True)
+    starts = torch.cumsum(counts, 0) - counts
+    c2 = counts * counts
+    pstart = torch.cumsum(c2, 0) - c2
+    gid = torch.repeat_interleave(torch.arange(counts.numel(), device=dev), c2)
+    local = torch.arange(int(c2.sum()), device=dev) - pstart[gid]
+    cg = counts[gid]
+    fa = fs[starts[gid] + local // cg]
+    fb = fs[starts[gid] + local % cg]
+    key = torch.unique(fa * nf + fb)
+    return torch.stack((key // nf, key % nf), dim=-1).to(torch.int32).contiguous()
+
+
 def compute_panel_relation(faces: torch.Tensor) -> torch.Tensor:
     """[F, F] uint8 shared-vertex relation (0 separate .. 3 same face), CUDA kernel."""
     faces = _lib.check_tensor(faces.contiguous(), "faces", dtype=torch.int32, ndim=2)

@@ -131,3 +131,18 @@ def test_ops_reject_cpu_tensors(pkg):
     z = torch.zeros((1, 3, 3))
     with pytest.raises(ValueError, match="CUDA"):
         pkg.mesh_MOM_3d.create_MOM_Zmat_3d_forward(v, f, a, n, p, w, p, w, z, z.clone(), 1.0)
+
+
+def test_shared_vertex_pairs_equal_dense_relation(pkg):
+    """The O(F) near-pair builder returns exactly the nonzeros of the dense shared-vertex
+    relation, in row-major order (closed meshes, a non-manifold fan and an empty mesh)."""
+    meshes = [pkg.meshes.icosphere(2), pkg.meshes.star_shape(2, seed=4), pkg.meshes.ellipsoid(1),
+              (None, np.array([[0, 1, 2], [1, 0, 3], [0, 1, 4], [5, 6, 7]], np.int32))]
+    for _, f in meshes:
+        got = pkg.utils.shared_vertex_pairs(torch.tensor(f, dtype=torch.int32)).numpy()
+        dense = np.zeros((f.shape[0], f.shape[0]), bool)
+        for a in range(3):
+            for b in range(3):
+                dense |= f[:, a][:, None] == f[:, b][None, :]
+        assert np.array_equal(got, np.argwhere(dense))
+    assert pkg.utils.shared_vertex_pairs(torch.zeros((0, 3), dtype=torch.int32)).shape == (0, 2)
