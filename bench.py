@@ -60,6 +60,9 @@ WORKLOADS = {
     "radiate_L5": (5, 10.0, 1024),
     # GPU mesh topology (unique edges + face-edge map + edge faces, near-pair list, Z-row map)
     "topology_L7": (7,),
+    # Laplace mixed Dirichlet / Neumann solve, u = z on the unit sphere: (icosphere level, dtype)
+    "laplace_mixed_L4": (4, "f32"),
+    "laplace_mixed_L3": (3, "f32"),
     # learned initial guess: (training meshes, held-out meshes, incidences per mesh)
     "learned_star": (5000, 256, 4),
     "learned_star_small": (500, 64, 4),
@@ -738,6 +741,180 @@ def main_topology(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def main_lapmixed(args, rank, world, local_rank):
+    """Mixed Dirichlet / Neumann Laplace solve through MeshBEMSolver3d.solve (the reference's
+    facade, mesh_BEM_solver_3d.py:197-373): symmetric-rule V, K and hypersingular D,
+    packed P1 matrices, the block system [[V, -K], [K', D]] and its dense solve."""
+    level, dts = WORKLOADS[args.workload]
+    import torch
+
+    pkg = importlib.import_module("mesh-ferrofluid_gb300")
+    R, L, U = pkg.roofline, pkg.layers, pkg.utils
+    v_np, f_np = pkg.meshes.icosphere(level, 1.0)
+    nf, nv = f_np.shape[0], v_np.shape[0]
+    config = {"workload": args.workload, "mesh": f"icosphere L{level}, radius 1", "n_faces": nf, "n_verts": nv,
+              "problem": "u = z: Dirichlet data on z > 0, Neumann data du/dn = z on z <= 0",
+              "rule": "dunavant7 (7 x 7 points, pairs sharing a vertex in closed form, FP64)",
+              "operators": f"V, K, D packed [V, V] {dts} straight from the face pairs (no [F, F, 3, 3] panels)",
+              "parallelism": "replicas"}
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference's Neumann / mixed branches never "
+                              "run (its hypersingular layer is None); the oracle's operators are timed by "
+                              "cpu_baseline"}), flush=True)
+        return
+    dev = torch.device("cuda", local_rank if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    dt = torch.float32 if dts == "f32" else torch.float64
+    verts = torch.tensor(v_np, dtype=dt, device=dev)
+    faces = torch.tensor(f_np, dtype=torch.int32, device=dev)
+    z = verts[:, 2:3].clone()
+    D_, N_ = int(pkg.BoundaryType.DIRICHLET), int(pkg.BoundaryType.NEUMANN)
+    flags = torch.where(z > 0, D_, N_).to(torch.uint8)[None]
+    g = torch.where(z > 0, z, 0.0)[None]
+    h = torch.where(z > 0, 0.0, z)[None]
+    solver = pkg.MeshBEMSolver3d(gaussQR=3, order_type=1, BEM_type=int(pkg.BEMType.LAPLACE), wavenumber=1.0,
+                                 logger=None, dtype=dt, device=dev, rule="dunavant7", solver="schur")
+    config["solver"] = ("schur: Cholesky factors of V on the Dirichlet vertices and of the Schur complement "
+                        "D + K V^-1 K^T on the Neumann ones (cuSOLVER / cuBLAS through torch)")
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        out = solver.solve(verts, faces, g, h, flags)
+    torch.cuda.synchronize(dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.3)
+    calls0 = pkg._lib.call_count
+    for e0, e1 in ev:
+        e0.record(stream)
+        out = solver.solve(verts, faces, g, h, flags)
+        e1.record(stream)
+    torch.cuda.synchronize(dev)
+    clocks.stop()
+    abi_calls = pkg._lib.call_count - calls0
+    ms = [a.elapsed_time(b) for a, b in ev]
+    ms_per_step = sum(ms) / args.steps
+    neu, dirv = out
+    lower = (z <= 0).reshape(-1)
+    far = (z > 0.3).reshape(-1)
+    err_u = float(torch.linalg.norm(dirv[0][lower] - z[lower]) / torch.linalg.norm(z[lower]))
+    err_t = float(torch.linalg.norm(neu[0][far] - z[far]) / torch.linalg.norm(z[far]))
+
+    # per-stage times (the same calls solve() makes, timed one by one)
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize(dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            r = fn()
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        return a.elapsed_time(b) / reps, r
+
+    t_near, near = timed(lambda: U.shared_vertex_pairs(faces))
+    t_v, Vt = timed(lambda: L.laplace_sym_tight(verts, faces, 1, near))
+    t_k, Kt = timed(lambda: L.laplace_sym_tight(verts, faces, 2, near))
+    t_d, Dt = timed(lambda: L.laplace_sym_tight(verts, faces, 3, near))
+    t_vp, Vp = timed(lambda: L.laplace_sym_panels(verts, faces, 1, 1, near))
+    t_pack, _ = timed(lambda: U.pack_matrix_tight(1, Vp, verts, faces))
+    del Vp
+    is_d, is_n = (z > 0).reshape(-1), (z <= 0).reshape(-1)
+    ks = Kt.transpose(0, 1)
+    A = torch.cat((torch.cat((Vt[is_d][:, is_d], -ks[is_d][:, is_n]), 1),
+                   torch.cat((ks.transpose(0, 1)[is_n][:, is_d], Dt[is_n][:, is_n]), 1)), 0)
+    rhs = torch.ones(nv, 1, dtype=dt, device=dev)
+    nd = int(is_d.sum())
+    t_lu, _ = timed(lambda: torch.linalg.solve(A, rhs))
+    SM = importlib.import_module("mesh-ferrofluid_gb300.mesh_BEM_solver_3d")
+    t_schur, _ = timed(lambda: SM._schur_solve(Vt[is_d][:, is_d], ks[is_d][:, is_n], Dt[is_n][:, is_n],
+                                               rhs[:nd, 0], rhs[nd:, 0]))
+    peaks = R.measured_peaks(REPO)
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = R.fp32_peak_tflops(sm_max)
+    flop_v = float(nf) ** 2 * 49 * R.LAPLACE_SYM_P1_FLOP_PER_EVAL
+    ach = flop_v / (t_v / 1e3) / 1e12
+    line = {"metric": "mixed Dirichlet/Neumann solve time", "value": ms_per_step, "unit": "ms",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": dts, "data": "synthetic",
+            "config": config,
+            "accuracy": {"u_rel_err_neumann_part": err_u, "dudn_rel_err_dirichlet_part_z_gt_0.3": err_t},
+            "breakdown_ms": {"near_pairs": t_near, "V_packed": t_v, "K_packed": t_k, "D_packed": t_d,
+                             "schur_solve_blocks": t_schur,
+                             "not_on_the_path": {"V_panels": t_vp, "pack_V_panels": t_pack,
+                                                 "lu_solve_block_system": t_lu}},
+            "roofline": {"kernel": "lap_sym_tight_kernel<float, 1> + lap_sym_near_kernel (packed V)",
+                         "bound": "fp32" if dts == "f32" else "fp64", "achieved": ach,
+                         "peak": fp32_peak if dts == "f32" else R.FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                         "frac": ach / (fp32_peak if dts == "f32" else R.FP64_NOMINAL_TFLOPS),
+                         "peak_source": "derived FP32 SIMT peak at the max SM clock",
+                         "traffic": None,
+                         "algorithmic": f"{R.LAPLACE_SYM_P1_FLOP_PER_EVAL} FLOP + 1 rsqrt per evaluation x 49 "
+                                        "evaluations per face pair x F^2 (near pairs counted as separated); the "
+                                        "packed path stores no panels (HBM traffic: mesh + 3 V reductions per row)",
+                         "kernel_ms": t_v},
+            "clocks": clocks.summary(), "gpu_launches": abi_calls,
+            "gpu_launches_note": "C-ABI calls in the timed region (each launches one or two of the library's "
+                                 "kernels); torch's sort / unique / LU kernels not counted"}
+    if not args.no_e2e:
+        h_v = torch.tensor(v_np, dtype=dt).pin_memory()
+        h_f = torch.tensor(f_np, dtype=torch.int32).pin_memory()
+        h_in = [t.cpu().pin_memory() for t in (g, h, flags)]
+        h_out = [torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in out]
+        d_v, d_f = torch.empty_like(verts), torch.empty_like(faces)
+        d_in = [torch.empty_like(t) for t in (g, h, flags)]
+
+        def e2e_step():
+            d_v.copy_(h_v, non_blocking=True)
+            d_f.copy_(h_f, non_blocking=True)
+            for d, hh in zip(d_in, h_in):
+                d.copy_(hh, non_blocking=True)
+            res = solver.solve(d_v, d_f, *d_in)
+            for hh, r in zip(h_out, res):
+                hh.copy_(r, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize(dev)
+        n_e2e = max(2, min(args.steps, 3))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n_e2e):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        e2e_ms = e0.elapsed_time(e1) / n_e2e
+        line["e2e"] = {"value": e2e_ms, "unit": "ms",
+                       "h2d_bytes_per_step": h_v.numel() * h_v.element_size() + h_f.numel() * 4 +
+                                             sum(t.numel() * t.element_size() for t in h_in),
+                       "d2h_bytes_per_step": sum(t.numel() * t.element_size() for t in h_out),
+                       "ms_per_step": e2e_ms, "steps": n_e2e,
+                       "path": "MeshBEMSolver3d.solve (C ABI mb_laplace_sym_tight_*), pinned host mesh and boundary "
+                               "data in, both traces back"}
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+
+        threads = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+        n_s = min(nf, 1024)
+        rows = (0, n_s)
+        t0 = time.perf_counter()
+        O.laplace_sym(v_np, f_np, 1, 1, rows=rows)
+        O.laplace_sym(v_np, f_np, 2, 1, rows=rows)
+        O.laplace_sym(v_np, f_np, 1, 0, rows=rows)
+        t_ops = (time.perf_counter() - t0) * nf / n_s
+        An = np.random.default_rng(0).normal(size=(nv, nv)) + nv * np.eye(nv)
+        t0 = time.perf_counter()
+        np.linalg.solve(An, np.ones(nv))
+        t_solve = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": (t_ops + t_solve) * 1e3, "unit": "ms", "cores": threads, "kind": "port",
+                                "sample": f"V, K and V0 panels of the first {n_s} of {nf} face rows with the double "
+                                          f"C oracle (same rule), scaled to all rows, plus a numpy LU solve of "
+                                          f"size {nv}; D from V0 and the packing not counted"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main_mrhs(args, rank, world, local_rank):
     level, k, ndir = WORKLOADS[args.workload]
     import torch
@@ -1224,6 +1401,8 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.workload.startswith("ray_"):
         return main_rays(args, rank, world, local_rank)
+    if args.workload.startswith("laplace_mixed"):
+        return main_lapmixed(args, rank, world, local_rank)
     if args.workload.startswith("laplace_"):
         return main_laplace(args, rank, world, local_rank)
     if args.workload.startswith("mrhs_"):

@@ -477,6 +477,16 @@ int mb_laplace_hypersingular_f32(const float* verts, int64_t n_verts, const int3
 int mb_laplace_hypersingular_f64(const double* verts, int64_t n_verts, const int32_t* faces,
                                  int64_t n_faces, const double* v0, double* out, void* stream);
 
+/* The same operator packed like mb_pack_tight_* with order 1, straight from v0 [F, F]:
+ * packed[faces[fy,a], faces[fx,b]] += curl phi_a(fy) . curl phi_b(fx) * v0[fy, fx], without
+ * storing the [F, F, 3, 3] panels (the matrix MeshBEMSolver3d.solve uses,
+ * src/mesh_BEM/mesh_BEM_solver_3d.py:268-281).  packed: [n_verts, n_verts], accumulated (+=);
+ * needs 3 * n_verts * sizeof(T) <= 160 KiB of shared memory (MB_ERR_SIZE otherwise). */
+int mb_laplace_hypersingular_tight_f32(const float* verts, int64_t n_verts, const int32_t* faces,
+                                       int64_t n_faces, const float* v0, float* packed, void* stream);
+int mb_laplace_hypersingular_tight_f64(const double* verts, int64_t n_verts, const int32_t* faces,
+                                       int64_t n_faces, const double* v0, double* packed, void* stream);
+
 /* Symmetric-rule Laplace operators (an accurate mode next to the reference's rule of
  * double_integration_on_panels_3d, integrations_3d.py:252-452; same output layout):
  * out[fy, fx, a, b] = int_fy int_fx phi_a(y) phi_b(x) k(x, y) for rows fy in
@@ -491,6 +501,21 @@ int mb_laplace_sym_f32(const float* verts, int64_t n_verts, const int32_t* faces
 int mb_laplace_sym_f64(const double* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
                        int layer, int order, const int32_t* near_pairs, int64_t n_near,
                        int64_t row_begin, int64_t row_end, double* out, void* stream);
+
+/* Packed symmetric-rule operators [n_verts, n_verts] (+=) without the [F, F, 3, 3] panels:
+ * op 1 single layer and 2 double layer, P1 x P1, equal to mb_pack_tight_* (order 1) of the
+ * mb_laplace_sym_* panels; op 3 the hypersingular operator, equal to
+ * mb_laplace_hypersingular_tight_* of the P0 single-layer panels.  These are the matrices
+ * MeshBEMSolver3d.solve works with (src/mesh_BEM/mesh_BEM_solver_3d.py:197-373, get_Vmat_tight /
+ * get_Kmat_tight, single_layer_3d.py and double_layer_3d.py).  Test rows [row_begin, row_end)
+ * contribute; near_pairs as for mb_laplace_sym_*.  Needs 3 * n_verts * sizeof(T) <= 160 KiB of
+ * shared memory (MB_ERR_SIZE otherwise). */
+int mb_laplace_sym_tight_f32(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                             int op, const int32_t* near_pairs, int64_t n_near, int64_t row_begin,
+                             int64_t row_end, float* packed, void* stream);
+int mb_laplace_sym_tight_f64(const double* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                             int op, const int32_t* near_pairs, int64_t n_near, int64_t row_begin,
+                             int64_t row_end, double* packed, void* stream);
 
 /* Single-layer collocation system at face centroids (the Laplace form of the large sphere
  * solve; no counterpart in the reference): out[i - row_begin, j] = int_{T_j} 1/(4 pi

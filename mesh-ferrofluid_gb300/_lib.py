@@ -60,8 +60,12 @@ _SIGS = {
     "mb_mom_sym_rhs_rwg_c128": [_P, _I64, _P, _I64, _P, _I64, _P, _I, _P, _P],
     "mb_laplace_hypersingular_f32": [_P, _I64, _P, _I64, _P, _P, _P],
     "mb_laplace_hypersingular_f64": [_P, _I64, _P, _I64, _P, _P, _P],
+    "mb_laplace_hypersingular_tight_f32": [_P, _I64, _P, _I64, _P, _P, _P],
+    "mb_laplace_hypersingular_tight_f64": [_P, _I64, _P, _I64, _P, _P, _P],
     "mb_laplace_sym_f32": [_P, _I64, _P, _I64, _I, _I, _P, _I64, _I64, _I64, _P, _P],
     "mb_laplace_sym_f64": [_P, _I64, _P, _I64, _I, _I, _P, _I64, _I64, _I64, _P, _P],
+    "mb_laplace_sym_tight_f32": [_P, _I64, _P, _I64, _I, _P, _I64, _I64, _I64, _P, _P],
+    "mb_laplace_sym_tight_f64": [_P, _I64, _P, _I64, _I, _P, _I64, _I64, _I64, _P, _P],
     "mb_laplace_colloc_sl_f32": [_P, _I64, _P, _I64, _P, _I64, _I64, _I64, _P, _P],
     "mb_laplace_colloc_sl_f64": [_P, _I64, _P, _I64, _P, _I64, _I64, _I64, _P, _P],
     "mb_tc_selftest": [_P, _P],
@@ -158,8 +162,14 @@ def load():
     return _lib
 
 
+# number of C-ABI calls made so far (each launches one or more of the library's kernels)
+call_count = 0
+
+
 def call(name: str, *args) -> None:
+    global call_count
     lib = load()
+    call_count += 1
     rc = getattr(lib, name)(*args)
     if rc != 0:
         msg = lib.mb_last_error().decode(errors="replace")

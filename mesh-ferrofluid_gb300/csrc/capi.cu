@@ -55,8 +55,13 @@ int launch_pack_tight(const T*, const T*, const int32_t*, int64_t, int64_t, int,
 template <typename T>
 int launch_hypersingular(const T*, const int32_t*, int64_t, const T*, T*, cudaStream_t);
 template <typename T>
+int launch_hypersingular_tight(const T*, const int32_t*, int64_t, int64_t, const T*, T*, cudaStream_t);
+template <typename T>
 int launch_laplace_sym(const T*, const int32_t*, int64_t, int, int, const int32_t*, int64_t, int64_t, int64_t, T*,
                        cudaStream_t);
+template <typename T>
+int launch_laplace_sym_tight(const T*, const int32_t*, int64_t, int64_t, int, const int32_t*, int64_t, int64_t,
+                             int64_t, T*, cudaStream_t);
 template <typename T>
 int launch_laplace_colloc_sl(const T*, const int32_t*, int64_t, const int32_t*, int64_t, int64_t, int64_t, T*,
                              cudaStream_t);
@@ -410,6 +415,19 @@ MB_HYP(f32, float)
 MB_HYP(f64, double)
 #undef MB_HYP
 
+#define MB_HYPT(SFX, T)                                                                               \
+    int mb_laplace_hypersingular_tight_##SFX(const T* verts, int64_t n_verts, const int32_t* faces,     \
+                                             int64_t n_faces, const T* v0, T* packed, void* stream) {  \
+        MB_REQUIRE(n_faces >= 0 && n_verts >= 0, "bad sizes");                                        \
+        if (n_faces == 0) return MB_OK;                                                               \
+        MB_REQUIRE(verts && faces && v0 && packed, "null pointer argument");                          \
+        return launch_hypersingular_tight<T>(verts, faces, n_faces, n_verts, v0, packed,              \
+                                             as_stream(stream));                                      \
+    }
+MB_HYPT(f32, float)
+MB_HYPT(f64, double)
+#undef MB_HYPT
+
 #define MB_LSYM(SFX, T)                                                                               \
     int mb_laplace_sym_##SFX(const T* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,    \
                              int layer, int order, const int32_t* near_pairs, int64_t n_near,          \
@@ -436,6 +454,21 @@ MB_HYP(f64, double)
 MB_LSYM(f32, float)
 MB_LSYM(f64, double)
 #undef MB_LSYM
+
+#define MB_LSYMT(SFX, T)                                                                              \
+    int mb_laplace_sym_tight_##SFX(const T* verts, int64_t n_verts, const int32_t* faces,               \
+                                   int64_t n_faces, int op, const int32_t* near_pairs, int64_t n_near,  \
+                                   int64_t row_begin, int64_t row_end, T* packed, void* stream) {      \
+        MB_REQUIRE(n_faces >= 0 && n_verts >= 0 && n_near >= 0, "bad sizes");                          \
+        if (n_faces == 0) return MB_OK;                                                               \
+        MB_REQUIRE(verts && faces && packed && (near_pairs || n_near == 0), "null pointer argument"); \
+        MB_REQUIRE(0 <= row_begin && row_begin <= row_end && row_end <= n_faces, "bad row range");    \
+        return launch_laplace_sym_tight<T>(verts, faces, n_faces, n_verts, op, near_pairs, n_near,    \
+                                           row_begin, row_end, packed, as_stream(stream));            \
+    }
+MB_LSYMT(f32, float)
+MB_LSYMT(f64, double)
+#undef MB_LSYMT
 
 #define MB_SYM(SFX, T)                                                                                \
     int mb_mom_sym_zmat_rwg_##SFX(const T* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,   \

@@ -30,71 +30,80 @@ static __constant__ double c_d7[7][4] = {
     {0.05971587178976982, 0.47014206410511509, 0.47014206410511509, 0.13239415278850619},
 };
 
-// int_T 1/R dS and int_T (y - x)/R dS (FP64).
-__device__ __forceinline__ double edge_log(double rp, double rm, double lp, double lm) {
-    if ((lm >= 0.0 || lp >= 0.0) && rm + lm > 0.0) return log((rp + lp) / (rm + lm));
-    return log((rm - lm) / (rp - lp));
+// int_T 1/R dS and int_T (y - x)/R dS, in the arithmetic of R (float or double).  The
+// float form serves float outputs: its absolute error is ~1e-7 of the integral, below the
+// rounding of the stored value; the caller moves the coordinates next to the origin first.
+__device__ __forceinline__ float log_t(float x) { return logf(x); }
+__device__ __forceinline__ double log_t(double x) { return log(x); }
+__device__ __forceinline__ float atan2_t(float y, float x) { return atan2f(y, x); }
+__device__ __forceinline__ double atan2_t(double y, double x) { return atan2(y, x); }
+
+template <typename R>
+__device__ __forceinline__ R edge_log(R rp, R rm, R lp, R lm) {
+    if ((lm >= R(0) || lp >= R(0)) && rm + lm > R(0)) return log_t((rp + lp) / (rm + lm));
+    return log_t((rm - lm) / (rp - lp));
 }
 
-__device__ __forceinline__ void potential_integrals(const V3<double>& x, const V3<double> P[3], double* I1,
-                                                    V3<double>* Iv) {
-    V3<double> n = cross(P[1] - P[0], P[2] - P[1]);
-    n = (1.0 / sqrt(dot(n, n))) * n;
-    const double d = dot(x - P[0], n);
-    const V3<double> rho = x - d * n;
-    const double ad = fabs(d);
-    double s1 = 0.0;
-    V3<double> sv = v3<double>(0, 0, 0);
+template <typename R>
+__device__ __forceinline__ void potential_integrals(const V3<R>& x, const V3<R> P[3], R* I1, V3<R>* Iv) {
+    V3<R> n = cross(P[1] - P[0], P[2] - P[1]);
+    n = (R(1) / sqrt_t(dot(n, n))) * n;
+    const R d = dot(x - P[0], n);
+    const V3<R> rho = x - d * n;
+    const R ad = d < R(0) ? -d : d;
+    R s1 = R(0);
+    V3<R> sv = v3<R>(0, 0, 0);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        const V3<double> pm = P[i], pp = P[(i + 1) % 3];
-        V3<double> l = pp - pm;
-        l = (1.0 / sqrt(dot(l, l))) * l;
-        const V3<double> u = cross(l, n);
-        const double lp = dot(pp - rho, l), lm = dot(pm - rho, l);
-        const double p0 = dot(pp - rho, u);
-        const double r0sq = p0 * p0 + d * d;
-        const double rp = sqrt(r0sq + lp * lp), rm = sqrt(r0sq + lm * lm);
-        const double lg = edge_log(rp, rm, lp, lm);
-        s1 += p0 * lg - ad * (atan2(p0 * lp, r0sq + ad * rp) - atan2(p0 * lm, r0sq + ad * rm));
-        sv = sv + (0.5 * (r0sq * lg + lp * rp - lm * rm)) * u;
+        const V3<R> pm = P[i], pp = P[(i + 1) % 3];
+        V3<R> l = pp - pm;
+        l = (R(1) / sqrt_t(dot(l, l))) * l;
+        const V3<R> u = cross(l, n);
+        const R lp = dot(pp - rho, l), lm = dot(pm - rho, l);
+        const R p0 = dot(pp - rho, u);
+        const R r0sq = p0 * p0 + d * d;
+        const R rp = sqrt_t(r0sq + lp * lp), rm = sqrt_t(r0sq + lm * lm);
+        const R lg = edge_log(rp, rm, lp, lm);
+        s1 += p0 * lg - ad * (atan2_t(p0 * lp, r0sq + ad * rp) - atan2_t(p0 * lm, r0sq + ad * rm));
+        sv = sv + (R(0.5) * (r0sq * lg + lp * rp - lm * rm)) * u;
     }
     *I1 = s1;
     *Iv = sv - (d * s1) * n;
 }
 
-// Double-layer integrals (FP64): *omega = int_T n.(y - x)/R^3 dS (signed solid angle) and
+// Double-layer integrals: *omega = int_T n.(y - x)/R^3 dS (signed solid angle) and
 // *J = int_T (rho_y - rho)/R^3 dS (in-plane vector); *d = n.(x - P0).  When |d| is below
 // dtol the point lies in the triangle's plane, where n.(x - y) vanishes: omega = 0 (the
 // principal value) and J is not needed (it is multiplied by d); both are returned as 0.
-__device__ __forceinline__ void dl_integrals(const V3<double>& x, const V3<double> P[3], double dtol,
-                                             double* omega, V3<double>* J, double* dout) {
-    V3<double> n = cross(P[1] - P[0], P[2] - P[1]);
-    n = (1.0 / sqrt(dot(n, n))) * n;
-    const double d = dot(x - P[0], n);
+template <typename R>
+__device__ __forceinline__ void dl_integrals(const V3<R>& x, const V3<R> P[3], R dtol, R* omega, V3<R>* J,
+                                             R* dout) {
+    V3<R> n = cross(P[1] - P[0], P[2] - P[1]);
+    n = (R(1) / sqrt_t(dot(n, n))) * n;
+    const R d = dot(x - P[0], n);
     *dout = d;
-    if (fabs(d) <= dtol) {
-        *omega = 0.0;
-        *J = v3<double>(0, 0, 0);
+    if ((d < R(0) ? -d : d) <= dtol) {
+        *omega = R(0);
+        *J = v3<R>(0, 0, 0);
         return;
     }
-    const V3<double> r0 = P[0] - x, r1 = P[1] - x, r2 = P[2] - x;
-    const double l0 = sqrt(dot(r0, r0)), l1 = sqrt(dot(r1, r1)), l2 = sqrt(dot(r2, r2));
-    const double num = dot(r0, cross(r1, r2));
-    const double den = l0 * l1 * l2 + dot(r0, r1) * l2 + dot(r0, r2) * l1 + dot(r1, r2) * l0;
-    *omega = 2.0 * atan2(num, den);
-    const V3<double> rho = x - d * n;
-    V3<double> jv = v3<double>(0, 0, 0);
+    const V3<R> r0 = P[0] - x, r1 = P[1] - x, r2 = P[2] - x;
+    const R l0 = sqrt_t(dot(r0, r0)), l1 = sqrt_t(dot(r1, r1)), l2 = sqrt_t(dot(r2, r2));
+    const R num = dot(r0, cross(r1, r2));
+    const R den = l0 * l1 * l2 + dot(r0, r1) * l2 + dot(r0, r2) * l1 + dot(r1, r2) * l0;
+    *omega = R(2) * atan2_t(num, den);
+    const V3<R> rho = x - d * n;
+    V3<R> jv = v3<R>(0, 0, 0);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        const V3<double> pm = P[i], pp = P[(i + 1) % 3];
-        V3<double> l = pp - pm;
-        l = (1.0 / sqrt(dot(l, l))) * l;
-        const V3<double> u = cross(l, n);
-        const double lp = dot(pp - rho, l), lm = dot(pm - rho, l);
-        const double p0 = dot(pp - rho, u);
-        const double r0sq = p0 * p0 + d * d;
-        const double rp = sqrt(r0sq + lp * lp), rm = sqrt(r0sq + lm * lm);
+        const V3<R> pm = P[i], pp = P[(i + 1) % 3];
+        V3<R> l = pp - pm;
+        l = (R(1) / sqrt_t(dot(l, l))) * l;
+        const V3<R> u = cross(l, n);
+        const R lp = dot(pp - rho, l), lm = dot(pm - rho, l);
+        const R p0 = dot(pp - rho, u);
+        const R r0sq = p0 * p0 + d * d;
+        const R rp = sqrt_t(r0sq + lp * lp), rm = sqrt_t(r0sq + lm * lm);
         jv = jv - edge_log(rp, rm, lp, lm) * u;
     }
     *J = jv;

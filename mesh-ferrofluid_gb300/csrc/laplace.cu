@@ -200,10 +200,79 @@ __global__ void pack_tight_kernel(const T* __restrict__ m_r, const T* __restrict
         }
 }
 
+// Surface curls of the three P1 hat functions of face f (defined with the hypersingular
+// operator below).
+template <typename T>
+__device__ __forceinline__ void face_curls(const T* verts, const int32_t* faces, int64_t f, V3<T> c[3]);
+
+// Real P1 packing by test-face rows: block fy accumulates the three rows faces[fy, a] of
+// its panels in shared memory (3 x V values, shared atomics over the ~6 faces that meet at
+// a vertex), then adds them to the packed rows with 3 V global reductions -- 6x fewer than
+// one global atomic per panel entry.  HS: the panels are the hypersingular ones, built on
+// the fly from the P0 single layer m = V0 [F, F] and the faces' surface curls, so the
+// [F, F, 3, 3] hypersingular panels are never stored.
+constexpr int kPackRowThreads = 256;
+constexpr int64_t kPackRowSmemMax = 160 * 1024;
+
+template <typename T, bool HS>
+__global__ void __launch_bounds__(kPackRowThreads)
+    pack_rows_kernel(const T* __restrict__ m, const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                     int64_t nf, int64_t nv, T* __restrict__ packed) {
+    extern __shared__ __align__(16) unsigned char pack_smem[];
+    T* rows = reinterpret_cast<T*>(pack_smem);
+    const int64_t fy = blockIdx.x;
+    for (int64_t j = threadIdx.x; j < 3 * nv; j += blockDim.x) rows[j] = T(0);
+    V3<T> cy[3];
+    if constexpr (HS) face_curls(verts, faces, fy, cy);
+    __syncthreads();
+    for (int64_t fx = threadIdx.x; fx < nf; fx += blockDim.x) {
+        const int32_t vx[3] = {__ldg(faces + 3 * fx), __ldg(faces + 3 * fx + 1), __ldg(faces + 3 * fx + 2)};
+        if constexpr (HS) {
+            V3<T> cx[3];
+            face_curls(verts, faces, fx, cx);
+            const T w = m[fy * nf + fx];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) atomicAdd(rows + a * nv + vx[b], dot(cy[a], cx[b]) * w);
+        } else {
+            const T* src = m + (fy * nf + fx) * 9;
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) atomicAdd(rows + a * nv + vx[b], src[3 * a + b]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        T* dst = packed + (int64_t)__ldg(faces + 3 * fy + a) * nv;
+        for (int64_t j = threadIdx.x; j < nv; j += blockDim.x) atomicAdd(dst + j, rows[a * nv + j]);
+    }
+}
+
+template <typename T, bool HS>
+int launch_pack_rows(const T* m, const T* verts, const int32_t* faces, int64_t nf, int64_t nv, T* packed,
+                     cudaStream_t stream) {
+    const int64_t smem = 3 * nv * (int64_t)sizeof(T);
+    if (smem > kPackRowSmemMax) return set_error(MB_ERR_SIZE, "too many vertices for the row packing");
+    if (nf > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "mesh too large for one launch");
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(pack_rows_kernel<T, HS>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return set_error(MB_ERR_CUDA, cudaGetErrorString(e));
+    }
+    pack_rows_kernel<T, HS><<<(unsigned)nf, kPackRowThreads, (size_t)smem, stream>>>(m, verts, faces, nf, nv,
+                                                                                     packed);
+    return check_launch("pack_rows");
+}
+
 template <typename T>
 int launch_pack_tight(const T* m_r, const T* m_i, const int32_t* faces, int64_t nf, int64_t nv,
                       int order, T* packed, cudaStream_t stream) {
     if (nf <= 0) return MB_OK;
+    if (m_i == nullptr && order == 1 && 3 * nv * (int64_t)sizeof(T) <= kPackRowSmemMax)
+        return launch_pack_rows<T, false>(m_r, nullptr, faces, nf, nv, packed, stream);
     const int threads = 256;
     const int64_t blocks = (nf * nf + threads - 1) / threads;
     if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "mesh too large for one launch");
@@ -266,6 +335,18 @@ template int launch_hypersingular<float>(const float*, const int32_t*, int64_t, 
                                          cudaStream_t);
 template int launch_hypersingular<double>(const double*, const int32_t*, int64_t, const double*, double*,
                                           cudaStream_t);
+
+// Packed P1 hypersingular matrix [V, V] straight from V0 [F, F] (the caller zeroes packed).
+template <typename T>
+int launch_hypersingular_tight(const T* verts, const int32_t* faces, int64_t nf, int64_t nv, const T* v0,
+                               T* packed, cudaStream_t stream) {
+    if (nf <= 0) return MB_OK;
+    return launch_pack_rows<T, true>(v0, verts, faces, nf, nv, packed, stream);
+}
+template int launch_hypersingular_tight<float>(const float*, const int32_t*, int64_t, int64_t, const float*,
+                                               float*, cudaStream_t);
+template int launch_hypersingular_tight<double>(const double*, const int32_t*, int64_t, int64_t, const double*,
+                                                double*, cudaStream_t);
 
 // compute_panel_relation (src/utils/mesh_utils.py:700-725): shared-vertex count per pair.
 __global__ void panel_relation_kernel(const int32_t* __restrict__ faces, int64_t nf,

@@ -100,6 +100,71 @@ def hypersingular_from_v0(verts: torch.Tensor, faces: torch.Tensor, v0: torch.Te
     return out
 
 
+# shared memory the row packing may use (3 x V values): mb_pack_tight_* and
+# mb_laplace_hypersingular_tight_* take the row-accumulating path up to this size
+PACK_ROWS_SMEM_MAX = 160 * 1024
+
+
+def hypersingular_tight(verts: torch.Tensor, faces: torch.Tensor, v0: torch.Tensor) -> torch.Tensor:
+    """Packed P1 hypersingular matrix [V, V] from P0 single-layer panels v0 [F, F(, 1, 1)]
+    (``mb_laplace_hypersingular_tight_*``; equal to packing ``hypersingular_from_v0``).
+    Meshes whose 3 V row values exceed the shared-memory budget take that two-step path."""
+    _lib.check_tensor(verts, "verts", dtype=(torch.float32, torch.float64), ndim=2)
+    faces = faces.to(torch.int32).contiguous()
+    _lib.check_tensor(faces, "faces", device=verts.device, ndim=2)
+    nf, nv = faces.shape[0], verts.shape[0]
+    if 3 * nv * verts.element_size() > PACK_ROWS_SMEM_MAX:
+        from .utils import pack_matrix_tight
+
+        return pack_matrix_tight(int(OrderType.LINEAR), hypersingular_from_v0(verts, faces, v0), verts, faces)
+    check_face_range(faces, nv)
+    v0 = v0.reshape(nf, nf).to(verts.dtype).contiguous()
+    out = torch.zeros((nv, nv), dtype=verts.dtype, device=verts.device)
+    _lib.call(f"mb_laplace_hypersingular_tight_{_lib.sfx(verts.dtype)}", _lib.ptr(verts), nv, _lib.ptr(faces), nf,
+              _lib.ptr(v0), _lib.ptr(out), _lib.stream_of(verts))
+    return out
+
+
+def laplace_sym_tight(verts: torch.Tensor, faces: torch.Tensor, op: int, near: torch.Tensor | None = None,
+                      rows=None, out: torch.Tensor | None = None) -> torch.Tensor:
+    """Packed symmetric-rule operator [V, V] (``mb_laplace_sym_tight_*``) without the
+    [F, F, 3, 3] panels: op 1 single layer, 2 double layer (both P1, equal to packing
+    ``laplace_sym_panels``), 3 hypersingular (equal to ``hypersingular_tight`` of the P0
+    single layer).  Accumulates into ``out`` when given.  Meshes whose 3 V row values
+    exceed the shared-memory budget take the panels-then-pack path."""
+    _lib.check_tensor(verts, "verts", dtype=(torch.float32, torch.float64), ndim=2)
+    faces = faces.to(torch.int32).contiguous()
+    _lib.check_tensor(faces, "faces", device=verts.device, ndim=2)
+    if int(op) not in (1, 2, 3):
+        raise ValueError("op must be 1 (single layer), 2 (double layer) or 3 (hypersingular)")
+    nf, nv = faces.shape[0], verts.shape[0]
+    check_face_range(faces, nv)
+    if near is None:
+        near = laplace_near_pairs(faces)
+    _lib.check_tensor(near, "near", dtype=torch.int32, device=verts.device)
+    if out is None:
+        out = torch.zeros((nv, nv), dtype=verts.dtype, device=verts.device)
+    else:
+        _lib.check_tensor(out, "out", dtype=verts.dtype, device=verts.device, shape=(nv, nv))
+    r0, r1 = (0, nf) if rows is None else rows
+    if 3 * nv * verts.element_size() > PACK_ROWS_SMEM_MAX:
+        from .utils import pack_matrix_tight
+
+        if int(op) == 3:
+            v0 = laplace_sym_panels(verts, faces, 1, int(OrderType.PLANAR), near)
+            part = hypersingular_from_v0(verts, faces, v0)
+        else:
+            part = laplace_sym_panels(verts, faces, int(op), int(OrderType.LINEAR), near)
+        if rows is not None:
+            part[:r0].zero_()
+            part[r1:].zero_()
+        out += pack_matrix_tight(int(OrderType.LINEAR), part, verts, faces)
+        return out
+    _lib.call(f"mb_laplace_sym_tight_{_lib.sfx(verts.dtype)}", _lib.ptr(verts), nv, _lib.ptr(faces), nf, int(op),
+              _lib.ptr(near), near.shape[0], r0, r1, _lib.ptr(out), _lib.stream_of(verts))
+    return out
+
+
 def laplace_near_pairs(faces: torch.Tensor) -> torch.Tensor:
     """Ordered face pairs sharing a vertex (incl. self), [n, 2] int32, sorted by first face."""
     from .utils import shared_vertex_pairs
@@ -211,8 +276,7 @@ class _AbstractLayer:
             near = None
             if panel_relations is not None:
                 near = torch.nonzero(panel_relations > 0).to(torch.int32).contiguous()
-            self._unpacked = self._sym(verts, faces, near)
-            self.initialized = True
+            self.compute_sym(verts, faces, near)
             return
         rands = torch.cat((self.r1, self.r2), dim=-1)
         self._unpacked = double_integration_on_panels_3d(
@@ -220,6 +284,14 @@ class _AbstractLayer:
             face_areas=face_areas, face_normals=face_normals, gauss_weightsx=self.gauss_weights,
             gauss_weightsy=self.gauss_weights, rands_x=rands, rands_y=rands,
             panel_relations=panel_relations, wavenumber=self.wavenumber, layer_type=self.layer_type)
+        self.initialized = True
+
+    def compute_sym(self, verts, faces, near=None):
+        """Symmetric-rule panels from a near-pair list ([n, 2] int32 face pairs sharing a
+        vertex, ``shared_vertex_pairs``; built here when None) instead of the dense relation."""
+        if self.rule != "dunavant7" or BEMType.belong_Helmholtz(self.BEM_type):
+            raise ValueError("compute_sym: Laplace layers with rule dunavant7 only")
+        self._unpacked = self._sym(verts, faces, near)
         self.initialized = True
 
     def _tight(self, verts, faces):

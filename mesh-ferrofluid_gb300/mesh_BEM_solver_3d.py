@@ -21,8 +21,11 @@ Same constructor and public methods as ``src/mesh_BEM/mesh_BEM_solver_3d.py:31-3
   compatible data).  For these cases use ``rule="dunavant7"``.
 
 Extra keyword ``solver`` selects "lu" (reference behaviour, ``torch.linalg.solve``) or
-"gmres" (``mb_gmres_c64``: FP32 matrix-vector products on the complex64 matrix, FP64
-Arnoldi and refinement residual; float32 meshes only, float64 meshes keep LU).  Extra
+"gmres" (``mb_gmres_c64`` for the MoM system, ``mb_gmres_f32`` for the Laplace systems:
+FP32 matrix-vector products, FP64 Arnoldi and refinement residual; float32 meshes only,
+float64 meshes keep LU) or "schur" (Laplace only: Cholesky factors of V on the
+Dirichlet vertices and of the Schur complement D + K V^-1 K^T on the Neumann ones, from
+the symmetric parts of V and D; other BEM types keep LU).  Extra
 keyword ``rule`` selects "reference" (the reference's EFIE + MFIE operator and collapsed
 Gauss rule, parity path) or "dunavant7" (EFIE with the 7-point rule on both triangles and
 closed-form singular integrals for pairs sharing a vertex, in FP64; excitation = the
@@ -35,25 +38,65 @@ from typing import List
 
 import torch
 
-from .layers import DoubleLayer3d, HyperSingularLayer3d, RhsLayer3d, SingleLayer3d
+from .layers import (
+    DoubleLayer3d,
+    HyperSingularLayer3d,
+    RhsLayer3d,
+    SingleLayer3d,
+    laplace_sym_tight,
+)
 from .mesh_MOM_3d import (
     assemble_rhs_rwg,
     assemble_rhs_rwg_sym,
     assemble_Z_rwg,
     assemble_Z_rwg_sym,
     gmres,
+    gmres_real,
     interpolate_vert_js,
     reference_plane_wave,
 )
 from .utils import (
     BEMType,
     BoundaryType,
+    OrderType,
     compute_face_areas,
     compute_face_normals,
     compute_panel_relation,
     compute_vert_areas,
     get_gaussion_integration_points_and_weights,
+    shared_vertex_pairs,
 )
+
+
+def _sym_part(A: torch.Tensor) -> torch.Tensor:
+    return 0.5 * (A + A.transpose(0, 1))
+
+
+def _cholesky(A: torch.Tensor) -> torch.Tensor:
+    L, info = torch.linalg.cholesky_ex(_sym_part(A))
+    if int(info) != 0:
+        raise RuntimeError(f"the symmetric part is not positive definite (cholesky info {int(info)})")
+    return L
+
+
+def _spd_solve(A: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    """A x = b through the Cholesky factor of A's symmetric part (V, or D + a a^T)."""
+    return torch.cholesky_solve(b.reshape(-1, 1), _cholesky(A)).reshape(-1)
+
+
+def _schur_solve(Vdd, B, Dnn, r1, r2):
+    """The mixed block system [[Vdd, -B], [B^T, Dnn]] [x1; x2] = [r1; r2] by Cholesky factors:
+    Vdd = L L^T, W = L^-1 B, S = Dnn + W^T W (symmetric positive definite),
+    x2 = S^-1 (r2 - W^T L^-1 r1), x1 = L^-T (L^-1 r1 + W x2).  Vdd and Dnn enter through
+    their symmetric parts (the Galerkin operators are symmetric; the assembled ones differ
+    at the quadrature error)."""
+    L = _cholesky(Vdd)
+    W = torch.linalg.solve_triangular(L, B, upper=False)
+    y = torch.linalg.solve_triangular(L, r1.reshape(-1, 1), upper=False)
+    Ls = _cholesky(Dnn + W.transpose(0, 1) @ W)
+    x2 = torch.cholesky_solve(r2.reshape(-1, 1) - W.transpose(0, 1) @ y, Ls)
+    x1 = torch.linalg.solve_triangular(L.transpose(0, 1), y + W @ x2, upper=True)
+    return torch.cat((x1, x2)).reshape(-1)
 
 
 class MeshBEMSolver3d:
@@ -70,7 +113,7 @@ class MeshBEMSolver3d:
         self.logger = logger
         self.device = torch.device(device)
         self.dtype = dtype
-        if solver not in ("lu", "gmres"):
+        if solver not in ("lu", "gmres", "schur"):
             raise ValueError(f"unknown solver {solver!r}")
         self.solver = solver
         self.gmres_restart = gmres_restart
@@ -153,11 +196,23 @@ class MeshBEMSolver3d:
         verts = verts.contiguous()
         areas = compute_face_areas(vertices=verts, faces=faces, keepdim=True).contiguous()
         normals = compute_face_normals(vertices=verts, faces=faces).contiguous()
-        panel_relations = compute_panel_relation(faces)
+        sym = self.rule == "dunavant7" and not BEMType.belong_Helmholtz(self.BEM_type)
+        # the symmetric rule needs only the face pairs sharing a vertex (O(F)), not the
+        # dense [F, F] relation of the reference rule
+        near = shared_vertex_pairs(faces) if sym else None
+        panel_relations = None if sym else compute_panel_relation(faces)
         neu_list, dir_list = [], []
         mats = {}
+        layers = {"V": self.single_layer, "K": self.double_layer, "D": self.hypersingular_layer}
+        schur = self.solver == "schur" and self.BEM_type == int(BEMType.LAPLACE)
 
         def tight(name):
+            if name not in mats and sym and self.order_type == int(OrderType.LINEAR):
+                # packed straight from the face pairs; the [F, F, 3, 3] panels are not kept
+                mats[name] = laplace_sym_tight(verts, faces, {"V": 1, "K": 2, "D": 3}[name], near)
+            if name not in mats and sym:
+                layers[name].compute_sym(verts, faces, near)
+                mats[name] = layers[name]._tight(verts, faces)
             if name not in mats:
                 if name == "V":
                     self.single_layer.compute_Vmat(verts, faces, areas, normals, panel_relations)
@@ -199,12 +254,28 @@ class MeshBEMSolver3d:
                     A = D + a @ a.T
             else:
                 ks = K.transpose(0, 1)  # Galerkin <phi_i, K phi_j>
-                A = torch.cat((torch.cat((V[is_d][:, is_d], -ks[is_d][:, is_n]), 1),
-                               torch.cat((ks.transpose(0, 1)[is_n][:, is_d], D[is_n][:, is_n]), 1)), 0)
                 rhs = torch.cat((rhs[is_d], rhs[is_n]))
-            if Amat_scaler is not None:
+                A = None if schur else torch.cat(
+                    (torch.cat((V[is_d][:, is_d], -ks[is_d][:, is_n]), 1),
+                     torch.cat((ks.transpose(0, 1)[is_n][:, is_d], D[is_n][:, is_n]), 1)), 0)
+            if Amat_scaler is not None and A is not None:
                 A = Amat_scaler * A
-            sol = torch.linalg.solve(A, rhs.to(A.dtype)).to(neu.dtype)
+            if schur:
+                if n_n and n_d:
+                    sol = _schur_solve(V[is_d][:, is_d], ks[is_d][:, is_n], D[is_n][:, is_n],
+                                       rhs[:n_d].to(K.dtype), rhs[n_d:].to(K.dtype))
+                    if Amat_scaler is not None:  # (s A) x = rhs
+                        sol = sol / Amat_scaler
+                else:
+                    sol = _spd_solve(A, rhs.to(A.dtype))
+                sol = sol.to(neu.dtype)
+            elif self.solver == "gmres" and A.dtype == torch.float32:
+                x, info = gmres_real(A.contiguous(), rhs, restart=self.gmres_restart, tol=self.gmres_tol,
+                                     max_iters=self.gmres_max_iters)
+                self.last_solve_info = info
+                sol = x.to(neu.dtype)
+            else:
+                sol = torch.linalg.solve(A, rhs.to(A.dtype)).to(neu.dtype)
             if n_n == 0:
                 neu = sol.reshape(n_verts, 1)
             elif n_d == 0:

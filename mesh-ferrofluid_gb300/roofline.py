@@ -27,6 +27,10 @@ EFIE_MUFU_PER_EVAL = 3
 LAPLACE_SL_FLOP_PER_EVAL = 15
 LAPLACE_DL_FLOP_PER_EVAL = 22
 LAPLACE_MUFU_PER_EVAL = 1
+# symmetric-rule P1 single layer (7 x 7 points per separated face pair): per evaluation
+# 3 (x - y) + 5 (|d|^2) + 1 (w / R) + 6 (three hat-weighted sums) FLOP and one rsqrt; per
+# outer point 15 (the point) + 1 (weight) + 21 (the 3 x 3 block) FLOP, ~5 per evaluation
+LAPLACE_SYM_P1_FLOP_PER_EVAL = 20
 RADIATE_FLOP_PER_PAIR = 61
 RADIATE_MUFU_PER_PAIR = 3
 # nominal FP64 rate of a GB300 (far below its FP32 SIMT rate); used only as the denominator

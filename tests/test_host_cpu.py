@@ -1,5 +1,6 @@
 """Host-side logic on the CPU: tables, mesh helpers, rule flattening, the C ABI surface."""
 import ctypes
+import importlib
 import os
 import re
 
@@ -146,3 +147,23 @@ def test_shared_vertex_pairs_equal_dense_relation(pkg):
                 dense |= f[:, a][:, None] == f[:, b][None, :]
         assert np.array_equal(got, np.argwhere(dense))
     assert pkg.utils.shared_vertex_pairs(torch.zeros((0, 3), dtype=torch.int32)).shape == (0, 2)
+
+
+def test_schur_solve_matches_dense_block_solve(pkg):
+    """The mixed block system [[V, -B], [B^T, D]] solved by Cholesky factors (solver="schur")."""
+    m = importlib.import_module("mesh-ferrofluid_gb300.mesh_BEM_solver_3d")
+    g = torch.Generator().manual_seed(0)
+    nd, nn = 30, 20
+    X = torch.randn(nd, nd, generator=g, dtype=torch.float64)
+    Y = torch.randn(nn, nn, generator=g, dtype=torch.float64)
+    V = X @ X.T + nd * torch.eye(nd, dtype=torch.float64)
+    D = Y @ Y.T + torch.eye(nn, dtype=torch.float64)
+    B = torch.randn(nd, nn, generator=g, dtype=torch.float64)
+    r1 = torch.randn(nd, generator=g, dtype=torch.float64)
+    r2 = torch.randn(nn, generator=g, dtype=torch.float64)
+    A = torch.cat((torch.cat((V, -B), 1), torch.cat((B.T, D), 1)), 0)
+    x = torch.linalg.solve(A, torch.cat((r1, r2)))
+    assert (m._schur_solve(V, B, D, r1, r2) - x).abs().max().item() < 1e-12
+    assert (m._spd_solve(V, r1) - torch.linalg.solve(V, r1)).abs().max().item() < 1e-12
+    with pytest.raises(RuntimeError):
+        m._spd_solve(-V, r1)

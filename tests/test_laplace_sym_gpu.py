@@ -119,6 +119,102 @@ def test_sphere_dirichlet_neumann_mixed_solves(pkg, cuda, dt):
     assert torch.equal(dirv[0][~lower], z[~lower]) and torch.equal(neu[0][lower], z[lower])
 
 
+@pytest.mark.parametrize("dt,tol", [(torch.float64, 1e-12), (torch.float32, 1e-5)])
+def test_row_packing_and_packed_hypersingular(pkg, cuda, dt, tol):
+    """mb_pack_tight_* (P1, row-accumulating path) against np.add.at, and the packed
+    hypersingular matrix straight from V0 against packing the stored panels."""
+    v_np, f_np = pkg.meshes.icosphere(3, 1.0)
+    nf, nv = f_np.shape[0], v_np.shape[0]
+    m = np.random.default_rng(3).normal(size=(nf, nf, 3, 3))
+    ref = np.zeros((nv, nv))
+    np.add.at(ref, (f_np[:, None, :, None], f_np[None, :, None, :]), m)
+    vt = torch.tensor(v_np, dtype=dt, device=cuda)
+    ft = torch.tensor(f_np, dtype=torch.int32, device=cuda)
+    got = pkg.utils.pack_matrix_tight(1, torch.tensor(m, dtype=dt, device=cuda), vt, ft)
+    assert rel_err(got.cpu().numpy(), ref) < tol
+    v0 = pkg.layers.laplace_sym_panels(vt, ft, 1, 0)
+    d_ref = pkg.utils.pack_matrix_tight(1, pkg.layers.hypersingular_from_v0(vt, ft, v0), vt, ft)
+    d_got = pkg.layers.hypersingular_tight(vt, ft, v0)
+    assert rel_err(d_got.cpu().numpy(), d_ref.cpu().numpy()) < tol
+    # rows sum to zero (D annihilates constants)
+    assert d_got.double().sum(1).abs().max().item() < 1e3 * tol * d_got.abs().max().item()
+
+
+@pytest.mark.parametrize("name", ["ico1", "ell1", "ico3"])
+@pytest.mark.parametrize("dt,tol", [(torch.float64, 1e-12), (torch.float32, 1e-5)])
+def test_packed_operators_match_packed_panels(pkg, cuda, golden, name, dt, tol):
+    """mb_laplace_sym_tight_* (no panels stored) against packing the stored panels."""
+    v, f, vt, ft = _mesh(pkg, name, golden, cuda, dt)
+    L, U = pkg.layers, pkg.utils
+    near = L.laplace_near_pairs(ft)
+    for op in (1, 2):
+        ref = U.pack_matrix_tight(1, L.laplace_sym_panels(vt, ft, op, 1, near), vt, ft)
+        got = L.laplace_sym_tight(vt, ft, op, near)
+        assert rel_err(got.cpu().numpy(), ref.cpu().numpy()) < tol, op
+    ref = L.hypersingular_tight(vt, ft, L.laplace_sym_panels(vt, ft, 1, 0, near))
+    got = L.laplace_sym_tight(vt, ft, 3)
+    assert rel_err(got.cpu().numpy(), ref.cpu().numpy()) < tol
+    # test-row windows add up to the whole operator
+    k = ft.shape[0] // 3
+    part = L.laplace_sym_tight(vt, ft, 2, near, rows=(0, k))
+    L.laplace_sym_tight(vt, ft, 2, near, rows=(k, ft.shape[0]), out=part)
+    full = L.laplace_sym_tight(vt, ft, 2, near)
+    assert rel_err(part.cpu().numpy(), full.cpu().numpy()) < tol
+
+
+@pytest.mark.parametrize("dt", [torch.float64, torch.float32])
+def test_schur_solver_matches_lu(pkg, cuda, dt):
+    """solver="schur" (Cholesky factors of V and of the Schur complement, symmetric parts)
+    against LU of the block system: Dirichlet, Neumann and mixed data on the L3 sphere."""
+    v_np, f_np = pkg.meshes.icosphere(3, 1.0)
+    v = torch.tensor(v_np, dtype=dt, device=cuda)
+    f = torch.tensor(f_np, dtype=torch.int32, device=cuda)
+    z = v[:, 2:3].clone()
+    nv = v.shape[0]
+    D_, N_ = int(pkg.BoundaryType.DIRICHLET), int(pkg.BoundaryType.NEUMANN)
+    lu = _solver(pkg, cuda, dt)
+    ch = pkg.MeshBEMSolver3d(gaussQR=3, order_type=1, BEM_type=int(pkg.BEMType.LAPLACE), wavenumber=1.0,
+                             logger=None, dtype=dt, device=cuda, rule="dunavant7", solver="schur")
+    zero = torch.zeros_like(z)
+    cases = [(torch.full((1, nv, 1), D_, dtype=torch.uint8, device=cuda), z[None], zero[None]),
+             (torch.full((1, nv, 1), N_, dtype=torch.uint8, device=cuda), zero[None], z[None]),
+             (torch.where(z > 0, D_, N_).to(torch.uint8)[None], torch.where(z > 0, z, 0.0)[None],
+              torch.where(z > 0, 0.0, z)[None])]
+    for flags, g, h in cases:
+        a = lu.solve(v, f, g, h, flags)
+        b = ch.solve(v, f, g, h, flags)
+        for x, y in zip(a, b):
+            # the two differ by the asymmetry of the assembled operators (quadrature error)
+            assert (torch.linalg.norm(x - y) / torch.linalg.norm(x)).item() < 2e-3
+    # Amat_scaler scales the matrix only: the solution scales by its inverse, as with LU
+    flags, g, h = cases[2]
+    a = lu.solve(v, f, g, h, flags, Amat_scaler=4.0)
+    b = ch.solve(v, f, g, h, flags, Amat_scaler=4.0)
+    for x, y in zip(a, b):
+        assert (torch.linalg.norm(x - y) / torch.linalg.norm(x)).item() < 2e-3
+
+
+def test_mixed_solve_gmres_matches_lu(pkg, cuda):
+    """solver="gmres" (mb_gmres_f32 on the block system) gives the LU solution."""
+    v_np, f_np = pkg.meshes.icosphere(3, 1.0)
+    v = torch.tensor(v_np, dtype=torch.float32, device=cuda)
+    f = torch.tensor(f_np, dtype=torch.int32, device=cuda)
+    z = v[:, 2:3].clone()
+    D_, N_ = int(pkg.BoundaryType.DIRICHLET), int(pkg.BoundaryType.NEUMANN)
+    flags = torch.where(z > 0, D_, N_).to(torch.uint8)[None]
+    g = torch.where(z > 0, z, 0.0)[None]
+    h = torch.where(z > 0, 0.0, z)[None]
+    lu = _solver(pkg, cuda, torch.float32).solve(v, f, g, h, flags)
+    it = pkg.MeshBEMSolver3d(gaussQR=3, order_type=1, BEM_type=int(pkg.BEMType.LAPLACE), wavenumber=1.0,
+                             logger=None, dtype=torch.float32, device=cuda, rule="dunavant7", solver="gmres",
+                             gmres_tol=1e-7)
+    gm = it.solve(v, f, g, h, flags)
+    info = it.last_solve_info[0]
+    assert info["converged"] and info["rel_residual"] < 1e-7
+    for a, b in zip(lu, gm):
+        assert (torch.linalg.norm(a - b) / torch.linalg.norm(a)).item() < 1e-4
+
+
 @pytest.mark.parametrize("dt,tol", [(torch.float64, 0.012), (torch.float32, 0.012)])
 def test_collocation_sphere_density(pkg, cuda, dt, tol):
     """V sigma = 1 on the sphere of radius a has sigma = 1/a (GMRES on the collocation matrix)."""
