@@ -97,9 +97,12 @@ __device__ __forceinline__ void sym_far_pair(const T (*s_rule)[4], const T (*s_y
 // instructions.  X0..X2 hold both faces' shifted corners per coordinate; acc as in
 // sym_far_pair, packed.
 template <int LAYER, int NPHI>
-__device__ __forceinline__ void sym_far_pair2(const float (*s_rule)[4], const float (*s_y)[4], const float3& ny,
+__device__ __forceinline__ void sym_far_pair2(const float4 (*s_r4)[2], const float4 (*s_y4)[2], const float3& ny,
                                               const float2 X0[3], const float2 X1[3], const float2 X2[3],
                                               float2 acc[9]) {
+    // s_r4[j] = {(r0, r0, r1, r1), (r2, r2, w, w)}, s_y4[j] = {(y.x, y.x, y.y, y.y),
+    // (y.z, y.z, wA, wA)}: every value already duplicated, so one 16-byte shared load yields two
+    // packed operands and no register moves are needed to broadcast them
     float2 e1[3], e2[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -113,24 +116,29 @@ __device__ __forceinline__ void sym_far_pair2(const float (*s_rule)[4], const fl
     const float2 ax = make_float2(0.5f * sqrtf(n2.x), 0.5f * sqrtf(n2.y));
 #pragma unroll 1
     for (int i = 0; i < 7; ++i) {
-        const float2 r0 = bc(s_rule[i][0]), r1 = bc(s_rule[i][1]), r2 = bc(s_rule[i][2]);
+        // re-read the tables every outer point instead of holding all 28 of them in registers
+        asm volatile("" ::: "memory");
+        const float4 ra = s_r4[i][0], rb = s_r4[i][1];
+        const float2 r0 = make_float2(ra.x, ra.y), r1 = make_float2(ra.z, ra.w), r2 = make_float2(rb.x, rb.y);
         float2 x[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) x[c] = fma2(r0, X0[c], fma2(r1, X1[c], mul2(r2, X2[c])));
         float2 s0 = bc(0.f), s1 = bc(0.f), s2 = bc(0.f);
 #pragma unroll
         for (int j = 0; j < 7; ++j) {
-            const float2 dx = sub2(x[0], bc(s_y[j][0]));
-            const float2 dy = sub2(x[1], bc(s_y[j][1]));
-            const float2 dz = sub2(x[2], bc(s_y[j][2]));
+            const float4 ya = s_y4[j][0], yb = s_y4[j][1];
+            const float2 dx = sub2(x[0], make_float2(ya.x, ya.y));
+            const float2 dy = sub2(x[1], make_float2(ya.z, ya.w));
+            const float2 dz = sub2(x[2], make_float2(yb.x, yb.y));
             const float2 d2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
             const float2 ri = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
-            float2 g = mul2(ri, bc(s_y[j][3]));
+            float2 g = mul2(ri, make_float2(yb.z, yb.w));
             if constexpr (LAYER == 2) g = mul2(g, mul2(ri, ri));
             if constexpr (NPHI == 3) {
-                s0 = fma2(g, bc(s_rule[j][0]), s0);
-                s1 = fma2(g, bc(s_rule[j][1]), s1);
-                s2 = fma2(g, bc(s_rule[j][2]), s2);
+                const float4 qa = s_r4[j][0], qb = s_r4[j][1];
+                s0 = fma2(g, make_float2(qa.x, qa.y), s0);
+                s1 = fma2(g, make_float2(qa.z, qa.w), s1);
+                s2 = fma2(g, make_float2(qb.x, qb.y), s2);
             } else {
                 s0 = add2(s0, g);
             }
@@ -141,12 +149,13 @@ __device__ __forceinline__ void sym_far_pair2(const float (*s_rule)[4], const fl
             s1 = mul2(s1, dn);
             s2 = mul2(s2, dn);
         }
-        const float2 wx = mul2(bc(s_rule[i][3]), ax);
+        const float2 wx = mul2(make_float2(rb.z, rb.w), ax);
         if constexpr (NPHI == 3) {
             const float2 sa[3] = {s0, s1, s2};
+            const float2 rr[3] = {r0, r1, r2};
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
-                const float2 wb = mul2(wx, bc(s_rule[i][b]));
+                const float2 wb = mul2(wx, rr[b]);
 #pragma unroll
                 for (int a = 0; a < 3; ++a) acc[3 * a + b] = fma2(sa[a], wb, acc[3 * a + b]);
             }
@@ -246,6 +255,8 @@ __global__ void __launch_bounds__(kSymThreads, sizeof(T) == 4 ? (OP == 3 ? 6 : 4
     __shared__ T s_rule[7][4];
     __shared__ T s_y[7][4];
     __shared__ T s_n[3];
+    __shared__ float4 s_r4[7][2];  // the same tables with every value duplicated (float path)
+    __shared__ float4 s_y4[7][2];
     extern __shared__ __align__(16) unsigned char tight_smem[];
     T* rows = reinterpret_cast<T*>(tight_smem);
     const int64_t fy = row_begin + blockIdx.x;
@@ -257,17 +268,34 @@ __global__ void __launch_bounds__(kSymThreads, sizeof(T) == 4 ? (OP == 3 ? 6 : 4
     V3<T> cy[3];
     if constexpr (OP == 3) tri_curls(v3<T>(0, 0, 0), Y1, Y2, cy);
     __syncthreads();
+    if (threadIdx.x < 7) {
+        const int j = threadIdx.x;
+        const float r0 = (float)s_rule[j][0], r1 = (float)s_rule[j][1], r2 = (float)s_rule[j][2];
+        const float rw = (float)s_rule[j][3];
+        s_r4[j][0] = make_float4(r0, r0, r1, r1);
+        s_r4[j][1] = make_float4(r2, r2, rw, rw);
+        const float y0 = (float)s_y[j][0], y1 = (float)s_y[j][1], y2 = (float)s_y[j][2], yw = (float)s_y[j][3];
+        s_y4[j][0] = make_float4(y0, y0, y1, y1);
+        s_y4[j][1] = make_float4(y2, y2, yw, yw);
+    }
+    __syncthreads();
     const V3<T> ny = v3<T>(s_n[0], s_n[1], s_n[2]);
+    // each thread sweeps its own strip of consecutive source faces: neighbouring faces share
+    // vertices, and lanes of a warp working on neighbours would collide in the shared-memory
+    // accumulators (same-address atomics serialise)
+    const int64_t strip = (nf + blockDim.x - 1) / blockDim.x;
+    const int64_t strip0 = (int64_t)threadIdx.x * strip;
+    const int64_t strip1 = strip0 + strip < nf ? strip0 + strip : nf;
     if constexpr (sizeof(T) == 4 && OP != 3) {
-        // two source faces per thread and iteration (fxa, fxa + blockDim), packed arithmetic
+        // two source faces per thread and iteration (fxa, fxa + 1), packed arithmetic
         // (the P0 sums of OP 3 are light enough that occupancy matters more)
         const float3 nyf = make_float3(ny.x, ny.y, ny.z);
 #pragma unroll 1
-        for (int64_t base = 0; base < nf; base += 2 * (int64_t)blockDim.x) {
-            const int64_t fxa = base + threadIdx.x;
-            if (fxa >= nf) break;
-            const int64_t fxb_raw = fxa + blockDim.x;
-            const bool has_b = fxb_raw < nf;
+        for (int64_t k = 0; k < strip; k += 2) {
+            const int64_t fxa = strip0 + k;
+            if (fxa >= strip1) break;
+            const int64_t fxb_raw = fxa + 1;
+            const bool has_b = fxb_raw < strip1;
             const int64_t fxb = has_b ? fxb_raw : fxa;
             const bool use_a = !share_vertex(faces, fy, fxa);
             const bool use_b = has_b && !share_vertex(faces, fy, fxb);
@@ -286,7 +314,7 @@ __global__ void __launch_bounds__(kSymThreads, sizeof(T) == 4 ? (OP == 3 ? 6 : 4
             float2 acc[9];
 #pragma unroll
             for (int c = 0; c < 9; ++c) acc[c] = bc(0.f);
-            sym_far_pair2<LAYER, NPHI>(s_rule, s_y, nyf, X[0], X[1], X[2], acc);
+            sym_far_pair2<LAYER, NPHI>(s_r4, s_y4, nyf, X[0], X[1], X[2], acc);
             {
 #pragma unroll
                 for (int a = 0; a < 3; ++a)
@@ -299,7 +327,7 @@ __global__ void __launch_bounds__(kSymThreads, sizeof(T) == 4 ? (OP == 3 ? 6 : 4
         }
     } else {
 #pragma unroll 1
-    for (int64_t fx = threadIdx.x; fx < nf; fx += blockDim.x) {
+    for (int64_t fx = strip0; fx < strip1; ++fx) {
         if (share_vertex(faces, fy, fx)) continue;
         const int32_t vx[3] = {__ldg(faces + 3 * fx), __ldg(faces + 3 * fx + 1), __ldg(faces + 3 * fx + 2)};
         const V3<T> X0 = load3(verts, vx[0]) - o;
