@@ -194,9 +194,11 @@ class MeshBEMSolver3d:
         batch = vert_bc_flags.shape[0]
         faces = faces.to(torch.int32).contiguous()
         verts = verts.contiguous()
-        areas = compute_face_areas(vertices=verts, faces=faces, keepdim=True).contiguous()
-        normals = compute_face_normals(vertices=verts, faces=faces).contiguous()
         sym = self.rule == "dunavant7" and not BEMType.belong_Helmholtz(self.BEM_type)
+        areas = normals = None
+        if not sym:  # the reference rule's layers take them
+            areas = compute_face_areas(vertices=verts, faces=faces, keepdim=True).contiguous()
+            normals = compute_face_normals(vertices=verts, faces=faces).contiguous()
         # the symmetric rule needs only the face pairs sharing a vertex (O(F)), not the
         # dense [F, F] relation of the reference rule
         near = shared_vertex_pairs(faces) if sym else None
@@ -262,7 +264,11 @@ class MeshBEMSolver3d:
                 A = Amat_scaler * A
             if schur:
                 if n_n and n_d:
-                    sol = _schur_solve(V[is_d][:, is_d], ks[is_d][:, is_n], D[is_n][:, is_n],
+                    # one index list per mask (each boolean index would synchronise again)
+                    i_d, i_n = torch.nonzero(is_d).reshape(-1), torch.nonzero(is_n).reshape(-1)
+                    sol = _schur_solve(V.index_select(0, i_d).index_select(1, i_d),
+                                       ks.index_select(0, i_d).index_select(1, i_n),
+                                       D.index_select(0, i_n).index_select(1, i_n),
                                        rhs[:n_d].to(K.dtype), rhs[n_d:].to(K.dtype))
                     if Amat_scaler is not None:  # (s A) x = rhs
                         sol = sol / Amat_scaler
