@@ -671,7 +671,7 @@ def main_topology(args, rank, world, local_rank):
 
     def topo(v, f):
         edges, fei, adj = U.get_edge_unique(v, f)
-        pairs = U.shared_vertex_pairs(f)
+        pairs = U.shared_vertex_pairs(f, v.shape[0])
         er = torch.empty(2 * edges.shape[0] + 1, dtype=torch.int32, device=f.device)
         pkg._lib.call("mb_mom_edge_rows", pkg._lib.ptr(fei), f.shape[0], edges.shape[0], pkg._lib.ptr(er),
                       pkg._lib.stream_of(f))
@@ -813,7 +813,7 @@ def main_lapmixed(args, rank, world, local_rank):
         torch.cuda.synchronize(dev)
         return a.elapsed_time(b) / reps, r
 
-    t_near, near = timed(lambda: U.shared_vertex_pairs(faces))
+    t_near, near = timed(lambda: U.shared_vertex_pairs(faces, nv))
     t_v, Vt = timed(lambda: L.laplace_sym_tight(verts, faces, 1, near))
     t_k, Kt = timed(lambda: L.laplace_sym_tight(verts, faces, 2, near))
     t_d, Dt = timed(lambda: L.laplace_sym_tight(verts, faces, 3, near))

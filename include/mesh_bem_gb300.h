@@ -102,6 +102,19 @@ int mb_mom_zmat_rwg_c128(const double* verts, int64_t n_verts, const int32_t* fa
  * exists).  edge_rows [2 n_edges + 1] int32: for Z row m (edge m) the face-edge rows 3f + e
  * of its faces (smaller first; -1 for a missing second face); edge_rows[2 n_edges] = 1 when
  * some edge has more than two faces (the edge-row operators below then do not apply). */
+/* Ordered face pairs sharing at least one vertex (each face with itself), sorted by first
+ * face then second: the nonzeros of compute_panel_relation (src/utils/mesh_utils.py:700-725)
+ * in row-major order -- the near-pair list of the symmetric-rule operators -- in O(F) memory.
+ * Two calls on one workspace of mb_shared_vertex_pairs_workspace_bytes bytes: _count builds
+ * the vertex-face incidences and per-face offsets and returns the list length in *n_pairs
+ * (host memory; the stream is synchronised), _fill writes pairs [n_pairs, 2] int32.  Vertex
+ * ids outside [0, n_verts) fail with MB_ERR_ARG. */
+int64_t mb_shared_vertex_pairs_workspace_bytes(int64_t n_faces, int64_t n_verts);
+int mb_shared_vertex_pairs_count(const int32_t* faces, int64_t n_faces, int64_t n_verts, void* workspace,
+                                 int64_t workspace_bytes, int64_t* n_pairs, void* stream);
+int mb_shared_vertex_pairs_fill(const int32_t* faces, int64_t n_faces, int64_t n_verts, void* workspace,
+                                int32_t* pairs, void* stream);
+
 int mb_mom_edge_rows(const int32_t* face_edge_indices, int64_t n_faces, int64_t n_edges, int32_t* edge_rows,
                      void* stream);
 /* The same matrix as mb_mom_zmat_rwg_c64, built Z row by Z row: rows [m_begin, m_end) of z

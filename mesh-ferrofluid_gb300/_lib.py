@@ -34,6 +34,9 @@ _SIGS = {
     "mb_mom_zmat_rwg_c128": [_P, _I64, _P, _I64, _P, _P, _P, _I64, _P, _P, _I, _P, _P, _I, _D,
                              _I64, _I64, _P, _P],
     "mb_mom_edge_rows": [_P, _I64, _I64, _P, _P],
+    "mb_shared_vertex_pairs_workspace_bytes": [_I64, _I64],
+    "mb_shared_vertex_pairs_count": [_P, _I64, _I64, _P, _I64, _P, _P],
+    "mb_shared_vertex_pairs_fill": [_P, _I64, _I64, _P, _P, _P],
     "mb_mom_sym_zmat_rwg_to_host_c64": [_P, _I64, _P, _I64, _P, _I64, _D, _P, _I64, _P, _P, _I, _P],
     "mb_gmres_blockdiag_column_steps": [_P, _I64, _I64, _I, _P, _P],
     "mb_gmres_multi_column_steps": [_P, _I64, _I64, _I, _P, _P],
@@ -111,7 +114,8 @@ _SIGS = {
 _RESTYPES = {"mb_gmres_workspace_bytes": ctypes.c_size_t, "mb_ray_bvh_bytes": ctypes.c_size_t,
              "mb_gmres_real_workspace_bytes": ctypes.c_size_t, "mb_cgemm_workspace_bytes": ctypes.c_size_t,
              "mb_gmres_multi_workspace_bytes": ctypes.c_size_t,
-             "mb_gmres_blockdiag_workspace_bytes": ctypes.c_size_t}
+             "mb_gmres_blockdiag_workspace_bytes": ctypes.c_size_t,
+             "mb_shared_vertex_pairs_workspace_bytes": ctypes.c_int64}
 
 
 class GmresInfo(ctypes.Structure):

@@ -57,7 +57,7 @@ class MeshBatch:
             f = torch.as_tensor(np.asarray(f)).to(device=dev, dtype=torch.int32)
             edges, fe, _ = get_edge_unique(v, f)
             ne, nf = int(edges.shape[0]), int(f.shape[0])
-            near.append(shared_vertex_pairs(f) + f_off)
+            near.append(shared_vertex_pairs(f, v.shape[0]) + f_off)
             verts.append(v)
             faces.append(f + v_off)
             fei.append(fe.reshape(-1, 3).to(torch.int32))

@@ -54,6 +54,10 @@ template <typename T>
 int launch_pack_tight(const T*, const T*, const int32_t*, int64_t, int64_t, int, T*, cudaStream_t);
 template <typename T>
 int launch_hypersingular(const T*, const int32_t*, int64_t, const T*, T*, cudaStream_t);
+int64_t near_pairs_workspace_bytes(int64_t nf, int64_t nv);
+int near_pairs_count(const int32_t* faces, int64_t nf, int64_t nv, void* ws, int64_t ws_bytes, int64_t* n_pairs,
+                     cudaStream_t s);
+int near_pairs_fill(const int32_t* faces, int64_t nf, int64_t nv, void* ws, int32_t* pairs, cudaStream_t s);
 template <typename T>
 int launch_hypersingular_tight(const T*, const int32_t*, int64_t, int64_t, const T*, T*, cudaStream_t);
 template <typename T>
@@ -414,6 +418,29 @@ MB_PACK(f64, double)
 MB_HYP(f32, float)
 MB_HYP(f64, double)
 #undef MB_HYP
+
+int64_t mb_shared_vertex_pairs_workspace_bytes(int64_t n_faces, int64_t n_verts) {
+    if (n_faces < 0 || n_verts < 0) return 0;
+    return near_pairs_workspace_bytes(n_faces, n_verts);
+}
+
+int mb_shared_vertex_pairs_count(const int32_t* faces, int64_t n_faces, int64_t n_verts, void* workspace,
+                                 int64_t workspace_bytes, int64_t* n_pairs, void* stream) {
+    MB_REQUIRE(n_faces >= 0 && n_verts >= 0, "bad sizes");
+    MB_REQUIRE(n_pairs, "null pointer argument");
+    *n_pairs = 0;
+    if (n_faces == 0) return MB_OK;
+    MB_REQUIRE(faces && workspace, "null pointer argument");
+    return near_pairs_count(faces, n_faces, n_verts, workspace, workspace_bytes, n_pairs, as_stream(stream));
+}
+
+int mb_shared_vertex_pairs_fill(const int32_t* faces, int64_t n_faces, int64_t n_verts, void* workspace,
+                                int32_t* pairs, void* stream) {
+    MB_REQUIRE(n_faces >= 0 && n_verts >= 0, "bad sizes");
+    if (n_faces == 0) return MB_OK;
+    MB_REQUIRE(faces && workspace && pairs, "null pointer argument");
+    return near_pairs_fill(faces, n_faces, n_verts, workspace, pairs, as_stream(stream));
+}
 
 #define MB_HYPT(SFX, T)                                                                               \
     int mb_laplace_hypersingular_tight_##SFX(const T* verts, int64_t n_verts, const int32_t* faces,     \

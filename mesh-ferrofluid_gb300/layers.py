@@ -140,7 +140,7 @@ def laplace_sym_tight(verts: torch.Tensor, faces: torch.Tensor, op: int, near: t
     nf, nv = faces.shape[0], verts.shape[0]
     check_face_range(faces, nv)
     if near is None:
-        near = laplace_near_pairs(faces)
+        near = laplace_near_pairs(faces, verts.shape[0])
     _lib.check_tensor(near, "near", dtype=torch.int32, device=verts.device)
     if out is None:
         out = torch.zeros((nv, nv), dtype=verts.dtype, device=verts.device)
@@ -165,11 +165,11 @@ def laplace_sym_tight(verts: torch.Tensor, faces: torch.Tensor, op: int, near: t
     return out
 
 
-def laplace_near_pairs(faces: torch.Tensor) -> torch.Tensor:
+def laplace_near_pairs(faces: torch.Tensor, n_verts: int | None = None) -> torch.Tensor:
     """Ordered face pairs sharing a vertex (incl. self), [n, 2] int32, sorted by first face."""
     from .utils import shared_vertex_pairs
 
-    return shared_vertex_pairs(faces)
+    return shared_vertex_pairs(faces, n_verts)
 
 
 def laplace_sym_panels(verts: torch.Tensor, faces: torch.Tensor, layer: int, order: int,
@@ -185,7 +185,7 @@ def laplace_sym_panels(verts: torch.Tensor, faces: torch.Tensor, layer: int, ord
     nf = faces.shape[0]
     check_face_range(faces, verts.shape[0])
     if near is None:
-        near = laplace_near_pairs(faces)
+        near = laplace_near_pairs(faces, verts.shape[0])
     _lib.check_tensor(near, "near", dtype=torch.int32, device=verts.device)
     r0, r1 = (0, nf) if rows is None else rows
     nphi = 3 if int(order) == int(OrderType.LINEAR) else 1
@@ -213,7 +213,7 @@ def laplace_colloc_sl(verts: torch.Tensor, faces: torch.Tensor, rows=None, out=N
     if check_indices:
         check_face_range(faces, verts.shape[0])
     if near is None:
-        near = laplace_near_pairs(faces)
+        near = laplace_near_pairs(faces, verts.shape[0])
     _lib.check_tensor(near, "near", dtype=torch.int32, device=verts.device)
     r0, r1 = (0, nf) if rows is None else rows
     if out is None:

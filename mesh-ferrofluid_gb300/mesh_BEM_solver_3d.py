@@ -201,7 +201,7 @@ class MeshBEMSolver3d:
             normals = compute_face_normals(vertices=verts, faces=faces).contiguous()
         # the symmetric rule needs only the face pairs sharing a vertex (O(F)), not the
         # dense [F, F] relation of the reference rule
-        near = shared_vertex_pairs(faces) if sym else None
+        near = shared_vertex_pairs(faces, n_verts) if sym else None
         panel_relations = None if sym else compute_panel_relation(faces)
         neu_list, dir_list = [], []
         mats = {}

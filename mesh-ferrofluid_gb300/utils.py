@@ -20,6 +20,7 @@ tensors.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 import sys
 from enum import Enum
@@ -281,17 +282,32 @@ def get_edge_unique(verts: torch.Tensor, faces: torch.Tensor):
     return edges, inv.to(faces.dtype), adj.to(faces.dtype)
 
 
-def shared_vertex_pairs(faces: torch.Tensor) -> torch.Tensor:
+def shared_vertex_pairs(faces: torch.Tensor, n_verts: int | None = None) -> torch.Tensor:
     """All ordered face pairs sharing at least one vertex (each face with itself included),
     [n, 2] int32 sorted by first face, then second: the nonzeros of
     ``compute_panel_relation`` (mesh_utils.py:700-725) in row-major order, built in O(F) memory
-    instead of from the dense [F, F] relation -- the vertex-face incidences sorted by vertex,
-    every ordered pair of faces around each vertex, one sorted unique of the pair keys."""
+    instead of from the dense [F, F] relation.  CUDA faces: ``mb_shared_vertex_pairs_*``
+    (vertex-face incidences, per-face merge of the three sorted vertex lists; one host
+    synchronisation for the length; ``n_verts`` defaults to max id + 1).  Host faces (the
+    CPU baseline and host tests): the same list from torch -- every ordered pair of faces
+    around each vertex, one sorted unique of the pair keys."""
     faces = faces.reshape(-1, 3)
     nf = faces.shape[0]
     dev = faces.device
     if nf == 0:
         return torch.zeros((0, 2), dtype=torch.int32, device=dev)
+    if faces.is_cuda:
+        faces = faces.to(torch.int32).contiguous()
+        nv = int(faces.max()) + 1 if n_verts is None else int(n_verts)
+        lib = _lib.load()
+        ws = torch.empty(int(lib.mb_shared_vertex_pairs_workspace_bytes(nf, nv)), dtype=torch.uint8, device=dev)
+        n = ctypes.c_int64(0)
+        _lib.call("mb_shared_vertex_pairs_count", _lib.ptr(faces), nf, nv, _lib.ptr(ws), ws.numel(),
+                  ctypes.byref(n), _lib.stream_of(faces))
+        pairs = torch.empty((int(n.value), 2), dtype=torch.int32, device=dev)
+        _lib.call("mb_shared_vertex_pairs_fill", _lib.ptr(faces), nf, nv, _lib.ptr(ws), _lib.ptr(pairs),
+                  _lib.stream_of(faces))
+        return pairs
     v = faces.reshape(-1).long()
     f = torch.arange(nf, device=dev, dtype=torch.long).repeat_interleave(3)
     order = torch.argsort(v, stable=True)
