@@ -126,19 +126,22 @@ def hypersingular_tight(verts: torch.Tensor, faces: torch.Tensor, v0: torch.Tens
 
 
 def laplace_sym_tight(verts: torch.Tensor, faces: torch.Tensor, op: int, near: torch.Tensor | None = None,
-                      rows=None, out: torch.Tensor | None = None) -> torch.Tensor:
+                      rows=None, out: torch.Tensor | None = None, check_indices: bool = True) -> torch.Tensor:
     """Packed symmetric-rule operator [V, V] (``mb_laplace_sym_tight_*``) without the
     [F, F, 3, 3] panels: op 1 single layer, 2 double layer (both P1, equal to packing
     ``laplace_sym_panels``), 3 hypersingular (equal to ``hypersingular_tight`` of the P0
     single layer).  Accumulates into ``out`` when given.  Meshes whose 3 V row values
-    exceed the shared-memory budget take the panels-then-pack path."""
+    exceed the shared-memory budget take the panels-then-pack path.  ``check_indices=False``
+    skips the vertex-id range check (one reduction and a host synchronisation) for faces
+    already validated, e.g. by ``shared_vertex_pairs``."""
     _lib.check_tensor(verts, "verts", dtype=(torch.float32, torch.float64), ndim=2)
     faces = faces.to(torch.int32).contiguous()
     _lib.check_tensor(faces, "faces", device=verts.device, ndim=2)
     if int(op) not in (1, 2, 3):
         raise ValueError("op must be 1 (single layer), 2 (double layer) or 3 (hypersingular)")
     nf, nv = faces.shape[0], verts.shape[0]
-    check_face_range(faces, nv)
+    if check_indices:
+        check_face_range(faces, nv)
     if near is None:
         near = laplace_near_pairs(faces, verts.shape[0])
     _lib.check_tensor(near, "near", dtype=torch.int32, device=verts.device)

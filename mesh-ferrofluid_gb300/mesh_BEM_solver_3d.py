@@ -72,16 +72,19 @@ def _sym_part(A: torch.Tensor) -> torch.Tensor:
     return 0.5 * (A + A.transpose(0, 1))
 
 
-def _cholesky(A: torch.Tensor) -> torch.Tensor:
-    L, info = torch.linalg.cholesky_ex(_sym_part(A))
-    if int(info) != 0:
-        raise RuntimeError(f"the symmetric part is not positive definite (cholesky info {int(info)})")
-    return L
+def _check_cholesky(*infos: torch.Tensor) -> None:
+    """One host synchronisation for all factorisations of a solve."""
+    bad = [int(i) for i in torch.stack([i.reshape(()) for i in infos]).cpu()]
+    if any(bad):
+        raise RuntimeError(f"a symmetric part is not positive definite (cholesky info {bad})")
 
 
 def _spd_solve(A: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     """A x = b through the Cholesky factor of A's symmetric part (V, or D + a a^T)."""
-    return torch.cholesky_solve(b.reshape(-1, 1), _cholesky(A)).reshape(-1)
+    L, info = torch.linalg.cholesky_ex(_sym_part(A))
+    x = torch.cholesky_solve(b.reshape(-1, 1), L).reshape(-1)
+    _check_cholesky(info)
+    return x
 
 
 def _schur_solve(Vdd, B, Dnn, r1, r2):
@@ -90,12 +93,13 @@ def _schur_solve(Vdd, B, Dnn, r1, r2):
     x2 = S^-1 (r2 - W^T L^-1 r1), x1 = L^-T (L^-1 r1 + W x2).  Vdd and Dnn enter through
     their symmetric parts (the Galerkin operators are symmetric; the assembled ones differ
     at the quadrature error)."""
-    L = _cholesky(Vdd)
+    L, info_v = torch.linalg.cholesky_ex(_sym_part(Vdd))
     W = torch.linalg.solve_triangular(L, B, upper=False)
     y = torch.linalg.solve_triangular(L, r1.reshape(-1, 1), upper=False)
-    Ls = _cholesky(Dnn + W.transpose(0, 1) @ W)
+    Ls, info_s = torch.linalg.cholesky_ex(_sym_part(Dnn + W.transpose(0, 1) @ W))
     x2 = torch.cholesky_solve(r2.reshape(-1, 1) - W.transpose(0, 1) @ y, Ls)
     x1 = torch.linalg.solve_triangular(L.transpose(0, 1), y + W @ x2, upper=True)
+    _check_cholesky(info_v, info_s)
     return torch.cat((x1, x2)).reshape(-1)
 
 
@@ -211,7 +215,9 @@ class MeshBEMSolver3d:
         def tight(name):
             if name not in mats and sym and self.order_type == int(OrderType.LINEAR):
                 # packed straight from the face pairs; the [F, F, 3, 3] panels are not kept
-                mats[name] = laplace_sym_tight(verts, faces, {"V": 1, "K": 2, "D": 3}[name], near)
+                # faces were validated by shared_vertex_pairs (its count phase checks the ids)
+                mats[name] = laplace_sym_tight(verts, faces, {"V": 1, "K": 2, "D": 3}[name], near,
+                                               check_indices=not faces.is_cuda)
             if name not in mats and sym:
                 layers[name].compute_sym(verts, faces, near)
                 mats[name] = layers[name]._tight(verts, faces)
