@@ -8,10 +8,11 @@ polarisation, the incident phase at the midpoint and the excitation coefficient 
 h' = relu([h, mean_nbr h] W + b) with hidden width 128, and a 128 -> 2 read-out giving the
 edge current J_e (normalised).  The initial guess of a column is the residual-minimising
 combination of the real and imaginary parts of the predictions for all incidences of its
-mesh (``subspace_guess``: a least-squares fit over a 2 nc-vector learned subspace).  Weights and activations are BF16, every product is accumulated in FP32, master
-weights and Adam moments are FP32; forward and backward run on this library's kernels
-(``mb_gnn_*``).  The prediction is used as the GMRES initial guess; plain GMRES from zero
-stays the fallback and the judge of the result.
+mesh (``subspace_guess``: a least-squares fit over a 2 nc-vector learned subspace).
+Weights and activations are BF16, every product is accumulated in FP32, master weights and
+Adam moments are FP32; forward and backward run on this library's kernels (``mb_gnn_*``).
+The prediction is only a GMRES initial guess: GMRES still iterates to the requested
+residual, so the guess changes the iteration count, never the accuracy of the result.
 """
 from __future__ import annotations
 

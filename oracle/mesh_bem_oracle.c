@@ -2,7 +2,7 @@
  * mesh_bem_oracle.c -- CPU restatement of the reference's boundary-element hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests, the smoke
- * check and the CPU-baseline leg of bench.py call it to judge the CUDA path.  The
+ * check and the CPU-baseline leg of bench.py call it to check the CUDA path.  The
  * product (the CUDA library and its Python host layer) never links, loads or calls it.
  *
  * It restates, loop for loop, what the reference computes (GeCao/Mesh-Ferrofluid):
