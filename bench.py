@@ -60,6 +60,9 @@ WORKLOADS = {
     "radiate_L5": (5, 10.0, 1024),
     # GPU mesh topology (unique edges + face-edge map + edge faces, near-pair list, Z-row map)
     "topology_L7": (7,),
+    # the reference's own Laplace path (demo_Laplace_3d.py): Dirichlet solve with its rule, P1:
+    # (icosphere level, gaussQR, radius)
+    "laplace_ref_L4": (4, 2, 0.5),
     # Laplace mixed Dirichlet / Neumann solve, u = z on the unit sphere: (icosphere level, dtype)
     "laplace_mixed_L4": (4, "f32"),
     "laplace_mixed_L3": (3, "f32"),
@@ -741,6 +744,173 @@ def main_topology(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def main_lapref(args, rank, world, local_rank):
+    """The reference's own Laplace path as demo_Laplace_3d.py drives it: MeshBEMSolver3d with
+    the reference rule (double Duffy collapse, integrations_3d.py:252-452), P1, all-Dirichlet
+    data, through solve (mesh_BEM_solver_3d.py:197-373): the shared-vertex relation, V and K
+    panels, their packing, the right-hand side and the dense LU solve."""
+    level, gq, radius = WORKLOADS[args.workload]
+    import torch
+
+    pkg = importlib.import_module("mesh-ferrofluid_gb300")
+    R, U = pkg.roofline, pkg.utils
+    v_np, f_np = pkg.meshes.icosphere(level, radius)
+    nf, nv = f_np.shape[0], v_np.shape[0]
+    config = {"workload": args.workload, "mesh": f"icosphere L{level}, radius {radius}", "n_faces": nf,
+              "n_verts": nv, "problem": "u = z on the whole surface (Dirichlet), unknown du/dn = z / a",
+              "rule": f"the reference's (gaussQR = {gq}: collapsed Gauss rule per sub-domain), P1, float32",
+              "solver": "dense LU (torch.linalg.solve), as the reference", "parallelism": "replicas"}
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference's Laplace path is torch code; its "
+                              "algorithm is timed by cpu_baseline (the C oracle)"}), flush=True)
+        return
+    dev = torch.device("cuda", local_rank if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    verts = torch.tensor(v_np, dtype=torch.float32, device=dev)
+    faces = torch.tensor(f_np, dtype=torch.int32, device=dev)
+    z = verts[:, 2:3].clone()
+    flags = torch.full((1, nv, 1), int(pkg.BoundaryType.DIRICHLET), dtype=torch.uint8, device=dev)
+    g, h = z[None], torch.zeros_like(z)[None]
+    solver = pkg.MeshBEMSolver3d(gaussQR=gq, order_type=1, BEM_type=int(pkg.BEMType.LAPLACE), wavenumber=1.0,
+                                 logger=None, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        out = solver.solve(verts, faces, g, h, flags)
+    torch.cuda.synchronize(dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.3)
+    calls0 = pkg._lib.call_count
+    for e0, e1 in ev:
+        e0.record(stream)
+        out = solver.solve(verts, faces, g, h, flags)
+        e1.record(stream)
+    torch.cuda.synchronize(dev)
+    clocks.stop()
+    abi_calls = pkg._lib.call_count - calls0
+    ms = [a.elapsed_time(b) for a, b in ev]
+    ms_per_step = sum(ms) / args.steps
+    neu = out[0][0]
+    err = float(torch.linalg.norm(neu - z / radius) / torch.linalg.norm(z / radius))
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize(dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            r = fn()
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        return a.elapsed_time(b) / reps, r
+
+    areas = U.compute_face_areas(vertices=verts, faces=faces, keepdim=True).contiguous()
+    normals = U.compute_face_normals(vertices=verts, faces=faces).contiguous()
+    t_rel, rel = timed(lambda: U.compute_panel_relation(faces))
+    rands = torch.cat((solver.single_layer.r1, solver.single_layer.r2), dim=-1)
+    w = solver.single_layer.gauss_weights
+
+    def panels(layer):
+        return pkg.double_integration_on_panels_3d(int(pkg.BEMType.LAPLACE), 1, verts, faces, areas, normals, w, w,
+                                                   rands, rands, rel, 1.0, layer)
+
+    t_v, Vp = timed(lambda: panels(1))
+    t_k, _ = timed(lambda: panels(2))
+    t_pack, Vt = timed(lambda: U.pack_matrix_tight(1, Vp, verts, faces))
+    rhs = torch.ones(nv, 1, device=dev)
+    t_lu, _ = timed(lambda: torch.linalg.solve(Vt, rhs))
+    del Vp
+    # evaluations per face pair of the reference rule: separated pairs use the plain tensor
+    # rule (n_w points on each face), the few pairs sharing a vertex their sub-domain tables
+    n_w = int(w.numel())
+    peaks = R.measured_peaks(REPO)
+    fp32_peak = R.fp32_peak_tflops(float(peaks.get("sm_max_mhz", 2070.0)))
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    flop = float(nf) ** 2 * n_w * n_w * (R.LAPLACE_SL_FLOP_PER_EVAL + 6)
+    out_bytes = float(nf) ** 2 * 36
+    line = {"metric": "Laplace Dirichlet solve time (reference rule)", "value": ms_per_step, "unit": "ms",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config, "accuracy": {"dudn_rel_err": err,
+                                           "note": "the reference rule's own discretisation error (double Duffy "
+                                                   "collapse, no vertex alignment of the singular sub-domains)"},
+            "breakdown_ms": {"panel_relation": t_rel, "V_panels": t_v, "K_panels": t_k, "pack_one_operator": t_pack,
+                             "lu_solve_VxV": t_lu},
+            "roofline": {"kernel": "laplace_panels_kernel<float, 3, 0, 1> (V panels)", "bound": "fp32 / hbm",
+                         "achieved": flop / (t_v / 1e3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": flop / (t_v / 1e3) / 1e12 / fp32_peak,
+                         "peak_source": "derived FP32 SIMT peak at the max SM clock",
+                         "hbm": {"achieved_gbs": out_bytes / (t_v / 1e3) / 1e9, "peak_gbs": hbm,
+                                 "frac": out_bytes / (t_v / 1e3) / 1e9 / hbm},
+                         "traffic": None,
+                         "algorithmic": f"{n_w} x {n_w} evaluations per separated pair, "
+                                        f"{R.LAPLACE_SL_FLOP_PER_EVAL} + 6 (P1 weights) FLOP and 1 rsqrt each; "
+                                        "output 36 B per pair",
+                         "kernel_ms": t_v},
+            "clocks": clocks.summary(), "gpu_launches": abi_calls,
+            "gpu_launches_note": "C-ABI calls in the timed region (each launches one or two of the library's "
+                                 "kernels); torch's LU kernels not counted"}
+    if not args.no_e2e:
+        h_v = torch.tensor(v_np, dtype=torch.float32).pin_memory()
+        h_f = torch.tensor(f_np, dtype=torch.int32).pin_memory()
+        h_in = [t.cpu().pin_memory() for t in (g, h, flags)]
+        h_out = [torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in out]
+        d_v, d_f = torch.empty_like(verts), torch.empty_like(faces)
+        d_in = [torch.empty_like(t) for t in (g, h, flags)]
+
+        def e2e_step():
+            d_v.copy_(h_v, non_blocking=True)
+            d_f.copy_(h_f, non_blocking=True)
+            for d, hh in zip(d_in, h_in):
+                d.copy_(hh, non_blocking=True)
+            res = solver.solve(d_v, d_f, *d_in)
+            for hh, r in zip(h_out, res):
+                hh.copy_(r, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize(dev)
+        n_e2e = max(2, min(args.steps, 3))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n_e2e):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        e2e_ms = e0.elapsed_time(e1) / n_e2e
+        line["e2e"] = {"value": e2e_ms, "unit": "ms",
+                       "h2d_bytes_per_step": h_v.numel() * 4 + h_f.numel() * 4 +
+                                             sum(t.numel() * t.element_size() for t in h_in),
+                       "d2h_bytes_per_step": sum(t.numel() * t.element_size() for t in h_out),
+                       "ms_per_step": e2e_ms, "steps": n_e2e,
+                       "path": "MeshBEMSolver3d.solve, reference rule (C ABI mb_panel_relation, "
+                               "mb_laplace_panels_f32, mb_pack_tight_f32), pinned host mesh and data in, both traces "
+                               "back"}
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+
+        threads = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+        n_s = min(nf, 1024)
+        a_np, n_np = areas.cpu().double().numpy(), normals.cpu().double().numpy()
+        rel_np, r_np, w_np = rel.cpu().numpy(), rands.cpu().double().numpy(), w.cpu().double().numpy()
+        t0 = time.perf_counter()
+        O.laplace_panels(v_np, f_np, a_np, n_np, r_np, w_np, rel_np, 1, 1, rows=(0, n_s))
+        O.laplace_panels(v_np, f_np, a_np, n_np, r_np, w_np, rel_np, 2, 1, rows=(0, n_s))
+        t_ops = (time.perf_counter() - t0) * nf / n_s
+        An = np.random.default_rng(0).normal(size=(nv, nv)) + nv * np.eye(nv)
+        t0 = time.perf_counter()
+        np.linalg.solve(An, np.ones(nv))
+        t_solve = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": (t_ops + t_solve) * 1e3, "unit": "ms", "cores": threads, "kind": "port",
+                                "sample": f"V and K panels of the first {n_s} of {nf} face rows with the double C "
+                                          "restatement of the reference rule, scaled to all rows, plus a numpy LU "
+                                          f"solve of size {nv}; packing not counted"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main_lapmixed(args, rank, world, local_rank):
     """Mixed Dirichlet / Neumann Laplace solve through MeshBEMSolver3d.solve (the reference's
     facade, mesh_BEM_solver_3d.py:197-373): symmetric-rule V, K and hypersingular D,
@@ -1403,6 +1573,8 @@ def main():
         return main_rays(args, rank, world, local_rank)
     if args.workload.startswith("laplace_mixed"):
         return main_lapmixed(args, rank, world, local_rank)
+    if args.workload.startswith("laplace_ref"):
+        return main_lapref(args, rank, world, local_rank)
     if args.workload.startswith("laplace_"):
         return main_laplace(args, rank, world, local_rank)
     if args.workload.startswith("mrhs_"):

@@ -67,9 +67,7 @@ def double_integration_on_panels_3d(BEM_type: int, order_type: int, verts: torch
     if areas.numel() != nf or face_normals.numel() != 3 * nf:
         raise ValueError("face_areas / face_normals must have F / 3F entries")
     normals = face_normals.to(dt).contiguous()
-    table, seg = panel_rule_table(rands_x.to(dt), rands_y.to(dt), gauss_weightsx.to(dt),
-                                  gauss_weightsy.to(dt))
-    table = table.to(dev).contiguous()
+    table, seg = _cached_rule_table(rands_x, rands_y, gauss_weightsx, gauss_weightsy, dt, dev)
     seg_c = (torch.tensor(seg, dtype=torch.int32)).numpy()
     rel = None
     if panel_relations is not None:
@@ -86,6 +84,27 @@ def double_integration_on_panels_3d(BEM_type: int, order_type: int, verts: torch
               1 if nphi == 3 else 0, kind, float(wavenumber), 0, nf, _lib.ptr(out_r), _lib.ptr(out_i),
               _lib.stream_of(verts))
     return torch.complex(out_r, out_i) if kind == 1 else out_r
+
+
+# Flattened sub-domain rule tables of recent calls, keyed by the rules' values (a few dozen
+# numbers, one small copy to the host).  Building a table takes ~150 small torch operations
+# and a solver passes the same rule on every call.
+_RULE_TABLES: list = []
+_RULE_TABLES_MAX = 8
+
+
+def _cached_rule_table(rx, ry, wx, wy, dt, dev):
+    ins = (rx, ry, wx, wy)
+    vals = torch.cat([t.reshape(-1).to(torch.float64) for t in ins]).cpu().tolist()
+    key = (tuple(tuple(t.shape) for t in ins), tuple(vals), dt, str(dev))
+    for k, val in _RULE_TABLES:
+        if k == key:
+            return val
+    table, seg = panel_rule_table(rx.to(dt), ry.to(dt), wx.to(dt), wy.to(dt))
+    val = (table.to(dev).contiguous(), seg)
+    _RULE_TABLES.append((key, val))
+    del _RULE_TABLES[:-_RULE_TABLES_MAX]
+    return val
 
 
 def hypersingular_from_v0(verts: torch.Tensor, faces: torch.Tensor, v0: torch.Tensor) -> torch.Tensor:
