@@ -63,6 +63,8 @@ WORKLOADS = {
     # the reference's own Laplace path (demo_Laplace_3d.py): Dirichlet solve with its rule, P1:
     # (icosphere level, gaussQR, radius)
     "laplace_ref_L4": (4, 2, 0.5),
+    # the ferrofluid pressure projection (MeshPressure.solve), hydrostatic droplet: (icosphere level,)
+    "pressure_L4": (4,),
     # Laplace mixed Dirichlet / Neumann solve, u = z on the unit sphere: (icosphere level, dtype)
     "laplace_mixed_L4": (4, "f32"),
     "laplace_mixed_L3": (3, "f32"),
@@ -911,6 +913,117 @@ def main_lapref(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def main_pressure(args, rank, world, local_rank):
+    """The ferrofluid pressure projection, MeshPressure.solve (src/mesh_ferrofluid/
+    mesh_pressure.py:54-163): curvature, boundary data, the mixed Laplace solve and the
+    velocity update, on a unit-sphere droplet resting on a solid (y <= 0: Neumann)."""
+    (level,) = WORKLOADS[args.workload]
+    import torch
+
+    pkg = importlib.import_module("mesh-ferrofluid_gb300")
+    v_np, f_np = pkg.meshes.icosphere(level, 1.0)
+    nf, nv = f_np.shape[0], v_np.shape[0]
+    g, rho, dt = 9.8, 2.0, 0.01
+    config = {"workload": args.workload, "mesh": f"icosphere L{level}, radius 1", "n_faces": nf, "n_verts": nv,
+              "data": f"hydrostatic: vel = (0, g dt, 0), rho = {rho}, g = {g}, dt = {dt}, surface tension 0.07; "
+                      "air (Dirichlet) for y > 0, solid (Neumann) below",
+              "solver": "MeshPressure(rule dunavant7, solver schur), float32", "parallelism": "replicas"}
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference's pressure solve cannot run (its "
+                              "hypersingular layer is None); the oracle's operators are timed by cpu_baseline"}),
+                  flush=True)
+        return
+    dev = torch.device("cuda", local_rank if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    verts = torch.tensor(v_np, dtype=torch.float32, device=dev)
+    faces = torch.tensor(f_np, dtype=torch.int32, device=dev)
+    mp = pkg.MeshPressure(density_fluid=rho, gravity_strength=g, surface_tension=0.07, contact_angle=0.0,
+                          gaussQR=3, order_type=1, logger=None, device=dev, dtype=torch.float32, solver="schur")
+    flags = torch.where(verts[:, 1:2] > 0, int(pkg.BoundaryType.DIRICHLET), int(pkg.BoundaryType.NEUMANN))
+    flags = flags.to(torch.uint8)[None]
+    vel = torch.zeros((1, nv, 3), dtype=torch.float32, device=dev)
+    vel[..., 1] = g * dt
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        new = mp.solve(verts, faces, dt, vel, flags)
+    torch.cuda.synchronize(dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.3)
+    calls0 = pkg._lib.call_count
+    for e0, e1 in ev:
+        e0.record(stream)
+        new = mp.solve(verts, faces, dt, vel, flags)
+        e1.record(stream)
+    torch.cuda.synchronize(dev)
+    clocks.stop()
+    abi_calls = pkg._lib.call_count - calls0
+    ms_per_step = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    n = pkg.utils.compute_vert_normals(verts, faces)
+    solid = flags[0, :, 0] == int(pkg.BoundaryType.NEUMANN)
+    vn = float((new[0] * n).sum(-1)[solid].abs().max()) / (g * dt)
+    line = {"metric": "pressure projection step time", "value": ms_per_step, "unit": "ms", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+            "accuracy": {"max_normal_velocity_on_solid_over_g_dt": vn},
+            "roofline": {"kernel": "the mixed Laplace solve inside (laplace_mixed_* workloads)", "bound": None,
+                         "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None},
+            "clocks": clocks.summary(), "gpu_launches": abi_calls,
+            "gpu_launches_note": "C-ABI calls in the timed region (each launches one or two of the library's "
+                                 "kernels); torch's kernels not counted"}
+    if not args.no_e2e:
+        h_v = torch.tensor(v_np, dtype=torch.float32).pin_memory()
+        h_f = torch.tensor(f_np, dtype=torch.int32).pin_memory()
+        h_vel, h_flags = vel.cpu().pin_memory(), flags.cpu().pin_memory()
+        h_new = torch.empty(new.shape, dtype=new.dtype, pin_memory=True)
+        d_v, d_f, d_vel, d_flags = (torch.empty_like(t) for t in (verts, faces, vel, flags))
+
+        def e2e_step():
+            d_v.copy_(h_v, non_blocking=True)
+            d_f.copy_(h_f, non_blocking=True)
+            d_vel.copy_(h_vel, non_blocking=True)
+            d_flags.copy_(h_flags, non_blocking=True)
+            h_new.copy_(mp.solve(d_v, d_f, dt, d_vel, d_flags), non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize(dev)
+        n_e2e = max(2, min(args.steps, 3))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n_e2e):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        e2e_ms = e0.elapsed_time(e1) / n_e2e
+        line["e2e"] = {"value": e2e_ms, "unit": "ms",
+                       "h2d_bytes_per_step": (h_v.numel() + h_f.numel() + h_vel.numel()) * 4 + h_flags.numel(),
+                       "d2h_bytes_per_step": h_new.numel() * 4, "ms_per_step": e2e_ms, "steps": n_e2e,
+                       "path": "MeshPressure.solve, pinned host mesh, velocities and flags in, new velocities back"}
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+
+        threads = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+        n_s = min(nf, 1024)
+        t0 = time.perf_counter()
+        O.laplace_sym(v_np, f_np, 1, 1, rows=(0, n_s))
+        O.laplace_sym(v_np, f_np, 2, 1, rows=(0, n_s))
+        O.laplace_sym(v_np, f_np, 1, 0, rows=(0, n_s))
+        t_ops = (time.perf_counter() - t0) * nf / n_s
+        An = np.random.default_rng(0).normal(size=(nv, nv)) + nv * np.eye(nv)
+        t0 = time.perf_counter()
+        np.linalg.solve(An, np.ones(nv))
+        t_solve = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": (t_ops + t_solve) * 1e3, "unit": "ms", "cores": threads, "kind": "port",
+                                "sample": f"V, K and V0 panels of the first {n_s} of {nf} face rows with the double "
+                                          f"C oracle, scaled to all rows, plus a numpy LU solve of size {nv} (the "
+                                          "projection's curvature and gradients not counted)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main_lapmixed(args, rank, world, local_rank):
     """Mixed Dirichlet / Neumann Laplace solve through MeshBEMSolver3d.solve (the reference's
     facade, mesh_BEM_solver_3d.py:197-373): symmetric-rule V, K and hypersingular D,
@@ -1571,6 +1684,8 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.workload.startswith("ray_"):
         return main_rays(args, rank, world, local_rank)
+    if args.workload.startswith("pressure_"):
+        return main_pressure(args, rank, world, local_rank)
     if args.workload.startswith("laplace_mixed"):
         return main_lapmixed(args, rank, world, local_rank)
     if args.workload.startswith("laplace_ref"):

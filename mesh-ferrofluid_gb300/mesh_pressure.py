@@ -10,7 +10,8 @@ gradient of p; v_new = v - (dt/rho) grad p.
 The reference cannot run this path (its hypersingular layer is None); here the solve uses
 ``HyperSingularLayer3d`` with ``rule="dunavant7"`` by default (the reference rule is
 available through ``rule="reference"`` but its hypersingular operator is indefinite on
-coarse meshes).  Diagnostics go to the logger instead of stdout.
+coarse meshes).  ``solver`` is passed to ``MeshBEMSolver3d`` ("lu" as the reference, or
+"schur").  Diagnostics go to the logger instead of stdout.
 """
 from __future__ import annotations
 
@@ -31,7 +32,7 @@ from .utils import (
 class MeshPressure:
     def __init__(self, density_fluid: float, gravity_strength: float, surface_tension, contact_angle,
                  gaussQR: int, order_type: int, logger, device: torch.device = torch.device("cpu"),
-                 dtype: torch.dtype = torch.float32, rule: str = "dunavant7"):
+                 dtype: torch.dtype = torch.float32, rule: str = "dunavant7", solver: str = "lu"):
         self.gaussQR = gaussQR
         self.order_type = order_type
         self.logger = logger
@@ -42,7 +43,8 @@ class MeshPressure:
         self.surface_tension = surface_tension
         self.contact_angle = contact_angle
         self.BEM_solver = MeshBEMSolver3d(gaussQR=gaussQR, order_type=order_type, BEM_type=int(BEMType.LAPLACE),
-                                          wavenumber=1.0, logger=logger, device=device, dtype=dtype, rule=rule)
+                                          wavenumber=1.0, logger=logger, device=device, dtype=dtype, rule=rule,
+                                          solver=solver)
 
     def signed_mean_curvature(self, verts: torch.Tensor, faces: torch.Tensor,
                               vert_normals: torch.Tensor) -> torch.Tensor:
