@@ -167,3 +167,30 @@ def test_schur_solve_matches_dense_block_solve(pkg):
     assert (m._spd_solve(V, r1) - torch.linalg.solve(V, r1)).abs().max().item() < 1e-12
     with pytest.raises(RuntimeError):
         m._spd_solve(-V, r1)
+
+
+def test_rule_table_cache_keys_on_values(pkg):
+    """The flattened sub-domain rule table is reused for equal rules (even new tensors) and
+    rebuilt when a rule value, the dtype or the rule size changes."""
+    L, U = pkg.layers, pkg.utils
+
+    def rule(q, dt):
+        p, w1 = U.get_gaussion_integration_points_and_weights(q, device="cpu", dtype=dt)
+        r, w = U.collapsed_rule_2d(p, w1)
+        return r, w
+
+    r, w = rule(2, torch.float64)
+    t1, s1 = L._cached_rule_table(r, r, w, w, torch.float64, torch.device("cpu"))
+    t2, s2 = L._cached_rule_table(r.clone(), r.clone(), w.clone(), w.clone(), torch.float64, torch.device("cpu"))
+    assert t2 is t1 and s2 == s1
+    ref, seg = U.panel_rule_table(r, r, w, w)
+    assert torch.equal(t1, ref) and s1 == seg
+    r2 = r.clone()
+    r2[0, 0] += 1e-3
+    t3, _ = L._cached_rule_table(r2, r2, w, w, torch.float64, torch.device("cpu"))
+    assert t3 is not t1 and torch.equal(t3, U.panel_rule_table(r2, r2, w, w)[0])
+    t4, _ = L._cached_rule_table(r, r, w, w, torch.float32, torch.device("cpu"))
+    assert t4.dtype == torch.float32
+    r3, w3 = rule(3, torch.float64)
+    t5, s5 = L._cached_rule_table(r3, r3, w3, w3, torch.float64, torch.device("cpu"))
+    assert t5.shape[0] != t1.shape[0] and s5 == U.panel_rule_table(r3, r3, w3, w3)[1]
