@@ -98,10 +98,6 @@ int mb_mom_zmat_rwg_c128(const double* verts, int64_t n_verts, const int32_t* fa
                          double wavenumber, int64_t row_begin, int64_t row_end, double* z,
                          void* stream);
 
-/* No counterpart in the reference (its scatter_add_ runs after the whole face-edge matrix
- * exists).  edge_rows [2 n_edges + 1] int32: for Z row m (edge m) the face-edge rows 3f + e
- * of its faces (smaller first; -1 for a missing second face); edge_rows[2 n_edges] = 1 when
- * some edge has more than two faces (the edge-row operators below then do not apply). */
 /* Ordered face pairs sharing at least one vertex (each face with itself), sorted by first
  * face then second: the nonzeros of compute_panel_relation (src/utils/mesh_utils.py:700-725)
  * in row-major order -- the near-pair list of the symmetric-rule operators -- in O(F) memory.
@@ -115,6 +111,10 @@ int mb_shared_vertex_pairs_count(const int32_t* faces, int64_t n_faces, int64_t 
 int mb_shared_vertex_pairs_fill(const int32_t* faces, int64_t n_faces, int64_t n_verts, void* workspace,
                                 int32_t* pairs, void* stream);
 
+/* No counterpart in the reference (its scatter_add_ runs after the whole face-edge matrix
+ * exists).  edge_rows [2 n_edges + 1] int32: for Z row m (edge m) the face-edge rows 3f + e
+ * of its faces (smaller first; -1 for a missing second face); edge_rows[2 n_edges] = 1 when
+ * some edge has more than two faces (the edge-row operators below then do not apply). */
 int mb_mom_edge_rows(const int32_t* face_edge_indices, int64_t n_faces, int64_t n_edges, int32_t* edge_rows,
                      void* stream);
 /* The same matrix as mb_mom_zmat_rwg_c64, built Z row by Z row: rows [m_begin, m_end) of z
@@ -431,16 +431,21 @@ int mb_gmres_blockdiag_c64(const float* z, const int64_t* desc, const int64_t* g
  * the library until the process exits), sized for at most MB_GMRES_NOALLOC_MAX_N unknowns
  * and restart <= MB_GMRES_NOALLOC_MAX_RESTART; larger requests fail with MB_ERR_SIZE.
  * The first call on each device looks up that array's device address (a one-time set-up
- * with that device current); make that first call before any stream capture.  All calls
- * share the array, which keeps the previous call's contents (the solver writes every
- * scratch value before reading it); calls that overlap on the GPU race on it. */
+ * with that device current) and keeps it for the life of the process; make that first call
+ * before any stream capture.  Calls after cudaDeviceReset() on that device are not supported
+ * (the kept address would be stale).  All calls share the array, which keeps the previous
+ * call's contents (the solver writes every scratch value before reading it); calls that
+ * overlap on the GPU race on it. */
 #define MB_GMRES_NOALLOC_MAX_N 8192
 #define MB_GMRES_NOALLOC_MAX_RESTART 50
 int mb_gmres_c64_noalloc(const float* z, int64_t n, const double* b, double* x, int restart,
                          int max_iters, double tol, mb_gmres_info* info, void* stream);
 
 /* y = Z v: Z interleaved complex64 [n, n], v complex64 [n], y complex128 [n] (FP32 products,
- * FP64 row reduction).  The HBM-bound kernel inside mb_gmres_c64. */
+ * FP64 row reduction).  The HBM-bound kernel inside mb_gmres_c64.  Alignment: z, v and y
+ * need only the natural alignment of their element type (8 bytes); rows and a v that start
+ * on a 16-byte boundary are read 16 bytes at a time, others one complex number at a time
+ * (slower), so a view such as X[1:n+1] of a complex64 array is accepted. */
 int mb_matvec_c64(const float* z, const float* v, int64_t n, double* y, void* stream);
 
 /* r = b - Z x in FP64: Z complex64 [n, n], x, b, r complex128 [n]. */

@@ -41,7 +41,9 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // y[row] = sum_j Z[row, j] v[j]; Z, v interleaved complex64; y complex128.
-// One warp per row; lane l reads float4 (two complex) at 16-byte granularity.
+// One warp per row; lane l reads float4 (two complex) at 16-byte granularity when both the
+// Z row and v start on a 16-byte boundary, else one complex at a time (v may be an
+// 8-byte-aligned view such as X[1:n+1] of a complex64 array).
 __global__ void __launch_bounds__(256) matvec_c64_kernel(const float* __restrict__ z,
                                                          const float* __restrict__ v, int64_t n,
                                                          double* __restrict__ y) {
@@ -53,7 +55,7 @@ __global__ void __launch_bounds__(256) matvec_c64_kernel(const float* __restrict
     const int64_t npair = n >> 1;  // float4 = two complex numbers
     const float4* z4 = reinterpret_cast<const float4*>(zr);
     const float4* v4 = reinterpret_cast<const float4*>(v);
-    const bool aligned = ((reinterpret_cast<uintptr_t>(zr) & 15) == 0);
+    const bool aligned = (((reinterpret_cast<uintptr_t>(zr) | reinterpret_cast<uintptr_t>(v)) & 15) == 0);
     if (aligned) {
         int64_t p = lane;
         for (; p + 96 < npair; p += 128) {
@@ -573,8 +575,10 @@ static int gmres_core(const GmresMatrix& A, int64_t n, const double* b, double* 
 // bookkeeping uses per-thread static storage.  Limits: n <= kNoAllocMaxN unknowns,
 // restart <= kNoAllocMaxRestart.
 // The first call on each device looks up the array's device address with
-// cudaGetSymbolAddress (with that device current) and caches it; make that first call
-// before any stream capture.  All calls on a device share the one array and it keeps the
+// cudaGetSymbolAddress (with that device current) and caches it for the life of the
+// process; make that first call before any stream capture.  Calls after cudaDeviceReset()
+// on that device are not supported: the module is loaded again and the cached address
+// would be stale.  All calls on a device share the one array and it keeps the
 // previous call's contents; the solver writes every scratch value before reading it.
 // Calls that overlap on the GPU (other streams, other host threads) race on the array.
 // ---------------------------------------------------------------------------------------

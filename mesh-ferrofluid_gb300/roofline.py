@@ -37,9 +37,22 @@ RADIATE_MUFU_PER_PAIR = 3
 # of FP64 kernels, which have no measured figure
 FP64_NOMINAL_TFLOPS = 1.25
 
-GB300_SMS = 152
+GB300_SMS = 152  # only used when no CUDA device can be queried (CPU-side reports)
 FP32_FLOP_PER_CLK_PER_SM = 256   # 128 FP32 lanes x FMA
 MUFU_OPS_PER_CLK_PER_SM = 16
+
+
+def device_sm_count(device: int = 0) -> int:
+    """Streaming multiprocessors of the CUDA device (cudaDevAttrMultiProcessorCount), or
+    GB300_SMS when no device is visible."""
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            return int(torch.cuda.get_device_properties(device).multi_processor_count)
+    except Exception:  # noqa: BLE001 -- a report must not fail on a missing device
+        pass
+    return GB300_SMS
 
 
 def ref_rule_evals_per_pair(gauss_qr: int) -> int:
@@ -58,9 +71,11 @@ def measured_peaks(repo_root: str) -> dict:
             "sm_max_mhz": 2070.0, "source": "fallback"}
 
 
-def fp32_peak_tflops(sm_mhz: float, sms: int = GB300_SMS) -> float:
+def fp32_peak_tflops(sm_mhz: float, sms: int | None = None) -> float:
+    sms = device_sm_count() if sms is None else sms
     return sms * FP32_FLOP_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e12
 
 
-def mufu_peak_gops(sm_mhz: float, sms: int = GB300_SMS) -> float:
+def mufu_peak_gops(sm_mhz: float, sms: int | None = None) -> float:
+    sms = device_sm_count() if sms is None else sms
     return sms * MUFU_OPS_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e9

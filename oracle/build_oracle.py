@@ -22,7 +22,9 @@ BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 LIB = os.path.join(BUILD_DIR, "libmeshbem_oracle.so")
 REF_LIB = os.path.join(REF_DIR, "libref_mom.so")
-REF_CU = "/root/reference/src/mesh_BEM/cuda/mesh_MOM_3d.cu"
+# the reference checkout (read-only); MESH_FERROFLUID_REF overrides where it lives
+REF_ROOT = os.environ.get("MESH_FERROFLUID_REF", "/root/reference")
+REF_CU = os.path.join(REF_ROOT, "src", "mesh_BEM", "cuda", "mesh_MOM_3d.cu")
 
 _CFLAGS = ["-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-std=c11"]
 

@@ -1,6 +1,7 @@
 """Generate the golden fixtures under tests/golden/ from the reference itself.
 
-Run where the reference checkout is present (it is read, never written):
+Run where the reference checkout is present (it is read, never written; the environment
+variable MESH_FERROFLUID_REF names its root if it is not at the default place):
 
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py
 
@@ -35,7 +36,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF_ROOT = "/root/reference"
+# the reference checkout (read-only); MESH_FERROFLUID_REF overrides where it lives
+REF_ROOT = os.environ.get("MESH_FERROFLUID_REF", "/root/reference")
 
 sys.dont_write_bytecode = True
 sys.path.insert(0, REPO)

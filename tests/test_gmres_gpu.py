@@ -37,6 +37,22 @@ def test_matvec_and_residual_match_torch(pkg, cuda):
     assert rel_err(r.cpu().numpy(), ref_r.cpu().numpy()) < 1e-12
 
 
+def test_matvec_accepts_an_8_byte_aligned_vector_view(pkg, cuda):
+    """v = X[1:n+1] of a complex64 array starts 8 bytes past a 16-byte boundary; the product
+    must read it element by element and equal the product with an aligned copy."""
+    Z, _ = _system(pkg, cuda)
+    n = Z.shape[0]
+    g = torch.Generator(device="cpu").manual_seed(1)
+    X = torch.randn(n + 1, dtype=torch.complex64, generator=g).to(cuda)
+    v = X[1:n + 1]
+    assert v.data_ptr() % 16 == 8
+    y = pkg.mesh_MOM_3d.matvec(Z, v)
+    y_aligned = pkg.mesh_MOM_3d.matvec(Z, v.clone())
+    ref = Z.to(torch.complex128) @ v.to(torch.complex128)
+    assert rel_err(y.cpu().numpy(), ref.cpu().numpy()) < 1e-6
+    assert rel_err(y.cpu().numpy(), y_aligned.cpu().numpy()) < 1e-6
+
+
 @pytest.mark.parametrize("restart", [50, 7])
 def test_gmres_matches_dense_solve(pkg, cuda, restart):
     Z, rhs = _system(pkg, cuda)

@@ -344,3 +344,136 @@ def test_radiate_H_f32_large_vs_oracle(pkg, cuda, oracle):
     f32 = lambda a: a.astype(np.float32).astype(np.float64)  # noqa: E731
     ref = oracle.radiate_h(f32(pts), f32(v_np), f32(va), f32(js.real) + 1j * f32(js.imag), 10.0)
     assert rel_err(H.cpu().numpy(), ref) < TOL32
+
+
+# ---- the benched kernel at the benched phases ---------------------------------------------
+# The bench assembles Z by Z rows (order="edges", float32, gaussQR 4) at ka = 10, so phases
+# kR up to ~20 rad go through the SFU sine / cosine.  These compare that exact code path with
+# the float64 oracle: the whole matrix on the 1280-face sphere and Z-row windows of the
+# 20480-face sphere of the bench itself.
+
+def _scatter_rows(zfe_rows, row_ids, e, ne):
+    """Z rows of the face-edge rows `row_ids` (rows of zfe_rows), columns scattered by e."""
+    out = np.zeros((len(row_ids), ne), np.complex128)
+    for i, r in enumerate(row_ids):
+        np.add.at(out[i], e, zfe_rows[r])
+    return out
+
+
+def test_zmat_rwg_edges_ka10_full_L3_vs_oracle(pkg, cuda, oracle):
+    v, f, a, n, fei, ne, rules = _ico_setup(pkg, cuda, 3)
+    k = 10.0
+    Z = pkg.mesh_MOM_3d.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, k, order="edges")
+    h = lambda t: t.cpu().double().numpy()  # noqa: E731
+    zfe = oracle.mom_zmat_fe(h(v), f.cpu().numpy(), h(a), h(n), *(h(t) for t in rules), k)
+    e = fei.cpu().numpy().reshape(-1).astype(np.int64)
+    zrow = np.zeros((ne, zfe.shape[1]), np.complex128)
+    np.add.at(zrow, e, zfe)
+    zref = np.zeros((ne, ne), np.complex128)
+    np.add.at(zref.T, e, zrow.T)
+    assert rel_err(Z.cpu().numpy(), zref) < TOL32
+
+
+def test_zmat_rwg_edges_ka10_L5_row_windows_vs_oracle(pkg, cuda, oracle):
+    """The bench workload itself (icosphere L5, F = 20480, E = 30720, ka = 10): the whole Z,
+    then the Z rows of three windows of 16 faces (the children of one level-3 face, 18 interior
+    edges each) against the oracle's face-edge rows."""
+    v, f, a, n, fei, ne, rules = _ico_setup(pkg, cuda, 5)
+    k = 10.0
+    er = pkg.mesh_MOM_3d.edge_rows(fei, f.shape[0], ne)
+    Z = pkg.mesh_MOM_3d.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, k, order="edges", edge_rows_map=er)
+    torch.cuda.synchronize()
+    er2 = er[:-1].cpu().numpy().reshape(ne, 2).astype(np.int64)
+    e = fei.cpu().numpy().reshape(-1).astype(np.int64)
+    h = lambda t: t.cpu().double().numpy()  # noqa: E731
+    vh, fh, ah, nh = h(v), f.cpu().numpy(), h(a), h(n)
+    rh = [h(t) for t in rules]
+    nf = f.shape[0]
+    compared = 0
+    for f0 in (0, nf // 2 + 96, nf - 16):
+        r0, r1 = 3 * f0, 3 * (f0 + 16)
+        # Z rows whose two face-edge rows both lie in the window
+        m = np.nonzero((er2[:, 0] >= r0) & (er2[:, 1] >= r0) & (er2[:, 0] < r1) & (er2[:, 1] < r1))[0]
+        assert m.size >= 16
+        zfe = oracle.mom_zmat_fe(vh, fh, ah, nh, *rh, k, rows=(r0, r1))
+        ref = _scatter_rows(zfe, er2[m, 0] - r0, e, ne) + _scatter_rows(zfe, er2[m, 1] - r0, e, ne)
+        got = Z[torch.as_tensor(m, device=cuda)].cpu().numpy()
+        assert rel_err(got, ref) < TOL32, f0
+        compared += m.size
+    assert compared >= 48
+
+
+# ---- the reference's own call sites ---------------------------------------------------------
+
+def _check_zfe(z, g, gq):
+    if f"mom_gq{gq}_zfe" in g:
+        assert rel_err(z, g[f"mom_gq{gq}_zfe"]) < TOL64
+    else:
+        ref_rows = g[f"mom_gq{gq}_zfe_rows"]
+        assert rel_err(z[: ref_rows.shape[0]], ref_rows) < TOL64
+    assert abs(np.linalg.norm(z) / float(g[f"mom_gq{gq}_zfe_fro"]) - 1) < TOL64
+
+
+@pytest.mark.parametrize("name", ["ico0", "ell1"])
+def test_kernel_functions_apply_match_reference(pkg, cuda, golden, name):
+    """MeshMOM{Zmat,Rhs,InterpolateJs}Kernel.apply -- the only way the reference reaches its
+    kernels (src/mesh_BEM/kernel_functions.py:26-171) -- against the reference's results."""
+    g = golden[name]
+    v, f, a, n = _dev_mesh(g, cuda, torch.float64)
+    px, wx, py, wy = _rules(pkg, 4, cuda, torch.float64)
+    KF = pkg.kernel_functions
+    k = float(g["mom_gq4_k"])
+    nf = f.shape[0]
+    Z = KF.MeshMOMZmatKernel.apply(v, f, a, n, px, wx, py, wy, k)
+    assert Z.shape == (1, 3 * nf, 3 * nf) and Z.dtype == torch.complex128
+    _check_zfe(Z[0].cpu().numpy(), g, 4)
+    R = KF.MeshMOMRhsKernel.apply(v, f, a, n, px, wx, k)
+    assert R.shape == (1, nf, 3, 1) and R.dtype == torch.complex128
+    assert rel_err(R[0, :, :, 0].cpu().numpy(), g["mom_gq4_rhsfe"]) < TOL64
+    fei = torch.tensor(g["face_edge_indices"], dtype=torch.int32, device=cuda)
+    ic = torch.tensor(g["mom_gq4_icoeff"], device=cuda)
+    J = KF.MeshMOMInterpolateJsKernel.apply(v, f, fei, a, ic)
+    assert J.shape == (1, 3 * nf, 3) and J.dtype == torch.complex128
+    assert rel_err(J.cpu().numpy(), g["mom_gq4_face_vert_js"]) < TOL64
+
+
+def test_kernel_functions_float32_close_to_reference(pkg, cuda, golden):
+    """The demo's dtype (float32): the same wrappers within the FP32 tolerance."""
+    g = golden["ell1"]
+    v, f, a, n = _dev_mesh(g, cuda, torch.float32)
+    px, wx, py, wy = _rules(pkg, 4, cuda, torch.float32)
+    KF = pkg.kernel_functions
+    k = float(g["mom_gq4_k"])
+    Z = KF.MeshMOMZmatKernel.apply(v, f, a, n, px, wx, py, wy, k)
+    assert Z.dtype == torch.complex64
+    ref_rows = g["mom_gq4_zfe_rows"]
+    assert rel_err(Z[0, : ref_rows.shape[0]].cpu().numpy(), ref_rows) < TOL32
+    R = KF.MeshMOMRhsKernel.apply(v, f, a, n, px, wx, k)
+    assert rel_err(R[0, :, :, 0].cpu().numpy(), g["mom_gq4_rhsfe"]) < TOL32
+
+
+def test_torch_ops_mesh_MOM_3d_match_reference(pkg, cuda, golden):
+    """torch.ops.mesh_MOM_3d.* (TORCH_LIBRARY(mesh_MOM_3d), mesh_MOM_3d.cpp:117-121) after
+    register_torch_ops(): the three ops write their outputs in place like the reference's."""
+    lib = pkg.mesh_MOM_3d.register_torch_ops()
+    assert pkg.mesh_MOM_3d.register_torch_ops() is lib  # registering twice is a no-op
+    ops = torch.ops.mesh_MOM_3d
+    g = golden["ico0"]
+    v, f, a, n = _dev_mesh(g, cuda, torch.float64)
+    px, wx, py, wy = _rules(pkg, 4, cuda, torch.float64)
+    k = float(g["mom_gq4_k"])
+    nf = f.shape[0]
+    zr = torch.zeros((1, 3 * nf, 3 * nf), dtype=torch.float64, device=cuda)
+    zi = torch.zeros_like(zr)
+    ops.create_MOM_Zmat_3d_forward(v, f, a, n, px, wx, py, wy, zr, zi, k)
+    _check_zfe((zr + 1j * zi)[0].cpu().numpy(), g, 4)
+    rr = torch.zeros((1, nf, 3, 1), dtype=torch.float64, device=cuda)
+    ri = torch.zeros_like(rr)
+    ops.create_MOM_rhs_3d_forward(v, f, a, n, px, wx, rr, ri, k)
+    assert rel_err((rr + 1j * ri)[0, :, :, 0].cpu().numpy(), g["mom_gq4_rhsfe"]) < TOL64
+    fei = torch.tensor(g["face_edge_indices"], dtype=torch.int32, device=cuda)
+    ic = torch.tensor(g["mom_gq4_icoeff"], device=cuda)
+    jr = torch.zeros((1, 3 * nf, 3), dtype=torch.float64, device=cuda)
+    ji = torch.zeros_like(jr)
+    ops.interpolate_Icoeff_to_Js_3d_forward(v, f, fei, a, ic.real.contiguous(), ic.imag.contiguous(), jr, ji)
+    assert rel_err((jr + 1j * ji).cpu().numpy(), g["mom_gq4_face_vert_js"]) < TOL64

@@ -50,13 +50,10 @@ def _p(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
-def test_noalloc_gmres_matches_workspace_gmres_twice(pkg, cuda):
-    lib = _lib(pkg)
-    Z, b = _system(pkg, cuda)
+def _solve_both(lib, pkg, cuda, Z, b, restart, max_iters=3000, tol=1e-9):
+    """Solve once with the workspace entry point and once with the allocation-free one."""
     n = Z.shape[0]
-    restart, max_iters, tol = 50, 3000, 1e-9
     stream = ctypes.c_void_p(torch.cuda.current_stream(cuda).cuda_stream)
-
     ws = torch.empty(lib.mb_gmres_workspace_bytes(n, restart), dtype=torch.uint8, device=cuda)
     x_ref = torch.zeros(n, dtype=torch.complex128, device=cuda)
     info_ref = pkg._lib.GmresInfo()
@@ -64,15 +61,38 @@ def test_noalloc_gmres_matches_workspace_gmres_twice(pkg, cuda):
                           ctypes.byref(info_ref), stream)
     assert rc == 0, lib.mb_last_error()
     assert info_ref.status == 0
+    x = torch.zeros(n, dtype=torch.complex128, device=cuda)
+    info = pkg._lib.GmresInfo()
+    rc = lib.mb_gmres_c64_noalloc(_p(Z), n, _p(b), _p(x), restart, max_iters, tol, ctypes.byref(info), stream)
+    assert rc == 0, lib.mb_last_error()
+    assert info.status == 0 and info.rel_residual <= tol
+    return x, x_ref
 
+
+def test_noalloc_gmres_matches_workspace_gmres_twice(pkg, cuda):
+    lib = _lib(pkg)
+    Z, b = _system(pkg, cuda)
     for _ in range(2):
-        x = torch.zeros(n, dtype=torch.complex128, device=cuda)
-        info = pkg._lib.GmresInfo()
-        rc = lib.mb_gmres_c64_noalloc(_p(Z), n, _p(b), _p(x), restart, max_iters, tol,
-                                      ctypes.byref(info), stream)
-        assert rc == 0, lib.mb_last_error()
-        assert info.status == 0 and info.rel_residual <= tol
+        x, x_ref = _solve_both(lib, pkg, cuda, Z, b, restart=50)
         assert rel_err(x.cpu().numpy(), x_ref.cpu().numpy()) < TOL
+
+
+def test_noalloc_gmres_smaller_system_after_larger(pkg, cuda):
+    """The scratch keeps the previous call's contents, and the offsets of the solver's arrays
+    inside it move with n and the restart length: a smaller, odd-sized system with a shorter
+    restart right after a larger one must not read the larger call's leftovers."""
+    lib = _lib(pkg)
+    Z, b = _system(pkg, cuda)
+    x, x_ref = _solve_both(lib, pkg, cuda, Z, b, restart=50)
+    assert rel_err(x.cpu().numpy(), x_ref.cpu().numpy()) < TOL
+    n2 = 97  # odd; a leading principal block of the Galerkin matrix is itself a Galerkin matrix
+    Z2 = Z[:n2, :n2].contiguous()
+    b2 = b[:n2].contiguous()
+    x2, x2_ref = _solve_both(lib, pkg, cuda, Z2, b2, restart=13)
+    assert rel_err(x2.cpu().numpy(), x2_ref.cpu().numpy()) < TOL
+    # and back to the larger system
+    x3, x3_ref = _solve_both(lib, pkg, cuda, Z, b, restart=31)
+    assert rel_err(x3.cpu().numpy(), x3_ref.cpu().numpy()) < TOL
 
 
 def test_noalloc_gmres_rejects_sizes_beyond_its_limits(pkg, cuda):
