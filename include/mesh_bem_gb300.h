@@ -452,6 +452,53 @@ int mb_matvec_c64(const float* z, const float* v, int64_t n, double* y, void* st
 int mb_residual_c128(const float* z, const double* x, const double* b, int64_t n, double* r,
                      void* stream);
 
+/* ---- Near-field preconditioner and preconditioned solve (no counterpart in the reference,
+ * which factors Z densely with torch.linalg.solve, mesh_BEM_solver_3d.py:174) ------------
+ * Sparse approximate inverse M of the RWG matrix, the right preconditioner of
+ * mb_pgmres_*: column j of M minimises ||Z[I_j, J_j] m - e_j|| with J_j the edges of the
+ * faces sharing a vertex with a face of edge j and I_j the edges of the faces sharing a
+ * vertex with those (least squares by Householder QR in FP32, one block per edge).  M is
+ * stored as rows of MB_SPAI_WIDTH (local column, complex64 value) pairs, m_cols [E,
+ * MB_SPAI_WIDTH] int32 (a row ends at its first -1) and m_vals [E, MB_SPAI_WIDTH]
+ * interleaved complex64.  Several meshes at once: desc [n_mesh, 6] int64 = (first face,
+ * faces, first edge, edges, offset of Z_i in complex entries, row pitch of Z_i); faces
+ * [total_faces, 3] (global vertex ids), fei [total_faces, 3] local edge ids, near_pairs
+ * [n_near, 2] (global face ids, sorted by first face; mb_shared_vertex_pairs_*), z the
+ * complex64 matrix (blocks).  For one mesh: desc = {0, F, 0, E, 0, E}.  Patterns above
+ * MB_SPAI_WIDTH columns or 128 rows keep the edges nearest to edge j.  Workspace:
+ * mb_spai_workspace_bytes(total_edges) bytes.  mb_spai_status copies the build's status word
+ * into *status (host or device memory; synchronises the stream): bit 0 a pattern was cut
+ * to its cap, bit 1 a least-squares block without full column rank, bit 2 a face-edge map
+ * with an out-of-range id or an edge without faces or with more than two. */
+#define MB_SPAI_WIDTH 48
+size_t mb_spai_workspace_bytes(int64_t total_edges);
+int mb_spai_build_c64(const float* verts, const int32_t* faces, const int32_t* fei, const int64_t* desc, int n_mesh,
+                      int64_t total_faces, int64_t total_edges, const int32_t* near_pairs, int64_t n_near,
+                      const float* z, int32_t* m_cols, float* m_vals, void* workspace, size_t workspace_bytes,
+                      void* stream);
+int mb_spai_status(const void* workspace, int64_t total_edges, int32_t* status, void* stream);
+/* y = M v for one mesh (complex64 v, y [n]). */
+int mb_spai_apply_c64(const int32_t* m_cols, const float* m_vals, int64_t n, const float* v, float* y,
+                      void* stream);
+
+/* GMRES(restart) on Z x = b with the right preconditioner M (m_cols / m_vals from
+ * mb_spai_build_c64, or both NULL for none): each restart cycle starts from the FP64 residual
+ * b - Z x, solves (Z M) u = r and adds M u to x.  The whole cycle runs on the device (CGS2
+ * Arnoldi on a complex128 basis, Givens rotations, the residual estimate and the back
+ * substitution in kernels; deterministic block reductions); use_graph = 1 captures it once as
+ * a CUDA graph and replays it.  The host reads the solver state once per cycle.
+ * mb_pgmres_c64: Z interleaved complex64 [n, n], FP32 products; mb_pgmres_c128: Z
+ * interleaved complex128, FP64 products.  b, x complex128 [n], 16-byte aligned (x: initial
+ * guess in, solution out).  info as for mb_gmres_c64.  Workspace:
+ * mb_pgmres_workspace_bytes(n, restart) bytes. */
+size_t mb_pgmres_workspace_bytes(int64_t n, int restart);
+int mb_pgmres_c64(const float* z, int64_t n, const int32_t* m_cols, const float* m_vals, const double* b, double* x,
+                  int restart, int max_iters, double tol, int use_graph, void* workspace, size_t workspace_bytes,
+                  mb_gmres_info* info, void* stream);
+int mb_pgmres_c128(const double* z, int64_t n, const int32_t* m_cols, const float* m_vals, const double* b,
+                   double* x, int restart, int max_iters, double tol, int use_graph, void* workspace,
+                   size_t workspace_bytes, mb_gmres_info* info, void* stream);
+
 /* ---- Laplace / Helmholtz-BEM layers ------------------------------------------------- */
 
 /* Replaces double_integration_on_panels_3d (src/mesh_BEM/utils/integrations_3d.py:252-452).

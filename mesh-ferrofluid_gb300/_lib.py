@@ -109,13 +109,21 @@ _SIGS = {
     "mb_gmres_c64_noalloc": [_P, _I64, _P, _P, _I, _I, _D, _P, _P],
     "mb_matvec_c64": [_P, _P, _I64, _P, _P],
     "mb_residual_c128": [_P, _P, _P, _I64, _P, _P],
+    "mb_spai_workspace_bytes": [_I64],
+    "mb_spai_build_c64": [_P, _P, _P, _P, _I, _I64, _I64, _P, _I64, _P, _P, _P, _P, ctypes.c_size_t, _P],
+    "mb_spai_status": [_P, _I64, _P, _P],
+    "mb_spai_apply_c64": [_P, _P, _I64, _P, _P, _P],
+    "mb_pgmres_workspace_bytes": [_I64, _I],
+    "mb_pgmres_c64": [_P, _I64, _P, _P, _P, _P, _I, _I, _D, _I, _P, ctypes.c_size_t, _P, _P],
+    "mb_pgmres_c128": [_P, _I64, _P, _P, _P, _P, _I, _I, _D, _I, _P, ctypes.c_size_t, _P, _P],
 }
 
 _RESTYPES = {"mb_gmres_workspace_bytes": ctypes.c_size_t, "mb_ray_bvh_bytes": ctypes.c_size_t,
              "mb_gmres_real_workspace_bytes": ctypes.c_size_t, "mb_cgemm_workspace_bytes": ctypes.c_size_t,
              "mb_gmres_multi_workspace_bytes": ctypes.c_size_t,
              "mb_gmres_blockdiag_workspace_bytes": ctypes.c_size_t,
-             "mb_shared_vertex_pairs_workspace_bytes": ctypes.c_int64}
+             "mb_shared_vertex_pairs_workspace_bytes": ctypes.c_int64,
+             "mb_spai_workspace_bytes": ctypes.c_size_t, "mb_pgmres_workspace_bytes": ctypes.c_size_t}
 
 
 class GmresInfo(ctypes.Structure):

@@ -138,6 +138,16 @@ template <typename T>
 int launch_radiate_h(const T*, int64_t, const T*, const T*, const T*, int64_t, double, T*, cudaStream_t);
 int gmres_c64(const float*, int64_t, const double*, double*, int, int, double, void*, size_t, int64_t*,
               int64_t*, double*, int*, cudaStream_t);
+size_t spai_workspace_bytes(int64_t total_edges);
+int spai_build(const float* verts, const int32_t* faces, const int32_t* fei, const int64_t* desc, int n_mesh,
+               int64_t total_faces, int64_t total_edges, const int32_t* pairs, int64_t n_pairs, const float* z,
+               int32_t* m_cols, float* m_vals, void* ws, size_t ws_bytes, cudaStream_t s);
+int spai_status(const void* ws, int64_t total_edges, int32_t* out, cudaStream_t s);
+int spai_apply_c64(const int32_t* m_cols, const float* m_vals, int64_t n, const float* v, float* y, cudaStream_t s);
+size_t pgmres_workspace_bytes(int64_t n, int m);
+int pgmres(int kind, const void* z, int64_t n, const int32_t* m_cols, const float* m_vals, const double* b,
+           double* x, int m, int max_iters, double tol, bool use_graph, void* workspace, size_t ws_bytes,
+           int64_t* iters_out, int64_t* cycles_out, double* relres_out, int* status_out, cudaStream_t s);
 int gmres_c64_noalloc(const float*, int64_t, const double*, double*, int, int, double, int64_t*, int64_t*,
                       double*, int*, cudaStream_t);
 int launch_matvec_c64(const float*, const float*, int64_t, double*, cudaStream_t);
@@ -847,6 +857,65 @@ int mb_residual_c128(const float* z, const double* x, const double* b, int64_t n
     if (n == 0) return MB_OK;
     MB_REQUIRE(z && x && b && r, "null pointer argument");
     return launch_residual_c128(z, x, b, n, r, as_stream(stream));
+}
+
+size_t mb_spai_workspace_bytes(int64_t total_edges) { return total_edges > 0 ? spai_workspace_bytes(total_edges) : 0; }
+
+int mb_spai_build_c64(const float* verts, const int32_t* faces, const int32_t* fei, const int64_t* desc, int n_mesh,
+                      int64_t total_faces, int64_t total_edges, const int32_t* near_pairs, int64_t n_near,
+                      const float* z, int32_t* m_cols, float* m_vals, void* workspace, size_t workspace_bytes,
+                      void* stream) {
+    return spai_build(verts, faces, fei, desc, n_mesh, total_faces, total_edges, near_pairs, n_near, z, m_cols,
+                      m_vals, workspace, workspace_bytes, as_stream(stream));
+}
+
+int mb_spai_status(const void* workspace, int64_t total_edges, int32_t* status, void* stream) {
+    MB_REQUIRE(workspace && status && total_edges > 0, "bad arguments");
+    return spai_status(workspace, total_edges, status, as_stream(stream));
+}
+
+int mb_spai_apply_c64(const int32_t* m_cols, const float* m_vals, int64_t n, const float* v, float* y,
+                      void* stream) {
+    MB_REQUIRE(n >= 0, "bad sizes");
+    if (n == 0) return MB_OK;
+    MB_REQUIRE(m_cols && m_vals && v && y, "null pointer argument");
+    return spai_apply_c64(m_cols, m_vals, n, v, y, as_stream(stream));
+}
+
+size_t mb_pgmres_workspace_bytes(int64_t n, int restart) {
+    return (n > 0 && restart > 0) ? pgmres_workspace_bytes(n, restart) : 0;
+}
+
+static int pgmres_entry(int kind, const void* z, int64_t n, const int32_t* m_cols, const float* m_vals,
+                        const double* b, double* x, int restart, int max_iters, double tol, int use_graph,
+                        void* workspace, size_t workspace_bytes, mb_gmres_info* info, void* stream) {
+    int64_t it = 0, cyc = 0;
+    double rr = 0.0;
+    int st = 1;
+    const int rc = pgmres(kind, z, n, m_cols, m_vals, b, x, restart, max_iters, tol, use_graph != 0, workspace,
+                          workspace_bytes, &it, &cyc, &rr, &st, as_stream(stream));
+    if (rc == MB_OK && info) {
+        info->iterations = it;
+        info->restarts = cyc;
+        info->rel_residual = rr;
+        info->status = st;
+        info->reserved = 0;
+    }
+    return rc;
+}
+
+int mb_pgmres_c64(const float* z, int64_t n, const int32_t* m_cols, const float* m_vals, const double* b, double* x,
+                  int restart, int max_iters, double tol, int use_graph, void* workspace, size_t workspace_bytes,
+                  mb_gmres_info* info, void* stream) {
+    return pgmres_entry(0, z, n, m_cols, m_vals, b, x, restart, max_iters, tol, use_graph, workspace,
+                        workspace_bytes, info, stream);
+}
+
+int mb_pgmres_c128(const double* z, int64_t n, const int32_t* m_cols, const float* m_vals, const double* b,
+                   double* x, int restart, int max_iters, double tol, int use_graph, void* workspace,
+                   size_t workspace_bytes, mb_gmres_info* info, void* stream) {
+    return pgmres_entry(1, z, n, m_cols, m_vals, b, x, restart, max_iters, tol, use_graph, workspace,
+                        workspace_bytes, info, stream);
 }
 
 int mb_panel_relation(const int32_t* faces, int64_t n_faces, uint8_t* relations, void* stream) {

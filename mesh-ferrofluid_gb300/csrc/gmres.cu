@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "spai_apply.cuh"
 
 namespace mb {
 
@@ -44,12 +45,15 @@ __device__ __forceinline__ double warp_sum(double v) {
 // One warp per row; lane l reads float4 (two complex) at 16-byte granularity when both the
 // Z row and v start on a 16-byte boundary, else one complex at a time (v may be an
 // 8-byte-aligned view such as X[1:n+1] of a complex64 array).
+// `active` (may be null): a device flag of the preconditioned solver; 0 makes the launch a
+// no-op (a step of a captured restart cycle after the cycle has ended).
 __global__ void __launch_bounds__(256) matvec_c64_kernel(const float* __restrict__ z,
                                                          const float* __restrict__ v, int64_t n,
-                                                         double* __restrict__ y) {
+                                                         double* __restrict__ y,
+                                                         const int* __restrict__ active = nullptr) {
     const int64_t row = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
-    if (row >= n) return;
+    if (row >= n || (active && !*active)) return;
     const float* zr = z + 2 * row * n;
     float ar = 0.f, ai = 0.f;
     const int64_t npair = n >> 1;  // float4 = two complex numbers
@@ -652,6 +656,523 @@ int launch_residual_c128(const float* z, const double* x, const double* b, int64
     if (n <= 0) return MB_OK;
     residual_c128_kernel<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(z, x, b, n, r);
     return check_launch("residual_c128");
+}
+
+// ---------------------------------------------------------------------------------------
+// Preconditioned GMRES(m) with the whole restart cycle on the device.
+//
+// Right preconditioning with the sparse approximate inverse M (spai.cu): each cycle solves
+// (Z M) u = r0 and updates x += M u, so the residual GMRES minimises is the residual of
+// Z x = b itself.  Arnoldi by CGS2 on a complex128 basis with FP64 sums; the Givens
+// rotations, the residual estimate, the stopping test and the back substitution run in
+// single-thread kernels on a device state record; every cycle starts from the FP64 residual
+// b - Z x (iterative refinement).  Sums over the vector run as fixed-size block partials
+// that the last block to finish adds in a fixed order (deterministic, no FP64 atomics).
+// A cycle is a fixed sequence of launches: once the state says the cycle has ended, the
+// remaining steps' launches return at once.  With use_graph the cycle is captured once
+// as a CUDA graph and replayed; the host reads the state once per cycle.
+// Z is complex64 (FP32 products, the solver of the FP32 path) or complex128 (FP64 products:
+// the FP64 reference solution of the same discretisation).
+// ---------------------------------------------------------------------------------------
+constexpr int kPgMaxBlocks = 256;
+
+struct PgState {
+    double bn2, bnorm, rn2, beta, relres, tol, hn2, hn;
+    long long iters, max_iters, cycles;
+    int m, jdone, active, converged;
+    unsigned int cnt;
+    int pad;
+};
+
+struct PgWork {
+    double2* V;     // [(m+1), n]
+    double2* w;     // [n]
+    double2* r;     // [n] residual, then the cycle's update V y
+    double2* z;     // [n] M v (float2 view for the FP32 product)
+    double2* part;  // [blocks, m+1] block partials
+    double* npart;  // [blocks]
+    PgState* st;
+    double2* g;     // [m+1]
+    double2* cs;    // [m]
+    double2* sn;    // [m]
+    double2* H;     // [m, m+1], column j at H[j (m+1) + i]
+    double2* y;     // [m]
+    double2* h1;    // [m+1] pass-1 projections
+    double2* h2;    // [m+1] pass-2 projections
+};
+
+static size_t pg_state_bytes(int m) { return al256(sizeof(PgState) + 16 * (size_t)(5 * m + 3 + m * (m + 1))); }
+
+size_t pgmres_workspace_bytes(int64_t n, int m) {
+    return al256(16 * (size_t)(m + 1) * n) + 3 * al256(16 * (size_t)n) + al256(16 * (size_t)kPgMaxBlocks * (m + 1)) +
+           al256(8 * (size_t)kPgMaxBlocks) + pg_state_bytes(m);
+}
+
+static PgWork pg_carve(void* ws, int64_t n, int m) {
+    char* p = static_cast<char*>(ws);
+    PgWork w;
+    w.V = reinterpret_cast<double2*>(p);
+    p += al256(16 * (size_t)(m + 1) * n);
+    w.w = reinterpret_cast<double2*>(p);
+    p += al256(16 * (size_t)n);
+    w.r = reinterpret_cast<double2*>(p);
+    p += al256(16 * (size_t)n);
+    w.z = reinterpret_cast<double2*>(p);
+    p += al256(16 * (size_t)n);
+    w.part = reinterpret_cast<double2*>(p);
+    p += al256(16 * (size_t)kPgMaxBlocks * (m + 1));
+    w.npart = reinterpret_cast<double*>(p);
+    p += al256(8 * (size_t)kPgMaxBlocks);
+    w.st = reinterpret_cast<PgState*>(p);
+    double2* a = reinterpret_cast<double2*>(p + ((sizeof(PgState) + 15) & ~size_t(15)));
+    w.g = a;
+    a += m + 1;
+    w.cs = a;
+    a += m;
+    w.sn = a;
+    a += m;
+    w.H = a;
+    a += (size_t)m * (m + 1);
+    w.y = a;
+    a += m;
+    w.h1 = a;
+    a += m + 1;
+    w.h2 = a;
+    return w;
+}
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cconjmul(double2 a, double2 b) {  // conj(a) b
+    return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ double cabs2(double2 a) { return a.x * a.x + a.y * a.y; }
+
+// Adds the blocks' partials npart[0..gridDim.x) in a fixed order into *out once every block
+// has written its own; the counter is left at zero for the next launch.
+__device__ __forceinline__ void pg_last_block_sum(double* npart, unsigned* cnt, double* out) {
+    __shared__ bool s_last;
+    __threadfence();
+    if (threadIdx.x == 0) s_last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (s_last && threadIdx.x < 32) {
+        double a = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) a += __ldcg(npart + b);
+        a = warp_sum(a);
+        if (threadIdx.x == 0) {
+            *out = a;
+            *cnt = 0;
+        }
+    }
+}
+
+// *out = sum |v_k|^2 (FP64).  active may be null.
+__global__ void __launch_bounds__(256) pg_norm2_kernel(const double2* __restrict__ v, int64_t n,
+                                                      double* __restrict__ npart, unsigned* cnt, double* out,
+                                                      const int* __restrict__ active) {
+    if (active && !*active) return;
+    __shared__ double s[8];
+    double a = 0.0;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        a += cabs2(v[k]);
+    a = warp_sum(a);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < 8; ++q) t += s[q];
+        npart[blockIdx.x] = t;
+    }
+    pg_last_block_sum(npart, cnt, out);
+}
+
+__global__ void pg_init_kernel(PgState* st, double tol, long long max_iters, int m) {
+    const double b = sqrt(st->bn2);
+    st->bnorm = b > 0.0 ? b : 1.0;
+    st->tol = tol;
+    st->max_iters = max_iters;
+    st->m = m;
+    st->iters = 0;
+    st->cycles = 0;
+    st->converged = 0;
+    st->active = 0;
+    st->jdone = 0;
+    st->relres = 0.0;
+}
+
+__global__ void pg_cycle_start_kernel(PgState* st, double2* g) {
+    const double beta = sqrt(st->rn2);
+    st->beta = beta;
+    st->relres = beta / st->bnorm;
+    st->jdone = 0;
+    st->active = 0;
+    if (st->relres <= st->tol) {
+        st->converged = 1;
+        return;
+    }
+    if (st->iters >= st->max_iters || !(beta > 0.0)) return;
+    st->active = 1;
+    st->cycles += 1;
+    g[0] = make_double2(beta, 0.0);
+    for (int i = 1; i <= st->m; ++i) g[i] = make_double2(0.0, 0.0);
+}
+
+// dst = src * s, s = 1 / beta (which = 0) or 1 / h_{j+1,j} (which = 1); only while active
+__global__ void pg_scale_kernel(const double2* __restrict__ src, int64_t n, const PgState* __restrict__ st, int which,
+                                double2* __restrict__ dst) {
+    if (!st->active) return;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double s = 1.0 / (which ? st->hn : st->beta);
+    const double2 v = src[k];
+    dst[k] = make_double2(v.x * s, v.y * s);
+}
+
+// z = M v: complex64 output (FP32 product path, F32 = true) or complex128 (FP64 path)
+template <bool F32>
+__global__ void pg_precond_kernel(const int32_t* __restrict__ cols, const float2* __restrict__ vals, int64_t n,
+                                  const double2* __restrict__ v, double2* __restrict__ z,
+                                  const PgState* __restrict__ st) {
+    if (!st->active) return;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (F32) {
+        float2 o;
+        if (cols) {
+            o = spai_row_f32(cols, vals, i, v);
+        } else {
+            const double2 x = v[i];
+            o = make_float2((float)x.x, (float)x.y);
+        }
+        reinterpret_cast<float2*>(z)[i] = o;
+    } else {
+        z[i] = cols ? spai_row_f64(cols, vals, i, v) : v[i];
+    }
+}
+
+// y = Z v in FP64 with Z complex128 [n, n]; one warp per row
+__global__ void __launch_bounds__(256) matvec_z128_kernel(const double2* __restrict__ z,
+                                                          const double2* __restrict__ v, int64_t n,
+                                                          double2* __restrict__ y, const int* __restrict__ active) {
+    const int64_t row = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n || (active && !*active)) return;
+    const double2* zr = z + row * n;
+    double ar = 0.0, ai = 0.0;
+    int64_t j = lane;
+    for (; j + 32 < n; j += 64) {
+        const double2 a0 = __ldcs(zr + j), a1 = __ldcs(zr + j + 32);
+        const double2 b0 = __ldg(v + j), b1 = __ldg(v + j + 32);
+        ar = fma(a0.x, b0.x, fma(-a0.y, b0.y, ar));
+        ai = fma(a0.x, b0.y, fma(a0.y, b0.x, ai));
+        ar = fma(a1.x, b1.x, fma(-a1.y, b1.y, ar));
+        ai = fma(a1.x, b1.y, fma(a1.y, b1.x, ai));
+    }
+    for (; j < n; j += 32) {
+        const double2 a0 = __ldcs(zr + j), b0 = __ldg(v + j);
+        ar = fma(a0.x, b0.x, fma(-a0.y, b0.y, ar));
+        ai = fma(a0.x, b0.y, fma(a0.y, b0.x, ai));
+    }
+    ar = warp_sum(ar);
+    ai = warp_sum(ai);
+    if (lane == 0) y[row] = make_double2(ar, ai);
+}
+
+// r = b - Z x, Z complex128
+__global__ void __launch_bounds__(256) residual_z128_kernel(const double2* __restrict__ z,
+                                                            const double2* __restrict__ x,
+                                                            const double2* __restrict__ b, int64_t n,
+                                                            double2* __restrict__ r) {
+    const int64_t row = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    const double2* zr = z + row * n;
+    double ar = 0.0, ai = 0.0;
+    for (int64_t j = lane; j < n; j += 32) {
+        const double2 a = __ldcs(zr + j), v = __ldg(x + j);
+        ar = fma(a.x, v.x, fma(-a.y, v.y, ar));
+        ai = fma(a.x, v.y, fma(a.y, v.x, ai));
+    }
+    ar = warp_sum(ar);
+    ai = warp_sum(ai);
+    if (lane == 0) r[row] = make_double2(b[row].x - ar, b[row].y - ai);
+}
+
+// h[i] = sum_k conj(V_i[k]) w[k], i < nb: block partials, then the last block's fixed-order sum
+__global__ void __launch_bounds__(256) pg_dots_kernel(const double2* __restrict__ V, const double2* __restrict__ w,
+                                                      int64_t n, int nb, double2* __restrict__ part, int ldp,
+                                                      unsigned* cnt, double2* __restrict__ h,
+                                                      const int* __restrict__ active) {
+    if (!*active) return;
+    __shared__ double2 s[kGmresMaxRestart + 1][8];
+    __shared__ bool s_last;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double2 wk = make_double2(0.0, 0.0);
+    const bool single = k0 + stride >= n;  // one element per thread (the common case)
+    if (single && k0 < n) wk = w[k0];
+    for (int i = 0; i < nb; ++i) {
+        const double2* vi = V + (int64_t)i * n;
+        double ar = 0.0, ai = 0.0;
+        if (single) {
+            if (k0 < n) {
+                const double2 p = cconjmul(vi[k0], wk);
+                ar = p.x;
+                ai = p.y;
+            }
+        } else {
+            for (int64_t k = k0; k < n; k += stride) {
+                const double2 p = cconjmul(vi[k], w[k]);
+                ar += p.x;
+                ai += p.y;
+            }
+        }
+        ar = warp_sum(ar);
+        ai = warp_sum(ai);
+        if (lane == 0) s[i][warp] = make_double2(ar, ai);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        double sr = 0.0, si = 0.0;
+        for (int q = 0; q < 8; ++q) {
+            sr += s[i][q].x;
+            si += s[i][q].y;
+        }
+        part[(int64_t)blockIdx.x * ldp + i] = make_double2(sr, si);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        double sr = 0.0, si = 0.0;
+        for (int b = 0; b < (int)gridDim.x; ++b) {
+            const double2 p = __ldcg(part + (int64_t)b * ldp + i);
+            sr += p.x;
+            si += p.y;
+        }
+        h[i] = make_double2(sr, si);
+    }
+    if (threadIdx.x == 0) *cnt = 0;
+}
+
+// w -= sum_{i<nb} V_i h_i; with npart, also |w|^2 into *hn2 (block partials + last block)
+__global__ void __launch_bounds__(256) pg_sub_kernel(const double2* __restrict__ V, const double2* __restrict__ h,
+                                                     int64_t n, int nb, double2* __restrict__ w,
+                                                     double* __restrict__ npart, unsigned* cnt, double* hn2,
+                                                     const int* __restrict__ active) {
+    if (!*active) return;
+    __shared__ double2 sh[kGmresMaxRestart + 1];
+    __shared__ double s[8];
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = h[i];
+    __syncthreads();
+    double a = 0.0;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        double2 x = w[k];
+        for (int i = 0; i < nb; ++i) {
+            const double2 p = cmul(V[(int64_t)i * n + k], sh[i]);
+            x.x -= p.x;
+            x.y -= p.y;
+        }
+        w[k] = x;
+        a += cabs2(x);
+    }
+    if (!npart) return;
+    a = warp_sum(a);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < 8; ++q) t += s[q];
+        npart[blockIdx.x] = t;
+    }
+    pg_last_block_sum(npart, cnt, hn2);
+}
+
+// One Arnoldi step's Hessenberg column: h = h1 + h2 and |w|; previous rotations, a new one,
+// the residual estimate and the end-of-cycle test.
+__global__ void pg_givens_kernel(PgState* st, double2* g, double2* cs, double2* sn, double2* H,
+                                 const double2* h1, const double2* h2, int j) {
+    if (!st->active) return;
+    const int m = st->m;
+    const double hn = sqrt(st->hn2);
+    st->hn = hn;
+    double2* col = H + (int64_t)j * (m + 1);
+    for (int i = 0; i <= j; ++i) col[i] = make_double2(h1[i].x + h2[i].x, h1[i].y + h2[i].y);
+    double2 below = make_double2(hn, 0.0);  // h[j+1]
+    for (int i = 0; i < j; ++i) {
+        const double2 a = col[i], b = col[i + 1];
+        // t = conj(cs) a + conj(sn) b; b' = -sn a + cs b
+        const double2 t1 = cconjmul(cs[i], a), t2 = cconjmul(sn[i], b);
+        const double2 u1 = cmul(sn[i], a), u2 = cmul(cs[i], b);
+        col[i] = make_double2(t1.x + t2.x, t1.y + t2.y);
+        col[i + 1] = make_double2(u2.x - u1.x, u2.y - u1.y);
+    }
+    const double a = sqrt(cabs2(col[j])), bb = hn;
+    const double rr = hypot(a, bb);
+    double2 c, sv;
+    if (rr == 0.0) {
+        c = make_double2(1.0, 0.0);
+        sv = make_double2(0.0, 0.0);
+    } else {
+        c = make_double2(col[j].x / rr, col[j].y / rr);
+        sv = make_double2(below.x / rr, below.y / rr);
+    }
+    cs[j] = c;
+    sn[j] = sv;
+    col[j] = make_double2(rr, 0.0);
+    const double2 gj = g[j];
+    const double2 ng = cmul(sv, gj);
+    g[j + 1] = make_double2(-ng.x, -ng.y);
+    g[j] = cconjmul(c, gj);
+    st->iters += 1;
+    st->jdone = j + 1;
+    const double est = sqrt(cabs2(g[j + 1])) / st->bnorm;
+    if (est <= 0.5 * st->tol || hn <= 1e-300 || st->iters >= st->max_iters || j + 1 == m) st->active = 0;
+}
+
+// y = R^{-1} g over the cycle's steps (R upper triangular in H)
+__global__ void pg_backsub_kernel(const PgState* st, const double2* H, const double2* g, double2* y) {
+    const int jd = st->jdone, m = st->m;
+    for (int i = jd - 1; i >= 0; --i) {
+        double2 acc = g[i];
+        for (int q = i + 1; q < jd; ++q) {
+            const double2 p = cmul(H[(int64_t)q * (m + 1) + i], y[q]);
+            acc.x -= p.x;
+            acc.y -= p.y;
+        }
+        const double2 d = H[(int64_t)i * (m + 1) + i];
+        const double dd = cabs2(d);
+        y[i] = make_double2((acc.x * d.x + acc.y * d.y) / dd, (acc.y * d.x - acc.x * d.y) / dd);
+    }
+}
+
+// u = sum_{i < jdone} V_i y_i
+__global__ void pg_combine_kernel(const double2* __restrict__ V, const double2* __restrict__ y,
+                                  const PgState* __restrict__ st, int64_t n, double2* __restrict__ u) {
+    const int jd = st->jdone;
+    if (jd == 0) return;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double2 a = make_double2(0.0, 0.0);
+    for (int i = 0; i < jd; ++i) {
+        const double2 p = cmul(V[(int64_t)i * n + k], y[i]);
+        a.x += p.x;
+        a.y += p.y;
+    }
+    u[k] = a;
+}
+
+// x += M u (FP64)
+__global__ void pg_update_kernel(const int32_t* __restrict__ cols, const float2* __restrict__ vals,
+                                 const double2* __restrict__ u, const PgState* __restrict__ st, int64_t n,
+                                 double2* __restrict__ x) {
+    if (st->jdone == 0) return;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double2 d = cols ? spai_row_f64(cols, vals, i, u) : u[i];
+    x[i] = make_double2(x[i].x + d.x, x[i].y + d.y);
+}
+
+// kind 0: Z complex64; kind 1: Z complex128
+static void pg_cycle(int kind, const void* z, int64_t n, const int32_t* cols, const float2* vals,
+                     const double2* b, double2* x, int m, const PgWork& W, unsigned* cnt, cudaStream_t s) {
+    const unsigned vb = (unsigned)((n + 255) / 256), rb = (unsigned)((n + 7) / 8);
+    const int nblk = (int)std::min<int64_t>(vb, kPgMaxBlocks);
+    const int* act = &W.st->active;
+    if (kind == 0)
+        residual_c128_kernel<<<rb, 256, 0, s>>>(static_cast<const float*>(z), reinterpret_cast<const double*>(x),
+                                                reinterpret_cast<const double*>(b), n, reinterpret_cast<double*>(W.r));
+    else
+        residual_z128_kernel<<<rb, 256, 0, s>>>(static_cast<const double2*>(z), x, b, n, W.r);
+    pg_norm2_kernel<<<nblk, 256, 0, s>>>(W.r, n, W.npart, cnt, &W.st->rn2, nullptr);
+    pg_cycle_start_kernel<<<1, 1, 0, s>>>(W.st, W.g);
+    pg_scale_kernel<<<vb, 256, 0, s>>>(W.r, n, W.st, 0, W.V);
+    for (int j = 0; j < m; ++j) {
+        const double2* vj = W.V + (int64_t)j * n;
+        if (kind == 0) {
+            pg_precond_kernel<true><<<vb, 256, 0, s>>>(cols, vals, n, vj, W.z, W.st);
+            matvec_c64_kernel<<<rb, 256, 0, s>>>(static_cast<const float*>(z), reinterpret_cast<const float*>(W.z), n,
+                                                 reinterpret_cast<double*>(W.w), act);
+        } else {
+            pg_precond_kernel<false><<<vb, 256, 0, s>>>(cols, vals, n, vj, W.z, W.st);
+            matvec_z128_kernel<<<rb, 256, 0, s>>>(static_cast<const double2*>(z), W.z, n, W.w, act);
+        }
+        pg_dots_kernel<<<nblk, 256, 0, s>>>(W.V, W.w, n, j + 1, W.part, m + 1, cnt, W.h1, act);
+        pg_sub_kernel<<<nblk, 256, 0, s>>>(W.V, W.h1, n, j + 1, W.w, nullptr, cnt, nullptr, act);
+        pg_dots_kernel<<<nblk, 256, 0, s>>>(W.V, W.w, n, j + 1, W.part, m + 1, cnt, W.h2, act);
+        pg_sub_kernel<<<nblk, 256, 0, s>>>(W.V, W.h2, n, j + 1, W.w, W.npart, cnt, &W.st->hn2, act);
+        pg_givens_kernel<<<1, 1, 0, s>>>(W.st, W.g, W.cs, W.sn, W.H, W.h1, W.h2, j);
+        pg_scale_kernel<<<vb, 256, 0, s>>>(W.w, n, W.st, 1, W.V + (int64_t)(j + 1) * n);
+    }
+    pg_backsub_kernel<<<1, 1, 0, s>>>(W.st, W.H, W.g, W.y);
+    pg_combine_kernel<<<vb, 256, 0, s>>>(W.V, W.y, W.st, n, W.r);
+    pg_update_kernel<<<vb, 256, 0, s>>>(cols, vals, W.r, W.st, n, x);
+}
+
+int pgmres(int kind, const void* z, int64_t n, const int32_t* m_cols, const float* m_vals, const double* b,
+           double* x, int m, int max_iters, double tol, bool use_graph, void* workspace, size_t ws_bytes,
+           int64_t* iters_out, int64_t* cycles_out, double* relres_out, int* status_out, cudaStream_t s) {
+    if (!z || !b || !x || !workspace) return set_error(MB_ERR_ARG, "pgmres: null pointer");
+    if (n <= 0) return set_error(MB_ERR_ARG, "n must be > 0");
+    if (m < 1 || m > kGmresMaxRestart) return set_error(MB_ERR_ARG, "restart must be in [1, %d]", kGmresMaxRestart);
+    if (max_iters < 1) return set_error(MB_ERR_ARG, "max_iters must be >= 1");
+    if (!(tol > 0)) return set_error(MB_ERR_ARG, "tol must be > 0");
+    if ((m_cols == nullptr) != (m_vals == nullptr)) return set_error(MB_ERR_ARG, "pgmres: give both m_cols and m_vals, or neither");
+    if (ws_bytes < pgmres_workspace_bytes(n, m)) return set_error(MB_ERR_ARG, "workspace too small");
+    if (((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(x)) & 15) != 0)
+        return set_error(MB_ERR_ARG, "pgmres: b and x must be 16-byte aligned");
+    PgWork W = pg_carve(workspace, n, m);
+    const unsigned vb = (unsigned)((n + 255) / 256);
+    const int nblk = (int)std::min<int64_t>(vb, kPgMaxBlocks);
+    const float2* vals = reinterpret_cast<const float2*>(m_vals);
+    const double2* b2 = reinterpret_cast<const double2*>(b);
+    double2* x2 = reinterpret_cast<double2*>(x);
+    unsigned* cnt = &W.st->cnt;
+    cudaMemsetAsync(W.st, 0, sizeof(PgState), s);
+    pg_norm2_kernel<<<nblk, 256, 0, s>>>(b2, n, W.npart, cnt, &W.st->bn2, nullptr);
+    pg_init_kernel<<<1, 1, 0, s>>>(W.st, tol, max_iters, m);
+    int rc = check_launch("pgmres init");
+    if (rc) return rc;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cap = nullptr;
+    auto cleanup = [&]() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (cap) cudaStreamDestroy(cap);
+    };
+    if (use_graph) {
+        if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+            return cleanup(), set_error(MB_ERR_CUDA, "pgmres: stream capture failed");
+        pg_cycle(kind, z, n, m_cols, vals, b2, x2, m, W, cnt, cap);
+        cudaError_t ce = cudaStreamEndCapture(cap, &graph);
+        if (ce != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+            return cleanup(), set_error(MB_ERR_CUDA, "pgmres: graph capture / instantiate failed");
+    }
+    PgState hs{};
+    const long long max_cycles = (long long)max_iters + 2;
+    for (long long c = 0; c < max_cycles; ++c) {
+        if (use_graph) {
+            if (cudaGraphLaunch(exec, s) != cudaSuccess)
+                return cleanup(), set_error(MB_ERR_CUDA, "pgmres: graph launch failed");
+        } else {
+            pg_cycle(kind, z, n, m_cols, vals, b2, x2, m, W, cnt, s);
+        }
+        cudaMemcpyAsync(&hs, W.st, sizeof(PgState), cudaMemcpyDeviceToHost, s);
+        if ((rc = sync_check(s, "pgmres cycle"))) return cleanup(), rc;
+        if (hs.converged || hs.jdone == 0) break;
+    }
+    cleanup();
+    if (iters_out) *iters_out = hs.iters;
+    if (cycles_out) *cycles_out = hs.cycles;
+    if (relres_out) *relres_out = hs.relres;
+    if (status_out) *status_out = hs.converged ? 0 : 1;
+    return MB_OK;
 }
 
 }  // namespace mb

@@ -453,6 +453,107 @@ def gmres(Z, b, x0=None, restart: int = 50, max_iters: int = 2000, tol: float = 
     return (xx[:, 0] if single else xx), infos
 
 
+SPAI_WIDTH = 48  # MB_SPAI_WIDTH: columns per row of the near-field preconditioner
+
+
+class SpaiPreconditioner:
+    """Sparse approximate inverse M of an RWG matrix on the mesh's near field (right
+    preconditioner of ``pgmres``): ``cols`` int32 [E, SPAI_WIDTH] local column ids (a row
+    ends at its first -1), ``vals`` complex64 [E, SPAI_WIDTH], ``status`` the build's status
+    word (bit 0: a pattern cut to its cap; bit 1: a rank-deficient least-squares block)."""
+
+    def __init__(self, cols, vals, status):
+        self.cols, self.vals, self.status = cols, vals, status
+
+    def apply(self, v):
+        """y = M v (complex64 [E])."""
+        n = self.cols.shape[0]
+        vv = v.to(device=self.cols.device, dtype=torch.complex64).reshape(n).contiguous()
+        y = torch.empty_like(vv)
+        _lib.call("mb_spai_apply_c64", _lib.ptr(self.cols), _lib.ptr(self.vals), n, _lib.ptr(vv), _lib.ptr(y),
+                  _lib.stream_of(vv))
+        return y
+
+
+def spai_preconditioner(Z, verts, faces, face_edge_indices, n_edges, pairs=None, workspace=None):
+    """Near-field sparse approximate inverse of the complex64 RWG matrix Z [E, E] of one mesh
+    (``mb_spai_build_c64``): column j minimises ||Z[I_j, J_j] m - e_j|| over the edges J_j of
+    the faces sharing a vertex with edge j's faces (rows I_j: one ring further).  ``pairs``:
+    the mesh's near-pair list (``near_pairs(faces)`` when None)."""
+    _lib.check_tensor(Z, "Z", dtype=torch.complex64, ndim=2, shape=(n_edges, n_edges))
+    dev = Z.device
+    _lib.check_tensor(verts, "verts", dtype=torch.float32, device=dev, ndim=2)
+    _lib.check_tensor(faces, "faces", dtype=torch.int32, device=dev, ndim=2)
+    _lib.check_tensor(face_edge_indices, "face_edge_indices", dtype=torch.int32, device=dev)
+    nf = faces.shape[0]
+    if pairs is None:
+        pairs = near_pairs(faces)
+    _lib.check_tensor(pairs, "pairs", dtype=torch.int32, device=dev, ndim=2)
+    desc = torch.tensor([[0, nf, 0, n_edges, 0, n_edges]], dtype=torch.int64, device=dev)
+    need = int(_lib.load().mb_spai_workspace_bytes(int(n_edges)))
+    if workspace is None:
+        workspace = torch.empty(need, dtype=torch.uint8, device=dev)
+    elif workspace.numel() < need:
+        raise ValueError(f"workspace needs {need} bytes")
+    cols = torch.empty((n_edges, SPAI_WIDTH), dtype=torch.int32, device=dev)
+    vals = torch.empty((n_edges, SPAI_WIDTH), dtype=torch.complex64, device=dev)
+    st = _lib.stream_of(Z)
+    _lib.call("mb_spai_build_c64", _lib.ptr(verts), _lib.ptr(faces), _lib.ptr(face_edge_indices), _lib.ptr(desc), 1,
+              nf, int(n_edges), _lib.ptr(pairs), pairs.shape[0], _lib.ptr(Z), _lib.ptr(cols), _lib.ptr(vals),
+              _lib.ptr(workspace), workspace.numel(), st)
+    status = __import__("ctypes").c_int32(0)
+    _lib.call("mb_spai_status", _lib.ptr(workspace), int(n_edges), __import__("ctypes").byref(status), st)
+    if status.value & 4:
+        raise ValueError("face_edge_indices: an edge id out of range, or an edge without faces or with more "
+                         "than two")
+    return SpaiPreconditioner(cols, vals, int(status.value))
+
+
+def pgmres_workspace_bytes(n: int, restart: int = 50) -> int:
+    return int(_lib.load().mb_pgmres_workspace_bytes(int(n), int(restart)))
+
+
+def pgmres(Z, b, M=None, x0=None, restart: int = 50, max_iters: int = 2000, tol: float = 1e-6,
+           use_graph: bool = True, workspace=None):
+    """Solve Z x = b by right-preconditioned GMRES(restart) with the whole restart cycle on the
+    device (``mb_pgmres_c64`` / ``mb_pgmres_c128``): FP32 products for complex64 Z, FP64 for
+    complex128 Z; FP64 refinement residual, CGS2 Arnoldi on a complex128 basis.  ``M``: a
+    ``SpaiPreconditioner`` or None.  b: [n] or [n, k].  Returns (x complex128 with b's shape,
+    per-column info dicts as ``gmres``)."""
+    _lib.check_tensor(Z, "Z", dtype=(torch.complex64, torch.complex128), ndim=2)
+    n = Z.shape[0]
+    if Z.shape[1] != n:
+        raise ValueError("Z must be square")
+    dev = Z.device
+    bb = b.to(device=dev, dtype=torch.complex128)
+    single = bb.dim() == 1
+    bb = bb.reshape(n, -1)
+    xx = torch.zeros_like(bb) if x0 is None else x0.to(device=dev, dtype=torch.complex128).reshape(n, -1).clone()
+    if M is not None and tuple(M.cols.shape) != (n, SPAI_WIDTH):
+        raise ValueError("preconditioner size does not match Z")
+    need = pgmres_workspace_bytes(n, restart)
+    if workspace is None:
+        workspace = torch.empty(need, dtype=torch.uint8, device=dev)
+    else:
+        _lib.check_tensor(workspace, "workspace", dtype=torch.uint8, device=dev)
+        if workspace.numel() < need:
+            raise ValueError(f"workspace needs {need} bytes")
+    fn = "mb_pgmres_c64" if Z.dtype == torch.complex64 else "mb_pgmres_c128"
+    infos = []
+    for c in range(bb.shape[1]):
+        bc_ = bb[:, c].contiguous()
+        xc = xx[:, c].contiguous()
+        info = _lib.GmresInfo()
+        _lib.call(fn, _lib.ptr(Z), n, _lib.ptr(M.cols if M is not None else None),
+                  _lib.ptr(M.vals if M is not None else None), _lib.ptr(bc_), _lib.ptr(xc), int(restart),
+                  int(max_iters), float(tol), int(bool(use_graph)), _lib.ptr(workspace), workspace.numel(),
+                  __import__("ctypes").byref(info), _lib.stream_of(Z))
+        xx[:, c] = xc
+        infos.append({"iterations": info.iterations, "restarts": info.restarts,
+                      "rel_residual": info.rel_residual, "converged": info.status == 0})
+    return (xx[:, 0] if single else xx), infos
+
+
 def gmres_real(A, b, x0=None, restart: int = 50, max_iters: int = 2000, tol: float = 1e-6,
                workspace=None):
     """Solve the real system A x = b by GMRES(restart) (``mb_gmres_f32`` / ``mb_gmres_f64``).
