@@ -1677,6 +1677,146 @@ def main_learned(args, rank, world, local_rank):
 # ---------------------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------------------
+# ---------------------------------------------------------------------------------------
+# time to a 1e-4 relative error in J: plain FP32 path against the mixed-precision path
+# ---------------------------------------------------------------------------------------
+TTS_TARGET = 1e-4
+TTS_LADDER = (1e-3, 3e-4, 1e-4, 3e-5, 1e-5, 3e-6, 1e-6, 3e-7, 1e-7, 3e-8)
+
+
+def time_to_solution(pkg, dev, level, k, sym, gq=4, Z=None, repeats=2):
+    """Time to a TTS_TARGET relative error in J (the RWG edge coefficients, x-polarised plane
+    wave along +z) against an FP64 reference J, for complete GPU paths, each run from the mesh
+    on the device to the solution inside the timed region (CUDA events):
+
+    * plain: the FP32 assembly + excitation, then GMRES(50) from zero with FP32 products and
+      no preconditioner (mb_gmres_c64: host-driven Arnoldi, FP64 refinement residual);
+    * plain_device: the same assembly, then the device-resident GMRES of the mixed path
+      without its preconditioner (mb_pgmres_c64 with no M);
+    * mixed: the same FP32 assembly + excitation, the near-field sparse approximate inverse
+      (mb_spai_build_c64), then right-preconditioned GMRES(50) with the restart cycle on the
+      device as a CUDA graph (mb_pgmres_c64: FP32 products, FP64 Arnoldi, compensated
+      refinement residual).
+
+    Each path's stopping tolerance is the loosest of TTS_LADDER whose solution reaches the
+    target (found by untimed solves on the same matrix); the timed runs' errors are reported.
+    """
+    import torch
+
+    M = pkg.mesh_MOM_3d
+    U = pkg.utils
+    v_np, f_np = pkg.meshes.icosphere(level)
+    verts = torch.tensor(v_np, dtype=torch.float32, device=dev)
+    faces = torch.tensor(f_np, dtype=torch.int32, device=dev)
+    edges, fei, _ = U.get_edge_unique(verts, faces)
+    E = int(edges.shape[0])
+    areas = U.compute_face_areas(verts, faces).contiguous()
+    normals = U.compute_face_normals(verts, faces).contiguous()
+    near = M.near_pairs(faces)
+    pw = M.plane_waves(k, [[0.0, 0.0, 1.0]], [[1.0, 0.0, 0.0]], device=dev)
+    if Z is None or tuple(Z.shape) != (E, E):
+        Z = torch.empty((E, E), dtype=torch.complex64, device=dev)
+    if not sym:
+        px, wx = U.get_gaussion_integration_points_and_weights(gq, device=dev)
+        py, wy = U.get_gaussion_integration_points_and_weights(gq - 1, device=dev)
+        er = M.edge_rows(fei, faces.shape[0], E)
+
+    def assemble():
+        Z.zero_()
+        if sym:
+            M.assemble_Z_rwg_sym(verts, faces, fei, E, k, out=Z, pairs=near, check_indices=False)
+            rhs = M.assemble_rhs_rwg_sym(verts, faces, fei, E, pw)
+        else:
+            M.assemble_Z_rwg(verts, faces, areas, normals, fei, E, px, wx, py, wy, k, out=Z, check_indices=False,
+                             order="edges", edge_rows_map=er)
+            rhs = M.assemble_rhs_rwg(verts, faces, areas, normals, fei, E, px, wx, pw)
+        return rhs[:, 0].to(torch.complex128)
+
+    def precond():
+        return M.spai_preconditioner(Z, verts, faces, fei, E, pairs=near)
+
+    def solve(path, b, tol, P=None):
+        if path == "plain":
+            return M.gmres(Z, b, restart=50, tol=tol, max_iters=20000)
+        if path == "plain_device":
+            return M.pgmres(Z, b, M=None, restart=50, tol=tol, max_iters=20000, use_graph=True)
+        return M.pgmres(Z, b, M=P, restart=50, tol=tol, max_iters=20000, use_graph=True)
+
+    # FP64 reference J (untimed)
+    t0 = time.perf_counter()
+    b = assemble()
+    P = precond()
+    if sym:
+        Z64 = M.assemble_Z_rwg_sym(verts.double(), faces, fei, E, k, pairs=near, check_indices=False)
+        b64 = M.assemble_rhs_rwg_sym(verts.double(), faces, fei, E, pw)[:, 0]
+        j_ref, rinfo = M.pgmres(Z64, b64, M=P, restart=50, tol=1e-12, max_iters=20000)
+        del Z64, b64
+        ref_what = ("FP64 assembly (complex128 Z: FP64 quadrature and closed-form singular integrals), FP64 "
+                    "GMRES (FP64 products) to a 1e-12 relative residual")
+    else:
+        j_ref, rinfo = M.pgmres(Z, b, M=P, restart=50, tol=1e-12, max_iters=20000)
+        ref_what = ("the FP32-assembled complex64 Z solved to a 1e-12 relative residual (an FP64 assembly of the "
+                    "reference rule takes about a minute at GB300's FP64 rate at this size; the FP32 assembly's "
+                    "own error is checked against the float64 oracle by the parity tests)")
+    torch.cuda.synchronize(dev)
+    ref_s = time.perf_counter() - t0
+    jn = float(j_ref.norm())
+
+    def err(x):
+        return float((x - j_ref).norm()) / jn
+
+    out = {"target_rel_err_J": TTS_TARGET, "reference_J": ref_what,
+           "reference_J_info": {"iterations": rinfo[0]["iterations"], "rel_residual": rinfo[0]["rel_residual"],
+                                "seconds": ref_s},
+           "mesh": f"icosphere L{level} ({faces.shape[0]} faces, {E} RWG unknowns)", "ka": k,
+           "formulation": ("EFIE, 7-point rule on both triangles, closed-form FP64 near pairs" if sym else
+                           f"reference CFIE (EFIE+MFIE), collapsed Gauss-Legendre gaussQR={gq}"),
+           "excitation": "x-polarised unit plane wave along +z"}
+    for path in ("plain", "plain_device", "mixed"):
+        chosen = None
+        for tol in TTS_LADDER:
+            x, inf = solve(path, b, tol, P)
+            e = err(x)
+            if e <= TTS_TARGET:
+                chosen = (tol, e, inf[0])
+                break
+        if chosen is None:
+            out[path] = {"reached": False, "last_tol": TTS_LADDER[-1], "last_err": e, "last_info": inf[0]}
+            continue
+        tol = chosen[0]
+        runs = []
+        for _ in range(repeats):
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            torch.cuda.synchronize(dev)
+            ev[0].record()
+            bb = assemble()
+            ev[1].record()
+            PP = precond() if path == "mixed" else None
+            ev[2].record()
+            x, inf = solve(path, bb, tol, PP)
+            ev[3].record()
+            torch.cuda.synchronize(dev)
+            runs.append({"total_ms": ev[0].elapsed_time(ev[3]), "assembly_ms": ev[0].elapsed_time(ev[1]),
+                         "precond_ms": ev[1].elapsed_time(ev[2]), "solve_ms": ev[2].elapsed_time(ev[3]),
+                         "iterations": inf[0]["iterations"], "restarts": inf[0]["restarts"],
+                         "rel_residual": inf[0]["rel_residual"], "rel_err_J": err(x)})
+        out[path] = {"reached": all(r["rel_err_J"] <= TTS_TARGET for r in runs), "tol": tol,
+                     "ms": statistics.mean(r["total_ms"] for r in runs), "runs": runs}
+    out["plain"]["what"] = ("FP32 assembly + excitation, GMRES(50) from zero with FP32 products and no "
+                            "preconditioner, host-driven Arnoldi, FP64 refinement residual (mb_gmres_c64)")
+    out["plain_device"]["what"] = ("FP32 assembly + excitation, the mixed path's device-resident GMRES(50) from "
+                                   "zero without the preconditioner (mb_pgmres_c64, no M)")
+    out["mixed"]["what"] = ("FP32 assembly + excitation, near-field SAI preconditioner (mb_spai_build_c64), "
+                            "right-preconditioned GMRES(50) with the restart cycle on the device as a CUDA graph, "
+                            "compensated-FP32 refinement residual (mb_pgmres_c64)")
+    if out["mixed"].get("reached"):
+        for p in ("plain", "plain_device"):
+            if out[p].get("reached"):
+                out[f"ratio_{p}_over_mixed"] = out[p]["ms"] / out["mixed"]["ms"]
+    del P, b, j_ref
+    return out
+
+
 def main():
     args = _args()
     rank = int(os.environ.get("RANK", "0"))
@@ -1852,27 +1992,17 @@ def main():
             "data": "synthetic", "config": config, "roofline": roof, "clocks": clocks.summary(),
             "gpu_launches": args.steps * (2 if sym else 1)}
 
-    # time to solution (reported beside the headline): excitation + GMRES on the assembled Z
+    # time to a 1e-4 error in J, plain FP32 path vs the mixed-precision path (reported beside the
+    # headline; both formulations on the same 30 720-unknown sphere for the default workload)
     if not args.no_solve:
-        pw = pkg.mesh_MOM_3d.plane_waves(k, [[0.0, 0.0, 1.0]], [[1.0, 0.0, 0.0]], device=dev)
-        if not sym:
-            gp, gw = pkg.utils.get_gaussion_integration_points_and_weights(gq, device=dev)
-        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s0.record(stream)
+        tts = {}
         if sym:
-            rhs = M.assemble_rhs_rwg_sym(verts, faces, fei, n_edges, pw)
+            tts["efie_7pt"] = time_to_solution(pkg, dev, level, k, True, Z=Z)
         else:
-            rhs = M.assemble_rhs_rwg(verts, faces, areas, normals, fei, n_edges, gp, gw, pw)
-        x, infos = M.gmres(Z, rhs[:, 0], restart=50, tol=1e-6, max_iters=3000)
-        s1.record(stream)
-        torch.cuda.synchronize(dev)
-        line["solve"] = {"what": "x-polarised plane wave along +z, GMRES(50) to 1e-6 relative residual "
-                                 "(FP32 matvec, FP64 Arnoldi and refinement residual)",
-                         "gmres_ms": s0.elapsed_time(s1), "iterations": infos[0]["iterations"],
-                         "restarts": infos[0]["restarts"], "rel_residual": infos[0]["rel_residual"],
-                         "converged": infos[0]["converged"],
-                         "time_to_solution_ms": ms_per_step + s0.elapsed_time(s1)}
-        del x, rhs
+            tts["cfie_ref_rule"] = time_to_solution(pkg, dev, level, k, False, gq=gq, Z=Z)
+            if level == 5:
+                tts["efie_7pt"] = time_to_solution(pkg, dev, level, k, True, Z=Z)
+        line["time_to_solution"] = tts
 
     # end to end through the public operator: host (pinned) inputs in, Z back to host memory
     if not args.no_e2e:

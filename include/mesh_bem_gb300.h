@@ -482,15 +482,16 @@ int mb_spai_apply_c64(const int32_t* m_cols, const float* m_vals, int64_t n, con
                       void* stream);
 
 /* GMRES(restart) on Z x = b with the right preconditioner M (m_cols / m_vals from
- * mb_spai_build_c64, or both NULL for none): each restart cycle starts from the FP64 residual
- * b - Z x, solves (Z M) u = r and adds M u to x.  The whole cycle runs on the device (CGS2
- * Arnoldi on a complex128 basis, Givens rotations, the residual estimate and the back
+ * mb_spai_build_c64, or both NULL for none): each restart cycle starts from the refinement
+ * residual b - Z x, solves (Z M) u = r and adds M u to x.  The whole cycle runs on the device
+ * (CGS2 Arnoldi on a complex128 basis, Givens rotations, the residual estimate and the back
  * substitution in kernels; deterministic block reductions); use_graph = 1 captures it once as
  * a CUDA graph and replays it.  The host reads the solver state once per cycle.
- * mb_pgmres_c64: Z interleaved complex64 [n, n], FP32 products; mb_pgmres_c128: Z
- * interleaved complex128, FP64 products.  b, x complex128 [n], 16-byte aligned (x: initial
- * guess in, solution out).  info as for mb_gmres_c64.  Workspace:
- * mb_pgmres_workspace_bytes(n, restart) bytes. */
+ * mb_pgmres_c64: Z interleaved complex64 [n, n], FP32 products, the refinement residual by
+ * compensated FP32 dot products (exact products and sums, ~1e-13 of sum |Z_ij x_j|);
+ * mb_pgmres_c128: Z interleaved complex128, FP64 products and residual.  z, b, x 16-byte
+ * aligned; b, x complex128 [n] (x: initial guess in, solution out).  info as for
+ * mb_gmres_c64.  Workspace: mb_pgmres_workspace_bytes(n, restart) bytes. */
 size_t mb_pgmres_workspace_bytes(int64_t n, int restart);
 int mb_pgmres_c64(const float* z, int64_t n, const int32_t* m_cols, const float* m_vals, const double* b, double* x,
                   int restart, int max_iters, double tol, int use_graph, void* workspace, size_t workspace_bytes,

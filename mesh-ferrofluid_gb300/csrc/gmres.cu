@@ -665,16 +665,23 @@ int launch_residual_c128(const float* z, const double* x, const double* b, int64
 // (Z M) u = r0 and updates x += M u, so the residual GMRES minimises is the residual of
 // Z x = b itself.  Arnoldi by CGS2 on a complex128 basis with FP64 sums; the Givens
 // rotations, the residual estimate, the stopping test and the back substitution run in
-// single-thread kernels on a device state record; every cycle starts from the FP64 residual
-// b - Z x (iterative refinement).  Sums over the vector run as fixed-size block partials
-// that the last block to finish adds in a fixed order (deterministic, no FP64 atomics).
-// A cycle is a fixed sequence of launches: once the state says the cycle has ended, the
-// remaining steps' launches return at once.  With use_graph the cycle is captured once
-// as a CUDA graph and replayed; the host reads the state once per cycle.
-// Z is complex64 (FP32 products, the solver of the FP32 path) or complex128 (FP64 products:
-// the FP64 reference solution of the same discretisation).
+// one-warp kernels on a device state record; every cycle starts from the refinement
+// residual b - Z x.  Sums over the vector run as block partials that the last block to
+// finish adds in a fixed order (deterministic, no FP64 atomics).  A cycle is a fixed
+// sequence of launches: once the state says the cycle has ended, the remaining steps'
+// launches return at once.  With use_graph the cycle is captured once as a CUDA graph and
+// replayed; the host reads the state once per cycle.
+//
+// complex64 Z (FP32 products): the refinement residual is a compensated FP32 dot product
+// -- x split into FP32 hi + lo parts, each product Z_ij x_hi,j made exact by TwoProduct
+// (mul + fma), sums kept exact by TwoSum, the rounding terms and the x_lo products summed
+// beside them, lane sums combined in FP64 -- accurate to ~1e-13 of sum |Z_ij x_j| at FP32
+// instruction speed (GB300's FP64 rate would make an FP64 residual ~10x slower than a
+// matrix pass).  complex128 Z (FP64 products, FP64 residual): the FP64 reference solution of
+// the same discretisation.
 // ---------------------------------------------------------------------------------------
 constexpr int kPgMaxBlocks = 256;
+constexpr int kPgRowsPerBlock = 8;   // warps per block in the one-warp-per-row kernels
 
 struct PgState {
     double bn2, bnorm, rn2, beta, relres, tol, hn2, hn;
@@ -688,7 +695,7 @@ struct PgWork {
     double2* V;     // [(m+1), n]
     double2* w;     // [n]
     double2* r;     // [n] residual, then the cycle's update V y
-    double2* z;     // [n] M v (float2 view for the FP32 product)
+    double2* z;     // [n] M v (float2 view for the FP32 product); x split (float4) at cycle start
     double2* part;  // [blocks, m+1] block partials
     double* npart;  // [blocks]
     PgState* st;
@@ -747,18 +754,23 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 __device__ __forceinline__ double2 cconjmul(double2 a, double2 b) {  // conj(a) b
     return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
 }
+__device__ __forceinline__ double2 cdiv(double2 a, double2 d) {
+    const double dd = d.x * d.x + d.y * d.y;
+    return make_double2((a.x * d.x + a.y * d.y) / dd, (a.y * d.x - a.x * d.y) / dd);
+}
 __device__ __forceinline__ double cabs2(double2 a) { return a.x * a.x + a.y * a.y; }
 
-// Adds the blocks' partials npart[0..gridDim.x) in a fixed order into *out once every block
+// Adds the blocks' partials npart[0..nblocks) in a fixed order into *out once every block
 // has written its own; the counter is left at zero for the next launch.
-__device__ __forceinline__ void pg_last_block_sum(double* npart, unsigned* cnt, double* out) {
+__device__ __forceinline__ void pg_last_block_sum(double* npart, unsigned* cnt, double* out, unsigned nblocks) {
     __shared__ bool s_last;
     __threadfence();
-    if (threadIdx.x == 0) s_last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(cnt, 1u) == nblocks - 1;
     __syncthreads();
     if (s_last && threadIdx.x < 32) {
         double a = 0.0;
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) a += __ldcg(npart + b);
+        for (unsigned b = threadIdx.x; b < nblocks; b += 32) a += __ldcg(npart + b);
         a = warp_sum(a);
         if (threadIdx.x == 0) {
             *out = a;
@@ -767,11 +779,9 @@ __device__ __forceinline__ void pg_last_block_sum(double* npart, unsigned* cnt, 
     }
 }
 
-// *out = sum |v_k|^2 (FP64).  active may be null.
+// *out = sum |v_k|^2 (FP64), grid-stride over at most kPgMaxBlocks blocks
 __global__ void __launch_bounds__(256) pg_norm2_kernel(const double2* __restrict__ v, int64_t n,
-                                                      double* __restrict__ npart, unsigned* cnt, double* out,
-                                                      const int* __restrict__ active) {
-    if (active && !*active) return;
+                                                      double* __restrict__ npart, unsigned* cnt, double* out) {
     __shared__ double s[8];
     double a = 0.0;
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
@@ -784,7 +794,7 @@ __global__ void __launch_bounds__(256) pg_norm2_kernel(const double2* __restrict
         for (int q = 0; q < 8; ++q) t += s[q];
         npart[blockIdx.x] = t;
     }
-    pg_last_block_sum(npart, cnt, out);
+    pg_last_block_sum(npart, cnt, out, gridDim.x);
 }
 
 __global__ void pg_init_kernel(PgState* st, double tol, long long max_iters, int m) {
@@ -829,25 +839,37 @@ __global__ void pg_scale_kernel(const double2* __restrict__ src, int64_t n, cons
     dst[k] = make_double2(v.x * s, v.y * s);
 }
 
-// z = M v: complex64 output (FP32 product path, F32 = true) or complex128 (FP64 path)
+// z = M v, one warp per row (lanes over the row's pattern, FP64 sums): complex64 output for the
+// FP32 product (F32 = true) or complex128 for the FP64 product.
 template <bool F32>
-__global__ void pg_precond_kernel(const int32_t* __restrict__ cols, const float2* __restrict__ vals, int64_t n,
-                                  const double2* __restrict__ v, double2* __restrict__ z,
-                                  const PgState* __restrict__ st) {
+__global__ void __launch_bounds__(256) pg_precond_kernel(const int32_t* __restrict__ cols,
+                                                         const float2* __restrict__ vals, int64_t n,
+                                                         const double2* __restrict__ v, double2* __restrict__ z,
+                                                         const PgState* __restrict__ st) {
     if (!st->active) return;
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (F32) {
-        float2 o;
-        if (cols) {
-            o = spai_row_f32(cols, vals, i, v);
-        } else {
-            const double2 x = v[i];
-            o = make_float2((float)x.x, (float)x.y);
+    const int64_t row = (int64_t)blockIdx.x * kPgRowsPerBlock + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    double2 acc = make_double2(0.0, 0.0);
+    if (cols) {
+#pragma unroll
+        for (int q = lane; q < MB_SPAI_WIDTH; q += 32) {
+            const int32_t c = __ldg(cols + row * MB_SPAI_WIDTH + q);
+            if (c >= 0) {
+                const float2 mq = __ldg(vals + row * MB_SPAI_WIDTH + q);
+                const double2 x = __ldg(v + c);
+                acc.x = fma((double)mq.x, x.x, fma(-(double)mq.y, x.y, acc.x));
+                acc.y = fma((double)mq.x, x.y, fma((double)mq.y, x.x, acc.y));
+            }
         }
-        reinterpret_cast<float2*>(z)[i] = o;
-    } else {
-        z[i] = cols ? spai_row_f64(cols, vals, i, v) : v[i];
+        acc.x = warp_sum(acc.x);
+        acc.y = warp_sum(acc.y);
+    } else if (lane == 0) {
+        acc = v[row];
+    }
+    if (lane == 0) {
+        if (F32) reinterpret_cast<float2*>(z)[row] = make_float2((float)acc.x, (float)acc.y);
+        else z[row] = acc;
     }
 }
 
@@ -899,80 +921,127 @@ __global__ void __launch_bounds__(256) residual_z128_kernel(const double2* __res
     if (lane == 0) r[row] = make_double2(b[row].x - ar, b[row].y - ai);
 }
 
-// h[i] = sum_k conj(V_i[k]) w[k], i < nb: block partials, then the last block's fixed-order sum
+// x (complex128) -> (hi, lo) FP32 parts: xs[k] = (Re hi, Im hi, Re lo, Im lo)
+__global__ void pg_split_kernel(const double2* __restrict__ x, int64_t n, float4* __restrict__ xs) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double2 v = x[k];
+    const float hr = (float)v.x, hi = (float)v.y;
+    xs[k] = make_float4(hr, hi, (float)(v.x - (double)hr), (float)(v.y - (double)hi));
+}
+
+// s + t exactly as s' + e (Knuth's TwoSum; rounding-mode intrinsics keep the compiler from
+// contracting or reordering it)
+__device__ __forceinline__ void two_sum(float& s, float t, float& e) {
+    const float u = __fadd_rn(s, t);
+    const float bb = __fsub_rn(u, s);
+    e = __fadd_rn(__fsub_rn(s, __fsub_rn(u, bb)), __fsub_rn(t, bb));
+    s = u;
+}
+
+// r = b - Z x with Z complex64 and x given by its FP32 split: compensated FP32 dot products
+// (exact products by TwoProduct, exact running sums by TwoSum), lane sums combined in FP64.
+__global__ void __launch_bounds__(256) residual_c64x_kernel(const float2* __restrict__ z,
+                                                            const float4* __restrict__ xs,
+                                                            const double2* __restrict__ b, int64_t n,
+                                                            double2* __restrict__ r) {
+    const int64_t row = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    const float2* zr = z + row * n;
+    float sr = 0.f, si = 0.f, cr = 0.f, ci = 0.f;
+    for (int64_t j = lane; j < n; j += 32) {
+        const float2 a = __ldcs(zr + j);
+        const float4 x = __ldg(xs + j);
+        const float p1 = __fmul_rn(a.x, x.x), e1 = fmaf(a.x, x.x, -p1);
+        const float p2 = __fmul_rn(-a.y, x.y), e2 = fmaf(-a.y, x.y, -p2);
+        const float p3 = __fmul_rn(a.x, x.y), e3 = fmaf(a.x, x.y, -p3);
+        const float p4 = __fmul_rn(a.y, x.x), e4 = fmaf(a.y, x.x, -p4);
+        float t1, t2, t3, t4;
+        two_sum(sr, p1, t1);
+        two_sum(sr, p2, t2);
+        two_sum(si, p3, t3);
+        two_sum(si, p4, t4);
+        cr += (t1 + t2) + (e1 + e2) + fmaf(a.x, x.z, -a.y * x.w);
+        ci += (t3 + t4) + (e3 + e4) + fmaf(a.x, x.w, a.y * x.z);
+    }
+    const double ar = warp_sum((double)sr + (double)cr), ai = warp_sum((double)si + (double)ci);
+    if (lane == 0) r[row] = make_double2(b[row].x - ar, b[row].y - ai);
+}
+
+// h[i] = sum_k conj(V_i[k]) w[k] for i < nb: block (c, g) has warp w on row i = 8 g + w over
+// chunk c; the last block to finish adds the chunks of every row in a fixed order.
 __global__ void __launch_bounds__(256) pg_dots_kernel(const double2* __restrict__ V, const double2* __restrict__ w,
-                                                      int64_t n, int nb, double2* __restrict__ part, int ldp,
-                                                      unsigned* cnt, double2* __restrict__ h,
+                                                      int64_t n, int nb, int64_t chunk, double2* __restrict__ part,
+                                                      int ldp, unsigned* cnt, double2* __restrict__ h,
                                                       const int* __restrict__ active) {
     if (!*active) return;
-    __shared__ double2 s[kGmresMaxRestart + 1][8];
     __shared__ bool s_last;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const int64_t k0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    double2 wk = make_double2(0.0, 0.0);
-    const bool single = k0 + stride >= n;  // one element per thread (the common case)
-    if (single && k0 < n) wk = w[k0];
-    for (int i = 0; i < nb; ++i) {
+    const int i = blockIdx.y * 8 + warp;
+    const int64_t k0 = (int64_t)blockIdx.x * chunk;
+    const int64_t k1 = k0 + chunk < n ? k0 + chunk : n;
+    if (i < nb) {
         const double2* vi = V + (int64_t)i * n;
-        double ar = 0.0, ai = 0.0;
-        if (single) {
-            if (k0 < n) {
-                const double2 p = cconjmul(vi[k0], wk);
-                ar = p.x;
-                ai = p.y;
-            }
-        } else {
-            for (int64_t k = k0; k < n; k += stride) {
-                const double2 p = cconjmul(vi[k], w[k]);
-                ar += p.x;
-                ai += p.y;
-            }
+        double ar0 = 0.0, ai0 = 0.0, ar1 = 0.0, ai1 = 0.0;
+        int64_t k = k0 + lane;
+        for (; k + 32 < k1; k += 64) {
+            const double2 a0 = vi[k], a1 = vi[k + 32], b0 = w[k], b1 = w[k + 32];
+            const double2 p0 = cconjmul(a0, b0), p1 = cconjmul(a1, b1);
+            ar0 += p0.x;
+            ai0 += p0.y;
+            ar1 += p1.x;
+            ai1 += p1.y;
         }
-        ar = warp_sum(ar);
-        ai = warp_sum(ai);
-        if (lane == 0) s[i][warp] = make_double2(ar, ai);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-        double sr = 0.0, si = 0.0;
-        for (int q = 0; q < 8; ++q) {
-            sr += s[i][q].x;
-            si += s[i][q].y;
+        if (k < k1) {
+            const double2 p0 = cconjmul(vi[k], w[k]);
+            ar0 += p0.x;
+            ai0 += p0.y;
         }
-        part[(int64_t)blockIdx.x * ldp + i] = make_double2(sr, si);
+        const double ar = warp_sum(ar0 + ar1), ai = warp_sum(ai0 + ai1);
+        if (lane == 0) part[(int64_t)blockIdx.x * ldp + i] = make_double2(ar, ai);
     }
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+    if (threadIdx.x == 0) s_last = atomicAdd(cnt, 1u) == gridDim.x * gridDim.y - 1;
     __syncthreads();
     if (!s_last) return;
-    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    for (int ii = threadIdx.x; ii < nb; ii += blockDim.x) {
         double sr = 0.0, si = 0.0;
-        for (int b = 0; b < (int)gridDim.x; ++b) {
-            const double2 p = __ldcg(part + (int64_t)b * ldp + i);
+        for (unsigned c = 0; c < gridDim.x; ++c) {
+            const double2 p = __ldcg(part + (int64_t)c * ldp + ii);
             sr += p.x;
             si += p.y;
         }
-        h[i] = make_double2(sr, si);
+        h[ii] = make_double2(sr, si);
     }
     if (threadIdx.x == 0) *cnt = 0;
 }
 
-// w -= sum_{i<nb} V_i h_i; with npart, also |w|^2 into *hn2 (block partials + last block)
-__global__ void __launch_bounds__(256) pg_sub_kernel(const double2* __restrict__ V, const double2* __restrict__ h,
+// w -= sum_{i<nb} V_i h_i (one element per thread, the sum over i unrolled by four); with
+// npart, also |w|^2 into *hn2 (block partials + last block).
+__global__ void __launch_bounds__(128) pg_sub_kernel(const double2* __restrict__ V, const double2* __restrict__ h,
                                                      int64_t n, int nb, double2* __restrict__ w,
                                                      double* __restrict__ npart, unsigned* cnt, double* hn2,
                                                      const int* __restrict__ active) {
     if (!*active) return;
     __shared__ double2 sh[kGmresMaxRestart + 1];
-    __shared__ double s[8];
+    __shared__ double s[4];
     for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = h[i];
     __syncthreads();
     double a = 0.0;
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
         double2 x = w[k];
-        for (int i = 0; i < nb; ++i) {
+        int i = 0;
+        for (; i + 4 <= nb; i += 4) {
+            const double2 v0 = V[(int64_t)i * n + k], v1 = V[(int64_t)(i + 1) * n + k];
+            const double2 v2 = V[(int64_t)(i + 2) * n + k], v3 = V[(int64_t)(i + 3) * n + k];
+            const double2 p0 = cmul(v0, sh[i]), p1 = cmul(v1, sh[i + 1]), p2 = cmul(v2, sh[i + 2]),
+                          p3 = cmul(v3, sh[i + 3]);
+            x.x -= (p0.x + p1.x) + (p2.x + p3.x);
+            x.y -= (p0.y + p1.y) + (p2.y + p3.y);
+        }
+        for (; i < nb; ++i) {
             const double2 p = cmul(V[(int64_t)i * n + k], sh[i]);
             x.x -= p.x;
             x.y -= p.y;
@@ -984,69 +1053,77 @@ __global__ void __launch_bounds__(256) pg_sub_kernel(const double2* __restrict__
     a = warp_sum(a);
     if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = a;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int q = 0; q < 8; ++q) t += s[q];
-        npart[blockIdx.x] = t;
-    }
-    pg_last_block_sum(npart, cnt, hn2);
+    if (threadIdx.x == 0) npart[blockIdx.x] = (s[0] + s[1]) + (s[2] + s[3]);
+    pg_last_block_sum(npart, cnt, hn2, gridDim.x);
 }
 
-// One Arnoldi step's Hessenberg column: h = h1 + h2 and |w|; previous rotations, a new one,
-// the residual estimate and the end-of-cycle test.
-__global__ void pg_givens_kernel(PgState* st, double2* g, double2* cs, double2* sn, double2* H,
-                                 const double2* h1, const double2* h2, int j) {
+// One Arnoldi step's Hessenberg column (one warp): h = h1 + h2 and |w| staged in shared
+// memory with the previous rotations; lane 0 applies them, forms the new rotation, updates
+// the residual estimate and decides whether the cycle ends.
+__global__ void __launch_bounds__(32) pg_givens_kernel(PgState* st, double2* g, double2* cs, double2* sn,
+                                                       double2* H, const double2* h1, const double2* h2, int j) {
     if (!st->active) return;
+    __shared__ double2 col[kGmresMaxRestart + 1], scs[kGmresMaxRestart], ssn[kGmresMaxRestart];
+    const int lane = threadIdx.x;
     const int m = st->m;
-    const double hn = sqrt(st->hn2);
-    st->hn = hn;
-    double2* col = H + (int64_t)j * (m + 1);
-    for (int i = 0; i <= j; ++i) col[i] = make_double2(h1[i].x + h2[i].x, h1[i].y + h2[i].y);
-    double2 below = make_double2(hn, 0.0);  // h[j+1]
-    for (int i = 0; i < j; ++i) {
-        const double2 a = col[i], b = col[i + 1];
-        // t = conj(cs) a + conj(sn) b; b' = -sn a + cs b
-        const double2 t1 = cconjmul(cs[i], a), t2 = cconjmul(sn[i], b);
-        const double2 u1 = cmul(sn[i], a), u2 = cmul(cs[i], b);
-        col[i] = make_double2(t1.x + t2.x, t1.y + t2.y);
-        col[i + 1] = make_double2(u2.x - u1.x, u2.y - u1.y);
+    for (int i = lane; i <= j; i += 32) col[i] = make_double2(h1[i].x + h2[i].x, h1[i].y + h2[i].y);
+    for (int i = lane; i < j; i += 32) {
+        scs[i] = cs[i];
+        ssn[i] = sn[i];
     }
-    const double a = sqrt(cabs2(col[j])), bb = hn;
-    const double rr = hypot(a, bb);
-    double2 c, sv;
-    if (rr == 0.0) {
-        c = make_double2(1.0, 0.0);
-        sv = make_double2(0.0, 0.0);
-    } else {
-        c = make_double2(col[j].x / rr, col[j].y / rr);
-        sv = make_double2(below.x / rr, below.y / rr);
+    __syncwarp();
+    if (lane == 0) {
+        const double hn = sqrt(st->hn2);
+        st->hn = hn;
+        for (int i = 0; i < j; ++i) {
+            const double2 a = col[i], b = col[i + 1];
+            // t = conj(cs) a + conj(sn) b; b' = -sn a + cs b
+            const double2 t1 = cconjmul(scs[i], a), t2 = cconjmul(ssn[i], b);
+            const double2 u1 = cmul(ssn[i], a), u2 = cmul(scs[i], b);
+            col[i] = make_double2(t1.x + t2.x, t1.y + t2.y);
+            col[i + 1] = make_double2(u2.x - u1.x, u2.y - u1.y);
+        }
+        const double rr = hypot(sqrt(cabs2(col[j])), hn);
+        double2 c, sv;
+        if (rr == 0.0) {
+            c = make_double2(1.0, 0.0);
+            sv = make_double2(0.0, 0.0);
+        } else {
+            c = make_double2(col[j].x / rr, col[j].y / rr);
+            sv = make_double2(hn / rr, 0.0);
+        }
+        cs[j] = c;
+        sn[j] = sv;
+        col[j] = make_double2(rr, 0.0);
+        const double2 gj = g[j];
+        const double2 ng = cmul(sv, gj);
+        g[j + 1] = make_double2(-ng.x, -ng.y);
+        g[j] = cconjmul(c, gj);
+        st->iters += 1;
+        st->jdone = j + 1;
+        const double est = sqrt(cabs2(g[j + 1])) / st->bnorm;
+        if (est <= 0.5 * st->tol || hn <= 1e-300 || st->iters >= st->max_iters || j + 1 == m) st->active = 0;
     }
-    cs[j] = c;
-    sn[j] = sv;
-    col[j] = make_double2(rr, 0.0);
-    const double2 gj = g[j];
-    const double2 ng = cmul(sv, gj);
-    g[j + 1] = make_double2(-ng.x, -ng.y);
-    g[j] = cconjmul(c, gj);
-    st->iters += 1;
-    st->jdone = j + 1;
-    const double est = sqrt(cabs2(g[j + 1])) / st->bnorm;
-    if (est <= 0.5 * st->tol || hn <= 1e-300 || st->iters >= st->max_iters || j + 1 == m) st->active = 0;
+    __syncwarp();
+    for (int i = lane; i <= j; i += 32) H[(int64_t)j * (m + 1) + i] = col[i];
 }
 
-// y = R^{-1} g over the cycle's steps (R upper triangular in H)
-__global__ void pg_backsub_kernel(const PgState* st, const double2* H, const double2* g, double2* y) {
-    const int jd = st->jdone, m = st->m;
+// y = R^{-1} g over the cycle's steps, column by column (one warp; g kept in shared memory)
+__global__ void __launch_bounds__(32) pg_backsub_kernel(const PgState* st, const double2* H, const double2* g,
+                                                        double2* y) {
+    __shared__ double2 sg[kGmresMaxRestart + 1];
+    const int jd = st->jdone, m = st->m, lane = threadIdx.x;
+    for (int r = lane; r < jd; r += 32) sg[r] = g[r];
+    __syncwarp();
     for (int i = jd - 1; i >= 0; --i) {
-        double2 acc = g[i];
-        for (int q = i + 1; q < jd; ++q) {
-            const double2 p = cmul(H[(int64_t)q * (m + 1) + i], y[q]);
-            acc.x -= p.x;
-            acc.y -= p.y;
+        const double2 yi = cdiv(sg[i], H[(int64_t)i * (m + 1) + i]);
+        if (lane == 0) y[i] = yi;
+        for (int r = lane; r < i; r += 32) {
+            const double2 p = cmul(H[(int64_t)i * (m + 1) + r], yi);
+            sg[r].x -= p.x;
+            sg[r].y -= p.y;
         }
-        const double2 d = H[(int64_t)i * (m + 1) + i];
-        const double dd = cabs2(d);
-        y[i] = make_double2((acc.x * d.x + acc.y * d.y) / dd, (acc.y * d.x - acc.x * d.y) / dd);
+        __syncwarp();
     }
 }
 
@@ -1082,33 +1159,41 @@ static void pg_cycle(int kind, const void* z, int64_t n, const int32_t* cols, co
                      const double2* b, double2* x, int m, const PgWork& W, unsigned* cnt, cudaStream_t s) {
     const unsigned vb = (unsigned)((n + 255) / 256), rb = (unsigned)((n + 7) / 8);
     const int nblk = (int)std::min<int64_t>(vb, kPgMaxBlocks);
+    const int sblk = (int)std::min<int64_t>((n + 127) / 128, kPgMaxBlocks);
+    // dot-product chunks: at least 1024 elements, at most kPgMaxBlocks chunks
+    int64_t chunk = 1024;
+    while ((n + chunk - 1) / chunk > kPgMaxBlocks) chunk *= 2;
+    const unsigned nchunk = (unsigned)((n + chunk - 1) / chunk);
     const int* act = &W.st->active;
-    if (kind == 0)
-        residual_c128_kernel<<<rb, 256, 0, s>>>(static_cast<const float*>(z), reinterpret_cast<const double*>(x),
-                                                reinterpret_cast<const double*>(b), n, reinterpret_cast<double*>(W.r));
-    else
+    if (kind == 0) {
+        pg_split_kernel<<<vb, 256, 0, s>>>(x, n, reinterpret_cast<float4*>(W.z));
+        residual_c64x_kernel<<<rb, 256, 0, s>>>(static_cast<const float2*>(z), reinterpret_cast<const float4*>(W.z),
+                                                b, n, W.r);
+    } else {
         residual_z128_kernel<<<rb, 256, 0, s>>>(static_cast<const double2*>(z), x, b, n, W.r);
-    pg_norm2_kernel<<<nblk, 256, 0, s>>>(W.r, n, W.npart, cnt, &W.st->rn2, nullptr);
+    }
+    pg_norm2_kernel<<<nblk, 256, 0, s>>>(W.r, n, W.npart, cnt, &W.st->rn2);
     pg_cycle_start_kernel<<<1, 1, 0, s>>>(W.st, W.g);
     pg_scale_kernel<<<vb, 256, 0, s>>>(W.r, n, W.st, 0, W.V);
     for (int j = 0; j < m; ++j) {
         const double2* vj = W.V + (int64_t)j * n;
+        const dim3 dgrid(nchunk, (unsigned)((j + 1 + 7) / 8));
         if (kind == 0) {
-            pg_precond_kernel<true><<<vb, 256, 0, s>>>(cols, vals, n, vj, W.z, W.st);
+            pg_precond_kernel<true><<<rb, 256, 0, s>>>(cols, vals, n, vj, W.z, W.st);
             matvec_c64_kernel<<<rb, 256, 0, s>>>(static_cast<const float*>(z), reinterpret_cast<const float*>(W.z), n,
                                                  reinterpret_cast<double*>(W.w), act);
         } else {
-            pg_precond_kernel<false><<<vb, 256, 0, s>>>(cols, vals, n, vj, W.z, W.st);
+            pg_precond_kernel<false><<<rb, 256, 0, s>>>(cols, vals, n, vj, W.z, W.st);
             matvec_z128_kernel<<<rb, 256, 0, s>>>(static_cast<const double2*>(z), W.z, n, W.w, act);
         }
-        pg_dots_kernel<<<nblk, 256, 0, s>>>(W.V, W.w, n, j + 1, W.part, m + 1, cnt, W.h1, act);
-        pg_sub_kernel<<<nblk, 256, 0, s>>>(W.V, W.h1, n, j + 1, W.w, nullptr, cnt, nullptr, act);
-        pg_dots_kernel<<<nblk, 256, 0, s>>>(W.V, W.w, n, j + 1, W.part, m + 1, cnt, W.h2, act);
-        pg_sub_kernel<<<nblk, 256, 0, s>>>(W.V, W.h2, n, j + 1, W.w, W.npart, cnt, &W.st->hn2, act);
-        pg_givens_kernel<<<1, 1, 0, s>>>(W.st, W.g, W.cs, W.sn, W.H, W.h1, W.h2, j);
+        pg_dots_kernel<<<dgrid, 256, 0, s>>>(W.V, W.w, n, j + 1, chunk, W.part, m + 1, cnt, W.h1, act);
+        pg_sub_kernel<<<sblk, 128, 0, s>>>(W.V, W.h1, n, j + 1, W.w, nullptr, cnt, nullptr, act);
+        pg_dots_kernel<<<dgrid, 256, 0, s>>>(W.V, W.w, n, j + 1, chunk, W.part, m + 1, cnt, W.h2, act);
+        pg_sub_kernel<<<sblk, 128, 0, s>>>(W.V, W.h2, n, j + 1, W.w, W.npart, cnt, &W.st->hn2, act);
+        pg_givens_kernel<<<1, 32, 0, s>>>(W.st, W.g, W.cs, W.sn, W.H, W.h1, W.h2, j);
         pg_scale_kernel<<<vb, 256, 0, s>>>(W.w, n, W.st, 1, W.V + (int64_t)(j + 1) * n);
     }
-    pg_backsub_kernel<<<1, 1, 0, s>>>(W.st, W.H, W.g, W.y);
+    pg_backsub_kernel<<<1, 32, 0, s>>>(W.st, W.H, W.g, W.y);
     pg_combine_kernel<<<vb, 256, 0, s>>>(W.V, W.y, W.st, n, W.r);
     pg_update_kernel<<<vb, 256, 0, s>>>(cols, vals, W.r, W.st, n, x);
 }
@@ -1121,10 +1206,11 @@ int pgmres(int kind, const void* z, int64_t n, const int32_t* m_cols, const floa
     if (m < 1 || m > kGmresMaxRestart) return set_error(MB_ERR_ARG, "restart must be in [1, %d]", kGmresMaxRestart);
     if (max_iters < 1) return set_error(MB_ERR_ARG, "max_iters must be >= 1");
     if (!(tol > 0)) return set_error(MB_ERR_ARG, "tol must be > 0");
-    if ((m_cols == nullptr) != (m_vals == nullptr)) return set_error(MB_ERR_ARG, "pgmres: give both m_cols and m_vals, or neither");
+    if ((m_cols == nullptr) != (m_vals == nullptr))
+        return set_error(MB_ERR_ARG, "pgmres: give both m_cols and m_vals, or neither");
     if (ws_bytes < pgmres_workspace_bytes(n, m)) return set_error(MB_ERR_ARG, "workspace too small");
-    if (((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(x)) & 15) != 0)
-        return set_error(MB_ERR_ARG, "pgmres: b and x must be 16-byte aligned");
+    if (((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(z)) & 15) != 0)
+        return set_error(MB_ERR_ARG, "pgmres: z, b and x must be 16-byte aligned");
     PgWork W = pg_carve(workspace, n, m);
     const unsigned vb = (unsigned)((n + 255) / 256);
     const int nblk = (int)std::min<int64_t>(vb, kPgMaxBlocks);
@@ -1133,7 +1219,7 @@ int pgmres(int kind, const void* z, int64_t n, const int32_t* m_cols, const floa
     double2* x2 = reinterpret_cast<double2*>(x);
     unsigned* cnt = &W.st->cnt;
     cudaMemsetAsync(W.st, 0, sizeof(PgState), s);
-    pg_norm2_kernel<<<nblk, 256, 0, s>>>(b2, n, W.npart, cnt, &W.st->bn2, nullptr);
+    pg_norm2_kernel<<<nblk, 256, 0, s>>>(b2, n, W.npart, cnt, &W.st->bn2);
     pg_init_kernel<<<1, 1, 0, s>>>(W.st, tol, max_iters, m);
     int rc = check_launch("pgmres init");
     if (rc) return rc;

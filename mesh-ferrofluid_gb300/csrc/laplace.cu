@@ -130,6 +130,244 @@ __global__ void __launch_bounds__(kLapThreads) laplace_panels_kernel(
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// Tiled form for the separated pairs.  The reference's separated-pair rule is a tensor
+// product (get_rands_and_jacobian_3d, integrations_3d.py:18-60): the x point of rule row
+// g = s Q + t depends on t only, the y point on s only.  A block takes kLapTileRows
+// consecutive y faces x 128 x faces; the y points of its rows and the rule weights times the
+// y shape functions, W[t][s][a] = w_g phi_a(y_s), sit in shared memory, each thread builds the
+// Q x points of its x face once for all rows, and per row sums
+//     out[a][b] = sum_t phi_b(x_t) sum_s f(x_t, y_s) W[t][s][a]
+// (the same terms as the flattened table, summed in another order).  Pairs that share a
+// vertex take the per-pair loop over their relation's table segment.  Coordinates are taken
+// relative to the first vertex of the block's first y face.
+// ---------------------------------------------------------------------------------------
+constexpr int kLapTileRows = 8;
+
+// The per-pair loop of laplace_panels_kernel (relation segment [beg, end)), added into acc.
+template <typename T, int NPHI, int KIND, int LAYER>
+__device__ __forceinline__ void panel_pair_loop(const T* __restrict__ verts, const int32_t* __restrict__ faces,
+                                                const T* __restrict__ normals, const T* __restrict__ tab, int beg,
+                                                int end, int64_t fy, int64_t fx, T k, T* accr, T* acci) {
+    const V3<T> o = load3(verts, __ldg(faces + 3 * fy));
+    const V3<T> Y1 = load3(verts, __ldg(faces + 3 * fy + 1)) - o;
+    const V3<T> Y2 = load3(verts, __ldg(faces + 3 * fy + 2)) - o;
+    const V3<T> X0 = load3(verts, __ldg(faces + 3 * fx)) - o;
+    const V3<T> X1 = load3(verts, __ldg(faces + 3 * fx + 1)) - o;
+    const V3<T> X2 = load3(verts, __ldg(faces + 3 * fx + 2)) - o;
+    const V3<T> ny = load3(normals, fy);
+    for (int t = beg; t < end; ++t) {
+        const T r1x = __ldg(tab + 5 * t), r2x = __ldg(tab + 5 * t + 1);
+        const T r1y = __ldg(tab + 5 * t + 2), r2y = __ldg(tab + 5 * t + 3);
+        const T wj = __ldg(tab + 5 * t + 4);
+        const V3<T> x = (T(1) - r1x) * X0 + (r1x - r2x) * X1 + r2x * X2;
+        const V3<T> y = (r1y - r2y) * Y1 + r2y * Y2;
+        const V3<T> d = x - y;
+        const T r2d = dot(d, d);
+        const T rinv = rsqrt_t(r2d);
+        T fr, fi = 0;
+        if constexpr (LAYER == 1) {
+            fr = rinv;
+        } else {
+            fr = dot(d, ny) * rinv * rinv * rinv;
+        }
+        if constexpr (KIND == 1) {
+            const T R = r2d * rinv;
+            T sn, cs;
+            sincos_turns(k * R * T(kInv2Pi), &sn, &cs);
+            if constexpr (LAYER == 1) {
+                fi = fr * sn;
+                fr = fr * cs;
+            } else {
+                const T kR = k * R;
+                fi = fr * (sn - kR * cs);
+                fr = fr * (cs + kR * sn);
+            }
+        }
+        fr *= wj;
+        fi *= wj;
+        T py[3], px[3];
+        if constexpr (NPHI == 3) {
+            py[0] = T(1) - r1y; py[1] = r1y - r2y; py[2] = r2y;
+            px[0] = T(1) - r1x; px[1] = r1x - r2x; px[2] = r2x;
+        } else {
+            py[0] = T(1); px[0] = T(1);
+        }
+#pragma unroll
+        for (int a = 0; a < NPHI; ++a) {
+#pragma unroll
+            for (int b = 0; b < NPHI; ++b) {
+                accr[a * NPHI + b] += fr * py[a] * px[b];
+                if constexpr (KIND == 1) acci[a * NPHI + b] += fi * py[a] * px[b];
+            }
+        }
+    }
+}
+
+template <typename T, int Q, int NPHI, int KIND, int LAYER>
+__global__ void __launch_bounds__(kLapThreads) laplace_panels_tiled_kernel(
+    const T* __restrict__ verts, const int32_t* __restrict__ faces, const T* __restrict__ areas,
+    const T* __restrict__ normals, const T* __restrict__ tab, int4 seg_lo, int seg_end,
+    const uint8_t* __restrict__ rel, int64_t nf, int64_t row_begin, int64_t row_end, int64_t col_blocks, T k,
+    T* __restrict__ out_r, T* __restrict__ out_i) {
+    constexpr int NN = NPHI * NPHI;
+    constexpr int NC = KIND == 1 ? 2 : 1;
+    __shared__ T s_w[Q][Q][NPHI];          // W[t][s][a]
+    __shared__ T s_rx[Q][2];               // (r1x, r2x) of x point t
+    __shared__ T s_px[Q][NPHI];            // phi_b(x_t)
+    __shared__ T s_y[kLapTileRows][Q][3];  // y points of the tile's rows
+    __shared__ T s_ny[kLapTileRows][3];
+    __shared__ T s_ay[kLapTileRows];
+    __shared__ __align__(16) T s_out[NC][kLapThreads * NN];
+    const int tid = threadIdx.x;
+    const int64_t col_block = (int64_t)blockIdx.x % col_blocks;
+    const int64_t fy0 = row_begin + ((int64_t)blockIdx.x / col_blocks) * kLapTileRows;
+    const int rows = (int)((row_end - fy0) < kLapTileRows ? (row_end - fy0) : kLapTileRows);
+    const int64_t col0 = col_block * kLapThreads;
+    const int64_t fx = col0 + tid;
+    const T* t0 = tab + 5 * seg_lo.x;  // relation-0 rows, g = s Q + t
+    for (int i = tid; i < Q * Q; i += kLapThreads) {
+        const int s = i / Q, t = i - s * Q;
+        const T r1y = __ldg(t0 + 5 * i + 2), r2y = __ldg(t0 + 5 * i + 3), w = __ldg(t0 + 5 * i + 4);
+        if constexpr (NPHI == 3) {
+            s_w[t][s][0] = w * (T(1) - r1y);
+            s_w[t][s][1] = w * (r1y - r2y);
+            s_w[t][s][2] = w * r2y;
+        } else {
+            s_w[t][s][0] = w;
+        }
+        if (s == 0) {
+            const T r1x = __ldg(t0 + 5 * i), r2x = __ldg(t0 + 5 * i + 1);
+            s_rx[t][0] = r1x;
+            s_rx[t][1] = r2x;
+            if constexpr (NPHI == 3) {
+                s_px[t][0] = T(1) - r1x;
+                s_px[t][1] = r1x - r2x;
+                s_px[t][2] = r2x;
+            } else {
+                s_px[t][0] = T(1);
+            }
+        }
+    }
+    const V3<T> o = load3(verts, __ldg(faces + 3 * fy0));
+    for (int i = tid; i < rows * Q; i += kLapThreads) {
+        const int r = i / Q, sq = i - r * Q;
+        const int64_t fy = fy0 + r;
+        const T r1y = __ldg(t0 + 5 * (sq * Q) + 2), r2y = __ldg(t0 + 5 * (sq * Q) + 3);
+        const V3<T> Y0 = load3(verts, __ldg(faces + 3 * fy)) - o;
+        const V3<T> Y1 = load3(verts, __ldg(faces + 3 * fy + 1)) - o;
+        const V3<T> Y2 = load3(verts, __ldg(faces + 3 * fy + 2)) - o;
+        const V3<T> y = (T(1) - r1y) * Y0 + (r1y - r2y) * Y1 + r2y * Y2;
+        s_y[r][sq][0] = y.x;
+        s_y[r][sq][1] = y.y;
+        s_y[r][sq][2] = y.z;
+    }
+    for (int r = tid; r < rows; r += kLapThreads) {
+        const V3<T> n = load3(normals, fy0 + r);
+        s_ny[r][0] = n.x;
+        s_ny[r][1] = n.y;
+        s_ny[r][2] = n.z;
+        s_ay[r] = __ldg(areas + fy0 + r);
+    }
+    __syncthreads();
+    T xp[Q][3];
+    T ax = 0;
+    if (fx < nf) {
+        const V3<T> X0 = load3(verts, __ldg(faces + 3 * fx)) - o;
+        const V3<T> X1 = load3(verts, __ldg(faces + 3 * fx + 1)) - o;
+        const V3<T> X2 = load3(verts, __ldg(faces + 3 * fx + 2)) - o;
+#pragma unroll
+        for (int t = 0; t < Q; ++t) {
+            const T r1x = s_rx[t][0], r2x = s_rx[t][1];
+            const V3<T> x = (T(1) - r1x) * X0 + (r1x - r2x) * X1 + r2x * X2;
+            xp[t][0] = x.x;
+            xp[t][1] = x.y;
+            xp[t][2] = x.z;
+        }
+        ax = __ldg(areas + fx);
+    }
+    const int64_t valid = (nf - col0) < kLapThreads ? (nf - col0) : kLapThreads;
+    for (int r = 0; r < rows; ++r) {
+        const int64_t fy = fy0 + r;
+        T accr[NN], acci[NN];
+#pragma unroll
+        for (int c = 0; c < NN; ++c) { accr[c] = 0; acci[c] = 0; }
+        if (fx < nf) {
+            const int rl = rel ? (int)rel[fy * nf + fx] : relation_of<T>(faces, fy, fx);
+            if (rl == 0) {
+                const T nyx = s_ny[r][0], nyy = s_ny[r][1], nyz = s_ny[r][2];
+#pragma unroll
+                for (int t = 0; t < Q; ++t) {
+                    T ur[NPHI], ui[NPHI];
+#pragma unroll
+                    for (int a = 0; a < NPHI; ++a) { ur[a] = 0; ui[a] = 0; }
+#pragma unroll
+                    for (int sq = 0; sq < Q; ++sq) {
+                        const T dx = xp[t][0] - s_y[r][sq][0], dy = xp[t][1] - s_y[r][sq][1],
+                                dz = xp[t][2] - s_y[r][sq][2];
+                        const T r2d = dx * dx + dy * dy + dz * dz;
+                        const T rinv = rsqrt_t(r2d);
+                        T fr, fi = 0;
+                        if constexpr (LAYER == 1) {
+                            fr = rinv;
+                        } else {
+                            fr = (dx * nyx + dy * nyy + dz * nyz) * rinv * rinv * rinv;
+                        }
+                        if constexpr (KIND == 1) {
+                            const T R = r2d * rinv;
+                            T sn, cs;
+                            sincos_turns(k * R * T(kInv2Pi), &sn, &cs);
+                            if constexpr (LAYER == 1) {
+                                fi = fr * sn;
+                                fr = fr * cs;
+                            } else {
+                                const T kR = k * R;
+                                fi = fr * (sn - kR * cs);
+                                fr = fr * (cs + kR * sn);
+                            }
+                        }
+#pragma unroll
+                        for (int a = 0; a < NPHI; ++a) {
+                            ur[a] += fr * s_w[t][sq][a];
+                            if constexpr (KIND == 1) ui[a] += fi * s_w[t][sq][a];
+                        }
+                    }
+#pragma unroll
+                    for (int a = 0; a < NPHI; ++a) {
+#pragma unroll
+                        for (int b = 0; b < NPHI; ++b) {
+                            accr[a * NPHI + b] += ur[a] * s_px[t][b];
+                            if constexpr (KIND == 1) acci[a * NPHI + b] += ui[a] * s_px[t][b];
+                        }
+                    }
+                }
+            } else {
+                const int beg = rl == 1 ? seg_lo.y : rl == 2 ? seg_lo.z : seg_lo.w;
+                const int end = rl == 1 ? seg_lo.z : rl == 2 ? seg_lo.w : seg_end;
+                panel_pair_loop<T, NPHI, KIND, LAYER>(verts, faces, normals, tab, beg, end, fy, fx, k, accr, acci);
+            }
+            const T scale = T(4) * s_ay[r] * ax * T(kInv4Pi);
+#pragma unroll
+            for (int c = 0; c < NN; ++c) {
+                accr[c] *= scale;
+                acci[c] *= scale;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < NN; ++c) {
+            s_out[0][tid * NN + c] = accr[c];
+            if constexpr (KIND == 1) s_out[NC - 1][tid * NN + c] = acci[c];
+        }
+        __syncthreads();
+        const int64_t base = ((fy - row_begin) * nf + col0) * NN;
+        for (int64_t c = tid; c < valid * NN; c += kLapThreads) {
+            out_r[base + c] = s_out[0][c];
+            if constexpr (KIND == 1) out_i[base + c] = s_out[NC - 1][c];
+        }
+        __syncthreads();
+    }
+}
+
 template <typename T>
 int launch_laplace_panels(const T* verts, const int32_t* faces, int64_t nf, const T* areas,
                           const T* normals, const T* tab, const int* seg, const uint8_t* rel,
@@ -146,6 +384,33 @@ int launch_laplace_panels(const T* verts, const int32_t* faces, int64_t nf, cons
     if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "mesh too large for one launch");
     const int4 lo = make_int4(seg[0], seg[1], seg[2], seg[3]);
     const int se = seg[4];
+    // the tiled kernel when the separated rule is a Q x Q product of a supported size
+    int q = 0;
+    for (int c = 1; c <= 16; ++c)
+        if (c * c == seg[1] - seg[0]) q = c;
+    if (q == 4 || q == 9 || q == 1) {
+        const int64_t tiles = (row_end - row_begin + kLapTileRows - 1) / kLapTileRows;
+        const int64_t tblocks = tiles * col_blocks;
+        if (tblocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "mesh too large for one launch");
+#define MB_LAPT(QQ, NP, KD, LY)                                                                        \
+    laplace_panels_tiled_kernel<T, QQ, NP, KD, LY><<<(unsigned)tblocks, kLapThreads, 0, stream>>>(      \
+        verts, faces, areas, normals, tab, lo, se, rel, nf, row_begin, row_end, col_blocks, (T)k, out_r, out_i)
+#define MB_LAPQ(QQ)                                                                                    \
+    switch ((order == 1 ? 4 : 0) + kind * 2 + (layer - 1)) {                                           \
+        case 0: MB_LAPT(QQ, 1, 0, 1); break;                                                           \
+        case 1: MB_LAPT(QQ, 1, 0, 2); break;                                                           \
+        case 2: MB_LAPT(QQ, 1, 1, 1); break;                                                           \
+        case 3: MB_LAPT(QQ, 1, 1, 2); break;                                                           \
+        case 4: MB_LAPT(QQ, 3, 0, 1); break;                                                           \
+        case 5: MB_LAPT(QQ, 3, 0, 2); break;                                                           \
+        case 6: MB_LAPT(QQ, 3, 1, 1); break;                                                           \
+        case 7: MB_LAPT(QQ, 3, 1, 2); break;                                                           \
+    }
+        if (q == 1) { MB_LAPQ(1) } else if (q == 4) { MB_LAPQ(4) } else { MB_LAPQ(9) }
+#undef MB_LAPQ
+#undef MB_LAPT
+        return check_launch("laplace_panels_tiled");
+    }
 #define MB_LAP(NP, KD, LY)                                                                          \
     laplace_panels_kernel<T, NP, KD, LY><<<(unsigned)blocks, kLapThreads, 0, stream>>>(             \
         verts, faces, areas, normals, tab, lo, se, rel, nf, row_begin, col_blocks, (T)k, out_r, out_i)

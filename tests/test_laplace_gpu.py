@@ -63,13 +63,14 @@ def test_panels_relation_derived_on_device(pkg, cuda, golden):
 
 @pytest.mark.parametrize("layer", [1, 2])
 @pytest.mark.parametrize("order", [0, 1])
-def test_panels_f32_vs_oracle(pkg, cuda, oracle, layer, order):
+@pytest.mark.parametrize("gq", [2, 3])
+def test_panels_f32_vs_oracle(pkg, cuda, oracle, layer, order, gq):
     v_np, f_np = pkg.meshes.ellipsoid(2, jitter=0.02, seed=1)
     v = torch.tensor(v_np, dtype=torch.float32, device=cuda)
     f = torch.tensor(f_np, dtype=torch.int32, device=cuda)
     a = pkg.utils.compute_face_areas(v, f).contiguous()
     n = pkg.utils.compute_face_normals(v, f).contiguous()
-    p, w1 = pkg.utils.get_gaussion_integration_points_and_weights(3, device=cuda)
+    p, w1 = pkg.utils.get_gaussion_integration_points_and_weights(gq, device=cuda)
     rands, w = pkg.utils.collapsed_rule_2d(p, w1)
     rel = pkg.utils.compute_panel_relation(f)
     out = pkg.double_integration_on_panels_3d(0, order, v, f, a, n, w, w, rands, rands, rel, 1.0, layer)
@@ -115,3 +116,28 @@ def test_solve_f64_matches_reference(pkg, cuda, golden, name, gq, order):
     assert rel_err(solver.rhs_layer.get_rhs_vec().cpu().numpy(), g[f"{tag}_rhs"]) < 1e-10
     assert rel_err(neu.cpu().numpy(), g[f"{tag}_neumann"]) < 1e-9
     assert rel_err(dirv.cpu().numpy(), g[f"{tag}_dirichlet"]) == 0.0
+
+
+@pytest.mark.parametrize("gq", [2, 3])
+def test_panels_row_window_equals_full(pkg, cuda, gq):
+    """Rows [3, 250) through the C ABI equal the same rows of the whole matrix (the tiled kernel
+    takes its tiles from the window's first row)."""
+    v_np, f_np = pkg.meshes.icosphere(2)
+    v = torch.tensor(v_np, dtype=torch.float32, device=cuda)
+    f = torch.tensor(f_np, dtype=torch.int32, device=cuda)
+    a = pkg.utils.compute_face_areas(v, f).contiguous()
+    n = pkg.utils.compute_face_normals(v, f).contiguous()
+    p, w1 = pkg.utils.get_gaussion_integration_points_and_weights(gq, device=cuda)
+    rands, w = pkg.utils.collapsed_rule_2d(p, w1)
+    full = pkg.double_integration_on_panels_3d(0, 1, v, f, a, n, w, w, rands, rands, None, 1.0, 2)
+    table, seg = pkg.layers._cached_rule_table(rands, rands, w, w, torch.float32, cuda)
+    seg_c = np.asarray(seg, dtype=np.int32)
+    nf = f.shape[0]
+    r0, r1 = 3, 250
+    win = torch.full((r1 - r0, nf, 3, 3), float("nan"), dtype=torch.float32, device=cuda)
+    L = pkg._lib
+    L.call("mb_laplace_panels_f32", L.ptr(v), v.shape[0], L.ptr(f), nf, L.ptr(a), L.ptr(n), L.ptr(table),
+           seg_c.ctypes.data_as(__import__("ctypes").c_void_p), None, 2, 1, 0, 1.0, r0, r1, L.ptr(win), None,
+           L.stream_of(v))
+    torch.cuda.synchronize()
+    assert rel_err(win.cpu().numpy(), full[r0:r1].cpu().numpy()) < 1e-6
