@@ -484,21 +484,33 @@ int mb_spai_apply_c64(const int32_t* m_cols, const float* m_vals, int64_t n, con
 /* GMRES(restart) on Z x = b with the right preconditioner M (m_cols / m_vals from
  * mb_spai_build_c64, or both NULL for none): each restart cycle starts from the refinement
  * residual b - Z x, solves (Z M) u = r and adds M u to x.  The whole cycle runs on the device
- * (CGS2 Arnoldi on a complex128 basis, Givens rotations, the residual estimate and the back
- * substitution in kernels; deterministic block reductions); use_graph = 1 captures it once as
- * a CUDA graph and replays it.  The host reads the solver state once per cycle.
- * mb_pgmres_c64: Z interleaved complex64 [n, n], FP32 products, the refinement residual by
- * compensated FP32 dot products (exact products and sums, ~1e-13 of sum |Z_ij x_j|);
- * mb_pgmres_c128: Z interleaved complex128, FP64 products and residual.  z, b, x 16-byte
- * aligned; b, x complex128 [n] (x: initial guess in, solution out).  info as for
- * mb_gmres_c64.  Workspace: mb_pgmres_workspace_bytes(n, restart) bytes. */
+ * (CGS2 Arnoldi, Givens rotations, the residual estimate and the back substitution in
+ * kernels; Hessenberg matrix, rotations and x in FP64; deterministic block reductions);
+ * use_graph = 1 captures it once as a CUDA graph and replays it.  The host reads the solver
+ * state once per cycle.
+ * mb_pgmres_c64: Z interleaved complex64 [n, n]; FP32 products, complex64 Krylov basis with
+ * FP32 Gram-Schmidt products and FP64 sums; the refinement residual by compensated FP32 dot
+ * products (exact products and sums, ~1e-13 of sum |Z_ij x_j|).  With z_half (from
+ * mb_half_copy_c64) and half_scale, the Arnoldi products read the half-precision copy instead,
+ * each cycle ends once its residual estimate has dropped by inner_rtol (e.g. 3e-3; the copy's
+ * ~2e-4 relative error bounds what one cycle can gain) and the next cycle restarts from the
+ * complex64 residual; pass NULL, NULL, 0 to use Z itself.
+ * mb_pgmres_c128: Z interleaved complex128; FP64 products, basis and residual.  z, b, x (and
+ * z_half) 16-byte aligned; b, x complex128 [n] (x: initial guess in, solution out).  info as
+ * for mb_gmres_c64.  Workspace: mb_pgmres_workspace_bytes(n, restart) bytes. */
 size_t mb_pgmres_workspace_bytes(int64_t n, int restart);
-int mb_pgmres_c64(const float* z, int64_t n, const int32_t* m_cols, const float* m_vals, const double* b, double* x,
-                  int restart, int max_iters, double tol, int use_graph, void* workspace, size_t workspace_bytes,
-                  mb_gmres_info* info, void* stream);
+int mb_pgmres_c64(const float* z, int64_t n, const void* z_half, const float* half_scale, double inner_rtol,
+                  const int32_t* m_cols, const float* m_vals, const double* b, double* x, int restart, int max_iters,
+                  double tol, int use_graph, void* workspace, size_t workspace_bytes, mb_gmres_info* info,
+                  void* stream);
 int mb_pgmres_c128(const double* z, int64_t n, const int32_t* m_cols, const float* m_vals, const double* b,
                    double* x, int restart, int max_iters, double tol, int use_graph, void* workspace,
                    size_t workspace_bytes, mb_gmres_info* info, void* stream);
+/* Half-precision copy for mb_pgmres_c64: *scale (device float) = max |Re|, |Im| over the
+ * complex64 array z (count complex entries, count even, z 16-byte aligned), and z_half
+ * (count pairs of IEEE binary16, interleaved like z, 8-byte aligned) = z / *scale rounded to
+ * nearest (magnitudes below 2^-24 of the scale, the smallest binary16 subnormal, become 0). */
+int mb_half_copy_c64(const float* z, int64_t count, void* z_half, float* scale, void* stream);
 
 /* ---- Laplace / Helmholtz-BEM layers ------------------------------------------------- */
 

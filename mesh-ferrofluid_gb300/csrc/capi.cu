@@ -145,9 +145,11 @@ int spai_build(const float* verts, const int32_t* faces, const int32_t* fei, con
 int spai_status(const void* ws, int64_t total_edges, int32_t* out, cudaStream_t s);
 int spai_apply_c64(const int32_t* m_cols, const float* m_vals, int64_t n, const float* v, float* y, cudaStream_t s);
 size_t pgmres_workspace_bytes(int64_t n, int m);
-int pgmres(int kind, const void* z, int64_t n, const int32_t* m_cols, const float* m_vals, const double* b,
-           double* x, int m, int max_iters, double tol, bool use_graph, void* workspace, size_t ws_bytes,
-           int64_t* iters_out, int64_t* cycles_out, double* relres_out, int* status_out, cudaStream_t s);
+int pgmres(int kind, const void* z, const void* z_half, const float* half_scale, double inner_rtol, int64_t n,
+           const int32_t* m_cols, const float* m_vals, const double* b, double* x, int m, int max_iters, double tol,
+           bool use_graph, void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out,
+           double* relres_out, int* status_out, cudaStream_t s);
+int half_copy_c64(const float* z, int64_t count, void* zh, float* scale, cudaStream_t s);
 int gmres_c64_noalloc(const float*, int64_t, const double*, double*, int, int, double, int64_t*, int64_t*,
                       double*, int*, cudaStream_t);
 int launch_matvec_c64(const float*, const float*, int64_t, double*, cudaStream_t);
@@ -886,14 +888,15 @@ size_t mb_pgmres_workspace_bytes(int64_t n, int restart) {
     return (n > 0 && restart > 0) ? pgmres_workspace_bytes(n, restart) : 0;
 }
 
-static int pgmres_entry(int kind, const void* z, int64_t n, const int32_t* m_cols, const float* m_vals,
-                        const double* b, double* x, int restart, int max_iters, double tol, int use_graph,
-                        void* workspace, size_t workspace_bytes, mb_gmres_info* info, void* stream) {
+static int pgmres_entry(int kind, const void* z, const void* z_half, const float* half_scale, double inner_rtol,
+                        int64_t n, const int32_t* m_cols, const float* m_vals, const double* b, double* x,
+                        int restart, int max_iters, double tol, int use_graph, void* workspace,
+                        size_t workspace_bytes, mb_gmres_info* info, void* stream) {
     int64_t it = 0, cyc = 0;
     double rr = 0.0;
     int st = 1;
-    const int rc = pgmres(kind, z, n, m_cols, m_vals, b, x, restart, max_iters, tol, use_graph != 0, workspace,
-                          workspace_bytes, &it, &cyc, &rr, &st, as_stream(stream));
+    const int rc = pgmres(kind, z, z_half, half_scale, inner_rtol, n, m_cols, m_vals, b, x, restart, max_iters, tol,
+                          use_graph != 0, workspace, workspace_bytes, &it, &cyc, &rr, &st, as_stream(stream));
     if (rc == MB_OK && info) {
         info->iterations = it;
         info->restarts = cyc;
@@ -904,18 +907,23 @@ static int pgmres_entry(int kind, const void* z, int64_t n, const int32_t* m_col
     return rc;
 }
 
-int mb_pgmres_c64(const float* z, int64_t n, const int32_t* m_cols, const float* m_vals, const double* b, double* x,
-                  int restart, int max_iters, double tol, int use_graph, void* workspace, size_t workspace_bytes,
-                  mb_gmres_info* info, void* stream) {
-    return pgmres_entry(0, z, n, m_cols, m_vals, b, x, restart, max_iters, tol, use_graph, workspace,
-                        workspace_bytes, info, stream);
+int mb_pgmres_c64(const float* z, int64_t n, const void* z_half, const float* half_scale, double inner_rtol,
+                  const int32_t* m_cols, const float* m_vals, const double* b, double* x, int restart, int max_iters,
+                  double tol, int use_graph, void* workspace, size_t workspace_bytes, mb_gmres_info* info,
+                  void* stream) {
+    return pgmres_entry(0, z, z_half, half_scale, inner_rtol, n, m_cols, m_vals, b, x, restart, max_iters, tol,
+                        use_graph, workspace, workspace_bytes, info, stream);
 }
 
 int mb_pgmres_c128(const double* z, int64_t n, const int32_t* m_cols, const float* m_vals, const double* b,
                    double* x, int restart, int max_iters, double tol, int use_graph, void* workspace,
                    size_t workspace_bytes, mb_gmres_info* info, void* stream) {
-    return pgmres_entry(1, z, n, m_cols, m_vals, b, x, restart, max_iters, tol, use_graph, workspace,
-                        workspace_bytes, info, stream);
+    return pgmres_entry(1, z, nullptr, nullptr, 0.0, n, m_cols, m_vals, b, x, restart, max_iters, tol, use_graph,
+                        workspace, workspace_bytes, info, stream);
+}
+
+int mb_half_copy_c64(const float* z, int64_t count, void* z_half, float* scale, void* stream) {
+    return half_copy_c64(z, count, z_half, scale, as_stream(stream));
 }
 
 int mb_panel_relation(const int32_t* faces, int64_t n_faces, uint8_t* relations, void* stream) {

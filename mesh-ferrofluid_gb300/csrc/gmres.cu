@@ -13,6 +13,7 @@
 // Each restart cycle starts from the FP64 residual, so the inner FP32 matvec limits only
 // the per-cycle reduction, not the final accuracy (GMRES with iterative refinement).
 // Every loop is bounded by max_iters; nothing waits on the device except cudaStreamSynchronize.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -663,28 +664,35 @@ int launch_residual_c128(const float* z, const double* x, const double* b, int64
 //
 // Right preconditioning with the sparse approximate inverse M (spai.cu): each cycle solves
 // (Z M) u = r0 and updates x += M u, so the residual GMRES minimises is the residual of
-// Z x = b itself.  Arnoldi by CGS2 on a complex128 basis with FP64 sums; the Givens
-// rotations, the residual estimate, the stopping test and the back substitution run in
-// one-warp kernels on a device state record; every cycle starts from the refinement
-// residual b - Z x.  Sums over the vector run as block partials that the last block to
-// finish adds in a fixed order (deterministic, no FP64 atomics).  A cycle is a fixed
-// sequence of launches: once the state says the cycle has ended, the remaining steps'
-// launches return at once.  With use_graph the cycle is captured once as a CUDA graph and
-// replayed; the host reads the state once per cycle.
+// Z x = b itself.  Every cycle starts from the refinement residual b - Z x; the Hessenberg
+// matrix, the Givens rotations, the residual estimate, the stopping test, the back
+// substitution and x stay in FP64, in one-warp kernels on a device state record.  Sums over
+// the vector run as block partials that the last block to finish adds in a fixed order
+// (deterministic, no FP64 atomics).  A cycle is a fixed sequence of launches: once the state
+// says the cycle has ended, the remaining steps' launches return at once.  With use_graph the
+// cycle is captured once as a CUDA graph and replayed; the host reads the state once per
+// cycle.
 //
-// complex64 Z (FP32 products): the refinement residual is a compensated FP32 dot product
-// -- x split into FP32 hi + lo parts, each product Z_ij x_hi,j made exact by TwoProduct
-// (mul + fma), sums kept exact by TwoSum, the rounding terms and the x_lo products summed
-// beside them, lane sums combined in FP64 -- accurate to ~1e-13 of sum |Z_ij x_j| at FP32
-// instruction speed (GB300's FP64 rate would make an FP64 residual ~10x slower than a
-// matrix pass).  complex128 Z (FP64 products, FP64 residual): the FP64 reference solution of
-// the same discretisation.
+// Three matrix kinds:
+//   0  complex64 Z: FP32 products; the Krylov basis is complex64 and the Gram-Schmidt
+//      products run in FP32 with FP64 sums across lanes and blocks (GB300's FP64 rate would
+//      make FP64 Gram-Schmidt a third of a step); the refinement residual is a compensated
+//      FP32 dot product -- x split into FP32 hi + lo parts, each product Z_ij x_hi,j made
+//      exact by TwoProduct (mul + fma), running sums kept exact by TwoSum, the rounding terms
+//      and the x_lo products summed beside them, lane sums combined in FP64 -- accurate to
+//      ~1e-13 of sum |Z_ij x_j| at FP32 instruction speed.
+//   1  complex128 Z: FP64 products, basis and residual (the FP64 reference solution of the
+//      same discretisation).
+//   2  as 0, but the Arnoldi products read a half-precision copy of Z (complex FP16 scaled by
+//      max |Re, Im Z|, half the bytes of complex64): each inner cycle stops once its residual
+//      estimate has dropped by inner_rtol (the copy's ~2e-4 relative error bounds what one
+//      cycle can gain) and the next cycle restarts from the complex64 refinement residual.
 // ---------------------------------------------------------------------------------------
 constexpr int kPgMaxBlocks = 256;
 constexpr int kPgRowsPerBlock = 8;   // warps per block in the one-warp-per-row kernels
 
 struct PgState {
-    double bn2, bnorm, rn2, beta, relres, tol, hn2, hn;
+    double bn2, bnorm, rn2, beta, relres, tol, hn2, hn, inner_rtol;
     long long iters, max_iters, cycles;
     int m, jdone, active, converged;
     unsigned int cnt;
@@ -692,10 +700,10 @@ struct PgState {
 };
 
 struct PgWork {
-    double2* V;     // [(m+1), n]
-    double2* w;     // [n]
+    void* V;        // [(m+1), n] basis (complex64 for kinds 0 and 2, complex128 for kind 1)
+    void* w;        // [n] product / new basis vector (same type as V)
     double2* r;     // [n] residual, then the cycle's update V y
-    double2* z;     // [n] M v (float2 view for the FP32 product); x split (float4) at cycle start
+    double2* z;     // [n] M v (float2 view for kinds 0, 2); x split (float4) at cycle start
     double2* part;  // [blocks, m+1] block partials
     double* npart;  // [blocks]
     PgState* st;
@@ -718,9 +726,9 @@ size_t pgmres_workspace_bytes(int64_t n, int m) {
 static PgWork pg_carve(void* ws, int64_t n, int m) {
     char* p = static_cast<char*>(ws);
     PgWork w;
-    w.V = reinterpret_cast<double2*>(p);
+    w.V = p;
     p += al256(16 * (size_t)(m + 1) * n);
-    w.w = reinterpret_cast<double2*>(p);
+    w.w = p;
     p += al256(16 * (size_t)n);
     w.r = reinterpret_cast<double2*>(p);
     p += al256(16 * (size_t)n);
@@ -760,6 +768,20 @@ __device__ __forceinline__ double2 cdiv(double2 a, double2 d) {
 }
 __device__ __forceinline__ double cabs2(double2 a) { return a.x * a.x + a.y * a.y; }
 
+// basis element type helpers: B = float2 (FP32 arithmetic) or double2 (FP64)
+template <typename B>
+struct PgB;
+template <>
+struct PgB<float2> {
+    using S = float;
+    static __device__ __forceinline__ float2 make(double re, double im) { return make_float2((float)re, (float)im); }
+};
+template <>
+struct PgB<double2> {
+    using S = double;
+    static __device__ __forceinline__ double2 make(double re, double im) { return make_double2(re, im); }
+};
+
 // Adds the blocks' partials npart[0..nblocks) in a fixed order into *out once every block
 // has written its own; the counter is left at zero for the next launch.
 __device__ __forceinline__ void pg_last_block_sum(double* npart, unsigned* cnt, double* out, unsigned nblocks) {
@@ -797,10 +819,11 @@ __global__ void __launch_bounds__(256) pg_norm2_kernel(const double2* __restrict
     pg_last_block_sum(npart, cnt, out, gridDim.x);
 }
 
-__global__ void pg_init_kernel(PgState* st, double tol, long long max_iters, int m) {
+__global__ void pg_init_kernel(PgState* st, double tol, long long max_iters, int m, double inner_rtol) {
     const double b = sqrt(st->bn2);
     st->bnorm = b > 0.0 ? b : 1.0;
     st->tol = tol;
+    st->inner_rtol = inner_rtol;
     st->max_iters = max_iters;
     st->m = m;
     st->iters = 0;
@@ -828,49 +851,148 @@ __global__ void pg_cycle_start_kernel(PgState* st, double2* g) {
     for (int i = 1; i <= st->m; ++i) g[i] = make_double2(0.0, 0.0);
 }
 
-// dst = src * s, s = 1 / beta (which = 0) or 1 / h_{j+1,j} (which = 1); only while active
-__global__ void pg_scale_kernel(const double2* __restrict__ src, int64_t n, const PgState* __restrict__ st, int which,
-                                double2* __restrict__ dst) {
+// V_0 = r / beta (r complex128)
+template <typename B>
+__global__ void pg_start_basis_kernel(const double2* __restrict__ r, int64_t n, const PgState* __restrict__ st,
+                                      B* __restrict__ v0) {
     if (!st->active) return;
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const double s = 1.0 / (which ? st->hn : st->beta);
-    const double2 v = src[k];
-    dst[k] = make_double2(v.x * s, v.y * s);
+    const double s = 1.0 / st->beta;
+    v0[k] = PgB<B>::make(r[k].x * s, r[k].y * s);
 }
 
-// z = M v, one warp per row (lanes over the row's pattern, FP64 sums): complex64 output for the
-// FP32 product (F32 = true) or complex128 for the FP64 product.
-template <bool F32>
+// V_{j+1} = w / h_{j+1,j}
+template <typename B>
+__global__ void pg_scale_kernel(const B* __restrict__ w, int64_t n, const PgState* __restrict__ st,
+                                B* __restrict__ dst) {
+    if (!st->active) return;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    using S = typename PgB<B>::S;
+    const S s = (S)(1.0 / st->hn);
+    const B v = w[k];
+    B o;
+    o.x = v.x * s;
+    o.y = v.y * s;
+    dst[k] = o;
+}
+
+// z = M v, one warp per row (lanes over the row's pattern), in the basis' precision with the
+// lane sums combined in FP64; z has the basis' type.
+template <typename B>
 __global__ void __launch_bounds__(256) pg_precond_kernel(const int32_t* __restrict__ cols,
                                                          const float2* __restrict__ vals, int64_t n,
-                                                         const double2* __restrict__ v, double2* __restrict__ z,
+                                                         const B* __restrict__ v, B* __restrict__ z,
                                                          const PgState* __restrict__ st) {
     if (!st->active) return;
+    using S = typename PgB<B>::S;
     const int64_t row = (int64_t)blockIdx.x * kPgRowsPerBlock + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (row >= n) return;
-    double2 acc = make_double2(0.0, 0.0);
-    if (cols) {
+    if (!cols) {
+        if (lane == 0) z[row] = v[row];
+        return;
+    }
+    S ar = 0, ai = 0;
 #pragma unroll
-        for (int q = lane; q < MB_SPAI_WIDTH; q += 32) {
-            const int32_t c = __ldg(cols + row * MB_SPAI_WIDTH + q);
-            if (c >= 0) {
-                const float2 mq = __ldg(vals + row * MB_SPAI_WIDTH + q);
-                const double2 x = __ldg(v + c);
-                acc.x = fma((double)mq.x, x.x, fma(-(double)mq.y, x.y, acc.x));
-                acc.y = fma((double)mq.x, x.y, fma((double)mq.y, x.x, acc.y));
-            }
+    for (int q = lane; q < MB_SPAI_WIDTH; q += 32) {
+        const int32_t c = __ldg(cols + row * MB_SPAI_WIDTH + q);
+        if (c >= 0) {
+            const float2 mq = __ldg(vals + row * MB_SPAI_WIDTH + q);
+            const B x = v[c];
+            ar += (S)mq.x * x.x - (S)mq.y * x.y;
+            ai += (S)mq.x * x.y + (S)mq.y * x.x;
         }
-        acc.x = warp_sum(acc.x);
-        acc.y = warp_sum(acc.y);
-    } else if (lane == 0) {
-        acc = v[row];
     }
-    if (lane == 0) {
-        if (F32) reinterpret_cast<float2*>(z)[row] = make_float2((float)acc.x, (float)acc.y);
-        else z[row] = acc;
+    const double sr = warp_sum((double)ar), si = warp_sum((double)ai);
+    if (lane == 0) z[row] = PgB<B>::make(sr, si);
+}
+
+// w = Z v with Z complex64, v complex64: FP32 products, FP64 lane combination, complex64 w
+__global__ void __launch_bounds__(256) pg_matvec_c64_kernel(const float* __restrict__ z, const float2* __restrict__ v,
+                                                            int64_t n, float2* __restrict__ w,
+                                                            const int* __restrict__ active) {
+    const int64_t row = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n || !*active) return;
+    const float* zr = z + 2 * row * n;
+    float ar = 0.f, ai = 0.f;
+    if ((n & 1) == 0 && (reinterpret_cast<uintptr_t>(zr) & 15) == 0) {
+        const float4* z4 = reinterpret_cast<const float4*>(zr);
+        const float4* v4 = reinterpret_cast<const float4*>(v);
+        const int64_t npair = n >> 1;
+        int64_t p = lane;
+#define MB_PGMAC(A, B)                         \
+    ar = fmaf(A.x, B.x, fmaf(-A.y, B.y, ar));  \
+    ai = fmaf(A.x, B.y, fmaf(A.y, B.x, ai));   \
+    ar = fmaf(A.z, B.z, fmaf(-A.w, B.w, ar));  \
+    ai = fmaf(A.z, B.w, fmaf(A.w, B.z, ai));
+        for (; p + 96 < npair; p += 128) {
+            const float4 a0 = __ldcs(z4 + p), a1 = __ldcs(z4 + p + 32), a2 = __ldcs(z4 + p + 64),
+                         a3 = __ldcs(z4 + p + 96);
+            const float4 b0 = __ldg(v4 + p), b1 = __ldg(v4 + p + 32), b2 = __ldg(v4 + p + 64),
+                         b3 = __ldg(v4 + p + 96);
+            MB_PGMAC(a0, b0) MB_PGMAC(a1, b1) MB_PGMAC(a2, b2) MB_PGMAC(a3, b3)
+        }
+        for (; p < npair; p += 32) {
+            const float4 a0 = __ldcs(z4 + p), b0 = __ldg(v4 + p);
+            MB_PGMAC(a0, b0)
+        }
+#undef MB_PGMAC
+    } else {
+        const float2* z2 = reinterpret_cast<const float2*>(zr);
+        for (int64_t j = lane; j < n; j += 32) {
+            const float2 a = __ldcs(z2 + j), b = __ldg(v + j);
+            ar = fmaf(a.x, b.x, fmaf(-a.y, b.y, ar));
+            ai = fmaf(a.x, b.y, fmaf(a.y, b.x, ai));
+        }
     }
+    const double sr = warp_sum((double)ar), si = warp_sum((double)ai);
+    if (lane == 0) w[row] = make_float2((float)sr, (float)si);
+}
+
+// w = scale * Zh v with Zh the complex FP16 copy (interleaved half pairs), v complex64
+__global__ void __launch_bounds__(256) pg_matvec_h16_kernel(const __half2* __restrict__ zh,
+                                                            const float* __restrict__ scale,
+                                                            const float2* __restrict__ v, int64_t n,
+                                                            float2* __restrict__ w, const int* __restrict__ active) {
+    const int64_t row = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n || !*active) return;
+    const __half2* zr = zh + row * n;
+    float ar = 0.f, ai = 0.f;
+    if ((n & 3) == 0 && (reinterpret_cast<uintptr_t>(zr) & 15) == 0) {
+        // four complex entries per 16-byte load
+        const uint4* z16 = reinterpret_cast<const uint4*>(zr);
+        const float4* v4 = reinterpret_cast<const float4*>(v);
+        const int64_t nq = n >> 2;
+        for (int64_t p = lane; p < nq; p += 32) {
+            const uint4 a = __ldcs(z16 + p);
+            const float4 b0 = __ldg(v4 + 2 * p), b1 = __ldg(v4 + 2 * p + 1);
+            const float2 z0 = __half22float2(*reinterpret_cast<const __half2*>(&a.x));
+            const float2 z1 = __half22float2(*reinterpret_cast<const __half2*>(&a.y));
+            const float2 z2 = __half22float2(*reinterpret_cast<const __half2*>(&a.z));
+            const float2 z3 = __half22float2(*reinterpret_cast<const __half2*>(&a.w));
+            ar = fmaf(z0.x, b0.x, fmaf(-z0.y, b0.y, ar));
+            ai = fmaf(z0.x, b0.y, fmaf(z0.y, b0.x, ai));
+            ar = fmaf(z1.x, b0.z, fmaf(-z1.y, b0.w, ar));
+            ai = fmaf(z1.x, b0.w, fmaf(z1.y, b0.z, ai));
+            ar = fmaf(z2.x, b1.x, fmaf(-z2.y, b1.y, ar));
+            ai = fmaf(z2.x, b1.y, fmaf(z2.y, b1.x, ai));
+            ar = fmaf(z3.x, b1.z, fmaf(-z3.y, b1.w, ar));
+            ai = fmaf(z3.x, b1.w, fmaf(z3.y, b1.z, ai));
+        }
+    } else {
+        for (int64_t j = lane; j < n; j += 32) {
+            const float2 a = __half22float2(zr[j]), b = __ldg(v + j);
+            ar = fmaf(a.x, b.x, fmaf(-a.y, b.y, ar));
+            ai = fmaf(a.x, b.y, fmaf(a.y, b.x, ai));
+        }
+    }
+    const double s = (double)*scale;
+    const double sr = warp_sum((double)ar), si = warp_sum((double)ai);
+    if (lane == 0) w[row] = make_float2((float)(sr * s), (float)(si * s));
 }
 
 // y = Z v in FP64 with Z complex128 [n, n]; one warp per row
@@ -970,35 +1092,38 @@ __global__ void __launch_bounds__(256) residual_c64x_kernel(const float2* __rest
 }
 
 // h[i] = sum_k conj(V_i[k]) w[k] for i < nb: block (c, g) has warp w on row i = 8 g + w over
-// chunk c; the last block to finish adds the chunks of every row in a fixed order.
-__global__ void __launch_bounds__(256) pg_dots_kernel(const double2* __restrict__ V, const double2* __restrict__ w,
-                                                      int64_t n, int nb, int64_t chunk, double2* __restrict__ part,
-                                                      int ldp, unsigned* cnt, double2* __restrict__ h,
+// chunk c (products and lane sums in the basis' precision, lanes combined in FP64); the last
+// block to finish adds the chunks of every row in a fixed order (a warp per row, lanes over
+// chunks).
+template <typename B>
+__global__ void __launch_bounds__(256) pg_dots_kernel(const B* __restrict__ V, const B* __restrict__ w, int64_t n,
+                                                      int nb, int64_t chunk, double2* __restrict__ part, int ldp,
+                                                      unsigned* cnt, double2* __restrict__ h,
                                                       const int* __restrict__ active) {
     if (!*active) return;
+    using S = typename PgB<B>::S;
     __shared__ bool s_last;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.y * 8 + warp;
     const int64_t k0 = (int64_t)blockIdx.x * chunk;
     const int64_t k1 = k0 + chunk < n ? k0 + chunk : n;
     if (i < nb) {
-        const double2* vi = V + (int64_t)i * n;
-        double ar0 = 0.0, ai0 = 0.0, ar1 = 0.0, ai1 = 0.0;
+        const B* vi = V + (int64_t)i * n;
+        S ar0 = 0, ai0 = 0, ar1 = 0, ai1 = 0;
         int64_t k = k0 + lane;
         for (; k + 32 < k1; k += 64) {
-            const double2 a0 = vi[k], a1 = vi[k + 32], b0 = w[k], b1 = w[k + 32];
-            const double2 p0 = cconjmul(a0, b0), p1 = cconjmul(a1, b1);
-            ar0 += p0.x;
-            ai0 += p0.y;
-            ar1 += p1.x;
-            ai1 += p1.y;
+            const B a0 = vi[k], a1 = vi[k + 32], b0 = w[k], b1 = w[k + 32];
+            ar0 += a0.x * b0.x + a0.y * b0.y;
+            ai0 += a0.x * b0.y - a0.y * b0.x;
+            ar1 += a1.x * b1.x + a1.y * b1.y;
+            ai1 += a1.x * b1.y - a1.y * b1.x;
         }
         if (k < k1) {
-            const double2 p0 = cconjmul(vi[k], w[k]);
-            ar0 += p0.x;
-            ai0 += p0.y;
+            const B a0 = vi[k], b0 = w[k];
+            ar0 += a0.x * b0.x + a0.y * b0.y;
+            ai0 += a0.x * b0.y - a0.y * b0.x;
         }
-        const double ar = warp_sum(ar0 + ar1), ai = warp_sum(ai0 + ai1);
+        const double ar = warp_sum((double)ar0 + (double)ar1), ai = warp_sum((double)ai0 + (double)ai1);
         if (lane == 0) part[(int64_t)blockIdx.x * ldp + i] = make_double2(ar, ai);
     }
     __threadfence();
@@ -1006,48 +1131,54 @@ __global__ void __launch_bounds__(256) pg_dots_kernel(const double2* __restrict_
     if (threadIdx.x == 0) s_last = atomicAdd(cnt, 1u) == gridDim.x * gridDim.y - 1;
     __syncthreads();
     if (!s_last) return;
-    for (int ii = threadIdx.x; ii < nb; ii += blockDim.x) {
+    for (int ii = warp; ii < nb; ii += 8) {
         double sr = 0.0, si = 0.0;
-        for (unsigned c = 0; c < gridDim.x; ++c) {
+        for (unsigned c = lane; c < gridDim.x; c += 32) {
             const double2 p = __ldcg(part + (int64_t)c * ldp + ii);
             sr += p.x;
             si += p.y;
         }
-        h[ii] = make_double2(sr, si);
+        sr = warp_sum(sr);
+        si = warp_sum(si);
+        if (lane == 0) h[ii] = make_double2(sr, si);
     }
     if (threadIdx.x == 0) *cnt = 0;
 }
 
-// w -= sum_{i<nb} V_i h_i (one element per thread, the sum over i unrolled by four); with
-// npart, also |w|^2 into *hn2 (block partials + last block).
-__global__ void __launch_bounds__(128) pg_sub_kernel(const double2* __restrict__ V, const double2* __restrict__ h,
-                                                     int64_t n, int nb, double2* __restrict__ w,
-                                                     double* __restrict__ npart, unsigned* cnt, double* hn2,
-                                                     const int* __restrict__ active) {
+// w -= sum_{i<nb} V_i h_i in the basis' precision (one element per thread, the sum over i
+// unrolled by four); with npart, also |w|^2 into *hn2 (FP64 block partials + last block).
+template <typename B>
+__global__ void __launch_bounds__(128) pg_sub_kernel(const B* __restrict__ V, const double2* __restrict__ h, int64_t n,
+                                                     int nb, B* __restrict__ w, double* __restrict__ npart,
+                                                     unsigned* cnt, double* hn2, const int* __restrict__ active) {
     if (!*active) return;
-    __shared__ double2 sh[kGmresMaxRestart + 1];
+    using S = typename PgB<B>::S;
+    __shared__ B sh[kGmresMaxRestart + 1];
     __shared__ double s[4];
-    for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = h[i];
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = PgB<B>::make(h[i].x, h[i].y);
     __syncthreads();
     double a = 0.0;
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-        double2 x = w[k];
+        B x = w[k];
         int i = 0;
         for (; i + 4 <= nb; i += 4) {
-            const double2 v0 = V[(int64_t)i * n + k], v1 = V[(int64_t)(i + 1) * n + k];
-            const double2 v2 = V[(int64_t)(i + 2) * n + k], v3 = V[(int64_t)(i + 3) * n + k];
-            const double2 p0 = cmul(v0, sh[i]), p1 = cmul(v1, sh[i + 1]), p2 = cmul(v2, sh[i + 2]),
-                          p3 = cmul(v3, sh[i + 3]);
-            x.x -= (p0.x + p1.x) + (p2.x + p3.x);
-            x.y -= (p0.y + p1.y) + (p2.y + p3.y);
+            const B v0 = V[(int64_t)i * n + k], v1 = V[(int64_t)(i + 1) * n + k];
+            const B v2 = V[(int64_t)(i + 2) * n + k], v3 = V[(int64_t)(i + 3) * n + k];
+            const B c0 = sh[i], c1 = sh[i + 1], c2 = sh[i + 2], c3 = sh[i + 3];
+            const S pr = (v0.x * c0.x - v0.y * c0.y) + (v1.x * c1.x - v1.y * c1.y) + (v2.x * c2.x - v2.y * c2.y) +
+                         (v3.x * c3.x - v3.y * c3.y);
+            const S pi = (v0.x * c0.y + v0.y * c0.x) + (v1.x * c1.y + v1.y * c1.x) + (v2.x * c2.y + v2.y * c2.x) +
+                         (v3.x * c3.y + v3.y * c3.x);
+            x.x -= pr;
+            x.y -= pi;
         }
         for (; i < nb; ++i) {
-            const double2 p = cmul(V[(int64_t)i * n + k], sh[i]);
-            x.x -= p.x;
-            x.y -= p.y;
+            const B v0 = V[(int64_t)i * n + k], c0 = sh[i];
+            x.x -= v0.x * c0.x - v0.y * c0.y;
+            x.y -= v0.x * c0.y + v0.y * c0.x;
         }
         w[k] = x;
-        a += cabs2(x);
+        a += (double)(x.x * x.x + x.y * x.y);
     }
     if (!npart) return;
     a = warp_sum(a);
@@ -1101,8 +1232,9 @@ __global__ void __launch_bounds__(32) pg_givens_kernel(PgState* st, double2* g, 
         g[j] = cconjmul(c, gj);
         st->iters += 1;
         st->jdone = j + 1;
-        const double est = sqrt(cabs2(g[j + 1])) / st->bnorm;
-        if (est <= 0.5 * st->tol || hn <= 1e-300 || st->iters >= st->max_iters || j + 1 == m) st->active = 0;
+        const double gres = sqrt(cabs2(g[j + 1]));
+        const double stop = fmax(0.5 * st->tol * st->bnorm, st->inner_rtol * st->beta);
+        if (gres <= stop || hn <= 1e-300 || st->iters >= st->max_iters || j + 1 == m) st->active = 0;
     }
     __syncwarp();
     for (int i = lane; i <= j; i += 32) H[(int64_t)j * (m + 1) + i] = col[i];
@@ -1127,8 +1259,9 @@ __global__ void __launch_bounds__(32) pg_backsub_kernel(const PgState* st, const
     }
 }
 
-// u = sum_{i < jdone} V_i y_i
-__global__ void pg_combine_kernel(const double2* __restrict__ V, const double2* __restrict__ y,
+// u = sum_{i < jdone} V_i y_i (FP64)
+template <typename B>
+__global__ void pg_combine_kernel(const B* __restrict__ V, const double2* __restrict__ y,
                                   const PgState* __restrict__ st, int64_t n, double2* __restrict__ u) {
     const int jd = st->jdone;
     if (jd == 0) return;
@@ -1136,7 +1269,8 @@ __global__ void pg_combine_kernel(const double2* __restrict__ V, const double2* 
     if (k >= n) return;
     double2 a = make_double2(0.0, 0.0);
     for (int i = 0; i < jd; ++i) {
-        const double2 p = cmul(V[(int64_t)i * n + k], y[i]);
+        const B v = V[(int64_t)i * n + k];
+        const double2 p = cmul(make_double2(v.x, v.y), y[i]);
         a.x += p.x;
         a.y += p.y;
     }
@@ -1154,9 +1288,16 @@ __global__ void pg_update_kernel(const int32_t* __restrict__ cols, const float2*
     x[i] = make_double2(x[i].x + d.x, x[i].y + d.y);
 }
 
-// kind 0: Z complex64; kind 1: Z complex128
-static void pg_cycle(int kind, const void* z, int64_t n, const int32_t* cols, const float2* vals,
-                     const double2* b, double2* x, int m, const PgWork& W, unsigned* cnt, cudaStream_t s) {
+struct PgMatrix {
+    int kind;            // 0: complex64, 1: complex128, 2: complex64 + half copy for the products
+    const void* z;       // the matrix of the refinement residual
+    const __half2* zh;   // kind 2: the half copy
+    const float* scale;  // kind 2: its scale (device)
+};
+
+template <typename B>
+static void pg_cycle_t(const PgMatrix& A, int64_t n, const int32_t* cols, const float2* vals, const double2* b,
+                       double2* x, int m, const PgWork& W, unsigned* cnt, cudaStream_t s) {
     const unsigned vb = (unsigned)((n + 255) / 256), rb = (unsigned)((n + 7) / 8);
     const int nblk = (int)std::min<int64_t>(vb, kPgMaxBlocks);
     const int sblk = (int)std::min<int64_t>((n + 127) / 128, kPgMaxBlocks);
@@ -1165,52 +1306,75 @@ static void pg_cycle(int kind, const void* z, int64_t n, const int32_t* cols, co
     while ((n + chunk - 1) / chunk > kPgMaxBlocks) chunk *= 2;
     const unsigned nchunk = (unsigned)((n + chunk - 1) / chunk);
     const int* act = &W.st->active;
-    if (kind == 0) {
-        pg_split_kernel<<<vb, 256, 0, s>>>(x, n, reinterpret_cast<float4*>(W.z));
-        residual_c64x_kernel<<<rb, 256, 0, s>>>(static_cast<const float2*>(z), reinterpret_cast<const float4*>(W.z),
-                                                b, n, W.r);
+    B* V = static_cast<B*>(W.V);
+    B* w = static_cast<B*>(W.w);
+    B* z = reinterpret_cast<B*>(W.z);
+    if (A.kind == 1) {
+        residual_z128_kernel<<<rb, 256, 0, s>>>(static_cast<const double2*>(A.z), x, b, n, W.r);
     } else {
-        residual_z128_kernel<<<rb, 256, 0, s>>>(static_cast<const double2*>(z), x, b, n, W.r);
+        pg_split_kernel<<<vb, 256, 0, s>>>(x, n, reinterpret_cast<float4*>(W.z));
+        residual_c64x_kernel<<<rb, 256, 0, s>>>(static_cast<const float2*>(A.z),
+                                                reinterpret_cast<const float4*>(W.z), b, n, W.r);
     }
     pg_norm2_kernel<<<nblk, 256, 0, s>>>(W.r, n, W.npart, cnt, &W.st->rn2);
     pg_cycle_start_kernel<<<1, 1, 0, s>>>(W.st, W.g);
-    pg_scale_kernel<<<vb, 256, 0, s>>>(W.r, n, W.st, 0, W.V);
+    pg_start_basis_kernel<B><<<vb, 256, 0, s>>>(W.r, n, W.st, V);
     for (int j = 0; j < m; ++j) {
-        const double2* vj = W.V + (int64_t)j * n;
+        const B* vj = V + (int64_t)j * n;
         const dim3 dgrid(nchunk, (unsigned)((j + 1 + 7) / 8));
-        if (kind == 0) {
-            pg_precond_kernel<true><<<rb, 256, 0, s>>>(cols, vals, n, vj, W.z, W.st);
-            matvec_c64_kernel<<<rb, 256, 0, s>>>(static_cast<const float*>(z), reinterpret_cast<const float*>(W.z), n,
-                                                 reinterpret_cast<double*>(W.w), act);
+        pg_precond_kernel<B><<<rb, 256, 0, s>>>(cols, vals, n, vj, z, W.st);
+        if constexpr (sizeof(B) == 8) {
+            if (A.kind == 2)
+                pg_matvec_h16_kernel<<<rb, 256, 0, s>>>(A.zh, A.scale, reinterpret_cast<const float2*>(z), n,
+                                                        reinterpret_cast<float2*>(w), act);
+            else
+                pg_matvec_c64_kernel<<<rb, 256, 0, s>>>(static_cast<const float*>(A.z),
+                                                        reinterpret_cast<const float2*>(z), n,
+                                                        reinterpret_cast<float2*>(w), act);
         } else {
-            pg_precond_kernel<false><<<rb, 256, 0, s>>>(cols, vals, n, vj, W.z, W.st);
-            matvec_z128_kernel<<<rb, 256, 0, s>>>(static_cast<const double2*>(z), W.z, n, W.w, act);
+            matvec_z128_kernel<<<rb, 256, 0, s>>>(static_cast<const double2*>(A.z),
+                                                  reinterpret_cast<const double2*>(z), n,
+                                                  reinterpret_cast<double2*>(w), act);
         }
-        pg_dots_kernel<<<dgrid, 256, 0, s>>>(W.V, W.w, n, j + 1, chunk, W.part, m + 1, cnt, W.h1, act);
-        pg_sub_kernel<<<sblk, 128, 0, s>>>(W.V, W.h1, n, j + 1, W.w, nullptr, cnt, nullptr, act);
-        pg_dots_kernel<<<dgrid, 256, 0, s>>>(W.V, W.w, n, j + 1, chunk, W.part, m + 1, cnt, W.h2, act);
-        pg_sub_kernel<<<sblk, 128, 0, s>>>(W.V, W.h2, n, j + 1, W.w, W.npart, cnt, &W.st->hn2, act);
+        pg_dots_kernel<B><<<dgrid, 256, 0, s>>>(V, w, n, j + 1, chunk, W.part, m + 1, cnt, W.h1, act);
+        pg_sub_kernel<B><<<sblk, 128, 0, s>>>(V, W.h1, n, j + 1, w, nullptr, cnt, nullptr, act);
+        pg_dots_kernel<B><<<dgrid, 256, 0, s>>>(V, w, n, j + 1, chunk, W.part, m + 1, cnt, W.h2, act);
+        pg_sub_kernel<B><<<sblk, 128, 0, s>>>(V, W.h2, n, j + 1, w, W.npart, cnt, &W.st->hn2, act);
         pg_givens_kernel<<<1, 32, 0, s>>>(W.st, W.g, W.cs, W.sn, W.H, W.h1, W.h2, j);
-        pg_scale_kernel<<<vb, 256, 0, s>>>(W.w, n, W.st, 1, W.V + (int64_t)(j + 1) * n);
+        pg_scale_kernel<B><<<vb, 256, 0, s>>>(w, n, W.st, V + (int64_t)(j + 1) * n);
     }
     pg_backsub_kernel<<<1, 32, 0, s>>>(W.st, W.H, W.g, W.y);
-    pg_combine_kernel<<<vb, 256, 0, s>>>(W.V, W.y, W.st, n, W.r);
+    pg_combine_kernel<B><<<vb, 256, 0, s>>>(V, W.y, W.st, n, W.r);
     pg_update_kernel<<<vb, 256, 0, s>>>(cols, vals, W.r, W.st, n, x);
 }
 
-int pgmres(int kind, const void* z, int64_t n, const int32_t* m_cols, const float* m_vals, const double* b,
-           double* x, int m, int max_iters, double tol, bool use_graph, void* workspace, size_t ws_bytes,
-           int64_t* iters_out, int64_t* cycles_out, double* relres_out, int* status_out, cudaStream_t s) {
+static void pg_cycle(const PgMatrix& A, int64_t n, const int32_t* cols, const float2* vals, const double2* b,
+                     double2* x, int m, const PgWork& W, unsigned* cnt, cudaStream_t s) {
+    if (A.kind == 1) pg_cycle_t<double2>(A, n, cols, vals, b, x, m, W, cnt, s);
+    else pg_cycle_t<float2>(A, n, cols, vals, b, x, m, W, cnt, s);
+}
+
+int pgmres(int kind, const void* z, const void* z_half, const float* half_scale, double inner_rtol, int64_t n,
+           const int32_t* m_cols, const float* m_vals, const double* b, double* x, int m, int max_iters, double tol,
+           bool use_graph, void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out,
+           double* relres_out, int* status_out, cudaStream_t s) {
     if (!z || !b || !x || !workspace) return set_error(MB_ERR_ARG, "pgmres: null pointer");
     if (n <= 0) return set_error(MB_ERR_ARG, "n must be > 0");
     if (m < 1 || m > kGmresMaxRestart) return set_error(MB_ERR_ARG, "restart must be in [1, %d]", kGmresMaxRestart);
     if (max_iters < 1) return set_error(MB_ERR_ARG, "max_iters must be >= 1");
     if (!(tol > 0)) return set_error(MB_ERR_ARG, "tol must be > 0");
+    if (!(inner_rtol >= 0 && inner_rtol < 1)) return set_error(MB_ERR_ARG, "inner_rtol must be in [0, 1)");
     if ((m_cols == nullptr) != (m_vals == nullptr))
         return set_error(MB_ERR_ARG, "pgmres: give both m_cols and m_vals, or neither");
+    if ((z_half == nullptr) != (half_scale == nullptr))
+        return set_error(MB_ERR_ARG, "pgmres: give both z_half and half_scale, or neither");
+    if (kind == 1 && z_half) return set_error(MB_ERR_ARG, "pgmres: the half copy applies to a complex64 matrix");
     if (ws_bytes < pgmres_workspace_bytes(n, m)) return set_error(MB_ERR_ARG, "workspace too small");
     if (((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(z)) & 15) != 0)
         return set_error(MB_ERR_ARG, "pgmres: z, b and x must be 16-byte aligned");
+    if (z_half && (reinterpret_cast<uintptr_t>(z_half) & 15) != 0)
+        return set_error(MB_ERR_ARG, "pgmres: z_half must be 16-byte aligned");
+    const PgMatrix A{z_half ? 2 : kind, z, static_cast<const __half2*>(z_half), half_scale};
     PgWork W = pg_carve(workspace, n, m);
     const unsigned vb = (unsigned)((n + 255) / 256);
     const int nblk = (int)std::min<int64_t>(vb, kPgMaxBlocks);
@@ -1220,7 +1384,7 @@ int pgmres(int kind, const void* z, int64_t n, const int32_t* m_cols, const floa
     unsigned* cnt = &W.st->cnt;
     cudaMemsetAsync(W.st, 0, sizeof(PgState), s);
     pg_norm2_kernel<<<nblk, 256, 0, s>>>(b2, n, W.npart, cnt, &W.st->bn2);
-    pg_init_kernel<<<1, 1, 0, s>>>(W.st, tol, max_iters, m);
+    pg_init_kernel<<<1, 1, 0, s>>>(W.st, tol, max_iters, m, z_half ? inner_rtol : 0.0);
     int rc = check_launch("pgmres init");
     if (rc) return rc;
     cudaGraph_t graph = nullptr;
@@ -1235,7 +1399,7 @@ int pgmres(int kind, const void* z, int64_t n, const int32_t* m_cols, const floa
         if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess ||
             cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
             return cleanup(), set_error(MB_ERR_CUDA, "pgmres: stream capture failed");
-        pg_cycle(kind, z, n, m_cols, vals, b2, x2, m, W, cnt, cap);
+        pg_cycle(A, n, m_cols, vals, b2, x2, m, W, cnt, cap);
         cudaError_t ce = cudaStreamEndCapture(cap, &graph);
         if (ce != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
             return cleanup(), set_error(MB_ERR_CUDA, "pgmres: graph capture / instantiate failed");
@@ -1247,7 +1411,7 @@ int pgmres(int kind, const void* z, int64_t n, const int32_t* m_cols, const floa
             if (cudaGraphLaunch(exec, s) != cudaSuccess)
                 return cleanup(), set_error(MB_ERR_CUDA, "pgmres: graph launch failed");
         } else {
-            pg_cycle(kind, z, n, m_cols, vals, b2, x2, m, W, cnt, s);
+            pg_cycle(A, n, m_cols, vals, b2, x2, m, W, cnt, s);
         }
         cudaMemcpyAsync(&hs, W.st, sizeof(PgState), cudaMemcpyDeviceToHost, s);
         if ((rc = sync_check(s, "pgmres cycle"))) return cleanup(), rc;
@@ -1259,6 +1423,47 @@ int pgmres(int kind, const void* z, int64_t n, const int32_t* m_cols, const floa
     if (relres_out) *relres_out = hs.relres;
     if (status_out) *status_out = hs.converged ? 0 : 1;
     return MB_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// half-precision copy of a complex64 matrix for the Arnoldi products of kind 2
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) half_scale_kernel(const float4* __restrict__ z, int64_t n4,
+                                                         unsigned* __restrict__ amax_bits) {
+    float a = 0.f;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += (int64_t)gridDim.x * blockDim.x) {
+        const float4 v = __ldcs(z + k);
+        a = fmaxf(a, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(amax_bits, __float_as_uint(a));  // a >= 0: bits order as values
+}
+
+__global__ void __launch_bounds__(256) half_copy_kernel(const float4* __restrict__ z, int64_t n4,
+                                                        const float* __restrict__ scale, uint2* __restrict__ zh) {
+    const float s = *scale;
+    const float inv = s > 0.f ? 1.f / s : 0.f;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += (int64_t)gridDim.x * blockDim.x) {
+        const float4 v = __ldcs(z + k);
+        const __half2 a = __floats2half2_rn(v.x * inv, v.y * inv), b = __floats2half2_rn(v.z * inv, v.w * inv);
+        zh[k] = make_uint2(*reinterpret_cast<const unsigned*>(&a), *reinterpret_cast<const unsigned*>(&b));
+    }
+}
+
+int half_copy_c64(const float* z, int64_t count, void* zh, float* scale, cudaStream_t s) {
+    if (!z || !zh || !scale) return set_error(MB_ERR_ARG, "half copy: null pointer");
+    if (count <= 0) return set_error(MB_ERR_ARG, "half copy: count must be > 0");
+    if (count & 1) return set_error(MB_ERR_ARG, "half copy: count must be even (pairs of complex entries)");
+    if (((reinterpret_cast<uintptr_t>(z) & 15) | (reinterpret_cast<uintptr_t>(zh) & 7)) != 0)
+        return set_error(MB_ERR_ARG, "half copy: z must be 16-byte and z_half 8-byte aligned");
+    const int64_t n4 = count / 2;  // float4 = two complex entries
+    const unsigned blocks = (unsigned)std::min<int64_t>((n4 + 255) / 256, 152 * 16);
+    cudaMemsetAsync(scale, 0, sizeof(float), s);
+    half_scale_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(z), n4,
+                                             reinterpret_cast<unsigned*>(scale));
+    half_copy_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(z), n4, scale, static_cast<uint2*>(zh));
+    return check_launch("half_copy_c64");
 }
 
 }  // namespace mb

@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kLapThreads) laplace_panels_kernel(
 // vertex take the per-pair loop over their relation's table segment.  Coordinates are taken
 // relative to the first vertex of the block's first y face.
 // ---------------------------------------------------------------------------------------
-constexpr int kLapTileRows = 8;
+constexpr int kLapTileRows = 16;
 
 // The per-pair loop of laplace_panels_kernel (relation segment [beg, end)), added into acc.
 template <typename T, int NPHI, int KIND, int LAYER>
@@ -286,6 +286,20 @@ __global__ void __launch_bounds__(kLapThreads) laplace_panels_tiled_kernel(
         }
         ax = __ldg(areas + fx);
     }
+    // small rules keep W and phi(x_t) in registers (no shared-memory load per evaluation)
+    constexpr bool kRegW = Q <= 4;
+    T wreg[kRegW ? Q : 1][kRegW ? Q : 1][NPHI], preg[kRegW ? Q : 1][NPHI];
+    if constexpr (kRegW) {
+#pragma unroll
+        for (int t = 0; t < Q; ++t) {
+#pragma unroll
+            for (int a = 0; a < NPHI; ++a) {
+                preg[t][a] = s_px[t][a];
+#pragma unroll
+                for (int sq = 0; sq < Q; ++sq) wreg[t][sq][a] = s_w[t][sq][a];
+            }
+        }
+    }
     const int64_t valid = (nf - col0) < kLapThreads ? (nf - col0) : kLapThreads;
     for (int r = 0; r < rows; ++r) {
         const int64_t fy = fy0 + r;
@@ -296,6 +310,13 @@ __global__ void __launch_bounds__(kLapThreads) laplace_panels_tiled_kernel(
             const int rl = rel ? (int)rel[fy * nf + fx] : relation_of<T>(faces, fy, fx);
             if (rl == 0) {
                 const T nyx = s_ny[r][0], nyy = s_ny[r][1], nyz = s_ny[r][2];
+                T yr[Q][3];
+#pragma unroll
+                for (int sq = 0; sq < Q; ++sq) {
+                    yr[sq][0] = s_y[r][sq][0];
+                    yr[sq][1] = s_y[r][sq][1];
+                    yr[sq][2] = s_y[r][sq][2];
+                }
 #pragma unroll
                 for (int t = 0; t < Q; ++t) {
                     T ur[NPHI], ui[NPHI];
@@ -303,8 +324,7 @@ __global__ void __launch_bounds__(kLapThreads) laplace_panels_tiled_kernel(
                     for (int a = 0; a < NPHI; ++a) { ur[a] = 0; ui[a] = 0; }
 #pragma unroll
                     for (int sq = 0; sq < Q; ++sq) {
-                        const T dx = xp[t][0] - s_y[r][sq][0], dy = xp[t][1] - s_y[r][sq][1],
-                                dz = xp[t][2] - s_y[r][sq][2];
+                        const T dx = xp[t][0] - yr[sq][0], dy = xp[t][1] - yr[sq][1], dz = xp[t][2] - yr[sq][2];
                         const T r2d = dx * dx + dy * dy + dz * dz;
                         const T rinv = rsqrt_t(r2d);
                         T fr, fi = 0;
@@ -328,16 +348,18 @@ __global__ void __launch_bounds__(kLapThreads) laplace_panels_tiled_kernel(
                         }
 #pragma unroll
                         for (int a = 0; a < NPHI; ++a) {
-                            ur[a] += fr * s_w[t][sq][a];
-                            if constexpr (KIND == 1) ui[a] += fi * s_w[t][sq][a];
+                            const T wv = kRegW ? wreg[kRegW ? t : 0][kRegW ? sq : 0][a] : s_w[t][sq][a];
+                            ur[a] += fr * wv;
+                            if constexpr (KIND == 1) ui[a] += fi * wv;
                         }
                     }
 #pragma unroll
                     for (int a = 0; a < NPHI; ++a) {
 #pragma unroll
                         for (int b = 0; b < NPHI; ++b) {
-                            accr[a * NPHI + b] += ur[a] * s_px[t][b];
-                            if constexpr (KIND == 1) acci[a * NPHI + b] += ui[a] * s_px[t][b];
+                            const T pv = kRegW ? preg[kRegW ? t : 0][b] : s_px[t][b];
+                            accr[a * NPHI + b] += ur[a] * pv;
+                            if constexpr (KIND == 1) acci[a * NPHI + b] += ui[a] * pv;
                         }
                     }
                 }

@@ -513,13 +513,27 @@ def pgmres_workspace_bytes(n: int, restart: int = 50) -> int:
     return int(_lib.load().mb_pgmres_workspace_bytes(int(n), int(restart)))
 
 
+def half_copy(Z):
+    """Half-precision copy of the complex64 matrix Z for ``pgmres(..., Z_half=...)``
+    (``mb_half_copy_c64``): (Zh float16 [n, 2n] = Z / scale interleaved, scale float32 [1] on
+    the device = max |Re|, |Im| of Z)."""
+    _lib.check_tensor(Z, "Z", dtype=torch.complex64, ndim=2)
+    n0, n1 = Z.shape
+    Zh = torch.empty((n0, 2 * n1), dtype=torch.float16, device=Z.device)
+    scale = torch.empty(1, dtype=torch.float32, device=Z.device)
+    _lib.call("mb_half_copy_c64", _lib.ptr(Z), n0 * n1, _lib.ptr(Zh), _lib.ptr(scale), _lib.stream_of(Z))
+    return Zh, scale
+
+
 def pgmres(Z, b, M=None, x0=None, restart: int = 50, max_iters: int = 2000, tol: float = 1e-6,
-           use_graph: bool = True, workspace=None):
+           use_graph: bool = True, workspace=None, Z_half=None, inner_rtol: float = 3e-3):
     """Solve Z x = b by right-preconditioned GMRES(restart) with the whole restart cycle on the
-    device (``mb_pgmres_c64`` / ``mb_pgmres_c128``): FP32 products for complex64 Z, FP64 for
-    complex128 Z; FP64 refinement residual, CGS2 Arnoldi on a complex128 basis.  ``M``: a
-    ``SpaiPreconditioner`` or None.  b: [n] or [n, k].  Returns (x complex128 with b's shape,
-    per-column info dicts as ``gmres``)."""
+    device (``mb_pgmres_c64`` / ``mb_pgmres_c128``): FP32 products and a complex64 basis for
+    complex64 Z, FP64 for complex128 Z; refinement residual every cycle.  ``M``: a
+    ``SpaiPreconditioner`` or None.  ``Z_half``: ``half_copy(Z)`` for complex64 Z -- the
+    Arnoldi products then read the half-precision copy and each cycle ends once its residual
+    estimate has dropped by ``inner_rtol``.  b: [n] or [n, k].  Returns (x complex128 with b's
+    shape, per-column info dicts as ``gmres``)."""
     _lib.check_tensor(Z, "Z", dtype=(torch.complex64, torch.complex128), ndim=2)
     n = Z.shape[0]
     if Z.shape[1] != n:
@@ -538,16 +552,29 @@ def pgmres(Z, b, M=None, x0=None, restart: int = 50, max_iters: int = 2000, tol:
         _lib.check_tensor(workspace, "workspace", dtype=torch.uint8, device=dev)
         if workspace.numel() < need:
             raise ValueError(f"workspace needs {need} bytes")
-    fn = "mb_pgmres_c64" if Z.dtype == torch.complex64 else "mb_pgmres_c128"
+    c64 = Z.dtype == torch.complex64
+    if Z_half is not None:
+        if not c64:
+            raise ValueError("Z_half applies to a complex64 Z")
+        zh, zscale = Z_half
+        _lib.check_tensor(zh, "Z_half", dtype=torch.float16, device=dev, shape=(n, 2 * n))
+        half_args = (_lib.ptr(zh), _lib.ptr(zscale), float(inner_rtol))
+    else:
+        half_args = (None, None, 0.0)
     infos = []
     for c in range(bb.shape[1]):
         bc_ = bb[:, c].contiguous()
         xc = xx[:, c].contiguous()
         info = _lib.GmresInfo()
-        _lib.call(fn, _lib.ptr(Z), n, _lib.ptr(M.cols if M is not None else None),
-                  _lib.ptr(M.vals if M is not None else None), _lib.ptr(bc_), _lib.ptr(xc), int(restart),
-                  int(max_iters), float(tol), int(bool(use_graph)), _lib.ptr(workspace), workspace.numel(),
-                  __import__("ctypes").byref(info), _lib.stream_of(Z))
+        mp = (_lib.ptr(M.cols if M is not None else None), _lib.ptr(M.vals if M is not None else None))
+        if c64:
+            _lib.call("mb_pgmres_c64", _lib.ptr(Z), n, *half_args, *mp, _lib.ptr(bc_), _lib.ptr(xc), int(restart),
+                      int(max_iters), float(tol), int(bool(use_graph)), _lib.ptr(workspace), workspace.numel(),
+                      __import__("ctypes").byref(info), _lib.stream_of(Z))
+        else:
+            _lib.call("mb_pgmres_c128", _lib.ptr(Z), n, *mp, _lib.ptr(bc_), _lib.ptr(xc), int(restart),
+                      int(max_iters), float(tol), int(bool(use_graph)), _lib.ptr(workspace), workspace.numel(),
+                      __import__("ctypes").byref(info), _lib.stream_of(Z))
         xx[:, c] = xc
         infos.append({"iterations": info.iterations, "restarts": info.restarts,
                       "rel_residual": info.rel_residual, "converged": info.status == 0})

@@ -120,3 +120,41 @@ def test_pgmres_iteration_cap_and_bad_arguments(pkg, cuda):
         M.pgmres(Z, b, restart=0)
     with pytest.raises(pkg.MeshBEMError):
         M.pgmres(Z, b, tol=0.0)
+
+
+def test_half_copy_scales_and_rounds(pkg, cuda):
+    _, _, _, ne, Z, _ = _efie(pkg, cuda, 2, 3.0)
+    Zh, scale = pkg.mesh_MOM_3d.half_copy(Z)
+    zr = torch.view_as_real(Z)
+    amax = float(zr.abs().max())
+    assert float(scale) == amax
+    back = Zh.float().reshape(ne, ne, 2) * float(scale)
+    err = (back - zr).abs().max().item()
+    assert err <= amax * 2.0 ** -11  # half a unit in the last place of binary16 at the scale
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_pgmres_half_inner_reaches_lu(pkg, cuda, use_graph):
+    """Arnoldi products on the half-precision copy, refinement against complex64 Z: the
+    solution still reaches the dense-LU solution of the complex64 system."""
+    v, f, fei, ne, Z, b = _efie(pkg, cuda, 3, 10.0)
+    M = pkg.mesh_MOM_3d
+    P = M.spai_preconditioner(Z, v, f, fei, ne)
+    ref = torch.linalg.solve(Z.to(torch.complex128), b).cpu().numpy()
+    x, info = M.pgmres(Z, b, M=P, restart=50, tol=1e-9, max_iters=4000, use_graph=use_graph,
+                       Z_half=M.half_copy(Z), inner_rtol=3e-3)
+    assert info[0]["converged"] and info[0]["restarts"] >= 2
+    assert rel_err(x.cpu().numpy(), ref) < 1e-6
+    r = b - Z.to(torch.complex128) @ x
+    assert float(r.norm() / b.norm()) <= 2e-9
+
+
+def test_pgmres_half_graph_and_direct_bitwise_equal(pkg, cuda):
+    v, f, fei, ne, Z, b = _efie(pkg, cuda, 2, 3.0)
+    M = pkg.mesh_MOM_3d
+    P = M.spai_preconditioner(Z, v, f, fei, ne)
+    H = M.half_copy(Z)
+    xa, ia = M.pgmres(Z, b, M=P, restart=20, tol=1e-10, use_graph=True, Z_half=H)
+    xb, ib = M.pgmres(Z, b, M=P, restart=20, tol=1e-10, use_graph=False, Z_half=H)
+    assert ia == ib
+    assert torch.equal(xa, xb)
