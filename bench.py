@@ -56,6 +56,7 @@ WORKLOADS = {
     "batch_star64": (64, 4, 0),
     "batch_star64_efie": (64, 4, 0),
     "batch_star8": (8, 4, 0),
+    "batch_star8_efie": (8, 4, 0),
     # scattered H on a field-point grid from vertex currents: (icosphere level, k, grid points per side)
     "radiate_L5": (5, 10.0, 1024),
     # GPU mesh topology (unique edges + face-edge map + edge faces, near-pair list, Z-row map)
@@ -1417,6 +1418,8 @@ def batch_meshes(n_mesh, seed):
 
 
 def main_batch(args, rank, world, local_rank):
+    """Config 4: time to a TTS_TARGET relative error in J (every column) for all meshes and
+    incidences of the batch, plain per-mesh path against the batched preconditioned path."""
     n_mesh, nc, seed = WORKLOADS[args.workload]
     import torch
 
@@ -1447,7 +1450,10 @@ def main_batch(args, rank, world, local_rank):
         p /= np.linalg.norm(p, axis=1, keepdims=True)
         waves.append(MM.plane_waves(ks[i], d, p))
     waves = torch.stack(waves).to(dev)
-    tol, restart, cap = 1e-5, 50, 2000
+    # the plain path is config 2's GMRES(50); the batched path restarts every 150 steps (near
+    # interior resonances of the EFIE a few eigenvalues of the preconditioned operator sit near
+    # zero and a 50-step cycle cannot capture them)
+    restart, restart_b, cap = 50, 150, 20000
     bt = pkg.batch.MeshBatch(meshes, ks, device=dev, formulation=formulation)
     if not efie:
         px, wx = pkg.utils.get_gaussion_integration_points_and_weights(4, device=dev)
@@ -1456,38 +1462,94 @@ def main_batch(args, rank, world, local_rank):
     stream = torch.cuda.current_stream(dev)
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
     z_flat = torch.zeros(bt.z_size, dtype=torch.complex64, device=dev)
+    bt.assemble(out=z_flat)
+    B = bt.excitation(waves)
+    rows = bt.autotune(z_flat)
+    P = bt.spai(z_flat)
 
-    def run_batched():
+    # FP64 reference J of every column (untimed)
+    t0 = time.perf_counter()
+    if efie:
+        z64 = torch.zeros(bt.z_size, dtype=torch.complex128, device=dev)
+        vd = bt.verts.double().contiguous()
+        pkg._lib.call("mb_mom_sym_zmat_batched_c128", pkg._lib.ptr(vd), pkg._lib.ptr(bt.faces),
+                      pkg._lib.ptr(bt.fei), pkg._lib.ptr(bt.desc), pkg._lib.ptr(bt.ks), bt.n_mesh, bt.total_blocks,
+                      pkg._lib.ptr(bt.near), bt.near.shape[0], pkg._lib.ptr(z64), pkg._lib.stream_of(z64))
+        b64 = torch.zeros((bt.n_rows, n_mesh * nc), dtype=torch.complex128, device=dev)
+        wv = waves.to(torch.float64).contiguous()
+        pkg._lib.call("mb_mom_sym_rhs_batched_c128", pkg._lib.ptr(vd), pkg._lib.ptr(bt.faces),
+                      pkg._lib.ptr(bt.fei), pkg._lib.ptr(bt.desc), bt.n_mesh, bt.total_faces, pkg._lib.ptr(wv), nc,
+                      n_mesh * nc, pkg._lib.ptr(b64), pkg._lib.stream_of(b64))
+        ref_what = ("FP64 batched assembly (complex128 Z_i, FP64 quadrature and singular integrals), per-mesh FP64 "
+                    "preconditioned GMRES (FP64 products) to a 1e-10 relative residual")
+    else:
+        ref_what = ("the FP32-assembled complex64 Z_i solved to a 1e-10 relative residual (compensated "
+                    "refinement residual); an FP64 assembly of the reference rule is too slow at GB300's FP64 rate")
+    refs = {}
+    for i in range(n_mesh):
+        e = bt.n_edges[i]
+        o = int(bt.edge_offsets[i])
+        Pi = MM.SpaiPreconditioner(P.cols[o:o + e], P.vals[o:o + e], 0)
+        if efie:
+            zi = bt.z_block(z64, i).contiguous()
+            bi = b64[:e, nc * i:nc * (i + 1)]
+        else:
+            zi = bt.z_block(z_flat, i).contiguous()
+            bi = B[:e, nc * i:nc * (i + 1)].to(torch.complex128)
+        refs[i], _ = MM.pgmres(zi, bi, M=Pi, restart=50, tol=1e-10, max_iters=20000)
+    if efie:
+        del z64, b64
+    torch.cuda.synchronize(dev)
+    ref_s = time.perf_counter() - t0
+
+    def col_errs(X):  # relative error of J per column of mesh i, all meshes -> max
+        worst = 0.0
+        for i in range(n_mesh):
+            e = bt.n_edges[i]
+            d = torch.linalg.norm(X[:e, nc * i:nc * (i + 1)] - refs[i], dim=0) / torch.linalg.norm(refs[i], dim=0)
+            worst = max(worst, float(d.max()))
+        return worst
+
+    # batched preconditioned path: calibrate the tolerance, then time it end to end
+    def run_batched(tol, precond=True):
         e = [ev() for _ in range(4)]
+        torch.cuda.synchronize(dev)
         e[0].record(stream)
         bt.assemble(out=z_flat)
-        B = bt.excitation(waves)
+        Bb = bt.excitation(waves)
         e[1].record(stream)
-        X, info = bt.solve(z_flat, B, restart=restart, tol=tol, max_iters=cap, use_graph=True)
+        Pb = bt.spai(z_flat) if precond else None
         e[2].record(stream)
+        X, info = bt.solve(z_flat, Bb, restart=restart_b, tol=tol, max_iters=cap, use_graph=True, M=Pb)
+        e[3].record(stream)
         torch.cuda.synchronize(dev)
-        return B, X, info, e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+        return X, info, e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2]), e[2].elapsed_time(e[3])
 
-    bt.assemble(out=z_flat)
-    bt.excitation(waves)
-    rows = bt.autotune(z_flat)
+    chosen = None
+    for tol in TTS_LADDER:
+        X, info, *_ = run_batched(tol)
+        if col_errs(X) <= TTS_TARGET:
+            chosen = tol
+            break
     for _ in range(max(1, min(args.warmup, 1))):
-        run_batched()
+        run_batched(chosen or TTS_LADDER[-1])
     clocks = ClockSampler(dev.index)
     clocks.start()
     time.sleep(0.3)
-    runs = [run_batched() for _ in range(args.steps)]
+    runs = [run_batched(chosen or TTS_LADDER[-1]) for _ in range(args.steps)]
     clocks.stop()
-    B, X, info = runs[-1][0], runs[-1][1], runs[-1][2]
-    asm_ms = statistics.mean(r[3] for r in runs)
+    X, info = runs[-1][0], runs[-1][1]
+    asm_ms = statistics.mean(r[2] for r in runs)
+    pc_ms = statistics.mean(r[3] for r in runs)
     solve_ms = statistics.mean(r[4] for r in runs)
-    total_ms = asm_ms + solve_ms
-    # plain path: each mesh assembled and each incidence solved on its own (GMRES, FP32 matvec)
-    e0, e1 = ev(), ev()
-    e0.record(stream)
-    plain_iters = []
-    plain_X = {}
-    for i, (v, f) in enumerate(meshes):
+    total_ms = asm_ms + pc_ms + solve_ms
+    batched_err = col_errs(X)
+
+    # plain path: each mesh assembled on its own, each incidence solved by GMRES(50) from zero
+    # with FP32 products and no preconditioner; each column stops at the loosest tolerance of
+    # the ladder that reaches the target (found beforehand, untimed)
+    def mesh_system(i):
+        v, f = meshes[i]
         vt = torch.tensor(np.asarray(v), dtype=torch.float32, device=dev)
         ft = torch.tensor(np.asarray(f), dtype=torch.int32, device=dev)
         edges, fei, _ = pkg.utils.get_edge_unique(vt, ft)
@@ -1500,38 +1562,72 @@ def main_batch(args, rank, world, local_rank):
             nn = pkg.utils.compute_face_normals(vt, ft).contiguous()
             Z = MM.assemble_Z_rwg(vt, ft, a, nn, fei, ne, px, wx, py, wy, ks[i])
             Bi = MM.assemble_rhs_rwg(vt, ft, a, nn, fei, ne, px, wx, waves[i])
+        return Z, Bi
+
+    plain_tol = {}
+    plain_reached = True
+    for i in range(n_mesh):
+        Z, Bi = mesh_system(i)
+        for r in range(nc):
+            ref = refs[i][:, r]
+            for tol in TTS_LADDER:
+                x1, inf1 = MM.gmres(Z, Bi[:, r], restart=restart, tol=tol, max_iters=cap)
+                if float((x1 - ref).norm() / ref.norm()) <= TTS_TARGET:
+                    plain_tol[(i, r)] = tol
+                    break
+                if inf1[0]["iterations"] >= cap:  # tighter tolerances cannot do better within the cap
+                    plain_tol[(i, r)] = tol
+                    plain_reached = False
+                    break
+            else:
+                plain_tol[(i, r)] = TTS_LADDER[-1]
+                plain_reached = False
+        del Z, Bi
+    e0, e1 = ev(), ev()
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    plain_iters, plain_err = [], 0.0
+    plain_X = {}
+    for i in range(n_mesh):
+        Z, Bi = mesh_system(i)
         xs = []
         for r in range(nc):
-            x1, inf1 = MM.gmres(Z, Bi[:, r], restart=restart, tol=tol, max_iters=cap)
+            x1, inf1 = MM.gmres(Z, Bi[:, r], restart=restart, tol=plain_tol[(i, r)], max_iters=cap)
             plain_iters.append(inf1[0]["iterations"])
             xs.append(x1)
         plain_X[i] = torch.stack(xs, 1)
+        del Z, Bi
     e1.record(stream)
     torch.cuda.synchronize(dev)
     plain_ms = e0.elapsed_time(e1)
-    # accuracy against FP64 LU on a sample of meshes (outside the timed regions)
-    errs, errs_plain = [], []
-    for i in range(0, n_mesh, max(1, n_mesh // 8)):
-        Zi = bt.z_block(z_flat, i).to(torch.complex128)
-        e = bt.n_edges[i]
-        ref = torch.linalg.solve(Zi, B[:e, nc * i:nc * (i + 1)].to(torch.complex128))
-        errs.append((torch.linalg.norm(X[:e, nc * i:nc * (i + 1)] - ref, dim=0) / torch.linalg.norm(ref, dim=0)).max().item())
-        errs_plain.append((torch.linalg.norm(plain_X[i] - ref, dim=0) / torch.linalg.norm(ref, dim=0)).max().item())
-    line = {"metric": "batch time to solution (assembly + solve of all meshes and incidences)",
+    for i in range(n_mesh):
+        d = torch.linalg.norm(plain_X[i] - refs[i], dim=0) / torch.linalg.norm(refs[i], dim=0)
+        plain_err = max(plain_err, float(d.max()))
+    line = {"metric": "batch time to a 1e-4 relative error in J (every mesh and incidence), plain FP32 path vs "
+                      "batched preconditioned path",
             "value": total_ms, "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 (FP64 near pairs, complex64 basis, FP64 Hessenberg and iterate)", "data": "synthetic", "config": config,
-            "batched": {"assembly_and_excitation_ms": asm_ms, "solve_ms": solve_ms,
+            "dtype": "f32 (FP64 near pairs, complex64 basis, FP64 Hessenberg and iterate)", "data": "synthetic",
+            "config": config, "target_rel_err_J": TTS_TARGET, "reference_J": ref_what, "reference_J_seconds": ref_s,
+            "batched": {"what": "1 assembly + 1 excitation launch for all meshes, the near-field SAI of every mesh "
+                                "in one launch, lockstep right-preconditioned GMRES(150) on all columns with the "
+                                "block-diagonal product (one CUDA graph per restart cycle)",
+                        "tol": chosen, "reached": chosen is not None and batched_err <= TTS_TARGET,
+                        "assembly_and_excitation_ms": asm_ms, "precond_ms": pc_ms, "solve_ms": solve_ms,
                         "arnoldi_steps": info["iterations"], "restarts": info["restarts"],
-                        "max_rel_residual": info["max_rel_residual"], "converged": info["converged"],
-                        "matvec_rows_per_warp": rows, "max_rel_err_J_vs_fp64_lu_sample": max(errs),
-                        "launches": ("assembly: 1 separated-pair + 1 near-pair launch for all meshes" if efie else
-                                     "assembly: 1 launch for all meshes") + "; excitation 1; solve: one CUDA graph "
-                                    "per restart cycle"},
-            "plain_path": {"what": "per mesh: assembly, then one GMRES(50) per incidence (FP32 matvec)",
-                           "time_to_solution_ms": plain_ms, "median_iterations": statistics.median(plain_iters),
-                           "max_iterations": max(plain_iters), "max_rel_err_J_vs_fp64_lu_sample": max(errs_plain)},
-            "speedup_vs_plain": plain_ms / total_ms, "clocks": clocks.summary(), "gpu_launches": None}
+                        "max_rel_residual": info["max_rel_residual"], "max_rel_err_J": batched_err,
+                        "matvec_rows_per_warp": rows, "precond_status": P.status},
+            "plain_path": {"what": "per mesh: FP32 assembly + excitation, then one GMRES(50) per incidence from zero "
+                                   "(FP32 products, no preconditioner, mb_gmres_c64), each column at the loosest "
+                                   "ladder tolerance that reaches the target (a column that hits the cap of "
+                                   f"{cap} steps stops there: its time is a lower bound)",
+                           "time_to_solution_ms": plain_ms, "reached": plain_reached,
+                           "median_iterations": statistics.median(plain_iters), "max_iterations": max(plain_iters),
+                           "max_rel_err_J": plain_err},
+            "speedup_vs_plain": plain_ms / total_ms,
+            "speedup_note": None if plain_reached else "the plain path did not reach the target on every column "
+                            "within the cap; its time and this ratio are lower bounds",
+            "clocks": clocks.summary(), "gpu_launches": None}
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -423,6 +423,18 @@ int mb_gmres_blockdiag_c64(const float* z, const int64_t* desc, const int64_t* g
                            double* x, int restart, int max_iters, double tol, int use_graph, void* workspace,
                            size_t workspace_bytes, mb_gmres_info* info, void* stream);
 
+/* mb_gmres_blockdiag_c64 with the near-field right preconditioner of every mesh: m_cols /
+ * m_vals from mb_spai_build_c64 run on the whole batch (desc rows (first face, F_i, first
+ * edge, E_i, offset of Z_i, row pitch)), edge_offsets [n_mesh] int64 the first global edge of
+ * each mesh (device).  Each Arnoldi step multiplies Z_i by M_i V_j; each cycle's update goes
+ * through M_i before it is added to X.  Same workspace as mb_gmres_blockdiag_c64 (its size
+ * includes the preconditioned vectors). */
+int mb_gmres_blockdiag_pc_c64(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh,
+                              int64_t total_warps, int rows_per_warp, int nc, int64_t n_rows, const int32_t* m_cols,
+                              const float* m_vals, const int64_t* edge_offsets, const double* b, double* x,
+                              int restart, int max_iters, double tol, int use_graph, void* workspace,
+                              size_t workspace_bytes, mb_gmres_info* info, void* stream);
+
 /* No counterpart in the reference.  The same solver as mb_gmres_c64 for callers that
  * cannot allocate device memory -- for example a host application or plugin that must
  * budget all GPU memory at start-up, or a foreign-language caller (Go, Java, ...) that has

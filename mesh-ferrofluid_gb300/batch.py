@@ -208,11 +208,44 @@ class MeshBatch:
         self.rows_per_warp = best
         return best
 
+    def spai(self, z_flat: torch.Tensor, workspace=None):
+        """Near-field sparse approximate inverse of every mesh's Z_i in one launch
+        (``mb_spai_build_c64`` over the batch): ``mesh_MOM_3d.SpaiPreconditioner`` with rows
+        [sum E_i, SPAI_WIDTH] (mesh i's rows start at ``self.edge_offsets[i]``; local columns)."""
+        from .mesh_MOM_3d import SPAI_WIDTH, SpaiPreconditioner
+
+        _lib.check_tensor(z_flat, "z_flat", dtype=torch.complex64, device=self.device)
+        if not hasattr(self, "edge_offsets"):
+            e = np.asarray(self.n_edges, np.int64)
+            eoff = np.concatenate([[0], np.cumsum(e)[:-1]]).astype(np.int64)
+            d = np.stack([self._desc_np[:, 0], self._desc_np[:, 1], eoff, e, self._desc_np[:, 3], e + (e & 1)], 1)
+            self._spai_desc = torch.tensor(np.ascontiguousarray(d), device=self.device)
+            self.edge_offsets = torch.tensor(eoff, device=self.device)
+            self.total_edges = int(e.sum())
+        ne = self.total_edges
+        need = int(_lib.load().mb_spai_workspace_bytes(ne))
+        if workspace is None or workspace.numel() < need:
+            workspace = torch.empty(need, dtype=torch.uint8, device=self.device)
+        cols = torch.empty((ne, SPAI_WIDTH), dtype=torch.int32, device=self.device)
+        vals = torch.empty((ne, SPAI_WIDTH), dtype=torch.complex64, device=self.device)
+        st = _lib.stream_of(z_flat)
+        _lib.call("mb_spai_build_c64", _lib.ptr(self.verts), _lib.ptr(self.faces), _lib.ptr(self.fei),
+                  _lib.ptr(self._spai_desc), self.n_mesh, self.total_faces, ne, _lib.ptr(self.near),
+                  self.near.shape[0], _lib.ptr(z_flat), _lib.ptr(cols), _lib.ptr(vals), _lib.ptr(workspace),
+                  workspace.numel(), st)
+        status = ctypes.c_int32(0)
+        _lib.call("mb_spai_status", _lib.ptr(workspace), ne, ctypes.byref(status), st)
+        if status.value & 4:
+            raise ValueError("a mesh of the batch has an edge without faces or with more than two")
+        return SpaiPreconditioner(cols, vals, int(status.value))
+
     def solve(self, z_flat: torch.Tensor, B: torch.Tensor, restart: int = 50, max_iters: int = 2000,
-              tol: float = 1e-6, use_graph: bool = True, workspace=None, X0: torch.Tensor | None = None):
+              tol: float = 1e-6, use_graph: bool = True, workspace=None, X0: torch.Tensor | None = None, M=None):
         """Lockstep GMRES on every (mesh, wave) column -> (X complex128 padded, info dict).
 
-        X0: optional initial guess on the padded layout (rows beyond E_i must be zero)."""
+        X0: optional initial guess on the padded layout (rows beyond E_i must be zero).
+        M: optional near-field preconditioner from ``spai`` (right preconditioning of every
+        mesh's system, ``mb_gmres_blockdiag_pc_c64``)."""
         if self.nc is None:
             raise RuntimeError("call excitation() first")
         rows = self.rows_per_warp or 2
@@ -224,10 +257,19 @@ class MeshBatch:
         if workspace is None:
             workspace = torch.empty(need, dtype=torch.uint8, device=self.device)
         info = _lib.GmresInfo()
-        _lib.call("mb_gmres_blockdiag_c64", _lib.ptr(z_flat), _lib.ptr(self.desc), _lib.ptr(goff), self.n_mesh,
-                  int(goff[-1]), rows, self.nc, self.n_rows, _lib.ptr(bb), _lib.ptr(X), int(restart), int(max_iters),
-                  float(tol), 1 if use_graph else 0, _lib.ptr(workspace), workspace.numel(), ctypes.byref(info),
-                  _lib.stream_of(bb))
+        if M is not None:
+            if tuple(M.cols.shape) != (self.total_edges, M.cols.shape[1]):
+                raise ValueError("preconditioner does not match the batch")
+            _lib.call("mb_gmres_blockdiag_pc_c64", _lib.ptr(z_flat), _lib.ptr(self.desc), _lib.ptr(goff), self.n_mesh,
+                      int(goff[-1]), rows, self.nc, self.n_rows, _lib.ptr(M.cols), _lib.ptr(M.vals),
+                      _lib.ptr(self.edge_offsets), _lib.ptr(bb), _lib.ptr(X), int(restart), int(max_iters),
+                      float(tol), 1 if use_graph else 0, _lib.ptr(workspace), workspace.numel(), ctypes.byref(info),
+                      _lib.stream_of(bb))
+        else:
+            _lib.call("mb_gmres_blockdiag_c64", _lib.ptr(z_flat), _lib.ptr(self.desc), _lib.ptr(goff), self.n_mesh,
+                      int(goff[-1]), rows, self.nc, self.n_rows, _lib.ptr(bb), _lib.ptr(X), int(restart),
+                      int(max_iters), float(tol), 1 if use_graph else 0, _lib.ptr(workspace), workspace.numel(),
+                      ctypes.byref(info), _lib.stream_of(bb))
         steps = torch.empty(m, dtype=torch.int32, device=self.device)
         _lib.call("mb_gmres_blockdiag_column_steps", _lib.ptr(workspace), self.n_rows, m, int(restart), _lib.ptr(steps),
                   _lib.stream_of(bb))

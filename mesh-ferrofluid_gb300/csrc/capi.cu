@@ -150,6 +150,11 @@ int pgmres(int kind, const void* z, const void* z_half, const float* half_scale,
            bool use_graph, void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out,
            double* relres_out, int* status_out, cudaStream_t s);
 int half_copy_c64(const float* z, int64_t count, void* zh, float* scale, cudaStream_t s);
+int gmres_blockdiag_pc(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
+                       int rows_per_warp, int nc, int64_t n_rows, const int32_t* m_cols, const float* m_vals,
+                       const int64_t* eoff, const double* b, double* x, int r, int max_iters, double tol,
+                       bool use_graph, void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out,
+                       double* max_relres_out, int* status_out, cudaStream_t s);
 int gmres_c64_noalloc(const float*, int64_t, const double*, double*, int, int, double, int64_t*, int64_t*,
                       double*, int*, cudaStream_t);
 int launch_matvec_c64(const float*, const float*, int64_t, double*, cudaStream_t);
@@ -920,6 +925,29 @@ int mb_pgmres_c128(const double* z, int64_t n, const int32_t* m_cols, const floa
                    size_t workspace_bytes, mb_gmres_info* info, void* stream) {
     return pgmres_entry(1, z, nullptr, nullptr, 0.0, n, m_cols, m_vals, b, x, restart, max_iters, tol, use_graph,
                         workspace, workspace_bytes, info, stream);
+}
+
+int mb_gmres_blockdiag_pc_c64(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh,
+                              int64_t total_warps, int rows_per_warp, int nc, int64_t n_rows, const int32_t* m_cols,
+                              const float* m_vals, const int64_t* edge_offsets, const double* b, double* x,
+                              int restart, int max_iters, double tol, int use_graph, void* workspace,
+                              size_t workspace_bytes, mb_gmres_info* info, void* stream) {
+    MB_REQUIRE(n_mesh > 0 && nc > 0 && n_rows > 0, "bad sizes");
+    MB_REQUIRE(z && desc && goff && b && x && workspace && m_cols && m_vals && edge_offsets, "null pointer argument");
+    int64_t it = 0, cyc = 0;
+    double rr = 0.0;
+    int st = 1;
+    const int rc = gmres_blockdiag_pc(z, desc, goff, n_mesh, total_warps, rows_per_warp, nc, n_rows, m_cols, m_vals,
+                                      edge_offsets, b, x, restart, max_iters, tol, use_graph != 0, workspace,
+                                      workspace_bytes, &it, &cyc, &rr, &st, as_stream(stream));
+    if (rc == MB_OK && info) {
+        info->iterations = it;
+        info->restarts = cyc;
+        info->rel_residual = rr;
+        info->status = st;
+        info->reserved = 0;
+    }
+    return rc;
 }
 
 int mb_half_copy_c64(const float* z, int64_t count, void* z_half, float* scale, void* stream) {

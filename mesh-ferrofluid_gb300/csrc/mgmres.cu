@@ -29,7 +29,7 @@ size_t cgemm_workspace_bytes(int64_t n, int64_t m);
 int cgemm_tf32x3(const float* z_hi, const float* z_lo, int64_t n, const float* x, int64_t m, float* y, void* ws,
                  size_t ws_bytes, cudaStream_t s);
 
-constexpr int kMgMaxRestart = 128;
+constexpr int kMgMaxRestart = 160;
 
 struct MgWork {
     float2* V;      // [(r+1), n, m] complex64 Krylov basis (V_j is the product's input at step j)
@@ -98,9 +98,15 @@ size_t gmres_multi_workspace_bytes(int64_t n, int64_t m, int r) {
 
 // (the product's slot holds the per-mesh tensor maps of the streamed variant: one per column
 // is more than enough)
+// and, after them, the preconditioned variant's buffers: the preconditioned basis vector
+// [n, mp] complex64 and the cycle's update before M, [n, m] complex128)
+static size_t bd_maps_bytes(int64_t m) { return a256(128 * (size_t)std::max<int64_t>(m, 1)); }
+static size_t bd_prod_bytes(int64_t n, int64_t m) {
+    return bd_maps_bytes(m) + a256(8 * (size_t)n * padded_width(m)) + a256(16 * (size_t)n * m);
+}
 size_t gmres_blockdiag_workspace_bytes(int64_t n, int64_t m, int r) {
     MgWork W;
-    return mg_layout(n, padded_width(m), r, 128 * (size_t)std::max<int64_t>(m, 1), nullptr, &W);
+    return mg_layout(n, padded_width(m), r, bd_prod_bytes(n, m), nullptr, &W);
 }
 
 // ---- kernels ---------------------------------------------------------------------------
@@ -940,17 +946,82 @@ static int gs_maps(GsMaps* g, const float2* V, const float2* src, int64_t n, int
     return tmap_encode(&g->src, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, src, dv, sv, bv, CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
+// ---------------------------------------------------------------------------------------
+// Near-field right preconditioner of the batched (block-diagonal) systems: column c belongs to
+// mesh i = c / nc and is preconditioned by M_i, rows eoff[i] .. eoff[i] + E_i of the ELL rows
+// of MB_SPAI_WIDTH (local column, value) pairs that mb_spai_build_c64 builds for the batch.
+// Each Arnoldi step multiplies Z by M V_j; each cycle's update V y goes through M before it
+// is added to X.
+// ---------------------------------------------------------------------------------------
+struct BdPrecond {
+    const int32_t* cols;
+    const float2* vals;
+    const int64_t* desc;  // the batch descriptor (E_i in column 2)
+    const int64_t* eoff;  // [n_mesh] first global edge of each mesh
+    int nc;
+    float2* z32;          // [n, mp] M V_j
+    double2* u;           // [n, m] the cycle's update before M
+};
+
+// z = M v on the padded [n, mp] complex64 layout (FP32); rows beyond E_i and padding columns 0
+__global__ void __launch_bounds__(256) bd_precond_kernel(BdPrecond P, int64_t n, int64_t m, int64_t mp,
+                                                         const float2* __restrict__ v, float2* __restrict__ z) {
+    const int64_t c = (int64_t)blockIdx.x * 32 + (threadIdx.x & 31);
+    const int64_t r = (int64_t)blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (r >= n || c >= mp) return;
+    float sr = 0.f, si = 0.f;
+    if (c < m) {
+        const int i = (int)(c / P.nc);
+        if (r < P.desc[6 * i + 2]) {
+            const int64_t g = P.eoff[i] + r;
+            for (int q = 0; q < MB_SPAI_WIDTH; ++q) {
+                const int32_t col = __ldg(P.cols + g * MB_SPAI_WIDTH + q);
+                if (col < 0) break;
+                const float2 mq = __ldg(P.vals + g * MB_SPAI_WIDTH + q), x = v[col * mp + c];
+                sr = fmaf(mq.x, x.x, fmaf(-mq.y, x.y, sr));
+                si = fmaf(mq.x, x.y, fmaf(mq.y, x.x, si));
+            }
+        }
+    }
+    z[r * mp + c] = make_float2(sr, si);
+}
+
+// x += M u on the [n, m] complex128 layout (FP64)
+__global__ void __launch_bounds__(256) bd_update_kernel(BdPrecond P, int64_t n, int64_t m,
+                                                        const double2* __restrict__ u, double2* __restrict__ x) {
+    const int64_t c = (int64_t)blockIdx.x * 32 + (threadIdx.x & 31);
+    const int64_t r = (int64_t)blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (r >= n || c >= m) return;
+    const int i = (int)(c / P.nc);
+    if (r >= P.desc[6 * i + 2]) return;
+    const int64_t g = P.eoff[i] + r;
+    double sr = 0.0, si = 0.0;
+    for (int q = 0; q < MB_SPAI_WIDTH; ++q) {
+        const int32_t col = __ldg(P.cols + g * MB_SPAI_WIDTH + q);
+        if (col < 0) break;
+        const float2 mq = __ldg(P.vals + g * MB_SPAI_WIDTH + q);
+        const double2 y = u[col * m + c];
+        sr = fma((double)mq.x, y.x, fma(-(double)mq.y, y.y, sr));
+        si = fma((double)mq.x, y.y, fma((double)mq.y, y.x, si));
+    }
+    double2 o = x[r * m + c];
+    o.x += sr;
+    o.y += si;
+    x[r * m + c] = o;
+}
+
 // The lockstep driver.  prod(v, y, stream) computes Y = Z V for [n, mp] complex64 blocks
 // (mp = m rounded up to even; the padding column has b = 0 and stays inactive).
 // desc / nc (optional): block-diagonal layout, column c of mesh c / nc has desc[.][2] rows.
 // With use_graph, the r Arnoldi steps of a cycle are captured once as a CUDA graph and
 // replayed every cycle (no host synchronisation inside a cycle; a cycle always runs its r
 // steps, columns that converged early are inactive).
+// pc (optional): right preconditioner of the block-diagonal systems (see BdPrecond).
 template <typename Prod>
 static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int64_t m, int r, int max_iters,
                           double tol, size_t prod_ws, const int64_t* desc, int nc, void* workspace, size_t ws_bytes,
                           bool use_graph, int64_t* iters_out, int64_t* cycles_out, double* max_relres_out,
-                          int* status_out, cudaStream_t s) {
+                          int* status_out, cudaStream_t s, const BdPrecond* pc = nullptr) {
     if (n <= 0 || m <= 0) return set_error(MB_ERR_ARG, "n and m must be > 0");
     if (((uintptr_t)x | (uintptr_t)b) & 15) return set_error(MB_ERR_ARG, "b and x must be 16-byte aligned");
     if (r < 1 || r > kMgMaxRestart) return set_error(MB_ERR_ARG, "restart must be in [1, %d]", kMgMaxRestart);
@@ -1022,8 +1093,13 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
         int e;
         const int nb = j + 1;
         const size_t dsm = gs_smem<kS>((size_t)nb * 32 * 16), csm = gs_smem<kS>((size_t)nb * 32 * 8);
-        if ((e = prod(reinterpret_cast<const float*>(W.V + (size_t)j * nm), reinterpret_cast<float*>(W.y32), st)))
-            return e;
+        const float2* vj = W.V + (size_t)j * nm;
+        if (pc) {
+            bd_precond_kernel<<<dim3((unsigned)((mp + 31) / 32), (unsigned)((n + 7) / 8)), 256, 0, st>>>(
+                *pc, n, m, mp, vj, pc->z32);
+            vj = pc->z32;
+        }
+        if ((e = prod(reinterpret_cast<const float*>(vj), reinterpret_cast<float*>(W.y32), st))) return e;
         // CGS2: pass 1 projects the product output y into w, pass 2 re-orthogonalises w and
         // accumulates |w|^2
         cudaMemsetAsync(W.hc, 0, 16 * (size_t)nb * mp, st);
@@ -1106,9 +1182,16 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
             }
         }
         mg_backsolve<<<cb, 32, (size_t)r * 32 * 16, s>>>(W.H, W.g, W.jend, r, mp, W.yv);
-        if (j > 0)
+        if (j > 0 && pc) {
+            cudaMemsetAsync(pc->u, 0, 16 * (size_t)n * m, s);
+            upd_k<<<cgrid, kGsThreads, gs_smem<kS>((size_t)j * 32 * 8), s>>>(maps_w, W.yv, n, mp, m, j, 1.f, pc->u,
+                                                                           nullptr, W.status);
+            bd_update_kernel<<<dim3((unsigned)((m + 31) / 32), (unsigned)((n + 7) / 8)), 256, 0, s>>>(
+                *pc, n, m, pc->u, reinterpret_cast<double2*>(x));
+        } else if (j > 0) {
             upd_k<<<cgrid, kGsThreads, gs_smem<kS>((size_t)j * 32 * 8), s>>>(maps_w, W.yv, n, mp, m, j, 1.f, x,
                                                                            nullptr, W.status);
+        }
         if ((rc = check_status())) return cleanup(), rc;
     }
     cleanup();
@@ -1133,7 +1216,7 @@ int gmres_multi_column_steps(const void* ws, int64_t n, int64_t m, int r, int32_
     return column_steps(ws, n, m, r, cgemm_workspace_bytes(n, padded_width(m)), out, s);
 }
 int gmres_blockdiag_column_steps(const void* ws, int64_t n, int64_t m, int r, int32_t* out, cudaStream_t s) {
-    return column_steps(ws, n, m, r, 128 * (size_t)std::max<int64_t>(m, 1), out, s);
+    return column_steps(ws, n, m, r, bd_prod_bytes(n, m), out, s);
 }
 
 int gmres_multi(const float* z_hi, const float* z_lo, int64_t n, const double* b, double* x, int64_t m, int r,
@@ -1154,15 +1237,22 @@ int gmres_multi(const float* z_hi, const float* z_lo, int64_t n, const double* b
 
 // Many meshes, each with its own Z_i and nc right-hand sides: the block-diagonal system on
 // the padded [n_rows, m] layout (m = n_mesh * nc columns).
-int gmres_blockdiag(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
-                    int rows_per_warp, int nc, int64_t n_rows, const double* b, double* x, int r, int max_iters,
-                    double tol, bool use_graph, void* workspace, size_t ws_bytes, int64_t* iters_out,
-                    int64_t* cycles_out, double* max_relres_out, int* status_out, cudaStream_t s) {
+static int blockdiag_solve(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
+                           int rows_per_warp, int nc, int64_t n_rows, const double* b, double* x, int r,
+                           int max_iters, double tol, bool use_graph, void* workspace, size_t ws_bytes,
+                           int64_t* iters_out, int64_t* cycles_out, double* max_relres_out, int* status_out,
+                           cudaStream_t s, const int32_t* m_cols, const float* m_vals, const int64_t* eoff) {
     const int64_t m = (int64_t)n_mesh * nc, mp = padded_width(m);
     MgWork W;
-    const size_t map_bytes = 128 * (size_t)std::max<int64_t>(m, 1);  // >= n_mesh tensor maps
+    const size_t map_bytes = bd_prod_bytes(n_rows, m);  // tensor maps (>= n_mesh) + preconditioner buffers
     if (ws_bytes < mg_layout(n_rows, mp, r, map_bytes, nullptr, &W)) return set_error(MB_ERR_ARG, "workspace too small");
     mg_layout(n_rows, mp, r, map_bytes, workspace, &W);
+    BdPrecond pc{};
+    if (m_cols) {
+        char* q = static_cast<char*>(W.gemm_ws) + bd_maps_bytes(m);
+        pc = BdPrecond{m_cols, reinterpret_cast<const float2*>(m_vals), desc, eoff, nc, reinterpret_cast<float2*>(q),
+                       reinterpret_cast<double2*>(q + a256(8 * (size_t)n_rows * mp))};
+    }
     int* status = W.status;
     const CUtensorMap* zmaps = static_cast<const CUtensorMap*>(W.gemm_ws);
     if (rows_per_warp == kBdRows) {
@@ -1178,7 +1268,27 @@ int gmres_blockdiag(const float* z, const int64_t* desc, const int64_t* goff, in
         return blockdiag_matvec(z, desc, goff, n_mesh, total_warps, v32, mp, nc, rows_per_warp, y32, st);
     };
     return gmres_lockstep(prod, n_rows, b, x, m, r, max_iters, tol, map_bytes, desc, nc, workspace, ws_bytes, use_graph,
-                          iters_out, cycles_out, max_relres_out, status_out, s);
+                          iters_out, cycles_out, max_relres_out, status_out, s, m_cols ? &pc : nullptr);
+}
+
+int gmres_blockdiag(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
+                    int rows_per_warp, int nc, int64_t n_rows, const double* b, double* x, int r, int max_iters,
+                    double tol, bool use_graph, void* workspace, size_t ws_bytes, int64_t* iters_out,
+                    int64_t* cycles_out, double* max_relres_out, int* status_out, cudaStream_t s) {
+    return blockdiag_solve(z, desc, goff, n_mesh, total_warps, rows_per_warp, nc, n_rows, b, x, r, max_iters, tol,
+                           use_graph, workspace, ws_bytes, iters_out, cycles_out, max_relres_out, status_out, s,
+                           nullptr, nullptr, nullptr);
+}
+
+int gmres_blockdiag_pc(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
+                       int rows_per_warp, int nc, int64_t n_rows, const int32_t* m_cols, const float* m_vals,
+                       const int64_t* eoff, const double* b, double* x, int r, int max_iters, double tol,
+                       bool use_graph, void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out,
+                       double* max_relres_out, int* status_out, cudaStream_t s) {
+    if (!m_cols || !m_vals || !eoff) return set_error(MB_ERR_ARG, "gmres_blockdiag_pc: null preconditioner");
+    return blockdiag_solve(z, desc, goff, n_mesh, total_warps, rows_per_warp, nc, n_rows, b, x, r, max_iters, tol,
+                           use_graph, workspace, ws_bytes, iters_out, cycles_out, max_relres_out, status_out, s, m_cols,
+                           m_vals, eoff);
 }
 
 }  // namespace mb

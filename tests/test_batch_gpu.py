@@ -130,3 +130,47 @@ def test_batched_reference_cfie_matches_per_mesh_and_solves(pkg, cuda):
         ref = torch.linalg.solve(bt.z_block(Z, i).to(torch.complex128), B[:e, 4 * i:4 * i + 4].to(torch.complex128))
         err = (torch.linalg.norm(X[:e, 4 * i:4 * i + 4] - ref, dim=0) / torch.linalg.norm(ref, dim=0)).max().item()
         assert err < 1e-4, (i, err)
+
+
+def test_batch_spai_equals_per_mesh_spai(pkg, cuda):
+    """The near-field preconditioner built over the whole batch (one launch, flat Z with even
+    row pitches, global near-pair list) equals the one built for each mesh alone."""
+    bt, meshes, ks = _batch(pkg, cuda)
+    bt.excitation(_waves(pkg, bt.n_mesh, 4, ks, cuda))
+    Z = bt.assemble()
+    P = bt.spai(Z)
+    assert P.status == 0
+    MM = pkg.mesh_MOM_3d
+    for i, (v, f) in enumerate(meshes):
+        vt = torch.tensor(np.asarray(v), dtype=torch.float32, device=cuda)
+        ft = torch.tensor(np.asarray(f), dtype=torch.int32, device=cuda)
+        edges, fei, _ = pkg.utils.get_edge_unique(vt, ft)
+        e = edges.shape[0]
+        Pi = MM.spai_preconditioner(bt.z_block(Z, i).contiguous(), vt, ft, fei, e)
+        o = int(bt.edge_offsets[i])
+        assert torch.equal(P.cols[o:o + e], Pi.cols)
+        assert torch.equal(P.vals[o:o + e], Pi.vals)
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_batched_preconditioned_solve_matches_dense(pkg, cuda, use_graph):
+    bt, meshes, ks = _batch(pkg, cuda)
+    waves = _waves(pkg, bt.n_mesh, 4, ks, cuda, seed=1)
+    Z = bt.assemble()
+    B = bt.excitation(waves)
+    bt.autotune(Z)
+    P = bt.spai(Z)
+    X, info = bt.solve(Z, B, restart=50, tol=1e-6, max_iters=3000, use_graph=use_graph, M=P)
+    X0, info0 = bt.solve(Z, B, restart=50, tol=1e-6, max_iters=3000, use_graph=use_graph)
+    assert info["converged"], info
+    assert info["iterations"] < info0["iterations"]
+    steps = info["column_iterations"].cpu().numpy()
+    assert steps.max() <= info["iterations"]
+    for i in range(bt.n_mesh):
+        Zi = bt.z_block(Z, i).to(torch.complex128)
+        e = bt.n_edges[i]
+        ref = torch.linalg.solve(Zi, B[:e, 4 * i:4 * i + 4].to(torch.complex128))
+        got = X[:e, 4 * i:4 * i + 4]
+        err = (torch.linalg.norm(got - ref, dim=0) / torch.linalg.norm(ref, dim=0)).max().item()
+        assert err < 1e-3, (i, err)
+        assert torch.all(X[e:, 4 * i:4 * i + 4] == 0)
