@@ -1790,7 +1790,7 @@ def time_to_solution(pkg, dev, level, k, sym, gq=4, Z=None, repeats=2):
     * plain_device: the same assembly, then the device-resident GMRES of the mixed path
       without its preconditioner (mb_pgmres_c64 with no M);
     * mixed_fp32 / mixed: the same FP32 assembly + excitation, the near-field sparse approximate
-      inverse (mb_spai_build_c64), then right-preconditioned GMRES(100) with the restart cycle
+      inverse (mb_spai_build_c64), then right-preconditioned GMRES(50) with the restart cycle
       on the device as a CUDA graph (mb_pgmres_c64: complex64 basis, FP64 Hessenberg and iterate,
       compensated refinement residual); mixed reads a half-precision copy of Z in the Arnoldi
       products.
@@ -1838,7 +1838,7 @@ def time_to_solution(pkg, dev, level, k, sym, gq=4, Z=None, repeats=2):
             return M.gmres(Z, b, restart=50, tol=tol, max_iters=20000)
         if path == "plain_device":
             return M.pgmres(Z, b, M=None, restart=50, tol=tol, max_iters=20000, use_graph=True)
-        return M.pgmres(Z, b, M=PH[0], restart=100, tol=tol, max_iters=20000, use_graph=True, Z_half=PH[1],
+        return M.pgmres(Z, b, M=PH[0], restart=50, tol=tol, max_iters=20000, use_graph=True, Z_half=PH[1],
                         inner_rtol=3e-3)
 
     # FP64 reference J (untimed)
@@ -1906,7 +1906,7 @@ def time_to_solution(pkg, dev, level, k, sym, gq=4, Z=None, repeats=2):
     out["plain_device"]["what"] = ("FP32 assembly + excitation, the mixed path's device-resident GMRES(50) from "
                                    "zero without the preconditioner (mb_pgmres_c64, no M)")
     out["mixed_fp32"]["what"] = ("FP32 assembly + excitation, near-field SAI preconditioner (mb_spai_build_c64), "
-                                 "right-preconditioned GMRES(100) with the restart cycle on the device as a CUDA "
+                                 "right-preconditioned GMRES(50) with the restart cycle on the device as a CUDA "
                                  "graph, complex64 basis, compensated-FP32 refinement residual (mb_pgmres_c64)")
     out["mixed"]["what"] = ("as mixed_fp32, with the Arnoldi products on a half-precision copy of Z "
                             "(mb_half_copy_c64, made inside the timed region) and each inner cycle ended at a 3e-3 "

@@ -126,9 +126,18 @@ int mb_mom_zmat_rwg_edges_c64(const float* verts, int64_t n_verts, const int32_t
                               const float* gp_x, const float* gw_x, int n_x, const float* gp_y,
                               const float* gw_y, int n_y, double wavenumber, int64_t m_begin, int64_t m_end,
                               float* z, void* stream);
+/* The same matrix in gather form: thread (m, n) sums the (up to 2 x 2) face-edge entries of
+ * Z[m, n] and writes the entry once (no atomics): rows [m_begin, m_end) of z are OVERWRITTEN
+ * (no zeroing needed; half the DRAM traffic of the edge order, ~3 % slower at 20480 faces).
+ * edge_rows from mb_mom_edge_rows; float32 meshes, gaussQR 2-5. */
+int mb_mom_zmat_rwg_gather_c64(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                               const float* face_areas, const float* face_normals, const int32_t* edge_rows,
+                               int64_t n_edges, const float* gp_x, const float* gw_x, int n_x, const float* gp_y,
+                               const float* gw_y, int n_y, double wavenumber, int64_t m_begin, int64_t m_end,
+                               float* z, void* stream);
 /* Z into host memory z_host [n_edges, n_edges] complex64 (pinned for overlap): the rows are
- * assembled in `chunks` ranges into the device scratch z_dev [n_edges, n_edges] and each range
- * is copied to z_host on a second stream while the next one is assembled; edge_rows device
+ * assembled in `chunks` ranges into the device scratch z_dev [n_edges, n_edges]
+ * and each range is copied to z_host on a second stream while the next one is assembled; edge_rows device
  * scratch [2 n_edges + 1].  Meshes with an edge of more than two faces, or rules without an
  * edge-row instance, are assembled face row by face row and copied once.  Returns when the
  * work is queued; the calling stream waits for the last copy. */
@@ -426,8 +435,10 @@ int mb_gmres_blockdiag_c64(const float* z, const int64_t* desc, const int64_t* g
 /* mb_gmres_blockdiag_c64 with the near-field right preconditioner of every mesh: m_cols /
  * m_vals from mb_spai_build_c64 run on the whole batch (desc rows (first face, F_i, first
  * edge, E_i, offset of Z_i, row pitch)), edge_offsets [n_mesh] int64 the first global edge of
- * each mesh (device).  Each Arnoldi step multiplies Z_i by M_i V_j; each cycle's update goes
- * through M_i before it is added to X.  Same workspace as mb_gmres_blockdiag_c64 (its size
+ * each mesh (device); nc in {1, 2, 4, 8}.  Each Arnoldi step multiplies Z_i by M_i V_j; each
+ * cycle's update goes through M_i before it is added to X, and each cycle starts from the
+ * residual B - Z X by compensated FP32 dot products (FP64-class accuracy, so tolerances below
+ * the FP32 product's ~1e-6 are reachable).  Same workspace as mb_gmres_blockdiag_c64 (its size
  * includes the preconditioned vectors). */
 int mb_gmres_blockdiag_pc_c64(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh,
                               int64_t total_warps, int rows_per_warp, int nc, int64_t n_rows, const int32_t* m_cols,

@@ -42,6 +42,8 @@ _SIGS = {
     "mb_gmres_multi_column_steps": [_P, _I64, _I64, _I, _P, _P],
     "mb_mom_zmat_rwg_edges_c64": [_P, _I64, _P, _I64, _P, _P, _P, _P, _I64, _P, _P, _I, _P, _P, _I, _D,
                                   _I64, _I64, _P, _P],
+    "mb_mom_zmat_rwg_gather_c64": [_P, _I64, _P, _I64, _P, _P, _P, _I64, _P, _P, _I, _P, _P, _I, _D, _I64, _I64,
+                                   _P, _P],
     "mb_mom_zmat_rwg_to_host_c64": [_P, _I64, _P, _I64, _P, _P, _P, _I64, _P, _P, _I, _P, _P, _I, _D,
                                     _P, _P, _P, _I, _P],
     "mb_mom_rhs_rwg_c64": [_P, _I64, _P, _I64, _P, _P, _P, _I64, _P, _P, _I, _P, _I, _P, _P],

@@ -93,6 +93,10 @@ bool launch_fast_zmat_edges(const float* verts, const int32_t* faces, const floa
                             const int32_t* fei, const int32_t* edge_rows, int64_t n_edges, const float* gpx,
                             const float* gwx, int nx, const float* gpy, const float* gwy, int ny, double k,
                             int64_t nf, int64_t m_begin, int64_t m_end, float* z, cudaStream_t stream);
+bool launch_fast_zmat_gather(const float* verts, const int32_t* faces, const float* areas, const float* normals,
+                             const int32_t* edge_rows, int64_t n_edges, const float* gpx, const float* gwx, int nx,
+                             const float* gpy, const float* gwy, int ny, double k, int64_t m_begin, int64_t m_end,
+                             float* z, cudaStream_t stream);
 int zmat_edges_to_host(const float* verts, const int32_t* faces, const float* areas, const float* normals,
                        const int32_t* fei, const int32_t* edge_rows, int64_t n_edges, const float* gpx,
                        const float* gwx, int nx, const float* gpy, const float* gwy, int ny, double k, int64_t nf,
@@ -267,6 +271,24 @@ int mb_mom_zmat_rwg_edges_c64(const float* verts, int64_t n_verts, const int32_t
                                 as_stream(stream)))
         return set_error(MB_ERR_UNSUPPORTED, "edge-row assembly: no instance for rule sizes (%d, %d)", n_x, n_y);
     return check_launch("mom_ref_zmat_edges");
+}
+
+int mb_mom_zmat_rwg_gather_c64(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,
+                               const float* face_areas, const float* face_normals, const int32_t* edge_rows,
+                               int64_t n_edges, const float* gp_x, const float* gw_x, int n_x, const float* gp_y,
+                               const float* gw_y, int n_y, double wavenumber, int64_t m_begin, int64_t m_end,
+                               float* z, void* stream) {
+    (void)n_verts;
+    MB_REQUIRE(n_faces >= 0 && n_edges >= 0, "bad sizes");
+    MB_REQUIRE(0 <= m_begin && m_begin <= m_end && m_end <= n_edges, "row range outside [0, n_edges)");
+    MB_REQUIRE(verts && faces && face_areas && face_normals && edge_rows && gp_x && gw_x && gp_y && gw_y && z,
+               "null pointer argument");
+    MB_REQUIRE(wavenumber > 0, "wavenumber must be > 0");
+    MB_REQUIRE((m_end - m_begin) * ((n_edges + 127) / 128) < 0x7fffffffLL, "mesh too large for one launch");
+    if (!launch_fast_zmat_gather(verts, faces, face_areas, face_normals, edge_rows, n_edges, gp_x, gw_x, n_x, gp_y,
+                                 gw_y, n_y, wavenumber, m_begin, m_end, z, as_stream(stream)))
+        return set_error(MB_ERR_UNSUPPORTED, "gather assembly: no instance for rule sizes (%d, %d)", n_x, n_y);
+    return check_launch("mom_ref_zmat_gather");
 }
 
 int mb_mom_zmat_rwg_to_host_c64(const float* verts, int64_t n_verts, const int32_t* faces, int64_t n_faces,

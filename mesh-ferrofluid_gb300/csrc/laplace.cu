@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(kLapThreads) laplace_panels_tiled_kernel(
     __shared__ T s_y[kLapTileRows][Q][3];  // y points of the tile's rows
     __shared__ T s_ny[kLapTileRows][3];
     __shared__ T s_ay[kLapTileRows];
-    __shared__ __align__(16) T s_out[NC][kLapThreads * NN];
+    __shared__ __align__(16) T s_out[2][NC][kLapThreads * NN];  // double-buffered row staging
     const int tid = threadIdx.x;
     const int64_t col_block = (int64_t)blockIdx.x % col_blocks;
     const int64_t fy0 = row_begin + ((int64_t)blockIdx.x / col_blocks) * kLapTileRows;
@@ -301,13 +301,27 @@ __global__ void __launch_bounds__(kLapThreads) laplace_panels_tiled_kernel(
         }
     }
     const int64_t valid = (nf - col0) < kLapThreads ? (nf - col0) : kLapThreads;
+    // the relations of this thread's pairs in all rows of the tile, loaded up front (one
+    // latency instead of one per row)
+    static_assert(kLapTileRows <= 16, "relations packed into two 64-bit words");
+    unsigned long long rel_lo = 0, rel_hi = 0;  // byte r: relation of row r
+#pragma unroll
+    for (int r = 0; r < kLapTileRows; ++r) {
+        const unsigned long long q =
+            (fx < nf && r < rows)
+                ? (rel ? __ldg(rel + (fy0 + r) * nf + fx) : (unsigned)relation_of<T>(faces, fy0 + r, fx))
+                : 0u;
+        if (r < 8) rel_lo |= q << (8 * r);
+        else rel_hi |= q << (8 * (r - 8));
+    }
+#pragma unroll 1
     for (int r = 0; r < rows; ++r) {
         const int64_t fy = fy0 + r;
         T accr[NN], acci[NN];
 #pragma unroll
         for (int c = 0; c < NN; ++c) { accr[c] = 0; acci[c] = 0; }
         if (fx < nf) {
-            const int rl = rel ? (int)rel[fy * nf + fx] : relation_of<T>(faces, fy, fx);
+            const int rl = (int)(((r < 8 ? rel_lo >> (8 * r) : rel_hi >> (8 * (r - 8)))) & 0xffull);
             if (rl == 0) {
                 const T nyx = s_ny[r][0], nyy = s_ny[r][1], nyz = s_ny[r][2];
                 T yr[Q][3];
@@ -375,18 +389,20 @@ __global__ void __launch_bounds__(kLapThreads) laplace_panels_tiled_kernel(
                 acci[c] *= scale;
             }
         }
+        // row r goes through buffer r & 1: the barrier below also orders the stores of row
+        // r - 1 before buffer (r + 1) & 1 is written again
+        T(&so)[NC][kLapThreads * NN] = s_out[r & 1];
 #pragma unroll
         for (int c = 0; c < NN; ++c) {
-            s_out[0][tid * NN + c] = accr[c];
-            if constexpr (KIND == 1) s_out[NC - 1][tid * NN + c] = acci[c];
+            so[0][tid * NN + c] = accr[c];
+            if constexpr (KIND == 1) so[NC - 1][tid * NN + c] = acci[c];
         }
         __syncthreads();
         const int64_t base = ((fy - row_begin) * nf + col0) * NN;
         for (int64_t c = tid; c < valid * NN; c += kLapThreads) {
-            out_r[base + c] = s_out[0][c];
-            if constexpr (KIND == 1) out_i[base + c] = s_out[NC - 1][c];
+            out_r[base + c] = so[0][c];
+            if constexpr (KIND == 1) out_i[base + c] = so[NC - 1][c];
         }
-        __syncthreads();
     }
 }
 

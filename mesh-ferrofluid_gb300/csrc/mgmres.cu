@@ -956,12 +956,109 @@ static int gs_maps(GsMaps* g, const float2* V, const float2* src, int64_t n, int
 struct BdPrecond {
     const int32_t* cols;
     const float2* vals;
-    const int64_t* desc;  // the batch descriptor (E_i in column 2)
+    const int64_t* desc;  // the batch descriptor (E_i in column 2, offset of Z_i in column 3)
     const int64_t* eoff;  // [n_mesh] first global edge of each mesh
+    int n_mesh;
     int nc;
+    const float2* z;      // the flat block-diagonal Z (row pitch E_i rounded up to even)
     float2* z32;          // [n, mp] M V_j
-    double2* u;           // [n, m] the cycle's update before M
+    double2* u;           // [n, m] the cycle's update before M (the split X at a cycle start)
 };
+
+// X (complex128 [n, m]) -> FP32 (hi, lo) parts, float4 [n, m]
+__global__ void bd_split_kernel(const double2* __restrict__ x, int64_t count, float4* __restrict__ xs) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const double2 v = x[k];
+    const float hr = (float)v.x, hi = (float)v.y;
+    xs[k] = make_float4(hr, hi, (float)(v.x - (double)hr), (float)(v.y - (double)hi));
+}
+
+__device__ __forceinline__ void bd_two_sum(float& s, float t, float& e) {
+    const float u = __fadd_rn(s, t);
+    const float bb = __fsub_rn(u, s);
+    e = __fadd_rn(__fsub_rn(s, __fsub_rn(u, bb)), __fsub_rn(t, bb));
+    s = u;
+}
+
+// Refinement residual of the block-diagonal systems, R = B - Z X with X given by its FP32
+// split: compensated FP32 dot products (exact products by TwoProduct, exact running sums by
+// TwoSum, the rounding terms and the x_lo products summed beside them, lane sums combined in
+// FP64) -- FP64-class accuracy at FP32 instruction speed.  One warp per Z row (global row g:
+// mesh i, local row k) and all NC columns of the mesh; R (complex64) into V_0 [n, mp] (the
+// caller zeroes it) and |R|^2 per column into sq.
+template <int NC>
+__global__ void __launch_bounds__(256) bd_residual_kernel(BdPrecond P, int64_t total_rows, int64_t m, int64_t mp,
+                                                          const float4* __restrict__ xs, const double2* __restrict__ b,
+                                                          float2* __restrict__ r, double* __restrict__ sq) {
+    const int64_t g = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (g >= total_rows) return;
+    int lo = 0, hi = P.n_mesh - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (P.eoff[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    const int i = lo;
+    const int64_t e = P.desc[6 * i + 2], k = g - P.eoff[i];
+    const float2* zr = P.z + P.desc[6 * i + 3] + k * (e + (e & 1));
+    const int64_t c0 = (int64_t)i * NC;
+    float sr[NC], si[NC], cr[NC], ci[NC];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) sr[q] = si[q] = cr[q] = ci[q] = 0.f;
+    for (int64_t j = lane; j < e; j += 32) {
+        const float2 a = __ldcs(zr + j);
+#pragma unroll
+        for (int q = 0; q < NC; ++q) {
+            const float4 x = __ldg(xs + j * m + c0 + q);
+            const float p1 = __fmul_rn(a.x, x.x), e1 = fmaf(a.x, x.x, -p1);
+            const float p2 = __fmul_rn(-a.y, x.y), e2 = fmaf(-a.y, x.y, -p2);
+            const float p3 = __fmul_rn(a.x, x.y), e3 = fmaf(a.x, x.y, -p3);
+            const float p4 = __fmul_rn(a.y, x.x), e4 = fmaf(a.y, x.x, -p4);
+            float t1, t2, t3, t4;
+            bd_two_sum(sr[q], p1, t1);
+            bd_two_sum(sr[q], p2, t2);
+            bd_two_sum(si[q], p3, t3);
+            bd_two_sum(si[q], p4, t4);
+            cr[q] += (t1 + t2) + (e1 + e2) + fmaf(a.x, x.z, -a.y * x.w);
+            ci[q] += (t3 + t4) + (e3 + e4) + fmaf(a.x, x.w, a.y * x.z);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+        double ar = (double)sr[q] + (double)cr[q], ai = (double)si[q] + (double)ci[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            ar += __shfl_xor_sync(0xffffffffu, ar, o);
+            ai += __shfl_xor_sync(0xffffffffu, ai, o);
+        }
+        if (lane == 0) {
+            const int64_t c = c0 + q;
+            const double2 bv = b[k * m + c];
+            const double re = bv.x - ar, im = bv.y - ai;
+            r[k * mp + c] = make_float2((float)re, (float)im);
+            atomicAdd(sq + c, re * re + im * im);
+        }
+    }
+}
+
+static int bd_residual(const BdPrecond& P, int64_t total_rows, int64_t n, int64_t m, int64_t mp, const double* x,
+                       const double* b, float2* v0, double* sq, cudaStream_t s) {
+    bd_split_kernel<<<(unsigned)((n * m + 255) / 256), 256, 0, s>>>(reinterpret_cast<const double2*>(x), n * m,
+                                                                     reinterpret_cast<float4*>(P.u));
+    cudaMemsetAsync(v0, 0, 8 * (size_t)n * mp, s);
+    const unsigned blocks = (unsigned)((total_rows + 7) / 8);
+    const float4* xs = reinterpret_cast<const float4*>(P.u);
+    const double2* b2 = reinterpret_cast<const double2*>(b);
+    switch (P.nc) {
+        case 1: bd_residual_kernel<1><<<blocks, 256, 0, s>>>(P, total_rows, m, mp, xs, b2, v0, sq); break;
+        case 2: bd_residual_kernel<2><<<blocks, 256, 0, s>>>(P, total_rows, m, mp, xs, b2, v0, sq); break;
+        case 4: bd_residual_kernel<4><<<blocks, 256, 0, s>>>(P, total_rows, m, mp, xs, b2, v0, sq); break;
+        case 8: bd_residual_kernel<8><<<blocks, 256, 0, s>>>(P, total_rows, m, mp, xs, b2, v0, sq); break;
+        default: return set_error(MB_ERR_UNSUPPORTED, "preconditioned batch solve: nc must be 1, 2, 4 or 8");
+    }
+    return check_launch("bd_residual");
+}
 
 // z = M v on the padded [n, mp] complex64 layout (FP32); rows beyond E_i and padding columns 0
 __global__ void __launch_bounds__(256) bd_precond_kernel(BdPrecond P, int64_t n, int64_t m, int64_t mp,
@@ -1072,6 +1169,13 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
         mg_column_rows<<<cb, 32, 0, s>>>(desc, m, mp, nc, W.crow);
         crow = W.crow;
     }
+    int64_t pc_rows = 0;  // sum of E_i (the preconditioned block-diagonal residual's rows)
+    if (pc) {
+        std::vector<int64_t> dh((size_t)6 * pc->n_mesh);
+        cudaMemcpyAsync(dh.data(), pc->desc, 48 * (size_t)pc->n_mesh, cudaMemcpyDeviceToHost, s);
+        if ((rc = mg_sync(s, "gmres_blockdiag descriptor"))) return rc;
+        for (int i = 0; i < pc->n_mesh; ++i) pc_rows += dh[(size_t)6 * i + 2];
+    }
     std::vector<double> hb(mp);
     cudaMemsetAsync(W.y32, 0, 8 * (size_t)nm, s);  // rows a product does not write stay 0
     cudaMemsetAsync(W.bnorm, 0, 8 * mp, s);
@@ -1132,11 +1236,16 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
     };
     while (true) {
         // residual of the current iterate through the same product (w holds complex64 X)
-        mg_to_c64<<<rgrid, rblk, 0, s>>>(reinterpret_cast<const double2*>(x), n, m, mp, W.w);
-        if ((rc = prod(reinterpret_cast<const float*>(W.w), reinterpret_cast<float*>(W.y32), s)))
-            return cleanup(), rc;
-        cudaMemsetAsync(W.beta, 0, 8 * mp, s);
-        mg_residual<<<rgrid, rblk, 0, s>>>(reinterpret_cast<const double2*>(b), W.y32, n, m, mp, W.V, W.beta);
+        if (pc) {  // compensated refinement residual of the block-diagonal systems
+            cudaMemsetAsync(W.beta, 0, 8 * mp, s);
+            if ((rc = bd_residual(*pc, pc_rows, n, m, mp, x, b, W.V, W.beta, s))) return cleanup(), rc;
+        } else {
+            mg_to_c64<<<rgrid, rblk, 0, s>>>(reinterpret_cast<const double2*>(x), n, m, mp, W.w);
+            if ((rc = prod(reinterpret_cast<const float*>(W.w), reinterpret_cast<float*>(W.y32), s)))
+                return cleanup(), rc;
+            cudaMemsetAsync(W.beta, 0, 8 * mp, s);
+            mg_residual<<<rgrid, rblk, 0, s>>>(reinterpret_cast<const double2*>(b), W.y32, n, m, mp, W.V, W.beta);
+        }
         cudaMemcpyAsync(hbeta.data(), W.beta, 8 * mp, cudaMemcpyDeviceToHost, s);
         if ((rc = mg_sync(s, "gmres_multi residual"))) return cleanup(), rc;
         worst = 0.0;
@@ -1250,7 +1359,8 @@ static int blockdiag_solve(const float* z, const int64_t* desc, const int64_t* g
     BdPrecond pc{};
     if (m_cols) {
         char* q = static_cast<char*>(W.gemm_ws) + bd_maps_bytes(m);
-        pc = BdPrecond{m_cols, reinterpret_cast<const float2*>(m_vals), desc, eoff, nc, reinterpret_cast<float2*>(q),
+        pc = BdPrecond{m_cols, reinterpret_cast<const float2*>(m_vals), desc, eoff, n_mesh, nc,
+                       reinterpret_cast<const float2*>(z), reinterpret_cast<float2*>(q),
                        reinterpret_cast<double2*>(q + a256(8 * (size_t)n_rows * mp))};
     }
     int* status = W.status;

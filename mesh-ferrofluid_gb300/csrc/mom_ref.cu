@@ -455,6 +455,41 @@ __global__ void __launch_bounds__(128, NX <= 4 ? MB_FAST_MIN_BLOCKS : 2) mom_ref
     atomicAdd(reinterpret_cast<float2*>(z + 2 * (m * n_edges + __ldg(fei + col))), make_float2(re, im));
 }
 
+// Gather form (RWG layout): thread (m, n) owns Z[m, n] and sums the (at most 2 x 2) face-edge
+// entries of test edge m and source edge n -- every face-edge pair still evaluated exactly
+// once -- then writes the entry with one coalesced store: no atomics, and no zeroing pass
+// (rows [m_begin, m_end) are overwritten).
+template <int NX, int NY>
+__global__ void __launch_bounds__(128, NX <= 4 ? MB_FAST_MIN_BLOCKS : 2) mom_ref_zmat_gather_kernel(
+    const float* __restrict__ verts, const int32_t* __restrict__ faces, const float* __restrict__ areas,
+    const float* __restrict__ normals, const int32_t* __restrict__ edge_rows, int64_t n_edges,
+    const float* __restrict__ gpx, const float* __restrict__ gwx, const float* __restrict__ gpy,
+    const float* __restrict__ gwy, float k, int64_t m_begin, int64_t col_blocks, float* __restrict__ z) {
+    __shared__ float4 s_t[NX * NX], s_s[NY * NY];
+    stage_rules<NX, NY>(gpx, gwx, gpy, gwy, s_t, s_s);
+    __syncthreads();
+    const int64_t m = m_begin + (int64_t)blockIdx.x / col_blocks;
+    const int64_t n = ((int64_t)blockIdx.x % col_blocks) * blockDim.x + threadIdx.x;
+    if (n >= n_edges) return;
+    float re = 0.f, im = 0.f;
+#pragma unroll 1
+    for (int j = 0; j < 2; ++j) {
+        const int32_t row = __ldg(edge_rows + 2 * m + j);
+        if (row < 0) continue;
+#pragma unroll 1
+        for (int q = 0; q < 2; ++q) {
+            const int32_t col = __ldg(edge_rows + 2 * n + q);
+            if (col < 0) continue;
+            float a, b;
+            mom_entry_fast<NX, NY>(verts, faces, areas, normals, s_t, s_s, k, row / 3, row % 3, col / 3, col % 3,
+                                   &a, &b);
+            re += a;
+            im += b;
+        }
+    }
+    reinterpret_cast<float2*>(z)[m * n_edges + n] = make_float2(re, im);
+}
+
 // Edge -> face-edge rows: slot 0 the smaller row, slot 1 the larger (or -1 for a boundary
 // edge); edge_rows[2E] is set to 1 when some edge has more than two faces.
 __global__ void edge_rows_init(int32_t* __restrict__ er, int64_t n_edges) {
@@ -523,6 +558,30 @@ bool launch_fast_zmat_edges(const float* verts, const int32_t* faces, const floa
 // ranges on stream s, each range copied to z_host on a second stream as soon as its kernel
 // ends (z_dev: device scratch [E, E]; edge_rows: from launch_edge_rows, every edge at most
 // two faces).  The calling stream waits for the last copy.
+// Gather-form launch over Z rows [m_begin, m_end) (overwritten); false when the rule sizes
+// have no fast instance.
+bool launch_fast_zmat_gather(const float* verts, const int32_t* faces, const float* areas, const float* normals,
+                             const int32_t* edge_rows, int64_t n_edges, const float* gpx, const float* gwx, int nx,
+                             const float* gpy, const float* gwy, int ny, double k, int64_t m_begin, int64_t m_end,
+                             float* z, cudaStream_t stream) {
+    const int64_t col_blocks = (n_edges + 127) / 128;
+    const int64_t blocks = (m_end - m_begin) * col_blocks;
+    if (blocks <= 0) return true;
+#define MB_FAST_G(NXV, NYV)                                                                           \
+    if (nx == NXV && ny == NYV) {                                                                     \
+        mom_ref_zmat_gather_kernel<NXV, NYV><<<(unsigned)blocks, 128, 0, stream>>>(                    \
+            verts, faces, areas, normals, edge_rows, n_edges, gpx, gwx, gpy, gwy, (float)k, m_begin,    \
+            col_blocks, z);                                                                           \
+        return true;                                                                                  \
+    }
+    MB_FAST_G(4, 3)
+    MB_FAST_G(3, 2)
+    MB_FAST_G(2, 1)
+    MB_FAST_G(5, 4)
+#undef MB_FAST_G
+    return false;
+}
+
 int zmat_edges_to_host(const float* verts, const int32_t* faces, const float* areas, const float* normals,
                        const int32_t* fei, const int32_t* edge_rows, int64_t n_edges, const float* gpx,
                        const float* gwx, int nx, const float* gpy, const float* gwy, int ny, double k, int64_t nf,

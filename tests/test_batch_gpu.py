@@ -160,10 +160,12 @@ def test_batched_preconditioned_solve_matches_dense(pkg, cuda, use_graph):
     B = bt.excitation(waves)
     bt.autotune(Z)
     P = bt.spai(Z)
-    X, info = bt.solve(Z, B, restart=50, tol=1e-6, max_iters=3000, use_graph=use_graph, M=P)
+    # tol 1e-9: reachable only because each cycle of the preconditioned path starts from a
+    # compensated (FP64-class) residual; the plain lockstep path's FP32 residual stops ~1e-6
+    X, info = bt.solve(Z, B, restart=50, tol=1e-9, max_iters=3000, use_graph=use_graph, M=P)
     X0, info0 = bt.solve(Z, B, restart=50, tol=1e-6, max_iters=3000, use_graph=use_graph)
     assert info["converged"], info
-    assert info["iterations"] < info0["iterations"]
+    assert info["iterations"] < 2 * info0["iterations"]
     steps = info["column_iterations"].cpu().numpy()
     assert steps.max() <= info["iterations"]
     for i in range(bt.n_mesh):
@@ -172,5 +174,5 @@ def test_batched_preconditioned_solve_matches_dense(pkg, cuda, use_graph):
         ref = torch.linalg.solve(Zi, B[:e, 4 * i:4 * i + 4].to(torch.complex128))
         got = X[:e, 4 * i:4 * i + 4]
         err = (torch.linalg.norm(got - ref, dim=0) / torch.linalg.norm(ref, dim=0)).max().item()
-        assert err < 1e-3, (i, err)
+        assert err < 1e-6, (i, err)
         assert torch.all(X[e:, 4 * i:4 * i + 4] == 0)

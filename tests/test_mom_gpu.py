@@ -191,7 +191,7 @@ def test_zmat_rwg_edge_order_equals_face_order(pkg, cuda, level, k):
 def test_zmat_rwg_to_host_equals_device(pkg, cuda, chunks):
     v, f, a, n, fei, ne, rules = _ico_setup(pkg, cuda, 3)
     M = pkg.mesh_MOM_3d
-    zd = M.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, 5.0, order="edges")
+    zd = M.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, 5.0, order="edges")  # the host path's kernel
     h = torch.empty((ne, ne), dtype=torch.complex64, pin_memory=True)
     scratch = torch.full((ne, ne), float("nan"), dtype=torch.complex64, device=cuda)  # overwritten
     M.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, 5.0, out=scratch, out_host=h, chunks=chunks)
@@ -360,10 +360,11 @@ def _scatter_rows(zfe_rows, row_ids, e, ne):
     return out
 
 
-def test_zmat_rwg_edges_ka10_full_L3_vs_oracle(pkg, cuda, oracle):
+@pytest.mark.parametrize("order", ["edges", "gather"])
+def test_zmat_rwg_edges_ka10_full_L3_vs_oracle(pkg, cuda, oracle, order):
     v, f, a, n, fei, ne, rules = _ico_setup(pkg, cuda, 3)
     k = 10.0
-    Z = pkg.mesh_MOM_3d.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, k, order="edges")
+    Z = pkg.mesh_MOM_3d.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, k, order=order)
     h = lambda t: t.cpu().double().numpy()  # noqa: E731
     zfe = oracle.mom_zmat_fe(h(v), f.cpu().numpy(), h(a), h(n), *(h(t) for t in rules), k)
     e = fei.cpu().numpy().reshape(-1).astype(np.int64)
@@ -381,7 +382,8 @@ def test_zmat_rwg_edges_ka10_L5_row_windows_vs_oracle(pkg, cuda, oracle):
     v, f, a, n, fei, ne, rules = _ico_setup(pkg, cuda, 5)
     k = 10.0
     er = pkg.mesh_MOM_3d.edge_rows(fei, f.shape[0], ne)
-    Z = pkg.mesh_MOM_3d.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, k, order="edges", edge_rows_map=er)
+    Z = torch.full((ne, ne), float("nan"), dtype=torch.complex64, device=cuda)  # gather overwrites every entry
+    pkg.mesh_MOM_3d.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, k, out=Z, order="gather", edge_rows_map=er)
     torch.cuda.synchronize()
     er2 = er[:-1].cpu().numpy().reshape(ne, 2).astype(np.int64)
     e = fei.cpu().numpy().reshape(-1).astype(np.int64)
@@ -477,3 +479,18 @@ def test_torch_ops_mesh_MOM_3d_match_reference(pkg, cuda, golden):
     ji = torch.zeros_like(jr)
     ops.interpolate_Icoeff_to_Js_3d_forward(v, f, fei, a, ic.real.contiguous(), ic.imag.contiguous(), jr, ji)
     assert rel_err((jr + 1j * ji).cpu().numpy(), g["mom_gq4_face_vert_js"]) < TOL64
+
+
+@pytest.mark.parametrize("level,k", [(2, 3.0), (3, 8.0)])
+def test_zmat_rwg_gather_equals_edge_order(pkg, cuda, level, k):
+    """Gather form: same entries as the atomic edge order; row windows overwrite exactly their rows."""
+    v, f, a, n, fei, ne, rules = _ico_setup(pkg, cuda, level)
+    M = pkg.mesh_MOM_3d
+    ze = M.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, k, order="edges")
+    zg = torch.full_like(ze, float("nan"))
+    M.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, k, out=zg, order="gather")
+    assert rel_err(zg.cpu().numpy(), ze.cpu().numpy()) < 1e-6
+    part = torch.full_like(ze, float("nan"))
+    for m0 in range(0, ne, 97):
+        M.assemble_Z_rwg(v, f, a, n, fei, ne, *rules, k, out=part, order="gather", rows=(m0, min(ne, m0 + 97)))
+    assert torch.equal(part, zg)
