@@ -69,6 +69,10 @@ WORKLOADS = {
     # Laplace mixed Dirichlet / Neumann solve, u = z on the unit sphere: (icosphere level, dtype)
     "laplace_mixed_L4": (4, "f32"),
     "laplace_mixed_L3": (3, "f32"),
+    # the mixed-precision EFIE solve alone (assembly + SAI + half copy + preconditioned GMRES to
+    # a 3e-5 residual, i.e. a <1e-4 error in J): (icosphere level, k)
+    "efie_solve_L5": (5, 10.0),
+    "efie_solve_L4": (4, 10.0),
     # learned initial guess: (training meshes, held-out meshes, incidences per mesh)
     "learned_star": (5000, 256, 4),
     "learned_star_small": (500, 64, 4),
@@ -147,6 +151,30 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------------------------------
+# replicas: one process per GPU, each timing its own copy of the workload (no exchange step)
+# ---------------------------------------------------------------------------------------
+def replica_barrier(world, dev=None):
+    """All ranks meet (torch.distributed.barrier when world > 1); then the device idles."""
+    import torch
+
+    if world > 1:
+        torch.distributed.barrier()
+    if dev is not None and dev.type == "cuda":
+        torch.cuda.synchronize(dev)
+
+
+def replica_max(value, world, dev=None):
+    """The largest of every rank's value (the slowest replica's time) -- all ranks get it."""
+    if world <= 1:
+        return float(value)
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev if dev is not None else "cpu")
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
 
 
 # ---------------------------------------------------------------------------------------
@@ -1919,11 +1947,81 @@ def time_to_solution(pkg, dev, level, k, sym, gq=4, Z=None, repeats=2):
     return out
 
 
+def main_efie_solve(args, rank, world, local_rank):
+    """The mixed-precision EFIE path of the time-to-solution comparison as its own workload:
+    each step assembles Z (7-point rule, complex64, FP64 near pairs), builds the near-field SAI
+    and the half-precision copy, and solves by right-preconditioned GMRES(50) to a 3e-5
+    relative residual; the error in J against an FP64 solution is checked after the timing."""
+    level, k = WORKLOADS[args.workload]
+    config = {"workload": args.workload, "mesh": f"icosphere L{level}", "ka": k, "formulation": "EFIE, 7-point rule",
+              "excitation": "x-polarised unit plane wave along +z", "parallelism": "replicas"}
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no symmetric-rule EFIE and "
+                              "solves by dense LU; its own algorithm is timed by mom_ref_*"}), flush=True)
+        return
+    import torch
+
+    pkg = importlib.import_module("mesh-ferrofluid_gb300")
+    M = pkg.mesh_MOM_3d
+    dev = torch.device("cuda", local_rank if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    v_np, f_np = pkg.meshes.icosphere(level)
+    verts = torch.tensor(v_np, dtype=torch.float32, device=dev)
+    faces = torch.tensor(f_np, dtype=torch.int32, device=dev)
+    edges, fei, _ = pkg.utils.get_edge_unique(verts, faces)
+    E = int(edges.shape[0])
+    near = M.near_pairs(faces)
+    pw = M.plane_waves(k, [[0.0, 0.0, 1.0]], [[1.0, 0.0, 0.0]], device=dev)
+    Z = torch.empty((E, E), dtype=torch.complex64, device=dev)
+
+    def step():
+        Z.zero_()
+        M.assemble_Z_rwg_sym(verts, faces, fei, E, k, out=Z, pairs=near, check_indices=False)
+        b = M.assemble_rhs_rwg_sym(verts, faces, fei, E, pw)[:, 0].to(torch.complex128)
+        P = M.spai_preconditioner(Z, verts, faces, fei, E, pairs=near)
+        x, info = M.pgmres(Z, b, M=P, restart=50, tol=3e-5, max_iters=5000, Z_half=M.half_copy(Z),
+                           inner_rtol=3e-3)
+        return x, info
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    stream = torch.cuda.current_stream(dev)
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        x, info = step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    Z64 = M.assemble_Z_rwg_sym(verts.double(), faces, fei, E, k, pairs=near, check_indices=False)
+    b64 = M.assemble_rhs_rwg_sym(verts.double(), faces, fei, E, pw)[:, 0]
+    P = M.spai_preconditioner(Z, verts, faces, fei, E, pairs=near)
+    j_ref, _ = M.pgmres(Z64, b64, M=P, restart=50, tol=1e-12, max_iters=20000)
+    err = float((x - j_ref).norm() / j_ref.norm())
+    line = {"metric": "time to a <1e-4 relative error in J, mixed-precision EFIE path", "value": ms, "unit": "ms",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 assembly (FP64 near pairs), binary16 Arnoldi products, FP64 Hessenberg and iterate",
+            "data": "synthetic", "config": config, "iterations": info[0]["iterations"],
+            "restarts": info[0]["restarts"], "rel_residual": info[0]["rel_residual"], "rel_err_J_vs_fp64": err,
+            "clocks": clocks.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = _args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload.startswith("efie_solve_"):
+        return main_efie_solve(args, rank, world, local_rank)
     if args.workload.startswith("ray_"):
         return main_rays(args, rank, world, local_rank)
     if args.workload.startswith("pressure_"):
@@ -2021,9 +2119,7 @@ def main():
         assemble(Z)
 
     def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize(dev)
+        replica_barrier(world, dev)
 
     for _ in range(args.warmup):
         step()
@@ -2045,11 +2141,7 @@ def main():
     clocks.stop()
     step_ms = [a.elapsed_time(c) for a, _, c in ev]
     kern_ms = [b.elapsed_time(c) for _, b, c in ev]
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = replica_max(sum(step_ms), world, dev)  # the slowest replica
     ms_per_step = total_ms / args.steps
     value = world * pairs / (ms_per_step / 1e3)
     kern_avg_s = statistics.mean(kern_ms) / 1e3
