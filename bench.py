@@ -869,7 +869,7 @@ def main_lapref(args, rank, world, local_rank):
                                                    "collapse, no vertex alignment of the singular sub-domains)"},
             "breakdown_ms": {"panel_relation": t_rel, "V_panels": t_v, "K_panels": t_k, "pack_one_operator": t_pack,
                              "lu_solve_VxV": t_lu},
-            "roofline": {"kernel": "laplace_panels_kernel<float, 3, 0, 1> (V panels)", "bound": "fp32 / hbm",
+            "roofline": {"kernel": "laplace_panels_pair2_kernel<3, 1> + laplace_near_rows_kernel (V panels)", "bound": "fp32 / hbm",
                          "achieved": flop / (t_v / 1e3) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": flop / (t_v / 1e3) / 1e12 / fp32_peak,
                          "peak_source": "derived FP32 SIMT peak at the max SM clock",
@@ -1490,8 +1490,9 @@ def main_batch(args, rank, world, local_rank):
     stream = torch.cuda.current_stream(dev)
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
     z_flat = torch.zeros(bt.z_size, dtype=torch.complex64, device=dev)
-    bt.assemble(out=z_flat)
     B = bt.excitation(waves)
+    asm_cfg = bt.autotune_assembly(z_flat)  # assembly tile and block schedule (EFIE)
+    bt.assemble(out=z_flat)
     rows = bt.autotune(z_flat)
     P = bt.spai(z_flat)
 
@@ -1644,7 +1645,8 @@ def main_batch(args, rank, world, local_rank):
                         "assembly_and_excitation_ms": asm_ms, "precond_ms": pc_ms, "solve_ms": solve_ms,
                         "arnoldi_steps": info["iterations"], "restarts": info["restarts"],
                         "max_rel_residual": info["max_rel_residual"], "max_rel_err_J": batched_err,
-                        "matvec_rows_per_warp": rows, "precond_status": P.status},
+                        "matvec_rows_per_warp": rows, "assembly_tile_schedule": asm_cfg,
+                        "precond_status": P.status},
             "plain_path": {"what": "per mesh: FP32 assembly + excitation, then one GMRES(50) per incidence from zero "
                                    "(FP32 products, no preconditioner, mb_gmres_c64), each column at the loosest "
                                    "ladder tolerance that reaches the target (a column that hits the cap of "
@@ -1805,7 +1807,7 @@ def main_learned(args, rank, world, local_rank):
 # time to a 1e-4 relative error in J: plain FP32 path against the mixed-precision path
 # ---------------------------------------------------------------------------------------
 TTS_TARGET = 1e-4
-TTS_LADDER = (1e-3, 3e-4, 1e-4, 3e-5, 1e-5, 3e-6, 1e-6, 3e-7, 1e-7, 3e-8)
+TTS_LADDER = (1e-3, 3e-4, 1e-4, 3e-5, 1e-5, 3e-6, 1e-6, 3e-7, 1e-7, 3e-8, 1e-8, 3e-9, 1e-9, 3e-10, 1e-10)
 
 
 def time_to_solution(pkg, dev, level, k, sym, gq=4, Z=None, repeats=2):
@@ -1999,11 +2001,13 @@ def main_efie_solve(args, rank, world, local_rank):
     torch.cuda.synchronize(dev)
     clocks.stop()
     ms = e0.elapsed_time(e1) / args.steps
-    Z64 = M.assemble_Z_rwg_sym(verts.double(), faces, fei, E, k, pairs=near, check_indices=False)
-    b64 = M.assemble_rhs_rwg_sym(verts.double(), faces, fei, E, pw)[:, 0]
-    P = M.spai_preconditioner(Z, verts, faces, fei, E, pairs=near)
-    j_ref, _ = M.pgmres(Z64, b64, M=P, restart=50, tol=1e-12, max_iters=20000)
-    err = float((x - j_ref).norm() / j_ref.norm())
+    err = None
+    if not args.no_solve:  # the FP64 check (skipped when profiling the timed path alone)
+        Z64 = M.assemble_Z_rwg_sym(verts.double(), faces, fei, E, k, pairs=near, check_indices=False)
+        b64 = M.assemble_rhs_rwg_sym(verts.double(), faces, fei, E, pw)[:, 0]
+        P = M.spai_preconditioner(Z, verts, faces, fei, E, pairs=near)
+        j_ref, _ = M.pgmres(Z64, b64, M=P, restart=50, tol=1e-12, max_iters=20000)
+        err = float((x - j_ref).norm() / j_ref.norm())
     line = {"metric": "time to a <1e-4 relative error in J, mixed-precision EFIE path", "value": ms, "unit": "ms",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,

@@ -388,6 +388,18 @@ int mb_mom_sym_rhs_batched_c128(const double* verts, const int32_t* faces, const
                                 const int64_t* desc, int n_mesh, int64_t total_faces, const double* waves,
                                 int nrhs, int64_t ld, double* rhs, void* stream);
 
+/* The same float matrices as mb_mom_sym_zmat_batched_c64 with the separated pairs in the rows
+ * layout: a block owns rows_per_block (8, 16 or 32) test faces of one mesh, staged in shared
+ * memory, and 128 of its source faces.  schedule [n_mesh] int32 is the order in which the
+ * meshes' blocks are laid out and block_offsets [n_mesh + 1] int64 the first block of the j-th
+ * scheduled mesh (mesh schedule[j], of F faces, takes ceil(F / rows_per_block) * ceil(F / 128)
+ * blocks; the last entry = total_blocks).  Chosen by MeshBatch.autotune_assembly.
+ * Accumulated into z (caller zeroes). */
+int mb_mom_sym_zmat_batched_rows_c64(const float* verts, const int32_t* faces, const int32_t* fei, const int64_t* desc,
+                                     const double* ks, int n_mesh, const int32_t* schedule,
+                                     const int64_t* block_offsets, int64_t total_blocks, int rows_per_block,
+                                     const int32_t* near_pairs, int64_t n_near, float* z, void* stream);
+
 /* The reference's operator and rule (as mb_mom_zmat_rwg_c64 / mb_mom_rhs_rwg_c64) for every
  * mesh of the batch in one launch each: face_areas, face_normals per packed face;
  * block_offsets [n_mesh + 1] = first block of each mesh with 3 F_i rows of

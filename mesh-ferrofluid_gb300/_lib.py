@@ -118,6 +118,7 @@ _SIGS = {
     "mb_pgmres_workspace_bytes": [_I64, _I],
     "mb_pgmres_c64": [_P, _I64, _P, _P, _D, _P, _P, _P, _P, _I, _I, _D, _I, _P, ctypes.c_size_t, _P, _P],
     "mb_half_copy_c64": [_P, _I64, _P, _P, _P],
+    "mb_mom_sym_zmat_batched_rows_c64": [_P, _P, _P, _P, _P, _I, _P, _P, _I64, _I, _P, _I64, _P, _P],
     "mb_gmres_blockdiag_pc_c64": [_P, _P, _P, _I, _I64, _I, _I, _I64, _P, _P, _P, _P, _P, _I, _I, _D, _I, _P,
                                   ctypes.c_size_t, _P, _P],
     "mb_pgmres_c128": [_P, _I64, _P, _P, _P, _P, _I, _I, _D, _I, _P, ctypes.c_size_t, _P, _P],

@@ -147,10 +147,60 @@ class MeshBatch:
                       self.gq, _lib.ptr(self.gpy), _lib.ptr(self.gwy), self.gq - 1, _lib.ptr(out),
                       _lib.stream_of(out))
             return out
+        cfg = getattr(self, "asm_config", None)
+        if cfg is not None and cfg[0] != "pair":
+            sched, boff, total = self._asm_schedule(*cfg)
+            _lib.call("mb_mom_sym_zmat_batched_rows_c64", _lib.ptr(self.verts), _lib.ptr(self.faces),
+                      _lib.ptr(self.fei), _lib.ptr(self.desc), _lib.ptr(self.ks), self.n_mesh, _lib.ptr(sched),
+                      _lib.ptr(boff), total, int(cfg[0]), _lib.ptr(self.near), self.near.shape[0], _lib.ptr(out),
+                      _lib.stream_of(out))
+            return out
         _lib.call("mb_mom_sym_zmat_batched_c64", _lib.ptr(self.verts), _lib.ptr(self.faces), _lib.ptr(self.fei),
                   _lib.ptr(self.desc), _lib.ptr(self.ks), self.n_mesh, self.total_blocks, _lib.ptr(self.near),
                   self.near.shape[0], _lib.ptr(out), _lib.stream_of(out))
         return out
+
+    def _asm_schedule(self, rows: int, order: str):
+        """(schedule int32 [n_mesh], block offsets int64 [n_mesh + 1], total blocks) of the rows
+        layout: meshes in packing order ("packed") or largest first ("largest")."""
+        key = (rows, order)
+        if not hasattr(self, "_asm_sched"):
+            self._asm_sched = {}
+        if key not in self._asm_sched:
+            nf = self._desc_np[:, 1]
+            idx = np.arange(self.n_mesh) if order == "packed" else np.argsort(-nf, kind="stable")
+            per = ((nf[idx] + rows - 1) // rows) * ((nf[idx] + 127) // 128)
+            off = np.concatenate([[0], np.cumsum(per)]).astype(np.int64)
+            self._asm_sched[key] = (torch.tensor(idx.astype(np.int32), device=self.device),
+                                    torch.tensor(off, device=self.device), int(off[-1]))
+        return self._asm_sched[key]
+
+    def autotune_assembly(self, out: torch.Tensor | None = None, reps: int = 2):
+        """Pick the EFIE assembly's tile and block schedule by timing each candidate: the one-pair-
+        per-thread kernel, or the rows layout with 8, 16 or 32 test faces per block and the meshes'
+        blocks in packing order or largest mesh first.  Returns the chosen (rows, order)."""
+        if self.formulation != "efie_sym":
+            return None
+        if self.desc is None:
+            self._set_nc(1)
+        if out is None:
+            out = torch.zeros(self.z_size, dtype=torch.complex64, device=self.device)
+        best, best_t = None, None
+        for cfg in [("pair", None)] + [(r, o) for r in (8, 16, 32) for o in ("packed", "largest")]:
+            self.asm_config = cfg
+            self.assemble(out=out)  # warm-up
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                self.assemble(out=out)
+            e1.record()
+            torch.cuda.synchronize(self.device)
+            t = e0.elapsed_time(e1) / reps
+            if best_t is None or t < best_t:
+                best, best_t = cfg, t
+        self.asm_config = best
+        self.asm_ms = best_t
+        return best
 
     def excitation(self, waves: torch.Tensor) -> torch.Tensor:
         """waves [n_mesh, nc, 9] (``mesh_MOM_3d.plane_waves`` records) -> B complex64

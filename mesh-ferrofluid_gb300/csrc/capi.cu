@@ -154,6 +154,10 @@ int pgmres(int kind, const void* z, const void* z_half, const float* half_scale,
            bool use_graph, void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out,
            double* relres_out, int* status_out, cudaStream_t s);
 int half_copy_c64(const float* z, int64_t count, void* zh, float* scale, cudaStream_t s);
+int launch_mom_sym_rows_batched(const float* verts, const int32_t* faces, const int32_t* fei, const int64_t* desc,
+                                const double* ks, int n_mesh, const int32_t* sched, const int64_t* boff,
+                                int64_t total_blocks, int rows_per_block, const int32_t* pairs, int64_t n_pairs,
+                                float* z, cudaStream_t s);
 int gmres_blockdiag_pc(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
                        int rows_per_warp, int nc, int64_t n_rows, const int32_t* m_cols, const float* m_vals,
                        const int64_t* eoff, const double* b, double* x, int r, int max_iters, double tol,
@@ -970,6 +974,18 @@ int mb_gmres_blockdiag_pc_c64(const float* z, const int64_t* desc, const int64_t
         info->reserved = 0;
     }
     return rc;
+}
+
+int mb_mom_sym_zmat_batched_rows_c64(const float* verts, const int32_t* faces, const int32_t* fei, const int64_t* desc,
+                                     const double* ks, int n_mesh, const int32_t* schedule,
+                                     const int64_t* block_offsets, int64_t total_blocks, int rows_per_block,
+                                     const int32_t* near_pairs, int64_t n_near, float* z, void* stream) {
+    MB_REQUIRE(n_mesh >= 0 && total_blocks >= 0 && n_near >= 0, "bad sizes");
+    if (n_mesh == 0) return MB_OK;
+    MB_REQUIRE(verts && faces && fei && desc && ks && schedule && block_offsets && z, "null pointer argument");
+    MB_REQUIRE(n_near == 0 || near_pairs, "null near-pair list");
+    return launch_mom_sym_rows_batched(verts, faces, fei, desc, ks, n_mesh, schedule, block_offsets, total_blocks,
+                                       rows_per_block, near_pairs, n_near, z, as_stream(stream));
 }
 
 int mb_half_copy_c64(const float* z, int64_t count, void* z_half, float* scale, void* stream) {

@@ -620,6 +620,98 @@ __global__ void mom_sym_rhs_batched_kernel(const T* __restrict__ verts, const in
     sym_rhs_face<T>(verts, faces, fei, waves + 9 * ((int64_t)i * nrhs + r), p, ld, desc[kDesc * i + 5] + r, rhs);
 }
 
+// Batched float separated pairs in the rows layout of mom_sym_regular_rows_kernel: a block
+// owns R test faces of one mesh (staged in shared memory) and 128 of its source faces.  The
+// blocks of the meshes are laid out in a schedule: sched[j] is the j-th mesh of the launch and
+// boff[j] its first block (boff[n_mesh] = the launch size), so the autotuner can put the
+// largest meshes first or keep the packing order, and pick R.
+template <int R>
+__global__ void __launch_bounds__(128) mom_sym_rows_batched_kernel(
+    const float* __restrict__ verts, const int32_t* __restrict__ faces, const int32_t* __restrict__ fei,
+    const int64_t* __restrict__ desc, const double* __restrict__ ks, const int32_t* __restrict__ sched,
+    const int64_t* __restrict__ boff, int n_mesh, float* __restrict__ z) {
+    __shared__ float s_b[7][4];
+    __shared__ float s_A[R][9], s_cm[R][3], s_ap[R];
+    __shared__ int32_t s_v[R][3], s_row[R][3];
+    if (threadIdx.x < 28) s_b[threadIdx.x / 4][threadIdx.x % 4] = (float)c_d7[threadIdx.x / 4][threadIdx.x % 4];
+    const int64_t b = blockIdx.x;
+    int lo = 0, hi = n_mesh - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(boff + mid) <= b) lo = mid; else hi = mid - 1;
+    }
+    const int i = __ldg(sched + lo);
+    const int64_t fo = __ldg(desc + kDesc * i), nf = __ldg(desc + kDesc * i + 1), ne = __ldg(desc + kDesc * i + 2);
+    const int64_t qb = (nf + 127) / 128, local = b - __ldg(boff + lo);
+    const int64_t p0 = fo + (local / qb) * R, p_end = fo + nf;
+    if (threadIdx.x < R && p0 + threadIdx.x < p_end) {
+        const int64_t p = p0 + threadIdx.x;
+        V3<float> A[3];
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {
+            s_v[threadIdx.x][v] = __ldg(faces + 3 * p + v);
+            s_row[threadIdx.x][v] = __ldg(fei + 3 * p + v);
+            A[v] = load3(verts, s_v[threadIdx.x][v]);
+            s_A[threadIdx.x][3 * v] = A[v].x;
+            s_A[threadIdx.x][3 * v + 1] = A[v].y;
+            s_A[threadIdx.x][3 * v + 2] = A[v].z;
+        }
+        float cm[3], ap;
+        rwg_consts<float>(faces, p, A, cm, &ap);
+        s_cm[threadIdx.x][0] = cm[0];
+        s_cm[threadIdx.x][1] = cm[1];
+        s_cm[threadIdx.x][2] = cm[2];
+        s_ap[threadIdx.x] = ap;
+    }
+    __syncthreads();
+    const int64_t q = fo + (local % qb) * 128 + threadIdx.x;
+    if (q >= p_end) return;
+    const float k = (float)__ldg(ks + i);
+    SymSource S;
+    sym_source(verts, faces, fei, k, q, s_b, S);
+    const int nr = (int)min((int64_t)R, p_end - p0);
+    float* zi = z + 2 * __ldg(desc + kDesc * i + 3);
+    const int64_t pitch = ne + (ne & 1);
+#pragma unroll 1
+    for (int r = 0; r < nr; ++r) {
+        int shared = 0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) shared += s_v[r][a] == S.v[c];
+        if (shared) continue;  // done by the FP64 near-pair kernel
+        V3<float> A[3];
+#pragma unroll
+        for (int v = 0; v < 3; ++v) A[v] = v3<float>(s_A[r][3 * v], s_A[r][3 * v + 1], s_A[r][3 * v + 2]) - S.o;
+        const float cm[3] = {s_cm[r][0], s_cm[r][1], s_cm[r][2]};
+        const int32_t rows[3] = {s_row[r][0], s_row[r][1], s_row[r][2]};
+        sym_pair_eval(S, A, cm, s_ap[r], rows, k, pitch, s_b, zi);
+    }
+}
+
+int launch_mom_sym_rows_batched(const float* verts, const int32_t* faces, const int32_t* fei, const int64_t* desc,
+                                const double* ks, int n_mesh, const int32_t* sched, const int64_t* boff,
+                                int64_t total_blocks, int rows_per_block, const int32_t* pairs, int64_t n_pairs,
+                                float* z, cudaStream_t s) {
+    if (n_mesh <= 0) return MB_OK;
+    if (total_blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "batch too large for one launch");
+    if (total_blocks > 0) {
+        const unsigned nb = (unsigned)total_blocks;
+        if (rows_per_block == 8)
+            mom_sym_rows_batched_kernel<8><<<nb, 128, 0, s>>>(verts, faces, fei, desc, ks, sched, boff, n_mesh, z);
+        else if (rows_per_block == 16)
+            mom_sym_rows_batched_kernel<16><<<nb, 128, 0, s>>>(verts, faces, fei, desc, ks, sched, boff, n_mesh, z);
+        else if (rows_per_block == 32)
+            mom_sym_rows_batched_kernel<32><<<nb, 128, 0, s>>>(verts, faces, fei, desc, ks, sched, boff, n_mesh, z);
+        else
+            return set_error(MB_ERR_UNSUPPORTED, "rows per block must be 8, 16 or 32");
+    }
+    if (n_pairs > 0)
+        mom_sym_near_batched_kernel<float><<<(unsigned)((n_pairs + 127) / 128), 128, 0, s>>>(
+            verts, faces, fei, desc, ks, n_mesh, pairs, n_pairs, z);
+    return check_launch("mom_sym_rows_batched");
+}
+
 template <typename T>
 int launch_mom_sym_batched(const T* verts, const int32_t* faces, const int32_t* fei, const int64_t* desc,
                            const double* ks, int n_mesh, int64_t total_blocks, const int32_t* pairs,

@@ -31,6 +31,7 @@ from .utils import (
     LayerType,
     OrderType,
     collapsed_rule_2d,
+    compute_panel_relation,
     compute_vert_areas,
     get_gaussion_integration_points_and_weights,
     pack_matrix_tight,
@@ -69,8 +70,9 @@ def double_integration_on_panels_3d(BEM_type: int, order_type: int, verts: torch
     normals = face_normals.to(dt).contiguous()
     table, seg = _cached_rule_table(rands_x, rands_y, gauss_weightsx, gauss_weightsy, dt, dev)
     seg_c = (torch.tensor(seg, dtype=torch.int32)).numpy()
-    rel = None
-    if panel_relations is not None:
+    if panel_relations is None:  # the tiled kernels take the relation matrix (F^2 bytes)
+        rel = compute_panel_relation(faces)
+    else:
         rel = panel_relations.to(device=dev, dtype=torch.uint8).contiguous()
         if rel.shape != (nf, nf):
             raise ValueError("panel_relations must be [F, F]")
@@ -86,23 +88,32 @@ def double_integration_on_panels_3d(BEM_type: int, order_type: int, verts: torch
     return torch.complex(out_r, out_i) if kind == 1 else out_r
 
 
-# Flattened sub-domain rule tables of recent calls, keyed by the rules' values (a few dozen
-# numbers, one small copy to the host).  Building a table takes ~150 small torch operations
-# and a solver passes the same rule on every call.
+# Flattened sub-domain rule tables of recent calls.  Building a table takes ~150 small torch
+# operations and a solver passes the same rule tensors on every call, so an entry is found
+# first by the identity and version counter of the four rule tensors (the entry holds them,
+# so their storage cannot be reused while it lives) -- no device synchronisation -- and
+# otherwise by their values (a few dozen numbers, one small copy to the host).
 _RULE_TABLES: list = []
 _RULE_TABLES_MAX = 8
 
 
 def _cached_rule_table(rx, ry, wx, wy, dt, dev):
     ins = (rx, ry, wx, wy)
+    vers = tuple(t._version for t in ins)
+    for held, held_vers, key, val in _RULE_TABLES:
+        if (key[2], key[3]) == (dt, str(dev)) and held_vers == vers and all(a is b for a, b in zip(held, ins)):
+            return val
     vals = torch.cat([t.reshape(-1).to(torch.float64) for t in ins]).cpu().tolist()
     key = (tuple(tuple(t.shape) for t in ins), tuple(vals), dt, str(dev))
-    for k, val in _RULE_TABLES:
+    val = None
+    for _, _, k, v in _RULE_TABLES:
         if k == key:
-            return val
-    table, seg = panel_rule_table(rx.to(dt), ry.to(dt), wx.to(dt), wy.to(dt))
-    val = (table.to(dev).contiguous(), seg)
-    _RULE_TABLES.append((key, val))
+            val = v
+            break
+    if val is None:
+        table, seg = panel_rule_table(rx.to(dt), ry.to(dt), wx.to(dt), wy.to(dt))
+        val = (table.to(dev).contiguous(), seg)
+    _RULE_TABLES.append((ins, vers, key, val))
     del _RULE_TABLES[:-_RULE_TABLES_MAX]
     return val
 
@@ -300,7 +311,13 @@ class _AbstractLayer:
                 near = torch.nonzero(panel_relations > 0).to(torch.int32).contiguous()
             self.compute_sym(verts, faces, near)
             return
-        rands = torch.cat((self.r1, self.r2), dim=-1)
+        # one [n, 2] rule tensor per (r1, r2): the same object on every call finds the rule
+        # table without a device synchronisation
+        key = (self.r1, self.r2, self.r1._version, self.r2._version)
+        held = getattr(self, "_rands_key", None)
+        if held is None or held[0] is not key[0] or held[1] is not key[1] or held[2:] != key[2:]:
+            self._rands_key, self._rands = key, torch.cat((self.r1, self.r2), dim=-1)
+        rands = self._rands
         self._unpacked = double_integration_on_panels_3d(
             BEM_type=self.BEM_type, order_type=self.order_type, verts=verts, faces=faces,
             face_areas=face_areas, face_normals=face_normals, gauss_weightsx=self.gauss_weights,

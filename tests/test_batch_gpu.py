@@ -176,3 +176,22 @@ def test_batched_preconditioned_solve_matches_dense(pkg, cuda, use_graph):
         err = (torch.linalg.norm(got - ref, dim=0) / torch.linalg.norm(ref, dim=0)).max().item()
         assert err < 1e-6, (i, err)
         assert torch.all(X[e:, 4 * i:4 * i + 4] == 0)
+
+
+def test_batched_rows_assembly_every_tile_and_schedule(pkg, cuda):
+    """The rows layout (8 / 16 / 32 test faces per block, meshes in packing order or largest
+    first) assembles the same matrices as the one-pair-per-thread kernel; the autotuner picks
+    one of them."""
+    bt, meshes, ks = _batch(pkg, cuda)
+    bt.excitation(_waves(pkg, bt.n_mesh, 4, ks, cuda))
+    ref = bt.assemble()
+    for cfg in [(r, o) for r in (8, 16, 32) for o in ("packed", "largest")]:
+        bt.asm_config = cfg
+        Z = bt.assemble()
+        for i in range(bt.n_mesh):
+            zi, zr = bt.z_block(Z, i), bt.z_block(ref, i)
+            assert (torch.linalg.norm(zi - zr) / torch.linalg.norm(zr)).item() < 1e-6, (cfg, i)
+    best = bt.autotune_assembly()
+    assert best in [("pair", None)] + [(r, o) for r in (8, 16, 32) for o in ("packed", "largest")]
+    Z = bt.assemble()
+    assert (torch.linalg.norm(Z - ref) / torch.linalg.norm(ref)).item() < 1e-6
