@@ -64,6 +64,9 @@ WORKLOADS = {
     # the reference's own Laplace path (demo_Laplace_3d.py): Dirichlet solve with its rule, P1:
     # (icosphere level, gaussQR, radius)
     "laplace_ref_L4": (4, 2, 0.5),
+    # its operator assembly alone: V and K panels [F, F, 3, 3] with the same rule and relation
+    "laplace_panels_L4": (4, 2, 0.5),
+    "laplace_panels_L5": (5, 2, 0.5),
     # the ferrofluid pressure projection (MeshPressure.solve), hydrostatic droplet: (icosphere level,)
     "pressure_L4": (4,),
     # Laplace mixed Dirichlet / Neumann solve, u = z on the unit sphere: (icosphere level, dtype)
@@ -938,6 +941,148 @@ def main_lapref(args, rank, world, local_rank):
                                 "sample": f"V and K panels of the first {n_s} of {nf} face rows with the double C "
                                           "restatement of the reference rule, scaled to all rows, plus a numpy LU "
                                           f"solve of size {nv}; packing not counted"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main_lappanels(args, rank, world, local_rank):
+    """The reference's Laplace operator assembly (double_integration_on_panels_3d,
+    integrations_3d.py:252-452, as SingleLayer3d / DoubleLayer3d call it from
+    mesh_BEM_solver_3d.py): V and K panels [F, F, 3, 3], P1, the reference rule, with the
+    shared-vertex relation computed once per mesh like the solver does.  A step is both
+    operators."""
+    level, gq, radius = WORKLOADS[args.workload]
+    import torch
+
+    pkg = importlib.import_module("mesh-ferrofluid_gb300")
+    R, U = pkg.roofline, pkg.utils
+    v_np, f_np = pkg.meshes.icosphere(level, radius)
+    nf = f_np.shape[0]
+    pairs = float(nf) ** 2
+    config = {"workload": args.workload, "mesh": f"icosphere L{level}, radius {radius}", "n_faces": nf,
+              "rule": f"the reference's (gaussQR = {gq}: collapsed Gauss rule per sub-domain), P1, float32",
+              "output": "V and K panels [F, F, 3, 3] float32 (2 x 36 B per face pair)",
+              "l2": f"outputs {2 * pairs * 36 / 1e9:.2f} GB per step > L2", "parallelism": "replicas"}
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference's Laplace path is torch code; its "
+                              "algorithm is timed by cpu_baseline (the C oracle)"}), flush=True)
+        return
+    dev = torch.device("cuda", local_rank if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    verts = torch.tensor(v_np, dtype=torch.float32, device=dev)
+    faces = torch.tensor(f_np, dtype=torch.int32, device=dev)
+    areas = U.compute_face_areas(vertices=verts, faces=faces, keepdim=True).contiguous()
+    normals = U.compute_face_normals(vertices=verts, faces=faces).contiguous()
+    rel = U.compute_panel_relation(faces)
+    p1, w1 = U.get_gaussion_integration_points_and_weights(gq, device=dev)
+    rands, w = U.collapsed_rule_2d(p1, w1)
+    stream = torch.cuda.current_stream(dev)
+
+    def panels(layer, v=verts, f=faces, a=areas, n=normals, r=rel):
+        return pkg.double_integration_on_panels_3d(int(pkg.BEMType.LAPLACE), 1, v, f, a, n, w, w, rands, rands, r,
+                                                   1.0, layer)
+
+    def step():
+        return panels(1), panels(2)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    replica_barrier(world, dev)
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    time.sleep(0.3)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    calls0 = pkg._lib.call_count
+    replica_barrier(world, dev)
+    for e0, e1, e2 in ev:
+        e0.record(stream)
+        vp = panels(1)
+        e1.record(stream)
+        kp = panels(2)
+        e2.record(stream)
+        del vp, kp
+    replica_barrier(world, dev)
+    clocks.stop()
+    abi_calls = pkg._lib.call_count - calls0
+    step_ms = [a.elapsed_time(c) for a, _, c in ev]
+    v_ms = statistics.mean(a.elapsed_time(b) for a, b, _ in ev)
+    ms_per_step = replica_max(sum(step_ms), world, dev) / args.steps
+    value = world * 2 * pairs / (ms_per_step / 1e3)
+    # roofline: the V call (packed tiled kernel + near-pair kernel), separated pairs 16
+    # evaluations of 15 + 6 FLOP and 1 rsqrt, 36 B written per pair
+    n_w = int(w.numel())
+    peaks = R.measured_peaks(REPO)
+    fp32_peak = R.fp32_peak_tflops(float(peaks.get("sm_max_mhz", 2070.0)))
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    flop = pairs * n_w * n_w * (R.LAPLACE_SL_FLOP_PER_EVAL + 6)
+    out_bytes = pairs * 36
+    traffic = None
+    prof = os.path.join(REPO, "profiles", f"{args.workload}_traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as fh:
+            traffic = json.load(fh).get("dram_bytes_per_launch")
+    line = {"metric": "Laplace panel pairs/s (V and K, reference rule)", "value": value, "unit": "pairs/s",
+            "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config,
+            "roofline": {"kernel": "laplace_panels_pair2_kernel<3, 1> + laplace_near_rows_kernel (V panels)",
+                         "bound": "hbm", "achieved": out_bytes / (v_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                         "frac": out_bytes / (v_ms / 1e3) / 1e9 / hbm, "traffic": traffic,
+                         "algorithmic": "36 B written per face pair (nine float32 panel entries)",
+                         "fp32": {"achieved_tflops": flop / (v_ms / 1e3) / 1e12, "peak_tflops": fp32_peak,
+                                  "frac": flop / (v_ms / 1e3) / 1e12 / fp32_peak,
+                                  "algorithmic": f"{n_w} x {n_w} evaluations per pair, "
+                                                 f"{R.LAPLACE_SL_FLOP_PER_EVAL} + 6 (P1 weights) FLOP each"},
+                         "kernel_ms": v_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)"},
+            "clocks": clocks.summary(), "gpu_launches": 2 * abi_calls,
+            "gpu_launches_note": "two kernels per C-ABI panel call (tiled + near pairs)"}
+    if not args.no_e2e:
+        h_v = torch.tensor(v_np, dtype=torch.float32).pin_memory()
+        h_f = torch.tensor(f_np, dtype=torch.int32).pin_memory()
+        h_out = [torch.empty((nf, nf, 3, 3), dtype=torch.float32, pin_memory=True) for _ in range(2)]
+        d_v, d_f = torch.empty_like(verts), torch.empty_like(faces)
+
+        def e2e_step():
+            d_v.copy_(h_v, non_blocking=True)
+            d_f.copy_(h_f, non_blocking=True)
+            a = U.compute_face_areas(vertices=d_v, faces=d_f, keepdim=True).contiguous()
+            n = U.compute_face_normals(vertices=d_v, faces=d_f).contiguous()
+            r = U.compute_panel_relation(d_f)
+            for hh, layer in zip(h_out, (1, 2)):
+                hh.copy_(panels(layer, d_v, d_f, a, n, r), non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize(dev)
+        n_e2e = max(2, min(args.steps, 3))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n_e2e):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        e2e_ms = e0.elapsed_time(e1) / n_e2e
+        line["e2e"] = {"value": world * 2 * pairs / (e2e_ms / 1e3), "unit": "pairs/s",
+                       "h2d_bytes_per_step": h_v.numel() * 4 + h_f.numel() * 4,
+                       "d2h_bytes_per_step": sum(t.numel() * 4 for t in h_out), "ms_per_step": e2e_ms,
+                       "steps": n_e2e,
+                       "path": "double_integration_on_panels_3d (C ABI mb_panel_relation, mb_laplace_panels_f32) "
+                               "from a pinned host mesh, both operators back to pinned host memory"}
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+
+        threads = os.cpu_count() or 1
+        n_s = min(nf, 512)
+        a_np, n_np = areas.cpu().double().numpy(), normals.cpu().double().numpy()
+        rel_np, r_np, w_np = rel.cpu().numpy(), rands.cpu().double().numpy(), w.cpu().double().numpy()
+        t0 = time.perf_counter()
+        O.laplace_panels(v_np, f_np, a_np, n_np, r_np, w_np, rel_np, 1, 1, rows=(0, n_s))
+        O.laplace_panels(v_np, f_np, a_np, n_np, r_np, w_np, rel_np, 2, 1, rows=(0, n_s))
+        t_cpu = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": 2 * n_s * nf / t_cpu, "unit": "pairs/s", "cores": threads, "kind": "port",
+                                "sample": f"V and K panels of the first {n_s} of {nf} face rows with the double C "
+                                          "restatement of the reference rule"}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -2032,6 +2177,8 @@ def main():
         return main_pressure(args, rank, world, local_rank)
     if args.workload.startswith("laplace_mixed"):
         return main_lapmixed(args, rank, world, local_rank)
+    if args.workload.startswith("laplace_panels"):
+        return main_lappanels(args, rank, world, local_rank)
     if args.workload.startswith("laplace_ref"):
         return main_lapref(args, rank, world, local_rank)
     if args.workload.startswith("laplace_"):

@@ -47,12 +47,24 @@ def _mesh_args(verts, faces, face_areas, face_normals):
     return dt, dev, verts.shape[0], nf
 
 
+# face tensors already checked: (tensor, version counter, vertex count); an entry holds its
+# tensor, so the identity cannot be taken by another tensor while the entry lives
+_CHECKED_FACES: list = []
+_CHECKED_FACES_MAX = 8
+
+
 def check_face_range(faces, n_verts):
-    """Vertex ids must index ``verts``; the kernels trust them (one reduction, one sync)."""
+    """Vertex ids must index ``verts``; the kernels trust them (one reduction, one sync -- once
+    per face tensor and vertex count while the tensor is not modified in place)."""
     if faces.numel():
+        for held, ver, nv in _CHECKED_FACES:
+            if held is faces and ver == faces._version and nv == n_verts:
+                return
         lo, hi = torch.aminmax(faces)
         if int(lo) < 0 or int(hi) >= n_verts:
             raise ValueError(f"faces reference vertex ids outside [0, {n_verts})")
+        _CHECKED_FACES.append((faces, faces._version, int(n_verts)))
+        del _CHECKED_FACES[:-_CHECKED_FACES_MAX]
 
 
 def _rule(p, w, name, dt, dev):

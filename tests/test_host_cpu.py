@@ -194,3 +194,27 @@ def test_rule_table_cache_keys_on_values(pkg):
     r3, w3 = rule(3, torch.float64)
     t5, s5 = L._cached_rule_table(r3, r3, w3, w3, torch.float64, torch.device("cpu"))
     assert t5.shape[0] != t1.shape[0] and s5 == U.panel_rule_table(r3, r3, w3, w3)[1]
+    # an in-place change of a rule tensor already found by identity rebuilds the table
+    r4 = r.clone()
+    t6, _ = L._cached_rule_table(r4, r4, w, w, torch.float64, torch.device("cpu"))
+    assert t6 is t1
+    r4[1, 1] += 1e-3
+    t7, _ = L._cached_rule_table(r4, r4, w, w, torch.float64, torch.device("cpu"))
+    assert t7 is not t1 and torch.equal(t7, U.panel_rule_table(r4, r4, w, w)[0])
+
+
+def test_face_range_check_is_cached_per_tensor_version(pkg):
+    """check_face_range reduces a face tensor once, then trusts it until it is modified in
+    place (its version counter moves) or checked against another vertex count."""
+    M = pkg.mesh_MOM_3d
+    f = torch.tensor([[0, 1, 2], [2, 1, 3]], dtype=torch.int32)
+    M.check_face_range(f, 4)
+    M.check_face_range(f, 4)
+    with pytest.raises(ValueError):
+        M.check_face_range(f, 3)
+    f[1, 2] = 7
+    with pytest.raises(ValueError):
+        M.check_face_range(f, 4)
+    f[1, 2] = -1
+    with pytest.raises(ValueError):
+        M.check_face_range(f, 8)
