@@ -411,6 +411,15 @@ int mb_mom_ref_zmat_batched_c64(const float* verts, const int32_t* faces, const 
                                 const int64_t* block_offsets, int64_t total_blocks, const double* ks,
                                 int n_mesh, const float* gpx, const float* gwx, int nx, const float* gpy,
                                 const float* gwy, int ny, float* z, void* stream);
+/* The same matrices from one resident grid (SMs x blocks per SM) whose blocks take the
+ * (mesh, row, 128-column tile) work items of block_offsets from a device counter until they
+ * run out (a counter of 8 bytes allocated stream-ordered per call).  Chosen against the grid
+ * form by MeshBatch.autotune_assembly. */
+int mb_mom_ref_zmat_batched_persistent_c64(const float* verts, const int32_t* faces, const float* face_areas,
+                                           const float* face_normals, const int32_t* fei, const int64_t* desc,
+                                           const int64_t* block_offsets, int64_t total_blocks, const double* ks,
+                                           int n_mesh, const float* gpx, const float* gwx, int nx, const float* gpy,
+                                           const float* gwy, int ny, float* z, void* stream);
 int mb_mom_ref_rhs_batched_c64(const float* verts, const int32_t* faces, const float* face_areas,
                                const float* face_normals, const int32_t* fei, const int64_t* desc,
                                int n_mesh, int64_t total_faces, const float* gp, const float* gw, int n,
@@ -457,6 +466,26 @@ int mb_gmres_blockdiag_pc_c64(const float* z, const int64_t* desc, const int64_t
                               const float* m_vals, const int64_t* edge_offsets, const double* b, double* x,
                               int restart, int max_iters, double tol, int use_graph, void* workspace,
                               size_t workspace_bytes, mb_gmres_info* info, void* stream);
+
+/* mb_gmres_blockdiag_c64 / _pc_c64 with a fixed augmentation (deflation) subspace per mesh:
+ * aug_k (4, 8 or 16) vectors U_i of x-space per mesh, given through the thin QR of their
+ * products, Z_i U_i = Q_i R_i: aug_q = Q_i and aug_ut = U_i R_i^{-1}, complex64 [n_rows,
+ * n_mesh * aug_k] with mesh i's vectors at columns i * aug_k (rows beyond E_i zero).  Every
+ * Arnoldi step removes the Q_i components of the product and keeps them; every cycle starts by
+ * adding the residual-minimising combination of U_i to X (at the first cycle this is the
+ * least-squares initial guess from U_i); the cycle's update subtracts U_i R_i^{-1} times the
+ * kept components (GCRO with a fixed recycled space), so the reported residual is the true
+ * one.  m_cols, m_vals and edge_offsets: all null (no preconditioner) or all given (as
+ * mb_gmres_blockdiag_pc_c64).  Buffers of (64 + restart + 1) * n_mesh * nc * aug_k * 16 bytes
+ * are allocated stream-ordered per call; the workspace is mb_gmres_blockdiag_c64's.
+ * New capability beside the dense LU the reference solves with (torch.linalg.solve,
+ * mesh_BEM_solver_3d.py:174). */
+int mb_gmres_blockdiag_aug_c64(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh,
+                               int64_t total_warps, int rows_per_warp, int nc, int64_t n_rows, const int32_t* m_cols,
+                               const float* m_vals, const int64_t* edge_offsets, const float* aug_q,
+                               const float* aug_ut, int aug_k, const double* b, double* x, int restart, int max_iters,
+                               double tol, int use_graph, void* workspace, size_t workspace_bytes, mb_gmres_info* info,
+                               void* stream);
 
 /* No counterpart in the reference.  The same solver as mb_gmres_c64 for callers that
  * cannot allocate device memory -- for example a host application or plugin that must

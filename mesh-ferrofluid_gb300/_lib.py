@@ -84,6 +84,8 @@ _SIGS = {
     "mb_mom_sym_rhs_batched_c64": [_P, _P, _P, _P, _I, _I64, _P, _I, _I64, _P, _P],
     "mb_mom_sym_rhs_batched_c128": [_P, _P, _P, _P, _I, _I64, _P, _I, _I64, _P, _P],
     "mb_mom_ref_zmat_batched_c64": [_P, _P, _P, _P, _P, _P, _P, _I64, _P, _I, _P, _P, _I, _P, _P, _I, _P, _P],
+    "mb_mom_ref_zmat_batched_persistent_c64": [_P, _P, _P, _P, _P, _P, _P, _I64, _P, _I, _P, _P, _I, _P, _P, _I, _P,
+                                               _P],
     "mb_mom_ref_rhs_batched_c64": [_P, _P, _P, _P, _P, _P, _I, _I64, _P, _P, _I, _P, _I, _I64, _P, _P],
     "mb_gnn_gemm": [_P, _I, _P, _I, _I, _P, _I64, _I, _I, _I, _P, _I, _P],
     "mb_gnn_gemm_tn": [_P, _I, _P, _I64, _I, _I, _P, _P],
@@ -94,6 +96,8 @@ _SIGS = {
     "mb_gnn_adam": [_P, _P, _P, _P, _I64, _D, _D, _D, _D, _I, _P, _P],
     "mb_blockdiag_matvec_c64": [_P, _P, _P, _I, _I64, _P, _I64, _I, _I, _P, _P],
     "mb_gmres_blockdiag_workspace_bytes": [_I64, _I64, _I],
+    "mb_gmres_blockdiag_aug_c64": [_P, _P, _P, _I, _I64, _I, _I, _I64, _P, _P, _P, _P, _P, _I, _P, _P, _I, _I, _D,
+                                   _I, _P, ctypes.c_size_t, _P, _P],
     "mb_gmres_blockdiag_c64": [_P, _P, _P, _I, _I64, _I, _I, _I64, _P, _P, _I, _I, _D, _I, _P, ctypes.c_size_t,
                                _P, _P],
     "mb_gmres_multi_c64": [_P, _P, _I64, _P, _P, _I64, _I, _I, _D, _P, ctypes.c_size_t, _P, _P],

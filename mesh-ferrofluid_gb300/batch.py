@@ -141,14 +141,17 @@ class MeshBatch:
             _lib.check_tensor(out, "out", dtype=torch.complex64, device=self.device)
             out.zero_()
         if self.formulation == "cfie_ref":
-            _lib.call("mb_mom_ref_zmat_batched_c64", _lib.ptr(self.verts), _lib.ptr(self.faces), _lib.ptr(self.areas),
+            cfg = getattr(self, "asm_config", None)
+            name = "mb_mom_ref_zmat_batched_persistent_c64" if cfg == ("persistent", None) else \
+                "mb_mom_ref_zmat_batched_c64"
+            _lib.call(name, _lib.ptr(self.verts), _lib.ptr(self.faces), _lib.ptr(self.areas),
                       _lib.ptr(self.normals), _lib.ptr(self.fei), _lib.ptr(self.desc), _lib.ptr(self.ref_boff),
                       int(self.ref_boff[-1]), _lib.ptr(self.ks), self.n_mesh, _lib.ptr(self.gpx), _lib.ptr(self.gwx),
                       self.gq, _lib.ptr(self.gpy), _lib.ptr(self.gwy), self.gq - 1, _lib.ptr(out),
                       _lib.stream_of(out))
             return out
         cfg = getattr(self, "asm_config", None)
-        if cfg is not None and cfg[0] != "pair":
+        if cfg is not None and cfg[0] not in ("pair", "grid", "persistent"):
             sched, boff, total = self._asm_schedule(*cfg)
             _lib.call("mb_mom_sym_zmat_batched_rows_c64", _lib.ptr(self.verts), _lib.ptr(self.faces),
                       _lib.ptr(self.fei), _lib.ptr(self.desc), _lib.ptr(self.ks), self.n_mesh, _lib.ptr(sched),
@@ -176,17 +179,22 @@ class MeshBatch:
         return self._asm_sched[key]
 
     def autotune_assembly(self, out: torch.Tensor | None = None, reps: int = 2):
-        """Pick the EFIE assembly's tile and block schedule by timing each candidate: the one-pair-
-        per-thread kernel, or the rows layout with 8, 16 or 32 test faces per block and the meshes'
-        blocks in packing order or largest mesh first.  Returns the chosen (rows, order)."""
-        if self.formulation != "efie_sym":
-            return None
+        """Pick the assembly's tile and block schedule by timing each candidate.  EFIE: the one-
+        pair-per-thread kernel, or the rows layout with 8, 16 or 32 test faces per block and the
+        meshes' blocks in packing order or largest mesh first.  Reference CFIE: one block per
+        (mesh, row, 128-column tile) ("grid", None) or a resident grid taking those tiles from a
+        work counter ("persistent", None).  Returns the chosen configuration."""
         if self.desc is None:
             self._set_nc(1)
         if out is None:
             out = torch.zeros(self.z_size, dtype=torch.complex64, device=self.device)
+        if self.formulation == "cfie_ref":
+            cands = [("grid", None), ("persistent", None)]
+        else:
+            cands = [("pair", None)] + [(r, o) for r in (8, 16, 32) for o in ("packed", "largest")]
         best, best_t = None, None
-        for cfg in [("pair", None)] + [(r, o) for r in (8, 16, 32) for o in ("packed", "largest")]:
+        self.asm_times = {}
+        for cfg in cands:
             self.asm_config = cfg
             self.assemble(out=out)  # warm-up
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -196,6 +204,7 @@ class MeshBatch:
             e1.record()
             torch.cuda.synchronize(self.device)
             t = e0.elapsed_time(e1) / reps
+            self.asm_times[cfg] = t
             if best_t is None or t < best_t:
                 best, best_t = cfg, t
         self.asm_config = best
@@ -289,13 +298,48 @@ class MeshBatch:
             raise ValueError("a mesh of the batch has an edge without faces or with more than two")
         return SpaiPreconditioner(cols, vals, int(status.value))
 
+    def augmentation(self, z_flat: torch.Tensor, U: torch.Tensor):
+        """The deflation subspace of every mesh for ``solve(aug=...)``: U [n_rows, n_mesh, K]
+        (K in {4, 8, 16}) vectors of x-space per mesh (rows beyond E_i are ignored).  Returns
+        (Q, Ut, K): C_i = Z_i U_i by block-diagonal products (8 columns per mesh at a time), an
+        orthonormal basis Q_i of its range (one batched FP64 thin SVD, C_i = Q_i S_i V_i^H) and
+        Ut_i = U_i V_i S_i^{-1} -- complex64 [n_rows, n_mesh K], so that Z_i Ut_i = Q_i.  Directions
+        whose singular value is below 1e-8 of the largest are dropped (zero columns)."""
+        n_rows, n_mesh, K = U.shape
+        if n_rows != self.n_rows or n_mesh != self.n_mesh or K not in (4, 8, 16):
+            raise ValueError("U must be [n_rows, n_mesh, K] with K in {4, 8, 16}")
+        rows = torch.arange(n_rows, device=self.device)[:, None]
+        valid = rows < torch.as_tensor(self.n_edges, device=self.device)[None, :]  # [n_rows, n_mesh]
+        U = torch.where(valid[:, :, None], U.to(torch.complex64), torch.zeros((), dtype=torch.complex64,
+                                                                              device=self.device))
+        parts = []
+        for h in range(0, K, 8):
+            w = min(8, K - h)
+            Uh = U[:, :, h:h + w].contiguous().view(n_rows, n_mesh * w)
+            parts.append(self.matvec(z_flat, Uh, nc=w).view(n_rows, n_mesh, w))
+        C = torch.cat(parts, 2).permute(1, 0, 2).to(torch.complex128)  # [n_mesh, n_rows, K]
+        # C_i = W S V^H: Q_i = W, Ut_i = U_i V S^{-1} (so Z_i Ut_i = Q_i exactly); directions with
+        # S below 1e-8 of the largest get zero columns in both
+        W, S, Vh = torch.linalg.svd(C, full_matrices=False)
+        keep = S > 1e-8 * S[:, :1].clamp_min(1e-300)
+        inv = torch.where(keep, 1.0 / S.clamp_min(1e-300), torch.zeros_like(S))
+        Q = W * keep[:, None, :]
+        Ut = (U.permute(1, 0, 2).to(torch.complex128) @ Vh.mH) * inv[:, None, :].to(torch.complex128)
+        q = Q.permute(1, 0, 2).reshape(n_rows, n_mesh * K).to(torch.complex64).contiguous()
+        ut = Ut.permute(1, 0, 2).reshape(n_rows, n_mesh * K).to(torch.complex64).contiguous()
+        return q, ut, K
+
     def solve(self, z_flat: torch.Tensor, B: torch.Tensor, restart: int = 50, max_iters: int = 2000,
-              tol: float = 1e-6, use_graph: bool = True, workspace=None, X0: torch.Tensor | None = None, M=None):
+              tol: float = 1e-6, use_graph: bool = True, workspace=None, X0: torch.Tensor | None = None, M=None,
+              aug=None):
         """Lockstep GMRES on every (mesh, wave) column -> (X complex128 padded, info dict).
 
         X0: optional initial guess on the padded layout (rows beyond E_i must be zero).
         M: optional near-field preconditioner from ``spai`` (right preconditioning of every
-        mesh's system, ``mb_gmres_blockdiag_pc_c64``)."""
+        mesh's system, ``mb_gmres_blockdiag_pc_c64``).
+        aug: optional deflation subspace from ``augmentation`` (``mb_gmres_blockdiag_aug_c64``:
+        every cycle starts from the residual-minimising combination of the subspace and the
+        Arnoldi steps work in its complement)."""
         if self.nc is None:
             raise RuntimeError("call excitation() first")
         rows = self.rows_per_warp or 2
@@ -307,9 +351,20 @@ class MeshBatch:
         if workspace is None:
             workspace = torch.empty(need, dtype=torch.uint8, device=self.device)
         info = _lib.GmresInfo()
-        if M is not None:
-            if tuple(M.cols.shape) != (self.total_edges, M.cols.shape[1]):
-                raise ValueError("preconditioner does not match the batch")
+        if M is not None and tuple(M.cols.shape) != (self.total_edges, M.cols.shape[1]):
+            raise ValueError("preconditioner does not match the batch")
+        if aug is not None:
+            q, ut, k = aug
+            if tuple(q.shape) != (self.n_rows, self.n_mesh * k) or q.shape != ut.shape:
+                raise ValueError("augmentation subspace does not match the batch")
+            _lib.call("mb_gmres_blockdiag_aug_c64", _lib.ptr(z_flat), _lib.ptr(self.desc), _lib.ptr(goff),
+                      self.n_mesh, int(goff[-1]), rows, self.nc, self.n_rows,
+                      _lib.ptr(M.cols) if M is not None else None, _lib.ptr(M.vals) if M is not None else None,
+                      _lib.ptr(self.edge_offsets) if M is not None else None, _lib.ptr(q),
+                      _lib.ptr(ut), int(k), _lib.ptr(bb), _lib.ptr(X), int(restart), int(max_iters), float(tol),
+                      1 if use_graph else 0, _lib.ptr(workspace), workspace.numel(), ctypes.byref(info),
+                      _lib.stream_of(bb))
+        elif M is not None:
             _lib.call("mb_gmres_blockdiag_pc_c64", _lib.ptr(z_flat), _lib.ptr(self.desc), _lib.ptr(goff), self.n_mesh,
                       int(goff[-1]), rows, self.nc, self.n_rows, _lib.ptr(M.cols), _lib.ptr(M.vals),
                       _lib.ptr(self.edge_offsets), _lib.ptr(bb), _lib.ptr(X), int(restart), int(max_iters),

@@ -40,7 +40,7 @@ int launch_mom_ref_rhs(const T*, const int32_t*, int64_t, const T*, const T*, co
                        const PlaneWave*, double, int, int, int64_t, const int32_t*, T*, T*, cudaStream_t);
 int launch_mom_ref_zmat_batched(const float*, const int32_t*, const float*, const float*, const int32_t*,
                                 const int64_t*, const int64_t*, int64_t, const double*, int, const float*, const float*,
-                                int, const float*, const float*, int, float*, cudaStream_t);
+                                int, const float*, const float*, int, float*, cudaStream_t, int);
 template <typename T>
 int launch_mom_ref_rhs_batched(const T*, const int32_t*, const T*, const T*, const int32_t*, const int64_t*, int,
                                int64_t, const T*, const T*, int, const PlaneWave*, int, int64_t, T*, cudaStream_t);
@@ -163,6 +163,9 @@ int gmres_blockdiag_pc(const float* z, const int64_t* desc, const int64_t* goff,
                        const int64_t* eoff, const double* b, double* x, int r, int max_iters, double tol,
                        bool use_graph, void* workspace, size_t ws_bytes, int64_t* iters_out, int64_t* cycles_out,
                        double* max_relres_out, int* status_out, cudaStream_t s);
+int gmres_blockdiag_aug(const float*, const int64_t*, const int64_t*, int, int64_t, int, int, int64_t, const int32_t*,
+                        const float*, const int64_t*, const float*, const float*, int, const double*, double*, int, int,
+                        double, bool, void*, size_t, int64_t*, int64_t*, double*, int*, cudaStream_t);
 int gmres_c64_noalloc(const float*, int64_t, const double*, double*, int, int, double, int64_t*, int64_t*,
                       double*, int*, cudaStream_t);
 int launch_matvec_c64(const float*, const float*, int64_t, double*, cudaStream_t);
@@ -718,7 +721,21 @@ int mb_mom_ref_zmat_batched_c64(const float* verts, const int32_t* faces, const 
                    gpy && gwy && z,
                "null pointer argument");
     return launch_mom_ref_zmat_batched(verts, faces, face_areas, face_normals, fei, desc, block_offsets,
-                                       total_blocks, ks, n_mesh, gpx, gwx, nx, gpy, gwy, ny, z, as_stream(stream));
+                                       total_blocks, ks, n_mesh, gpx, gwx, nx, gpy, gwy, ny, z, as_stream(stream), 0);
+}
+
+int mb_mom_ref_zmat_batched_persistent_c64(const float* verts, const int32_t* faces, const float* face_areas,
+                                           const float* face_normals, const int32_t* fei, const int64_t* desc,
+                                           const int64_t* block_offsets, int64_t total_blocks, const double* ks,
+                                           int n_mesh, const float* gpx, const float* gwx, int nx, const float* gpy,
+                                           const float* gwy, int ny, float* z, void* stream) {
+    MB_REQUIRE(n_mesh >= 0 && total_blocks >= 0, "bad sizes");
+    if (n_mesh == 0) return MB_OK;
+    MB_REQUIRE(verts && faces && face_areas && face_normals && fei && desc && block_offsets && ks && gpx && gwx &&
+                   gpy && gwy && z,
+               "null pointer argument");
+    return launch_mom_ref_zmat_batched(verts, faces, face_areas, face_normals, fei, desc, block_offsets,
+                                       total_blocks, ks, n_mesh, gpx, gwx, nx, gpy, gwy, ny, z, as_stream(stream), 1);
 }
 
 int mb_mom_ref_rhs_batched_c64(const float* verts, const int32_t* faces, const float* face_areas,
@@ -966,6 +983,31 @@ int mb_gmres_blockdiag_pc_c64(const float* z, const int64_t* desc, const int64_t
     const int rc = gmres_blockdiag_pc(z, desc, goff, n_mesh, total_warps, rows_per_warp, nc, n_rows, m_cols, m_vals,
                                       edge_offsets, b, x, restart, max_iters, tol, use_graph != 0, workspace,
                                       workspace_bytes, &it, &cyc, &rr, &st, as_stream(stream));
+    if (rc == MB_OK && info) {
+        info->iterations = it;
+        info->restarts = cyc;
+        info->rel_residual = rr;
+        info->status = st;
+        info->reserved = 0;
+    }
+    return rc;
+}
+
+int mb_gmres_blockdiag_aug_c64(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh,
+                               int64_t total_warps, int rows_per_warp, int nc, int64_t n_rows, const int32_t* m_cols,
+                               const float* m_vals, const int64_t* edge_offsets, const float* aug_q,
+                               const float* aug_ut, int aug_k, const double* b, double* x, int restart, int max_iters,
+                               double tol, int use_graph, void* workspace, size_t workspace_bytes, mb_gmres_info* info,
+                               void* stream) {
+    MB_REQUIRE(n_mesh > 0 && nc > 0 && n_rows > 0, "bad sizes");
+    MB_REQUIRE(z && desc && goff && b && x && workspace && aug_q && aug_ut, "null pointer argument");
+    int64_t it = 0, cyc = 0;
+    double rr = 0.0;
+    int st = 1;
+    const int rc = gmres_blockdiag_aug(z, desc, goff, n_mesh, total_warps, rows_per_warp, nc, n_rows, m_cols, m_vals,
+                                       edge_offsets, aug_q, aug_ut, aug_k, b, x, restart, max_iters, tol,
+                                       use_graph != 0, workspace, workspace_bytes, &it, &cyc, &rr, &st,
+                                       as_stream(stream));
     if (rc == MB_OK && info) {
         info->iterations = it;
         info->restarts = cyc;

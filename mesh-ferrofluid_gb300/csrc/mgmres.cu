@@ -1114,11 +1114,209 @@ __global__ void __launch_bounds__(256) bd_update_kernel(BdPrecond P, int64_t n, 
 // replayed every cycle (no host synchronisation inside a cycle; a cycle always runs its r
 // steps, columns that converged early are inactive).
 // pc (optional): right preconditioner of the block-diagonal systems (see BdPrecond).
+// ---- augmentation subspace (deflation) ---------------------------------------------------
+// Per mesh i a fixed subspace U_i of K vectors of x-space (K in {4, 8, 16}) enters every
+// cycle.  The caller factors C_i = Z_i U_i = Q_i R_i (thin QR) and passes Q_i and
+// Ut_i = U_i R_i^{-1} (so Z_i Ut_i = Q_i), complex64 [n_rows, ld] with mesh i's K columns at
+// i K and zero rows beyond E_i.  The Arnoldi operator becomes (I - Q Q^H) Z M: step j keeps
+// b_j = Q^H Z M v_j (K values per column) and removes Q b_j from the product; a cycle start
+// adds Ut Q^H r to X and removes Q Q^H r from r (at the first cycle: the residual-minimising
+// combination of U, the initial guess); a cycle's update is X += M V y - Ut (B y), so the
+// minimised residual is again the true one (GCRO with a fixed recycled space).
+constexpr int kAugChunks = 64;
+
+struct AugSpace {
+    const float2* q;
+    const float2* ut;
+    int64_t ld;      // row pitch of q and ut (complex entries)
+    int k;           // vectors per mesh
+    int nc;          // columns per mesh
+    double2* part;   // [kAugChunks][mp][k] chunk partials of Q^H y
+    double2* bq;     // [r][mp][k] b_j of the cycle's steps
+    double2* coef;   // [mp][k]
+};
+
+// part[chunk][c][q] = sum over the chunk's rows of conj(Q[row, mesh(c) K + q]) src[row, c]
+template <int K>
+__global__ void __launch_bounds__(128) aug_coef_kernel(AugSpace A, const float2* __restrict__ src,
+                                                       const int* __restrict__ crow, int64_t n, int64_t m,
+                                                       int64_t mp) {
+    const int64_t c = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    if (c >= m) return;
+    const int64_t nr = rows_of(crow, c, n);
+    const int64_t rpc = (n + kAugChunks - 1) / kAugChunks;
+    const int64_t k0 = (int64_t)blockIdx.y * rpc, k1 = k0 + rpc < nr ? k0 + rpc : nr;
+    const float2* qc = A.q + (c / A.nc) * K;
+    float ar[K], ai[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) { ar[q] = 0.f; ai[q] = 0.f; }
+    for (int64_t k = k0; k < k1; ++k) {
+        const float2 v = src[k * mp + c];
+        const float2* qk = qc + k * A.ld;
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            const float2 w = __ldg(qk + q);
+            ar[q] = fmaf(w.x, v.x, fmaf(w.y, v.y, ar[q]));
+            ai[q] = fmaf(w.x, v.y, fmaf(-w.y, v.x, ai[q]));
+        }
+    }
+    double2* p = A.part + ((int64_t)blockIdx.y * mp + c) * K;
+#pragma unroll
+    for (int q = 0; q < K; ++q) p[q] = make_double2(ar[q], ai[q]);
+}
+
+// dst[c][q] = sum of the chunk partials in chunk order (columns c >= m get 0)
+__global__ void aug_reduce_kernel(AugSpace A, int64_t m, int64_t mp, double2* __restrict__ dst) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= mp * A.k) return;
+    double sr = 0.0, si = 0.0;
+    if (t / A.k < m) {
+        for (int ch = 0; ch < kAugChunks; ++ch) {
+            const double2 v = A.part[(int64_t)ch * mp * A.k + t];
+            sr += v.x;
+            si += v.y;
+        }
+    }
+    dst[t] = make_double2(sr, si);
+}
+
+// y[row, c] -= sum_q Q[row, mesh(c) K + q] coef[c][q] (complex64 y [n, mp])
+template <int K>
+__global__ void __launch_bounds__(128) aug_sub_kernel(AugSpace A, const double2* __restrict__ coef,
+                                                      const int* __restrict__ crow, int64_t n, int64_t m, int64_t mp,
+                                                      float2* __restrict__ y) {
+    const int64_t c = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    if (c >= m) return;
+    const int64_t nr = rows_of(crow, c, n);
+    const int64_t rpc = (n + gridDim.y - 1) / gridDim.y;
+    const int64_t k0 = (int64_t)blockIdx.y * rpc, k1 = k0 + rpc < nr ? k0 + rpc : nr;
+    float cr[K], ci[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+        const double2 v = coef[c * K + q];
+        cr[q] = (float)v.x;
+        ci[q] = (float)v.y;
+    }
+    const float2* qc = A.q + (c / A.nc) * K;
+    for (int64_t k = k0; k < k1; ++k) {
+        const float2* qk = qc + k * A.ld;
+        float sr = 0.f, si = 0.f;
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            const float2 w = __ldg(qk + q);
+            sr = fmaf(w.x, cr[q], fmaf(-w.y, ci[q], sr));
+            si = fmaf(w.x, ci[q], fmaf(w.y, cr[q], si));
+        }
+        float2 v = y[k * mp + c];
+        v.x -= sr;
+        v.y -= si;
+        y[k * mp + c] = v;
+    }
+}
+
+// x[row, c] += sgn sum_q Ut[row, mesh(c) K + q] coef[c][q] in FP64 (complex128 x [n, m])
+template <int K>
+__global__ void __launch_bounds__(128) aug_x_kernel(AugSpace A, const double2* __restrict__ coef, double sgn,
+                                                    const int* __restrict__ crow, int64_t n, int64_t m,
+                                                    double2* __restrict__ x) {
+    const int64_t c = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    if (c >= m) return;
+    const int64_t nr = rows_of(crow, c, n);
+    const int64_t rpc = (n + gridDim.y - 1) / gridDim.y;
+    const int64_t k0 = (int64_t)blockIdx.y * rpc, k1 = k0 + rpc < nr ? k0 + rpc : nr;
+    double cr[K], ci[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+        const double2 v = coef[c * K + q];
+        cr[q] = sgn * v.x;
+        ci[q] = sgn * v.y;
+    }
+    const float2* uc = A.ut + (c / A.nc) * K;
+    for (int64_t k = k0; k < k1; ++k) {
+        const float2* uk = uc + k * A.ld;
+        double sr = 0.0, si = 0.0;
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            const float2 w = __ldg(uk + q);
+            sr += (double)w.x * cr[q] - (double)w.y * ci[q];
+            si += (double)w.x * ci[q] + (double)w.y * cr[q];
+        }
+        double2 v = x[k * m + c];
+        v.x += sr;
+        v.y += si;
+        x[k * m + c] = v;
+    }
+}
+
+// coef[c][q] = sum_{j < r} bq[j][c][q] yv[j][c]  (yv is zero beyond the column's last step)
+__global__ void aug_by_kernel(AugSpace A, const double* __restrict__ yv, int r, int64_t m, int64_t mp) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= mp * A.k) return;
+    const int64_t c = t / A.k;
+    double sr = 0.0, si = 0.0;
+    if (c < m) {
+        for (int j = 0; j < r; ++j) {
+            const double2 bv = A.bq[(int64_t)j * mp * A.k + t];
+            const double yr = yv[2 * ((int64_t)j * mp + c)], yi = yv[2 * ((int64_t)j * mp + c) + 1];
+            sr += bv.x * yr - bv.y * yi;
+            si += bv.x * yi + bv.y * yr;
+        }
+    }
+    A.coef[t] = make_double2(sr, si);
+}
+
+// sq[c] = sum_rows |v[row, c]|^2 (FP64), complex64 v [n, mp]
+__global__ void aug_colnorm2_kernel(const float2* __restrict__ v, int64_t n, int64_t m, int64_t mp,
+                                    double* __restrict__ sq) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m) return;
+    double a = 0.0;
+    for (int64_t k = 0; k < n; ++k) {
+        const float2 w = v[k * mp + c];
+        a += (double)w.x * w.x + (double)w.y * w.y;
+    }
+    sq[c] = a;
+}
+
+// Q^H src into dst (via the chunk partials), then src -= Q dst
+static int aug_project(const AugSpace& A, float2* src, const int* crow, int64_t n, int64_t m, int64_t mp,
+                       double2* dst, cudaStream_t s) {
+    const unsigned cbk = (unsigned)((m + 127) / 128);
+    const dim3 g(cbk, kAugChunks);
+    const unsigned rb = (unsigned)((mp * A.k + 255) / 256);
+    const dim3 gs(cbk, (unsigned)std::max<int64_t>(1, std::min<int64_t>(n, 256)));
+    switch (A.k) {
+        case 4: aug_coef_kernel<4><<<g, 128, 0, s>>>(A, src, crow, n, m, mp); break;
+        case 8: aug_coef_kernel<8><<<g, 128, 0, s>>>(A, src, crow, n, m, mp); break;
+        default: aug_coef_kernel<16><<<g, 128, 0, s>>>(A, src, crow, n, m, mp); break;
+    }
+    aug_reduce_kernel<<<rb, 256, 0, s>>>(A, m, mp, dst);
+    switch (A.k) {
+        case 4: aug_sub_kernel<4><<<gs, 128, 0, s>>>(A, dst, crow, n, m, mp, src); break;
+        case 8: aug_sub_kernel<8><<<gs, 128, 0, s>>>(A, dst, crow, n, m, mp, src); break;
+        default: aug_sub_kernel<16><<<gs, 128, 0, s>>>(A, dst, crow, n, m, mp, src); break;
+    }
+    return check_launch("gmres_blockdiag augmentation projection");
+}
+
+static int aug_update_x(const AugSpace& A, const double2* coef, double sgn, const int* crow, int64_t n, int64_t m,
+                        double* x, cudaStream_t s) {
+    const dim3 gs((unsigned)((m + 127) / 128), (unsigned)std::max<int64_t>(1, std::min<int64_t>(n, 256)));
+    double2* xd = reinterpret_cast<double2*>(x);
+    switch (A.k) {
+        case 4: aug_x_kernel<4><<<gs, 128, 0, s>>>(A, coef, sgn, crow, n, m, xd); break;
+        case 8: aug_x_kernel<8><<<gs, 128, 0, s>>>(A, coef, sgn, crow, n, m, xd); break;
+        default: aug_x_kernel<16><<<gs, 128, 0, s>>>(A, coef, sgn, crow, n, m, xd); break;
+    }
+    return check_launch("gmres_blockdiag augmentation update");
+}
+
 template <typename Prod>
 static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int64_t m, int r, int max_iters,
                           double tol, size_t prod_ws, const int64_t* desc, int nc, void* workspace, size_t ws_bytes,
                           bool use_graph, int64_t* iters_out, int64_t* cycles_out, double* max_relres_out,
-                          int* status_out, cudaStream_t s, const BdPrecond* pc = nullptr) {
+                          int* status_out, cudaStream_t s, const BdPrecond* pc = nullptr,
+                          const AugSpace* aug = nullptr) {
     if (n <= 0 || m <= 0) return set_error(MB_ERR_ARG, "n and m must be > 0");
     if (((uintptr_t)x | (uintptr_t)b) & 15) return set_error(MB_ERR_ARG, "b and x must be 16-byte aligned");
     if (r < 1 || r > kMgMaxRestart) return set_error(MB_ERR_ARG, "restart must be in [1, %d]", kMgMaxRestart);
@@ -1169,6 +1367,7 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
         mg_column_rows<<<cb, 32, 0, s>>>(desc, m, mp, nc, W.crow);
         crow = W.crow;
     }
+    if (aug && !crow) return set_error(MB_ERR_ARG, "gmres: an augmentation subspace needs the batch descriptor");
     int64_t pc_rows = 0;  // sum of E_i (the preconditioned block-diagonal residual's rows)
     if (pc) {
         std::vector<int64_t> dh((size_t)6 * pc->n_mesh);
@@ -1204,6 +1403,7 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
             vj = pc->z32;
         }
         if ((e = prod(reinterpret_cast<const float*>(vj), reinterpret_cast<float*>(W.y32), st))) return e;
+        if (aug && (e = aug_project(*aug, W.y32, crow, n, m, mp, aug->bq + (size_t)j * mp * aug->k, st))) return e;
         // CGS2: pass 1 projects the product output y into w, pass 2 re-orthogonalises w and
         // accumulates |w|^2
         cudaMemsetAsync(W.hc, 0, 16 * (size_t)nb * mp, st);
@@ -1245,6 +1445,12 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
                 return cleanup(), rc;
             cudaMemsetAsync(W.beta, 0, 8 * mp, s);
             mg_residual<<<rgrid, rblk, 0, s>>>(reinterpret_cast<const double2*>(b), W.y32, n, m, mp, W.V, W.beta);
+        }
+        if (aug) {  // X += Ut Q^H r, r -= Q Q^H r, then |r|^2 again
+            if ((rc = aug_project(*aug, W.V, crow, n, m, mp, aug->coef, s)) ||
+                (rc = aug_update_x(*aug, aug->coef, 1.0, crow, n, m, x, s)))
+                return cleanup(), rc;
+            aug_colnorm2_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(W.V, n, m, mp, W.beta);
         }
         cudaMemcpyAsync(hbeta.data(), W.beta, 8 * mp, cudaMemcpyDeviceToHost, s);
         if ((rc = mg_sync(s, "gmres_multi residual"))) return cleanup(), rc;
@@ -1301,6 +1507,10 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
             upd_k<<<cgrid, kGsThreads, gs_smem<kS>((size_t)j * 32 * 8), s>>>(maps_w, W.yv, n, mp, m, j, 1.f, x,
                                                                            nullptr, W.status);
         }
+        if (j > 0 && aug) {  // X -= Ut (B y)
+            aug_by_kernel<<<(unsigned)((mp * aug->k + 255) / 256), 256, 0, s>>>(*aug, W.yv, j, m, mp);
+            if ((rc = aug_update_x(*aug, aug->coef, -1.0, crow, n, m, x, s))) return cleanup(), rc;
+        }
         if ((rc = check_status())) return cleanup(), rc;
     }
     cleanup();
@@ -1350,7 +1560,8 @@ static int blockdiag_solve(const float* z, const int64_t* desc, const int64_t* g
                            int rows_per_warp, int nc, int64_t n_rows, const double* b, double* x, int r,
                            int max_iters, double tol, bool use_graph, void* workspace, size_t ws_bytes,
                            int64_t* iters_out, int64_t* cycles_out, double* max_relres_out, int* status_out,
-                           cudaStream_t s, const int32_t* m_cols, const float* m_vals, const int64_t* eoff) {
+                           cudaStream_t s, const int32_t* m_cols, const float* m_vals, const int64_t* eoff,
+                           const float* aug_q = nullptr, const float* aug_ut = nullptr, int aug_k = 0) {
     const int64_t m = (int64_t)n_mesh * nc, mp = padded_width(m);
     MgWork W;
     const size_t map_bytes = bd_prod_bytes(n_rows, m);  // tensor maps (>= n_mesh) + preconditioner buffers
@@ -1377,8 +1588,25 @@ static int blockdiag_solve(const float* z, const int64_t* desc, const int64_t* g
             return bd_launch(zmaps, v32, n_rows, desc, goff, n_mesh, total_warps, mp, nc, y32, status, st);
         return blockdiag_matvec(z, desc, goff, n_mesh, total_warps, v32, mp, nc, rows_per_warp, y32, st);
     };
-    return gmres_lockstep(prod, n_rows, b, x, m, r, max_iters, tol, map_bytes, desc, nc, workspace, ws_bytes, use_graph,
-                          iters_out, cycles_out, max_relres_out, status_out, s, m_cols ? &pc : nullptr);
+    if (!aug_q)
+        return gmres_lockstep(prod, n_rows, b, x, m, r, max_iters, tol, map_bytes, desc, nc, workspace, ws_bytes,
+                              use_graph, iters_out, cycles_out, max_relres_out, status_out, s, m_cols ? &pc : nullptr);
+    if (r < 1 || r > kMgMaxRestart) return set_error(MB_ERR_ARG, "restart must be in [1, %d]", kMgMaxRestart);
+    // the subspace's coefficients: chunk partials, the cycle's b_j and one scratch set
+    const size_t per = (size_t)mp * aug_k * sizeof(double2);
+    char* abuf = nullptr;
+    if (cudaMallocAsync(reinterpret_cast<void**>(&abuf), per * (kAugChunks + r + 1), s) != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(MB_ERR_CUDA, "gmres_blockdiag: augmentation buffers could not be allocated");
+    }
+    AugSpace A{reinterpret_cast<const float2*>(aug_q), reinterpret_cast<const float2*>(aug_ut), (int64_t)n_mesh * aug_k,
+               aug_k, nc, reinterpret_cast<double2*>(abuf), reinterpret_cast<double2*>(abuf + per * kAugChunks),
+               reinterpret_cast<double2*>(abuf + per * (kAugChunks + r))};
+    const int rc = gmres_lockstep(prod, n_rows, b, x, m, r, max_iters, tol, map_bytes, desc, nc, workspace, ws_bytes,
+                                  use_graph, iters_out, cycles_out, max_relres_out, status_out, s,
+                                  m_cols ? &pc : nullptr, &A);
+    cudaFreeAsync(abuf, s);
+    return rc;
 }
 
 int gmres_blockdiag(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
@@ -1399,6 +1627,21 @@ int gmres_blockdiag_pc(const float* z, const int64_t* desc, const int64_t* goff,
     return blockdiag_solve(z, desc, goff, n_mesh, total_warps, rows_per_warp, nc, n_rows, b, x, r, max_iters, tol,
                            use_graph, workspace, ws_bytes, iters_out, cycles_out, max_relres_out, status_out, s, m_cols,
                            m_vals, eoff);
+}
+
+int gmres_blockdiag_aug(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
+                        int rows_per_warp, int nc, int64_t n_rows, const int32_t* m_cols, const float* m_vals,
+                        const int64_t* eoff, const float* aug_q, const float* aug_ut, int aug_k, const double* b,
+                        double* x, int r, int max_iters, double tol, bool use_graph, void* workspace, size_t ws_bytes,
+                        int64_t* iters_out, int64_t* cycles_out, double* max_relres_out, int* status_out,
+                        cudaStream_t s) {
+    if (!aug_q || !aug_ut) return set_error(MB_ERR_ARG, "gmres_blockdiag_aug: null subspace");
+    if (aug_k != 4 && aug_k != 8 && aug_k != 16) return set_error(MB_ERR_UNSUPPORTED, "subspace size must be 4, 8 or 16");
+    if ((m_cols != nullptr) != (m_vals != nullptr) || (m_cols != nullptr) != (eoff != nullptr))
+        return set_error(MB_ERR_ARG, "gmres_blockdiag_aug: give all of m_cols, m_vals, edge_offsets or none");
+    return blockdiag_solve(z, desc, goff, n_mesh, total_warps, rows_per_warp, nc, n_rows, b, x, r, max_iters, tol,
+                           use_graph, workspace, ws_bytes, iters_out, cycles_out, max_relres_out, status_out, s, m_cols,
+                           m_vals, eoff, aug_q, aug_ut, aug_k);
 }
 
 }  // namespace mb

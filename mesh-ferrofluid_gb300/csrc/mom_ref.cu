@@ -881,24 +881,85 @@ __global__ void __launch_bounds__(128, NX <= 4 ? MB_FAST_MIN_BLOCKS : 2) mom_ref
               make_float2(re, im));
 }
 
+// Persistent form: one resident grid (SMs x blocks per SM); each block takes work items --
+// the same (mesh, row, 128-column tile) items as the grid form's blocks, in the same order --
+// from a counter in device memory until they run out.  No wait on another block: a block
+// only increments the counter.
+template <int NX, int NY>
+__global__ void __launch_bounds__(128, NX <= 4 ? MB_FAST_MIN_BLOCKS : 2) mom_ref_zmat_batched_persistent_kernel(
+    const float* __restrict__ verts, const int32_t* __restrict__ faces, const float* __restrict__ areas,
+    const float* __restrict__ normals, const int32_t* __restrict__ fei, const int64_t* __restrict__ desc,
+    const int64_t* __restrict__ boff, int64_t total_items, unsigned long long* queue,
+    const double* __restrict__ ks, int n_mesh, const float* __restrict__ gpx, const float* __restrict__ gwx,
+    const float* __restrict__ gpy, const float* __restrict__ gwy, float* __restrict__ z) {
+    __shared__ float4 s_t[NX * NX], s_s[NY * NY];
+    __shared__ long long s_item;
+    stage_rules<NX, NY>(gpx, gwx, gpy, gwy, s_t, s_s);
+    for (;;) {
+        __syncthreads();  // the rules are staged / every thread has read the previous item
+        if (threadIdx.x == 0) s_item = (long long)atomicAdd(queue, 1ull);
+        __syncthreads();
+        const int64_t b = s_item;
+        if (b >= total_items) return;
+        const int i = seg_find(boff, 1, n_mesh, b);
+        const int64_t fo = __ldg(desc + 6 * i), nf = __ldg(desc + 6 * i + 1), ne = __ldg(desc + 6 * i + 2);
+        const int64_t ncol = 3 * nf, cb = (ncol + 127) / 128, local = b - __ldg(boff + i);
+        const int64_t row = local / cb, col = (local % cb) * 128 + threadIdx.x;
+        if (col < ncol) {
+            float re, im;
+            mom_entry_fast<NX, NY>(verts, faces, areas, normals, s_t, s_s, (float)__ldg(ks + i), fo + row / 3,
+                                   (int)(row % 3), fo + col / 3, (int)(col % 3), &re, &im);
+            const int64_t m = __ldg(fei + 3 * fo + row), n = __ldg(fei + 3 * fo + col);
+            atomicAdd(reinterpret_cast<float2*>(z + 2 * (__ldg(desc + 6 * i + 3) + m * (ne + (ne & 1)) + n)),
+                      make_float2(re, im));
+        }
+    }
+}
+
 int launch_mom_ref_zmat_batched(const float* verts, const int32_t* faces, const float* areas, const float* normals,
                                 const int32_t* fei, const int64_t* desc, const int64_t* boff, int64_t total_blocks,
                                 const double* ks, int n_mesh, const float* gpx, const float* gwx, int nx,
-                                const float* gpy, const float* gwy, int ny, float* z, cudaStream_t s) {
+                                const float* gpy, const float* gwy, int ny, float* z, cudaStream_t s,
+                                int persistent) {
     if (n_mesh <= 0 || total_blocks <= 0) return MB_OK;
-    if (total_blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "batch too large for one launch");
+    if (!persistent && total_blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "batch too large for one launch");
+    unsigned long long* queue = nullptr;
+    unsigned grid = 0;
+    if (persistent) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaMallocAsync(reinterpret_cast<void**>(&queue), sizeof(unsigned long long), s) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(MB_ERR_CUDA, "mom_ref_zmat_batched: work counter allocation failed");
+        }
+        cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
+        grid = (unsigned)sms;
+    }
+    int rc = MB_ERR_UNSUPPORTED;
 #define MB_RB(NXV, NYV)                                                                                      \
-    if (nx == NXV && ny == NYV) {                                                                            \
-        mom_ref_zmat_batched_kernel<NXV, NYV><<<(unsigned)total_blocks, 128, 0, s>>>(                        \
-            verts, faces, areas, normals, fei, desc, boff, ks, n_mesh, gpx, gwx, gpy, gwy, z);              \
-        return check_launch("mom_ref_zmat_batched");                                                        \
+    if (rc == MB_ERR_UNSUPPORTED && nx == NXV && ny == NYV) {                                                \
+        if (persistent) {                                                                                    \
+            int per_sm = 1;                                                                                  \
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mom_ref_zmat_batched_persistent_kernel<NXV, NYV>, \
+                                                          128, 0);                                           \
+            const int64_t g = std::min<int64_t>(total_blocks, (int64_t)grid * std::max(per_sm, 1));          \
+            mom_ref_zmat_batched_persistent_kernel<NXV, NYV><<<(unsigned)g, 128, 0, s>>>(                    \
+                verts, faces, areas, normals, fei, desc, boff, total_blocks, queue, ks, n_mesh, gpx, gwx, gpy, gwy, z); \
+        } else {                                                                                             \
+            mom_ref_zmat_batched_kernel<NXV, NYV><<<(unsigned)total_blocks, 128, 0, s>>>(                    \
+                verts, faces, areas, normals, fei, desc, boff, ks, n_mesh, gpx, gwx, gpy, gwy, z);          \
+        }                                                                                                    \
+        rc = check_launch("mom_ref_zmat_batched");                                                          \
     }
     MB_RB(4, 3)
     MB_RB(3, 2)
     MB_RB(2, 1)
     MB_RB(5, 4)
 #undef MB_RB
-    return set_error(MB_ERR_UNSUPPORTED, "batched reference rule: gaussQR in {2, 3, 4, 5}");
+    if (queue) cudaFreeAsync(queue, s);
+    if (rc == MB_ERR_UNSUPPORTED) return set_error(MB_ERR_UNSUPPORTED, "batched reference rule: gaussQR in {2, 3, 4, 5}");
+    return rc;
 }
 
 // waves [n_mesh * nrhs] plane-wave records; rhs: [rows, ld] interleaved complex64,

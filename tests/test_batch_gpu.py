@@ -195,3 +195,96 @@ def test_batched_rows_assembly_every_tile_and_schedule(pkg, cuda):
     assert best in [("pair", None)] + [(r, o) for r in (8, 16, 32) for o in ("packed", "largest")]
     Z = bt.assemble()
     assert (torch.linalg.norm(Z - ref) / torch.linalg.norm(ref)).item() < 1e-6
+
+
+def test_batched_cfie_persistent_assembly_equals_grid(pkg, cuda):
+    """The reference-rule batch assembled by the resident grid that takes its tiles from a
+    work counter equals the one-block-per-tile launch (the same entries, summed by the same
+    atomics: equal to 1e-6), on every mesh; the autotuner picks one of the two."""
+    M = pkg.meshes
+    meshes = [M.icosphere(1, 1.0), _bipyramid(), M.ellipsoid(2), M.star_shape(2, seed=3)]
+    ks = [1.5, 2.0, 2.5, 3.0]
+    bt = pkg.batch.MeshBatch(meshes, ks, device=cuda, formulation="cfie_ref")
+    bt.excitation(_waves(pkg, bt.n_mesh, 4, ks, cuda))
+    bt.asm_config = ("grid", None)
+    ref = bt.assemble()
+    bt.asm_config = ("persistent", None)
+    for _ in range(2):  # the counter starts from zero on every call
+        Z = bt.assemble()
+        for i in range(bt.n_mesh):
+            zi, zr = bt.z_block(Z, i), bt.z_block(ref, i)
+            assert (torch.linalg.norm(zi - zr) / torch.linalg.norm(zr)).item() < 1e-6, i
+    best = bt.autotune_assembly()
+    assert best in [("grid", None), ("persistent", None)] and set(bt.asm_times) == {("grid", None),
+                                                                                    ("persistent", None)}
+
+
+def _dense_refs(bt, Z, B, nc=4):
+    refs = []
+    for i in range(bt.n_mesh):
+        e = bt.n_edges[i]
+        refs.append(torch.linalg.solve(bt.z_block(Z, i).to(torch.complex128), B[:e, nc * i:nc * (i + 1)].to(
+            torch.complex128)))
+    return refs
+
+
+@pytest.mark.parametrize("k,precond,use_graph", [(8, False, False), (16, True, True), (4, True, False)])
+def test_augmented_solve_matches_dense(pkg, cuda, k, precond, use_graph):
+    """Lockstep GMRES with a random K-vector deflation subspace per mesh (with and without the
+    near-field preconditioner, graph-captured or not) converges to the dense solution; the
+    reported residual is the true one."""
+    bt, meshes, ks = _batch(pkg, cuda)
+    waves = _waves(pkg, bt.n_mesh, 4, ks, cuda, seed=1)
+    Z = bt.assemble()
+    B = bt.excitation(waves)
+    g = torch.Generator(device="cpu").manual_seed(3)
+    U = torch.randn(bt.n_rows, bt.n_mesh, k, dtype=torch.complex64, generator=g).to(cuda)
+    aug = bt.augmentation(Z, U)
+    P = bt.spai(Z) if precond else None
+    X, info = bt.solve(Z, B, restart=30, tol=1e-9, max_iters=3000, use_graph=use_graph, M=P, aug=aug)
+    assert info["converged"], info
+    refs = _dense_refs(bt, Z, B)
+    for i in range(bt.n_mesh):
+        e = bt.n_edges[i]
+        got = X[:e, 4 * i:4 * i + 4]
+        err = (torch.linalg.norm(got - refs[i], dim=0) / torch.linalg.norm(refs[i], dim=0)).max().item()
+        assert err < 1e-5, (i, err)
+        assert torch.all(X[e:, 4 * i:4 * i + 4] == 0)
+        r = B[:e, 4 * i:4 * i + 4].to(torch.complex128) - bt.z_block(Z, i).to(torch.complex128) @ got
+        rel = (torch.linalg.norm(r, dim=0) / torch.linalg.norm(B[:e, 4 * i:4 * i + 4].to(torch.complex128),
+                                                                 dim=0)).max().item()
+        assert rel < 1e-8, (i, rel)
+
+
+def test_augmented_subspace_holding_the_solutions_needs_no_arnoldi_step(pkg, cuda):
+    """When each mesh's subspace holds its columns' solutions (real and imaginary parts of the
+    four dense solutions: K = 8), the first cycle start already solves every column: no
+    Arnoldi step is taken and the answer equals the dense one."""
+    bt, meshes, ks = _batch(pkg, cuda)
+    waves = _waves(pkg, bt.n_mesh, 4, ks, cuda, seed=4)
+    Z = bt.assemble()
+    B = bt.excitation(waves)
+    refs = _dense_refs(bt, Z, B)
+    U = torch.zeros(bt.n_rows, bt.n_mesh, 8, dtype=torch.complex64, device=cuda)
+    for i in range(bt.n_mesh):
+        e = bt.n_edges[i]
+        U[:e, i, :4] = refs[i].real.to(torch.complex64)
+        U[:e, i, 4:] = refs[i].imag.to(torch.complex64)
+    X, info = bt.solve(Z, B, restart=20, tol=1e-5, max_iters=100, use_graph=False, aug=bt.augmentation(Z, U))
+    assert info["converged"] and info["iterations"] == 0, info
+    for i in range(bt.n_mesh):
+        e = bt.n_edges[i]
+        err = (torch.linalg.norm(X[:e, 4 * i:4 * i + 4] - refs[i], dim=0) / torch.linalg.norm(refs[i], dim=0))
+        assert err.max().item() < 1e-5, (i, err)
+
+
+def test_augmented_solve_rejects_bad_subspace(pkg, cuda):
+    bt, meshes, ks = _batch(pkg, cuda)
+    Z = bt.assemble()
+    bt.excitation(_waves(pkg, bt.n_mesh, 4, ks, cuda))
+    with pytest.raises(ValueError):
+        bt.augmentation(Z, torch.zeros(bt.n_rows, bt.n_mesh, 5, dtype=torch.complex64, device=cuda))
+    q, ut, k = bt.augmentation(Z, torch.ones(bt.n_rows, bt.n_mesh, 4, dtype=torch.complex64, device=cuda))
+    B = bt.excitation(_waves(pkg, bt.n_mesh, 4, ks, cuda))
+    with pytest.raises(ValueError):
+        bt.solve(Z, B, aug=(q[:, :-1], ut[:, :-1], k))
