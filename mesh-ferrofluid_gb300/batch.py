@@ -302,9 +302,10 @@ class MeshBatch:
         """The deflation subspace of every mesh for ``solve(aug=...)``: U [n_rows, n_mesh, K]
         (K in {4, 8, 16}) vectors of x-space per mesh (rows beyond E_i are ignored).  Returns
         (Q, Ut, K): C_i = Z_i U_i by block-diagonal products (8 columns per mesh at a time), an
-        orthonormal basis Q_i of its range (one batched FP64 thin SVD, C_i = Q_i S_i V_i^H) and
-        Ut_i = U_i V_i S_i^{-1} -- complex64 [n_rows, n_mesh K], so that Z_i Ut_i = Q_i.  Directions
-        whose singular value is below 1e-8 of the largest are dropped (zero columns)."""
+        orthonormal basis Q_i of its range from the FP64 Gram matrix (C_i^H C_i = V_i S_i^2 V_i^H,
+        one batched K x K eigensolve; Q_i = C_i V_i S_i^{-1}) and Ut_i = U_i V_i S_i^{-1} --
+        complex64 [n_rows, n_mesh K], so that Z_i Ut_i = Q_i.  Directions whose singular value is
+        below 1e-6 of the largest are dropped (zero columns)."""
         n_rows, n_mesh, K = U.shape
         if n_rows != self.n_rows or n_mesh != self.n_mesh or K not in (4, 8, 16):
             raise ValueError("U must be [n_rows, n_mesh, K] with K in {4, 8, 16}")
@@ -318,13 +319,15 @@ class MeshBatch:
             Uh = U[:, :, h:h + w].contiguous().view(n_rows, n_mesh * w)
             parts.append(self.matvec(z_flat, Uh, nc=w).view(n_rows, n_mesh, w))
         C = torch.cat(parts, 2).permute(1, 0, 2).to(torch.complex128)  # [n_mesh, n_rows, K]
-        # C_i = W S V^H: Q_i = W, Ut_i = U_i V S^{-1} (so Z_i Ut_i = Q_i exactly); directions with
-        # S below 1e-8 of the largest get zero columns in both
-        W, S, Vh = torch.linalg.svd(C, full_matrices=False)
-        keep = S > 1e-8 * S[:, :1].clamp_min(1e-300)
-        inv = torch.where(keep, 1.0 / S.clamp_min(1e-300), torch.zeros_like(S))
-        Q = W * keep[:, None, :]
-        Ut = (U.permute(1, 0, 2).to(torch.complex128) @ Vh.mH) * inv[:, None, :].to(torch.complex128)
+        # C_i^H C_i = V S^2 V^H (a K x K Hermitian eigenproblem per mesh, batched): Q_i = C_i V S^-1,
+        # Ut_i = U_i V S^-1, so Z_i Ut_i = Q_i holds by construction whatever the rounding of Q's
+        # orthonormality; directions with S^2 below 1e-12 of the largest get zero columns
+        lam, V = torch.linalg.eigh(C.mH @ C)
+        keep = lam > 1e-12 * lam[:, -1:].clamp_min(1e-300)
+        inv = torch.where(keep, lam.clamp_min(1e-300).rsqrt(), torch.zeros_like(lam)).to(torch.complex128)
+        VS = V * inv[:, None, :]
+        Q = C @ VS
+        Ut = U.permute(1, 0, 2).to(torch.complex128) @ VS
         q = Q.permute(1, 0, 2).reshape(n_rows, n_mesh * K).to(torch.complex64).contiguous()
         ut = Ut.permute(1, 0, 2).reshape(n_rows, n_mesh * K).to(torch.complex64).contiguous()
         return q, ut, K

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "packed.cuh"
 #include "spai_apply.cuh"
 
 namespace mb {
@@ -1059,12 +1060,12 @@ __global__ void pg_split_kernel(const double2* __restrict__ x, int64_t n, float4
     xs[k] = make_float4(hr, hi, (float)(v.x - (double)hr), (float)(v.y - (double)hi));
 }
 
-// s + t exactly as s' + e (Knuth's TwoSum; rounding-mode intrinsics keep the compiler from
-// contracting or reordering it)
-__device__ __forceinline__ void two_sum(float& s, float t, float& e) {
-    const float u = __fadd_rn(s, t);
-    const float bb = __fsub_rn(u, s);
-    e = __fadd_rn(__fsub_rn(s, __fsub_rn(u, bb)), __fsub_rn(t, bb));
+// s + t exactly as s' + e on both lanes of a packed pair (Knuth's TwoSum; the explicit
+// add / sub .rn.f32x2 instructions keep the compiler from contracting or reordering it)
+__device__ __forceinline__ void two_sum2(float2& s, float2 t, float2& e) {
+    const float2 u = add2(s, t);
+    const float2 bb = sub2(u, s);
+    e = add2(sub2(s, sub2(u, bb)), sub2(t, bb));
     s = u;
 }
 
@@ -1078,23 +1079,24 @@ __global__ void __launch_bounds__(256) residual_c64x_kernel(const float2* __rest
     const int lane = threadIdx.x & 31;
     if (row >= n) return;
     const float2* zr = z + row * n;
-    float sr = 0.f, si = 0.f, cr = 0.f, ci = 0.f;
+    // real and imaginary chains side by side in packed f32x2 instructions (lane x: real,
+    // lane y: imaginary), the same operations in the same order as two scalar chains:
+    // p1 = a.x (x_r, x_i), p2 = (-a.y x_i, a.y x_r); en = -(rounding error of p), exact
+    float2 s = bc(0.f), c = bc(0.f);
     for (int64_t j = lane; j < n; j += 32) {
         const float2 a = __ldcs(zr + j);
         const float4 x = __ldg(xs + j);
-        const float p1 = __fmul_rn(a.x, x.x), e1 = fmaf(a.x, x.x, -p1);
-        const float p2 = __fmul_rn(-a.y, x.y), e2 = fmaf(-a.y, x.y, -p2);
-        const float p3 = __fmul_rn(a.x, x.y), e3 = fmaf(a.x, x.y, -p3);
-        const float p4 = __fmul_rn(a.y, x.x), e4 = fmaf(a.y, x.x, -p4);
-        float t1, t2, t3, t4;
-        two_sum(sr, p1, t1);
-        two_sum(sr, p2, t2);
-        two_sum(si, p3, t3);
-        two_sum(si, p4, t4);
-        cr += (t1 + t2) + (e1 + e2) + fmaf(a.x, x.z, -a.y * x.w);
-        ci += (t3 + t4) + (e3 + e4) + fmaf(a.x, x.w, a.y * x.z);
+        const float2 xh = make_float2(x.x, x.y), xhs = make_float2(x.y, x.x);
+        const float2 xl = make_float2(x.z, x.w), xls = make_float2(x.w, x.z);
+        const float2 A1 = bc(a.x), A1n = bc(-a.x), A2 = make_float2(-a.y, a.y), A2n = make_float2(a.y, -a.y);
+        const float2 p1 = mul2(A1, xh), en1 = fma2(A1n, xh, p1);
+        const float2 p2 = mul2(A2, xhs), en2 = fma2(A2n, xhs, p2);
+        float2 t1, t2;
+        two_sum2(s, p1, t1);
+        two_sum2(s, p2, t2);
+        c = add2(c, add2(sub2(add2(t1, t2), add2(en1, en2)), fma2(A1, xl, mul2(A2, xls))));
     }
-    const double ar = warp_sum((double)sr + (double)cr), ai = warp_sum((double)si + (double)ci);
+    const double ar = warp_sum((double)s.x + (double)c.x), ai = warp_sum((double)s.y + (double)c.y);
     if (lane == 0) r[row] = make_double2(b[row].x - ar, b[row].y - ai);
 }
 
