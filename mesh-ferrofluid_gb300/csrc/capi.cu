@@ -105,7 +105,7 @@ size_t gmres_blockdiag_workspace_bytes(int64_t n, int64_t m, int r);
 int gmres_multi_column_steps(const void* ws, int64_t n, int64_t m, int r, int32_t* out, cudaStream_t s);
 int gmres_blockdiag_column_steps(const void* ws, int64_t n, int64_t m, int r, int32_t* out, cudaStream_t s);
 int blockdiag_matvec(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
-                     const float* x, int64_t ld, int nc, int rows, float* y, cudaStream_t s);
+                     const float* x, int64_t ld, int nc, int rows, float* y, cudaStream_t s, const int* cact);
 int gmres_blockdiag(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
                     int rows_per_warp, int nc, int64_t n_rows, const double* b, double* x, int r, int max_iters,
                     double tol, bool use_graph, void* workspace, size_t ws_bytes, int64_t* iters_out,
@@ -757,7 +757,8 @@ int mb_blockdiag_matvec_c64(const float* z, const int64_t* desc, const int64_t* 
     MB_REQUIRE(n_mesh >= 0 && total_warps >= 0, "bad sizes");
     if (n_mesh == 0) return MB_OK;
     MB_REQUIRE(z && desc && goff && x && y, "null pointer argument");
-    return blockdiag_matvec(z, desc, goff, n_mesh, total_warps, x, ld, nc, rows_per_warp, y, as_stream(stream));
+    return blockdiag_matvec(z, desc, goff, n_mesh, total_warps, x, ld, nc, rows_per_warp, y, as_stream(stream),
+                            nullptr);
 }
 
 size_t mb_gmres_blockdiag_workspace_bytes(int64_t n_rows, int64_t m, int restart) {

@@ -625,17 +625,29 @@ __device__ __forceinline__ int seg_of(const int64_t* __restrict__ off, int n, in
     return lo;
 }
 
+// A mesh is live while any of its nc columns (first column co) is still iterating in the
+// current cycle (cact = the solver's per-column flags; null: every mesh is live).  The
+// products of an Arnoldi step skip the other meshes: their columns' next basis vectors are
+// scaled by 0, so their (stale, finite) product rows are never used.
+__device__ __forceinline__ bool mesh_live(const int* __restrict__ cact, int64_t co, int nc) {
+    if (!cact) return true;
+    for (int c = 0; c < nc; ++c)
+        if (cact[co + c]) return true;
+    return false;
+}
+
 template <int ROWS, int NC>
 __global__ void __launch_bounds__(256) blockdiag_matvec_kernel(const float* __restrict__ z,
                                                                const int64_t* __restrict__ desc,
                                                                const int64_t* __restrict__ goff, int n_mesh,
                                                                const float* __restrict__ x, int64_t ld,
-                                                               float* __restrict__ y) {
+                                                               float* __restrict__ y, const int* __restrict__ cact) {
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= __ldg(goff + n_mesh)) return;
     const int i = seg_of(goff, n_mesh, w);
     const int64_t E = __ldg(desc + 6 * i + 2), zo = __ldg(desc + 6 * i + 3), co = __ldg(desc + 6 * i + 5);
+    if (!mesh_live(cact, co, NC)) return;  // warp-uniform
     const int64_t P = E + (E & 1);
     const int64_t r0 = (w - __ldg(goff + i)) * ROWS;
     const float2* zc = reinterpret_cast<const float2*>(z) + zo;
@@ -711,7 +723,8 @@ __global__ void __launch_bounds__(kBdThreads) blockdiag_stream_kernel(const CUte
                                                                       const int64_t* __restrict__ desc,
                                                                       const int64_t* __restrict__ uoff, int n_mesh,
                                                                       int64_t ld, float* __restrict__ y,
-                                                                      int* __restrict__ status) {
+                                                                      int* __restrict__ status,
+                                                                      const int* __restrict__ cact) {
     extern __shared__ unsigned char bd_raw[];
     unsigned char* stage =
         reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(bd_raw) + 1023) & ~uintptr_t(1023));
@@ -735,6 +748,7 @@ __global__ void __launch_bounds__(kBdThreads) blockdiag_stream_kernel(const CUte
             for (int64_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
                 const int i = seg_of(uoff, n_mesh, u);
                 const int64_t E = __ldg(desc + 6 * i + 2), co = __ldg(desc + 6 * i + 5);
+                if (!mesh_live(cact, co, NC)) continue;  // the consumers skip the same units
                 const int r0 = (int)((u - __ldg(uoff + i)) * kBdRows);
                 const CUtensorMap* zm = zmaps + i;
                 for (int64_t l0 = 0; l0 < E; l0 += kBdCols, ++p) {
@@ -761,6 +775,7 @@ __global__ void __launch_bounds__(kBdThreads) blockdiag_stream_kernel(const CUte
         for (int64_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
             const int i = seg_of(uoff, n_mesh, u);
             const int64_t E = __ldg(desc + 6 * i + 2), co = __ldg(desc + 6 * i + 5);
+            if (!mesh_live(cact, co, NC)) continue;
             const int64_t r0 = (u - __ldg(uoff + i)) * kBdRows + warp * 4;
             const int cb0 = (int)(co & 1) * 8;  // byte column of the mesh's first column in the x tile
             float ar[4][NC], ai[4][NC];
@@ -857,7 +872,7 @@ static int bd_xmap(CUtensorMap* map, const float* x, int64_t n_rows, int64_t ld)
 
 static int bd_launch(const CUtensorMap* zmaps, const float* x, int64_t n_rows, const int64_t* desc,
                      const int64_t* goff, int n_mesh, int64_t total_units, int64_t ld, int nc, float* y, int* status,
-                     cudaStream_t s) {
+                     cudaStream_t s, const int* cact = nullptr) {
     CUtensorMap xm;
     int rc = bd_xmap(&xm, x, n_rows, ld);
     if (rc) return rc;
@@ -870,7 +885,7 @@ static int bd_launch(const CUtensorMap* zmaps, const float* x, int64_t n_rows, c
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, blockdiag_stream_kernel<C>, kBdThreads, kBdSmem);   \
         const int64_t g = std::max<int64_t>(1, std::min<int64_t>(total_units, (int64_t)std::max(per_sm, 1) * sms)); \
         blockdiag_stream_kernel<C><<<(unsigned)g, kBdThreads, kBdSmem, s>>>(zmaps, xm, desc, goff, n_mesh, ld, y,  \
-                                                                           status);                             \
+                                                                           status, cact);                       \
         return check_launch("blockdiag_matvec (streamed)");                                                     \
     }
     MB_BDS(1) MB_BDS(2) MB_BDS(4) MB_BDS(8)
@@ -879,7 +894,7 @@ static int bd_launch(const CUtensorMap* zmaps, const float* x, int64_t n_rows, c
 }
 
 int blockdiag_matvec(const float* z, const int64_t* desc, const int64_t* goff, int n_mesh, int64_t total_warps,
-                     const float* x, int64_t ld, int nc, int rows, float* y, cudaStream_t s) {
+                     const float* x, int64_t ld, int nc, int rows, float* y, cudaStream_t s, const int* cact) {
     if (n_mesh <= 0 || total_warps <= 0) return MB_OK;
     if (rows == kBdRows) {
         // standalone call: the tensor maps and the time-out word in stream-ordered buffers of
@@ -914,7 +929,7 @@ int blockdiag_matvec(const float* z, const int64_t* desc, const int64_t* goff, i
     if (blocks > 0x7fffffffLL) return set_error(MB_ERR_SIZE, "batch too large for one launch");
 #define MB_BD(R, C)                                                                                           \
     if (rows == R && nc == C) {                                                                               \
-        blockdiag_matvec_kernel<R, C><<<(unsigned)blocks, 256, 0, s>>>(z, desc, goff, n_mesh, x, ld, y);      \
+        blockdiag_matvec_kernel<R, C><<<(unsigned)blocks, 256, 0, s>>>(z, desc, goff, n_mesh, x, ld, y, cact); \
         return check_launch("blockdiag_matvec");                                                              \
     }
     MB_BD(1, 1) MB_BD(2, 1) MB_BD(4, 1) MB_BD(8, 1)
@@ -1107,7 +1122,8 @@ __global__ void __launch_bounds__(256) bd_update_kernel(BdPrecond P, int64_t n, 
     x[r * m + c] = o;
 }
 
-// The lockstep driver.  prod(v, y, stream) computes Y = Z V for [n, mp] complex64 blocks
+// The lockstep driver.  prod(v, y, stream, cact) computes Y = Z V for [n, mp] complex64 blocks
+// (cact: the per-column active flags of an Arnoldi step, or null for every column)
 // (mp = m rounded up to even; the padding column has b = 0 and stays inactive).
 // desc / nc (optional): block-diagonal layout, column c of mesh c / nc has desc[.][2] rows.
 // With use_graph, the r Arnoldi steps of a cycle are captured once as a CUDA graph and
@@ -1402,7 +1418,8 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
                 *pc, n, m, mp, vj, pc->z32);
             vj = pc->z32;
         }
-        if ((e = prod(reinterpret_cast<const float*>(vj), reinterpret_cast<float*>(W.y32), st))) return e;
+        // an Arnoldi step's product skips the meshes none of whose columns is still iterating
+        if ((e = prod(reinterpret_cast<const float*>(vj), reinterpret_cast<float*>(W.y32), st, W.active))) return e;
         if (aug && (e = aug_project(*aug, W.y32, crow, n, m, mp, aug->bq + (size_t)j * mp * aug->k, st))) return e;
         // CGS2: pass 1 projects the product output y into w, pass 2 re-orthogonalises w and
         // accumulates |w|^2
@@ -1441,7 +1458,7 @@ static int gmres_lockstep(Prod prod, int64_t n, const double* b, double* x, int6
             if ((rc = bd_residual(*pc, pc_rows, n, m, mp, x, b, W.V, W.beta, s))) return cleanup(), rc;
         } else {
             mg_to_c64<<<rgrid, rblk, 0, s>>>(reinterpret_cast<const double2*>(x), n, m, mp, W.w);
-            if ((rc = prod(reinterpret_cast<const float*>(W.w), reinterpret_cast<float*>(W.y32), s)))
+            if ((rc = prod(reinterpret_cast<const float*>(W.w), reinterpret_cast<float*>(W.y32), s, nullptr)))
                 return cleanup(), rc;
             cudaMemsetAsync(W.beta, 0, 8 * mp, s);
             mg_residual<<<rgrid, rblk, 0, s>>>(reinterpret_cast<const double2*>(b), W.y32, n, m, mp, W.V, W.beta);
@@ -1547,7 +1564,7 @@ int gmres_multi(const float* z_hi, const float* z_lo, int64_t n, const double* b
     if (ws_bytes < mg_layout(n, mp, r, gws, nullptr, &W)) return set_error(MB_ERR_ARG, "workspace too small");
     mg_layout(n, mp, r, gws, workspace, &W);
     void* gemm_ws = W.gemm_ws;
-    auto prod = [&](const float* v32, float* y32, cudaStream_t st) {
+    auto prod = [&](const float* v32, float* y32, cudaStream_t st, const int*) {
         return cgemm_tf32x3(z_hi, z_lo, n, v32, mp, y32, gemm_ws, gws, st);
     };
     return gmres_lockstep(prod, n, b, x, m, r, max_iters, tol, gws, nullptr, 1, workspace, ws_bytes, false,
@@ -1583,10 +1600,10 @@ static int blockdiag_solve(const float* z, const int64_t* desc, const int64_t* g
         int rc = bd_zmaps(z, dh.data(), n_mesh, static_cast<CUtensorMap*>(W.gemm_ws), s);
         if (rc) return rc;
     }
-    auto prod = [&](const float* v32, float* y32, cudaStream_t st) {
+    auto prod = [&](const float* v32, float* y32, cudaStream_t st, const int* cact) {
         if (rows_per_warp == kBdRows)
-            return bd_launch(zmaps, v32, n_rows, desc, goff, n_mesh, total_warps, mp, nc, y32, status, st);
-        return blockdiag_matvec(z, desc, goff, n_mesh, total_warps, v32, mp, nc, rows_per_warp, y32, st);
+            return bd_launch(zmaps, v32, n_rows, desc, goff, n_mesh, total_warps, mp, nc, y32, status, st, cact);
+        return blockdiag_matvec(z, desc, goff, n_mesh, total_warps, v32, mp, nc, rows_per_warp, y32, st, cact);
     };
     if (!aug_q)
         return gmres_lockstep(prod, n_rows, b, x, m, r, max_iters, tol, map_bytes, desc, nc, workspace, ws_bytes,
