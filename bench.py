@@ -234,13 +234,15 @@ def cpu_sample_run(workload, seconds, steps=1, warmup=0):
     rows = max(3, min(3 * nf, int(rate_rows * seconds)))
     for _ in range(warmup):
         run(max(3, rows // 4))
-    vals = []
+    vals, step_ms = [], []
     for _ in range(steps):
         dt = run(rows)
         vals.append(rows * 3 * nf / 9.0 / dt)  # face-edge entries / 9 = triangle pairs
+        step_ms.append(dt * 1e3)
     info = {"kind": "port", "cores": threads,
             "sample": f"{rows} of {3 * nf} face-edge test rows x all {3 * nf} columns "
-                      f"({rows * nf // 3} triangle-pair equivalents), float32 C restatement"}
+                      f"({rows * nf // 3} triangle-pair equivalents), float32 C restatement",
+            "sample_ms_per_step": statistics.mean(step_ms)}
     return vals, info
 
 
@@ -2280,9 +2282,12 @@ def main():
         vals, info = cpu_sample_run(args.workload, args.cpu_seconds, steps=args.steps,
                                     warmup=min(args.warmup, 1))
         v = statistics.mean(vals)
+        # a step of this arm is the bounded sample it times (the metric is a rate): ms_per_step
+        # is that sample's wall time; the whole matrix at this rate is reported beside it
         line = {"metric": "Z-assembly triangle pairs/s", "value": v, "unit": "pairs/s",
                 "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": pairs / v * 1e3, "higher_is_better": True, "scaling": "weak",
+                "ms_per_step": info["sample_ms_per_step"], "full_matrix_ms_at_this_rate": pairs / v * 1e3,
+                "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
                 "cpu_baseline": {"value": v, "unit": "pairs/s", **info},
                 "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
