@@ -1,4 +1,4 @@
-"""Numpy restatements of two solver algorithms of the GPU path (test infrastructure only).
+"""Numpy restatements of three solver algorithms of the GPU path (test infrastructure only).
 
 * ``aug_gmres``: restarted right-preconditioned GMRES with a fixed augmentation subspace U
   (GCRO with a fixed recycled space), the algorithm of ``mb_gmres_blockdiag_aug_c64`` for one
@@ -11,6 +11,9 @@
   terms and the x_lo products summed beside them.  Float32 arithmetic is numpy's
   round-to-nearest; the exact product error uses float64 (a product of two float32 values is
   exact in float64), which is what the GPU's fused multiply-add gives.
+* ``half_refined_gmres``: GMRES cycles whose Arnoldi products read a binary16 copy of Z, each
+  started from the exact residual and ended at a fixed reduction of its own estimate
+  (``mb_pgmres_c64`` with ``Z_half``).
 """
 from __future__ import annotations
 
@@ -123,3 +126,43 @@ def compensated_residual(Z: np.ndarray, x: np.ndarray, b: np.ndarray, lanes: int
             tot_i += float(si) + float(ci)
         r[i] = b[i] - complex(tot_r, tot_i)
     return r
+
+
+def half_refined_gmres(Z, b, restart=40, inner_rtol=3e-3, tol=1e-10, max_cycles=200):
+    """The mixed-precision scheme of ``mb_pgmres_c64`` with a binary16 copy of Z: every cycle
+    starts from the exact residual r = b - Z x, runs GMRES on Zh = scale * half(Z / scale) (the
+    Arnoldi products read only the rounded copy) until its residual estimate has dropped by
+    inner_rtol, and adds the correction.  Returns (x, cycles, products)."""
+    scale = max(np.abs(Z.real).max(), np.abs(Z.imag).max())
+    Zh = (Z.real / scale).astype(np.float16).astype(np.float64) + 1j * (Z.imag / scale).astype(
+        np.float16).astype(np.float64)
+    Zh = Zh * scale
+    x = np.zeros(Z.shape[0], dtype=complex)
+    bn = np.linalg.norm(b)
+    products = 0
+    for cycle in range(max_cycles):
+        r = b - Z @ x
+        beta = np.linalg.norm(r)
+        if beta / bn <= tol:
+            return x, cycle, products
+        n = Z.shape[0]
+        V = np.zeros((n, restart + 1), dtype=complex)
+        H = np.zeros((restart + 1, restart), dtype=complex)
+        V[:, 0] = r / beta
+        for j in range(restart):
+            w = Zh @ V[:, j]
+            products += 1
+            for _ in range(2):
+                h = V[:, :j + 1].conj().T @ w
+                H[:j + 1, j] += h
+                w = w - V[:, :j + 1] @ h
+            H[j + 1, j] = np.linalg.norm(w)
+            e1 = np.zeros(j + 2, dtype=complex)
+            e1[0] = beta
+            y, *_ = np.linalg.lstsq(H[:j + 2, :j + 1], e1, rcond=None)
+            est = np.linalg.norm(e1 - H[:j + 2, :j + 1] @ y)
+            if est <= max(inner_rtol * beta, 0.5 * tol * bn) or H[j + 1, j] == 0:
+                break
+            V[:, j + 1] = w / H[j + 1, j]
+        x = x + V[:, :j + 1] @ y
+    return x, max_cycles, products

@@ -95,3 +95,20 @@ def test_compensated_residual_is_fp64_class():
     assert np.linalg.norm(got - exact) < 1e-3 * np.linalg.norm(exact)
     naive = b - (Z @ x.astype(np.complex64)).astype(np.complex128)
     assert np.linalg.norm(naive - exact) > np.linalg.norm(exact)
+
+
+def test_binary16_products_with_exact_refinement_reach_fp64_accuracy():
+    """Arnoldi products on a binary16 copy of Z (relative rounding ~5e-4) limit only how much
+    each cycle gains; with every cycle restarted from the exact residual the iterate reaches a
+    1e-10 residual, and the total products stay close to those of the exact-Z GMRES."""
+    from aug_gmres_reference import half_refined_gmres
+
+    Z, _ = _system(n=150, seed=9)
+    rng = np.random.default_rng(10)
+    b = rng.normal(size=150) + 1j * rng.normal(size=150)
+    x, cycles, products = half_refined_gmres(Z, b, restart=40, inner_rtol=3e-3, tol=1e-10)
+    ref = np.linalg.solve(Z, b)
+    assert np.linalg.norm(Z @ x - b) / np.linalg.norm(b) <= 1e-10
+    assert np.linalg.norm(x - ref) / np.linalg.norm(ref) < 1e-9
+    _, steps_exact, _, _ = aug_gmres(Z, b, restart=40, tol=1e-10)
+    assert cycles >= 2 and products <= 2 * steps_exact, (cycles, products, steps_exact)
